@@ -1,0 +1,163 @@
+// dev_types.h — data layout of a scene, a film and the wavefront queues in HBM.
+//
+// Shared by the host C++ code and the CUDA kernels.  Everything the traversal
+// and shading kernels read per ray is 16-byte aligned so each record is moved
+// with 128-bit loads.
+#pragma once
+#include <cstdint>
+
+#include <vector_types.h>
+
+#include "../../include/asuna_rt.h"
+
+namespace asuna {
+
+// ---- acceleration structure -------------------------------------------------
+// Binary BVH node, 64 B: the two child boxes as x/y/z slab quads, then the
+// child references.  ref >= 0: inner node index; ref < 0: leaf, decoded by
+// leafFirst/leafCount (BLAS: first triangle, count <= 8; TLAS: instance).
+struct __align__(16) BvhNode {
+  float4 xs;  // c0.lo.x, c0.hi.x, c1.lo.x, c1.hi.x
+  float4 ys;
+  float4 zs;
+  int4 ref;   // c0, c1, unused, unused
+};
+static_assert(sizeof(BvhNode) == 64, "BvhNode is 64 bytes");
+
+constexpr int kMaxLeafTris = 8;
+constexpr int32_t kStackSentinel = INT32_MIN;  // "leave the BLAS" marker
+inline __host__ __device__ int32_t encodeLeaf(uint32_t first, uint32_t count) {
+  return ~int32_t(first * 8u + (count - 1u));
+}
+inline __host__ __device__ uint32_t leafFirst(int32_t ref) { return uint32_t(~ref) >> 3; }
+inline __host__ __device__ uint32_t leafCount(int32_t ref) { return (uint32_t(~ref) & 7u) + 1u; }
+constexpr uint32_t kMaxLeafFirst = (1u << 28) - 1u;
+
+// Leaf triangle in BVH order, 48 B: object-space vertices; v0.w holds the
+// mesh-local primitive id (float bits).
+struct __align__(16) TriDev {
+  float4 v0, v1, v2;
+};
+
+// Shading vertex, 32 B: (pos.xyz, uv.x), (normal.xyz, uv.y).
+struct __align__(16) VtxDev {
+  float4 pu;
+  float4 nv;
+};
+
+// Instance record, 128 B.
+struct __align__(16) InstDev {
+  float4 w2o[3];  // world -> object rows (double inverse rounded once)
+  float4 o2w[3];  // object -> world rows (as given)
+  int32_t blasRoot;  // inner-node index of the mesh BLAS (-1: empty mesh)
+  uint32_t vtxBase;  // first vertex of the mesh in the vertex arrays
+  uint32_t idxBase;  // first triangle of the mesh in the index array
+  int32_t matId;     // material (-1 for emitters)
+  int32_t lightId;   // >= 0: emitter instance
+  uint32_t matType;
+  uint32_t pad[2];
+};
+static_assert(sizeof(InstDev) == 128, "InstDev is 128 bytes");
+
+// Packed material, 32 B: (diffuse.xyz, type bits), (alpha.x, alpha.y, ior, fdrInt).
+struct __align__(16) MatDev {
+  float4 a;
+  float4 b;
+};
+
+// Packed light, 80 B: (position, type bits), (direction, radius),
+// (radiance, 0), (u, area), (v, doubleSide bits).
+struct __align__(16) LightDev {
+  float4 pos;
+  float4 dir;
+  float4 rad;
+  float4 u;
+  float4 v;
+};
+
+// Device view of one uploaded scene.
+struct SceneDev {
+  const BvhNode* nodes;  // all BLAS nodes, then the TLAS nodes
+  const TriDev* tris;
+  const VtxDev* vtx;
+  const uint4* idx;  // mesh-local vertex indices (x, y, z), w unused
+  const InstDev* inst;
+  const MatDev* mats;
+  const LightDev* lights;
+  const float4* env;    // W*H rgba
+  const float2* marg;   // W*H (.x inverse CDF, .y pdf)
+  const float2* cond;   // W*H
+  int32_t tlasRoot;
+  int32_t envW, envH;
+  int32_t numInst;
+};
+
+// ---- shots, films, batches ----------------------------------------------------
+struct __align__(16) ShotDev {
+  asuna_camera cam;       // 224 B
+  asuna_rt_state state;   // 84 B
+  uint32_t width, height;
+  uint32_t seed, flags;
+  uint32_t rrDepth;
+  int32_t depthSlot;
+  float4* filmRad;        // image 0
+  float4* filmW;          // image 8
+  float4* filmCh;         // images 1..7, contiguous (7 * W * H)
+};
+
+// A contiguous run of paths: frames [frameBegin, frameBegin + nframes) of
+// one shot, all pixels, path index = pathBegin + (frame - frameBegin) * npix + pixel.
+struct __align__(16) RangeDev {
+  uint32_t pathBegin;
+  uint32_t shot;
+  uint32_t frameBegin;
+  uint32_t nframes;
+  uint32_t npix;
+  uint32_t pad[3];
+};
+
+// Counters in device memory (one 4 KB page).
+enum CounterSlot {
+  kCntExtend0 = 0,  // rays in extend queue 0
+  kCntExtend1 = 1,  // rays in extend queue 1
+  kCntShadow = 2,   // rays in the shadow queue
+  kCntFetchExtend = 3,
+  kCntFetchShadow = 4,
+  kCntNum32 = 8
+};
+struct DevCounters {
+  uint32_t c[kCntNum32];
+  unsigned long long extendRays;
+  unsigned long long shadowRays;
+  unsigned long long nodes;
+  unsigned long long tris;
+  unsigned long long paths;
+  unsigned long long stackOverflow;  // traversals cut short by a full stack (must stay 0)
+  unsigned long long pad[2];
+};
+
+// Wavefront buffers (structure of arrays, indexed by queue slot or path).
+struct WaveDev {
+  // extend queues (ping-pong): (o.xyz, tmax), (d.xyz, path index bits)
+  float4* rayO[2];
+  float4* rayD[2];
+  // closest-hit results of the current extend queue: (t, u, v, prim bits), inst
+  float4* hit;
+  uint32_t* hitInst;
+  // shadow queue: (o.xyz, tmax), (d.xyz, path bits), (contribution.xyz, 0)
+  float4* shO;
+  float4* shD;
+  float4* shC;
+  // path state
+  float4* thp;  // throughput.xyz, pdf of the last BSDF sample
+  float4* rad;  // radiance.xyz, filter weight
+  uint4* info;  // seed, last BSDF lobe flags, range index, local index
+  uint4* rec;   // parity records: signature, unoccluded bits, shadow bits, depth
+  DevCounters* cnt;
+  const RangeDev* ranges;
+  const ShotDev* shots;
+  uint32_t numRanges;
+  uint32_t numPaths;
+};
+
+}  // namespace asuna

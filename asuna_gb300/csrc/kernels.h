@@ -1,0 +1,33 @@
+// kernels.h — launch interface of the wavefront kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "dev_types.h"
+
+namespace asuna {
+
+struct KParams {
+  SceneDev S;
+  WaveDev W;
+  uint32_t depth;  // bounce being processed (1-based)
+  int32_t cur;     // extend queue holding this bounce's rays (0/1)
+  int32_t records; // write per-path parity records
+  int32_t counters;
+};
+
+constexpr int kTraceThreads = 128;
+constexpr int kStackDepth = 64;
+
+void launchRaygen(const KParams& P, int grid, cudaStream_t s);
+void launchShade(const KParams& P, int grid, cudaStream_t s);
+void launchAccumulate(const KParams& P, uint32_t maxPix, uint32_t nranges, cudaStream_t s);
+void launchRecords(const KParams& P, asuna_path_record* out, int grid, cudaStream_t s);
+void launchExtend(const KParams& P, int grid, cudaStream_t s);
+void launchConnect(const KParams& P, int grid, cudaStream_t s);
+int traceBlocksPerSm();
+
+// Standalone ray queries (tests): rays are (o.xyz, tmin), (d.xyz, tmax).
+void launchTraceQuery(const SceneDev& S, const float4* o, const float4* d, uint32_t n, int anyHit, float4* hit,
+                      uint32_t* inst, cudaStream_t s);
+
+}  // namespace asuna

@@ -1,0 +1,607 @@
+// shade.cu — ray generation, shading and film accumulation kernels.
+//
+// One wavefront iteration per path depth: raygen fills extend queue 0 with
+// camera rays; after each closest-hit pass, `shade` runs the miss shader or
+// the closest-hit shader of the hit material (emitters use the Lambertian
+// light branch), writes next-event shadow rays into the shadow queue and the
+// continuation rays into the other extend queue (warp-aggregated ballot/popc
+// compaction, one atomic per warp); `accumulate` folds the finished samples
+// into the film in frame order.
+//
+// Restates (file:line of the reference):
+//   raygen      raytrace.projective.rgen:26-100 (seed, jitter, cameras)
+//   shade/miss  raytrace.default.rmiss:24-56
+//   shade/hit   rchit_layouts.glsl:61-167, brdf_lambertian.rchit:12-151,
+//               brdf_rough_plastic.rchit:191-269, bsdf_dielectric.rchit:74-139
+//   accumulate  raytrace.projective.rgen:134-179
+//
+// Compiled with -fmad=false: the float arithmetic rounds operation by
+// operation in the order of the reference's GLSL source.
+#include <cuda_runtime.h>
+
+#include "dev_math.cuh"
+#include "kernels.h"
+
+namespace asuna {
+using namespace dm;
+
+namespace {
+
+__device__ __forceinline__ uint32_t laneId() { return threadIdx.x & 31u; }
+
+// Warp-aggregated queue append: every lane of the warp calls it.
+__device__ __forceinline__ uint32_t warpAppend(bool want, uint32_t* counter) {
+  unsigned mask = __ballot_sync(0xffffffffu, want);
+  if (!mask) return 0;
+  int leader = __ffs(mask) - 1;
+  uint32_t base = 0;
+  if (int(laneId()) == leader) base = atomicAdd(counter, uint32_t(__popc(mask)));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  return base + uint32_t(__popc(mask & ((1u << laneId()) - 1u)));
+}
+
+__device__ __forceinline__ uint32_t findRange(const RangeDev* r, uint32_t n, uint32_t p) {
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(&r[mid].pathBegin) <= p)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ uint32_t sigMix(uint32_t h, uint32_t v) {
+  return h ^ (v + 0x9e3779b9u + (h << 6) + (h >> 2));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// raygen: raytrace.projective.rgen:26-100
+__global__ void __launch_bounds__(256) k_raygen(KParams P) {
+  const WaveDev& W = P.W;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    W.cnt->c[kCntExtend0] = W.numPaths;
+    W.cnt->c[kCntExtend1] = 0;
+    W.cnt->c[kCntShadow] = 0;
+    W.cnt->c[kCntFetchExtend] = 0;
+    W.cnt->c[kCntFetchShadow] = 0;
+    W.cnt->paths += W.numPaths;
+  }
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < W.numPaths; p += stride) {
+    const uint32_t ri = findRange(W.ranges, W.numRanges, p);
+    const RangeDev R = W.ranges[ri];
+    const ShotDev& sh = W.shots[R.shot];
+    const uint32_t local = p - R.pathBegin;
+    const uint32_t frame = R.frameBegin + local / R.npix;
+    const uint32_t pix = local % R.npix;
+    const uint32_t x = pix % sh.width, y = pix / sh.width;
+    uint32_t seed = xxhash32(x, y, hashFrame(frame, sh.seed));
+    const asuna_camera& cam = sh.cam;
+    f3 origin = transformPoint(cam.camera_to_world, splat(0.0f));
+    f2 jitter = (frame == 0) ? f2{0.5f, 0.5f} : rnd2(seed);
+    f2 pixel{float(x) + jitter.x, float(y) + jitter.y};
+    f3 ro = origin, rd = splat(0.0f);
+    if (cam.type == ASUNA_CAMERA_PERSPECTIVE) {
+      f3 pCamera = transformPoint(cam.raster_to_camera, f3{pixel.x, pixel.y, 0.0f});
+      f3 r = makeNormal(pCamera);
+      if (cam.aperture > 0.0f) {
+        f2 uLens = rnd2(seed);
+        f2 d = concentricSampleDisk(uLens);
+        f2 pLens{cam.aperture * d.x, cam.aperture * d.y};
+        float ft = cam.focal_distance / r.z;
+        f3 pFocus = ft * r;
+        f3 o{pLens.x, pLens.y, 0.0f};
+        ro = transformPoint(cam.camera_to_world, o);
+        r = pFocus - o;
+      }
+      rd = transformDirection(cam.camera_to_world, r);
+    } else if (cam.type == ASUNA_CAMERA_OPENCV) {
+      float px = (pixel.x - cam.fxfycxcy[2]) / cam.fxfycxcy[0];
+      float py = (pixel.y - cam.fxfycxcy[3]) / cam.fxfycxcy[1];
+      rd = transformDirection(cam.camera_to_world, f3{px, py, 1.0f});
+    }
+    // Gaussian filter weight of this sample, rgen:134-145
+    const float alpha = -2.0f;
+    const float expXY = expf(alpha * 2.0f * 2.0f);
+    float ox = jitter.x - 0.5f, oy = jitter.y - 0.5f;
+    float fw = gmax(0.0f, expf(alpha * ox * ox) - expXY) * gmax(0.0f, expf(alpha * oy * oy) - expXY);
+    W.rayO[0][p] = make_float4(ro.x, ro.y, ro.z, INF);
+    W.rayD[0][p] = make_float4(rd.x, rd.y, rd.z, __uint_as_float(p));
+    W.thp[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    W.rad[p] = make_float4(0.0f, 0.0f, 0.0f, fw);
+    W.info[p] = make_uint4(seed, EBsdfNull, ri, local);
+    if (P.records) W.rec[p] = make_uint4(0u, 0u, 0u, 1u);
+    if (frame == 0) {
+      // AOV images are rewritten at frame 0 (rgen:155-162): clear to (0,0,0,1)
+      const uint32_t npx = sh.width * sh.height;
+      for (uint32_t c = 0; c < sh.state.n_multi_channel && c < ASUNA_MAX_CHANNELS; ++c)
+        sh.filmCh[size_t(c) * npx + pix] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+namespace {
+
+struct HitSt {
+  f3 pos, V, N, ffN, X, Y;
+  float u, v;
+};
+
+// rchit_layouts.glsl:61-95 (getHitState + configureShadingFrame)
+__device__ __forceinline__ HitSt hitState(const SceneDev& S, const InstDev& in, uint32_t prim, float bu, float bv,
+                                          f3 rd, uint32_t useFaceNormal) {
+  HitSt st;
+  const uint4 id = __ldg(&S.idx[in.idxBase + prim]);
+  const VtxDev* vb = S.vtx + in.vtxBase;
+  const float4 p0 = __ldg(&vb[id.x].pu), n0 = __ldg(&vb[id.x].nv);
+  const float4 p1 = __ldg(&vb[id.y].pu), n1 = __ldg(&vb[id.y].nv);
+  const float4 p2 = __ldg(&vb[id.z].pu), n2 = __ldg(&vb[id.z].nv);
+  float bx = 1.0f - bu - bv, by = bu, bz = bv;
+  st.u = p0.w * bx + p1.w * by + p2.w * bz;
+  st.v = n0.w * bx + n1.w * by + n2.w * bz;
+  f3 po = ld3(p0) * bx + ld3(p1) * by + ld3(p2) * bz;
+  const float4 o0 = in.o2w[0], o1 = in.o2w[1], o2 = in.o2w[2];
+  st.pos = f3{o0.x * po.x + o0.y * po.y + o0.z * po.z + o0.w, o1.x * po.x + o1.y * po.y + o1.z * po.z + o1.w,
+              o2.x * po.x + o2.y * po.y + o2.z * po.z + o2.w};
+  const float4 w0 = in.w2o[0], w1 = in.w2o[1], w2 = in.w2o[2];
+  f3 n = ld3(n0) * bx + ld3(n1) * by + ld3(n2) * bz;
+  st.N = makeNormal(f3{n.x * w0.x + n.y * w1.x + n.z * w2.x, n.x * w0.y + n.y * w1.y + n.z * w2.y,
+                       n.x * w0.z + n.y * w1.z + n.z * w2.z});
+  if (useFaceNormal == 1) {
+    f3 g = cross(ld3(p1) - ld3(p0), ld3(p2) - ld3(p0));
+    st.N = makeNormal(f3{g.x * w0.x + g.y * w1.x + g.z * w2.x, g.x * w0.y + g.y * w1.y + g.z * w2.y,
+                         g.x * w0.z + g.y * w1.z + g.z * w2.z});
+  }
+  st.V = makeNormal(-rd);
+  basis(st.N, st.X, st.Y);
+  st.ffN = dot(st.N, st.V) > 0.0f ? st.N : -st.N;
+  return st;
+}
+
+struct PathIO {
+  uint32_t seed;
+  uint32_t bflags;
+  float bpdf;
+  f3 thp;
+  f3 rad;
+  bool stop;
+  // next-event record of this bounce
+  bool dskip;
+  f3 drad, dro, drd;
+  float ddist;
+  // continuation
+  f3 nro, nrd;
+};
+
+// rchit_layouts.glsl:118-167 (sampleLights, with sampleEnvironmentLight 98-116)
+__device__ __forceinline__ f3 sampleLights(const SceneDev& S, const ShotDev& sh, PathIO& io, f3 rd, f3 pos, f3 nrm,
+                                           bool& visible, LRec& lRec) {
+  bool allowDoubleSide = false;
+  f3 radiance = splat(0.0f);
+  const bool hasEnv = sh.state.has_env_map == 1u;
+  const bool hasLight = sh.state.num_lights > 0;
+  float envSel, anaSel;
+  if (hasEnv && hasLight) {
+    envSel = anaSel = 0.5f;
+  } else if (hasEnv) {
+    envSel = 1.0f;
+    anaSel = 0.0f;
+  } else if (hasLight) {
+    envSel = 0.0f;
+    anaSel = 1.0f;
+  } else {
+    envSel = anaSel = 0.0f;
+  }
+  float sel = rnd(io.seed);
+  if (sel < envSel) {
+    lRec.flags = EArea;
+    lRec.dist = INF;
+    lRec.n = -makeNormal(rd);
+    f2 u = rnd2(io.seed);
+    radiance = sampleEnvmap(S, sh, u, lRec.d, lRec.pdf) / envSel;
+    allowDoubleSide = true;
+  } else if (sel < envSel + anaSel) {
+    const int n = sh.state.num_lights;
+    int idx = min(1 + __float2int_rz(rnd(io.seed) * float(n)), n);
+    const LightDev l = S.lights[idx];
+    f2 u = rnd2(io.seed);
+    radiance = sampleOneLight(u, l, pos, lRec) * float(n) / anaSel;
+    allowDoubleSide = (__float_as_uint(l.v.w) == 1u);
+  }
+  io.dro = offsetPositionAlongNormal(pos, nrm);
+  io.drd = lRec.d;
+  io.ddist = lRec.dist;
+  visible = (dot(lRec.d, nrm) > 0.0f && lRec.pdf > 0.0f);
+  visible = visible && (dot(lRec.n, lRec.d) < 0.0f || allowDoubleSide);
+  return radiance;
+}
+
+// brdf_lambertian.rchit:70-151 (after getHitState)
+__device__ __forceinline__ void shadeLambertian(const SceneDev& S, const ShotDev& sh, PathIO& io, const HitSt& st,
+                                                f3 kd, f3 rd) {
+  {
+    bool visible;
+    LRec lRec{splat(0.0f), splat(0.0f), 0.0f, 0.0f, 0u};
+    f3 Ld = splat(0.0f);
+    f3 r = sampleLights(S, sh, io, rd, st.pos, st.ffN, visible, lRec);
+    if (visible) {
+      f3 w = splat(0.0f);
+      float NdotL = dot(st.ffN, lRec.d), NdotV = dot(st.ffN, st.V);
+      if (!(NdotL < 0.0f || NdotV < 0.0f)) w = kd * INV_PI * NdotL;
+      float bpdf = (lRec.flags & EArea) ? cosineHemispherePdf(dot(st.ffN, lRec.d)) : 0.0f;
+      float mis = powerHeuristic(lRec.pdf, bpdf);
+      Ld = Ld + mis * w * r * io.thp / (lRec.pdf + EPS);
+    }
+    io.drad = Ld;
+    io.dskip = !visible;
+  }
+  f2 u = rnd2(io.seed);
+  f3 wi = cosineSampleHemisphere(u);
+  float pdf = cosineHemispherePdf(wi.z);
+  f3 d = toWorld(st.X, st.Y, st.ffN, wi);
+  f3 w = kd * INV_PI * fabsf(wi.z);
+  if (pdf <= 0.0f || length(w) == 0.0f) {
+    io.stop = true;
+    return;
+  }
+  io.bflags = EDiffuseReflection;
+  io.bpdf = pdf;
+  io.nro = offsetPositionAlongNormal(st.pos, st.ffN);
+  io.nrd = d;
+  io.thp = io.thp * (w / pdf);
+}
+
+// brdf_rough_plastic.rchit:191-269
+__device__ __forceinline__ void shadeRoughPlastic(const SceneDev& S, const ShotDev& sh, PathIO& io, const HitSt& st,
+                                                  const MatDev& m, f3 rd) {
+  const float eta = m.b.z;
+  const float fdrInt = m.b.w;
+  const float invEta2 = 1.0f / (eta * eta);
+  const float ax = gmax(EPS, m.b.x);
+  const float ay = gmax(EPS, m.b.y);
+  const f3 kd = ld3(m.a);
+  const float ssw = luminance(kd);
+  const f3 ks = splat(1.0f);
+  {
+    bool visible;
+    LRec lRec{splat(0.0f), splat(0.0f), 0.0f, 0.0f, 0u};
+    f3 Ld = splat(0.0f);
+    f3 r = sampleLights(S, sh, io, rd, st.pos, st.ffN, visible, lRec);
+    if (visible) {
+      // The reference's call sites (brdf_rough_plastic.rchit:234-240) pass
+      // (.., fdrInt, ax, ay, invEta2, ..) and (.., eta, ax, ay, ..) into
+      // parameters declared (.., fdrInt, invEta2, ax, ay, ..) and
+      // (.., ax, ay, eta, ..); kept as written.
+      f3 w = rpEval(lRec.d, st.V, st.ffN, st.X, st.Y, kd, ks, eta, fdrInt, ax, ay, invEta2, EArea);
+      float bpdf = rpPdf(lRec.d, st.V, st.ffN, st.X, st.Y, eta, ax, ay, ssw, lRec.flags);
+      float mis = powerHeuristic(lRec.pdf, bpdf);
+      Ld = Ld + mis * w * r * io.thp / (lRec.pdf + EPS);
+    }
+    io.drad = Ld;
+    io.dskip = !visible;
+  }
+  f2 u = rnd2(io.seed);
+  const f3 V = st.V, N = st.ffN, X = st.X, Y = st.Y;
+  f3 weight = splat(0.0f);
+  float bpdf = 0.0f;
+  uint32_t bflags = EBsdfNull;
+  f3 bd = splat(0.0f);
+  const float NdotV = dot(V, N);
+  if (NdotV > 0.0f) {
+    float ct;
+    float Fo = fresnelDielectricExt(NdotV, ct, eta);
+    float substrateWeight = ssw * (1.0f - Fo);
+    float specularWeight = Fo;
+    float probSpecular = specularWeight / (specularWeight + substrateWeight);
+    if (u.x < probSpecular) {
+      u.x = u.x / probSpecular;
+      f3 wo = toLocal(X, Y, N, V);
+      f3 wi = importanceSampleAnisoGGX(u, wo, ax, ay);
+      f3 L = toWorld(X, Y, N, wi);
+      bd = L;
+      f3 H = makeNormal(V + L);
+      f3 wh = makeNormal(wi + wo);
+      float NdotL = dot(N, L);
+      float ct2;
+      float Fs = fresnelDielectricExt(dot(H, V), ct2, eta);
+      float Gs = g1SmithAnisoGGX(NdotV, dot(V, X), dot(V, Y), ax, ay);
+      Gs = Gs * g1SmithAnisoGGX(NdotL, dot(L, X), dot(L, Y), ax, ay);
+      float Ds = dAnisoGGX(dot(H, N), dot(H, X), dot(H, Y), ax, ay);
+      bflags = EGlossyReflection;
+      bpdf = importanceAnisoGGXPdf(wh, wo, ax, ay) * probSpecular;
+      weight = ks * Fs * Gs * Ds * NdotL;
+    } else {
+      u.x = (u.x - probSpecular) / (1.0f + EPS - probSpecular);
+      f3 wi = cosineSampleHemisphere(u);
+      float ct2;
+      float Fi = fresnelDielectricExt(wi.z, ct2, eta);
+      f3 diff = kd;
+      diff = diff / (splat(1.0f) - diff * fdrInt);
+      bpdf = (1.0f - probSpecular) * cosineHemispherePdf(wi.z);
+      bd = toWorld(X, Y, N, wi);
+      bflags = EDiffuseReflection;
+      weight = (1.0f - Fi) * (1.0f - Fo) * invEta2 * diff * INV_PI * fabsf(wi.z);
+    }
+  }
+  if (bpdf <= 0.0f || length(weight) == 0.0f) {
+    io.stop = true;
+    return;
+  }
+  io.bflags = bflags;
+  io.bpdf = bpdf;
+  io.nro = offsetPositionAlongNormal(st.pos, st.ffN);
+  io.nrd = bd;
+  io.thp = io.thp * (weight / (bpdf + EPS));
+}
+
+// bsdf_dielectric.rchit:74-139
+__device__ __forceinline__ void shadeDielectric(const SceneDev& S, const ShotDev& sh, PathIO& io, const HitSt& st,
+                                                const MatDev& m, f3 rd) {
+  const float ior = m.b.z;
+  const float eta = dot(st.V, st.N) > 0.0f ? (1.0f / ior) : ior;
+  {
+    bool visible;
+    LRec lRec{splat(0.0f), splat(0.0f), 0.0f, 0.0f, 0u};
+    f3 Ld = splat(0.0f);
+    f3 r = sampleLights(S, sh, io, rd, st.pos, st.ffN, visible, lRec);
+    if (visible) {
+      // eval() with EArea returns 0 (bsdf_dielectric.rchit:26-38)
+      f3 w = splat(0.0f);
+      float bpdf = 0.0f;
+      if (lRec.flags & EDelta) {
+        f3 L = lRec.d, V = st.V, N = st.ffN;
+        float F = dielectricFresnel(fabsf(dot(V, N)), eta);
+        if (dot(L, N) > 0.0f) {
+          if (fabsf(dot(reflect(-V, N), L) - 1.0f) < EPS) bpdf = F;
+        } else {
+          if (fabsf(dot(refract(-V, N, eta), L) - 1.0f) < EPS) bpdf = 1.0f - F;
+        }
+      }
+      float mis = powerHeuristic(lRec.pdf, bpdf);
+      Ld = Ld + mis * w * r * io.thp / (lRec.pdf + EPS);
+    }
+    io.drad = Ld;
+    io.dskip = !visible;
+  }
+  float u = rnd(io.seed);
+  const f3 V = st.V, N = st.ffN;
+  float F = dielectricFresnel(fabsf(dot(V, N)), eta);
+  f3 bd, weight;
+  float bpdf;
+  uint32_t bflags;
+  if (u < F) {
+    bd = makeNormal(reflect(-V, N));
+    bpdf = F;
+    bflags = ESpecularReflection;
+    weight = F * splat(1.0f);
+  } else {
+    bd = makeNormal(refract(-V, N, eta));
+    bpdf = 1.0f - F;
+    bflags = ESpecularTransmission;
+    weight = (1.0f - F) * splat(1.0f) * eta * eta;
+  }
+  if (bpdf <= 0.0f || length(weight) == 0.0f) {
+    io.stop = true;
+    return;
+  }
+  io.bflags = bflags;
+  io.bpdf = bpdf;
+  io.nro = offsetPositionAlongNormal(st.pos, gsign(dot(bd, st.N)) * st.N);
+  io.nrd = bd;
+  io.thp = io.thp * (weight / (bpdf + EPS));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_shade(KParams P) {
+  const WaveDev& W = P.W;
+  const SceneDev& S = P.S;
+  const int cur = P.cur, nxt = cur ^ 1;
+  const uint32_t n = W.cnt->c[kCntExtend0 + cur];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    // the connect kernel that follows fetches shadow rays from 0
+    W.cnt->c[kCntFetchShadow] = 0;
+  }
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+    const uint32_t i = i0 + threadIdx.x;
+    const bool valid = i < n;
+    bool wantNext = false, wantShadow = false;
+    PathIO io;
+    uint32_t p = 0;
+    uint4 rc = make_uint4(0, 0, 0, 0);
+    if (valid) {
+      const float4 o4 = W.rayO[cur][i];
+      const float4 d4 = W.rayD[cur][i];
+      p = __float_as_uint(d4.w);
+      const f3 ro = ld3(o4), rd = ld3(d4);
+      const float4 h4 = W.hit[i];
+      const uint32_t inst = W.hitInst[i];
+      const float4 t4 = W.thp[p];
+      const float4 r4 = W.rad[p];
+      const uint4 inf = W.info[p];
+      if (P.records) rc = W.rec[p];
+      const RangeDev R = W.ranges[inf.z];
+      const ShotDev& sh = W.shots[R.shot];
+      const uint32_t frame = R.frameBegin + inf.w / R.npix;
+      const uint32_t pix = inf.w % R.npix;
+      const uint32_t depth = P.depth;
+      io.seed = inf.x;
+      io.bflags = inf.y;
+      io.bpdf = t4.w;
+      io.thp = ld3(t4);
+      io.rad = ld3(r4);
+      io.stop = false;
+      io.dskip = true;
+      io.drad = splat(0.0f);
+      if (inst == 0xffffffffu) {
+        // raytrace.default.rmiss:24-56
+        io.stop = true;
+        f3 env = (sh.state.has_env_map == 1u) ? evalEnvmap(S, sh, rd) : ld3(sh.state.bg_color);
+        float mis = 1.0f;
+        if (depth != 1u && isNonSpecular(io.bflags)) {
+          float envPdf = (sh.state.has_env_map == 1u) ? pdfEnvmap(S, sh, rd) : INV_4PI;
+          mis = powerHeuristic(io.bpdf, envPdf);
+        }
+        io.rad = io.rad + io.thp * env * mis;
+        rc.x = sigMix(rc.x, 0xffffffffu);
+      } else {
+        const InstDev& in = S.inst[inst];
+        const uint32_t prim = __float_as_uint(h4.w);
+        rc.x = sigMix(rc.x, (inst << 20) ^ prim);
+        const HitSt st = hitState(S, in, prim, h4.y, h4.z, rd, sh.state.use_face_normal);
+        if (in.lightId >= 0) {
+          // brdf_lambertian.rchit:44-68 (hitLight)
+          const LightDev l = S.lights[in.lightId];
+          f3 ldir = makeNormal(rd);
+          f3 lnrm = makeNormal(cross(ld3(l.u), ld3(l.v)));
+          float proj = dot(lnrm, ldir);
+          io.stop = true;
+          if (!(proj > 0.0f && __float_as_uint(l.v.w) == 0u)) {
+            float mis = 1.0f;
+            if (isNonSpecular(io.bflags) && depth != 1u) {
+              float dist = length(st.pos - ro);
+              float d2 = dist * dist;
+              float lpdf = d2 / (l.u.w * fabsf(proj) + EPS);
+              mis = powerHeuristic(io.bpdf, lpdf);
+            }
+            io.rad = io.rad + io.thp * ld3(l.rad) * mis;
+          }
+        } else {
+          const MatDev m = S.mats[in.matId];
+          const uint32_t type = in.matType;
+          if (depth == 1u && frame == 0u && sh.state.n_multi_channel > 0u && type == ASUNA_MAT_LAMBERTIAN) {
+            // brdf_lambertian.rchit:93-108
+            const asuna_rt_state& ps = sh.state;
+            float4* ch = sh.filmCh;
+            const size_t npx = size_t(sh.width) * sh.height;
+            auto put = [&](int slot, f3 v) {
+              if (slot >= 0 && slot < ASUNA_MAX_CHANNELS) ch[size_t(slot) * npx + pix] = make_float4(v.x, v.y, v.z, 1.0f);
+            };
+            put(ps.diffuse_out_channel, ld3(m.a));
+            put(ps.normal_out_channel, st.N);
+            put(ps.specular_out_channel, splat(0.0f));
+            put(ps.tangent_out_channel, st.X);
+            put(ps.roughness_out_channel, f3{1.0f, 1.0f, 0.0f});
+            put(ps.position_out_channel, st.pos);
+            put(ps.uv_out_channel, f3{st.u, st.v, 1.0f});
+          }
+          if (type == ASUNA_MAT_ROUGH_PLASTIC)
+            shadeRoughPlastic(S, sh, io, st, m, rd);
+          else if (type == ASUNA_MAT_DIELECTRIC)
+            shadeDielectric(S, sh, io, st, m, rd);
+          else
+            shadeLambertian(S, sh, io, st, ld3(m.a), rd);
+          rc.x = sigMix(rc.x, io.stop ? 0xfffu : io.bflags);
+        }
+        if (depth == 1u && frame == 0u && sh.depthSlot >= 0 && sh.depthSlot < ASUNA_MAX_CHANNELS) {
+          const size_t npx = size_t(sh.width) * sh.height;
+          sh.filmCh[size_t(sh.depthSlot) * npx + pix] = make_float4(h4.x, h4.x, h4.x, 1.0f);
+        }
+      }
+      wantShadow = !io.dskip;
+      bool alive = !io.stop && depth < uint32_t(sh.state.max_path_depth);
+      if (alive && (sh.flags & ASUNA_SHOT_RR) && depth >= sh.rrDepth) {
+        // Russian roulette (extension; off for the reference's streams)
+        float q = gmin(0.95f, gmax(io.thp.x, gmax(io.thp.y, io.thp.z)));
+        float u = rnd(io.seed);
+        if (!(u < q))
+          alive = false;
+        else
+          io.thp = io.thp / q;
+      }
+      wantNext = alive;
+      if (P.records) {
+        rc.w = depth;
+        if (wantShadow) rc.z |= 1u << (depth - 1u);
+      }
+      // path state
+      W.thp[p] = make_float4(io.thp.x, io.thp.y, io.thp.z, io.bpdf);
+      W.rad[p] = make_float4(io.rad.x, io.rad.y, io.rad.z, r4.w);
+      W.info[p] = make_uint4(io.seed, io.bflags, inf.z, inf.w);
+      if (P.records) W.rec[p] = rc;
+    }
+    __syncwarp();
+    const uint32_t sslot = warpAppend(wantShadow, &W.cnt->c[kCntShadow]);
+    const uint32_t nslot = warpAppend(wantNext, &W.cnt->c[kCntExtend0 + nxt]);
+    if (wantShadow) {
+      float maxDist = io.ddist - 2.0f * EPS;
+      W.shO[sslot] = make_float4(io.dro.x, io.dro.y, io.dro.z, maxDist);
+      W.shD[sslot] = make_float4(io.drd.x, io.drd.y, io.drd.z, __uint_as_float(p));
+      W.shC[sslot] = make_float4(io.drad.x, io.drad.y, io.drad.z, 0.0f);
+    }
+    if (wantNext) {
+      W.rayO[nxt][nslot] = make_float4(io.nro.x, io.nro.y, io.nro.z, INF);
+      W.rayD[nxt][nslot] = make_float4(io.nrd.x, io.nrd.y, io.nrd.z, __uint_as_float(p));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// accumulate: rgen:147-179, frames in order, one thread per pixel of a range
+__global__ void __launch_bounds__(256) k_accumulate(KParams P) {
+  const WaveDev& W = P.W;
+  const RangeDev R = W.ranges[blockIdx.y];
+  const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= R.npix) return;
+  const ShotDev& sh = W.shots[R.shot];
+  float4 old = sh.filmRad[pix];
+  float ow = sh.filmW[pix].x;
+  for (uint32_t f = 0; f < R.nframes; ++f) {
+    const uint32_t p = R.pathBegin + f * R.npix + pix;
+    const uint32_t frame = R.frameBegin + f;
+    const float4 r4 = W.rad[p];
+    const float fw = r4.w;
+    float rcl[3] = {gclamp(r4.x, 0.0f, 10.0f), gclamp(r4.y, 0.0f, 10.0f), gclamp(r4.z, 0.0f, 10.0f)};
+    float rws[3] = {fw * rcl[0], fw * rcl[1], fw * rcl[2]};
+    if (frame == 0) {
+      old = make_float4(rws[0] / fw, rws[1] / fw, rws[2] / fw, 1.0f);
+      ow = fw;
+    } else {
+      float nw = ow + fw;
+      old = make_float4((old.x * ow + rws[0]) / nw, (old.y * ow + rws[1]) / nw, (old.z * ow + rws[2]) / nw, 1.0f);
+      ow = nw;
+    }
+  }
+  sh.filmRad[pix] = old;
+  sh.filmW[pix] = make_float4(ow, ow, ow, ow);
+}
+
+// ---------------------------------------------------------------------------
+// parity records: copy per-path radiance / filter weight with the record
+__global__ void __launch_bounds__(256) k_records(KParams P, asuna_path_record* out) {
+  const WaveDev& W = P.W;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < W.numPaths; p += gridDim.x * blockDim.x) {
+    const float4 r4 = W.rad[p];
+    const uint4 rc = W.rec[p];
+    asuna_path_record o;
+    o.radiance[0] = r4.x;
+    o.radiance[1] = r4.y;
+    o.radiance[2] = r4.z;
+    o.filter_weight = r4.w;
+    o.depth = rc.w;
+    o.signature = rc.x;
+    o.events = rc.y;
+    o.shadows = rc.z;
+    out[p] = o;
+  }
+}
+
+// ---------------------------------------------------------------------------
+void launchRaygen(const KParams& P, int grid, cudaStream_t s) { k_raygen<<<grid, 256, 0, s>>>(P); }
+void launchShade(const KParams& P, int grid, cudaStream_t s) { k_shade<<<grid, 256, 0, s>>>(P); }
+void launchAccumulate(const KParams& P, uint32_t maxPix, uint32_t nranges, cudaStream_t s) {
+  dim3 g((maxPix + 255) / 256, nranges);
+  k_accumulate<<<g, 256, 0, s>>>(P);
+}
+void launchRecords(const KParams& P, asuna_path_record* out, int grid, cudaStream_t s) {
+  k_records<<<grid, 256, 0, s>>>(P, out);
+}
+
+}  // namespace asuna

@@ -1,0 +1,338 @@
+// trace.cu — two-level BVH traversal kernels (closest hit and occlusion).
+//
+// Software replacement for the RT-core traversal behind traceRayEXT
+// (src/shaders/raytrace.projective.rgen:108-109 closest hit with tmin 1e-5 and
+// tmax 1e10; rgen:117-122 occlusion with tmin 0, tmax dist - 2*EPS,
+// terminate-on-first-hit).  Facing culling is off, as the reference's
+// instances set VK_GEOMETRY_INSTANCE_TRIANGLE_FACING_CULL_DISABLE_BIT_KHR
+// (src/pipeline/pipeline_raytrace.cpp:132).
+//
+// Persistent warps fetch 32 rays at a time from the queue (one atomic per
+// warp); each thread walks TLAS -> BLAS with a per-thread stack in shared
+// memory (entry k of thread t at sstack[k * 128 + t], bank-conflict free).
+// Node and triangle records are read with 128-bit read-only loads.  The ray
+// is moved into object space and tested against triangles with the watertight
+// algorithm of Woop, Benthin and Wald (JCGT 2013) using explicitly rounded
+// operations, so the hits equal the CPU oracle's bit for bit; box tests use
+// (lo - o) * (1/d) with the far distance widened by 2^-20, which keeps them
+// conservative.
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+
+namespace asuna {
+namespace {
+
+struct WT {
+  int kx, ky, kz;
+  float Sx, Sy, Sz;
+};
+
+__device__ __forceinline__ float sel(float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+__device__ __forceinline__ WT wtPre(float3 d) {
+  WT w;
+  float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+  int kx = kz + 1 == 3 ? 0 : kz + 1;
+  int ky = kx + 1 == 3 ? 0 : kx + 1;
+  float dz = sel(d, kz);
+  if (dz < 0.0f) {
+    int t = kx;
+    kx = ky;
+    ky = t;
+  }
+  w.kx = kx;
+  w.ky = ky;
+  w.kz = kz;
+  w.Sx = __fdiv_rn(sel(d, kx), dz);
+  w.Sy = __fdiv_rn(sel(d, ky), dz);
+  w.Sz = __fdiv_rn(1.0f, dz);
+  return w;
+}
+
+// Watertight test; same operations and order as the CPU oracle.
+__device__ __forceinline__ bool wtTri(const WT& w, float3 o, float4 p0, float4 p1, float4 p2, float tmin, float tmax,
+                                      bool strict, float& t, float& b1, float& b2) {
+  const float3 A = make_float3(__fsub_rn(p0.x, o.x), __fsub_rn(p0.y, o.y), __fsub_rn(p0.z, o.z));
+  const float3 B = make_float3(__fsub_rn(p1.x, o.x), __fsub_rn(p1.y, o.y), __fsub_rn(p1.z, o.z));
+  const float3 C = make_float3(__fsub_rn(p2.x, o.x), __fsub_rn(p2.y, o.y), __fsub_rn(p2.z, o.z));
+  const float Akz = sel(A, w.kz), Bkz = sel(B, w.kz), Ckz = sel(C, w.kz);
+  const float Ax = __fsub_rn(sel(A, w.kx), __fmul_rn(w.Sx, Akz)), Ay = __fsub_rn(sel(A, w.ky), __fmul_rn(w.Sy, Akz));
+  const float Bx = __fsub_rn(sel(B, w.kx), __fmul_rn(w.Sx, Bkz)), By = __fsub_rn(sel(B, w.ky), __fmul_rn(w.Sy, Bkz));
+  const float Cx = __fsub_rn(sel(C, w.kx), __fmul_rn(w.Sx, Ckz)), Cy = __fsub_rn(sel(C, w.ky), __fmul_rn(w.Sy, Ckz));
+  float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+  float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+  float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+  if (U == 0.0f || V == 0.0f || W == 0.0f) {
+    U = __double2float_rn(__dsub_rn(__dmul_rn(double(Cx), double(By)), __dmul_rn(double(Cy), double(Bx))));
+    V = __double2float_rn(__dsub_rn(__dmul_rn(double(Ax), double(Cy)), __dmul_rn(double(Ay), double(Cx))));
+    W = __double2float_rn(__dsub_rn(__dmul_rn(double(Bx), double(Ay)), __dmul_rn(double(By), double(Ax))));
+  }
+  if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+  const float det = __fadd_rn(__fadd_rn(U, V), W);
+  if (det == 0.0f) return false;
+  const float Az = __fmul_rn(w.Sz, Akz), Bz = __fmul_rn(w.Sz, Bkz), Cz = __fmul_rn(w.Sz, Ckz);
+  const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+  const float rcp = __fdiv_rn(1.0f, det);
+  const float tt = __fmul_rn(T, rcp);
+  if (!(tt >= tmin && (strict ? tt < tmax : tt <= tmax))) return false;
+  t = tt;
+  b1 = __fmul_rn(V, rcp);
+  b2 = __fmul_rn(W, rcp);
+  return true;
+}
+
+__device__ __forceinline__ float3 safeInv(float3 d) {
+  auto inv = [](float x) { return 1.0f / (fabsf(x) > 1e-30f ? x : copysignf(1e-30f, x)); };
+  return make_float3(inv(d.x), inv(d.y), inv(d.z));
+}
+
+__device__ __forceinline__ void xformRay(const float4* w, float3 o, float3 d, float3& oo, float3& dd) {
+  float4 r0 = __ldg(&w[0]), r1 = __ldg(&w[1]), r2 = __ldg(&w[2]);
+  auto po = [&](float4 r) {
+    return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(r.x, o.x), __fmul_rn(r.y, o.y)), __fmul_rn(r.z, o.z)), r.w);
+  };
+  auto pd = [&](float4 r) { return __fadd_rn(__fadd_rn(__fmul_rn(r.x, d.x), __fmul_rn(r.y, d.y)), __fmul_rn(r.z, d.z)); };
+  oo = make_float3(po(r0), po(r1), po(r2));
+  dd = make_float3(pd(r0), pd(r1), pd(r2));
+}
+
+constexpr float kFarScale = 1.00000095367431640625f;  // 1 + 2^-20
+
+struct HitOut {
+  float t, u, v;
+  uint32_t prim, inst;
+};
+
+// Returns true on hit (closest hit fills `h`; any-hit returns at the first).
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool traverse(const SceneDev& S, float3 wo, float3 wd, float tmin, float tmax,
+                                         int32_t* stack, HitOut& h, uint32_t& nNodes, uint32_t& nTris,
+                                         bool& overflow) {
+  float3 o = wo, d = wd, id = safeInv(wd);
+  WT wt;
+  bool inBlas = false, found = false;
+  uint32_t curInst = 0;
+  float best = tmax;
+  int sp = 0;
+  int32_t ref = S.tlasRoot;
+  for (;;) {
+    if (ref >= 0) {
+      const BvhNode* n = S.nodes + ref;
+      const float4 xs = __ldg(&n->xs), ys = __ldg(&n->ys), zs = __ldg(&n->zs);
+      const int4 rr = __ldg(&n->ref);
+      if (COUNT) ++nNodes;
+      const float tx0 = (xs.x - o.x) * id.x, tx1 = (xs.y - o.x) * id.x;
+      const float ty0 = (ys.x - o.y) * id.y, ty1 = (ys.y - o.y) * id.y;
+      const float tz0 = (zs.x - o.z) * id.z, tz1 = (zs.y - o.z) * id.z;
+      const float ux0 = (xs.z - o.x) * id.x, ux1 = (xs.w - o.x) * id.x;
+      const float uy0 = (ys.z - o.y) * id.y, uy1 = (ys.w - o.y) * id.y;
+      const float uz0 = (zs.z - o.z) * id.z, uz1 = (zs.w - o.z) * id.z;
+      const float lim = found ? best : tmax;
+      const float a0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+      const float a1 = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), lim)) * kFarScale;
+      const float b0 = fmaxf(fmaxf(fminf(ux0, ux1), fminf(uy0, uy1)), fmaxf(fminf(uz0, uz1), tmin));
+      const float b1 = fminf(fminf(fmaxf(ux0, ux1), fmaxf(uy0, uy1)), fminf(fmaxf(uz0, uz1), lim)) * kFarScale;
+      const bool h0 = a0 <= a1, h1 = b0 <= b1;
+      if (h0 && h1) {
+        int32_t nearRef = rr.x, farRef = rr.y;
+        if (b0 < a0) {
+          nearRef = rr.y;
+          farRef = rr.x;
+        }
+        if (sp < kStackDepth) {
+          stack[sp * kTraceThreads] = farRef;
+          ++sp;
+        } else {
+          overflow = true;
+        }
+        ref = nearRef;
+        continue;
+      } else if (h0) {
+        ref = rr.x;
+        continue;
+      } else if (h1) {
+        ref = rr.y;
+        continue;
+      }
+    } else if (ref != kStackSentinel) {
+      if (!inBlas) {
+        // TLAS leaf: enter the instance's BLAS in object space
+        curInst = leafFirst(ref);
+        const InstDev* in = S.inst + curInst;
+        const int32_t root = __ldg(&in->blasRoot);
+        if (root >= 0) {
+          xformRay(in->w2o, wo, wd, o, d);
+          id = safeInv(d);
+          wt = wtPre(d);
+          if (sp < kStackDepth) {
+            inBlas = true;
+            stack[sp * kTraceThreads] = kStackSentinel;
+            ++sp;
+            ref = root;
+            continue;
+          }
+          overflow = true;
+        }
+      } else {
+        const uint32_t first = leafFirst(ref), cnt = leafCount(ref);
+        for (uint32_t k = 0; k < cnt; ++k) {
+          const TriDev* tr = S.tris + first + k;
+          const float4 p0 = __ldg(&tr->v0), p1 = __ldg(&tr->v1), p2 = __ldg(&tr->v2);
+          if (COUNT) ++nTris;
+          float t, b1, b2;
+          if (wtTri(wt, o, p0, p1, p2, tmin, best, found, t, b1, b2)) {
+            found = true;
+            best = t;
+            h.t = t;
+            h.u = b1;
+            h.v = b2;
+            h.prim = __float_as_uint(p0.w);
+            h.inst = curInst;
+            if (ANY) return true;
+          }
+        }
+      }
+    } else {
+      // leaving a BLAS: back to the world-space ray
+      inBlas = false;
+      o = wo;
+      d = wd;
+      id = safeInv(wd);
+    }
+    if (sp == 0) break;
+    --sp;
+    ref = stack[sp * kTraceThreads];
+  }
+  return found;
+}
+
+template <bool ANY, bool COUNT>
+__global__ void __launch_bounds__(kTraceThreads) k_trace(KParams P) {
+  __shared__ int32_t sstack[kStackDepth * kTraceThreads];
+  int32_t* stack = sstack + threadIdx.x;
+  const WaveDev& W = P.W;
+  const SceneDev& S = P.S;
+  const int cur = P.cur;
+  uint32_t* countPtr = ANY ? &W.cnt->c[kCntShadow] : &W.cnt->c[kCntExtend0 + cur];
+  uint32_t* fetch = ANY ? &W.cnt->c[kCntFetchShadow] : &W.cnt->c[kCntFetchExtend];
+  const uint32_t count = *countPtr;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (ANY) {
+      W.cnt->shadowRays += count;
+      W.cnt->c[kCntFetchExtend] = 0;  // the next extend pass fetches from 0
+    } else {
+      W.cnt->extendRays += count;
+      W.cnt->c[kCntExtend0 + (cur ^ 1)] = 0;  // shade appends into the other queue
+      W.cnt->c[kCntShadow] = 0;
+    }
+  }
+  const float4* rO = ANY ? W.shO : W.rayO[cur];
+  const float4* rD = ANY ? W.shD : W.rayD[cur];
+  const unsigned lane = threadIdx.x & 31u;
+  uint32_t nNodes = 0, nTris = 0;
+  bool overflow = false;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(fetch, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= count) break;
+    const uint32_t i = base + lane;
+    if (i < count) {
+      const float4 o4 = __ldg(&rO[i]);
+      const float4 d4 = __ldg(&rD[i]);
+      HitOut h;
+      if (ANY) {
+        const bool occ = traverse<true, COUNT>(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), 0.0f,
+                                               o4.w, stack, h, nNodes, nTris, overflow);
+        if (!occ) {
+          const uint32_t p = __float_as_uint(d4.w);
+          const float4 c = __ldg(&W.shC[i]);
+          float4 r = W.rad[p];
+          r.x = r.x + c.x;
+          r.y = r.y + c.y;
+          r.z = r.z + c.z;
+          W.rad[p] = r;
+          if (P.records) W.rec[p].y |= 1u << (P.depth - 1u);
+        }
+      } else {
+        const bool hit = traverse<false, COUNT>(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z),
+                                                0.00001f, 10000000000.0f, stack, h, nNodes, nTris, overflow);
+        if (hit) {
+          W.hit[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
+          W.hitInst[i] = h.inst;
+        } else {
+          W.hit[i] = make_float4(-1.0f, 0.0f, 0.0f, 0.0f);
+          W.hitInst[i] = 0xffffffffu;
+        }
+      }
+    }
+  }
+  if (overflow) atomicAdd(&W.cnt->stackOverflow, 1ull);
+  if (COUNT) {
+    unsigned long long a = nNodes, b = nTris;
+    for (int off = 16; off; off >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, off);
+      b += __shfl_down_sync(0xffffffffu, b, off);
+    }
+    if (lane == 0) {
+      atomicAdd(&W.cnt->nodes, a);
+      atomicAdd(&W.cnt->tris, b);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kTraceThreads) k_query(SceneDev S, const float4* o, const float4* d, uint32_t n,
+                                                         int anyHit, float4* hit, uint32_t* inst) {
+  __shared__ int32_t sstack[kStackDepth * kTraceThreads];
+  int32_t* stack = sstack + threadIdx.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 o4 = o[i], d4 = d[i];
+    HitOut h;
+    uint32_t a = 0, b = 0;
+    bool r, ovf = false;
+    if (anyHit)
+      r = traverse<true, false>(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), o4.w, d4.w, stack,
+                                h, a, b, ovf);
+    else
+      r = traverse<false, false>(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), o4.w, d4.w, stack,
+                                 h, a, b, ovf);
+    if (r) {
+      hit[i] = anyHit ? make_float4(1.0f, 0.0f, 0.0f, 0.0f) : make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
+      inst[i] = anyHit ? 0u : h.inst;
+    } else {
+      hit[i] = make_float4(-1.0f, 0.0f, 0.0f, 0.0f);
+      inst[i] = 0xffffffffu;
+    }
+  }
+}
+
+}  // namespace
+
+void launchExtend(const KParams& P, int grid, cudaStream_t s) {
+  if (P.counters)
+    k_trace<false, true><<<grid, kTraceThreads, 0, s>>>(P);
+  else
+    k_trace<false, false><<<grid, kTraceThreads, 0, s>>>(P);
+}
+void launchConnect(const KParams& P, int grid, cudaStream_t s) {
+  if (P.counters)
+    k_trace<true, true><<<grid, kTraceThreads, 0, s>>>(P);
+  else
+    k_trace<true, false><<<grid, kTraceThreads, 0, s>>>(P);
+}
+int traceBlocksPerSm() {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace<false, false>, kTraceThreads, 0);
+  return n > 0 ? n : 1;
+}
+void launchTraceQuery(const SceneDev& S, const float4* o, const float4* d, uint32_t n, int anyHit, float4* hit,
+                      uint32_t* inst, cudaStream_t s) {
+  int grid = int((n + kTraceThreads - 1) / kTraceThreads);
+  if (grid > 4096) grid = 4096;
+  if (grid < 1) grid = 1;
+  k_query<<<grid, kTraceThreads, 0, s>>>(S, o, d, n, anyHit, hit, inst);
+}
+
+}  // namespace asuna

@@ -1,0 +1,466 @@
+"""Scene assembly and the render context (Python mirror of the C ABI).
+
+``SceneBuilder`` assembles the device-ABI arrays the way the reference's
+``Scene`` class does (src/scene/scene.cpp:87-316): material 0 and light 0 are
+the reference's dummies, rect lights become two-triangle emitter instances,
+triangle (mesh-facet) lights one-triangle emitter instances.  ``Context`` owns
+one CUDA device + stream of the native library; scenes, films and renders go
+through the C ABI in include/asuna_rt.h.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _abi as A
+from ._abi import check, lib
+
+
+def default_material():
+    """Material() of src/core/material.h:9-35."""
+    m = A.Material()
+    m.ior = 1.5
+    m.roughness = 0.5
+    m.radiance_factor = A.f3(1.0, 1.0, 1.0)
+    for f in ("diffuse", "radiance", "metalness", "normal", "roughness", "tangent", "opacity"):
+        setattr(m, f + "_texture_id", -1)
+    m.type = A.MAT_LAMBERTIAN
+    return m
+
+
+def default_state():
+    """State() of src/core/state.h:15-63 (ray-tracing part)."""
+    s = A.RtState()
+    s.cur_frame = -1
+    s.spp = 1
+    s.max_path_depth = 3
+    s.env_map_intensity = 1.0
+    for f in ("diffuse", "specular", "roughness", "normal", "position", "tangent", "uv"):
+        setattr(s, f + "_out_channel", -1)
+    return s
+
+
+CHANNEL_NAMES = {"diffuse": A.CH_DIFFUSE, "albedo": A.CH_DIFFUSE, "normal": A.CH_NORMAL,
+                 "specular": A.CH_SPECULAR, "tangent": A.CH_TANGENT, "roughness": A.CH_ROUGHNESS,
+                 "position": A.CH_POSITION, "uv": A.CH_UV, "depth": A.CH_DEPTH}
+_FIELD = {A.CH_DIFFUSE: "diffuse", A.CH_NORMAL: "normal", A.CH_SPECULAR: "specular", A.CH_TANGENT: "tangent",
+          A.CH_ROUGHNESS: "roughness", A.CH_POSITION: "position", A.CH_UV: "uv"}
+
+
+def set_channels(state, names):
+    """multi_channel list -> out-channel slots (src/loader/loader.cpp:163-185).
+    Returns the slot of the depth channel (an addition; -1 if absent)."""
+    if len(names) > A.MAX_CHANNELS:
+        raise ValueError(f"channel numbers can not exceed {A.MAX_CHANNELS}")
+    state.n_multi_channel = len(names)
+    depth = -1
+    for i, n in enumerate(names):
+        kind = CHANNEL_NAMES[n]
+        if kind == A.CH_DEPTH:
+            depth = i
+        else:
+            setattr(state, _FIELD[kind] + "_out_channel", i)
+    return depth
+
+
+def _identity34():
+    return np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 0]], np.float32)
+
+
+class SceneBuilder:
+    """Host scene in the reference's device-ABI form."""
+
+    def __init__(self):
+        self.meshes = []  # (vertices[VERTEX_DTYPE], indices uint32 [3n])
+        self.mesh_names = []
+        self.materials = [default_material()]
+        self.material_names = ["add_by_default_dummy_material"]
+        self.lights = []
+        self.instances = []  # (transform 3x4, mesh, material, light)
+        self.env = None
+        dummy = A.Light()
+        dummy.type = A.LIGHT_DIRECTIONAL
+        dummy.double_side = 1
+        self.lights.append(dummy)
+
+    # -- materials (src/loader/material.cpp:104-231) --
+    def add_lambertian(self, name, diffuse):
+        m = default_material()
+        m.type = A.MAT_LAMBERTIAN
+        m.diffuse = A.f3(*diffuse)
+        return self._add_material(name, m)
+
+    def add_rough_plastic(self, name, diffuse, alpha, ior=1.5):
+        m = default_material()
+        m.type = A.MAT_ROUGH_PLASTIC
+        m.diffuse = A.f3(*diffuse)
+        m.aniso_alpha = (C.c_float * 2)(*alpha)
+        m.ior = ior
+        m.radiance[0] = lib().asuna_diffuse_fresnel(C.c_float(ior), 1000)
+        return self._add_material(name, m)
+
+    def add_dielectric(self, name, ior=1.5):
+        m = default_material()
+        m.type = A.MAT_DIELECTRIC
+        m.ior = ior
+        return self._add_material(name, m)
+
+    def _add_material(self, name, m):
+        if name in self.material_names:
+            raise ValueError(f"material [{name}] defined twice")
+        self.material_names.append(name)
+        self.materials.append(m)
+        return len(self.materials) - 1
+
+    # -- meshes / instances --
+    def add_mesh(self, name, vertices, indices):
+        v = np.ascontiguousarray(vertices, dtype=A.VERTEX_DTYPE)
+        i = np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1)
+        if i.size % 3:
+            raise ValueError("indices must hold whole triangles")
+        self.meshes.append((v, i))
+        self.mesh_names.append(name)
+        return len(self.meshes) - 1
+
+    def add_instance(self, mesh, material, transform=None):
+        m = self.mesh_names.index(mesh) if isinstance(mesh, str) else int(mesh)
+        mat = self.material_names.index(material) if isinstance(material, str) else int(material)
+        t = _identity34() if transform is None else np.asarray(transform, np.float32).reshape(3, 4)
+        self.instances.append((t, m, mat, -1))
+        return len(self.instances) - 1
+
+    # -- lights (src/scene/scene.cpp:220-283, src/loader/loader.cpp:270-332) --
+    def add_rect_light(self, position, v1, v2, radiance, double_side=False, triangle=False):
+        """JSON "rect" / "triangle" light: LightTypeRect, half area for "triangle"."""
+        p = np.asarray(position, np.float32)
+        u = np.asarray(v1, np.float32) - p
+        v = np.asarray(v2, np.float32) - p
+        l = A.Light()
+        l.type = A.LIGHT_RECT
+        l.position = A.f3(*p)
+        l.u = A.f3(*u)
+        l.v = A.f3(*v)
+        l.radiance = A.f3(*radiance)
+        area = float(np.linalg.norm(np.cross(u, v)))
+        l.area = area * 0.5 if triangle else area
+        l.double_side = 1 if double_side else 0
+        light_id = len(self.lights)
+        verts = np.zeros(4, A.VERTEX_DTYPE)
+        verts["pos"] = [p, p + u, p + u + v, p + v]
+        self.meshes.append((verts, np.array([0, 1, 2, 0, 2, 3], np.uint32)))
+        self.mesh_names.append(f"__rectLight:{light_id}")
+        self.instances.append((_identity34(), len(self.meshes) - 1, 0, light_id))
+        self.lights.append(l)
+        return light_id
+
+    def add_triangle_light(self, p0, p1, p2, radiance):
+        """One facet of a JSON "mesh" light: LightTypeTriangle, single sided."""
+        p0 = np.asarray(p0, np.float32)
+        u = np.asarray(p1, np.float32) - p0
+        v = np.asarray(p2, np.float32) - p0
+        l = A.Light()
+        l.type = A.LIGHT_TRIANGLE
+        l.position = A.f3(*p0)
+        l.u = A.f3(*u)
+        l.v = A.f3(*v)
+        l.radiance = A.f3(*radiance)
+        l.area = float(np.linalg.norm(np.cross(u, v))) * np.float32(0.5)
+        light_id = len(self.lights)
+        verts = np.zeros(3, A.VERTEX_DTYPE)
+        verts["pos"] = [p0, p0 + u, p0 + v]
+        self.meshes.append((verts, np.array([0, 1, 2], np.uint32)))
+        self.mesh_names.append(f"__meshLight:{light_id}")
+        self.instances.append((_identity34(), len(self.meshes) - 1, 0, light_id))
+        self.lights.append(l)
+        return light_id
+
+    def add_point_light(self, position, radiance):
+        l = A.Light()
+        l.type = A.LIGHT_POINT
+        l.position = A.f3(*position)
+        l.radiance = A.f3(*radiance)
+        self.lights.append(l)
+        return len(self.lights) - 1
+
+    def add_distant_light(self, direction, radiance):
+        l = A.Light()
+        l.type = A.LIGHT_DIRECTIONAL
+        l.direction = A.f3(*direction)
+        l.radiance = A.f3(*radiance)
+        self.lights.append(l)
+        return len(self.lights) - 1
+
+    def set_envmap(self, rgba):
+        rgba = np.ascontiguousarray(rgba, np.float32)
+        if rgba.ndim != 3 or rgba.shape[2] not in (3, 4):
+            raise ValueError("envmap must be HxWx3 or HxWx4")
+        if rgba.shape[2] == 3:
+            rgba = np.concatenate([rgba, np.ones(rgba.shape[:2] + (1,), np.float32)], axis=2)
+        self.env = np.ascontiguousarray(rgba)
+
+    @property
+    def num_lights(self):
+        return len(self.lights) - 1  # Scene::submit, scene.cpp:33
+
+    def state(self, spp=1, max_path_depth=3, channels=(), bg_color=(0, 0, 0), env_intensity=1.0):
+        s = default_state()
+        s.spp = spp
+        s.max_path_depth = max_path_depth
+        s.num_lights = self.num_lights
+        s.bg_color = A.f3(*bg_color)
+        s.env_map_intensity = env_intensity
+        if self.env is not None:
+            s.has_env_map = 1
+            s.env_map_resolution = (C.c_float * 2)(self.env.shape[1], self.env.shape[0])
+        depth = set_channels(s, list(channels))
+        return s, depth
+
+    def desc(self):
+        return SceneDescHandle(self)
+
+
+class SceneDescHandle:
+    """An asuna_scene_desc whose arrays stay alive with this object."""
+
+    def __init__(self, b):
+        self._keep = []
+        nm = len(b.meshes)
+        self.meshes = (A.MeshDesc * max(nm, 1))()
+        for k, (v, i) in enumerate(b.meshes):
+            self.meshes[k] = A.MeshDesc(len(v), i.size // 3, v.ctypes.data, i.ctypes.data)
+            self._keep += [v, i]
+        ni = len(b.instances)
+        self.instances = (A.InstanceDesc * max(ni, 1))()
+        for k, (t, m, mat, light) in enumerate(b.instances):
+            d = self.instances[k]
+            d.transform = (C.c_float * 12)(*np.asarray(t, np.float32).reshape(-1))
+            d.mesh_id = m
+            d.material_id = mat
+            d.light_id = light
+        self.materials = (A.Material * len(b.materials))(*b.materials)
+        self.lights = (A.Light * len(b.lights))(*b.lights)
+        d = A.SceneDesc()
+        d.num_meshes = nm
+        d.meshes = self.meshes
+        d.num_instances = ni
+        d.instances = self.instances
+        d.num_materials = len(b.materials)
+        d.materials = self.materials
+        d.num_lights = len(b.lights)
+        d.lights = self.lights
+        if b.env is not None:
+            d.envmap.width = b.env.shape[1]
+            d.envmap.height = b.env.shape[0]
+            d.envmap.rgba = b.env.ctypes.data
+            self._keep.append(b.env)
+        self.desc = d
+
+    @property
+    def ptr(self):
+        return C.byref(self.desc)
+
+
+def perspective_camera(eye, lookat, up, fov, width, height, aperture=0.0, focal_distance=0.1):
+    """GpuCamera of CameraPerspective::toGpuStruct (src/core/camera.cpp:87-99);
+    fov in degrees is horizontal."""
+    cam = A.Camera()
+    e, l, u = (np.asarray(x, np.float32) for x in (eye, lookat, up))
+    check(lib().asuna_camera_perspective(A.fptr(e), A.fptr(l), A.fptr(u), fov, aperture, focal_distance, width,
+                                         height, C.byref(cam)))
+    return cam
+
+
+def opencv_camera(eye, lookat, up, fxfycxcy):
+    cam = A.Camera()
+    e, l, u, f = (np.asarray(x, np.float32) for x in (eye, lookat, up, fxfycxcy))
+    check(lib().asuna_camera_opencv(A.fptr(e), A.fptr(l), A.fptr(u), A.fptr(f), C.byref(cam)))
+    return cam
+
+
+def make_shot(camera, state, width, height, frames, frame0=0, seed=0, depth_channel=-1, rr_depth=None):
+    s = A.Shot()
+    s.camera = camera
+    s.state = state
+    s.width, s.height = width, height
+    s.frames = frames
+    s.frame0 = frame0
+    s.seed = seed
+    s.depth_out_channel = depth_channel
+    if rr_depth is not None:
+        s.flags |= A.SHOT_RR
+        s.rr_depth = rr_depth
+    return s
+
+
+class Film:
+    def __init__(self, ctx, width, height):
+        self.ctx = ctx
+        self.width, self.height = width, height
+        h = C.c_void_p()
+        check(lib().asuna_film_create(ctx.handle, width, height, C.byref(h)))
+        self.handle = h
+
+    def read(self, image=0, out=None):
+        if out is None:
+            out = np.empty((self.height, self.width, 4), np.float32)
+        check(lib().asuna_film_read(self.ctx.handle, self.handle, image, out.ctypes.data))
+        return out
+
+    def clear(self):
+        check(lib().asuna_film_clear(self.ctx.handle, self.handle))
+
+    def close(self):
+        if self.handle:
+            lib().asuna_film_destroy(self.handle)
+            self.handle = None
+
+    __del__ = close
+
+
+class DeviceScene:
+    def __init__(self, ctx, desc):
+        self.ctx = ctx
+        h = C.c_void_p()
+        check(lib().asuna_scene_create(ctx.handle, desc.ptr, C.byref(h)))
+        self.handle = h
+
+    def stats(self):
+        s = A.SceneStats()
+        check(lib().asuna_scene_get_stats(self.handle, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in A.SceneStats._fields_}
+
+    def trace(self, origins, dirs, tmin=1e-5, tmax=1e10, any_hit=False):
+        n = len(origins)
+        rays = np.zeros((n, 8), np.float32)
+        rays[:, 0:3] = origins
+        rays[:, 3] = tmin
+        rays[:, 4:7] = dirs
+        rays[:, 7] = tmax
+        hits = np.zeros((n, 4), np.float32)
+        inst = np.zeros(n, np.uint32)
+        check(lib().asuna_scene_trace(self.ctx.handle, self.handle, rays.ctypes.data, n, 1 if any_hit else 0,
+                                      hits.ctypes.data, inst.ctypes.data))
+        return hits, inst
+
+    def close(self):
+        if self.handle:
+            lib().asuna_scene_destroy(self.handle)
+            self.handle = None
+
+    __del__ = close
+
+
+def _stats_dict(s):
+    return {k: getattr(s, k) for k, _ in A.RenderStats._fields_}
+
+
+class Context:
+    """One CUDA device + stream of the native library (asuna_ctx)."""
+
+    def __init__(self, device=0):
+        h = C.c_void_p()
+        check(lib().asuna_ctx_create(device, C.byref(h)))
+        self.handle = h
+
+    def set_counters(self, on):
+        check(lib().asuna_ctx_set_counters(self.handle, 1 if on else 0))
+
+    def set_path_budget(self, nbytes):
+        check(lib().asuna_ctx_set_path_budget(self.handle, int(nbytes)))
+
+    def create_scene(self, desc):
+        return DeviceScene(self, desc)
+
+    def create_film(self, width, height):
+        return Film(self, width, height)
+
+    def render(self, scene, shot, film, stats=False):
+        st = A.RenderStats() if stats else None
+        check(lib().asuna_render(self.handle, scene.handle, C.byref(shot), film.handle,
+                                 C.byref(st) if st is not None else None))
+        return _stats_dict(st) if st is not None else None
+
+    def render_batch(self, scene, shots, films, stats=False):
+        n = len(shots)
+        sh = (A.Shot * n)(*shots)
+        fh = (C.c_void_p * n)(*[f.handle for f in films])
+        st = A.RenderStats() if stats else None
+        check(lib().asuna_render_batch(self.handle, scene.handle, sh, fh, n, C.byref(st) if st is not None else None))
+        return _stats_dict(st) if st is not None else None
+
+    def render_paths(self, scene, shot, film):
+        rec = np.zeros(shot.frames * shot.width * shot.height, A.PATH_RECORD_DTYPE)
+        check(lib().asuna_render_paths(self.handle, scene.handle, C.byref(shot), film.handle, rec.ctypes.data))
+        return rec
+
+    def sync(self):
+        check(lib().asuna_ctx_sync(self.handle))
+
+    def run_offline(self, scene_json, out_prefix):
+        check(lib().asuna_tracer_run_offline(self.handle, scene_json.encode(), out_prefix.encode()))
+
+    def close(self):
+        if self.handle:
+            lib().asuna_ctx_destroy(self.handle)
+            self.handle = None
+
+    __del__ = close
+
+
+class JsonScene:
+    """A scene file parsed and assembled by the native host code
+    (Loader::parse + Scene, src/loader/loader.cpp:91-144)."""
+
+    def __init__(self, path=None, text=None, base_dir="."):
+        h = C.c_void_p()
+        if path is not None:
+            check(lib().asuna_json_load(path.encode(), C.byref(h)))
+        else:
+            check(lib().asuna_json_load_string(text.encode(), base_dir.encode(), C.byref(h)))
+        self.handle = h
+
+    def desc(self):
+        d = A.SceneDesc()
+        check(lib().asuna_json_scene_desc(self.handle, C.byref(d)))
+        return _DescView(d, self)
+
+    def shots(self):
+        n = C.c_uint32()
+        check(lib().asuna_json_num_shots(self.handle, C.byref(n)))
+        out = []
+        for i in range(n.value):
+            s = A.Shot()
+            check(lib().asuna_json_get_shot(self.handle, i, C.byref(s)))
+            out.append(s)
+        return out
+
+    def channels(self):
+        n = C.c_uint32()
+        kinds = (C.c_int32 * A.MAX_CHANNELS)()
+        check(lib().asuna_json_channels(self.handle, C.byref(n), kinds))
+        return list(kinds[: n.value])
+
+    def close(self):
+        if self.handle:
+            lib().asuna_json_free(self.handle)
+            self.handle = None
+
+    __del__ = close
+
+
+class _DescView:
+    def __init__(self, d, owner):
+        self.desc = d
+        self._owner = owner
+
+    @property
+    def ptr(self):
+        return C.byref(self.desc)
+
+
+def envmap_tables(rgba):
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    h, w = rgba.shape[:2]
+    marg = np.zeros((h, w, 2), np.float32)
+    cond = np.zeros((h, w, 2), np.float32)
+    check(lib().asuna_envmap_tables(w, h, rgba.ctypes.data, marg.ctypes.data, cond.ctypes.data))
+    return marg, cond

@@ -1,0 +1,218 @@
+"""Seeded procedural scenes of the benchmark configurations.
+
+* ``box_scene``   — small closed box (5 quads, 10 triangles, open toward the
+  camera), two cuboids rotated +-18 deg about y (24 triangles), Lambertian
+  white 0.73 / red (0.65,0.05,0.05) / green (0.12,0.45,0.15), one 0.5 x 0.4
+  rectangle light at the ceiling with radiance (17,12,4), pinhole camera at
+  z = 3.9 with a 40 deg field of view.
+* ``mixed_scene`` — N subdivided icospheres (level 7: 327,680 triangles each)
+  displaced by seeded 3-octave value noise (amplitude 0.05), placed uniformly
+  in a 20^3 box above a ground quad; materials 40% Lambertian (albedo
+  U[0.1,0.9]^3), 40% rough plastic (GGX alpha U[0.05,0.8], ior 1.5), 20%
+  dielectric (ior 1.5); a 1024x512 environment map, lognormal(0, 1.5) per
+  texel with one 8x8 hotspot x1000; 4 triangle lights; thin-lens camera with
+  aperture 0.05.
+
+All data are synthetic (no dataset): shapes and value distributions follow
+the configurations, values come from numpy's seeded generator.
+"""
+import math
+
+import numpy as np
+
+from . import _abi as A
+from .scene import SceneBuilder, make_shot, perspective_camera
+
+
+def _quad(p0, p1, p2, p3, normal):
+    v = np.zeros(4, A.VERTEX_DTYPE)
+    v["pos"] = [p0, p1, p2, p3]
+    v["normal"] = normal
+    v["uv"] = [(0, 0), (1, 0), (1, 1), (0, 1)]
+    return v, np.array([0, 1, 2, 0, 2, 3], np.uint32)
+
+
+def cuboid_mesh(hx, hy, hz):
+    """Axis-aligned cuboid centred at the origin, 24 vertices (flat faces), 12 triangles."""
+    faces = []
+    for axis in range(3):
+        for sgn in (-1.0, 1.0):
+            n = np.zeros(3, np.float32)
+            n[axis] = sgn
+            u = np.zeros(3, np.float32)
+            w = np.zeros(3, np.float32)
+            u[(axis + 1) % 3] = 1
+            w[(axis + 2) % 3] = 1
+            if sgn < 0:
+                u, w = w, u
+            h = np.array([hx, hy, hz], np.float32)
+            c = n * h
+            du, dw = u * h, w * h
+            faces.append(_quad(c - du - dw, c + du - dw, c + du + dw, c - du + dw, n))
+    verts = np.concatenate([f[0] for f in faces])
+    idx = np.concatenate([f[1] + 4 * k for k, f in enumerate(faces)]).astype(np.uint32)
+    return verts, idx
+
+
+def rot_y(deg, t):
+    a = math.radians(deg)
+    c, s = math.cos(a), math.sin(a)
+    return np.array([[c, 0, s, t[0]], [0, 1, 0, t[1]], [-s, 0, c, t[2]]], np.float32)
+
+
+def box_scene(width=256, height=256, frames=16, max_depth=8, channels=("albedo", "normal", "depth"), seed=0):
+    """The small box scene; returns (builder, shot)."""
+    b = SceneBuilder()
+    white = b.add_lambertian("white", (0.73, 0.73, 0.73))
+    red = b.add_lambertian("red", (0.65, 0.05, 0.05))
+    green = b.add_lambertian("green", (0.12, 0.45, 0.15))
+    # the light is added first, as the reference's loader parses lights before meshes
+    b.add_rect_light((-0.25, 0.999, -0.2), (0.25, 0.999, -0.2), (-0.25, 0.999, 0.2), (17.0, 12.0, 4.0))
+    quads = {
+        "floor": ([(-1, -1, -1), (1, -1, -1), (1, -1, 1), (-1, -1, 1)], (0, 1, 0), white),
+        "ceiling": ([(-1, 1, 1), (1, 1, 1), (1, 1, -1), (-1, 1, -1)], (0, -1, 0), white),
+        "back": ([(-1, -1, -1), (-1, 1, -1), (1, 1, -1), (1, -1, -1)], (0, 0, 1), white),
+        "left": ([(-1, -1, 1), (-1, 1, 1), (-1, 1, -1), (-1, -1, -1)], (1, 0, 0), red),
+        "right": ([(1, -1, -1), (1, 1, -1), (1, 1, 1), (1, -1, 1)], (-1, 0, 0), green),
+    }
+    for name, (pts, n, mat) in quads.items():
+        v, i = _quad(*[np.array(p, np.float32) for p in pts], np.array(n, np.float32))
+        b.add_mesh(name, v, i)
+        b.add_instance(name, mat)
+    v, i = cuboid_mesh(0.3, 0.3, 0.3)
+    b.add_mesh("short_box", v, i)
+    b.add_instance("short_box", white, rot_y(-18.0, (0.35, -0.7, 0.35)))
+    v, i = cuboid_mesh(0.3, 0.6, 0.3)
+    b.add_mesh("tall_box", v, i)
+    b.add_instance("tall_box", white, rot_y(18.0, (-0.35, -0.4, -0.35)))
+    state, depth = b.state(spp=frames, max_path_depth=max_depth, channels=channels)
+    cam = perspective_camera((0, 0, 3.9), (0, 0, 0), (0, 1, 0), 40.0, width, height)
+    return b, make_shot(cam, state, width, height, frames, seed=seed, depth_channel=depth)
+
+
+# ---- icospheres + value noise ---------------------------------------------------
+def icosphere(level):
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = np.array([(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+                  (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)], np.float64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    f = np.array([(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+                  (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5),
+                  (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)], np.int64)
+    for _ in range(level):
+        a, b_, c = f[:, 0], f[:, 1], f[:, 2]
+        e = np.concatenate([np.stack([a, b_], 1), np.stack([b_, c], 1), np.stack([c, a], 1)])
+        lo, hi = e.min(1), e.max(1)
+        key = lo * len(v) + hi
+        uk, inv = np.unique(key, return_inverse=True)
+        mid = v[uk // len(v)] + v[uk % len(v)]
+        mid /= np.linalg.norm(mid, axis=1, keepdims=True)
+        base = len(v)
+        v = np.concatenate([v, mid])
+        m = inv.reshape(3, -1) + base
+        ab, bc, ca = m[0], m[1], m[2]
+        f = np.concatenate([np.stack([a, ab, ca], 1), np.stack([b_, bc, ab], 1), np.stack([c, ca, bc], 1),
+                            np.stack([ab, bc, ca], 1)])
+    return v, f
+
+
+def _hash3(ix, iy, iz, seed):
+    h = (ix.astype(np.uint32) * np.uint32(73856093)) ^ (iy.astype(np.uint32) * np.uint32(19349663)) ^ \
+        (iz.astype(np.uint32) * np.uint32(83492791)) ^ np.uint32(seed)
+    h ^= h >> np.uint32(16)
+    h *= np.uint32(0x7FEB352D)
+    h ^= h >> np.uint32(15)
+    h *= np.uint32(0x846CA68B)
+    h ^= h >> np.uint32(16)
+    return h.astype(np.float64) * (2.0 / 4294967295.0) - 1.0
+
+
+def value_noise(p, seed):
+    """3D value noise in [-1, 1]: hashed lattice values, smoothstep-trilinear."""
+    fl = np.floor(p)
+    i = fl.astype(np.int64)
+    t = p - fl
+    w = t * t * (3.0 - 2.0 * t)
+    out = np.zeros(len(p))
+    for dx in (0, 1):
+        for dy in (0, 1):
+            for dz in (0, 1):
+                val = _hash3(i[:, 0] + dx, i[:, 1] + dy, i[:, 2] + dz, seed)
+                wx = w[:, 0] if dx else 1 - w[:, 0]
+                wy = w[:, 1] if dy else 1 - w[:, 1]
+                wz = w[:, 2] if dz else 1 - w[:, 2]
+                out += val * wx * wy * wz
+    return out
+
+
+def displaced_sphere(base_v, faces, seed, amplitude=0.05, octaves=3, freq=2.0):
+    n = np.zeros(len(base_v))
+    amp, norm = 1.0, 0.0
+    for o in range(octaves):
+        n += amp * value_noise(base_v * (freq * 2 ** o) + 17.0 * o, seed * 7919 + o)
+        norm += amp
+        amp *= 0.5
+    pos = base_v * (1.0 + amplitude * n / norm)[:, None]
+    # area-weighted vertex normals of the displaced surface
+    e1 = pos[faces[:, 1]] - pos[faces[:, 0]]
+    e2 = pos[faces[:, 2]] - pos[faces[:, 0]]
+    fn = np.cross(e1, e2)
+    vn = np.zeros_like(pos)
+    for k in range(3):
+        for c in range(3):
+            vn[:, c] += np.bincount(faces[:, k], weights=fn[:, c], minlength=len(pos))
+    vn /= np.maximum(np.linalg.norm(vn, axis=1, keepdims=True), 1e-30)
+    v = np.zeros(len(pos), A.VERTEX_DTYPE)
+    v["pos"] = pos.astype(np.float32)
+    v["normal"] = vn.astype(np.float32)
+    return v
+
+
+def lognormal_envmap(rng, width=1024, height=512, hotspot=8, boost=1000.0):
+    env = rng.lognormal(0.0, 1.5, size=(height, width, 3)).astype(np.float32)
+    y = int(rng.integers(height // 8, height // 3))
+    x = int(rng.integers(0, width - hotspot))
+    env[y:y + hotspot, x:x + hotspot] *= np.float32(boost)
+    return env
+
+
+def mixed_scene(width=1920, height=1080, frames=64, max_depth=12, n_spheres=64, level=7, seed=1234,
+                rr_depth=3, env_size=(1024, 512), channels=("albedo", "normal", "depth"), verbose=False):
+    """The mid-size mixed-material scene; returns (builder, shot)."""
+    rng = np.random.default_rng(seed)
+    b = SceneBuilder()
+    # lights first (the reference's loader order): 4 triangle lights above the spheres
+    for k in range(4):
+        cx, cz = -6.0 + 4.0 * k, float(rng.uniform(-6, 6))
+        y = 14.0
+        b.add_triangle_light((cx - 1.2, y, cz - 1.0), (cx, y, cz + 1.4), (cx + 1.2, y, cz - 1.0), (40.0, 38.0, 34.0))
+    b.set_envmap(lognormal_envmap(rng, env_size[0], env_size[1]))
+    ground = b.add_lambertian("ground", (0.5, 0.5, 0.5))
+    v, i = _quad(np.array((-40, -11, 40), np.float32), np.array((40, -11, 40), np.float32),
+                 np.array((40, -11, -40), np.float32), np.array((-40, -11, -40), np.float32),
+                 np.array((0, 1, 0), np.float32))
+    b.add_mesh("ground", v, i)
+    b.add_instance("ground", ground)
+    base_v, faces = icosphere(level)
+    idx = faces.astype(np.uint32).reshape(-1)
+    for k in range(n_spheres):
+        u = rng.random()
+        if u < 0.4:
+            mat = b.add_lambertian(f"m{k}", rng.uniform(0.1, 0.9, 3))
+        elif u < 0.8:
+            a = float(rng.uniform(0.05, 0.8))
+            mat = b.add_rough_plastic(f"m{k}", rng.uniform(0.1, 0.9, 3), (a, a), 1.5)
+        else:
+            mat = b.add_dielectric(f"m{k}", 1.5)
+        pos = rng.uniform(-10.0, 10.0, 3)
+        b.add_mesh(f"sphere{k}", displaced_sphere(base_v, faces, seed + 31 * k), idx)
+        b.add_instance(f"sphere{k}", mat, np.array([[1, 0, 0, pos[0]], [0, 1, 0, pos[1]], [0, 0, 1, pos[2]]],
+                                                   np.float32))
+        if verbose and k % 16 == 15:
+            print(f"mixed_scene: {k + 1}/{n_spheres} spheres", flush=True)
+    state, depth = b.state(spp=frames, max_path_depth=max_depth, channels=channels)
+    eye, at = np.array((0.0, 4.0, 30.0)), np.array((0.0, -2.0, 0.0))
+    cam = perspective_camera(eye, at, (0, 1, 0), 50.0, width, height, aperture=0.05,
+                             focal_distance=float(np.linalg.norm(eye - at)))
+    shot = make_shot(cam, state, width, height, frames, seed=0, depth_channel=depth, rr_depth=rr_depth)
+    return b, shot

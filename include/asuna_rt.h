@@ -1,0 +1,389 @@
+/*
+ * asuna_rt.h — C ABI of the GB300 path-tracer core.
+ *
+ * This is the drop-in boundary for Asuna's Vulkan ray-tracing path
+ * (camera rays -> BVH traversal -> BSDF/NEE/MIS shading -> accumulation into
+ * radiance/AOV images).  Every entry point takes plain pointers and sizes and
+ * returns an int status (ASUNA_OK == 0); the text of the last failure on the
+ * calling thread is returned by asuna_last_error().  No call ever exits the
+ * process (the reference calls exit(1) on every error, src/loader/utils.h:11-16).
+ *
+ * Device ABI.  The structs below are byte-for-byte the reference's shared
+ * host/shader structs (src/shared/), so a caller that already fills
+ * GpuVertex / GpuMaterial / GpuLight / GpuCamera / GpuPushConstantRaytrace can
+ * pass its arrays unchanged.  Matrices are 16 floats in column-major order,
+ * the GLSL/nvmath convention of the reference (src/shared/camera.h:15-24).
+ *
+ * Replaced reference interfaces (file:line in the reference project):
+ *   asuna_scene_create      Scene::submit (src/scene/scene.cpp:26-85) +
+ *                           PipelineRaytrace::createBottomLevelAS/TopLevelAS
+ *                           (src/pipeline/pipeline_raytrace.cpp:107-147)
+ *   asuna_render            the offline frame loop of Tracer::runOffline
+ *                           (src/tracer/tracer.cpp:204-258) around
+ *                           PipelineRaytrace::run (pipeline_raytrace.cpp:36-74)
+ *   asuna_film_read         Tracer::saveBufferToImage read-back
+ *                           (src/tracer/tracer.cpp:313-395)
+ *   asuna_json_load         Loader::loadSceneFromJson + Loader::parse
+ *                           (src/loader/loader.cpp:67-144) with Scene::reset /
+ *                           addLight / addInstance (src/scene/scene.cpp:87-316)
+ *   asuna_tracer_run_offline Tracer::runOffline + callSavingImage
+ *                           (src/tracer/tracer.cpp:177-291)
+ */
+#ifndef ASUNA_RT_H
+#define ASUNA_RT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ASUNA_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  ASUNA_OK = 0,
+  ASUNA_ERR_INVALID = 1,     /* bad argument, size or handle               */
+  ASUNA_ERR_CUDA = 2,        /* a CUDA runtime call failed                 */
+  ASUNA_ERR_OOM = 3,         /* device or host allocation failed           */
+  ASUNA_ERR_IO = 4,          /* file could not be read or written          */
+  ASUNA_ERR_PARSE = 5,       /* JSON / OBJ / image syntax or schema error  */
+  ASUNA_ERR_TIMEOUT = 6,     /* a bounded device wait gave up              */
+  ASUNA_ERR_UNSUPPORTED = 7, /* feature outside the implemented plugin set */
+  ASUNA_ERR_NO_DEVICE = 8    /* no CUDA device / library built without it  */
+};
+
+/* ---- enums of the reference's plugin dispatch --------------------------- */
+/* CameraType, src/shared/camera.h:7-11 */
+enum { ASUNA_CAMERA_PERSPECTIVE = 0, ASUNA_CAMERA_OPENCV = 1, ASUNA_CAMERA_UNDEFINED = 2 };
+/* LightType, src/shared/light.h:7-13 */
+enum {
+  ASUNA_LIGHT_DIRECTIONAL = 0,
+  ASUNA_LIGHT_RECT = 1,
+  ASUNA_LIGHT_TRIANGLE = 2,
+  ASUNA_LIGHT_POINT = 3,
+  ASUNA_LIGHT_UNDEFINED = 4
+};
+/* MaterialType, src/shared/material.h:7-21 (only the three marked (*) are
+ * implemented; others are rejected with ASUNA_ERR_UNSUPPORTED) */
+enum {
+  ASUNA_MAT_LAMBERTIAN = 0, /* (*) brdf_lambertian   */
+  ASUNA_MAT_KANG18 = 1,
+  ASUNA_MAT_EMISSIVE = 2,
+  ASUNA_MAT_PBR_METALNESS_ROUGHNESS = 3,
+  ASUNA_MAT_PLASTIC = 4,
+  ASUNA_MAT_ROUGH_PLASTIC = 5, /* (*) brdf_rough_plastic */
+  ASUNA_MAT_CONDUCTOR = 6,
+  ASUNA_MAT_ROUGH_CONDUCTOR = 7,
+  ASUNA_MAT_MIRROR = 8,
+  ASUNA_MAT_DISNEY = 9,
+  ASUNA_MAT_DIELECTRIC = 10, /* (*) bsdf_dielectric    */
+  ASUNA_MAT_PHONG = 11,
+  ASUNA_MAT_NUM = 12
+};
+
+/* Number of RGBA32F output images of the reference: image 0 = radiance,
+ * 1..7 = multi-channel AOVs, 8 = filter-weight sum (src/shared/binding.h:70). */
+#define ASUNA_NUM_OUTPUT_IMAGES 9
+#define ASUNA_MAX_CHANNELS 7
+
+/* AOV channel kinds; "multi_channel" strings of src/loader/loader.cpp:177-183.
+ * ASUNA_CH_DEPTH (primary-hit distance) is an addition of this library. */
+enum {
+  ASUNA_CH_DIFFUSE = 0, /* "diffuse" (alias "albedo") */
+  ASUNA_CH_NORMAL = 1,
+  ASUNA_CH_SPECULAR = 2,
+  ASUNA_CH_TANGENT = 3,
+  ASUNA_CH_ROUGHNESS = 4,
+  ASUNA_CH_POSITION = 5,
+  ASUNA_CH_UV = 6,
+  ASUNA_CH_DEPTH = 7
+};
+
+/* ---- device ABI structs (byte-identical to src/shared/) --------------- */
+
+/* GpuVertex, src/shared/vertex.h:6-11 — 44 bytes, scalar layout. */
+typedef struct asuna_vertex {
+  float pos[3];
+  float uv[2];
+  float normal[3];
+  float tangent[3];
+} asuna_vertex;
+
+/* GpuMaterial, src/shared/material.h:24-49 — 132 bytes, scalar layout.
+ * For rough plastic, radiance[0] holds fdrInt (src/loader/material.cpp:230). */
+typedef struct asuna_material {
+  float diffuse[3];
+  float rho_spec[3];
+  float aniso_alpha[2];
+  float ior;
+  float roughness;
+  float subsurface;
+  float specular;
+  float specular_tint;
+  float anisotropic;
+  float sheen;
+  float sheen_tint;
+  float clearcoat;
+  float clearcoat_gloss;
+  float radiance[3];
+  float metalness;
+  float radiance_factor[3];
+  int32_t diffuse_texture_id;
+  int32_t roughness_texture_id;
+  int32_t metalness_texture_id;
+  int32_t radiance_texture_id;
+  int32_t normal_texture_id;
+  int32_t tangent_texture_id;
+  int32_t opacity_texture_id;
+  uint32_t type;
+} asuna_material;
+
+/* GpuLight, src/shared/light.h:16-25 — 76 bytes, scalar layout. */
+typedef struct asuna_light {
+  int32_t type;
+  float position[3];
+  float direction[3];
+  float radiance[3];
+  float u[3];
+  float v[3];
+  float radius;
+  float area;
+  uint32_t double_side;
+} asuna_light;
+
+/* GpuCamera, src/shared/camera.h:15-24 — 224 bytes, std140 layout. */
+typedef struct asuna_camera {
+  float raster_to_camera[16];
+  float camera_to_world[16];
+  float env_transform[16];
+  float fxfycxcy[4];
+  uint32_t type;
+  float aperture;
+  float focal_distance;
+  float padding;
+} asuna_camera;
+
+/* GpuPushConstantRaytrace, src/shared/pushconstant.h:10-34 — 84 bytes. */
+typedef struct asuna_rt_state {
+  int32_t spp;
+  int32_t cur_frame;
+  int32_t max_path_depth;
+  int32_t num_lights;
+  float bg_color[3];
+  uint32_t use_face_normal;
+  uint32_t ignore_emissive;
+  uint32_t has_env_map;
+  float env_map_resolution[2];
+  float env_map_intensity;
+  uint32_t n_multi_channel;
+  int32_t diffuse_out_channel;
+  int32_t specular_out_channel;
+  int32_t roughness_out_channel;
+  int32_t normal_out_channel;
+  int32_t position_out_channel;
+  int32_t tangent_out_channel;
+  int32_t uv_out_channel;
+} asuna_rt_state;
+
+/* ---- scene description (the reference's device buffers, flattened) ------ */
+
+/* One mesh = one BLAS of the reference (src/core/mesh.cpp:147-192):
+ * opaque triangles, uint32 indices, GpuVertex attributes. */
+typedef struct asuna_mesh_desc {
+  uint32_t num_vertices;
+  uint32_t num_triangles;
+  const asuna_vertex* vertices; /* num_vertices entries            */
+  const uint32_t* indices;      /* 3 * num_triangles entries       */
+} asuna_mesh_desc;
+
+/* One TLAS instance (src/core/instance.h:46-68, src/shared/instance.h:7-16).
+ * transform: object->world, 3 rows x 4 columns, row-major (the 3x4 of
+ * VkTransformMatrixKHR).  light_id >= 0 marks an emitter instance whose hits
+ * run the light branch of the Lambertian hit shader; material_id is then unused. */
+typedef struct asuna_instance_desc {
+  float transform[12];
+  uint32_t mesh_id;
+  int32_t material_id;
+  int32_t light_id;
+  uint32_t reserved;
+} asuna_instance_desc;
+
+/* Equirectangular environment map (src/core/texture.cpp:144-226).  The
+ * inverse-CDF tables are computed by the library from the texels. */
+typedef struct asuna_envmap_desc {
+  uint32_t width;
+  uint32_t height;
+  const float* rgba; /* width*height*4 floats, row-major, NULL = none */
+} asuna_envmap_desc;
+
+typedef struct asuna_scene_desc {
+  uint32_t num_meshes;
+  const asuna_mesh_desc* meshes;
+  uint32_t num_instances;
+  const asuna_instance_desc* instances;
+  uint32_t num_materials;
+  const asuna_material* materials;
+  uint32_t num_lights; /* lights[0] is the reference's dummy light   */
+  const asuna_light* lights;
+  asuna_envmap_desc envmap;
+} asuna_scene_desc;
+
+/* ---- shots ----------------------------------------------------------------
+ * One shot = one camera pose + pipeline state rendered for `frames` frames of
+ * one sample each, exactly the offline loop of src/tracer/tracer.cpp:204-258:
+ * frame f hashes (x, y, f) into the pixel seed and frame 0 samples the pixel
+ * centre.  frame0 > 0 resumes an existing film.  `seed` is folded into the
+ * hashed frame word (seed 0 = the reference's streams). */
+enum {
+  ASUNA_SHOT_RR = 1u << 0 /* Russian roulette after rr_depth (extension; off = reference) */
+};
+
+typedef struct asuna_shot {
+  asuna_camera camera;
+  asuna_rt_state state; /* state.spp and state.cur_frame are ignored */
+  uint32_t width;
+  uint32_t height;
+  uint32_t frames;
+  uint32_t frame0;
+  uint32_t seed;
+  uint32_t flags;
+  uint32_t rr_depth;
+  int32_t depth_out_channel; /* AOV slot (0..6) of the depth channel, -1 = none */
+} asuna_shot;
+
+/* Per-path record for parity checks (one per (frame, pixel)). */
+typedef struct asuna_path_record {
+  float radiance[3];   /* path radiance before the [0,10] clamp           */
+  float filter_weight; /* Gaussian filter weight of the sample            */
+  uint32_t depth;      /* last depth reached (1-based)                    */
+  uint32_t signature;  /* hash of hit instance/primitive/lobe sequence    */
+  uint32_t events;     /* bit d: shadow ray at depth d+1 was unoccluded   */
+  uint32_t shadows;    /* bit d: a shadow ray was traced at depth d+1      */
+} asuna_path_record;
+
+/* Counters of one render call (device-side, exact). */
+typedef struct asuna_render_stats {
+  uint64_t paths;          /* camera rays = samples                         */
+  uint64_t extend_rays;    /* closest-hit rays (camera + continuation)      */
+  uint64_t shadow_rays;    /* occlusion rays                                */
+  uint64_t nodes_visited;  /* only when traversal counters are enabled      */
+  uint64_t tris_tested;    /* only when traversal counters are enabled      */
+  double ms_total;         /* device time of the call (CUDA events)         */
+  double ms_extend;        /* device time of closest-hit traversal kernels  */
+  double ms_connect;       /* device time of occlusion traversal kernels    */
+  double ms_shade;         /* device time of shading kernels                */
+  uint64_t extend_launches;
+  uint64_t connect_launches;
+} asuna_render_stats;
+
+typedef struct asuna_scene_stats {
+  uint64_t triangles;
+  uint64_t instances;
+  uint64_t blas_nodes;
+  uint64_t tlas_nodes;
+  uint64_t device_bytes;
+  double build_ms;
+} asuna_scene_stats;
+
+typedef struct asuna_ctx asuna_ctx;
+typedef struct asuna_scene asuna_scene;
+typedef struct asuna_film asuna_film;
+typedef struct asuna_json_scene asuna_json_scene;
+
+/* ---- library ------------------------------------------------------------- */
+int asuna_abi_version(void);
+const char* asuna_last_error(void);
+
+/* ---- context: one CUDA device + one stream ------------------------------- */
+/* Replaces ContextAware::init (src/context/context.cpp:8-27); the context is
+ * bound to one CUDA stream; calls on one context are serialised on it. */
+int asuna_ctx_create(int device_ordinal, asuna_ctx** out);
+int asuna_ctx_destroy(asuna_ctx* ctx);
+int asuna_ctx_sync(asuna_ctx* ctx);
+/* The cudaStream_t the context launches on (for interop), as void*. */
+void* asuna_ctx_stream(asuna_ctx* ctx);
+/* Traversal counters (nodes/triangles) for the next renders: 0 off, 1 on.
+ * Counting adds global atomics; keep it off when timing. */
+int asuna_ctx_set_counters(asuna_ctx* ctx, int enable);
+/* Device memory budget for wavefront path state, in bytes (0 = default). */
+int asuna_ctx_set_path_budget(asuna_ctx* ctx, uint64_t bytes);
+
+/* ---- scene: upload + acceleration-structure build ------------------------ */
+/* Replaces Scene::submit + BLAS/TLAS build.  Host arrays are deep-copied; the
+ * scene is immutable afterwards and may be shared by renders on any context
+ * of the same device. */
+int asuna_scene_create(asuna_ctx* ctx, const asuna_scene_desc* desc, asuna_scene** out);
+int asuna_scene_destroy(asuna_scene* scene);
+int asuna_scene_get_stats(const asuna_scene* scene, asuna_scene_stats* out);
+
+/* ---- film: the 9 RGBA32F output images ---------------------------------- */
+int asuna_film_create(asuna_ctx* ctx, uint32_t width, uint32_t height, asuna_film** out);
+int asuna_film_destroy(asuna_film* film);
+/* image: 0 radiance, 1..7 AOV channels, 8 filter-weight sum.  Copies
+ * width*height*4 floats into host memory (pinned or pageable). */
+int asuna_film_read(asuna_ctx* ctx, asuna_film* film, int image, float* host_rgba);
+int asuna_film_clear(asuna_ctx* ctx, asuna_film* film);
+
+/* ---- render --------------------------------------------------------------- */
+/* Renders shot->frames frames into film (asynchronous on the context's
+ * stream; stats, if non-NULL, forces a synchronisation and is filled). */
+int asuna_render(asuna_ctx* ctx, const asuna_scene* scene, const asuna_shot* shot,
+                 asuna_film* film, asuna_render_stats* stats);
+/* Renders n shots (any resolutions / frame counts) in one wavefront. */
+int asuna_render_batch(asuna_ctx* ctx, const asuna_scene* scene, const asuna_shot* shots,
+                       asuna_film* const* films, uint32_t n, asuna_render_stats* stats);
+/* Parity mode: renders one shot and writes one asuna_path_record per
+ * (frame, pixel) into host memory, ordered [frame][y][x]. */
+int asuna_render_paths(asuna_ctx* ctx, const asuna_scene* scene, const asuna_shot* shot,
+                       asuna_film* film, asuna_path_record* host_records);
+
+/* Traversal query (tests, tools): n rays of 8 floats (o.xyz, tmin, d.xyz,
+ * tmax); hits receive (t, u, v, primitive bits) or t = -1 on a miss, inst the
+ * instance index or 0xffffffff.  any_hit = 1 gives occlusion only. */
+int asuna_scene_trace(asuna_ctx* ctx, const asuna_scene* scene, const float* rays, uint32_t n, int any_hit,
+                      float* hits, uint32_t* inst);
+
+/* ---- host side: JSON scene description ---------------------------------- */
+/* Parses an Asuna scene JSON file (Loader::parse, src/loader/loader.cpp:91-144)
+ * and assembles the device-ABI arrays the way Scene does (dummy light 0,
+ * dummy material 0, rect lights as two-triangle emitter instances, mesh
+ * lights as one triangle light per facet). */
+int asuna_json_load(const char* path, asuna_json_scene** out);
+int asuna_json_load_string(const char* text, const char* base_dir, asuna_json_scene** out);
+int asuna_json_free(asuna_json_scene* js);
+/* View of the assembled arrays; valid until asuna_json_free. */
+int asuna_json_scene_desc(const asuna_json_scene* js, asuna_scene_desc* out);
+/* Number of shots (autofit adds one when the file has none). */
+int asuna_json_num_shots(const asuna_json_scene* js, uint32_t* out);
+int asuna_json_get_shot(const asuna_json_scene* js, uint32_t index, asuna_shot* out);
+/* Channel kinds of the scene's multi_channel list (ASUNA_CH_*), count in *n. */
+int asuna_json_channels(const asuna_json_scene* js, uint32_t* n, int32_t* kinds);
+
+/* ---- host side: camera helpers (src/core/camera.cpp:28-99) ---------------- */
+/* Fills a perspective GpuCamera from look-at parameters; fov in degrees is
+ * the horizontal field of view of the reference. */
+int asuna_camera_perspective(const float eye[3], const float lookat[3], const float up[3],
+                             float fov_deg, float aperture, float focal_distance,
+                             uint32_t width, uint32_t height, asuna_camera* out);
+int asuna_camera_opencv(const float eye[3], const float lookat[3], const float up[3],
+                        const float fxfycxcy[4], asuna_camera* out);
+/* Builds the env-map importance tables exactly as EnvMap::EnvMap
+ * (src/core/texture.cpp:144-226): marginal/conditional are width*height*2
+ * floats (.x = inverse CDF, .y = pdf). */
+int asuna_envmap_tables(uint32_t width, uint32_t height, const float* rgba, float* marginal_xy,
+                        float* conditional_xy);
+/* Diffuse Fresnel reflectance fdrInt (src/loader/material.cpp:25-37). */
+float asuna_diffuse_fresnel(float ior, int sample_count);
+
+/* ---- offline tracer ------------------------------------------------------- */
+/* Renders every shot of a scene file and writes <out_prefix>_shot_%04d.pfm
+ * (+ _channel_%04d.pfm per AOV), the offline mode of Tracer::runOffline. */
+int asuna_tracer_run_offline(asuna_ctx* ctx, const char* scene_json, const char* out_prefix);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* ASUNA_RT_H */

@@ -1,0 +1,1509 @@
+// asuna_oracle.cpp — CPU oracle of the path-tracer hot path.
+//
+// TEST INFRASTRUCTURE ONLY (the checker of the CUDA path; never linked into
+// the library).  A scalar restatement of the reference's GLSL ray-tracing
+// path, templated on the arithmetic type: float reproduces the reference's
+// FP32 streams for per-path parity, double gives the quality reference.
+// Each function names the reference lines it follows.  Compile with
+// -ffp-contract=off so the float instantiation rounds every operation the way
+// the GLSL source spells it.
+#include "asuna_oracle.h"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <thread>
+#include <vector>
+
+namespace ora {
+
+// ----------------------------------------------------------------------------
+// Scalar/vector helpers with GLSL semantics (GLSL 4.60 §8).
+template <class R>
+struct V2 {
+  R x, y;
+};
+template <class R>
+struct V3 {
+  R x, y, z;
+};
+
+template <class R> inline V3<R> mk(R a, R b, R c) { return V3<R>{a, b, c}; }
+template <class R> inline V3<R> splat(R a) { return V3<R>{a, a, a}; }
+template <class R> inline V3<R> operator+(V3<R> a, V3<R> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class R> inline V3<R> operator-(V3<R> a, V3<R> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class R> inline V3<R> operator*(V3<R> a, V3<R> b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+template <class R> inline V3<R> operator/(V3<R> a, V3<R> b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
+template <class R> inline V3<R> operator*(V3<R> a, R s) { return {a.x * s, a.y * s, a.z * s}; }
+template <class R> inline V3<R> operator*(R s, V3<R> a) { return {s * a.x, s * a.y, s * a.z}; }
+template <class R> inline V3<R> operator/(V3<R> a, R s) { return {a.x / s, a.y / s, a.z / s}; }
+template <class R> inline V3<R> operator-(V3<R> a) { return {-a.x, -a.y, -a.z}; }
+template <class R> inline R dot(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class R> inline V3<R> cross(V3<R> a, V3<R> b) {
+  return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y};
+}
+template <class R> inline R length(V3<R> a) { return std::sqrt(dot(a, a)); }
+template <class R> inline V3<R> normalize(V3<R> a) {
+  R l = length(a);
+  return {a.x / l, a.y / l, a.z / l};
+}
+template <class R> inline R gmin(R a, R b) { return b < a ? b : a; }  // GLSL min
+template <class R> inline R gmax(R a, R b) { return a < b ? b : a; }  // GLSL max
+template <class R> inline R gclamp(R x, R lo, R hi) { return gmin(gmax(x, lo), hi); }
+template <class R> inline R gsign(R x) { return x > R(0) ? R(1) : (x < R(0) ? R(-1) : R(0)); }
+// reflect/refract, GLSL 4.60 §8.5
+template <class R> inline V3<R> reflect(V3<R> I, V3<R> N) { return I - R(2) * dot(N, I) * N; }
+template <class R> inline V3<R> refract(V3<R> I, V3<R> N, R eta) {
+  R d = dot(N, I);
+  R k = R(1) - eta * eta * (R(1) - d * d);
+  if (k < R(0)) return splat(R(0));
+  return eta * I - (eta * d + std::sqrt(k)) * N;
+}
+
+template <class R>
+struct K {
+  static constexpr R PI = R(3.14159265358979323846);
+  static constexpr R TWO_PI = R(6.28318530717958647692);
+  static constexpr R INV_PI = R(0.31830988618379067154);
+  static constexpr R INV_2PI = R(0.15915494309189533577);
+  static constexpr R INV_4PI = R(0.07957747154594766788);
+  static constexpr R PI_OVER_2 = R(1.57079632679489661923);
+  static constexpr R PI_OVER_4 = R(0.78539816339744830961);
+  static constexpr R EPS = R(0.001);
+  static constexpr R INF = R(10000000000.0);
+  static constexpr R MINIMUM = R(0.00001);
+};
+
+// math.glsl:20-30
+inline uint32_t xxhash32(uint32_t x, uint32_t y, uint32_t z) {
+  const uint32_t p0 = 2246822519u, p1 = 3266489917u, p2 = 668265263u, p3 = 374761393u;
+  uint32_t h = z + p3 + x * p1;
+  h = p2 * ((h << 17) | (h >> 15));
+  h += y * p1;
+  h = p2 * ((h << 17) | (h >> 15));
+  h = p0 * (h ^ (h >> 15));
+  h = p1 * (h ^ (h >> 13));
+  return h ^ (h >> 16);
+}
+// math.glsl:34-39
+inline uint32_t pcg(uint32_t& state) {
+  uint32_t prev = state * 747796405u + 2891336453u;
+  uint32_t word = ((prev >> ((prev >> 28u) + 4u)) ^ prev) * 277803737u;
+  state = prev;
+  return (word >> 22u) ^ word;
+}
+// math.glsl:42 — uint -> float rounds to nearest, times 2^-32 (exact).
+template <class R> inline R rnd(uint32_t& s) { return R(float(pcg(s))) * R(2.3283064365386963e-10); }
+template <> inline double rnd<double>(uint32_t& s) { return double(pcg(s)) * 2.3283064365386963e-10; }
+template <class R> inline V2<R> rnd2(uint32_t& s) {
+  R a = rnd<R>(s);
+  R b = rnd<R>(s);
+  return V2<R>{a, b};
+}
+
+// math.glsl:58-61
+template <class R> inline V3<R> makeNormal(V3<R> n) {
+  if (length(n) == R(0)) return n;
+  return normalize(n);
+}
+// column-major mat4 * vec4 (m[c*4+r])
+template <class R> inline void mat4mul(const float* m, R x, R y, R z, R w, R out[4]) {
+  for (int r = 0; r < 4; ++r)
+    out[r] = R(m[0 * 4 + r]) * x + R(m[1 * 4 + r]) * y + R(m[2 * 4 + r]) * z + R(m[3 * 4 + r]) * w;
+}
+template <class R> inline void mat4Tmul(const float* m, R x, R y, R z, R w, R out[4]) {
+  // transpose(m) * v
+  for (int r = 0; r < 4; ++r)
+    out[r] = R(m[r * 4 + 0]) * x + R(m[r * 4 + 1]) * y + R(m[r * 4 + 2]) * z + R(m[r * 4 + 3]) * w;
+}
+// math.glsl:46-50
+template <class R> inline V3<R> transformPoint(const float* m, V3<R> p) {
+  R o[4];
+  mat4mul<R>(m, p.x, p.y, p.z, R(1), o);
+  return {o[0] / o[3], o[1] / o[3], o[2] / o[3]};
+}
+// math.glsl:52-66
+template <class R> inline V3<R> transformDirection(const float* m, V3<R> d) {
+  R o[4];
+  mat4mul<R>(m, d.x, d.y, d.z, R(0), o);
+  return makeNormal(V3<R>{o[0], o[1], o[2]});
+}
+template <class R> inline V3<R> transformDirectionT(const float* m, V3<R> d) {
+  R o[4];
+  mat4Tmul<R>(m, d.x, d.y, d.z, R(0), o);
+  return makeNormal(V3<R>{o[0], o[1], o[2]});
+}
+// math.glsl:133-138
+template <class R> inline V3<R> uniformSampleSphere(V2<R> u) {
+  R z = R(1) - R(2) * u.x;
+  R r = std::sqrt(gmax(R(0), R(1) - z * z));
+  R phi = K<R>::TWO_PI * u.y;
+  return {r * std::cos(phi), r * std::sin(phi), z};
+}
+// math.glsl:148-163
+template <class R> inline V2<R> concentricSampleDisk(V2<R> u) {
+  R ox = R(2) * u.x - R(1), oy = R(2) * u.y - R(1);
+  if (ox == R(0) && oy == R(0)) return V2<R>{R(0), R(0)};
+  R theta, r;
+  if (std::fabs(ox) > std::fabs(oy)) {
+    r = ox;
+    theta = K<R>::PI_OVER_4 * (oy / ox);
+  } else {
+    r = oy;
+    theta = K<R>::PI_OVER_2 - K<R>::PI_OVER_4 * (ox / oy);
+  }
+  return V2<R>{r * std::cos(theta), r * std::sin(theta)};
+}
+// math.glsl:165-174
+template <class R> inline V3<R> cosineSampleHemisphere(V2<R> u) {
+  V2<R> d = concentricSampleDisk(u);
+  R z = std::sqrt(gmax(R(0), R(1) - d.x * d.x - d.y * d.y));
+  return {d.x, d.y, z};
+}
+template <class R> inline R cosineHemispherePdf(R c) { return c <= R(0) ? R(0) : c * K<R>::INV_PI; }
+// math.glsl:184-189
+template <class R> inline R powerHeuristic(R a, R b) {
+  a = a * a;
+  b = b * b + a;
+  if (b == R(0)) return R(0);
+  return a / b;
+}
+// math.glsl:199-216
+template <class R> inline void basis(V3<R> n, V3<R>& f, V3<R>& r) {
+  if (n.z < R(-0.999999)) {
+    f = {R(0), R(-1), R(0)};
+    r = {R(-1), R(0), R(0)};
+  } else {
+    R a = R(1) / (R(1) + n.z);
+    R b = -n.x * n.y * a;
+    f = {R(1) - n.x * n.x * a, b, -n.x};
+    r = {b, R(1) - n.y * n.y * a, -n.y};
+  }
+}
+template <class R> inline V3<R> toWorld(V3<R> X, V3<R> Y, V3<R> Z, V3<R> v) { return v.x * X + v.y * Y + v.z * Z; }
+template <class R> inline V3<R> toLocal(V3<R> X, V3<R> Y, V3<R> Z, V3<R> v) {
+  return {dot(v, X), dot(v, Y), dot(v, Z)};
+}
+// math.glsl:241-266 — integer ulp offset on the float bits.
+inline float offsetComp(float p, float n) {
+  int32_t ofi = int32_t(256.0f * n);
+  int32_t bits;
+  std::memcpy(&bits, &p, 4);
+  bits += (p < 0.0f) ? -ofi : ofi;
+  float pi;
+  std::memcpy(&pi, &bits, 4);
+  return std::fabs(p) < (1.0f / 32.0f) ? p + (1.0f / 65536.0f) * n : pi;
+}
+inline double offsetComp(double p, double n) {
+  // FP64 instantiation: same rule on the float image of the point.
+  return double(offsetComp(float(p), float(n))) + (p - double(float(p)));
+}
+template <class R> inline V3<R> offsetPositionAlongNormal(V3<R> p, V3<R> n) {
+  return {offsetComp(p.x, n.x), offsetComp(p.y, n.y), offsetComp(p.z, n.z)};
+}
+// sun_and_sky.glsl:29-31
+template <class R> inline R luminance(V3<R> c) {
+  return R(0.2126f) * c.x + R(0.7152f) * c.y + R(0.0722f) * c.z;
+}
+
+// structs.glsl:7-20
+enum : uint32_t {
+  EBsdfNull = 0,
+  EDiffuseReflection = 1,
+  EDiffuseTransmission = 2,
+  EGlossyReflection = 4,
+  EGlossyTransmission = 8,
+  ESpecularReflection = 16,
+  ESpecularTransmission = 32,
+  ESmooth = 1 | 2 | 4 | 8,
+  EDelta = 1,
+  EArea = 2
+};
+inline bool isNonSpecular(uint32_t f) { return (f & ESmooth) != 0; }
+
+// ----------------------------------------------------------------------------
+// Bilinear, REPEAT-wrapped fetch at the base level: what texture() returns in
+// a ray-tracing stage for the reference's samplers (linear filter, default
+// address mode 0 = REPEAT; src/core/texture.cpp:244-248).
+struct Tex {
+  int w = 0, h = 0, c = 0;
+  std::vector<float> d;
+};
+template <class R> inline void texFetch(const Tex& t, R u, R v, R out[4]) {
+  R x = u * R(t.w) - R(0.5), y = v * R(t.h) - R(0.5);
+  R fx0 = std::floor(x), fy0 = std::floor(y);
+  R a = x - fx0, b = y - fy0;
+  long i0 = long(fx0), j0 = long(fy0);
+  auto wrap = [](long i, int n) { long m = i % n; return int(m < 0 ? m + n : m); };
+  int i0w = wrap(i0, t.w), i1w = wrap(i0 + 1, t.w), j0w = wrap(j0, t.h), j1w = wrap(j0 + 1, t.h);
+  for (int k = 0; k < t.c; ++k) {
+    R t00 = t.d[(size_t(j0w) * t.w + i0w) * t.c + k], t10 = t.d[(size_t(j0w) * t.w + i1w) * t.c + k];
+    R t01 = t.d[(size_t(j1w) * t.w + i0w) * t.c + k], t11 = t.d[(size_t(j1w) * t.w + i1w) * t.c + k];
+    out[k] = (R(1) - a) * (R(1) - b) * t00 + a * (R(1) - b) * t10 + (R(1) - a) * b * t01 + a * b * t11;
+  }
+}
+
+// ----------------------------------------------------------------------------
+// Watertight ray/triangle test (Woop, Benthin, Wald, JCGT 2013), float.
+struct RayPre {
+  int kx, ky, kz;
+  float Sx, Sy, Sz;
+  float o[3], d[3];
+};
+inline RayPre precompute(const float o[3], const float d[3]) {
+  RayPre r;
+  float ax = std::fabs(d[0]), ay = std::fabs(d[1]), az = std::fabs(d[2]);
+  int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+  int kx = kz + 1 == 3 ? 0 : kz + 1;
+  int ky = kx + 1 == 3 ? 0 : kx + 1;
+  if (d[kz] < 0.0f) std::swap(kx, ky);
+  r.kx = kx;
+  r.ky = ky;
+  r.kz = kz;
+  r.Sx = d[kx] / d[kz];
+  r.Sy = d[ky] / d[kz];
+  r.Sz = 1.0f / d[kz];
+  for (int i = 0; i < 3; ++i) {
+    r.o[i] = o[i];
+    r.d[i] = d[i];
+  }
+  return r;
+}
+// Returns true and (t, b1, b2) for a hit with tmin <= t <= tmax.
+inline bool intersectTri(const RayPre& r, const float* p0, const float* p1, const float* p2, float tmin,
+                         float tmax, float& t, float& b1, float& b2) {
+  float A[3], B[3], C[3];
+  for (int i = 0; i < 3; ++i) {
+    A[i] = p0[i] - r.o[i];
+    B[i] = p1[i] - r.o[i];
+    C[i] = p2[i] - r.o[i];
+  }
+  float Ax = A[r.kx] - r.Sx * A[r.kz], Ay = A[r.ky] - r.Sy * A[r.kz];
+  float Bx = B[r.kx] - r.Sx * B[r.kz], By = B[r.ky] - r.Sy * B[r.kz];
+  float Cx = C[r.kx] - r.Sx * C[r.kz], Cy = C[r.ky] - r.Sy * C[r.kz];
+  float U = Cx * By - Cy * Bx;
+  float V = Ax * Cy - Ay * Cx;
+  float W = Bx * Ay - By * Ax;
+  if (U == 0.0f || V == 0.0f || W == 0.0f) {
+    U = float(double(Cx) * double(By) - double(Cy) * double(Bx));
+    V = float(double(Ax) * double(Cy) - double(Ay) * double(Cx));
+    W = float(double(Bx) * double(Ay) - double(By) * double(Ax));
+  }
+  if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+  float det = U + V + W;
+  if (det == 0.0f) return false;
+  float Az = r.Sz * A[r.kz], Bz = r.Sz * B[r.kz], Cz = r.Sz * C[r.kz];
+  float T = U * Az + V * Bz + W * Cz;
+  float rcp = 1.0f / det;
+  float tt = T * rcp;
+  if (!(tt >= tmin && tt <= tmax)) return false;
+  t = tt;
+  b1 = V * rcp;
+  b2 = W * rcp;
+  return true;
+}
+
+// ----------------------------------------------------------------------------
+// Scene: per-mesh BVH (object-median split, <= 4 triangles per leaf) and a
+// flat list of instances.  Independent of the library's builder.
+struct BNode {
+  float lo[3], hi[3];
+  uint32_t left;   // inner: index of left child (right = left + 1)
+  uint32_t start;  // leaf: first triangle in `order`
+  uint32_t count;  // 0 = inner
+};
+struct Mesh {
+  std::vector<asuna_vertex> v;
+  std::vector<uint32_t> idx;
+  uint32_t ntri = 0;
+  std::vector<BNode> nodes;
+  std::vector<uint32_t> order;
+  std::vector<float> tri;  // 9 floats per triangle in `order`
+  float lo[3], hi[3];
+};
+struct Inst {
+  asuna_instance_desc d;
+  float w2o[12];
+  float lo[3], hi[3];
+};
+
+struct Scene {
+  std::vector<Mesh> meshes;
+  std::vector<Inst> insts;
+  std::vector<asuna_material> mats;
+  std::vector<asuna_light> lights;
+  bool hasEnv = false;
+  Tex env, marg, cond;
+};
+
+static void buildBvh(Mesh& m) {
+  const uint32_t n = m.ntri;
+  std::vector<float> cen(size_t(n) * 3), blo(size_t(n) * 3), bhi(size_t(n) * 3);
+  for (uint32_t i = 0; i < n; ++i) {
+    for (int k = 0; k < 3; ++k) {
+      float a = m.v[m.idx[3 * i]].pos[k], b = m.v[m.idx[3 * i + 1]].pos[k], c = m.v[m.idx[3 * i + 2]].pos[k];
+      blo[3 * i + k] = std::min(a, std::min(b, c));
+      bhi[3 * i + k] = std::max(a, std::max(b, c));
+      cen[3 * i + k] = 0.5f * (blo[3 * i + k] + bhi[3 * i + k]);
+    }
+  }
+  m.order.resize(n);
+  for (uint32_t i = 0; i < n; ++i) m.order[i] = i;
+  m.nodes.clear();
+  m.nodes.reserve(2 * size_t(n) + 1);
+  struct Item {
+    uint32_t node, start, count;
+  };
+  std::vector<Item> stack;
+  m.nodes.push_back(BNode{});
+  if (n) stack.push_back({0, 0, n});
+  while (!stack.empty()) {
+    Item it = stack.back();
+    stack.pop_back();
+    BNode nd;
+    float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int k = 0; k < 3; ++k) {
+      nd.lo[k] = INFINITY;
+      nd.hi[k] = -INFINITY;
+    }
+    for (uint32_t i = it.start; i < it.start + it.count; ++i) {
+      uint32_t t = m.order[i];
+      for (int k = 0; k < 3; ++k) {
+        nd.lo[k] = std::min(nd.lo[k], blo[3 * t + k]);
+        nd.hi[k] = std::max(nd.hi[k], bhi[3 * t + k]);
+        clo[k] = std::min(clo[k], cen[3 * t + k]);
+        chi[k] = std::max(chi[k], cen[3 * t + k]);
+      }
+    }
+    // Conservative expansion so the slab test never rejects a triangle the
+    // watertight test would accept.
+    for (int k = 0; k < 3; ++k) {
+      float e = 1e-6f * std::max(std::fabs(nd.lo[k]), std::fabs(nd.hi[k])) + 1e-30f;
+      nd.lo[k] -= e;
+      nd.hi[k] += e;
+    }
+    if (it.count <= 4) {
+      nd.left = 0;
+      nd.start = it.start;
+      nd.count = it.count;
+      m.nodes[it.node] = nd;
+      continue;
+    }
+    int axis = 0;
+    float ext = chi[0] - clo[0];
+    for (int k = 1; k < 3; ++k)
+      if (chi[k] - clo[k] > ext) {
+        ext = chi[k] - clo[k];
+        axis = k;
+      }
+    uint32_t mid = it.start + it.count / 2;
+    std::nth_element(m.order.begin() + it.start, m.order.begin() + mid, m.order.begin() + it.start + it.count,
+                     [&](uint32_t a, uint32_t b) {
+                       float ca = cen[3 * a + axis], cb = cen[3 * b + axis];
+                       return ca < cb || (ca == cb && a < b);
+                     });
+    uint32_t l = uint32_t(m.nodes.size());
+    m.nodes.push_back(BNode{});
+    m.nodes.push_back(BNode{});
+    nd.left = l;
+    nd.start = 0;
+    nd.count = 0;
+    m.nodes[it.node] = nd;
+    stack.push_back({l, it.start, mid - it.start});
+    stack.push_back({l + 1, mid, it.start + it.count - mid});
+  }
+  m.tri.resize(size_t(n) * 9);
+  for (uint32_t i = 0; i < n; ++i) {
+    uint32_t t = m.order[i];
+    for (int c = 0; c < 3; ++c)
+      for (int k = 0; k < 3; ++k) m.tri[size_t(i) * 9 + c * 3 + k] = m.v[m.idx[3 * t + c]].pos[k];
+  }
+  if (n) {
+    for (int k = 0; k < 3; ++k) {
+      m.lo[k] = m.nodes[0].lo[k];
+      m.hi[k] = m.nodes[0].hi[k];
+    }
+  } else {
+    for (int k = 0; k < 3; ++k) {
+      m.lo[k] = INFINITY;
+      m.hi[k] = -INFINITY;
+    }
+  }
+}
+
+// 3x4 row-major inverse, computed in double and rounded once to float.  The
+// library computes gl_WorldToObjectEXT the same way so both traverse with the
+// same object-space rays.
+static void invert3x4(const float* m, float* out) {
+  double a[3][3], t[3];
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 3; ++c) a[r][c] = m[r * 4 + c];
+    t[r] = m[r * 4 + 3];
+  }
+  double det = a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) - a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
+               a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
+  double inv[3][3];
+  inv[0][0] = (a[1][1] * a[2][2] - a[1][2] * a[2][1]) / det;
+  inv[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) / det;
+  inv[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) / det;
+  inv[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) / det;
+  inv[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) / det;
+  inv[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) / det;
+  inv[2][0] = (a[1][0] * a[2][1] - a[1][1] * a[2][0]) / det;
+  inv[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) / det;
+  inv[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) / det;
+  for (int r = 0; r < 3; ++r) {
+    double tt = -(inv[r][0] * t[0] + inv[r][1] * t[1] + inv[r][2] * t[2]);
+    for (int c = 0; c < 3; ++c) out[r * 4 + c] = float(inv[r][c]);
+    out[r * 4 + 3] = float(tt);
+  }
+}
+
+// Object-space ray: o' = W2O (o,1), d' = W2O (d,0); fixed operation order
+// (the CUDA traversal uses the same order with non-contracted ops).
+inline void xformRay(const float* w, const float o[3], const float d[3], float oo[3], float dd[3]) {
+  for (int r = 0; r < 3; ++r) {
+    oo[r] = ((w[r * 4 + 0] * o[0] + w[r * 4 + 1] * o[1]) + w[r * 4 + 2] * o[2]) + w[r * 4 + 3];
+    dd[r] = (w[r * 4 + 0] * d[0] + w[r * 4 + 1] * d[1]) + w[r * 4 + 2] * d[2];
+  }
+}
+
+inline bool slab(const float lo[3], const float hi[3], const float o[3], const float inv[3], float tmin, float tmax) {
+  float t0 = tmin, t1 = tmax;
+  for (int k = 0; k < 3; ++k) {
+    float a = (lo[k] - o[k]) * inv[k], b = (hi[k] - o[k]) * inv[k];
+    if (a > b) std::swap(a, b);
+    if (std::isnan(a) || std::isnan(b)) {
+      // 0 * inf: the ray lies in the slab plane; keep it (conservative).
+      continue;
+    }
+    t0 = std::max(t0, a);
+    t1 = std::min(t1, b);
+  }
+  return t0 <= t1;
+}
+
+struct Hit {
+  float t;
+  uint32_t inst, prim;
+  float u, v;
+};
+
+struct TravStats {
+  uint64_t nodes = 0, tris = 0;
+};
+
+// Closest hit (anyHit=false) or any hit (anyHit=true) in [tmin, tmax].
+static bool traceScene(const Scene& s, const float o[3], const float d[3], float tmin, float tmax, bool anyHit,
+                       Hit& hit, TravStats* st) {
+  bool found = false;
+  float best = tmax;
+  for (uint32_t ii = 0; ii < s.insts.size(); ++ii) {
+    const Inst& in = s.insts[ii];
+    const Mesh& m = s.meshes[in.d.mesh_id];
+    if (!m.ntri) continue;
+    float oo[3], dd[3];
+    xformRay(in.w2o, o, d, oo, dd);
+    float inv[3] = {1.0f / dd[0], 1.0f / dd[1], 1.0f / dd[2]};
+    if (!slab(m.lo, m.hi, oo, inv, tmin, best)) continue;
+    RayPre rp = precompute(oo, dd);
+    uint32_t stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp) {
+      const BNode& nd = m.nodes[stack[--sp]];
+      if (st) st->nodes++;
+      if (!slab(nd.lo, nd.hi, oo, inv, tmin, best)) continue;
+      if (nd.count) {
+        for (uint32_t k = 0; k < nd.count; ++k) {
+          const float* tv = &m.tri[size_t(nd.start + k) * 9];
+          float t, b1, b2;
+          if (st) st->tris++;
+          if (intersectTri(rp, tv, tv + 3, tv + 6, tmin, best, t, b1, b2)) {
+            if (!found || t < best) {
+              found = true;
+              best = t;
+              hit = Hit{t, ii, m.order[nd.start + k], b1, b2};
+              if (anyHit) return true;
+            }
+          }
+        }
+      } else {
+        stack[sp++] = nd.left + 1;
+        stack[sp++] = nd.left;
+      }
+    }
+  }
+  return found;
+}
+
+// ----------------------------------------------------------------------------
+// Env map importance tables, restating EnvMap::EnvMap (src/core/texture.cpp:
+// 144-226) including its double-precision literals and float storage.
+static void envTables(int width, int height, const float* px, float* marg, float* cond) {
+  std::vector<float> pdf2D(size_t(width) * height), cdf2D(size_t(width) * height), pdf1D(height), cdf1D(height);
+  for (size_t i = 0; i < size_t(width) * height * 2; ++i) marg[i] = cond[i] = 0.0f;
+  float weightSum = 0.0f;
+  for (int j = 0; j < height; j++) {
+    float rowWeightSum = 0.0f;
+    for (int i = 0; i < width; i++) {
+      const float* c = &px[(size_t(j) * width + i) * 4];
+      float weight = float(0.3 * c[0] + 0.6 * c[1] + 0.1 * c[2]);
+      rowWeightSum += weight;
+      pdf2D[size_t(j) * width + i] = weight;
+      cdf2D[size_t(j) * width + i] = rowWeightSum;
+    }
+    for (int i = 0; i < width; i++) {
+      pdf2D[size_t(j) * width + i] = float(pdf2D[size_t(j) * width + i] / (rowWeightSum + 1e-7));
+      cdf2D[size_t(j) * width + i] = float(cdf2D[size_t(j) * width + i] / (rowWeightSum + 1e-7));
+    }
+    weightSum += rowWeightSum;
+    pdf1D[j] = rowWeightSum;
+    cdf1D[j] = weightSum;
+  }
+  for (int j = 0; j < height; j++) {
+    cdf1D[j] = float(cdf1D[j] / (weightSum + 1e-7));
+    pdf1D[j] = float(pdf1D[j] / (weightSum + 1e-7));
+  }
+  auto lowerBound = [](const float* a, int lo, int hi, float v) {
+    while (lo < hi) {
+      int mid = (lo + hi) / 2;
+      if (a[mid] < v)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    return lo;
+  };
+  for (int j = 0; j < height; j++) {
+    float invHeight = float(j + 1) / float(height);
+    float row = float(lowerBound(cdf1D.data(), 0, height, invHeight));
+    marg[(size_t(j) * width) * 2 + 0] = row / float(height);
+    marg[(size_t(j) * width) * 2 + 1] = pdf1D[j];
+  }
+  for (int j = 0; j < height; j++)
+    for (int i = 0; i < width; i++) {
+      float invWidth = float(i + 1) / float(width);
+      float col = float(lowerBound(cdf2D.data(), j * width, (j + 1) * width, invWidth) - j * width);
+      cond[(size_t(j) * width + i) * 2 + 0] = col / float(width);
+      cond[(size_t(j) * width + i) * 2 + 1] = pdf2D[size_t(j) * width + i];
+    }
+}
+
+// ----------------------------------------------------------------------------
+// The path (one sample of one pixel of one frame).
+template <class R>
+struct Ctx {
+  const Scene* s;
+  const asuna_shot* shot;
+  TravStats* st;
+  uint64_t* shadowRays;
+  uint64_t* extendRays;
+};
+
+template <class R> inline V3<R> L3(const float* a) { return V3<R>{R(a[0]), R(a[1]), R(a[2])}; }
+
+// sample_light.glsl:84-95
+template <class R> R pdfEnvmap(const Scene& s, const asuna_shot& sh, V3<R> L) {
+  L = transformDirectionT<R>(sh.camera.env_transform, L);
+  R theta = std::acos(gclamp(L.y, R(-1), R(1)));
+  R u = (K<R>::PI + std::atan2(L.z, L.x)) * K<R>::INV_2PI, v = theta * K<R>::INV_PI;
+  R c[4], m[4];
+  texFetch<R>(s.cond, u, v, c);
+  texFetch<R>(s.marg, R(0), v, m);
+  R pdf = c[1] * m[1];
+  R sinTheta = std::sin(theta);
+  if (sinTheta == R(0)) return R(0);
+  return (pdf * R(sh.state.env_map_resolution[0]) * R(sh.state.env_map_resolution[1])) /
+         (K<R>::TWO_PI * K<R>::PI * sinTheta);
+}
+// sample_light.glsl:97-104
+template <class R> V3<R> evalEnvmap(const Scene& s, const asuna_shot& sh, V3<R> L) {
+  L = transformDirectionT<R>(sh.camera.env_transform, L);
+  R theta = std::acos(gclamp(L.y, R(-1), R(1)));
+  R u = (K<R>::PI + std::atan2(L.z, L.x)) * K<R>::INV_2PI, v = theta * K<R>::INV_PI;
+  R e[4];
+  texFetch<R>(s.env, u, v, e);
+  R k = R(sh.state.env_map_intensity);
+  return V3<R>{k * e[0], k * e[1], k * e[2]};
+}
+// sample_light.glsl:106-129
+template <class R> V3<R> sampleEnvmap(const Scene& s, const asuna_shot& sh, V2<R> r, V3<R>& L, R& pdf) {
+  R m[4], c[4];
+  texFetch<R>(s.marg, R(0), r.x, m);
+  R uvy = m[0];
+  texFetch<R>(s.cond, r.y, uvy, c);
+  R uvx = c[0];
+  texFetch<R>(s.cond, uvx, uvy, c);
+  texFetch<R>(s.marg, R(0), uvy, m);
+  pdf = c[1] * m[1];
+  R phi = uvx * K<R>::TWO_PI;
+  R theta = uvy * K<R>::PI;
+  if (std::sin(theta) == R(0)) pdf = R(0);
+  pdf = (pdf * R(sh.state.env_map_resolution[0]) * R(sh.state.env_map_resolution[1])) /
+        (K<R>::TWO_PI * K<R>::PI * std::sin(theta));
+  L = V3<R>{-std::sin(theta) * std::cos(phi), std::cos(theta), -std::sin(theta) * std::sin(phi)};
+  L = transformDirection<R>(sh.camera.env_transform, L);
+  R e[4];
+  texFetch<R>(s.env, uvx, uvy, e);
+  R k = R(sh.state.env_map_intensity);
+  return V3<R>{k * e[0], k * e[1], k * e[2]};
+}
+
+template <class R>
+struct LRec {
+  V3<R> d{R(0), R(0), R(0)}, n{R(0), R(0), R(0)};
+  R dist = R(0), pdf = R(0);
+  uint32_t flags = 0;
+};
+
+// sample_light.glsl:10-82
+template <class R> V3<R> sampleOneLight(V2<R> r, const asuna_light& l, V3<R> P, LRec<R>& rec) {
+  if (l.type == ASUNA_LIGHT_RECT || l.type == ASUNA_LIGHT_TRIANGLE) {
+    R r1 = r.x, r2 = (l.type == ASUNA_LIGHT_TRIANGLE) ? (R(1) - r1) * r.y : r.y;
+    V3<R> pos = L3<R>(l.position) + L3<R>(l.u) * r1 + L3<R>(l.v) * r2;
+    rec.d = pos - P;
+    rec.dist = length(rec.d);
+    R distSq = rec.dist * rec.dist;
+    rec.d = rec.d / rec.dist;
+    rec.n = makeNormal(cross(L3<R>(l.u), L3<R>(l.v)));
+    rec.pdf = distSq / (R(l.area) * std::fabs(dot(rec.n, rec.d)) + K<R>::EPS);
+    rec.flags = EArea;
+    return L3<R>(l.radiance);
+  } else if (l.type == ASUNA_LIGHT_DIRECTIONAL) {
+    rec.d = makeNormal(L3<R>(l.direction));
+    rec.n = -rec.d;
+    rec.dist = K<R>::INF;
+    rec.pdf = R(1);
+    rec.flags = EDelta;
+    return L3<R>(l.radiance);
+  } else if (l.type == ASUNA_LIGHT_POINT) {
+    rec.d = L3<R>(l.position) - P;
+    rec.n = -rec.d;
+    rec.dist = length(rec.d);
+    R distSq = rec.dist * rec.dist;
+    rec.d = rec.d / (rec.dist + K<R>::EPS);
+    rec.pdf = R(1);
+    rec.flags = EDelta;
+    return L3<R>(l.radiance) / (distSq + K<R>::EPS);
+  }
+  return splat(R(0));  // undefined type: the reference returns nothing
+}
+
+template <class R>
+struct PathState {
+  V3<R> ro, rd;
+  V3<R> radiance, throughput;
+  uint32_t depth, seed;
+  bool stop;
+  uint32_t bflags;
+  R bpdf;
+  V3<R> ch[ASUNA_MAX_CHANNELS];
+  // NEE record of the current bounce
+  bool dskip;
+  V3<R> drad, dro, drd;
+  R ddist;
+  uint32_t sig;
+};
+
+inline uint32_t sigMix(uint32_t h, uint32_t v) {
+  h ^= v + 0x9e3779b9u + (h << 6) + (h >> 2);
+  return h;
+}
+
+// rchit_layouts.glsl:118-167
+template <class R>
+V3<R> sampleLights(const Scene& s, const asuna_shot& sh, PathState<R>& p, V3<R> pos, V3<R> nrm, bool& visible,
+                   LRec<R>& lRec) {
+  bool allowDoubleSide = false;
+  V3<R> radiance = splat(R(0));
+  bool hasEnv = sh.state.has_env_map == 1;
+  bool hasLight = sh.state.num_lights > 0;
+  R envSel, anaSel;
+  if (hasEnv && hasLight)
+    envSel = anaSel = R(0.5);
+  else if (hasEnv)
+    envSel = R(1), anaSel = R(0);
+  else if (hasLight)
+    envSel = R(0), anaSel = R(1);
+  else
+    envSel = anaSel = R(0);
+  R sel = rnd<R>(p.seed);
+  if (sel < envSel) {
+    // rchit_layouts.glsl:98-116 (sun-sky branch not implemented: in_use = 0)
+    lRec.flags = EArea;
+    lRec.dist = K<R>::INF;
+    lRec.n = -makeNormal(p.rd);
+    V2<R> u = rnd2<R>(p.seed);
+    radiance = sampleEnvmap<R>(s, sh, u, lRec.d, lRec.pdf) / envSel;
+    allowDoubleSide = true;
+  } else if (sel < envSel + anaSel) {
+    int n = sh.state.num_lights;
+    int idx = std::min(1 + int(rnd<R>(p.seed) * R(n)), n);
+    const asuna_light& l = s.lights[idx];
+    V2<R> u = rnd2<R>(p.seed);
+    radiance = sampleOneLight<R>(u, l, pos, lRec) * R(n) / anaSel;
+    allowDoubleSide = (l.double_side == 1);
+  }
+  p.dro = offsetPositionAlongNormal(pos, nrm);
+  p.drd = lRec.d;
+  p.ddist = lRec.dist;
+  visible = (dot(lRec.d, nrm) > R(0) && lRec.pdf > R(0));
+  visible = visible && (dot(lRec.n, lRec.d) < R(0) || allowDoubleSide);
+  return radiance;
+}
+
+template <class R>
+struct HitState {
+  int lightId;
+  V2<R> uv;
+  V3<R> pos, V, N, geoN, ffN, X, Y;
+  asuna_material mat;
+};
+
+// rchit_layouts.glsl:61-95
+template <class R> HitState<R> getHitState(const Scene& s, const asuna_shot& sh, const PathState<R>& p, const Hit& h) {
+  HitState<R> st;
+  const Inst& in = s.insts[h.inst];
+  const Mesh& m = s.meshes[in.d.mesh_id];
+  const asuna_vertex& v0 = m.v[m.idx[3 * h.prim]];
+  const asuna_vertex& v1 = m.v[m.idx[3 * h.prim + 1]];
+  const asuna_vertex& v2 = m.v[m.idx[3 * h.prim + 2]];
+  R bx = R(1) - R(h.u) - R(h.v), by = R(h.u), bz = R(h.v);
+  st.lightId = in.d.light_id;
+  st.uv = V2<R>{R(v0.uv[0]) * bx + R(v1.uv[0]) * by + R(v2.uv[0]) * bz,
+                R(v0.uv[1]) * bx + R(v1.uv[1]) * by + R(v2.uv[1]) * bz};
+  V3<R> po = L3<R>(v0.pos) * bx + L3<R>(v1.pos) * by + L3<R>(v2.pos) * bz;
+  const float* o = in.d.transform;
+  st.pos = V3<R>{R(o[0]) * po.x + R(o[1]) * po.y + R(o[2]) * po.z + R(o[3]),
+                 R(o[4]) * po.x + R(o[5]) * po.y + R(o[6]) * po.z + R(o[7]),
+                 R(o[8]) * po.x + R(o[9]) * po.y + R(o[10]) * po.z + R(o[11])};
+  const float* w = in.w2o;
+  auto nxf = [&](V3<R> n) {
+    return makeNormal(V3<R>{n.x * R(w[0]) + n.y * R(w[4]) + n.z * R(w[8]),
+                            n.x * R(w[1]) + n.y * R(w[5]) + n.z * R(w[9]),
+                            n.x * R(w[2]) + n.y * R(w[6]) + n.z * R(w[10])});
+  };
+  V3<R> n = L3<R>(v0.normal) * bx + L3<R>(v1.normal) * by + L3<R>(v2.normal) * bz;
+  st.N = nxf(n);
+  // The reference stores this in ffN and never sets geoN; the geometric
+  // normal is kept here for use_face_normal (reference reads geoN unset).
+  st.geoN = nxf(cross(L3<R>(v1.pos) - L3<R>(v0.pos), L3<R>(v2.pos) - L3<R>(v0.pos)));
+  st.V = makeNormal(-p.rd);
+  if (st.lightId < 0) st.mat = s.mats[in.d.material_id];
+  // configureShadingFrame, rchit_layouts.glsl:61-65
+  if (sh.state.use_face_normal == 1) st.N = st.geoN;
+  basis(st.N, st.X, st.Y);
+  st.ffN = dot(st.N, st.V) > R(0) ? st.N : -st.N;
+  return st;
+}
+
+// brdf_lambertian.rchit:44-68
+template <class R> void hitLight(const Scene& s, PathState<R>& p, int lightId, V3<R> hitPos) {
+  const asuna_light& l = s.lights[lightId];
+  V3<R> ldir = makeNormal(p.rd);
+  V3<R> lnrm = makeNormal(cross(L3<R>(l.u), L3<R>(l.v)));
+  R proj = dot(lnrm, ldir);
+  p.stop = true;
+  if (proj > R(0) && l.double_side == 0) return;
+  R mis = R(1);
+  if (isNonSpecular(p.bflags) && p.depth != 1) {
+    R dist = length(hitPos - p.ro);
+    R d2 = dist * dist;
+    R lpdf = d2 / (R(l.area) * std::fabs(proj) + K<R>::EPS);
+    mis = powerHeuristic(p.bpdf, lpdf);
+  }
+  p.radiance = p.radiance + p.throughput * L3<R>(l.radiance) * mis;
+}
+
+// AOVs at depth 1 (brdf_lambertian.rchit:93-108), plus the depth channel.
+template <class R> void writeAovs(const asuna_rt_state& ps, PathState<R>& p, const HitState<R>& st) {
+  if (ps.diffuse_out_channel >= 0) p.ch[ps.diffuse_out_channel] = L3<R>(st.mat.diffuse);
+  if (ps.normal_out_channel >= 0) p.ch[ps.normal_out_channel] = st.N;
+  if (ps.specular_out_channel >= 0) p.ch[ps.specular_out_channel] = splat(R(0));
+  if (ps.tangent_out_channel >= 0) p.ch[ps.tangent_out_channel] = st.X;
+  if (ps.roughness_out_channel >= 0) p.ch[ps.roughness_out_channel] = V3<R>{R(1), R(1), R(0)};
+  if (ps.position_out_channel >= 0) p.ch[ps.position_out_channel] = st.pos;
+  if (ps.uv_out_channel >= 0) p.ch[ps.uv_out_channel] = V3<R>{st.uv.x, st.uv.y, R(1)};
+}
+
+// brdf_lambertian.rchit:70-151
+template <class R> void shadeLambertian(const Scene& s, const asuna_shot& sh, PathState<R>& p, HitState<R>& st) {
+  const asuna_rt_state& ps = sh.state;
+  V3<R> kd = L3<R>(st.mat.diffuse);
+  if (p.depth == 1) writeAovs(ps, p, st);
+  {
+    bool visible;
+    LRec<R> lRec;
+    V3<R> Ld = splat(R(0));
+    V3<R> rad = sampleLights<R>(s, sh, p, st.pos, st.ffN, visible, lRec);
+    if (visible) {
+      // eval (12-21) with flag EArea, pdf (23-29) with lRec.flags
+      V3<R> w = splat(R(0));
+      R NdotL = dot(st.ffN, lRec.d), NdotV = dot(st.ffN, st.V);
+      if (!(NdotL < R(0) || NdotV < R(0))) w = kd * K<R>::INV_PI * NdotL;
+      R bpdf = (lRec.flags & EArea) ? cosineHemispherePdf(dot(st.ffN, lRec.d)) : R(0);
+      R mis = powerHeuristic(lRec.pdf, bpdf);
+      Ld = Ld + mis * w * rad * p.throughput / (lRec.pdf + K<R>::EPS);
+    }
+    p.drad = Ld;
+    p.dskip = !visible;
+  }
+  // sampleBsdf (31-42)
+  V2<R> u = rnd2<R>(p.seed);
+  V3<R> wi = cosineSampleHemisphere(u);
+  R pdf = cosineHemispherePdf(wi.z);
+  V3<R> d = toWorld(st.X, st.Y, st.ffN, wi);
+  V3<R> w = kd * K<R>::INV_PI * std::fabs(wi.z);
+  if (pdf <= R(0) || length(w) == R(0)) {
+    p.stop = true;
+    return;
+  }
+  p.bflags = EDiffuseReflection;
+  p.bpdf = pdf;
+  p.ro = offsetPositionAlongNormal(st.pos, st.ffN);
+  p.rd = d;
+  p.throughput = p.throughput * (w / pdf);
+}
+
+// brdf_rough_plastic.rchit:12-41
+template <class R> R fresnelDielectricExt(R cosThetaI_, R& cosThetaT_, R eta) {
+  if (eta == R(1)) {
+    cosThetaT_ = -cosThetaI_;
+    return R(0);
+  }
+  R scale = (cosThetaI_ > R(0)) ? R(1) / eta : eta;
+  R cosThetaTSqr = R(1) - (R(1) - cosThetaI_ * cosThetaI_) * (scale * scale);
+  if (cosThetaTSqr <= R(0)) {
+    cosThetaT_ = R(0);
+    return R(1);
+  }
+  R cosThetaI = std::fabs(cosThetaI_);
+  R cosThetaT = std::sqrt(cosThetaTSqr);
+  R Rs = (cosThetaI - eta * cosThetaT) / (cosThetaI + eta * cosThetaT);
+  R Rp = (eta * cosThetaI - cosThetaT) / (eta * cosThetaI + cosThetaT);
+  cosThetaT_ = (cosThetaI_ > R(0)) ? -cosThetaT : cosThetaT;
+  return R(0.5) * (Rs * Rs + Rp * Rp);
+}
+template <class R> inline R sqr(R x) { return x * x; }
+// 45-50
+template <class R> R dAnisoGGX(R HdotN, R HdotX, R HdotY, R ax, R ay) {
+  return R(1) / (K<R>::PI * ax * ay * sqr(sqr(HdotX / ax) + sqr(HdotY / ay) + sqr(HdotN)) + K<R>::EPS);
+}
+// 52-65
+template <class R> V3<R> importanceSampleAnisoGGX(V2<R> u, V3<R> wo, R ax, R ay) {
+  R factor = std::sqrt(gmax(R(0), u.x / gmax(R(1) - u.x, K<R>::EPS)));
+  R phi = K<R>::TWO_PI * u.y;
+  V3<R> wh{R(0), R(0), R(1)};
+  wh.x = -ax * factor * std::cos(phi);
+  wh.y = -ay * factor * std::sin(phi);
+  wh = makeNormal(wh);
+  return reflect(-wo, wh);
+}
+// 67-73
+template <class R> R importanceAnisoGGXPdf(V3<R> wh, V3<R> wo, R ax, R ay) {
+  R pdf = R(0), HdotV = dot(wh, wo);
+  V3<R> wi = reflect(-wo, wh);
+  if (wi.z > R(0) && wo.z > R(0) && wh.z > R(0))
+    pdf = dAnisoGGX(wh.z, wh.x, wh.y, ax, ay) * std::fabs(wh.z) / (R(4) * HdotV + K<R>::EPS);
+  return pdf;
+}
+// 75-80
+template <class R> R g1SmithAnisoGGX(R NdotV, R VdotX, R VdotY, R ax, R ay) {
+  if (NdotV <= R(0)) return R(0);
+  V3<R> f{ax * VdotX, ay * VdotY, NdotV};
+  return R(1) / (NdotV + length(f));
+}
+// 82-111 (parameter order of the definition)
+template <class R>
+V3<R> rpEval(V3<R> L, V3<R> V, V3<R> N, V3<R> X, V3<R> Y, V3<R> kd, V3<R> ks, R eta, R fdrInt, R invEta2, R ax, R ay,
+             uint32_t flags) {
+  V3<R> weight = splat(R(0));
+  R NdotL = dot(L, N), NdotV = dot(V, N);
+  if (((flags & EArea) == 0) || NdotL < R(0) || NdotV < R(0)) return weight;
+  {
+    V3<R> H = makeNormal(L + V);
+    R ct;
+    R Fs = fresnelDielectricExt(dot(H, V), ct, eta);
+    R Gs = g1SmithAnisoGGX(NdotV, dot(V, X), dot(V, Y), ax, ay);
+    Gs = Gs * g1SmithAnisoGGX(NdotL, dot(L, X), dot(L, Y), ax, ay);
+    R Ds = dAnisoGGX(dot(H, N), dot(H, X), dot(H, Y), ax, ay);
+    weight = weight + ks * Fs * Gs * Ds * NdotL;
+  }
+  {
+    R c1, c2;
+    R Fo = fresnelDielectricExt(NdotV, c1, eta);
+    R Fi = fresnelDielectricExt(NdotL, c2, eta);
+    V3<R> diff = kd;
+    diff = diff / (splat(R(1)) - diff * fdrInt);
+    weight = weight + (R(1) - Fi) * (R(1) - Fo) * diff * invEta2 * K<R>::INV_PI * NdotL;
+  }
+  return weight;
+}
+// 113-136 (parameter order of the definition)
+template <class R>
+R rpPdf(V3<R> L, V3<R> V, V3<R> N, V3<R> X, V3<R> Y, R ax, R ay, R eta, R ssw, uint32_t flags) {
+  R pdf = R(0);
+  R NdotL = dot(L, N), NdotV = dot(V, N);
+  if (NdotL < R(0) || NdotV < R(0) || ((flags & EArea) == 0)) return pdf;
+  R ct;
+  R Fo = fresnelDielectricExt(NdotV, ct, eta);
+  R substrateWeight = ssw * (R(1) - Fo);
+  R specularWeight = Fo;
+  R probSpecular = specularWeight / (specularWeight + substrateWeight);
+  V3<R> wi = toLocal(X, Y, N, L), wo = toLocal(X, Y, N, V);
+  V3<R> wh = makeNormal(wi + wo);
+  R glossyPdf = importanceAnisoGGXPdf(wh, wo, ax, ay);
+  pdf = pdf + probSpecular * glossyPdf;
+  R diffusePdf = cosineHemispherePdf(wi.z);
+  pdf = pdf + (R(1) - probSpecular) * diffusePdf;
+  return pdf;
+}
+
+// brdf_rough_plastic.rchit:191-269
+template <class R> void shadeRoughPlastic(const Scene& s, const asuna_shot& sh, PathState<R>& p, HitState<R>& st) {
+  R eta = R(st.mat.ior);
+  R fdrInt = R(st.mat.radiance[0]);
+  R invEta2 = R(1) / (eta * eta);
+  R ax = gmax(K<R>::EPS, R(st.mat.aniso_alpha[0]));
+  R ay = gmax(K<R>::EPS, R(st.mat.aniso_alpha[1]));
+  V3<R> kd = L3<R>(st.mat.diffuse);
+  R ssw = luminance(kd);
+  const V3<R> ks = splat(R(1));
+  if (p.depth == 1 && sh.state.n_multi_channel > 0) {
+    // The reference writes no AOV here (219-222 are commented out).
+  }
+  {
+    bool visible;
+    LRec<R> lRec;
+    V3<R> Ld = splat(R(0));
+    V3<R> rad = sampleLights<R>(s, sh, p, st.pos, st.ffN, visible, lRec);
+    if (visible) {
+      // Reference call sites 234-240 pass (.., fdrInt, ax, ay, invEta2, ..)
+      // into (.., fdrInt, invEta2, ax, ay, ..) and (.., eta, ax, ay, ..) into
+      // (.., ax, ay, eta, ..): kept as written.
+      V3<R> w = rpEval<R>(lRec.d, st.V, st.ffN, st.X, st.Y, kd, ks, eta, fdrInt, ax, ay, invEta2, EArea);
+      R bpdf = rpPdf<R>(lRec.d, st.V, st.ffN, st.X, st.Y, eta, ax, ay, ssw, lRec.flags);
+      R mis = powerHeuristic(lRec.pdf, bpdf);
+      Ld = Ld + mis * w * rad * p.throughput / (lRec.pdf + K<R>::EPS);
+    }
+    p.drad = Ld;
+    p.dskip = !visible;
+  }
+  // sampleBsdf 138-189
+  V2<R> u = rnd2<R>(p.seed);
+  V3<R> V = st.V, N = st.ffN, X = st.X, Y = st.Y;
+  V3<R> weight = splat(R(0));
+  R bpdf = R(0);
+  uint32_t bflags = EBsdfNull;
+  V3<R> bd = splat(R(0));
+  R NdotV = dot(V, N);
+  if (NdotV > R(0)) {
+    R ct;
+    R Fo = fresnelDielectricExt(NdotV, ct, eta);
+    R substrateWeight = ssw * (R(1) - Fo);
+    R specularWeight = Fo;
+    R probSpecular = specularWeight / (specularWeight + substrateWeight);
+    if (u.x < probSpecular) {
+      u.x = u.x / probSpecular;
+      V3<R> wo = toLocal(X, Y, N, V);
+      V3<R> wi = importanceSampleAnisoGGX(u, wo, ax, ay);
+      V3<R> L = toWorld(X, Y, N, wi);
+      bd = L;
+      V3<R> H = makeNormal(V + L);
+      V3<R> wh = makeNormal(wi + wo);
+      R NdotL = dot(N, L);
+      R ct2;
+      R Fs = fresnelDielectricExt(dot(H, V), ct2, eta);
+      R Gs = g1SmithAnisoGGX(NdotV, dot(V, X), dot(V, Y), ax, ay);
+      Gs = Gs * g1SmithAnisoGGX(NdotL, dot(L, X), dot(L, Y), ax, ay);
+      R Ds = dAnisoGGX(dot(H, N), dot(H, X), dot(H, Y), ax, ay);
+      bflags = EGlossyReflection;
+      bpdf = importanceAnisoGGXPdf(wh, wo, ax, ay) * probSpecular;
+      weight = ks * Fs * Gs * Ds * NdotL;
+    } else {
+      u.x = (u.x - probSpecular) / (R(1) + K<R>::EPS - probSpecular);
+      V3<R> wi = cosineSampleHemisphere(u);
+      R ct2;
+      R Fi = fresnelDielectricExt(wi.z, ct2, eta);
+      V3<R> diff = kd;
+      diff = diff / (splat(R(1)) - diff * fdrInt);
+      bpdf = (R(1) - probSpecular) * cosineHemispherePdf(wi.z);
+      bd = toWorld(X, Y, N, wi);
+      bflags = EDiffuseReflection;
+      weight = (R(1) - Fi) * (R(1) - Fo) * invEta2 * diff * K<R>::INV_PI * std::fabs(wi.z);
+    }
+  }
+  if (bpdf <= R(0) || length(weight) == R(0)) {
+    p.stop = true;
+    return;
+  }
+  p.bflags = bflags;
+  p.bpdf = bpdf;
+  p.ro = offsetPositionAlongNormal(st.pos, st.ffN);
+  p.rd = bd;
+  p.throughput = p.throughput * (weight / (bpdf + K<R>::EPS));
+}
+
+// bsdf_dielectric.rchit:12-24
+template <class R> R dielectricFresnel(R cosThetaI, R eta) {
+  R sinThetaTSq = eta * eta * (R(1) - cosThetaI * cosThetaI);
+  if (sinThetaTSq > R(1)) return R(1);
+  R cosThetaT = std::sqrt(gmax(R(1) - sinThetaTSq, R(0)));
+  R rs = (eta * cosThetaT - cosThetaI) / (eta * cosThetaT + cosThetaI);
+  R rp = (eta * cosThetaI - cosThetaT) / (eta * cosThetaI + cosThetaT);
+  return R(0.5) * (rs * rs + rp * rp);
+}
+
+// bsdf_dielectric.rchit:74-139
+template <class R> void shadeDielectric(const Scene& s, const asuna_shot& sh, PathState<R>& p, HitState<R>& st) {
+  R eta = dot(st.V, st.N) > R(0) ? (R(1) / R(st.mat.ior)) : R(st.mat.ior);
+  {
+    bool visible;
+    LRec<R> lRec;
+    V3<R> Ld = splat(R(0));
+    V3<R> rad = sampleLights<R>(s, sh, p, st.pos, st.ffN, visible, lRec);
+    if (visible) {
+      // eval (26-38) with EArea: (EArea & EDelta) == 0 -> weight 0.
+      V3<R> w = splat(R(0));
+      // pdf (41-52)
+      R bpdf = R(0);
+      if (lRec.flags & EDelta) {
+        V3<R> L = lRec.d, V = st.V, N = st.ffN;
+        R F = dielectricFresnel(std::fabs(dot(V, N)), eta);
+        if (dot(L, N) > R(0)) {
+          if (std::fabs(dot(reflect(-V, N), L) - R(1)) < K<R>::EPS) bpdf = F;
+        } else {
+          if (std::fabs(dot(refract(-V, N, eta), L) - R(1)) < K<R>::EPS) bpdf = R(1) - F;
+        }
+      }
+      R mis = powerHeuristic(lRec.pdf, bpdf);
+      Ld = Ld + mis * w * rad * p.throughput / (lRec.pdf + K<R>::EPS);
+    }
+    p.drad = Ld;
+    p.dskip = !visible;
+  }
+  // sampleBsdf 54-72
+  R u = rnd<R>(p.seed);
+  V3<R> V = st.V, N = st.ffN;
+  R F = dielectricFresnel(std::fabs(dot(V, N)), eta);
+  V3<R> bd, weight;
+  R bpdf;
+  uint32_t bflags;
+  if (u < F) {
+    bd = makeNormal(reflect(-V, N));
+    bpdf = F;
+    bflags = ESpecularReflection;
+    weight = F * splat(R(1));
+  } else {
+    bd = makeNormal(refract(-V, N, eta));
+    bpdf = R(1) - F;
+    bflags = ESpecularTransmission;
+    weight = (R(1) - F) * splat(R(1)) * eta * eta;
+  }
+  if (bpdf <= R(0) || length(weight) == R(0)) {
+    p.stop = true;
+    return;
+  }
+  p.bflags = bflags;
+  p.bpdf = bpdf;
+  p.ro = offsetPositionAlongNormal(st.pos, gsign(dot(bd, st.N)) * st.N);
+  p.rd = bd;
+  p.throughput = p.throughput * (weight / (bpdf + K<R>::EPS));
+}
+
+struct PathOut {
+  float rad[3];
+  float fw;
+  uint32_t depth, sig, events, shadows;
+  float t1;
+  float ch[ASUNA_MAX_CHANNELS][3];
+  double radd[3];
+};
+
+inline uint32_t hashFrame(uint32_t frame, uint32_t seed) { return frame + seed * 0x9E3779B9u; }
+
+template <class R>
+void tracePath(const Scene& s, const asuna_shot& sh, uint32_t x, uint32_t y, uint32_t frame, PathOut& out,
+               TravStats* st, uint64_t& nExt, uint64_t& nShadow) {
+  const asuna_camera& cam = sh.camera;
+  const asuna_rt_state& ps = sh.state;
+  PathState<R> p;
+  // raytrace.projective.rgen:26-100
+  p.seed = xxhash32(x, y, hashFrame(frame, sh.seed));
+  V3<R> origin = transformPoint<R>(cam.camera_to_world, splat(R(0)));
+  V2<R> jitter = (frame == 0) ? V2<R>{R(0.5), R(0.5)} : rnd2<R>(p.seed);
+  V2<R> pixel{R(x) + jitter.x, R(y) + jitter.y};
+  V3<R> ro = origin, rd = splat(R(0));
+  if (cam.type == ASUNA_CAMERA_PERSPECTIVE) {
+    V3<R> pCamera = transformPoint<R>(cam.raster_to_camera, V3<R>{pixel.x, pixel.y, R(0)});
+    V3<R> r = makeNormal(pCamera);
+    if (cam.aperture > 0.0f) {
+      V2<R> uLens = rnd2<R>(p.seed);
+      V2<R> d = concentricSampleDisk(uLens);
+      V2<R> pLens{R(cam.aperture) * d.x, R(cam.aperture) * d.y};
+      R ft = R(cam.focal_distance) / r.z;
+      V3<R> pFocus = ft * r;
+      V3<R> o{pLens.x, pLens.y, R(0)};
+      ro = transformPoint<R>(cam.camera_to_world, o);
+      r = pFocus - o;
+    }
+    rd = transformDirection<R>(cam.camera_to_world, r);
+  } else if (cam.type == ASUNA_CAMERA_OPENCV) {
+    R px = (pixel.x - R(cam.fxfycxcy[2])) / R(cam.fxfycxcy[0]);
+    R py = (pixel.y - R(cam.fxfycxcy[3])) / R(cam.fxfycxcy[1]);
+    rd = transformDirection<R>(cam.camera_to_world, V3<R>{px, py, R(1)});
+  }
+  p.ro = ro;
+  p.rd = rd;
+  p.stop = false;
+  p.radiance = splat(R(0));
+  p.throughput = splat(R(1));
+  p.bflags = EBsdfNull;
+  p.bpdf = R(0);
+  for (int i = 0; i < ASUNA_MAX_CHANNELS; ++i) p.ch[i] = splat(R(0));
+  p.sig = 0;
+  uint32_t events = 0, shadows = 0;
+  R t1 = R(0);  // primary-hit distance (depth channel, an extension)
+  const bool rr = (sh.flags & ASUNA_SHOT_RR) != 0;
+  // rgen:102-132
+  for (p.depth = 1; p.depth <= uint32_t(ps.max_path_depth);) {
+    p.dskip = true;
+    p.drad = splat(R(0));
+    float of[3] = {float(p.ro.x), float(p.ro.y), float(p.ro.z)}, df[3] = {float(p.rd.x), float(p.rd.y), float(p.rd.z)};
+    Hit h;
+    nExt++;
+    bool hit = traceScene(s, of, df, float(K<float>::MINIMUM), float(K<float>::INF), false, h, st);
+    if (!hit) {
+      // raytrace.default.rmiss:24-56
+      p.stop = true;
+      V3<R> env;
+      if (ps.has_env_map == 1)
+        env = evalEnvmap<R>(s, sh, p.rd);
+      else
+        env = L3<R>(ps.bg_color);
+      R mis = R(1);
+      if (p.depth != 1 && isNonSpecular(p.bflags)) {
+        R envPdf = (ps.has_env_map == 1) ? pdfEnvmap<R>(s, sh, p.rd) : K<R>::INV_4PI;
+        mis = powerHeuristic(p.bpdf, envPdf);
+      }
+      p.radiance = p.radiance + p.throughput * env * mis;
+      p.sig = sigMix(p.sig, 0xffffffffu);
+    } else {
+      HitState<R> hs = getHitState<R>(s, sh, p, h);
+      p.sig = sigMix(p.sig, (h.inst << 20) ^ h.prim);
+      if (p.depth == 1) t1 = R(h.t);
+      if (hs.lightId >= 0) {
+        hitLight<R>(s, p, hs.lightId, hs.pos);
+      } else {
+        uint32_t type = hs.mat.type;
+        if (type == ASUNA_MAT_ROUGH_PLASTIC)
+          shadeRoughPlastic<R>(s, sh, p, hs);
+        else if (type == ASUNA_MAT_DIELECTRIC)
+          shadeDielectric<R>(s, sh, p, hs);
+        else
+          shadeLambertian<R>(s, sh, p, hs);
+        p.sig = sigMix(p.sig, p.stop ? 0xfffu : p.bflags);
+      }
+    }
+    // rgen:111-127
+    if (!p.dskip) {
+      float o2[3] = {float(p.dro.x), float(p.dro.y), float(p.dro.z)},
+            d2[3] = {float(p.drd.x), float(p.drd.y), float(p.drd.z)};
+      float maxDist = float(p.ddist - R(2) * K<R>::EPS);
+      nShadow++;
+      shadows |= 1u << (p.depth - 1);
+      Hit sh2;
+      if (!traceScene(s, o2, d2, 0.0f, maxDist, true, sh2, st)) {
+        p.radiance = p.radiance + p.drad;
+        events |= 1u << (p.depth - 1);
+      }
+    }
+    if (p.stop) break;
+    // Russian roulette (extension, off for the reference's streams).
+    if (rr && p.depth >= sh.rr_depth) {
+      R q = gmin(R(0.95), gmax(p.throughput.x, gmax(p.throughput.y, p.throughput.z)));
+      R u = rnd<R>(p.seed);
+      if (!(u < q)) break;
+      p.throughput = p.throughput / q;
+    }
+    p.depth++;
+  }
+  if (p.depth > uint32_t(ps.max_path_depth)) p.depth = ps.max_path_depth;
+  // rgen:134-149
+  const R alpha = R(-2);
+  const R expXY = std::exp(alpha * R(2) * R(2));
+  R ox = jitter.x - R(0.5), oy = jitter.y - R(0.5);
+  R fw = gmax(R(0), std::exp(alpha * ox * ox) - expXY) * gmax(R(0), std::exp(alpha * oy * oy) - expXY);
+  out.rad[0] = float(p.radiance.x);
+  out.rad[1] = float(p.radiance.y);
+  out.rad[2] = float(p.radiance.z);
+  out.radd[0] = double(p.radiance.x);
+  out.radd[1] = double(p.radiance.y);
+  out.radd[2] = double(p.radiance.z);
+  out.fw = float(fw);
+  out.depth = p.depth;
+  out.sig = p.sig;
+  out.events = events;
+  out.shadows = shadows;
+  out.t1 = float(t1);
+  for (int i = 0; i < ASUNA_MAX_CHANNELS; ++i) {
+    out.ch[i][0] = float(p.ch[i].x);
+    out.ch[i][1] = float(p.ch[i].y);
+    out.ch[i][2] = float(p.ch[i].z);
+  }
+}
+
+}  // namespace ora
+
+using namespace ora;
+
+struct oracle_scene {
+  Scene s;
+};
+
+extern "C" {
+
+uint32_t oracle_xxhash32(uint32_t x, uint32_t y, uint32_t z) { return xxhash32(x, y, z); }
+void oracle_invert3x4(const float* m, float* out) { invert3x4(m, out); }
+uint32_t oracle_pcg(uint32_t* state) { return pcg(*state); }
+float oracle_rand(uint32_t* state) { return rnd<float>(*state); }
+
+int oracle_envmap_tables(uint32_t w, uint32_t h, const float* rgba, float* marg, float* cond) {
+  if (!w || !h || !rgba || !marg || !cond) return ASUNA_ERR_INVALID;
+  envTables(int(w), int(h), rgba, marg, cond);
+  return ASUNA_OK;
+}
+
+int oracle_scene_create(const asuna_scene_desc* d, oracle_scene** out) {
+  if (!d || !out) return ASUNA_ERR_INVALID;
+  oracle_scene* os = new (std::nothrow) oracle_scene;
+  if (!os) return ASUNA_ERR_OOM;
+  Scene& s = os->s;
+  s.meshes.resize(d->num_meshes);
+  for (uint32_t i = 0; i < d->num_meshes; ++i) {
+    const asuna_mesh_desc& md = d->meshes[i];
+    Mesh& m = s.meshes[i];
+    m.v.assign(md.vertices, md.vertices + md.num_vertices);
+    m.idx.assign(md.indices, md.indices + size_t(md.num_triangles) * 3);
+    m.ntri = md.num_triangles;
+    for (uint32_t k = 0; k < m.idx.size(); ++k)
+      if (m.idx[k] >= md.num_vertices) {
+        delete os;
+        return ASUNA_ERR_INVALID;
+      }
+  }
+  {
+    std::vector<std::thread> th;
+    std::atomic<uint32_t> next{0};
+    unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    for (unsigned t = 0; t < nt; ++t)
+      th.emplace_back([&] {
+        for (uint32_t i; (i = next++) < s.meshes.size();) buildBvh(s.meshes[i]);
+      });
+    for (auto& t : th) t.join();
+  }
+  s.insts.resize(d->num_instances);
+  for (uint32_t i = 0; i < d->num_instances; ++i) {
+    s.insts[i].d = d->instances[i];
+    if (d->instances[i].mesh_id >= d->num_meshes) {
+      delete os;
+      return ASUNA_ERR_INVALID;
+    }
+    invert3x4(d->instances[i].transform, s.insts[i].w2o);
+  }
+  s.mats.assign(d->materials, d->materials + d->num_materials);
+  s.lights.assign(d->lights, d->lights + d->num_lights);
+  if (d->envmap.rgba && d->envmap.width && d->envmap.height) {
+    int w = int(d->envmap.width), h = int(d->envmap.height);
+    s.hasEnv = true;
+    s.env.w = s.marg.w = s.cond.w = w;
+    s.env.h = s.marg.h = s.cond.h = h;
+    s.env.c = 4;
+    s.marg.c = s.cond.c = 2;
+    s.env.d.assign(d->envmap.rgba, d->envmap.rgba + size_t(w) * h * 4);
+    s.marg.d.resize(size_t(w) * h * 2);
+    s.cond.d.resize(size_t(w) * h * 2);
+    envTables(w, h, d->envmap.rgba, s.marg.d.data(), s.cond.d.data());
+  } else {
+    // Dummy 1x1 env of the reference (src/core/texture.cpp:137-142).
+    s.env.w = s.marg.w = s.cond.w = 1;
+    s.env.h = s.marg.h = s.cond.h = 1;
+    s.env.c = 4;
+    s.marg.c = s.cond.c = 2;
+    s.env.d.assign(4, 0.0f);
+    s.marg.d.assign(2, 0.0f);
+    s.cond.d.assign(2, 0.0f);
+  }
+  *out = os;
+  return ASUNA_OK;
+}
+
+void oracle_scene_destroy(oracle_scene* s) { delete s; }
+
+int oracle_trace(const oracle_scene* s, const float o[3], const float d[3], float tmin, float tmax, float* t,
+                 uint32_t* inst, uint32_t* prim, float* bu, float* bv) {
+  Hit h;
+  if (!traceScene(s->s, o, d, tmin, tmax, false, h, nullptr)) return 0;
+  *t = h.t;
+  *inst = h.inst;
+  *prim = h.prim;
+  *bu = h.u;
+  *bv = h.v;
+  return 1;
+}
+
+int oracle_occluded(const oracle_scene* s, const float o[3], const float d[3], float tmin, float tmax) {
+  Hit h;
+  return traceScene(s->s, o, d, tmin, tmax, true, h, nullptr) ? 1 : 0;
+}
+
+int oracle_render(const oracle_scene* os, const asuna_shot* shot, float* film, asuna_path_record* records,
+                  const uint32_t* pixels, uint32_t npixels, int nthreads, int precision, oracle_stats* stats) {
+  if (!os || !shot || (!film && !records)) return ASUNA_ERR_INVALID;
+  const Scene& s = os->s;
+  const uint32_t W = shot->width, H = shot->height;
+  if (!W || !H || shot->state.max_path_depth < 1 || shot->state.max_path_depth > 32) return ASUNA_ERR_INVALID;
+  const uint32_t npix = pixels ? npixels : W * H;
+  if (pixels)
+    for (uint32_t i = 0; i < npix; ++i)
+      if (pixels[i] >= W * H) return ASUNA_ERR_INVALID;
+  if (nthreads <= 0) nthreads = int(std::max(1u, std::thread::hardware_concurrency()));
+  const size_t img = size_t(W) * H * 4;
+  const asuna_rt_state& ps = shot->state;
+  const int depthSlot = shot->depth_out_channel;
+  std::atomic<uint32_t> next{0};
+  std::atomic<uint64_t> gExt{0}, gSh{0}, gNodes{0}, gTris{0};
+  auto t0 = std::chrono::steady_clock::now();
+  auto worker = [&] {
+    TravStats st;
+    uint64_t nExt = 0, nSh = 0;
+    const uint32_t chunk = 64;
+    for (;;) {
+      uint32_t b = next.fetch_add(chunk);
+      if (b >= npix) break;
+      uint32_t e = std::min(npix, b + chunk);
+      for (uint32_t i = b; i < e; ++i) {
+        uint32_t pix = pixels ? pixels[i] : i;
+        uint32_t x = pix % W, y = pix / W;
+        float* rad0 = film ? film + size_t(pix) * 4 : nullptr;
+        float* wimg = film ? film + 8 * img + size_t(pix) * 4 : nullptr;
+        for (uint32_t f = 0; f < shot->frames; ++f) {
+          uint32_t frame = shot->frame0 + f;
+          PathOut po;
+          if (precision == 64)
+            tracePath<double>(s, *shot, x, y, frame, po, &st, nExt, nSh);
+          else
+            tracePath<float>(s, *shot, x, y, frame, po, &st, nExt, nSh);
+          if (records) {
+            asuna_path_record& r = records[size_t(f) * npix + i];
+            r.radiance[0] = po.rad[0];
+            r.radiance[1] = po.rad[1];
+            r.radiance[2] = po.rad[2];
+            r.filter_weight = po.fw;
+            r.depth = po.depth;
+            r.signature = po.sig;
+            r.events = po.events;
+            r.shadows = po.shadows;
+          }
+          if (film) {
+            // rgen:147-179 (spp = 1 per frame)
+            float rc[3];
+            for (int c = 0; c < 3; ++c) rc[c] = gclamp(po.rad[c], 0.0f, 10.0f);
+            float rws[3] = {po.fw * rc[0], po.fw * rc[1], po.fw * rc[2]};
+            float fws = po.fw;
+            if (frame == 0) {
+              for (int c = 0; c < 3; ++c) rad0[c] = rws[c] / fws;
+              rad0[3] = 1.0f;
+              for (uint32_t cid = 0; cid < ps.n_multi_channel && cid < ASUNA_MAX_CHANNELS; ++cid) {
+                float* ch = film + size_t(cid + 1) * img + size_t(pix) * 4;
+                if (int(cid) == depthSlot) {
+                  ch[0] = ch[1] = ch[2] = po.t1;
+                } else {
+                  ch[0] = po.ch[cid][0];
+                  ch[1] = po.ch[cid][1];
+                  ch[2] = po.ch[cid][2];
+                }
+                ch[3] = 1.0f;
+              }
+              wimg[0] = wimg[1] = wimg[2] = wimg[3] = fws;
+            } else {
+              float ow = wimg[0];
+              float nw = ow + fws;
+              for (int c = 0; c < 3; ++c) rad0[c] = (rad0[c] * ow + rws[c]) / nw;
+              rad0[3] = 1.0f;
+              wimg[0] = wimg[1] = wimg[2] = wimg[3] = nw;
+            }
+          }
+        }
+      }
+    }
+    gExt += nExt;
+    gSh += nSh;
+    gNodes += st.nodes;
+    gTris += st.tris;
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nthreads; ++t) th.emplace_back(worker);
+  worker();
+  for (auto& t : th) t.join();
+  if (stats) {
+    stats->paths = uint64_t(npix) * shot->frames;
+    stats->extend_rays = gExt;
+    stats->shadow_rays = gSh;
+    stats->nodes_visited = gNodes;
+    stats->tris_tested = gTris;
+    stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    stats->threads = nthreads;
+  }
+  return ASUNA_OK;
+}
+
+int oracle_render_pixels_f64(const oracle_scene* os, const asuna_shot* shot, const uint32_t* pixels, uint32_t npixels,
+                             int nthreads, double* out_rgb, oracle_stats* stats) {
+  if (!os || !shot || !out_rgb) return ASUNA_ERR_INVALID;
+  const Scene& s = os->s;
+  const uint32_t W = shot->width, H = shot->height;
+  const uint32_t npix = pixels ? npixels : W * H;
+  if (nthreads <= 0) nthreads = int(std::max(1u, std::thread::hardware_concurrency()));
+  std::atomic<uint32_t> next{0};
+  std::atomic<uint64_t> gExt{0}, gSh{0};
+  auto t0 = std::chrono::steady_clock::now();
+  auto worker = [&] {
+    uint64_t nExt = 0, nSh = 0;
+    for (;;) {
+      uint32_t i = next.fetch_add(1);
+      if (i >= npix) break;
+      uint32_t pix = pixels ? pixels[i] : i;
+      uint32_t x = pix % W, y = pix / W;
+      double acc[3] = {0, 0, 0}, wsum = 0;
+      for (uint32_t f = 0; f < shot->frames; ++f) {
+        PathOut po;
+        tracePath<double>(s, *shot, x, y, shot->frame0 + f, po, nullptr, nExt, nSh);
+        double fw = po.fw;
+        for (int c = 0; c < 3; ++c) acc[c] += fw * std::min(std::max(po.radd[c], 0.0), 10.0);
+        wsum += fw;
+      }
+      for (int c = 0; c < 3; ++c) out_rgb[size_t(i) * 3 + c] = acc[c] / wsum;
+    }
+    gExt += nExt;
+    gSh += nSh;
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nthreads; ++t) th.emplace_back(worker);
+  worker();
+  for (auto& t : th) t.join();
+  if (stats) {
+    stats->paths = uint64_t(npix) * shot->frames;
+    stats->extend_rays = gExt;
+    stats->shadow_rays = gSh;
+    stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    stats->threads = nthreads;
+  }
+  return ASUNA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,144 @@
+"""Translate the reference's ray-tracing shaders into host C++ (test infrastructure).
+
+Reads the GLSL source of Asuna's hot path where it lies in the reference tree
+and writes mechanically rewritten copies into ``oracle/_ref/gen/`` (git-ignored,
+never committed).  ``oracle/ref_harness.cpp`` includes them and provides the
+ray-tracing built-ins (traceRayEXT, gl_* variables, descriptor bindings), so
+the reference's own shading, sampling and accumulation code runs on the CPU.
+It is the pin of the CPU restatement in ``oracle/asuna_oracle.cpp``.
+
+Rewrites (all mechanical, no logic changes):
+  * drop ``#version`` / ``#extension`` lines and the single-line ``layout(...)``
+    / payload / hit-attribute declarations (the harness defines those globals);
+  * ``#include`` of a GLSL file -> the translated file; of ``shared/*.h`` ->
+    dropped (the harness includes them at global scope);
+  * ``inout T x`` / ``out T x`` -> ``T& x``; ``in T x`` -> ``T x``;
+  * rvalue swizzles ``.xy .xyz .rg .rgb .rgba`` -> accessor calls;
+  * unsuffixed floating literals get an ``f`` suffix (GLSL literals are float);
+  * the macro ``INFINITY`` is renamed (it clashes with C's);
+  * ``vec2(rand(s), rand(s))`` -> brace initialisation, because C++ does not
+    order function arguments and GLSL evaluates them left to right;
+  * stage bodies (rgen / rmiss / rchit) are wrapped in their own namespaces;
+  * only ``luminance`` is taken from utils/sun_and_sky.glsl (sun & sky itself
+    is disabled in the reference's default scene state, in_use = 0);
+  * raytrace.projective.rgen clears ``mRec.channel[i]`` for i < 9 although the
+    array has 8 entries (an out-of-bounds write on the GPU); the loop bound is
+    reduced to 8 so host C++ stays defined.
+
+Usage: python oracle/gen_ref.py [--ref /root/reference] [--out oracle/_ref/gen]
+"""
+import argparse
+import os
+import re
+import sys
+
+SHADERS = {
+    # file (relative to src/shaders) -> stage namespace (None = shared utility)
+    "utils/structs.glsl": None,
+    "utils/math.glsl": None,
+    "utils/sample_light.glsl": None,
+    "utils/rchit_layouts.glsl": None,
+    "raytrace.projective.rgen": "stage_rgen",
+    "raytrace.default.rmiss": "stage_miss",
+    "raytrace.shadow.rmiss": "stage_shadow",
+    "bxdf/raytrace.brdf_lambertian.rchit": "stage_lambertian",
+    "bxdf/raytrace.brdf_rough_plastic.rchit": "stage_rough_plastic",
+    "bxdf/raytrace.bsdf_dielectric.rchit": "stage_dielectric",
+}
+
+FLOAT_LIT = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")
+SWIZZLE = re.compile(r"\.(xyz|xy|rgba|rgb|rg)\b")
+DROP_LINE = re.compile(r"^\s*(#version|#extension|layout\s*\(|hitAttributeEXT)")
+
+
+def out_name(rel):
+    return os.path.basename(rel) + ".h"
+
+
+def translate(text, rel, stage):
+    lines = []
+    body_start = 0
+    for line in text.splitlines():
+        if DROP_LINE.match(line):
+            if line.lstrip().startswith("layout") and not line.rstrip().endswith(";"):
+                raise SystemExit(f"{rel}: multi-line layout declaration not handled: {line!r}")
+            lines.append("// [dropped] " + line.strip())
+            continue
+        m = re.match(r'^\s*#include\s+"([^"]+)"', line)
+        if m:
+            inc = m.group(1)
+            base = os.path.basename(inc)
+            if "/shared/" in inc or inc.startswith("shared/"):
+                lines.append(f"// [shared header at global scope] {inc}")
+            elif base == "sun_and_sky.glsl":
+                lines.append('#include "sun_and_sky_min.glsl.h"')
+            else:
+                lines.append(f'#include "{base}.h"')
+            body_start = len(lines)
+            continue
+        lines.append(line)
+    src = "\n".join(lines)
+    # code-level rewrites (comments are rewritten too, harmlessly)
+    src = re.sub(r"\b(inout|out)\s+(\w+)\s+(\w+)", r"\2& \3", src)
+    src = re.sub(r"\bin\s+(?=(const\s+)?\w+\s+\w+\s*[,)\[])", "", src)
+    src = SWIZZLE.sub(lambda m: "." + m.group(1) + "()", src)
+    src = FLOAT_LIT.sub(lambda m: m.group(1) + "f", src)
+    src = re.sub(r"\bINFINITY\b", "GLSL_INFINITY", src)
+    src = src.replace("vec2(rand(seed), rand(seed))", "vec2{rand(seed), rand(seed)}")
+    src = src.replace("vec3(rand(seed), rand(seed), rand(seed))", "vec3{rand(seed), rand(seed), rand(seed)}")
+    if rel == "raytrace.projective.rgen":
+        new = src.replace("for (int i = 0; i < NUM_OUTPUT_IMAGES; i++)\n      payload.mRec.channel[i]",
+                          "for (int i = 0; i < NUM_OUTPUT_IMAGES - 1; i++)\n      payload.mRec.channel[i]")
+        if new == src:
+            raise SystemExit("rgen: channel-clear loop not found")
+        src = new
+    # no other call may take two side-effecting rand() arguments
+    for ln in src.splitlines():
+        if ln.count("rand(") + ln.count("rand2(") >= 2 and "{rand(seed)" not in ln and not ln.strip().startswith("//"):
+            raise SystemExit(f"{rel}: multiple RNG draws in one expression: {ln.strip()}")
+    if stage:
+        out = src.splitlines()
+        out.insert(body_start, f"namespace {stage} {{")
+        out.append(f"}}  // namespace {stage}")
+        src = "\n".join(out)
+    header = f"// Generated by oracle/gen_ref.py from the reference's src/shaders/{rel}; do not commit.\n"
+    return header + src + "\n"
+
+
+def sun_and_sky_min(text):
+    m = re.search(r"float luminance\(vec3 rgb\)\s*\{[^}]*\}", text)
+    if not m:
+        raise SystemExit("luminance() not found in sun_and_sky.glsl")
+    fn = FLOAT_LIT.sub(lambda mm: mm.group(1) + "f", m.group(0))
+    return ("// Generated by oracle/gen_ref.py: luminance() of the reference's\n"
+            "// src/shaders/utils/sun_and_sky.glsl; the sun & sky model is disabled\n"
+            "// (GpuSunAndSky.in_use = 0 in Scene::reset) and stubbed.\n"
+            "#ifndef SUN_AND_SKY_MIN\n#define SUN_AND_SKY_MIN\n" + fn + "\n"
+            "inline vec3 sun_and_sky(GpuSunAndSky, vec3) { return vec3(0.0f); }\n#endif\n")
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    here = os.path.dirname(os.path.abspath(__file__))
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--out", default=os.path.join(here, "_ref", "gen"))
+    a = ap.parse_args(argv)
+    shaders = os.path.join(a.ref, "src", "shaders")
+    if not os.path.isdir(shaders):
+        print(f"reference shaders not found under {shaders}", file=sys.stderr)
+        return 2
+    os.makedirs(a.out, exist_ok=True)
+    for rel, stage in SHADERS.items():
+        with open(os.path.join(shaders, rel)) as f:
+            txt = f.read()
+        with open(os.path.join(a.out, out_name(rel)), "w") as f:
+            f.write(translate(txt, rel, stage))
+    with open(os.path.join(shaders, "utils", "sun_and_sky.glsl")) as f:
+        txt = f.read()
+    with open(os.path.join(a.out, "sun_and_sky_min.glsl.h"), "w") as f:
+        f.write(sun_and_sky_min(txt))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
