@@ -98,7 +98,8 @@ class Shot(C.Structure):
 
 class RenderStats(C.Structure):
     _fields_ = [("paths", C.c_uint64), ("extend_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
-                ("nodes_visited", C.c_uint64), ("tris_tested", C.c_uint64), ("ms_total", C.c_double),
+                ("nodes_visited", C.c_uint64), ("tris_tested", C.c_uint64),
+                ("shadow_nodes_visited", C.c_uint64), ("shadow_tris_tested", C.c_uint64), ("ms_total", C.c_double),
                 ("ms_extend", C.c_double), ("ms_connect", C.c_double), ("ms_shade", C.c_double),
                 ("extend_launches", C.c_uint64), ("connect_launches", C.c_uint64)]
 

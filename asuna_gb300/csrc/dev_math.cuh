@@ -189,22 +189,25 @@ __device__ __forceinline__ f3 offsetPositionAlongNormal(f3 p, f3 n) {
 __device__ __forceinline__ float luminance(f3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
 
 // Bilinear REPEAT fetch at the base level (the reference's env samplers).
+__device__ __forceinline__ int wrapIndex(int i, int n) {
+  // REPEAT: i mod n in [0, n); the common in-range case costs one compare
+  if (unsigned(i) >= unsigned(n)) {
+    i %= n;
+    if (i < 0) i += n;
+  }
+  return i;
+}
 __device__ __forceinline__ void texCoords(int w, int h, float u, float v, int& i0, int& i1, int& j0, int& j1, float& a,
                                           float& b) {
   float x = u * float(w) - 0.5f, y = v * float(h) - 0.5f;
   float fx0 = floorf(x), fy0 = floorf(y);
   a = x - fx0;
   b = y - fy0;
-  long long ii = (long long)fx0, jj = (long long)fy0;
-  long long m;
-  m = ii % w;
-  i0 = int(m < 0 ? m + w : m);
-  m = (ii + 1) % w;
-  i1 = int(m < 0 ? m + w : m);
-  m = jj % h;
-  j0 = int(m < 0 ? m + h : m);
-  m = (jj + 1) % h;
-  j1 = int(m < 0 ? m + h : m);
+  const int ii = __float2int_rd(fx0), jj = __float2int_rd(fy0);
+  i0 = wrapIndex(ii, w);
+  i1 = wrapIndex(ii + 1, w);
+  j0 = wrapIndex(jj, h);
+  j1 = wrapIndex(jj + 1, h);
 }
 __device__ __forceinline__ float blerp(float a, float b, float t00, float t10, float t01, float t11) {
   return (1.0f - a) * (1.0f - b) * t00 + a * (1.0f - b) * t10 + (1.0f - a) * b * t01 + a * b * t11;

@@ -129,11 +129,12 @@ struct DevCounters {
   uint32_t c[kCntNum32];
   unsigned long long extendRays;
   unsigned long long shadowRays;
-  unsigned long long nodes;
+  unsigned long long nodes;   // closest-hit traversal
   unsigned long long tris;
   unsigned long long paths;
   unsigned long long stackOverflow;  // traversals cut short by a full stack (must stay 0)
-  unsigned long long pad[2];
+  unsigned long long shNodes;  // occlusion traversal
+  unsigned long long shTris;
 };
 
 // Wavefront buffers (structure of arrays, indexed by queue slot or path).

@@ -655,6 +655,8 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
     stats->shadow_rays = c->hostCnt->shadowRays;
     stats->nodes_visited = c->hostCnt->nodes;
     stats->tris_tested = c->hostCnt->tris;
+    stats->shadow_nodes_visited = c->hostCnt->shNodes;
+    stats->shadow_tris_tested = c->hostCnt->shTris;
     float ms = 0;
     cudaEventElapsedTime(&ms, c->events[0], c->events[1]);
     stats->ms_total = ms;

@@ -53,7 +53,7 @@ __device__ __forceinline__ WT wtPre(float3 d) {
 
 // Watertight test; same operations and order as the CPU oracle.
 __device__ __forceinline__ bool wtTri(const WT& w, float3 o, float4 p0, float4 p1, float4 p2, float tmin, float tmax,
-                                      bool strict, float& t, float& b1, float& b2) {
+                                      float& t, float& b1, float& b2) {
   const float3 A = make_float3(__fsub_rn(p0.x, o.x), __fsub_rn(p0.y, o.y), __fsub_rn(p0.z, o.z));
   const float3 B = make_float3(__fsub_rn(p1.x, o.x), __fsub_rn(p1.y, o.y), __fsub_rn(p1.z, o.z));
   const float3 C = make_float3(__fsub_rn(p2.x, o.x), __fsub_rn(p2.y, o.y), __fsub_rn(p2.z, o.z));
@@ -76,7 +76,7 @@ __device__ __forceinline__ bool wtTri(const WT& w, float3 o, float4 p0, float4 p
   const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
   const float rcp = __fdiv_rn(1.0f, det);
   const float tt = __fmul_rn(T, rcp);
-  if (!(tt >= tmin && (strict ? tt < tmax : tt <= tmax))) return false;
+  if (!(tt >= tmin && tt <= tmax)) return false;
   t = tt;
   b1 = __fmul_rn(V, rcp);
   b2 = __fmul_rn(W, rcp);
@@ -129,7 +129,7 @@ __device__ __forceinline__ bool traverse(const SceneDev& S, float3 wo, float3 wd
       const float ux0 = (xs.z - o.x) * id.x, ux1 = (xs.w - o.x) * id.x;
       const float uy0 = (ys.z - o.y) * id.y, uy1 = (ys.w - o.y) * id.y;
       const float uz0 = (zs.z - o.z) * id.z, uz1 = (zs.w - o.z) * id.z;
-      const float lim = found ? best : tmax;
+      const float lim = best;
       const float a0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
       const float a1 = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), lim)) * kFarScale;
       const float b0 = fmaxf(fmaxf(fminf(ux0, ux1), fminf(uy0, uy1)), fmaxf(fminf(uz0, uz1), tmin));
@@ -182,15 +182,20 @@ __device__ __forceinline__ bool traverse(const SceneDev& S, float3 wo, float3 wd
           const float4 p0 = __ldg(&tr->v0), p1 = __ldg(&tr->v1), p2 = __ldg(&tr->v2);
           if (COUNT) ++nTris;
           float t, b1, b2;
-          if (wtTri(wt, o, p0, p1, p2, tmin, best, found, t, b1, b2)) {
-            found = true;
-            best = t;
-            h.t = t;
-            h.u = b1;
-            h.v = b2;
-            h.prim = __float_as_uint(p0.w);
-            h.inst = curInst;
+          if (wtTri(wt, o, p0, p1, p2, tmin, best, t, b1, b2)) {
             if (ANY) return true;
+            const uint32_t prim = __float_as_uint(p0.w);
+            // exact ties resolve to the lowest (instance, primitive), so the
+            // result does not depend on traversal order
+            if (!found || t < best || (curInst < h.inst || (curInst == h.inst && prim < h.prim))) {
+              found = true;
+              best = t;
+              h.t = t;
+              h.u = b1;
+              h.v = b2;
+              h.prim = prim;
+              h.inst = curInst;
+            }
           }
         }
       }
@@ -277,8 +282,8 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(KParams P) {
       b += __shfl_down_sync(0xffffffffu, b, off);
     }
     if (lane == 0) {
-      atomicAdd(&W.cnt->nodes, a);
-      atomicAdd(&W.cnt->tris, b);
+      atomicAdd(ANY ? &W.cnt->shNodes : &W.cnt->nodes, a);
+      atomicAdd(ANY ? &W.cnt->shTris : &W.cnt->tris, b);
     }
   }
 }

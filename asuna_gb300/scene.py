@@ -62,6 +62,12 @@ def set_channels(state, names):
     return depth
 
 
+def _length(v):
+    # float32 length as the reference's host code computes it (no BLAS reduction)
+    v = np.asarray(v, np.float32)
+    return np.sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2], dtype=np.float32)
+
+
 def _identity34():
     return np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 0]], np.float32)
 
@@ -140,8 +146,8 @@ class SceneBuilder:
         l.u = A.f3(*u)
         l.v = A.f3(*v)
         l.radiance = A.f3(*radiance)
-        area = float(np.linalg.norm(np.cross(u, v)))
-        l.area = area * 0.5 if triangle else area
+        area = np.float32(_length(np.cross(u, v)))
+        l.area = area * np.float32(0.5) if triangle else area
         l.double_side = 1 if double_side else 0
         light_id = len(self.lights)
         verts = np.zeros(4, A.VERTEX_DTYPE)
@@ -163,7 +169,7 @@ class SceneBuilder:
         l.u = A.f3(*u)
         l.v = A.f3(*v)
         l.radiance = A.f3(*radiance)
-        l.area = float(np.linalg.norm(np.cross(u, v))) * np.float32(0.5)
+        l.area = np.float32(_length(np.cross(u, v))) * np.float32(0.5)
         light_id = len(self.lights)
         verts = np.zeros(3, A.VERTEX_DTYPE)
         verts["pos"] = [p0, p0 + u, p0 + v]
@@ -309,7 +315,7 @@ class Film:
         check(lib().asuna_film_clear(self.ctx.handle, self.handle))
 
     def close(self):
-        if self.handle:
+        if getattr(self, "handle", None):
             lib().asuna_film_destroy(self.handle)
             self.handle = None
 
@@ -342,7 +348,7 @@ class DeviceScene:
         return hits, inst
 
     def close(self):
-        if self.handle:
+        if getattr(self, "handle", None):
             lib().asuna_scene_destroy(self.handle)
             self.handle = None
 
@@ -399,7 +405,7 @@ class Context:
         check(lib().asuna_tracer_run_offline(self.handle, scene_json.encode(), out_prefix.encode()))
 
     def close(self):
-        if self.handle:
+        if getattr(self, "handle", None):
             lib().asuna_ctx_destroy(self.handle)
             self.handle = None
 
@@ -440,7 +446,7 @@ class JsonScene:
         return list(kinds[: n.value])
 
     def close(self):
-        if self.handle:
+        if getattr(self, "handle", None):
             lib().asuna_json_free(self.handle)
             self.handle = None
 

@@ -216,3 +216,46 @@ def mixed_scene(width=1920, height=1080, frames=64, max_depth=12, n_spheres=64, 
                              focal_distance=float(np.linalg.norm(eye - at)))
     shot = make_shot(cam, state, width, height, frames, seed=0, depth_channel=depth, rr_depth=rr_depth)
     return b, shot
+
+
+def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=False, seed=11,
+                 channels=("albedo", "normal", "depth", "position", "uv", "tangent", "roughness")):
+    """Every implemented plugin in one small scene: Lambertian, anisotropic
+    rough plastic and dielectric spheres on a ground quad; a single-sided rect
+    light, a double-sided JSON "triangle" light (rect with half area), a mesh
+    triangle light, a point light and a distant light; an optional lognormal
+    environment map (else a background colour); a thin-lens perspective or an
+    OpenCV pinhole camera."""
+    rng = np.random.default_rng(seed)
+    b = SceneBuilder()
+    b.add_rect_light((-1.0, 3.0, -1.0), (0.0, 3.0, -1.0), (-1.0, 3.0, 0.0), (6.0, 5.0, 4.0))
+    b.add_rect_light((1.5, 2.0, -2.0), (2.5, 2.0, -2.0), (1.5, 3.0, -2.0), (3.0, 3.0, 5.0), double_side=True,
+                     triangle=True)
+    b.add_triangle_light((-2.5, 2.5, 0.5), (-1.5, 2.5, 0.5), (-2.0, 2.5, -0.5), (8.0, 8.0, 8.0))
+    b.add_point_light((0.5, 2.0, 1.5), (4.0, 4.0, 4.0))
+    b.add_distant_light((0.3, -1.0, -0.2), (0.8, 0.7, 0.6))
+    if env:
+        b.set_envmap(lognormal_envmap(rng, 32, 16, hotspot=2, boost=50.0))
+    g = b.add_lambertian("ground", (0.6, 0.6, 0.55))
+    lam = b.add_lambertian("lam", (0.8, 0.3, 0.2))
+    rp = b.add_rough_plastic("plastic", (0.2, 0.4, 0.8), (0.2, 0.5), 1.5)
+    di = b.add_dielectric("glass", 1.5)
+    v, i = _quad(np.array((-4, -1, 4), np.float32), np.array((4, -1, 4), np.float32),
+                 np.array((4, -1, -4), np.float32), np.array((-4, -1, -4), np.float32),
+                 np.array((0, 1, 0), np.float32))
+    b.add_mesh("ground", v, i)
+    b.add_instance("ground", g)
+    base_v, faces = icosphere(3)
+    idx = faces.astype(np.uint32).reshape(-1)
+    for k, (mat, pos) in enumerate([(lam, (-1.3, -0.2, 0.0)), (rp, (0.0, -0.1, -0.6)), (di, (1.2, -0.2, 0.3))]):
+        b.add_mesh(f"s{k}", displaced_sphere(base_v, faces, seed + k, amplitude=0.05), idx)
+        s = 0.8
+        b.add_instance(f"s{k}", mat, np.array([[s, 0, 0, pos[0]], [0, s, 0, pos[1]], [0, 0, s, pos[2]]], np.float32))
+    state, depth = b.state(spp=frames, max_path_depth=max_depth, channels=channels, bg_color=(0.2, 0.25, 0.3))
+    eye, at = (0.0, 1.0, 5.0), (0.0, -0.3, 0.0)
+    if opencv:
+        from .scene import opencv_camera
+        cam = opencv_camera(eye, at, (0, 1, 0), (0.9 * width, 0.9 * width, 0.5 * width, 0.5 * height))
+    else:
+        cam = perspective_camera(eye, at, (0, 1, 0), 55.0, width, height, aperture=0.05, focal_distance=5.0)
+    return b, make_shot(cam, state, width, height, frames, seed=0, depth_channel=depth)

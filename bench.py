@@ -1,0 +1,308 @@
+"""Benchmark of the path-tracer hot path on the mid-size mixed-material scene.
+
+Workload (one GPU): 64 icospheres of 327,680 triangles (20,971,520 + ground +
+4 light triangles), 1920x1080, max depth 12, Russian roulette after depth 3,
+1024x512 lognormal environment map + 4 triangle lights, thin lens 0.05.  A
+step renders one 1-sample frame of the film (2,073,600 paths) through the
+wavefront: raygen -> (closest hit -> shade -> occlusion) x 12 -> accumulate.
+Synthetic seeded data; the BVH (~2.7 GB) is far larger than L2 (129 MB), so
+no L2 flush is needed between steps.
+
+Metric: Mrays/s = (camera + continuation + occlusion rays traced) / time.
+`value` is device time of K steps (CUDA events on the library's stream);
+`e2e` is wall time of the same steps through the C ABI with the film read
+back to pinned host memory every step.  `roofline` is the closest-hit
+traversal kernel: algorithmic bytes = BVH nodes x 64 B + triangles x 48 B per
+ray (counted by a separate instrumented frame), over its event-timed
+duration, against the measured HBM copy bandwidth.
+
+--impl reference: the CPU oracle (the reference's hot path restated in C++,
+pinned bit-exactly to the reference's own shader source) on all host cores
+over a bounded seeded pixel sample of the same workload.
+Under torchrun (N > 1) every rank renders its own frames of the shot
+(replicas, weak scaling); rank 0 reports the max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s"
+CONFIG = {"workload": "mixed-material scene, 64 x level-7 icospheres (20.97M tris), 1920x1080, depth 12, RR>3, "
+                      "1024x512 env + 4 triangle lights, aperture 0.05",
+          "triangles": 20971526, "width": 1920, "height": 1080, "max_depth": 12, "rr_depth": 3,
+          "frames_per_step": 1, "l2": "inputs larger than L2 (BVH ~2.7 GB), no flush"}
+
+
+def dist_env():
+    r = int(os.environ.get("RANK", "0"))
+    w = int(os.environ.get("WORLD_SIZE", "1"))
+    lr = int(os.environ.get("LOCAL_RANK", "0"))
+    return r, w, lr
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+                for k, n in enumerate(names):
+                    if r[5 + k].lower() in ("active", "1", "yes"):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def build_workload(args, verbose):
+    from asuna_gb300 import scenes
+
+    b, shot = scenes.mixed_scene(args.width, args.height, frames=1, max_depth=12, n_spheres=args.spheres,
+                                 level=args.level, seed=1234, rr_depth=3, verbose=verbose)
+    return b, shot
+
+
+def cpu_leg(b, shot, seconds, threads):
+    """Oracle throughput on a bounded seeded pixel sample of the same workload."""
+    from oracle import oracle_py
+
+    t0 = time.time()
+    osc = oracle_py.OracleScene(b.desc())
+    build_s = time.time() - t0
+    rng = np.random.default_rng(0)
+    npix = shot.width * shot.height
+    n = 2048
+    while True:
+        px = np.sort(rng.choice(npix, size=min(n, npix), replace=False)).astype(np.uint32)
+        _, _, st = osc.render(shot, records=False, film=None, pixels=px, threads=threads)
+        if st["seconds"] >= seconds * 0.5 or n >= npix:
+            break
+        n = int(min(npix, n * max(2.0, seconds / max(st["seconds"], 1e-3))))
+    rays = st["extend_rays"] + st["shadow_rays"]
+    return {"value": rays / st["seconds"] / 1e6, "unit": METRIC, "cores": st["threads"], "kind": "port",
+            "sample": f"{len(px)} seeded pixels x 1 frame of the benchmark workload ({st['paths']} paths, "
+                      f"{rays} rays, {st['seconds']:.1f} s; oracle BVH build {build_s:.1f} s excluded)",
+            "msamples_per_s": st["paths"] / st["seconds"] / 1e6}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    b, shot = build_workload(args, verbose=False)
+    threads = os.cpu_count() or 1
+    vals = []
+    cb = None
+    for _ in range(args.warmup):
+        cpu_leg(b, shot, 2.0, threads)
+    for _ in range(args.steps):
+        cb = cpu_leg(b, shot, args.ref_seconds, threads)
+        vals.append(cb["value"])
+    v = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)", "config": CONFIG,
+            "cpu_baseline": {**cb, "value": v},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run(args):
+    rank, world, local = dist_env()
+    import asuna_gb300 as ag
+    from asuna_gb300 import _abi as A
+
+    torch_dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        torch_dist = dist
+    b, shot = build_workload(args, verbose=(rank == 0 and args.verbose))
+    ctx = ag.Context(local)
+    t0 = time.time()
+    scene = ctx.create_scene(b.desc())
+    sstats = scene.stats()
+    if rank == 0 and args.verbose:
+        print(f"scene built in {time.time() - t0:.1f} s: {sstats}", file=sys.stderr, flush=True)
+    film = ctx.create_film(shot.width, shot.height)
+    # per-rank frames: replicas render disjoint frames of the same shot
+    frame_base = 1 + rank * (args.warmup + args.steps + 2) * args.frames_per_step
+
+    def step(i, stats=True):
+        shot.frame0 = frame_base + i * args.frames_per_step
+        shot.frames = args.frames_per_step
+        return ctx.render(scene, shot, film, stats=stats)
+
+    # instrumented frame: traversal counters for the algorithmic bytes per ray
+    ctx.set_counters(True)
+    cst = step(0)
+    ctx.set_counters(False)
+    bytes_per_ext = (cst["nodes_visited"] * 64 + cst["tris_tested"] * 48) / max(cst["extend_rays"], 1)
+    bytes_per_sh = (cst["shadow_nodes_visited"] * 64 + cst["shadow_tris_tested"] * 48) / max(cst["shadow_rays"], 1)
+    for i in range(args.warmup):
+        step(1 + i)
+    if torch_dist:
+        torch_dist.barrier()
+    ctx.sync()
+    tot = {k: 0.0 for k in ("extend_rays", "shadow_rays", "paths", "ms_total", "ms_extend", "ms_connect",
+                            "ms_shade", "extend_launches", "connect_launches")}
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            st = step(1 + args.warmup + i)
+            for k in tot:
+                tot[k] += st[k]
+    ctx.sync()
+    ms = tot["ms_total"]
+    rays = tot["extend_rays"] + tot["shadow_rays"]
+    # e2e: the same steps through the C ABI with a host read-back of the film each step
+    host = np.empty((shot.height, shot.width, 4), np.float32)
+    try:
+        import torch
+
+        pinned = torch.empty(host.nbytes, dtype=torch.uint8).pin_memory()
+        host = np.frombuffer(pinned.numpy(), dtype=np.float32).reshape(shot.height, shot.width, 4)
+    except Exception:
+        pass
+    e2e_rays = 0
+    ctx.sync()
+    te = time.perf_counter()
+    for i in range(args.steps):
+        st = step(1 + args.warmup + args.steps + i, stats=True)
+        film.read(0, out=host)
+        e2e_rays += st["extend_rays"] + st["shadow_rays"]
+    e2e_s = time.perf_counter() - te
+    if torch_dist:
+        import torch
+
+        t = torch.tensor([ms, e2e_s], dtype=torch.float64, device=f"cuda:{local}")
+        torch_dist.all_reduce(t, op=torch_dist.ReduceOp.MAX)
+        r = torch.tensor([rays, e2e_rays], dtype=torch.float64, device=f"cuda:{local}")
+        torch_dist.all_reduce(r, op=torch_dist.ReduceOp.SUM)
+        ms, e2e_s = float(t[0]), float(t[1])
+        rays, e2e_rays = float(r[0]), float(r[1])
+    if rank != 0:
+        if torch_dist:
+            torch_dist.destroy_process_group()
+        return 0
+    peak, peak_kind = peaks()
+    ext_ms_per_launch = tot["ms_extend"] / max(tot["extend_launches"], 1)
+    ext_bytes_per_launch = bytes_per_ext * tot["extend_rays"] / max(tot["extend_launches"], 1)
+    achieved = ext_bytes_per_launch / (ext_ms_per_launch * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "extend_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tj = json.load(f)
+        traffic = tj.get("dram_bytes_per_ray", 0) * tot["extend_rays"] / max(tot["extend_launches"], 1)
+    launches = int(args.steps * (2 + 3 * 12))
+    line = {
+        "metric": METRIC, "value": rays / (ms * 1e-3) / 1e6, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": {**CONFIG, "width": shot.width, "height": shot.height, "parallelism": f"replicas{world}"},
+        "msamples_per_s": tot["paths"] * world / (ms * 1e-3) / 1e6 if world == 1 else None,
+        "rays_per_step": rays / args.steps,
+        "e2e": {"value": e2e_rays / e2e_s / 1e6, "unit": METRIC, "h2d_bytes_per_step": C_SHOT_BYTES,
+                "d2h_bytes_per_step": int(host.nbytes)},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "k_trace<closest-hit>", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": traffic, "bytes_per_ray": bytes_per_ext, "shadow_bytes_per_ray": bytes_per_sh,
+                     "ms_per_launch": ext_ms_per_launch},
+        "kernel_ms": {"extend": tot["ms_extend"], "shade": tot["ms_shade"], "connect": tot["ms_connect"]},
+        "clocks": clk.summary(),
+        "scene": {"triangles": sstats["triangles"], "device_bytes": sstats["device_bytes"],
+                  "build_ms": sstats["build_ms"]},
+    }
+    if not args.no_cpu and world == 1:
+        line["cpu_baseline"] = cpu_leg(b, shot, args.cpu_seconds, os.cpu_count() or 1)
+    print(json.dumps(line), flush=True)
+    if torch_dist:
+        torch_dist.destroy_process_group()
+    return 0
+
+
+C_SHOT_BYTES = 340  # sizeof(asuna_shot): the only host->device input of a step
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--spheres", type=int, default=64)
+    ap.add_argument("--level", type=int, default=7)
+    ap.add_argument("--frames-per-step", type=int, default=1)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--verbose", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

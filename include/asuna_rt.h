@@ -268,8 +268,10 @@ typedef struct asuna_render_stats {
   uint64_t paths;          /* camera rays = samples                         */
   uint64_t extend_rays;    /* closest-hit rays (camera + continuation)      */
   uint64_t shadow_rays;    /* occlusion rays                                */
-  uint64_t nodes_visited;  /* only when traversal counters are enabled      */
-  uint64_t tris_tested;    /* only when traversal counters are enabled      */
+  uint64_t nodes_visited;  /* closest-hit BVH nodes (traversal counters on)  */
+  uint64_t tris_tested;    /* closest-hit triangle tests (counters on)      */
+  uint64_t shadow_nodes_visited; /* occlusion BVH nodes (counters on)       */
+  uint64_t shadow_tris_tested;   /* occlusion triangle tests (counters on)  */
   double ms_total;         /* device time of the call (CUDA events)         */
   double ms_extend;        /* device time of closest-hit traversal kernels  */
   double ms_connect;       /* device time of occlusion traversal kernels    */

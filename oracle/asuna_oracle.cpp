@@ -523,11 +523,17 @@ static bool traceScene(const Scene& s, const float o[3], const float d[3], float
           float t, b1, b2;
           if (st) st->tris++;
           if (intersectTri(rp, tv, tv + 3, tv + 6, tmin, best, t, b1, b2)) {
-            if (!found || t < best) {
+            if (anyHit) {
+              hit = Hit{t, ii, m.order[nd.start + k], b1, b2};
+              return true;
+            }
+            const uint32_t prim = m.order[nd.start + k];
+            // exact ties resolve to the lowest (instance, primitive): the
+            // closest hit does not depend on traversal order
+            if (!found || t < best || ii < hit.inst || (ii == hit.inst && prim < hit.prim)) {
               found = true;
               best = t;
-              hit = Hit{t, ii, m.order[nd.start + k], b1, b2};
-              if (anyHit) return true;
+              hit = Hit{t, ii, prim, b1, b2};
             }
           }
         }

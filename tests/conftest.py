@@ -1,0 +1,21 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the sm_103a kernels)")
+
+
+@pytest.fixture(scope="session")
+def ctx():
+    import asuna_gb300 as ag
+
+    c = ag.Context(0)
+    yield c
+    c.close()

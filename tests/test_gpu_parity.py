@@ -1,0 +1,69 @@
+"""GPU path records and films against the CPU oracle (same seeded inputs).
+
+Tolerance (stated in tests/parity.py): per path every radiance channel within
+1e-4 relative (+1e-6 absolute); at least 99.9% of paths must agree; paths
+that took a different branch (hit / lobe / visibility signature) are counted
+as flips and reported.  Integer parts (RNG streams, depths, signatures) are
+compared bit for bit on the paths without flips.
+"""
+import numpy as np
+import pytest
+
+from asuna_gb300 import scenes
+from oracle import oracle_py
+from tests.parity import compare
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(ctx, b, shot):
+    d = b.desc()
+    scene = ctx.create_scene(d)
+    film = ctx.create_film(shot.width, shot.height)
+    rec = ctx.render_paths(scene, shot, film)
+    imgs = np.stack([film.read(k) for k in range(9)])
+    ofilm, orec, _ = oracle_py.OracleScene(d).render(shot)
+    return rec, orec, imgs, ofilm
+
+
+def _check(rec, orec, imgs, ofilm, film_tol=1e-3):
+    c = compare(rec, orec)
+    print(c)
+    assert c["within"] >= 0.999, c
+    same = (rec["signature"] == orec["signature"]) & (rec["events"] == orec["events"])
+    assert np.array_equal(rec["depth"][same], orec["depth"][same])
+    # films: radiance, AOVs and weight sums
+    assert np.abs(imgs[8] - ofilm[8]).max() <= 1e-5
+    err = np.abs(imgs[0] - ofilm[0])
+    assert np.quantile(err, 0.999) <= film_tol
+    return c
+
+
+def test_box_scene_small(ctx):
+    b, shot = scenes.box_scene(64, 64, frames=4, max_depth=8)
+    rec, orec, imgs, ofilm = _run(ctx, b, shot)
+    c = _check(rec, orec, imgs, ofilm)
+    assert c["exact"] > 0.5  # FP32 arithmetic in the same order: most paths are bit-identical
+    for k in (1, 2, 3):  # albedo, normal, depth AOVs
+        assert np.quantile(np.abs(imgs[k] - ofilm[k]), 0.999) <= 1e-4
+
+
+def test_box_scene_full_config(ctx):
+    # the small-box configuration: 256x256, 16 spp (frames), depth 8
+    b, shot = scenes.box_scene(256, 256, frames=16, max_depth=8)
+    rec, orec, imgs, ofilm = _run(ctx, b, shot)
+    _check(rec, orec, imgs, ofilm)
+
+
+@pytest.mark.parametrize("env,opencv", [(True, False), (False, True), (True, True)])
+def test_every_plugin(ctx, env, opencv):
+    b, shot = scenes.plugin_scene(96, 64, frames=4, max_depth=8, env=env, opencv=opencv)
+    rec, orec, imgs, ofilm = _run(ctx, b, shot)
+    _check(rec, orec, imgs, ofilm, film_tol=5e-3)
+
+
+def test_mixed_scene_small(ctx):
+    b, shot = scenes.mixed_scene(160, 90, frames=2, max_depth=12, n_spheres=12, level=4, seed=3, rr_depth=3,
+                                 env_size=(128, 64))
+    rec, orec, imgs, ofilm = _run(ctx, b, shot)
+    _check(rec, orec, imgs, ofilm, film_tol=5e-2)

@@ -1,0 +1,90 @@
+"""BVH traversal on the GPU against the oracle's independent BVH: closest
+hits (t, instance, primitive, barycentrics) bit for bit, occlusion queries,
+watertightness on shared edges and vertices, and the tmin/tmax contract."""
+import numpy as np
+import pytest
+
+import asuna_gb300 as ag
+from asuna_gb300 import scenes
+from oracle import oracle_py
+
+pytestmark = pytest.mark.gpu
+
+
+def _random_rays(rng, n, center, radius):
+    o = center + rng.normal(size=(n, 3)) * radius * 1.5
+    tgt = center + rng.normal(size=(n, 3)) * radius * 0.5
+    d = tgt - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return o.astype(np.float32), d.astype(np.float32)
+
+
+def test_closest_hit_matches_oracle(ctx):
+    b, _ = scenes.mixed_scene(8, 8, frames=1, n_spheres=16, level=4, seed=5, env_size=(8, 4))
+    d = b.desc()
+    scene = ctx.create_scene(d)
+    o_sc = oracle_py.OracleScene(d)
+    rng = np.random.default_rng(0)
+    o, dirs = _random_rays(rng, 4000, np.zeros(3), 10.0)
+    hits, inst = scene.trace(o, dirs)
+    mism = 0
+    for k in range(len(o)):
+        r = o_sc.trace(o[k], dirs[k])
+        if r is None:
+            mism += inst[k] != 0xFFFFFFFF
+            continue
+        t, ii, prim, u, v = r
+        got = (hits[k, 0], inst[k], hits[k, 3].view(np.uint32), hits[k, 1], hits[k, 2])
+        if not (got[0] == np.float32(t) and got[1] == ii and got[2] == prim and got[3] == np.float32(u)
+                and got[4] == np.float32(v)):
+            mism += 1
+    assert mism <= 2, mism  # only exact-tie order may differ
+
+
+def test_occlusion_matches_oracle(ctx):
+    b, _ = scenes.mixed_scene(8, 8, frames=1, n_spheres=16, level=3, seed=6, env_size=(8, 4))
+    d = b.desc()
+    scene = ctx.create_scene(d)
+    o_sc = oracle_py.OracleScene(d)
+    rng = np.random.default_rng(1)
+    o, dirs = _random_rays(rng, 3000, np.zeros(3), 10.0)
+    tmax = rng.uniform(0.5, 30.0, len(o)).astype(np.float32)
+    hits, inst = scene.trace(o, dirs, tmin=0.0, tmax=tmax, any_hit=True)
+    got = hits[:, 0] > 0
+    want = np.array([o_sc.occluded(o[k], dirs[k], 0.0, float(tmax[k])) for k in range(len(o))])
+    assert np.mean(got == want) >= 0.999
+
+
+def test_watertight_shared_edges_and_vertices(ctx):
+    # rays aimed exactly at vertices and edge midpoints of a closed icosphere never miss it
+    v, f = scenes.icosphere(3)
+    b = ag.SceneBuilder()
+    m = b.add_lambertian("m", (0.5, 0.5, 0.5))
+    verts = np.zeros(len(v), ag._abi.VERTEX_DTYPE)
+    verts["pos"] = v.astype(np.float32)
+    b.add_mesh("ico", verts, f.astype(np.uint32))
+    b.add_instance("ico", m)
+    scene = ctx.create_scene(b.desc())
+    p = verts["pos"].astype(np.float64)
+    targets = np.concatenate([p, 0.5 * (p[f[:, 0]] + p[f[:, 1]]), (p[f[:, 0]] + p[f[:, 1]] + p[f[:, 2]]) / 3])
+    rng = np.random.default_rng(2)
+    origins = rng.normal(size=targets.shape) * 0.05  # from inside the sphere
+    dirs = targets - origins
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    hits, inst = scene.trace(origins.astype(np.float32), dirs.astype(np.float32), tmin=0.0)
+    assert np.all(inst != 0xFFFFFFFF), int(np.sum(inst == 0xFFFFFFFF))
+
+
+def test_tmin_tmax_contract(ctx):
+    b, _ = scenes.box_scene(8, 8, frames=1)
+    scene = ctx.create_scene(b.desc())
+    o = np.array([[0.5, 0.5, 0.0]] * 3, np.float32)
+    dirs = np.array([[0.0, 0.0, -1.0]] * 3, np.float32)  # back wall at z = -1 (t = 1), above both cuboids
+    hits, inst = scene.trace(o, dirs, tmin=0.0, tmax=np.float32(1e10))
+    assert np.allclose(hits[:, 0], 1.0)
+    occ, _ = scene.trace(o, dirs, tmin=0.0, tmax=np.float32(0.999), any_hit=True)
+    assert np.all(occ[:, 0] < 0)
+    occ, _ = scene.trace(o, dirs, tmin=0.0, tmax=np.float32(1.001), any_hit=True)
+    assert np.all(occ[:, 0] > 0)
+    hits, inst = scene.trace(o, dirs, tmin=1.5, tmax=np.float32(1e10))
+    assert np.all(inst == 0xFFFFFFFF)

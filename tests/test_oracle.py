@@ -1,0 +1,73 @@
+"""The CPU oracle against the reference: golden vectors generated from the
+reference's own shader code (tests/golden/make_golden.py) and, where the
+reference tree is present, a live comparison with it."""
+import os
+
+import numpy as np
+import pytest
+
+from asuna_gb300 import scenes
+from oracle import oracle_py
+from tests.golden.make_golden import CASES
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_rng_known_answers():
+    g = np.load(os.path.join(GOLDEN, "rng_kat.npz"))
+    L = oracle_py.port()
+    import ctypes as C
+
+    for (x, y, z), h in zip(g["xyz"], g["hash"]):
+        assert L.oracle_xxhash32(int(x), int(y), int(z)) == int(h)
+    for s, row in zip(g["seeds"], g["rand"]):
+        st = C.c_uint32(int(s))
+        got = np.array([L.oracle_rand(C.byref(st)) for _ in range(len(row))], np.float32)
+        assert np.array_equal(got, row)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_oracle_matches_golden(name):
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    b, shot = CASES[name]()
+    shot.depth_out_channel = -1
+    film, rec, st = oracle_py.OracleScene(b.desc()).render(shot)
+    # the reference's payload holds the clamped radiance (rgen:147)
+    assert np.array_equal(np.clip(rec["radiance"], 0, 10), g["radiance"])
+    for k in ("depth", "signature", "events", "shadows"):
+        assert np.array_equal(rec[k], g[k]), k
+    assert np.array_equal(film, g["film"])
+    assert st["extend_rays"] > st["paths"] and st["shadow_rays"] > 0
+
+
+@pytest.mark.skipif(oracle_py.ref() is None, reason="reference tree not present")
+def test_oracle_matches_reference_live():
+    b, shot = scenes.plugin_scene(40, 30, frames=4, max_depth=6, env=True, seed=23)
+    shot.depth_out_channel = -1
+    d = b.desc()
+    film, rec, _ = oracle_py.OracleScene(d).render(shot)
+    rfilm, rrec = oracle_py.ref_render(d, shot, threads=1)
+    assert np.array_equal(np.clip(rec["radiance"], 0, 10), rrec["radiance"])
+    assert np.array_equal(rec["signature"], rrec["signature"])
+    assert np.array_equal(film, rfilm)
+
+
+def test_oracle_resume_equals_single_call():
+    b, shot = scenes.box_scene(16, 16, frames=6, max_depth=5)
+    o = oracle_py.OracleScene(b.desc())
+    full, _, _ = o.render(shot, records=False)
+    shot.frames = 2
+    part, _, _ = o.render(shot, records=False)
+    shot.frame0, shot.frames = 2, 4
+    part, _, _ = o.render(shot, film=part, records=False)
+    assert np.array_equal(full, part)
+
+
+def test_oracle_double_precision_close_to_float():
+    b, shot = scenes.box_scene(16, 16, frames=64, max_depth=6)
+    o = oracle_py.OracleScene(b.desc())
+    f32, _, _ = o.render(shot, records=False)
+    px = np.arange(256, dtype=np.uint32)
+    f64, _ = o.pixels_f64(shot, px)
+    a = f32[0, ..., :3].reshape(-1, 3)
+    assert np.abs(a.mean() - f64.mean()) < 0.02 * f64.mean()
