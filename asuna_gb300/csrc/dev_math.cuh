@@ -8,6 +8,7 @@
 #pragma once
 #include <cstdint>
 
+#include "../../include/asuna_math.h"
 #include "dev_types.h"
 
 namespace asuna {
@@ -52,6 +53,14 @@ __device__ __forceinline__ f3 refract(f3 I, f3 N, float eta) {
 }
 __device__ __forceinline__ f3 ld3(float4 v) { return {v.x, v.y, v.z}; }
 __device__ __forceinline__ f3 ld3(const float* a) { return {a[0], a[1], a[2]}; }
+
+// Transcendentals: the shared implementation of include/asuna_math.h, so the
+// CPU oracle computes the same bits.
+__device__ __forceinline__ float msin(float x) { return asuna_math::sinf_(x); }
+__device__ __forceinline__ float mcos(float x) { return asuna_math::cosf_(x); }
+__device__ __forceinline__ float macos(float x) { return asuna_math::acosf_(x); }
+__device__ __forceinline__ float matan2(float y, float x) { return asuna_math::atan2f_(y, x); }
+__device__ __forceinline__ float mexp(float x) { return asuna_math::expf_(x); }
 
 constexpr float PI = 3.14159265358979323846f;
 constexpr float TWO_PI = 6.28318530717958647692f;
@@ -145,7 +154,7 @@ __device__ __forceinline__ f2 concentricSampleDisk(f2 u) {
     r = oy;
     theta = PI_OVER_2 - PI_OVER_4 * (ox / oy);
   }
-  return f2{r * cosf(theta), r * sinf(theta)};
+  return f2{r * mcos(theta), r * msin(theta)};
 }
 __device__ __forceinline__ f3 cosineSampleHemisphere(f2 u) {
   f2 d = concentricSampleDisk(u);
@@ -233,20 +242,20 @@ __device__ __forceinline__ f3 tex4rgb(const float4* t, int w, int h, float u, fl
 // sample_light.glsl:84-95
 __device__ __forceinline__ float pdfEnvmap(const SceneDev& S, const ShotDev& sh, f3 L) {
   L = transformDirectionT(sh.cam.env_transform, L);
-  float theta = acosf(gclamp(L.y, -1.0f, 1.0f));
-  float u = (PI + atan2f(L.z, L.x)) * INV_2PI, v = theta * INV_PI;
+  float theta = macos(gclamp(L.y, -1.0f, 1.0f));
+  float u = (PI + matan2(L.z, L.x)) * INV_2PI, v = theta * INV_PI;
   f2 c = tex2(S.cond, S.envW, S.envH, u, v);
   f2 m = tex2(S.marg, S.envW, S.envH, 0.0f, v);
   float pdf = c.y * m.y;
-  float sinTheta = sinf(theta);
+  float sinTheta = msin(theta);
   if (sinTheta == 0.0f) return 0.0f;
   return (pdf * sh.state.env_map_resolution[0] * sh.state.env_map_resolution[1]) / (TWO_PI * PI * sinTheta);
 }
 // sample_light.glsl:97-104
 __device__ __forceinline__ f3 evalEnvmap(const SceneDev& S, const ShotDev& sh, f3 L) {
   L = transformDirectionT(sh.cam.env_transform, L);
-  float theta = acosf(gclamp(L.y, -1.0f, 1.0f));
-  float u = (PI + atan2f(L.z, L.x)) * INV_2PI, v = theta * INV_PI;
+  float theta = macos(gclamp(L.y, -1.0f, 1.0f));
+  float u = (PI + matan2(L.z, L.x)) * INV_2PI, v = theta * INV_PI;
   f3 e = tex4rgb(S.env, S.envW, S.envH, u, v);
   float k = sh.state.env_map_intensity;
   return f3{k * e.x, k * e.y, k * e.z};
@@ -262,9 +271,9 @@ __device__ __forceinline__ f3 sampleEnvmap(const SceneDev& S, const ShotDev& sh,
   pdf = c.y * m.y;
   float phi = uvx * TWO_PI;
   float theta = uvy * PI;
-  if (sinf(theta) == 0.0f) pdf = 0.0f;
-  pdf = (pdf * sh.state.env_map_resolution[0] * sh.state.env_map_resolution[1]) / (TWO_PI * PI * sinf(theta));
-  L = f3{-sinf(theta) * cosf(phi), cosf(theta), -sinf(theta) * sinf(phi)};
+  if (msin(theta) == 0.0f) pdf = 0.0f;
+  pdf = (pdf * sh.state.env_map_resolution[0] * sh.state.env_map_resolution[1]) / (TWO_PI * PI * msin(theta));
+  L = f3{-msin(theta) * mcos(phi), mcos(theta), -msin(theta) * msin(phi)};
   L = transformDirection(sh.cam.env_transform, L);
   f3 e = tex4rgb(S.env, S.envW, S.envH, uvx, uvy);
   float k = sh.state.env_map_intensity;
@@ -339,8 +348,8 @@ __device__ __forceinline__ f3 importanceSampleAnisoGGX(f2 u, f3 wo, float ax, fl
   float factor = sqrtf(gmax(0.0f, u.x / gmax(1.0f - u.x, EPS)));
   float phi = TWO_PI * u.y;
   f3 wh{0.0f, 0.0f, 1.0f};
-  wh.x = -ax * factor * cosf(phi);
-  wh.y = -ay * factor * sinf(phi);
+  wh.x = -ax * factor * mcos(phi);
+  wh.y = -ay * factor * msin(phi);
   wh = makeNormal(wh);
   return reflect(-wo, wh);
 }

@@ -106,9 +106,9 @@ __global__ void __launch_bounds__(256) k_raygen(KParams P) {
     }
     // Gaussian filter weight of this sample, rgen:134-145
     const float alpha = -2.0f;
-    const float expXY = expf(alpha * 2.0f * 2.0f);
+    const float expXY = mexp(alpha * 2.0f * 2.0f);
     float ox = jitter.x - 0.5f, oy = jitter.y - 0.5f;
-    float fw = gmax(0.0f, expf(alpha * ox * ox) - expXY) * gmax(0.0f, expf(alpha * oy * oy) - expXY);
+    float fw = gmax(0.0f, mexp(alpha * ox * ox) - expXY) * gmax(0.0f, mexp(alpha * oy * oy) - expXY);
     W.rayO[0][p] = make_float4(ro.x, ro.y, ro.z, INF);
     W.rayD[0][p] = make_float4(rd.x, rd.y, rd.z, __uint_as_float(p));
     W.thp[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);

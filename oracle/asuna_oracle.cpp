@@ -8,6 +8,7 @@
 // -ffp-contract=off so the float instantiation rounds every operation the way
 // the GLSL source spells it.
 #include "asuna_oracle.h"
+#include "../include/asuna_math.h"
 
 #include <algorithm>
 #include <atomic>
@@ -30,6 +31,19 @@ template <class R>
 struct V3 {
   R x, y, z;
 };
+
+// Transcendentals: float uses the shared implementation of
+// include/asuna_math.h (the same bits as the CUDA kernels), double the C library.
+inline float msin(float x) { return asuna_math::sinf_(x); }
+inline float mcos(float x) { return asuna_math::cosf_(x); }
+inline float macos(float x) { return asuna_math::acosf_(x); }
+inline float matan2(float y, float x) { return asuna_math::atan2f_(y, x); }
+inline float mexp(float x) { return asuna_math::expf_(x); }
+inline double msin(double x) { return std::sin(x); }
+inline double mcos(double x) { return std::cos(x); }
+inline double macos(double x) { return std::acos(x); }
+inline double matan2(double y, double x) { return std::atan2(y, x); }
+inline double mexp(double x) { return std::exp(x); }
 
 template <class R> inline V3<R> mk(R a, R b, R c) { return V3<R>{a, b, c}; }
 template <class R> inline V3<R> splat(R a) { return V3<R>{a, a, a}; }
@@ -141,7 +155,7 @@ template <class R> inline V3<R> uniformSampleSphere(V2<R> u) {
   R z = R(1) - R(2) * u.x;
   R r = std::sqrt(gmax(R(0), R(1) - z * z));
   R phi = K<R>::TWO_PI * u.y;
-  return {r * std::cos(phi), r * std::sin(phi), z};
+  return {r * mcos(phi), r * msin(phi), z};
 }
 // math.glsl:148-163
 template <class R> inline V2<R> concentricSampleDisk(V2<R> u) {
@@ -155,7 +169,7 @@ template <class R> inline V2<R> concentricSampleDisk(V2<R> u) {
     r = oy;
     theta = K<R>::PI_OVER_2 - K<R>::PI_OVER_4 * (ox / oy);
   }
-  return V2<R>{r * std::cos(theta), r * std::sin(theta)};
+  return V2<R>{r * mcos(theta), r * msin(theta)};
 }
 // math.glsl:165-174
 template <class R> inline V3<R> cosineSampleHemisphere(V2<R> u) {
@@ -615,13 +629,13 @@ template <class R> inline V3<R> L3(const float* a) { return V3<R>{R(a[0]), R(a[1
 // sample_light.glsl:84-95
 template <class R> R pdfEnvmap(const Scene& s, const asuna_shot& sh, V3<R> L) {
   L = transformDirectionT<R>(sh.camera.env_transform, L);
-  R theta = std::acos(gclamp(L.y, R(-1), R(1)));
-  R u = (K<R>::PI + std::atan2(L.z, L.x)) * K<R>::INV_2PI, v = theta * K<R>::INV_PI;
+  R theta = macos(gclamp(L.y, R(-1), R(1)));
+  R u = (K<R>::PI + matan2(L.z, L.x)) * K<R>::INV_2PI, v = theta * K<R>::INV_PI;
   R c[4], m[4];
   texFetch<R>(s.cond, u, v, c);
   texFetch<R>(s.marg, R(0), v, m);
   R pdf = c[1] * m[1];
-  R sinTheta = std::sin(theta);
+  R sinTheta = msin(theta);
   if (sinTheta == R(0)) return R(0);
   return (pdf * R(sh.state.env_map_resolution[0]) * R(sh.state.env_map_resolution[1])) /
          (K<R>::TWO_PI * K<R>::PI * sinTheta);
@@ -629,8 +643,8 @@ template <class R> R pdfEnvmap(const Scene& s, const asuna_shot& sh, V3<R> L) {
 // sample_light.glsl:97-104
 template <class R> V3<R> evalEnvmap(const Scene& s, const asuna_shot& sh, V3<R> L) {
   L = transformDirectionT<R>(sh.camera.env_transform, L);
-  R theta = std::acos(gclamp(L.y, R(-1), R(1)));
-  R u = (K<R>::PI + std::atan2(L.z, L.x)) * K<R>::INV_2PI, v = theta * K<R>::INV_PI;
+  R theta = macos(gclamp(L.y, R(-1), R(1)));
+  R u = (K<R>::PI + matan2(L.z, L.x)) * K<R>::INV_2PI, v = theta * K<R>::INV_PI;
   R e[4];
   texFetch<R>(s.env, u, v, e);
   R k = R(sh.state.env_map_intensity);
@@ -648,10 +662,10 @@ template <class R> V3<R> sampleEnvmap(const Scene& s, const asuna_shot& sh, V2<R
   pdf = c[1] * m[1];
   R phi = uvx * K<R>::TWO_PI;
   R theta = uvy * K<R>::PI;
-  if (std::sin(theta) == R(0)) pdf = R(0);
+  if (msin(theta) == R(0)) pdf = R(0);
   pdf = (pdf * R(sh.state.env_map_resolution[0]) * R(sh.state.env_map_resolution[1])) /
-        (K<R>::TWO_PI * K<R>::PI * std::sin(theta));
-  L = V3<R>{-std::sin(theta) * std::cos(phi), std::cos(theta), -std::sin(theta) * std::sin(phi)};
+        (K<R>::TWO_PI * K<R>::PI * msin(theta));
+  L = V3<R>{-msin(theta) * mcos(phi), mcos(theta), -msin(theta) * msin(phi)};
   L = transformDirection<R>(sh.camera.env_transform, L);
   R e[4];
   texFetch<R>(s.env, uvx, uvy, e);
@@ -904,8 +918,8 @@ template <class R> V3<R> importanceSampleAnisoGGX(V2<R> u, V3<R> wo, R ax, R ay)
   R factor = std::sqrt(gmax(R(0), u.x / gmax(R(1) - u.x, K<R>::EPS)));
   R phi = K<R>::TWO_PI * u.y;
   V3<R> wh{R(0), R(0), R(1)};
-  wh.x = -ax * factor * std::cos(phi);
-  wh.y = -ay * factor * std::sin(phi);
+  wh.x = -ax * factor * mcos(phi);
+  wh.y = -ay * factor * msin(phi);
   wh = makeNormal(wh);
   return reflect(-wo, wh);
 }
@@ -1241,9 +1255,9 @@ void tracePath(const Scene& s, const asuna_shot& sh, uint32_t x, uint32_t y, uin
   if (p.depth > uint32_t(ps.max_path_depth)) p.depth = ps.max_path_depth;
   // rgen:134-149
   const R alpha = R(-2);
-  const R expXY = std::exp(alpha * R(2) * R(2));
+  const R expXY = mexp(alpha * R(2) * R(2));
   R ox = jitter.x - R(0.5), oy = jitter.y - R(0.5);
-  R fw = gmax(R(0), std::exp(alpha * ox * ox) - expXY) * gmax(R(0), std::exp(alpha * oy * oy) - expXY);
+  R fw = gmax(R(0), mexp(alpha * ox * ox) - expXY) * gmax(R(0), mexp(alpha * oy * oy) - expXY);
   out.rad[0] = float(p.radiance.x);
   out.rad[1] = float(p.radiance.y);
   out.rad[2] = float(p.radiance.z);
@@ -1275,6 +1289,15 @@ extern "C" {
 
 uint32_t oracle_xxhash32(uint32_t x, uint32_t y, uint32_t z) { return xxhash32(x, y, z); }
 void oracle_invert3x4(const float* m, float* out) { invert3x4(m, out); }
+float oracle_math(int which, float x, float y) {
+  switch (which) {
+    case 0: return msin(x);
+    case 1: return mcos(x);
+    case 2: return mexp(x);
+    case 3: return macos(x);
+    default: return matan2(x, y);
+  }
+}
 uint32_t oracle_pcg(uint32_t* state) { return pcg(*state); }
 float oracle_rand(uint32_t* state) { return rnd<float>(*state); }
 

@@ -14,6 +14,8 @@
 #include <cstring>
 #include <type_traits>
 
+#include "../include/asuna_math.h"
+
 namespace glslx {
 
 using uint = unsigned int;
@@ -153,11 +155,13 @@ inline vec3 operator*(const mat4x3& m, vec4 v) {
 inline float abs(float x) { return std::fabs(x); }
 inline int abs(int x) { return x < 0 ? -x : x; }
 inline float sqrt(float x) { return std::sqrt(x); }
-inline float exp(float x) { return std::exp(x); }
-inline float sin(float x) { return std::sin(x); }
-inline float cos(float x) { return std::cos(x); }
-inline float acos(float x) { return std::acos(x); }
-inline float atan(float y, float x) { return std::atan2(y, x); }
+// The driver's transcendentals are implementation-defined in GLSL; the
+// project's shared implementation stands in for them (include/asuna_math.h).
+inline float exp(float x) { return asuna_math::expf_(x); }
+inline float sin(float x) { return asuna_math::sinf_(x); }
+inline float cos(float x) { return asuna_math::cosf_(x); }
+inline float acos(float x) { return asuna_math::acosf_(x); }
+inline float atan(float y, float x) { return asuna_math::atan2f_(y, x); }
 inline float sign(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
 inline bool isnan(float x) { return std::isnan(x); }
 inline bool isinf(float x) { return std::isinf(x); }

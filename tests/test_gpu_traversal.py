@@ -20,7 +20,7 @@ def _random_rays(rng, n, center, radius):
 
 
 def test_closest_hit_matches_oracle(ctx):
-    b, _ = scenes.mixed_scene(8, 8, frames=1, n_spheres=16, level=4, seed=5, env_size=(8, 4))
+    b, _ = scenes.mixed_scene(8, 8, frames=1, n_spheres=16, level=4, seed=5, env_size=(32, 16))
     d = b.desc()
     scene = ctx.create_scene(d)
     o_sc = oracle_py.OracleScene(d)
@@ -42,7 +42,7 @@ def test_closest_hit_matches_oracle(ctx):
 
 
 def test_occlusion_matches_oracle(ctx):
-    b, _ = scenes.mixed_scene(8, 8, frames=1, n_spheres=16, level=3, seed=6, env_size=(8, 4))
+    b, _ = scenes.mixed_scene(8, 8, frames=1, n_spheres=16, level=3, seed=6, env_size=(32, 16))
     d = b.desc()
     scene = ctx.create_scene(d)
     o_sc = oracle_py.OracleScene(d)
