@@ -27,39 +27,7 @@
 
 using namespace asuna;
 
-struct WaveAlloc {
-  void* base = nullptr;
-  uint64_t capacity = 0;
-  WaveDev view{};
-};
-
-struct asuna_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  int numSMs = 0;
-  int traceGrid = 0, shadeGrid = 0, raygenGrid = 0;
-  DevCounters* cnt = nullptr;
-  DevCounters* hostCnt = nullptr;
-  WaveAlloc wave;
-  uint64_t pathBudget = 4ull << 30;
-  int counters = 0;
-  std::vector<cudaEvent_t> events;
-};
-
-struct asuna_scene {
-  int device = 0;
-  std::vector<void*> allocs;
-  SceneDev view{};
-  asuna_scene_stats stats{};
-};
-
-struct asuna_film {
-  int device = 0;
-  uint32_t width = 0, height = 0;
-  float4* rad = nullptr;
-  float4* w = nullptr;
-  float4* ch = nullptr;
-};
+#include "handles.h"
 
 namespace {
 

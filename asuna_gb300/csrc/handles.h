@@ -1,0 +1,43 @@
+// handles.h — the opaque handles of the C ABI (context, scene, film), shared
+// by the translation units that launch the render path.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "dev_types.h"
+
+struct WaveAlloc {
+  void* base = nullptr;
+  uint64_t capacity = 0;
+  asuna::WaveDev view{};
+};
+
+struct asuna_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int numSMs = 0;
+  int traceGrid = 0, shadeGrid = 0, raygenGrid = 0;
+  asuna::DevCounters* cnt = nullptr;
+  asuna::DevCounters* hostCnt = nullptr;
+  WaveAlloc wave;
+  uint64_t pathBudget = 4ull << 30;
+  int counters = 0;
+  std::vector<cudaEvent_t> events;
+};
+
+struct asuna_scene {
+  int device = 0;
+  std::vector<void*> allocs;
+  asuna::SceneDev view{};
+  asuna_scene_stats stats{};
+};
+
+struct asuna_film {
+  int device = 0;
+  uint32_t width = 0, height = 0;
+  float4* rad = nullptr;
+  float4* w = nullptr;
+  float4* ch = nullptr;
+};
+

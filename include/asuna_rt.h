@@ -347,6 +347,21 @@ int asuna_render_paths(asuna_ctx* ctx, const asuna_scene* scene, const asuna_sho
 int asuna_scene_trace(asuna_ctx* ctx, const asuna_scene* scene, const float* rays, uint32_t n, int any_hit,
                       float* hits, uint32_t* inst);
 
+/* ---- allocation-free render ------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory while they render (an owner holds the memory pool or budget, a
+ * fixed footprint was granted up front, or a render thread must stay out of
+ * the allocator): renders shot->frames frames of one shot into `film` like
+ * asuna_render, on `stream` (a cudaStream_t; NULL = default stream), with
+ * all scratch in one fixed device array compiled into the library.  The
+ * array holds ASUNA_NOALLOC_MAX_PATHS path slots (about 49 MiB, kept by
+ * every GPU that loads the library until exit); a frame with more pixels is
+ * rejected with ASUNA_ERR_INVALID.  The array's address is set up on a
+ * device by the first call there: make that call before any stream capture.
+ * Calls share the array; calls that overlap on the GPU race. */
+#define ASUNA_NOALLOC_MAX_PATHS 262144
+int asuna_render_noalloc(const asuna_scene* scene, const asuna_shot* shot, asuna_film* film, void* stream);
+
 /* ---- host side: JSON scene description ---------------------------------- */
 /* Parses an Asuna scene JSON file (Loader::parse, src/loader/loader.cpp:91-144)
  * and assembles the device-ABI arrays the way Scene does (dummy light 0,
