@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(_HERE, "_build", "libasuna_rt.so")
 OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_IO, ERR_PARSE, ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_NO_DEVICE = range(9)
 CAMERA_PERSPECTIVE, CAMERA_OPENCV = 0, 1
 LIGHT_DIRECTIONAL, LIGHT_RECT, LIGHT_TRIANGLE, LIGHT_POINT = 0, 1, 2, 3
-MAT_LAMBERTIAN, MAT_ROUGH_PLASTIC, MAT_DIELECTRIC = 0, 5, 10
+MAT_LAMBERTIAN, MAT_EMISSIVE, MAT_ROUGH_PLASTIC, MAT_DIELECTRIC = 0, 2, 5, 10
 CH_DIFFUSE, CH_NORMAL, CH_SPECULAR, CH_TANGENT, CH_ROUGHNESS, CH_POSITION, CH_UV, CH_DEPTH = range(8)
 SHOT_RR = 1
 NUM_OUTPUT_IMAGES = 9
@@ -148,6 +148,8 @@ SIGNATURES = [
     ("asuna_envmap_tables", C.c_int, [C.c_uint32, C.c_uint32, P, P, P]),
     ("asuna_diffuse_fresnel", C.c_float, [C.c_float, C.c_int]),
     ("asuna_tracer_run_offline", C.c_int, [P, C.c_char_p, C.c_char_p]),
+    ("asuna_image_write", C.c_int, [C.c_char_p, C.c_uint32, C.c_uint32, P]),
+    ("asuna_image_read", C.c_int, [C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), P, C.c_uint64]),
 ]
 
 

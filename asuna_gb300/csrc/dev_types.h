@@ -59,7 +59,8 @@ struct __align__(16) InstDev {
 };
 static_assert(sizeof(InstDev) == 128, "InstDev is 128 bytes");
 
-// Packed material, 32 B: (diffuse.xyz, type bits), (alpha.x, alpha.y, ior, fdrInt).
+// Packed material, 32 B: (diffuse.xyz, type bits), (alpha.x, alpha.y, ior, fdrInt);
+// an emissive material holds its radiance in place of the diffuse albedo.
 struct __align__(16) MatDev {
   float4 a;
   float4 b;

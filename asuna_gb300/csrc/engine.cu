@@ -341,7 +341,9 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
     const asuna_material& m = d->materials[i];
     float tb;
     std::memcpy(&tb, &m.type, 4);
-    mats[i].a = make_float4(m.diffuse[0], m.diffuse[1], m.diffuse[2], tb);
+    // emissive materials carry their radiance where the others carry the albedo
+    const float* rgb = m.type == ASUNA_MAT_EMISSIVE ? m.radiance : m.diffuse;
+    mats[i].a = make_float4(rgb[0], rgb[1], rgb[2], tb);
     mats[i].b = make_float4(m.aniso_alpha[0], m.aniso_alpha[1], m.ior, m.radiance[0]);
   }
   std::vector<LightDev> lights(std::max(1u, d->num_lights));

@@ -60,10 +60,12 @@ int validateSceneDesc(const asuna_scene_desc* d) {
   }
   for (uint32_t i = 0; i < d->num_materials; ++i) {
     uint32_t t = d->materials[i].type;
-    if (t != ASUNA_MAT_LAMBERTIAN && t != ASUNA_MAT_ROUGH_PLASTIC && t != ASUNA_MAT_DIELECTRIC)
+    if (t != ASUNA_MAT_LAMBERTIAN && t != ASUNA_MAT_ROUGH_PLASTIC && t != ASUNA_MAT_DIELECTRIC &&
+        t != ASUNA_MAT_EMISSIVE)
       return fail(ASUNA_ERR_UNSUPPORTED, "material %u: type %u is not implemented", i, t);
     const asuna_material& m = d->materials[i];
-    if (m.diffuse_texture_id >= 0 || m.normal_texture_id >= 0 || m.roughness_texture_id >= 0)
+    if (m.diffuse_texture_id >= 0 || m.normal_texture_id >= 0 || m.roughness_texture_id >= 0 ||
+        (t == ASUNA_MAT_EMISSIVE && m.radiance_texture_id >= 0))
       return fail(ASUNA_ERR_UNSUPPORTED, "material %u: textures are not implemented", i);
   }
   for (uint32_t i = 0; i < d->num_instances; ++i) {
@@ -628,6 +630,157 @@ int writePfm(const std::string& path, uint32_t w, uint32_t h, const float* rgba)
   return f ? ASUNA_OK : fail(ASUNA_ERR_IO, "write failed: %s", path.c_str());
 }
 
+// OpenEXR (scanline, no compression, FLOAT R,G,B,A): the layout of the
+// public OpenEXR file-format description (magic, attribute header, offset
+// table, one chunk per scanline with channels in alphabetical order).
+int writeExr(const std::string& path, uint32_t w, uint32_t h, const float* rgba) {
+  std::string hdr;
+  auto u8 = [&](uint8_t v) { hdr.push_back(char(v)); };
+  auto i32 = [&](int32_t v) {
+    for (int k = 0; k < 4; ++k) u8(uint8_t(uint32_t(v) >> (8 * k)));
+  };
+  auto f32 = [&](float v) {
+    uint32_t b;
+    std::memcpy(&b, &v, 4);
+    i32(int32_t(b));
+  };
+  auto str = [&](const char* s) { hdr.append(s, std::strlen(s) + 1); };
+  auto attr = [&](const char* name, const char* type, int32_t size) {
+    str(name);
+    str(type);
+    i32(size);
+  };
+  i32(20000630);  // magic
+  i32(2);         // version 2, single-part scanline
+  attr("channels", "chlist", 4 * 18 + 1);
+  for (const char* c : {"A", "B", "G", "R"}) {
+    str(c);
+    i32(2);  // FLOAT
+    u8(0);
+    u8(0);
+    u8(0);
+    u8(0);
+    i32(1);
+    i32(1);
+  }
+  u8(0);
+  attr("compression", "compression", 1);
+  u8(0);
+  attr("dataWindow", "box2i", 16);
+  i32(0);
+  i32(0);
+  i32(int32_t(w) - 1);
+  i32(int32_t(h) - 1);
+  attr("displayWindow", "box2i", 16);
+  i32(0);
+  i32(0);
+  i32(int32_t(w) - 1);
+  i32(int32_t(h) - 1);
+  attr("lineOrder", "lineOrder", 1);
+  u8(0);
+  attr("pixelAspectRatio", "float", 4);
+  f32(1.0f);
+  attr("screenWindowCenter", "v2f", 8);
+  f32(0.0f);
+  f32(0.0f);
+  attr("screenWindowWidth", "float", 4);
+  f32(1.0f);
+  u8(0);  // end of header
+  std::ofstream f(path, std::ios::binary);
+  if (!f) return fail(ASUNA_ERR_IO, "cannot write %s", path.c_str());
+  f.write(hdr.data(), std::streamsize(hdr.size()));
+  const uint64_t lineBytes = 8 + uint64_t(w) * 4 * 4;
+  const uint64_t first = hdr.size() + uint64_t(h) * 8;
+  for (uint32_t y = 0; y < h; ++y) {
+    uint64_t off = first + y * lineBytes;
+    f.write(reinterpret_cast<const char*>(&off), 8);  // little-endian hosts
+  }
+  std::vector<float> line(size_t(w) * 4);
+  for (uint32_t y = 0; y < h; ++y) {
+    int32_t hy[2] = {int32_t(y), int32_t(w * 16)};
+    f.write(reinterpret_cast<const char*>(hy), 8);
+    const float* src = rgba + size_t(y) * w * 4;
+    for (uint32_t x = 0; x < w; ++x) {
+      line[x] = src[x * 4 + 3];
+      line[w + x] = src[x * 4 + 2];
+      line[2 * size_t(w) + x] = src[x * 4 + 1];
+      line[3 * size_t(w) + x] = src[x * 4 + 0];
+    }
+    f.write(reinterpret_cast<const char*>(line.data()), std::streamsize(line.size() * 4));
+  }
+  return f ? ASUNA_OK : fail(ASUNA_ERR_IO, "write failed: %s", path.c_str());
+}
+
+// PNG, 8-bit RGBA, clamp(v, 0, 1) * 255 with gamma 1 (the reference writes LDR
+// channels through stbi with stbi_hdr_to_ldr_gamma(1.0)); zlib stream of
+// stored (uncompressed) deflate blocks, as the PNG and zlib specifications allow.
+int writePng(const std::string& path, uint32_t w, uint32_t h, const float* rgba) {
+  auto crcTable = [] {
+    std::vector<uint32_t> t(256);
+    for (uint32_t n = 0; n < 256; ++n) {
+      uint32_t c = n;
+      for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+      t[n] = c;
+    }
+    return t;
+  }();
+  auto crc = [&](const std::string& d) {
+    uint32_t c = 0xFFFFFFFFu;
+    for (unsigned char b : d) c = crcTable[(c ^ b) & 0xFF] ^ (c >> 8);
+    return c ^ 0xFFFFFFFFu;
+  };
+  auto be32 = [](std::string& o, uint32_t v) {
+    for (int k = 3; k >= 0; --k) o.push_back(char((v >> (8 * k)) & 0xFF));
+  };
+  std::string raw;
+  raw.reserve(size_t(h) * (1 + size_t(w) * 4));
+  for (uint32_t y = 0; y < h; ++y) {
+    raw.push_back(0);  // filter: none
+    for (uint32_t x = 0; x < w * 4; ++x) {
+      float v = rgba[size_t(y) * w * 4 + x];
+      v = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
+      raw.push_back(char(uint8_t(v * 255.0f + 0.5f)));
+    }
+  }
+  std::string z;
+  z.push_back(char(0x78));
+  z.push_back(char(0x01));
+  uint32_t a = 1, b = 0;
+  for (size_t p = 0; p < raw.size() || p == 0; p += 65535) {
+    size_t n = std::min<size_t>(65535, raw.size() - p);
+    z.push_back(char(p + n >= raw.size() ? 1 : 0));
+    z.push_back(char(n & 0xFF));
+    z.push_back(char(n >> 8));
+    z.push_back(char(~n & 0xFF));
+    z.push_back(char((~n >> 8) & 0xFF));
+    z.append(raw, p, n);
+    if (n == 0) break;
+  }
+  for (unsigned char c : raw) {
+    a = (a + c) % 65521u;
+    b = (b + a) % 65521u;
+  }
+  be32(z, (b << 16) | a);
+  std::string png("\x89PNG\r\n\x1a\n", 8);
+  auto chunk = [&](const char* type, const std::string& data) {
+    be32(png, uint32_t(data.size()));
+    std::string td = std::string(type, 4) + data;
+    png += td;
+    be32(png, crc(td));
+  };
+  std::string ihdr;
+  be32(ihdr, w);
+  be32(ihdr, h);
+  ihdr += std::string("\x08\x06\x00\x00\x00", 5);
+  chunk("IHDR", ihdr);
+  chunk("IDAT", z);
+  chunk("IEND", std::string());
+  std::ofstream f(path, std::ios::binary);
+  if (!f) return fail(ASUNA_ERR_IO, "cannot write %s", path.c_str());
+  f.write(png.data(), std::streamsize(png.size()));
+  return f ? ASUNA_OK : fail(ASUNA_ERR_IO, "write failed: %s", path.c_str());
+}
+
 // ---- scene-file loader ------------------------------------------------------------------
 namespace {
 
@@ -809,8 +962,14 @@ int addMaterial(LoadCtx& L, const Json& mj) {
     if (mj.has("alpha")) REQUIRE(vecN(mj["alpha"], 2, m.aniso_alpha), "bad alpha");
     if ((rc = tex("alpha_texture", m.roughness_texture_id))) return rc;
     m.radiance[0] = asuna_diffuse_fresnel(m.ior, 1000);
+  } else if (t == "brdf_emissive") {
+    // src/loader/material.cpp:145-155
+    m.type = ASUNA_MAT_EMISSIVE;
+    if (mj.has("radiance")) REQUIRE(vecN(mj["radiance"], 3, m.radiance), "bad radiance");
+    if (mj.has("radiance_factor")) REQUIRE(vecN(mj["radiance_factor"], 3, m.radiance_factor), "bad radiance_factor");
+    if ((rc = tex("radiance_texture", m.radiance_texture_id))) return rc;
   } else {
-    static const char* known[] = {"brdf_pbr_metalness_roughness", "brdf_emissive", "brdf_kang18", "brdf_plastic",
+    static const char* known[] = {"brdf_pbr_metalness_roughness", "brdf_kang18", "brdf_plastic",
                                   "brdf_mirror", "brdf_conductor", "brdf_rough_conductor", "brdf_disney", "brdf_phong"};
     for (const char* k : known)
       if (t == k) return fail(ASUNA_ERR_UNSUPPORTED, "material type [%s] is not implemented", t.c_str());
@@ -1130,6 +1289,31 @@ float asuna_diffuse_fresnel(float ior, int sampleCount) {
   return float(diffuseFresnel);
 }
 
+int asuna_image_write(const char* path, uint32_t width, uint32_t height, const float* rgba) {
+  clearError();
+  if (!path || !rgba || !width || !height) return fail(ASUNA_ERR_INVALID, "asuna_image_write: bad argument");
+  std::string p(path);
+  std::string ext = p.substr(p.find_last_of('.') + 1);
+  if (ext == "exr") return writeExr(p, width, height, rgba);
+  if (ext == "png") return writePng(p, width, height, rgba);
+  if (ext == "pfm") return writePfm(p, width, height, rgba);
+  return fail(ASUNA_ERR_UNSUPPORTED, "asuna_image_write: .%s (use .exr, .png or .pfm)", ext.c_str());
+}
+
+int asuna_image_read(const char* path, uint32_t* width, uint32_t* height, float* rgba, uint64_t capacity) {
+  clearError();
+  if (!path || !width || !height) return fail(ASUNA_ERR_INVALID, "asuna_image_read: bad argument");
+  std::vector<float> px;
+  int rc = loadImageRGBA(path, *width, *height, px);
+  if (rc) return rc;
+  if (rgba) {
+    if (capacity < px.size()) return fail(ASUNA_ERR_INVALID, "asuna_image_read: buffer holds %llu of %zu floats",
+                                          (unsigned long long)capacity, px.size());
+    std::memcpy(rgba, px.data(), px.size() * sizeof(float));
+  }
+  return ASUNA_OK;
+}
+
 int asuna_json_load_string(const char* text, const char* base_dir, asuna_json_scene** out) {
   clearError();
   if (!text || !out) return fail(ASUNA_ERR_INVALID, "null argument");
@@ -1187,7 +1371,11 @@ int asuna_json_channels(const asuna_json_scene* js, uint32_t* n, int32_t* kinds)
 }
 
 // Tracer::runOffline + callSavingImage (src/tracer/tracer.cpp:177-291): every
-// shot rendered for its spp frames, radiance and AOVs written as PFM.
+// shot rendered for its spp frames; radiance written as <prefix>_shot_%04d.exr,
+// AOV channel c as <prefix>_shot_%04d_channel_%04d.exr (or .png where the
+// scene's multi_channel_ldr asks for it).  The reference's LDR radiance output
+// goes through its tonemapping post pass, which is outside this path, so the
+// radiance is always written as HDR.
 int asuna_tracer_run_offline(asuna_ctx* ctx, const char* scene_json, const char* out_prefix) {
   clearError();
   if (!ctx || !scene_json || !out_prefix) return fail(ASUNA_ERR_INVALID, "null argument");
@@ -1211,15 +1399,17 @@ int asuna_tracer_run_offline(asuna_ctx* ctx, const char* scene_json, const char*
     if ((rc = asuna_render(ctx, scene, &shot, film, nullptr))) return rc;
     if (!S.state.outputRenderResult) continue;
     char name[64];
-    std::snprintf(name, sizeof(name), "_shot_%04u.pfm", i);
-    if ((rc = asuna_film_read(ctx, film, 0, px.data())) || (rc = writePfm(out_prefix + std::string(name), S.width,
+    std::snprintf(name, sizeof(name), "_shot_%04u.exr", i);
+    if ((rc = asuna_film_read(ctx, film, 0, px.data())) || (rc = writeExr(out_prefix + std::string(name), S.width,
                                                                           S.height, px.data())))
       return rc;
     for (uint32_t c = 0; c < S.state.rtx.n_multi_channel; ++c) {
-      std::snprintf(name, sizeof(name), "_shot_%04u_channel_%04u.pfm", i, c);
-      if ((rc = asuna_film_read(ctx, film, int(c + 1), px.data())) ||
-          (rc = writePfm(out_prefix + std::string(name), S.width, S.height, px.data())))
-        return rc;
+      const bool ldr = c < S.state.channelLdr.size() && S.state.channelLdr[c];
+      std::snprintf(name, sizeof(name), "_shot_%04u_channel_%04u.%s", i, c, ldr ? "png" : "exr");
+      if ((rc = asuna_film_read(ctx, film, int(c + 1), px.data()))) return rc;
+      rc = ldr ? writePng(out_prefix + std::string(name), S.width, S.height, px.data())
+               : writeExr(out_prefix + std::string(name), S.width, S.height, px.data());
+      if (rc) return rc;
     }
   }
   return ASUNA_OK;

@@ -70,6 +70,8 @@ struct HostScene {
 int loadObj(const std::string& path, std::vector<asuna_vertex>& v, std::vector<uint32_t>& idx);
 int loadImageRGBA(const std::string& path, uint32_t& w, uint32_t& h, std::vector<float>& rgba);
 int writePfm(const std::string& path, uint32_t w, uint32_t h, const float* rgba);
+int writeExr(const std::string& path, uint32_t w, uint32_t h, const float* rgba);
+int writePng(const std::string& path, uint32_t w, uint32_t h, const float* rgba);
 
 // Scene-file loader (src/loader/loader.cpp:67-468, src/loader/material.cpp).
 int loadSceneJson(const std::string& text, const std::string& baseDir, HostScene& scene);

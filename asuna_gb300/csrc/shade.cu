@@ -12,7 +12,8 @@
 //   raygen      raytrace.projective.rgen:26-100 (seed, jitter, cameras)
 //   shade/miss  raytrace.default.rmiss:24-56
 //   shade/hit   rchit_layouts.glsl:61-167, brdf_lambertian.rchit:12-151,
-//               brdf_rough_plastic.rchit:191-269, bsdf_dielectric.rchit:74-139
+//               brdf_rough_plastic.rchit:191-269, bsdf_dielectric.rchit:74-139,
+//               brdf_emissive.rchit:12-27
 //   accumulate  raytrace.projective.rgen:134-179
 //
 // Compiled with -fmad=false: the float arithmetic rounds operation by
@@ -399,7 +400,7 @@ __device__ __forceinline__ void shadeDielectric(const SceneDev& S, const ShotDev
 }  // namespace
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_shade(KParams P) {
+__global__ void __launch_bounds__(256, kShadeMinBlocks) k_shade(KParams P) {
   const WaveDev& W = P.W;
   const SceneDev& S = P.S;
   const int cur = P.cur, nxt = cur ^ 1;
@@ -492,7 +493,11 @@ __global__ void __launch_bounds__(256) k_shade(KParams P) {
             put(ps.position_out_channel, st.pos);
             put(ps.uv_out_channel, f3{st.u, st.v, 1.0f});
           }
-          if (type == ASUNA_MAT_ROUGH_PLASTIC)
+          if (type == ASUNA_MAT_EMISSIVE) {
+            // brdf_emissive.rchit:12-27: add the emitted radiance and stop
+            io.stop = true;
+            if (sh.state.ignore_emissive == 0u) io.rad = io.rad + ld3(m.a) * io.thp;
+          } else if (type == ASUNA_MAT_ROUGH_PLASTIC)
             shadeRoughPlastic(S, sh, io, st, m, rd);
           else if (type == ASUNA_MAT_DIELECTRIC)
             shadeDielectric(S, sh, io, st, m, rd);

@@ -105,118 +105,151 @@ struct HitOut {
   uint32_t prim, inst;
 };
 
-// Returns true on hit (closest hit fills `h`; any-hit returns at the first).
-template <bool ANY, bool COUNT>
-__device__ __forceinline__ bool traverse(const SceneDev& S, float3 wo, float3 wd, float tmin, float tmax,
-                                         int32_t* stack, HitOut& h, uint32_t& nNodes, uint32_t& nTris,
-                                         bool& overflow) {
-  float3 o = wo, d = wd, id = safeInv(wd);
+// Traversal state of one ray.  step() walks the two-level BVH until it has
+// tested the triangles of one BLAS leaf or the traversal is over, so a warp
+// can hand finished lanes new rays between steps.
+struct Trav {
+  float3 wo, wd;  // world-space ray
+  float3 o, d, id;  // ray in the current space (world or instance object space)
   WT wt;
-  bool inBlas = false, found = false;
-  uint32_t curInst = 0;
-  float best = tmax;
-  int sp = 0;
-  int32_t ref = S.tlasRoot;
-  for (;;) {
-    if (ref >= 0) {
-      const BvhNode* n = S.nodes + ref;
-      const float4 xs = __ldg(&n->xs), ys = __ldg(&n->ys), zs = __ldg(&n->zs);
-      const int4 rr = __ldg(&n->ref);
-      if (COUNT) ++nNodes;
-      const float tx0 = (xs.x - o.x) * id.x, tx1 = (xs.y - o.x) * id.x;
-      const float ty0 = (ys.x - o.y) * id.y, ty1 = (ys.y - o.y) * id.y;
-      const float tz0 = (zs.x - o.z) * id.z, tz1 = (zs.y - o.z) * id.z;
-      const float ux0 = (xs.z - o.x) * id.x, ux1 = (xs.w - o.x) * id.x;
-      const float uy0 = (ys.z - o.y) * id.y, uy1 = (ys.w - o.y) * id.y;
-      const float uz0 = (zs.z - o.z) * id.z, uz1 = (zs.w - o.z) * id.z;
-      const float lim = best;
-      const float a0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-      const float a1 = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), lim)) * kFarScale;
-      const float b0 = fmaxf(fmaxf(fminf(ux0, ux1), fminf(uy0, uy1)), fmaxf(fminf(uz0, uz1), tmin));
-      const float b1 = fminf(fminf(fmaxf(ux0, ux1), fmaxf(uy0, uy1)), fminf(fmaxf(uz0, uz1), lim)) * kFarScale;
-      const bool h0 = a0 <= a1, h1 = b0 <= b1;
-      if (h0 && h1) {
-        int32_t nearRef = rr.x, farRef = rr.y;
-        if (b0 < a0) {
-          nearRef = rr.y;
-          farRef = rr.x;
+  float tmin, best;
+  uint32_t curInst;
+  int sp;
+  int32_t ref;
+  bool found, inBlas;
+  HitOut h;
+
+  __device__ __forceinline__ void init(const SceneDev& S, float3 ro, float3 rd, float t0, float t1) {
+    wo = ro;
+    wd = rd;
+    o = ro;
+    d = rd;
+    id = safeInv(rd);
+    tmin = t0;
+    best = t1;
+    curInst = 0;
+    sp = 0;
+    ref = S.tlasRoot;
+    found = false;
+    inBlas = false;
+  }
+
+  // Stack: the first kSharedStack entries in shared memory (stride
+  // kTraceThreads: bank-conflict free), deeper ones in thread-local memory.
+  __device__ __forceinline__ void push(int32_t* sh, int32_t* loc, int32_t v, bool& ovf) {
+    if (sp < kSharedStack)
+      sh[sp * kTraceThreads] = v;
+    else if (sp < kStackDepth)
+      loc[sp - kSharedStack] = v;
+    else {
+      ovf = true;
+      return;
+    }
+    ++sp;
+  }
+  __device__ __forceinline__ int32_t pop(const int32_t* sh, const int32_t* loc) {
+    --sp;
+    return sp < kSharedStack ? sh[sp * kTraceThreads] : loc[sp - kSharedStack];
+  }
+
+  // Returns true when the traversal is finished.
+  template <bool ANY, bool COUNT>
+  __device__ __forceinline__ bool step(const SceneDev& S, int32_t* sh, int32_t* loc, uint32_t& nNodes,
+                                       uint32_t& nTris, bool& ovf) {
+    for (;;) {
+      if (ref >= 0) {
+        const BvhNode* n = S.nodes + ref;
+        const float4 xs = __ldg(&n->xs), ys = __ldg(&n->ys), zs = __ldg(&n->zs);
+        const int4 rr = __ldg(&n->ref);
+        if (COUNT) ++nNodes;
+        const float tx0 = (xs.x - o.x) * id.x, tx1 = (xs.y - o.x) * id.x;
+        const float ty0 = (ys.x - o.y) * id.y, ty1 = (ys.y - o.y) * id.y;
+        const float tz0 = (zs.x - o.z) * id.z, tz1 = (zs.y - o.z) * id.z;
+        const float ux0 = (xs.z - o.x) * id.x, ux1 = (xs.w - o.x) * id.x;
+        const float uy0 = (ys.z - o.y) * id.y, uy1 = (ys.w - o.y) * id.y;
+        const float uz0 = (zs.z - o.z) * id.z, uz1 = (zs.w - o.z) * id.z;
+        const float a0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+        const float a1 = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), best)) * kFarScale;
+        const float b0 = fmaxf(fmaxf(fminf(ux0, ux1), fminf(uy0, uy1)), fmaxf(fminf(uz0, uz1), tmin));
+        const float b1 = fminf(fminf(fmaxf(ux0, ux1), fmaxf(uy0, uy1)), fminf(fmaxf(uz0, uz1), best)) * kFarScale;
+        const bool h0 = a0 <= a1, h1 = b0 <= b1;
+        if (h0 && h1) {
+          const bool swap = b0 < a0;
+          push(sh, loc, swap ? rr.x : rr.y, ovf);
+          ref = swap ? rr.y : rr.x;
+          continue;
         }
-        if (sp < kStackDepth) {
-          stack[sp * kTraceThreads] = farRef;
-          ++sp;
-        } else {
-          overflow = true;
+        if (h0 || h1) {
+          ref = h0 ? rr.x : rr.y;
+          continue;
         }
-        ref = nearRef;
-        continue;
-      } else if (h0) {
-        ref = rr.x;
-        continue;
-      } else if (h1) {
-        ref = rr.y;
-        continue;
-      }
-    } else if (ref != kStackSentinel) {
-      if (!inBlas) {
-        // TLAS leaf: enter the instance's BLAS in object space
-        curInst = leafFirst(ref);
-        const InstDev* in = S.inst + curInst;
-        const int32_t root = __ldg(&in->blasRoot);
-        if (root >= 0) {
-          xformRay(in->w2o, wo, wd, o, d);
-          id = safeInv(d);
-          wt = wtPre(d);
-          if (sp < kStackDepth) {
+      } else if (ref != kStackSentinel) {
+        if (!inBlas) {
+          // TLAS leaf: enter the instance's BLAS in object space
+          curInst = leafFirst(ref);
+          const InstDev* in = S.inst + curInst;
+          const int32_t root = __ldg(&in->blasRoot);
+          if (root >= 0 && sp < kStackDepth) {
+            xformRay(in->w2o, wo, wd, o, d);
+            id = safeInv(d);
+            wt = wtPre(d);
             inBlas = true;
-            stack[sp * kTraceThreads] = kStackSentinel;
-            ++sp;
+            push(sh, loc, kStackSentinel, ovf);
             ref = root;
             continue;
           }
-          overflow = true;
-        }
-      } else {
-        const uint32_t first = leafFirst(ref), cnt = leafCount(ref);
-        for (uint32_t k = 0; k < cnt; ++k) {
-          const TriDev* tr = S.tris + first + k;
-          const float4 p0 = __ldg(&tr->v0), p1 = __ldg(&tr->v1), p2 = __ldg(&tr->v2);
-          if (COUNT) ++nTris;
-          float t, b1, b2;
-          if (wtTri(wt, o, p0, p1, p2, tmin, best, t, b1, b2)) {
-            if (ANY) return true;
-            const uint32_t prim = __float_as_uint(p0.w);
-            // exact ties resolve to the lowest (instance, primitive), so the
-            // result does not depend on traversal order
-            if (!found || t < best || (curInst < h.inst || (curInst == h.inst && prim < h.prim))) {
-              found = true;
-              best = t;
-              h.t = t;
-              h.u = b1;
-              h.v = b2;
-              h.prim = prim;
-              h.inst = curInst;
+          if (root >= 0) ovf = true;
+        } else {
+          const uint32_t first = leafFirst(ref), cnt = leafCount(ref);
+          for (uint32_t k = 0; k < cnt; ++k) {
+            const TriDev* tr = S.tris + first + k;
+            const float4 p0 = __ldg(&tr->v0), p1 = __ldg(&tr->v1), p2 = __ldg(&tr->v2);
+            if (COUNT) ++nTris;
+            float t, b1, b2;
+            if (wtTri(wt, o, p0, p1, p2, tmin, best, t, b1, b2)) {
+              if (ANY) {
+                found = true;
+                return true;
+              }
+              const uint32_t prim = __float_as_uint(p0.w);
+              // exact ties resolve to the lowest (instance, primitive), so
+              // the result does not depend on traversal order
+              if (!found || t < best || (curInst < h.inst || (curInst == h.inst && prim < h.prim))) {
+                found = true;
+                best = t;
+                h.t = t;
+                h.u = b1;
+                h.v = b2;
+                h.prim = prim;
+                h.inst = curInst;
+              }
             }
           }
+          if (sp == 0) return true;
+          ref = pop(sh, loc);
+          return false;  // a leaf was processed: let the warp refill idle lanes
         }
+      } else {
+        // leaving a BLAS: back to the world-space ray
+        inBlas = false;
+        o = wo;
+        d = wd;
+        id = safeInv(wd);
       }
-    } else {
-      // leaving a BLAS: back to the world-space ray
-      inBlas = false;
-      o = wo;
-      d = wd;
-      id = safeInv(wd);
+      if (sp == 0) return true;
+      ref = pop(sh, loc);
     }
-    if (sp == 0) break;
-    --sp;
-    ref = stack[sp * kTraceThreads];
   }
-  return found;
-}
+};
 
+// Persistent warps over a ray queue.  Lanes whose ray is finished take the
+// next rays of the queue (one atomic per refill, per warp) while the other
+// lanes keep traversing.
 template <bool ANY, bool COUNT>
-__global__ void __launch_bounds__(kTraceThreads) k_trace(KParams P) {
-  __shared__ int32_t sstack[kStackDepth * kTraceThreads];
-  int32_t* stack = sstack + threadIdx.x;
+__global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_trace(KParams P) {
+  __shared__ int32_t sstack[kSharedStack * kTraceThreads];
+  int32_t lstack[kStackDepth - kSharedStack];
+  int32_t* sh = sstack + threadIdx.x;
   const WaveDev& W = P.W;
   const SceneDev& S = P.S;
   const int cur = P.cur;
@@ -236,24 +269,44 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(KParams P) {
   const float4* rO = ANY ? W.shO : W.rayO[cur];
   const float4* rD = ANY ? W.shD : W.rayD[cur];
   const unsigned lane = threadIdx.x & 31u;
+  const unsigned lanesBelow = (1u << lane) - 1u;
   uint32_t nNodes = 0, nTris = 0;
-  bool overflow = false;
+  bool ovf = false;
+  bool active = false, drained = false;
+  uint32_t idx = 0;
+  Trav tr;
   for (;;) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(fetch, 32u);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= count) break;
-    const uint32_t i = base + lane;
-    if (i < count) {
-      const float4 o4 = __ldg(&rO[i]);
-      const float4 d4 = __ldg(&rD[i]);
-      HitOut h;
+    const unsigned idle = __ballot_sync(0xffffffffu, !active);
+    if (idle && !drained && (__popc(idle) >= kRefillLanes || idle == 0xffffffffu)) {
+      const int leader = __ffs(idle) - 1;
+      uint32_t base = 0;
+      if (int(lane) == leader) base = atomicAdd(fetch, uint32_t(__popc(idle)));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      drained = base + uint32_t(__popc(idle)) >= count;
+      if (!active) {
+        const uint32_t r = base + uint32_t(__popc(idle & lanesBelow));
+        if (r < count) {
+          idx = r;
+          active = true;
+          const float4 o4 = __ldg(&rO[r]);
+          const float4 d4 = __ldg(&rD[r]);
+          if (ANY)
+            tr.init(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), 0.0f, o4.w);
+          else
+            tr.init(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), 0.00001f, 10000000000.0f);
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, active)) {
+      if (drained) break;
+      continue;
+    }
+    if (active && tr.template step<ANY, COUNT>(S, sh, lstack, nNodes, nTris, ovf)) {
+      active = false;
       if (ANY) {
-        const bool occ = traverse<true, COUNT>(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), 0.0f,
-                                               o4.w, stack, h, nNodes, nTris, overflow);
-        if (!occ) {
-          const uint32_t p = __float_as_uint(d4.w);
-          const float4 c = __ldg(&W.shC[i]);
+        if (!tr.found) {
+          const uint32_t p = __float_as_uint(__ldg(&rD[idx].w));
+          const float4 c = __ldg(&W.shC[idx]);
           float4 r = W.rad[p];
           r.x = r.x + c.x;
           r.y = r.y + c.y;
@@ -261,20 +314,16 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(KParams P) {
           W.rad[p] = r;
           if (P.records) W.rec[p].y |= 1u << (P.depth - 1u);
         }
+      } else if (tr.found) {
+        W.hit[idx] = make_float4(tr.h.t, tr.h.u, tr.h.v, __uint_as_float(tr.h.prim));
+        W.hitInst[idx] = tr.h.inst;
       } else {
-        const bool hit = traverse<false, COUNT>(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z),
-                                                0.00001f, 10000000000.0f, stack, h, nNodes, nTris, overflow);
-        if (hit) {
-          W.hit[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
-          W.hitInst[i] = h.inst;
-        } else {
-          W.hit[i] = make_float4(-1.0f, 0.0f, 0.0f, 0.0f);
-          W.hitInst[i] = 0xffffffffu;
-        }
+        W.hit[idx] = make_float4(-1.0f, 0.0f, 0.0f, 0.0f);
+        W.hitInst[idx] = 0xffffffffu;
       }
     }
   }
-  if (overflow) atomicAdd(&W.cnt->stackOverflow, 1ull);
+  if (ovf) atomicAdd(&W.cnt->stackOverflow, 1ull);
   if (COUNT) {
     unsigned long long a = nNodes, b = nTris;
     for (int off = 16; off; off >>= 1) {
@@ -290,22 +339,26 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(KParams P) {
 
 __global__ void __launch_bounds__(kTraceThreads) k_query(SceneDev S, const float4* o, const float4* d, uint32_t n,
                                                          int anyHit, float4* hit, uint32_t* inst) {
-  __shared__ int32_t sstack[kStackDepth * kTraceThreads];
-  int32_t* stack = sstack + threadIdx.x;
+  __shared__ int32_t sstack[kSharedStack * kTraceThreads];
+  int32_t lstack[kStackDepth - kSharedStack];
+  int32_t* sh = sstack + threadIdx.x;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float4 o4 = o[i], d4 = d[i];
-    HitOut h;
+    Trav tr;
+    tr.init(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), o4.w, d4.w);
     uint32_t a = 0, b = 0;
-    bool r, ovf = false;
-    if (anyHit)
-      r = traverse<true, false>(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), o4.w, d4.w, stack,
-                                h, a, b, ovf);
-    else
-      r = traverse<false, false>(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), o4.w, d4.w, stack,
-                                 h, a, b, ovf);
-    if (r) {
-      hit[i] = anyHit ? make_float4(1.0f, 0.0f, 0.0f, 0.0f) : make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
-      inst[i] = anyHit ? 0u : h.inst;
+    bool ovf = false;
+    if (anyHit) {
+      while (!tr.template step<true, false>(S, sh, lstack, a, b, ovf)) {
+      }
+    } else {
+      while (!tr.template step<false, false>(S, sh, lstack, a, b, ovf)) {
+      }
+    }
+    if (tr.found) {
+      hit[i] = anyHit ? make_float4(1.0f, 0.0f, 0.0f, 0.0f)
+                      : make_float4(tr.h.t, tr.h.u, tr.h.v, __uint_as_float(tr.h.prim));
+      inst[i] = anyHit ? 0u : tr.h.inst;
     } else {
       hit[i] = make_float4(-1.0f, 0.0f, 0.0f, 0.0f);
       inst[i] = 0xffffffffu;

@@ -110,6 +110,13 @@ class SceneBuilder:
         m.ior = ior
         return self._add_material(name, m)
 
+    def add_emissive(self, name, radiance, radiance_factor=(1.0, 1.0, 1.0)):
+        m = default_material()
+        m.type = A.MAT_EMISSIVE
+        m.radiance = A.f3(*radiance)
+        m.radiance_factor = A.f3(*radiance_factor)
+        return self._add_material(name, m)
+
     def _add_material(self, name, m):
         if name in self.material_names:
             raise ValueError(f"material [{name}] defined twice")

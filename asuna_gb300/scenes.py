@@ -240,6 +240,10 @@ def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=Fa
     lam = b.add_lambertian("lam", (0.8, 0.3, 0.2))
     rp = b.add_rough_plastic("plastic", (0.2, 0.4, 0.8), (0.2, 0.5), 1.5)
     di = b.add_dielectric("glass", 1.5)
+    em = b.add_emissive("lamp", (3.0, 1.5, 0.5))
+    v, i = cuboid_mesh(0.15, 0.15, 0.15)
+    b.add_mesh("lamp", v, i)
+    b.add_instance("lamp", em, rot_y(30.0, (0.6, -0.85, 1.2)))
     v, i = _quad(np.array((-4, -1, 4), np.float32), np.array((4, -1, 4), np.float32),
                  np.array((4, -1, -4), np.float32), np.array((-4, -1, -4), np.float32),
                  np.array((0, 1, 0), np.float32))

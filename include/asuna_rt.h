@@ -65,12 +65,12 @@ enum {
   ASUNA_LIGHT_POINT = 3,
   ASUNA_LIGHT_UNDEFINED = 4
 };
-/* MaterialType, src/shared/material.h:7-21 (only the three marked (*) are
+/* MaterialType, src/shared/material.h:7-21 (the four marked (*) are
  * implemented; others are rejected with ASUNA_ERR_UNSUPPORTED) */
 enum {
   ASUNA_MAT_LAMBERTIAN = 0, /* (*) brdf_lambertian   */
   ASUNA_MAT_KANG18 = 1,
-  ASUNA_MAT_EMISSIVE = 2,
+  ASUNA_MAT_EMISSIVE = 2, /* (*) brdf_emissive      */
   ASUNA_MAT_PBR_METALNESS_ROUGHNESS = 3,
   ASUNA_MAT_PLASTIC = 4,
   ASUNA_MAT_ROUGH_PLASTIC = 5, /* (*) brdf_rough_plastic */
@@ -394,9 +394,16 @@ int asuna_envmap_tables(uint32_t width, uint32_t height, const float* rgba, floa
 /* Diffuse Fresnel reflectance fdrInt (src/loader/material.cpp:25-37). */
 float asuna_diffuse_fresnel(float ior, int sample_count);
 
+/* ---- image files ----------------------------------------------------------- */
+/* RGBA32F images: .exr (uncompressed FLOAT scanlines), .png (8-bit, clamped,
+ * gamma 1), .pfm.  Readers: .hdr (Radiance RGBE, env maps) and .pfm; with
+ * rgba NULL only the size is returned; capacity counts floats. */
+int asuna_image_write(const char* path, uint32_t width, uint32_t height, const float* rgba);
+int asuna_image_read(const char* path, uint32_t* width, uint32_t* height, float* rgba, uint64_t capacity);
+
 /* ---- offline tracer ------------------------------------------------------- */
-/* Renders every shot of a scene file and writes <out_prefix>_shot_%04d.pfm
- * (+ _channel_%04d.pfm per AOV), the offline mode of Tracer::runOffline. */
+/* Renders every shot of a scene file and writes <out_prefix>_shot_%04d.exr
+ * (+ _channel_%04d.exr/.png per AOV), the offline mode of Tracer::runOffline. */
 int asuna_tracer_run_offline(asuna_ctx* ctx, const char* scene_json, const char* out_prefix);
 
 #ifdef __cplusplus

@@ -1220,7 +1220,11 @@ void tracePath(const Scene& s, const asuna_shot& sh, uint32_t x, uint32_t y, uin
         hitLight<R>(s, p, hs.lightId, hs.pos);
       } else {
         uint32_t type = hs.mat.type;
-        if (type == ASUNA_MAT_ROUGH_PLASTIC)
+        if (type == ASUNA_MAT_EMISSIVE) {
+          // brdf_emissive.rchit:12-27
+          p.stop = true;
+          if (ps.ignore_emissive == 0) p.radiance = p.radiance + L3<R>(hs.mat.radiance) * p.throughput;
+        } else if (type == ASUNA_MAT_ROUGH_PLASTIC)
           shadeRoughPlastic<R>(s, sh, p, hs);
         else if (type == ASUNA_MAT_DIELECTRIC)
           shadeDielectric<R>(s, sh, p, hs);

@@ -5,7 +5,7 @@
  * reference's ray-tracing path (Asuna's GLSL shaders: raytrace.projective.rgen,
  * raytrace.default.rmiss, raytrace.shadow.rmiss, utils/{math,structs,
  * rchit_layouts,sample_light}.glsl, bxdf/{brdf_lambertian,brdf_rough_plastic,
- * bsdf_dielectric}.rchit) used as the checker of the CUDA path.  Only the
+ * bsdf_dielectric,brdf_emissive}.rchit) used as the checker of the CUDA path.  Only the
  * tests, the smoke check and the CPU-baseline leg of the benchmark load it;
  * the library never does.
  *

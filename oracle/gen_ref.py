@@ -44,6 +44,7 @@ SHADERS = {
     "bxdf/raytrace.brdf_lambertian.rchit": "stage_lambertian",
     "bxdf/raytrace.brdf_rough_plastic.rchit": "stage_rough_plastic",
     "bxdf/raytrace.bsdf_dielectric.rchit": "stage_dielectric",
+    "bxdf/raytrace.brdf_emissive.rchit": "stage_emissive",
 }
 
 FLOAT_LIT = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")

@@ -89,6 +89,7 @@ static thread_local RayPayload payload;
 #include "raytrace.brdf_lambertian.rchit.h"
 #include "raytrace.brdf_rough_plastic.rchit.h"
 #include "raytrace.bsdf_dielectric.rchit.h"
+#include "raytrace.brdf_emissive.rchit.h"
 }  // namespace glslx
 
 namespace {
@@ -155,6 +156,9 @@ void traceRayEXT(accelerationStructureEXT, uint, uint, uint, uint, uint, vec3 or
       break;
     case MaterialTypeBsdfDielectric:
       stage_dielectric::main();
+      break;
+    case MaterialTypeBrdfEmissive:
+      stage_emissive::main();
       break;
     default:
       stage_lambertian::main();

@@ -295,3 +295,65 @@ def test_json_shot_types_and_lights(tmp_path):
     assert shots[0].camera.type == A.CAMERA_OPENCV and shots[0].state.num_lights == 5
     c2w = np.array(shots[0].camera.camera_to_world).reshape(4, 4).T
     assert np.allclose(c2w[:3, 3], [0, 1, -4])
+
+
+def _read_exr(path):
+    """Reader for the uncompressed FLOAT scanline files the library writes."""
+    import struct
+    data = open(path, "rb").read()
+    assert struct.unpack_from("<i", data, 0)[0] == 20000630
+    p = 8
+    attrs = {}
+    while data[p] != 0:
+        name_end = data.index(b"\0", p)
+        name = data[p:name_end].decode()
+        type_end = data.index(b"\0", name_end + 1)
+        size = struct.unpack_from("<i", data, type_end + 1)[0]
+        attrs[name] = data[type_end + 5:type_end + 5 + size]
+        p = type_end + 5 + size
+    p += 1
+    x0, y0, x1, y1 = struct.unpack("<4i", attrs["dataWindow"])
+    w, h = x1 - x0 + 1, y1 - y0 + 1
+    assert attrs["compression"] == b"\0"
+    offsets = struct.unpack_from(f"<{h}Q", data, p)
+    img = np.zeros((h, w, 4), np.float32)
+    for y, off in enumerate(offsets):
+        yy, size = struct.unpack_from("<ii", data, off)
+        ch = np.frombuffer(data, np.float32, 4 * w, off + 8).reshape(4, w)  # A, B, G, R
+        img[yy] = ch[::-1].T
+    return img
+
+
+def test_image_writers(tmp_path):
+    rng = np.random.default_rng(0)
+    img = rng.uniform(-0.5, 4.0, size=(13, 21, 4)).astype(np.float32)
+    L = A.lib()
+    for ext in ("exr", "png", "pfm"):
+        path = str(tmp_path / f"x.{ext}")
+        A.check(L.asuna_image_write(path.encode(), 21, 13, img.ctypes.data))
+    assert np.array_equal(_read_exr(str(tmp_path / "x.exr")), img)
+    import zlib
+    data = open(tmp_path / "x.png", "rb").read()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    idat = data.index(b"IDAT")
+    n = int.from_bytes(data[idat - 4:idat], "big")
+    raw = np.frombuffer(zlib.decompress(data[idat + 4:idat + 4 + n]), np.uint8).reshape(13, 1 + 21 * 4)
+    assert np.all(raw[:, 0] == 0)
+    want = (np.clip(img, 0, 1) * 255 + 0.5).astype(np.uint8).reshape(13, -1)
+    assert np.array_equal(raw[:, 1:], want)
+    w, h = C.c_uint32(), C.c_uint32()
+    back = np.zeros((13, 21, 4), np.float32)
+    A.check(L.asuna_image_read(str(tmp_path / "x.pfm").encode(), C.byref(w), C.byref(h), back.ctypes.data, back.size))
+    assert (w.value, h.value) == (21, 13) and np.array_equal(back[..., :3], img[..., :3])
+
+
+def test_hdr_envmap_reader(tmp_path):
+    # flat (non run-length) Radiance RGBE file
+    w, h = 4, 2
+    rgbe = np.array([[[128, 64, 32, 129]] * w] * h, np.uint8)
+    (tmp_path / "e.hdr").write_bytes(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y 2 +X 4\n" + rgbe.tobytes())
+    ww, hh = C.c_uint32(), C.c_uint32()
+    out = np.zeros((h, w, 4), np.float32)
+    A.check(A.lib().asuna_image_read(str(tmp_path / "e.hdr").encode(), C.byref(ww), C.byref(hh), out.ctypes.data,
+                                     out.size))
+    assert np.allclose(out[..., :3], np.array([128, 64, 32]) * 2.0 ** (129 - 136))
