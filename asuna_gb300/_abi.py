@@ -123,6 +123,7 @@ SIGNATURES = [
     ("asuna_ctx_stream", P, [P]),
     ("asuna_ctx_set_counters", C.c_int, [P, C.c_int]),
     ("asuna_ctx_set_path_budget", C.c_int, [P, C.c_uint64]),
+    ("asuna_ctx_set_launch", C.c_int, [P, C.c_int, C.c_int]),
     ("asuna_scene_create", C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(P)]),
     ("asuna_scene_destroy", C.c_int, [P]),
     ("asuna_scene_get_stats", C.c_int, [P, C.POINTER(SceneStats)]),

@@ -1,0 +1,56 @@
+"""Autotuner of the wavefront launch configuration.
+
+Picks, for one scene and shot, the number of frames packed into one wavefront
+(the path-queue capacity: more frames keep the deep-bounce passes full) and
+the persistent-grid sizes of the traversal and shading kernels, by timing
+short renders of the real workload on the device (CUDA events inside the
+library).  Frames rendered while tuning use frame indices far from the
+caller's, so they never touch its sample streams.
+"""
+import itertools
+
+BYTES_PER_PATH = 196  # wavefront state per path slot (asuna_gb300/csrc/engine.cu)
+
+
+def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16), trace_options=(0, 4, 6),
+         shade_options=(0, 2), memory_bytes=16 << 30, reps=2, frame_base=1 << 20):
+    """Returns {"frames": f, "trace_blocks_per_sm": t, "shade_blocks_per_sm": s, "mrays": best, "trials": [...]}
+    and leaves the context configured with the best choice."""
+    npix = shot.width * shot.height
+    saved = (shot.frame0, shot.frames)
+    trials = []
+    best = None
+
+    def run(frames, t, s):
+        ctx.set_launch(t, s)
+        ctx.set_path_budget(max(frames * npix * BYTES_PER_PATH, 1))
+        shot.frames = frames
+        vals = []
+        for r in range(reps):
+            shot.frame0 = frame_base + r * frames
+            st = ctx.render(scene, shot, film, stats=True)
+            vals.append((st["extend_rays"] + st["shadow_rays"]) / (st["ms_total"] * 1e3))
+        return max(vals)
+
+    try:
+        cands = [f for f in frames_options if f * npix * BYTES_PER_PATH <= memory_bytes]
+        # frames first with the default grids, then the grids at the best frame count
+        for f in cands:
+            v = run(f, 0, 0)
+            trials.append({"frames": f, "trace": 0, "shade": 0, "mrays": v})
+            if best is None or v > best["mrays"]:
+                best = {"frames": f, "trace_blocks_per_sm": 0, "shade_blocks_per_sm": 0, "mrays": v}
+        for t, s in itertools.product(trace_options, shade_options):
+            if t == 0 and s == 0:
+                continue
+            v = run(best["frames"], t, s)
+            trials.append({"frames": best["frames"], "trace": t, "shade": s, "mrays": v})
+            if v > best["mrays"]:
+                best = {**best, "trace_blocks_per_sm": t, "shade_blocks_per_sm": s, "mrays": v}
+    finally:
+        shot.frame0, shot.frames = saved
+    ctx.set_launch(best["trace_blocks_per_sm"], best["shade_blocks_per_sm"])
+    ctx.set_path_budget(best["frames"] * npix * BYTES_PER_PATH)
+    film.clear()
+    best["trials"] = trials
+    return best

@@ -132,7 +132,7 @@ int asuna_ctx_create(int device_ordinal, asuna_ctx** out) {
   }
   cudaMemset(c->cnt, 0, sizeof(DevCounters));
   c->traceGrid = c->numSMs * traceBlocksPerSm();
-  c->shadeGrid = c->numSMs * 8;
+  c->shadeGrid = c->numSMs * shadeBlocksPerSm();
   c->raygenGrid = c->numSMs * 16;
   *out = c;
   return ASUNA_OK;
@@ -162,6 +162,16 @@ void* asuna_ctx_stream(asuna_ctx* c) { return c ? static_cast<void*>(c->stream) 
 int asuna_ctx_set_counters(asuna_ctx* c, int enable) {
   if (!c) return fail(ASUNA_ERR_INVALID, "null context");
   c->counters = enable ? 1 : 0;
+  return ASUNA_OK;
+}
+
+int asuna_ctx_set_launch(asuna_ctx* c, int traceBlocks, int shadeBlocks) {
+  if (!c) return fail(ASUNA_ERR_INVALID, "null context");
+  const int tmax = traceBlocksPerSm(), smax = shadeBlocksPerSm();
+  const int t = traceBlocks <= 0 ? tmax : std::min(traceBlocks, tmax);
+  const int sh = shadeBlocks <= 0 ? smax : std::min(shadeBlocks, smax);
+  c->traceGrid = c->numSMs * t;
+  c->shadeGrid = c->numSMs * sh;
   return ASUNA_OK;
 }
 

@@ -29,6 +29,7 @@ void launchRecords(const KParams& P, asuna_path_record* out, int grid, cudaStrea
 void launchExtend(const KParams& P, int grid, cudaStream_t s);
 void launchConnect(const KParams& P, int grid, cudaStream_t s);
 int traceBlocksPerSm();
+int shadeBlocksPerSm();
 
 // Standalone ray queries (tests): rays are (o.xyz, tmin), (d.xyz, tmax).
 void launchTraceQuery(const SceneDev& S, const float4* o, const float4* d, uint32_t n, int anyHit, float4* hit,

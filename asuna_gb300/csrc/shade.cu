@@ -222,25 +222,59 @@ __device__ __forceinline__ f3 sampleLights(const SceneDev& S, const ShotDev& sh,
   return radiance;
 }
 
-// brdf_lambertian.rchit:70-151 (after getHitState)
-__device__ __forceinline__ void shadeLambertian(const SceneDev& S, const ShotDev& sh, PathIO& io, const HitSt& st,
-                                                f3 kd, f3 rd) {
-  {
-    bool visible;
-    LRec lRec{splat(0.0f), splat(0.0f), 0.0f, 0.0f, 0u};
-    f3 Ld = splat(0.0f);
-    f3 r = sampleLights(S, sh, io, rd, st.pos, st.ffN, visible, lRec);
-    if (visible) {
-      f3 w = splat(0.0f);
-      float NdotL = dot(st.ffN, lRec.d), NdotV = dot(st.ffN, st.V);
-      if (!(NdotL < 0.0f || NdotV < 0.0f)) w = kd * INV_PI * NdotL;
-      float bpdf = (lRec.flags & EArea) ? cosineHemispherePdf(dot(st.ffN, lRec.d)) : 0.0f;
-      float mis = powerHeuristic(lRec.pdf, bpdf);
-      Ld = Ld + mis * w * r * io.thp / (lRec.pdf + EPS);
+// Next-event estimation of a material hit.  The three material hit shaders
+// (brdf_lambertian.rchit:110-134, brdf_rough_plastic.rchit:224-250,
+// bsdf_dielectric.rchit:248-271) all start with sampleLights(pos, ffN) and
+// differ only in the BSDF eval/pdf pair, so light sampling runs once here and
+// the material selects the pair.
+__device__ __forceinline__ void nextEvent(const SceneDev& S, const ShotDev& sh, PathIO& io, const HitSt& st,
+                                          const MatDev& m, uint32_t type, f3 rd) {
+  bool visible;
+  LRec lRec{splat(0.0f), splat(0.0f), 0.0f, 0.0f, 0u};
+  f3 Ld = splat(0.0f);
+  const f3 r = sampleLights(S, sh, io, rd, st.pos, st.ffN, visible, lRec);
+  if (visible) {
+    f3 w = splat(0.0f);
+    float bpdf = 0.0f;
+    if (type == ASUNA_MAT_ROUGH_PLASTIC) {
+      const float eta = m.b.z, fdrInt = m.b.w, invEta2 = 1.0f / (eta * eta);
+      const float ax = gmax(EPS, m.b.x), ay = gmax(EPS, m.b.y);
+      const f3 kd = ld3(m.a);
+      const float ssw = luminance(kd);
+      // The reference's call sites (brdf_rough_plastic.rchit:234-240) pass
+      // (.., fdrInt, ax, ay, invEta2, ..) and (.., eta, ax, ay, ..) into
+      // parameters declared (.., fdrInt, invEta2, ax, ay, ..) and
+      // (.., ax, ay, eta, ..); kept as written.
+      w = rpEval(lRec.d, st.V, st.ffN, st.X, st.Y, kd, splat(1.0f), eta, fdrInt, ax, ay, invEta2, EArea);
+      bpdf = rpPdf(lRec.d, st.V, st.ffN, st.X, st.Y, eta, ax, ay, ssw, lRec.flags);
+    } else if (type == ASUNA_MAT_DIELECTRIC) {
+      // eval() with EArea returns 0 (bsdf_dielectric.rchit:26-38); pdf 41-52
+      const float ior = m.b.z;
+      const float eta = dot(st.V, st.N) > 0.0f ? (1.0f / ior) : ior;
+      if (lRec.flags & EDelta) {
+        const f3 L = lRec.d, V = st.V, N = st.ffN;
+        const float F = dielectricFresnel(fabsf(dot(V, N)), eta);
+        if (dot(L, N) > 0.0f) {
+          if (fabsf(dot(reflect(-V, N), L) - 1.0f) < EPS) bpdf = F;
+        } else {
+          if (fabsf(dot(refract(-V, N, eta), L) - 1.0f) < EPS) bpdf = 1.0f - F;
+        }
+      }
+    } else {
+      // Lambertian eval 12-21 (flag EArea), pdf 23-29 (lRec.flags)
+      const float NdotL = dot(st.ffN, lRec.d), NdotV = dot(st.ffN, st.V);
+      if (!(NdotL < 0.0f || NdotV < 0.0f)) w = ld3(m.a) * INV_PI * NdotL;
+      bpdf = (lRec.flags & EArea) ? cosineHemispherePdf(dot(st.ffN, lRec.d)) : 0.0f;
     }
-    io.drad = Ld;
-    io.dskip = !visible;
+    const float mis = powerHeuristic(lRec.pdf, bpdf);
+    Ld = Ld + mis * w * r * io.thp / (lRec.pdf + EPS);
   }
+  io.drad = Ld;
+  io.dskip = !visible;
+}
+
+// BSDF sampling of the continuation ray: brdf_lambertian.rchit:31-42,136-151
+__device__ __noinline__ void sampleLambertian(PathIO& io, const HitSt& st, f3 kd) {
   f2 u = rnd2(io.seed);
   f3 wi = cosineSampleHemisphere(u);
   float pdf = cosineHemispherePdf(wi.z);
@@ -257,9 +291,8 @@ __device__ __forceinline__ void shadeLambertian(const SceneDev& S, const ShotDev
   io.thp = io.thp * (w / pdf);
 }
 
-// brdf_rough_plastic.rchit:191-269
-__device__ __forceinline__ void shadeRoughPlastic(const SceneDev& S, const ShotDev& sh, PathIO& io, const HitSt& st,
-                                                  const MatDev& m, f3 rd) {
+// brdf_rough_plastic.rchit:138-189,252-269
+__device__ __noinline__ void sampleRoughPlastic(PathIO& io, const HitSt& st, const MatDev& m) {
   const float eta = m.b.z;
   const float fdrInt = m.b.w;
   const float invEta2 = 1.0f / (eta * eta);
@@ -268,24 +301,6 @@ __device__ __forceinline__ void shadeRoughPlastic(const SceneDev& S, const ShotD
   const f3 kd = ld3(m.a);
   const float ssw = luminance(kd);
   const f3 ks = splat(1.0f);
-  {
-    bool visible;
-    LRec lRec{splat(0.0f), splat(0.0f), 0.0f, 0.0f, 0u};
-    f3 Ld = splat(0.0f);
-    f3 r = sampleLights(S, sh, io, rd, st.pos, st.ffN, visible, lRec);
-    if (visible) {
-      // The reference's call sites (brdf_rough_plastic.rchit:234-240) pass
-      // (.., fdrInt, ax, ay, invEta2, ..) and (.., eta, ax, ay, ..) into
-      // parameters declared (.., fdrInt, invEta2, ax, ay, ..) and
-      // (.., ax, ay, eta, ..); kept as written.
-      f3 w = rpEval(lRec.d, st.V, st.ffN, st.X, st.Y, kd, ks, eta, fdrInt, ax, ay, invEta2, EArea);
-      float bpdf = rpPdf(lRec.d, st.V, st.ffN, st.X, st.Y, eta, ax, ay, ssw, lRec.flags);
-      float mis = powerHeuristic(lRec.pdf, bpdf);
-      Ld = Ld + mis * w * r * io.thp / (lRec.pdf + EPS);
-    }
-    io.drad = Ld;
-    io.dskip = !visible;
-  }
   f2 u = rnd2(io.seed);
   const f3 V = st.V, N = st.ffN, X = st.X, Y = st.Y;
   f3 weight = splat(0.0f);
@@ -340,35 +355,10 @@ __device__ __forceinline__ void shadeRoughPlastic(const SceneDev& S, const ShotD
   io.thp = io.thp * (weight / (bpdf + EPS));
 }
 
-// bsdf_dielectric.rchit:74-139
-__device__ __forceinline__ void shadeDielectric(const SceneDev& S, const ShotDev& sh, PathIO& io, const HitSt& st,
-                                                const MatDev& m, f3 rd) {
+// bsdf_dielectric.rchit:54-72,273-289
+__device__ __noinline__ void sampleDielectric(PathIO& io, const HitSt& st, const MatDev& m) {
   const float ior = m.b.z;
   const float eta = dot(st.V, st.N) > 0.0f ? (1.0f / ior) : ior;
-  {
-    bool visible;
-    LRec lRec{splat(0.0f), splat(0.0f), 0.0f, 0.0f, 0u};
-    f3 Ld = splat(0.0f);
-    f3 r = sampleLights(S, sh, io, rd, st.pos, st.ffN, visible, lRec);
-    if (visible) {
-      // eval() with EArea returns 0 (bsdf_dielectric.rchit:26-38)
-      f3 w = splat(0.0f);
-      float bpdf = 0.0f;
-      if (lRec.flags & EDelta) {
-        f3 L = lRec.d, V = st.V, N = st.ffN;
-        float F = dielectricFresnel(fabsf(dot(V, N)), eta);
-        if (dot(L, N) > 0.0f) {
-          if (fabsf(dot(reflect(-V, N), L) - 1.0f) < EPS) bpdf = F;
-        } else {
-          if (fabsf(dot(refract(-V, N, eta), L) - 1.0f) < EPS) bpdf = 1.0f - F;
-        }
-      }
-      float mis = powerHeuristic(lRec.pdf, bpdf);
-      Ld = Ld + mis * w * r * io.thp / (lRec.pdf + EPS);
-    }
-    io.drad = Ld;
-    io.dskip = !visible;
-  }
   float u = rnd(io.seed);
   const f3 V = st.V, N = st.ffN;
   float F = dielectricFresnel(fabsf(dot(V, N)), eta);
@@ -497,12 +487,15 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shade(KParams P) {
             // brdf_emissive.rchit:12-27: add the emitted radiance and stop
             io.stop = true;
             if (sh.state.ignore_emissive == 0u) io.rad = io.rad + ld3(m.a) * io.thp;
-          } else if (type == ASUNA_MAT_ROUGH_PLASTIC)
-            shadeRoughPlastic(S, sh, io, st, m, rd);
-          else if (type == ASUNA_MAT_DIELECTRIC)
-            shadeDielectric(S, sh, io, st, m, rd);
-          else
-            shadeLambertian(S, sh, io, st, ld3(m.a), rd);
+          } else {
+            nextEvent(S, sh, io, st, m, type, rd);
+            if (type == ASUNA_MAT_ROUGH_PLASTIC)
+              sampleRoughPlastic(io, st, m);
+            else if (type == ASUNA_MAT_DIELECTRIC)
+              sampleDielectric(io, st, m);
+            else
+              sampleLambertian(io, st, ld3(m.a));
+          }
           rc.x = sigMix(rc.x, io.stop ? 0xfffu : io.bflags);
         }
         if (depth == 1u && frame == 0u && sh.depthSlot >= 0 && sh.depthSlot < ASUNA_MAX_CHANNELS) {
@@ -601,6 +594,11 @@ __global__ void __launch_bounds__(256) k_records(KParams P, asuna_path_record* o
 // ---------------------------------------------------------------------------
 void launchRaygen(const KParams& P, int grid, cudaStream_t s) { k_raygen<<<grid, 256, 0, s>>>(P); }
 void launchShade(const KParams& P, int grid, cudaStream_t s) { k_shade<<<grid, 256, 0, s>>>(P); }
+int shadeBlocksPerSm() {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shade, 256, 0);
+  return n > 0 ? n : 1;
+}
 void launchAccumulate(const KParams& P, uint32_t maxPix, uint32_t nranges, cudaStream_t s) {
   dim3 g((maxPix + 255) / 256, nranges);
   k_accumulate<<<g, 256, 0, s>>>(P);

@@ -380,6 +380,9 @@ class Context:
     def set_path_budget(self, nbytes):
         check(lib().asuna_ctx_set_path_budget(self.handle, int(nbytes)))
 
+    def set_launch(self, trace_blocks_per_sm=0, shade_blocks_per_sm=0):
+        check(lib().asuna_ctx_set_launch(self.handle, int(trace_blocks_per_sm), int(shade_blocks_per_sm)))
+
     def create_scene(self, desc):
         return DeviceScene(self, desc)
 

@@ -40,7 +40,7 @@ METRIC = "Mrays/s"
 CONFIG = {"workload": "mixed-material scene, 64 x level-7 icospheres (20.97M tris), 1920x1080, depth 12, RR>3, "
                       "1024x512 env + 4 triangle lights, aperture 0.05",
           "triangles": 20971526, "width": 1920, "height": 1080, "max_depth": 12, "rr_depth": 3,
-          "frames_per_step": 1, "l2": "inputs larger than L2 (BVH ~2.7 GB), no flush"}
+          "l2": "inputs larger than L2 (BVH ~2.7 GB), no flush"}
 
 
 def dist_env():
@@ -182,8 +182,22 @@ def run(args):
     if rank == 0 and args.verbose:
         print(f"scene built in {time.time() - t0:.1f} s: {sstats}", file=sys.stderr, flush=True)
     film = ctx.create_film(shot.width, shot.height)
+    tuned = None
+    if args.frames_per_step <= 0:
+        # autotune the wavefront size (frames per call) and the persistent grids
+        from asuna_gb300 import autotune
+
+        tuned = autotune.tune(ctx, scene, shot, film)
+        args.frames_per_step = tuned["frames"]
+        if rank == 0 and args.verbose:
+            print(f"autotune: {tuned}", file=sys.stderr, flush=True)
+    else:
+        ctx.set_path_budget(args.frames_per_step * shot.width * shot.height * 196)
     # per-rank frames: replicas render disjoint frames of the same shot
-    frame_base = 1 + rank * (args.warmup + args.steps + 2) * args.frames_per_step
+    from asuna_gb300 import replicas
+
+    per_rank = (args.warmup + 2 * args.steps + 2) * args.frames_per_step
+    frame_base = replicas.frame_shard(rank, world, 1, world * per_rank)[0]
 
     def step(i, stats=True):
         shot.frame0 = frame_base + i * args.frames_per_step
@@ -251,12 +265,17 @@ def run(args):
         with open(tpath) as f:
             tj = json.load(f)
         traffic = tj.get("dram_bytes_per_ray", 0) * tot["extend_rays"] / max(tot["extend_launches"], 1)
-    launches = int(args.steps * (2 + 3 * 12))
+    # per wavefront: raygen + accumulate, and extend + shade + connect per depth
+    # (one wavefront per step: the path budget holds frames_per_step frames)
+    launches = int(tot["extend_launches"] * 2 + tot["connect_launches"] + 2 * args.steps)
     line = {
         "metric": METRIC, "value": rays / (ms * 1e-3) / 1e6, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-        "config": {**CONFIG, "width": shot.width, "height": shot.height, "parallelism": f"replicas{world}"},
+        "config": {**CONFIG, "width": shot.width, "height": shot.height, "parallelism": f"replicas{world}",
+                   "frames_per_step": args.frames_per_step,
+                   "autotune": None if tuned is None else {k: tuned[k] for k in
+                                                           ("frames", "trace_blocks_per_sm", "shade_blocks_per_sm")}},
         "msamples_per_s": tot["paths"] * world / (ms * 1e-3) / 1e6 if world == 1 else None,
         "rays_per_step": rays / args.steps,
         "e2e": {"value": e2e_rays / e2e_s / 1e6, "unit": METRIC, "h2d_bytes_per_step": C_SHOT_BYTES,
@@ -292,7 +311,7 @@ def main():
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--spheres", type=int, default=64)
     ap.add_argument("--level", type=int, default=7)
-    ap.add_argument("--frames-per-step", type=int, default=1)
+    ap.add_argument("--frames-per-step", type=int, default=0, help="0 = autotune")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")

@@ -309,8 +309,12 @@ void* asuna_ctx_stream(asuna_ctx* ctx);
 /* Traversal counters (nodes/triangles) for the next renders: 0 off, 1 on.
  * Counting adds global atomics; keep it off when timing. */
 int asuna_ctx_set_counters(asuna_ctx* ctx, int enable);
-/* Device memory budget for wavefront path state, in bytes (0 = default). */
+/* Device memory budget for wavefront path state, in bytes (0 = default):
+ * sets how many paths (frames x pixels) one wavefront carries. */
 int asuna_ctx_set_path_budget(asuna_ctx* ctx, uint64_t bytes);
+/* Persistent-grid sizes in resident blocks per SM of the traversal and
+ * shading kernels (0 = default, capped at the occupancy limit). */
+int asuna_ctx_set_launch(asuna_ctx* ctx, int trace_blocks_per_sm, int shade_blocks_per_sm);
 
 /* ---- scene: upload + acceleration-structure build ------------------------ */
 /* Replaces Scene::submit + BLAS/TLAS build.  Host arrays are deep-copied; the
