@@ -13,7 +13,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libasuna_rt.so")
 
 # ---- status codes and enums (asuna_rt.h) -----------------------------------
-OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_IO, ERR_PARSE, ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_NO_DEVICE = range(9)
+OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_IO, ERR_PARSE, ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_NO_DEVICE, ERR_BUSY = range(10)
 CAMERA_PERSPECTIVE, CAMERA_OPENCV = 0, 1
 LIGHT_DIRECTIONAL, LIGHT_RECT, LIGHT_TRIANGLE, LIGHT_POINT = 0, 1, 2, 3
 MAT_LAMBERTIAN, MAT_EMISSIVE, MAT_ROUGH_PLASTIC, MAT_DIELECTRIC = 0, 2, 5, 10
@@ -104,6 +104,11 @@ class RenderStats(C.Structure):
                 ("extend_launches", C.c_uint64), ("connect_launches", C.c_uint64)]
 
 
+class DenoiserOpts(C.Structure):
+    _fields_ = [("levels", C.c_uint32), ("channels", C.c_uint32 * 6), ("seed", C.c_uint64),
+                ("max_pixels", C.c_uint64), ("training", C.c_uint32), ("reserved", C.c_uint32)]
+
+
 class SceneStats(C.Structure):
     _fields_ = [("triangles", C.c_uint64), ("instances", C.c_uint64), ("blas_nodes", C.c_uint64),
                 ("tlas_nodes", C.c_uint64), ("device_bytes", C.c_uint64), ("build_ms", C.c_double)]
@@ -124,6 +129,7 @@ SIGNATURES = [
     ("asuna_ctx_set_counters", C.c_int, [P, C.c_int]),
     ("asuna_ctx_set_path_budget", C.c_int, [P, C.c_uint64]),
     ("asuna_ctx_set_launch", C.c_int, [P, C.c_int, C.c_int]),
+    ("asuna_ctx_set_graphs", C.c_int, [P, C.c_int]),
     ("asuna_scene_create", C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(P)]),
     ("asuna_scene_destroy", C.c_int, [P]),
     ("asuna_scene_get_stats", C.c_int, [P, C.POINTER(SceneStats)]),
@@ -151,6 +157,33 @@ SIGNATURES = [
     ("asuna_tracer_run_offline", C.c_int, [P, C.c_char_p, C.c_char_p]),
     ("asuna_image_write", C.c_int, [C.c_char_p, C.c_uint32, C.c_uint32, P]),
     ("asuna_image_read", C.c_int, [C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), P, C.c_uint64]),
+    # include/asuna_denoise.h
+    ("asuna_denoiser_create", C.c_int, [P, C.POINTER(DenoiserOpts), C.POINTER(P)]),
+    ("asuna_denoiser_destroy", C.c_int, [P]),
+    ("asuna_denoiser_num_params", C.c_uint64, [P]),
+    ("asuna_denoiser_get_params", C.c_int, [P, P, C.c_uint64]),
+    ("asuna_denoiser_set_params", C.c_int, [P, P, C.c_uint64]),
+    ("asuna_denoiser_get_grads", C.c_int, [P, P, C.c_uint64]),
+    ("asuna_denoiser_forward", C.c_int, [P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, P]),
+    ("asuna_denoiser_loss_grad", C.c_int, [P, P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32,
+                                            C.POINTER(C.c_float)]),
+    ("asuna_denoiser_adam", C.c_int, [P, C.c_float, C.c_float, C.c_float, C.c_float]),
+    ("asuna_denoise", C.c_int, [P, P, P, C.c_int, C.c_int, P]),
+    ("asuna_denoise_estimate", C.c_int, [P, P, P, P, C.c_int, C.c_int, P, C.POINTER(C.c_double),
+                                          C.POINTER(C.c_double)]),
+    ("asuna_nn_conv3x3", C.c_int, [P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, C.c_int, C.c_int, P, P,
+                                    C.c_int]),
+    ("asuna_nn_conv3x3_wgrad", C.c_int, [P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P]),
+    ("asuna_nn_bias_grad", C.c_int, [P, P, C.c_int, C.c_int, P]),
+    ("asuna_nn_flip_weights", C.c_int, [P, P, P, C.c_int, C.c_int]),
+    ("asuna_nn_avgpool2", C.c_int, [P, P, P, C.c_int, C.c_int, C.c_int, C.c_int]),
+    ("asuna_nn_avgpool2_bwd", C.c_int, [P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+    ("asuna_nn_upsample2", C.c_int, [P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+    ("asuna_nn_upsample2_bwd", C.c_int, [P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+    ("asuna_nn_copy_channels", C.c_int, [P, P, C.c_int, C.c_int, P, C.c_int, C.c_int, C.c_int, C.c_uint64,
+                                          C.c_int]),
+    ("asuna_nn_relu_mask", C.c_int, [P, P, P, C.c_uint64]),
+    ("asuna_nn_f32_to_bf16", C.c_int, [P, P, P, C.c_uint64]),
 ]
 
 

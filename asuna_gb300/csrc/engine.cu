@@ -45,8 +45,11 @@ int devUpload(asuna_scene* s, const T* host, size_t n, const T** out) {
   return ASUNA_OK;
 }
 
+void dropGraphs(asuna_ctx* c);
+
 int ensureWave(asuna_ctx* c, uint64_t paths) {
   if (c->wave.capacity >= paths) return ASUNA_OK;
+  dropGraphs(c);
   if (c->wave.base) {
     cudaStreamSynchronize(c->stream);
     cudaFree(c->wave.base);
@@ -89,6 +92,24 @@ int ensureWave(asuna_ctx* c, uint64_t paths) {
   c->wave.base = base;
   c->wave.capacity = paths;
   return ASUNA_OK;
+}
+
+template <class T>
+int ensureDevArray(asuna_ctx* c, T** ptr, size_t* cap, size_t n) {
+  if (*cap >= n) return ASUNA_OK;
+  ASUNA_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (*ptr) cudaFree(*ptr);
+  *ptr = nullptr;
+  *cap = 0;
+  size_t want = std::max<size_t>(n, 64);
+  ASUNA_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(ptr), want * sizeof(T)));
+  *cap = want;
+  return ASUNA_OK;
+}
+
+void dropGraphs(asuna_ctx* c) {
+  for (auto& g : c->gcache) cudaGraphExecDestroy(g.exec);
+  c->gcache.clear();
 }
 
 struct Batch {
@@ -143,6 +164,9 @@ int asuna_ctx_destroy(asuna_ctx* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   for (auto ev : c->events) cudaEventDestroy(ev);
+  for (auto& g : c->gcache) cudaGraphExecDestroy(g.exec);
+  if (c->dShots) cudaFree(c->dShots);
+  if (c->dRanges) cudaFree(c->dRanges);
   if (c->wave.base) cudaFree(c->wave.base);
   if (c->cnt) cudaFree(c->cnt);
   if (c->hostCnt) cudaFreeHost(c->hostCnt);
@@ -172,6 +196,12 @@ int asuna_ctx_set_launch(asuna_ctx* c, int traceBlocks, int shadeBlocks) {
   const int sh = shadeBlocks <= 0 ? smax : std::min(shadeBlocks, smax);
   c->traceGrid = c->numSMs * t;
   c->shadeGrid = c->numSMs * sh;
+  return ASUNA_OK;
+}
+
+int asuna_ctx_set_graphs(asuna_ctx* c, int enable) {
+  if (!c) return fail(ASUNA_ERR_INVALID, "null context");
+  c->graphs = enable ? 1 : 0;
   return ASUNA_OK;
 }
 
@@ -478,6 +508,7 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
   if (!c || !s || !shots || !films || n == 0) return fail(ASUNA_ERR_INVALID, "render: null or empty argument");
   if (s->device != c->device) return fail(ASUNA_ERR_INVALID, "scene and context are on different devices");
   ASUNA_CUDA_TRY(cudaSetDevice(c->device));
+  cudaGetLastError();  // a non-sticky error left by the caller's own CUDA calls is not this call's failure
   std::vector<ShotDev> sd(n);
   uint64_t maxPix = 0;
   for (uint32_t i = 0; i < n; ++i) {
@@ -558,11 +589,17 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
     }
   }
   if (batches.empty()) return ASUNA_OK;
-  ShotDev* dShots = nullptr;
-  RangeDev* dRanges = nullptr;
   asuna_path_record* dRec = nullptr;
-  ASUNA_CUDA_TRY(cudaMallocAsync(&dShots, sd.size() * sizeof(ShotDev), c->stream));
-  ASUNA_CUDA_TRY(cudaMallocAsync(&dRanges, ranges.size() * sizeof(RangeDev), c->stream));
+  {
+    const void* oldS = c->dShots;
+    const void* oldR = c->dRanges;
+    if ((rc = ensureDevArray(c, &c->dShots, &c->shotsCap, sd.size())) ||
+        (rc = ensureDevArray(c, &c->dRanges, &c->rangesCap, ranges.size())))
+      return rc;
+    if (oldS != c->dShots || oldR != c->dRanges) dropGraphs(c);
+  }
+  ShotDev* dShots = c->dShots;
+  RangeDev* dRanges = c->dRanges;
   ASUNA_CUDA_TRY(cudaMemcpyAsync(dShots, sd.data(), sd.size() * sizeof(ShotDev), cudaMemcpyHostToDevice, c->stream));
   ASUNA_CUDA_TRY(
       cudaMemcpyAsync(dRanges, ranges.data(), ranges.size() * sizeof(RangeDev), cudaMemcpyHostToDevice, c->stream));
@@ -583,6 +620,28 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
   }
   size_t evi = 2;
   std::vector<std::pair<int, size_t>> timed;  // (kind, first event index)
+  // CUDA graph of the whole launch sequence, reused while the key matches
+  const bool useGraph = c->graphs && !hostRecords;
+  GraphEntry* hitEntry = nullptr;
+  std::vector<uint64_t> key;
+  if (useGraph) {
+    key.resize((sizeof(SceneDev) + 7) / 8, 0);
+    std::memcpy(key.data(), &s->view, sizeof(SceneDev));  // every scene pointer and size
+    key.insert(key.end(), {uint64_t(uintptr_t(c->wave.base)), c->wave.capacity,
+           uint64_t(uintptr_t(dShots)), uint64_t(uintptr_t(dRanges)), uint64_t(c->traceGrid), uint64_t(c->shadeGrid),
+           uint64_t(c->raygenGrid), uint64_t(c->counters), uint64_t(stats ? 1 : 0)});
+    for (const Batch& b : batches)
+      key.insert(key.end(), {b.rangeBegin, b.rangeEnd, b.paths, b.maxPix, uint64_t(b.maxDepth)});
+    for (auto& g : c->gcache)
+      if (g.key == key) hitEntry = &g;
+  }
+  if (hitEntry) {
+    hitEntry->lastUse = ++c->useClock;
+    ASUNA_CUDA_TRY(cudaGraphLaunch(hitEntry->exec, c->stream));
+    timed = hitEntry->timed;
+  } else {
+  if (useGraph) ASUNA_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  bool evFail = false;
   KParams P{};
   P.S = s->view;
   P.W = c->wave.view;
@@ -599,11 +658,17 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
     launchRaygen(P, std::max(rg, 1), c->stream);
     for (int depth = 1; depth <= b.maxDepth; ++depth) {
       P.depth = uint32_t(depth);
+      // inside a capture the events become event-record nodes of the graph,
+      // so every replay records them again
+      auto record = [&](cudaEvent_t ev) {
+        return useGraph ? cudaEventRecordWithFlags(ev, c->stream, cudaEventRecordExternal)
+                        : cudaEventRecord(ev, c->stream);
+      };
       auto timedLaunch = [&](int kind, auto&& fn) {
-        if (stats) cudaEventRecord(c->events[evi], c->stream);
+        if (stats && record(c->events[evi]) != cudaSuccess) evFail = true;
         fn();
         if (stats) {
-          cudaEventRecord(c->events[evi + 1], c->stream);
+          if (record(c->events[evi + 1]) != cudaSuccess) evFail = true;
           timed.push_back({kind, evi});
           evi += 2;
         }
@@ -616,10 +681,34 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
     launchAccumulate(P, b.maxPix, P.W.numRanges, c->stream);
     if (hostRecords) launchRecords(P, dRec + b.pathOffset, c->raygenGrid, c->stream);
   }
+  if (useGraph) {
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    if (e != cudaSuccess) return fail(ASUNA_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    if (evFail) {
+      cudaGraphDestroy(graph);
+      return fail(ASUNA_ERR_CUDA, "recording the timing events failed");
+    }
+    GraphEntry g;
+    e = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(ASUNA_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+    g.key = key;
+    g.timed = timed;
+    g.lastUse = ++c->useClock;
+    if (c->gcache.size() >= 8) {
+      auto lru = std::min_element(c->gcache.begin(), c->gcache.end(),
+                                  [](const GraphEntry& a, const GraphEntry& b) { return a.lastUse < b.lastUse; });
+      cudaGraphExecDestroy(lru->exec);
+      c->gcache.erase(lru);
+    }
+    c->gcache.push_back(g);
+    ASUNA_CUDA_TRY(cudaGraphLaunch(g.exec, c->stream));
+  }
+    if (evFail) return fail(ASUNA_ERR_CUDA, "recording the timing events failed");
+  }
   ASUNA_CUDA_TRY(cudaGetLastError());
   if (stats) ASUNA_CUDA_TRY(cudaEventRecord(c->events[1], c->stream));
-  ASUNA_CUDA_TRY(cudaFreeAsync(dShots, c->stream));
-  ASUNA_CUDA_TRY(cudaFreeAsync(dRanges, c->stream));
   if (hostRecords) {
     ASUNA_CUDA_TRY(cudaMemcpyAsync(hostRecords, dRec, totalPaths * sizeof(asuna_path_record), cudaMemcpyDeviceToHost,
                                    c->stream));
@@ -638,11 +727,11 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
     stats->shadow_nodes_visited = c->hostCnt->shNodes;
     stats->shadow_tris_tested = c->hostCnt->shTris;
     float ms = 0;
-    cudaEventElapsedTime(&ms, c->events[0], c->events[1]);
+    ASUNA_CUDA_TRY(cudaEventElapsedTime(&ms, c->events[0], c->events[1]));
     stats->ms_total = ms;
     for (auto& t : timed) {
       float m = 0;
-      cudaEventElapsedTime(&m, c->events[t.second], c->events[t.second + 1]);
+      ASUNA_CUDA_TRY(cudaEventElapsedTime(&m, c->events[t.second], c->events[t.second + 1]));
       if (t.first == 0) {
         stats->ms_extend += m;
         stats->extend_launches++;
@@ -654,7 +743,8 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
       }
     }
     if (c->hostCnt->stackOverflow)
-      return fail(ASUNA_ERR_INVALID, "traversal stack overflow in %llu rays", c->hostCnt->stackOverflow);
+      return fail(ASUNA_ERR_INVALID, "traversal stack overflow or runaway traversal in %llu warps or rays",
+                  c->hostCnt->stackOverflow);
   }
   return ASUNA_OK;
 }

@@ -13,6 +13,15 @@ struct WaveAlloc {
   asuna::WaveDev view{};
 };
 
+// One captured wavefront sequence, replayed while its key (scene, buffers,
+// grids, batch structure) stays the same.
+struct GraphEntry {
+  std::vector<uint64_t> key;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<std::pair<int, size_t>> timed;  // (kernel kind, first event index)
+  uint64_t lastUse = 0;
+};
+
 struct asuna_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -24,6 +33,14 @@ struct asuna_ctx {
   uint64_t pathBudget = 4ull << 30;
   int counters = 0;
   std::vector<cudaEvent_t> events;
+  // device-resident shot and batch records at stable addresses (graph replay)
+  asuna::ShotDev* dShots = nullptr;
+  size_t shotsCap = 0;
+  asuna::RangeDev* dRanges = nullptr;
+  size_t rangesCap = 0;
+  int graphs = 1;
+  uint64_t useClock = 0;
+  std::vector<GraphEntry> gcache;
 };
 
 struct asuna_scene {

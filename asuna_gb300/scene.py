@@ -380,6 +380,9 @@ class Context:
     def set_path_budget(self, nbytes):
         check(lib().asuna_ctx_set_path_budget(self.handle, int(nbytes)))
 
+    def set_graphs(self, on):
+        check(lib().asuna_ctx_set_graphs(self.handle, 1 if on else 0))
+
     def set_launch(self, trace_blocks_per_sm=0, shade_blocks_per_sm=0):
         check(lib().asuna_ctx_set_launch(self.handle, int(trace_blocks_per_sm), int(shade_blocks_per_sm)))
 

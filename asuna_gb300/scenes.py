@@ -177,7 +177,8 @@ def lognormal_envmap(rng, width=1024, height=512, hotspot=8, boost=1000.0):
 
 
 def mixed_scene(width=1920, height=1080, frames=64, max_depth=12, n_spheres=64, level=7, seed=1234,
-                rr_depth=3, env_size=(1024, 512), channels=("albedo", "normal", "depth"), verbose=False):
+                rr_depth=3, env_size=(1024, 512), channels=("albedo", "normal", "depth"), verbose=False,
+                eye=(0.0, 4.0, 30.0), at=(0.0, -2.0, 0.0)):
     """The mid-size mixed-material scene; returns (builder, shot)."""
     rng = np.random.default_rng(seed)
     b = SceneBuilder()
@@ -211,7 +212,7 @@ def mixed_scene(width=1920, height=1080, frames=64, max_depth=12, n_spheres=64, 
         if verbose and k % 16 == 15:
             print(f"mixed_scene: {k + 1}/{n_spheres} spheres", flush=True)
     state, depth = b.state(spp=frames, max_path_depth=max_depth, channels=channels)
-    eye, at = np.array((0.0, 4.0, 30.0)), np.array((0.0, -2.0, 0.0))
+    eye, at = np.asarray(eye, np.float64), np.asarray(at, np.float64)
     cam = perspective_camera(eye, at, (0, 1, 0), 50.0, width, height, aperture=0.05,
                              focal_distance=float(np.linalg.norm(eye - at)))
     shot = make_shot(cam, state, width, height, frames, seed=0, depth_channel=depth, rr_depth=rr_depth)
@@ -263,3 +264,17 @@ def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=Fa
     else:
         cam = perspective_camera(eye, at, (0, 1, 0), 55.0, width, height, aperture=0.05, focal_distance=5.0)
     return b, make_shot(cam, state, width, height, frames, seed=0, depth_channel=depth)
+
+
+def training_scene(seed, width=128, height=128, frames=4, max_depth=8, level=4):
+    """A scene of the mixed-scene recipe with a seeded sphere count (4..24)
+    and a seeded camera on a ring around the spheres: the denoiser's
+    training and evaluation scenes.  Returns (builder, shot)."""
+    rng = np.random.default_rng(10_000 + seed)
+    n = int(rng.integers(4, 25))
+    ang = float(rng.uniform(0.0, 2.0 * np.pi))
+    r = float(rng.uniform(16.0, 30.0))
+    eye = (r * np.sin(ang), float(rng.uniform(-4.0, 12.0)), r * np.cos(ang))
+    at = tuple(float(v) for v in rng.uniform(-4.0, 4.0, 3))
+    return mixed_scene(width, height, frames=frames, max_depth=max_depth, n_spheres=n, level=level, seed=seed,
+                       rr_depth=3, env_size=(128, 64), eye=eye, at=at)

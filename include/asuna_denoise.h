@@ -1,0 +1,108 @@
+/* asuna_denoise.h — C ABI of the learned denoiser.
+ *
+ * Replaces the reference's denoise step, DenoiserOptix::denoiseImageBuffer
+ * (src/tracer/denoiser.cpp:143-224, driven by Tracer::denoise at
+ * src/tracer/tracer.cpp:531-573): radiance with albedo (multi_channel[0],
+ * "diffuse") and normal (multi_channel[1]) guides in, denoised radiance out.
+ * The reference calls the closed OptiX AOV denoiser; here a U-Net with
+ * hand-written BF16 tensor-core kernels (FP32 accumulation) takes its place,
+ * trained on low/high sample-count pairs the renderer produces.
+ *
+ * Network: levels L (default 5) with channels c[0..L-1] (default
+ * 32/48/64/96/128).  Encoder level l: two 3x3 conv + ReLU, then 2x2 average
+ * pooling; decoder level l: nearest x2 upsampling, concatenation with the
+ * encoder output of level l, two 3x3 conv + ReLU; a 3x3 head gives a residual
+ * added to log1p(radiance).  Input channels (padded to 16): log1p(radiance),
+ * albedo, normal.  Activations NHWC bf16; images are padded to multiples of
+ * 2^(L-1) internally.
+ *
+ * Parameter layout (asuna_denoiser_get_params / set_params / get_grads): for
+ * each convolution in order (encoder 0..L-1 conv1, conv2; decoder L-2..0
+ * conv1, conv2; head), its weights [cout][3*3][cin] then its bias [cout], as
+ * float32.  cin of encoder conv1 of level 0 is 16; the head has cout 16, of
+ * which outputs 0..2 are used.
+ *
+ * Images passed as `const float*` are DEVICE pointers to n images of h x w
+ * RGBA32F pixels, contiguous (the layout of a film image).  All calls are
+ * asynchronous on the context's stream unless they return host values.
+ */
+#ifndef ASUNA_DENOISE_H
+#define ASUNA_DENOISE_H
+
+#include <stdint.h>
+
+#include "asuna_rt.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ASUNA_DENOISER_MAX_LEVELS 6
+
+typedef struct asuna_denoiser_opts {
+  uint32_t levels;                               /* 2..6, default 5 */
+  uint32_t channels[ASUNA_DENOISER_MAX_LEVELS];  /* multiples of 16 */
+  uint64_t seed;                                 /* He-normal initialisation */
+  uint64_t max_pixels;                           /* n*h*w of the largest call (padded) */
+  uint32_t training;                             /* 1: allocate gradient and Adam state */
+  uint32_t reserved;
+} asuna_denoiser_opts;
+
+typedef struct asuna_denoiser asuna_denoiser;
+
+int asuna_denoiser_create(asuna_ctx* ctx, const asuna_denoiser_opts* opts, asuna_denoiser** out);
+int asuna_denoiser_destroy(asuna_denoiser* d);
+uint64_t asuna_denoiser_num_params(const asuna_denoiser* d);
+int asuna_denoiser_get_params(asuna_denoiser* d, float* host, uint64_t n);
+int asuna_denoiser_set_params(asuna_denoiser* d, const float* host, uint64_t n);
+int asuna_denoiser_get_grads(asuna_denoiser* d, float* host, uint64_t n);
+
+/* Forward pass: out = expm1(log1p(radiance) + head), clamped at 0 (RGBA, alpha 1). */
+int asuna_denoiser_forward(asuna_denoiser* d, const float* radiance, const float* albedo, const float* normal,
+                           uint32_t n, uint32_t h, uint32_t w, float* out);
+/* Zeroes the gradients, runs forward, the L1 loss on log1p radiance against
+ * `target` (mean over valid pixels and 3 channels) and the backward pass.
+ * *loss (host) receives the loss; the call synchronises the stream. */
+int asuna_denoiser_loss_grad(asuna_denoiser* d, const float* radiance, const float* albedo, const float* normal,
+                             const float* target, uint32_t n, uint32_t h, uint32_t w, float* loss);
+/* One Adam step (bias-corrected) on the gradients of the last loss_grad. */
+int asuna_denoiser_adam(asuna_denoiser* d, float lr, float beta1, float beta2, float eps);
+
+/* Denoises image 0 of `film` (radiance) with guides `albedo_image` and
+ * `normal_image` (film image indices 1..7; -1 = none) into `out` (device,
+ * film-sized RGBA32F).  Stands in for DenoiserOptix::denoiseImageBuffer. */
+int asuna_denoise(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* film, int albedo_image, int normal_image,
+                  float* out);
+
+/* Error estimate of the denoised image from two independent half renders
+ * `a` and `b` of the same shot (disjoint frames, equal counts): with D the
+ * denoised a,  err_denoised^2 = mean((D - b)^2) - mean((a - b)^2) / 2  and
+ * err_plain^2 = mean((a - b)^2) / 4  estimate the RMSE of D and of the plain
+ * average of a and b against the converged image (means over pixels and RGB).
+ * The caller takes the plain path when err_denoised exceeds its threshold or
+ * err_plain.  Writes D into `out` (device, film-sized RGBA32F). */
+int asuna_denoise_estimate(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asuna_film* b, int albedo_image,
+                           int normal_image, float* out, double* err_denoised, double* err_plain);
+
+/* Device-side building blocks (raw device pointers, NHWC bf16, the context
+ * stream as `stream`); exported for kernel-level tests.  cin % 16 == 0 and
+ * cout % 8 == 0 for the convolutions. */
+int asuna_nn_conv3x3(void* stream, const void* in, int n, int h, int w, int cin, const void* weight, const float* bias,
+                     int cout, int relu, const void* mask, void* out, int out_f32);
+int asuna_nn_conv3x3_wgrad(void* stream, const void* dz, const void* x, int n, int h, int w, int cin, int cout,
+                           float* dweight);
+int asuna_nn_bias_grad(void* stream, const void* dz, int pixels, int c, float* dbias);
+int asuna_nn_flip_weights(void* stream, const void* w, void* wt, int cout, int cin);
+int asuna_nn_avgpool2(void* stream, const void* in, void* out, int n, int h, int w, int c);
+int asuna_nn_avgpool2_bwd(void* stream, const void* dout, void* din, int n, int h, int w, int c, int accumulate);
+int asuna_nn_upsample2(void* stream, const void* in, void* out, int n, int h, int w, int c, int ctot, int coff);
+int asuna_nn_upsample2_bwd(void* stream, const void* dout, void* din, int n, int h, int w, int c, int ctot, int coff);
+int asuna_nn_copy_channels(void* stream, const void* src, int csrc, int soff, void* dst, int cdst, int doff, int c,
+                           uint64_t pixels, int accumulate);
+int asuna_nn_relu_mask(void* stream, void* grad, const void* y, uint64_t count);
+int asuna_nn_f32_to_bf16(void* stream, const float* a, void* b, uint64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ASUNA_DENOISE_H */

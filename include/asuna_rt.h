@@ -51,7 +51,8 @@ enum {
   ASUNA_ERR_PARSE = 5,       /* JSON / OBJ / image syntax or schema error  */
   ASUNA_ERR_TIMEOUT = 6,     /* a bounded device wait gave up              */
   ASUNA_ERR_UNSUPPORTED = 7, /* feature outside the implemented plugin set */
-  ASUNA_ERR_NO_DEVICE = 8    /* no CUDA device / library built without it  */
+  ASUNA_ERR_NO_DEVICE = 8,   /* no CUDA device / library built without it  */
+  ASUNA_ERR_BUSY = 9         /* server queue full: request rejected        */
 };
 
 /* ---- enums of the reference's plugin dispatch --------------------------- */
@@ -312,6 +313,9 @@ int asuna_ctx_set_counters(asuna_ctx* ctx, int enable);
 /* Device memory budget for wavefront path state, in bytes (0 = default):
  * sets how many paths (frames x pixels) one wavefront carries. */
 int asuna_ctx_set_path_budget(asuna_ctx* ctx, uint64_t bytes);
+/* Capture each render's launch sequence as a CUDA graph and replay it while
+ * the scene, buffers and batch structure repeat (1 = on, the default). */
+int asuna_ctx_set_graphs(asuna_ctx* ctx, int enable);
 /* Persistent-grid sizes in resident blocks per SM of the traversal and
  * shading kernels (0 = default, capped at the occupancy limit). */
 int asuna_ctx_set_launch(asuna_ctx* ctx, int trace_blocks_per_sm, int shade_blocks_per_sm);
@@ -397,6 +401,53 @@ int asuna_envmap_tables(uint32_t width, uint32_t height, const float* rgba, floa
                         float* conditional_xy);
 /* Diffuse Fresnel reflectance fdrInt (src/loader/material.cpp:25-37). */
 float asuna_diffuse_fresnel(float ior, int sample_count);
+
+/* ---- render server (continuous batching) -------------------------------------
+ * No counterpart in the reference (an addition for serving).  Requests on
+ * resident scenes arrive at any time; `slots` worker contexts render them
+ * concurrently on the device, each slot batching the active requests of one
+ * scene into one multi-shot wavefront per chunk of frames, with requests
+ * leaving and joining at chunk boundaries.  Admission: a request's result
+ * film must fit the memory budget (else it waits) and the pending queue must
+ * have room (else it is rejected with ASUNA_ERR_BUSY, reported by poll). */
+typedef struct asuna_server asuna_server;
+typedef struct asuna_server_opts {
+  int32_t device;
+  uint32_t slots;            /* concurrent worker slots (each a context + stream) */
+  uint32_t frames_per_chunk; /* frames per wavefront pass of an active set */
+  uint32_t max_batch;        /* requests per active set (0 = 8) */
+  uint32_t max_queue;        /* pending requests before arrivals are rejected (0 = unbounded) */
+  uint32_t reserved;
+  uint64_t memory_budget;    /* bytes for resident scenes + result films (0 = 150 GiB) */
+  uint64_t path_budget;      /* wavefront state per slot, bytes (0 = default) */
+} asuna_server_opts;
+typedef struct asuna_request {
+  uint32_t scene; /* id from asuna_server_add_scene */
+  uint32_t reserved;
+  asuna_shot shot; /* shot.frames = spp */
+} asuna_request;
+typedef struct asuna_request_result {
+  uint64_t id;
+  int32_t status; /* ASUNA_OK, or why the request was rejected / failed */
+  uint32_t scene;
+  double arrival_s, start_s, finish_s; /* server clock */
+  uint64_t samples;
+} asuna_request_result;
+typedef struct asuna_server_stats {
+  uint64_t admitted, rejected, pending, samples, memory_used;
+  double elapsed_s;
+} asuna_server_stats;
+int asuna_server_create(const asuna_server_opts* opts, asuna_server** out);
+int asuna_server_add_scene(asuna_server* server, const asuna_scene_desc* desc, uint32_t* scene_id);
+int asuna_server_submit(asuna_server* server, const asuna_request* req, uint64_t* id);
+/* Finished (or rejected) requests since the last poll, oldest first. */
+int asuna_server_poll(asuna_server* server, asuna_request_result* out, uint32_t max, uint32_t* n);
+int asuna_server_read(asuna_server* server, uint64_t id, int image, float* host_rgba);
+/* Frees a finished request's film (returns its memory to the budget). */
+int asuna_server_release(asuna_server* server, uint64_t id);
+int asuna_server_drain(asuna_server* server, double timeout_s);
+int asuna_server_get_stats(asuna_server* server, asuna_server_stats* out);
+int asuna_server_destroy(asuna_server* server);
 
 /* ---- image files ----------------------------------------------------------- */
 /* RGBA32F images: .exr (uncompressed FLOAT scanlines), .png (8-bit, clamped,

@@ -1496,7 +1496,7 @@ int oracle_render(const oracle_scene* os, const asuna_shot* shot, float* film, a
 }
 
 int oracle_render_pixels_f64(const oracle_scene* os, const asuna_shot* shot, const uint32_t* pixels, uint32_t npixels,
-                             int nthreads, double* out_rgb, oracle_stats* stats) {
+                             int nthreads, double* out_rgb, double* out_var, oracle_stats* stats) {
   if (!os || !shot || !out_rgb) return ASUNA_ERR_INVALID;
   const Scene& s = os->s;
   const uint32_t W = shot->width, H = shot->height;
@@ -1512,15 +1512,32 @@ int oracle_render_pixels_f64(const oracle_scene* os, const asuna_shot* shot, con
       if (i >= npix) break;
       uint32_t pix = pixels ? pixels[i] : i;
       uint32_t x = pix % W, y = pix / W;
-      double acc[3] = {0, 0, 0}, wsum = 0;
+      // weighted mean of the clamped samples; for its variance also
+      // sum fw^2 x^2, sum fw^2 x and sum fw^2
+      double acc[3] = {0, 0, 0}, s2[3] = {0, 0, 0}, s3[3] = {0, 0, 0}, wsum = 0, w2 = 0;
       for (uint32_t f = 0; f < shot->frames; ++f) {
         PathOut po;
         tracePath<double>(s, *shot, x, y, shot->frame0 + f, po, nullptr, nExt, nSh);
         double fw = po.fw;
-        for (int c = 0; c < 3; ++c) acc[c] += fw * std::min(std::max(po.radd[c], 0.0), 10.0);
+        for (int c = 0; c < 3; ++c) {
+          const double v = std::min(std::max(po.radd[c], 0.0), 10.0);
+          acc[c] += fw * v;
+          s2[c] += fw * fw * v * v;
+          s3[c] += fw * fw * v;
+        }
         wsum += fw;
+        w2 += fw * fw;
       }
-      for (int c = 0; c < 3; ++c) out_rgb[size_t(i) * 3 + c] = acc[c] / wsum;
+      for (int c = 0; c < 3; ++c) {
+        const double m = acc[c] / wsum;
+        out_rgb[size_t(i) * 3 + c] = m;
+        // variance of the weighted mean: sum fw^2 (x - m)^2 / (sum fw)^2 / (1 - sum fw^2 / (sum fw)^2)
+        if (out_var) {
+          const double ss = std::max(0.0, s2[c] - 2.0 * m * s3[c] + m * m * w2);
+          const double corr = 1.0 - w2 / (wsum * wsum);
+          out_var[size_t(i) * 3 + c] = corr > 0.0 ? ss / (wsum * wsum) / corr : 0.0;
+        }
+      }
     }
     gExt += nExt;
     gSh += nSh;

@@ -54,7 +54,8 @@ int oracle_render(const oracle_scene* s, const asuna_shot* shot, float* film,
  * pixel subset: out[i*3+c] = mean clamped radiance weighted by the filter,
  * i.e. the converged pixel value estimate after `shot->frames` frames. */
 int oracle_render_pixels_f64(const oracle_scene* s, const asuna_shot* shot, const uint32_t* pixels,
-                             uint32_t npixels, int nthreads, double* out_rgb, oracle_stats* stats);
+                             uint32_t npixels, int nthreads, double* out_rgb, double* out_var,
+                             oracle_stats* stats);
 
 /* Known-answer hooks. */
 uint32_t oracle_xxhash32(uint32_t x, uint32_t y, uint32_t z);

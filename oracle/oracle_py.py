@@ -38,7 +38,7 @@ def port():
         L.oracle_render.argtypes = [C.c_void_p, C.POINTER(A.Shot), C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
                                     C.c_int, C.c_int, C.POINTER(OracleStats)]
         L.oracle_render_pixels_f64.argtypes = [C.c_void_p, C.POINTER(A.Shot), C.c_void_p, C.c_uint32, C.c_int,
-                                               C.c_void_p, C.POINTER(OracleStats)]
+                                               C.c_void_p, C.c_void_p, C.POINTER(OracleStats)]
         L.oracle_xxhash32.restype = C.c_uint32
         L.oracle_xxhash32.argtypes = [C.c_uint32] * 3
         L.oracle_pcg.restype = C.c_uint32
@@ -96,15 +96,20 @@ class OracleScene:
             raise RuntimeError(f"oracle_render failed: {rc}")
         return film, rec, {k: getattr(st, k) for k, _ in OracleStats._fields_}
 
-    def pixels_f64(self, shot, pixels, threads=0):
+    def pixels_f64(self, shot, pixels, threads=0, variance=False):
+        """FP64 render of the listed pixels: (mean rgb [n, 3], stats), or
+        (mean, variance of the mean, stats) with `variance`."""
         px = np.ascontiguousarray(pixels, np.uint32)
         out = np.zeros((len(px), 3), np.float64)
+        var = np.zeros((len(px), 3), np.float64) if variance else None
         st = OracleStats()
         rc = self.L.oracle_render_pixels_f64(self.h, C.byref(shot), px.ctypes.data, len(px), threads,
-                                             out.ctypes.data, C.byref(st))
+                                             out.ctypes.data, None if var is None else var.ctypes.data,
+                                             C.byref(st))
         if rc:
             raise RuntimeError(f"oracle_render_pixels_f64 failed: {rc}")
-        return out, {k: getattr(st, k) for k, _ in OracleStats._fields_}
+        stats = {k: getattr(st, k) for k, _ in OracleStats._fields_}
+        return (out, var, stats) if variance else (out, stats)
 
     def trace(self, o, d, tmin=1e-5, tmax=1e10):
         o = np.ascontiguousarray(o, np.float32)

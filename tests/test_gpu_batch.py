@@ -60,3 +60,18 @@ def test_seed_changes_streams(ctx):
     c = _film(ctx, scene, shot)
     assert not np.array_equal(a[0], c[0])
     assert abs(float(a[0, ..., :3].mean()) - float(c[0, ..., :3].mean())) < 0.1
+
+
+def test_graph_replay_equals_direct_launches(ctx):
+    b, shot = scenes.plugin_scene(64, 48, frames=2, max_depth=6)
+    scene = ctx.create_scene(b.desc())
+    films = []
+    for graphs in (False, True):
+        ctx.set_graphs(graphs)
+        f = ctx.create_film(64, 48)
+        for k in range(3):  # the second and third calls replay the captured graph
+            shot.frame0 = 2 * k
+            ctx.render(scene, shot, f, stats=(k == 2))
+        films.append(np.stack([f.read(i) for i in range(9)]))
+    ctx.set_graphs(True)
+    assert np.array_equal(films[0], films[1])
