@@ -627,7 +627,8 @@ struct InitRng {
 }  // namespace
 
 struct asuna_denoiser {
-  asuna_ctx* ctx = nullptr;
+  asuna_ctx* ctx = nullptr;  // the stream it runs on; not touched by destroy
+  int device = 0;
   int L = 0;
   int ch[ASUNA_DENOISER_MAX_LEVELS] = {};
   bool training = false;
@@ -814,6 +815,7 @@ int asuna_denoiser_create(asuna_ctx* ctx, const asuna_denoiser_opts* o, asuna_de
   asuna_denoiser* d = new (std::nothrow) asuna_denoiser;
   if (!d) return fail(ASUNA_ERR_OOM, "host allocation failed");
   d->ctx = ctx;
+  d->device = ctx->device;
   d->L = L;
   for (int l = 0; l < L; ++l) d->ch[l] = int(o->channels[l]);
   d->training = o->training != 0;
@@ -902,10 +904,11 @@ int asuna_denoiser_create(asuna_ctx* ctx, const asuna_denoiser_opts* o, asuna_de
   return ASUNA_OK;
 }
 
+// May run after the context is gone (garbage-collected handles): uses only
+// the device ordinal; cudaFree waits for the device's work.
 int asuna_denoiser_destroy(asuna_denoiser* d) {
   if (!d) return ASUNA_OK;
-  cudaSetDevice(d->ctx->device);
-  cudaStreamSynchronize(d->ctx->stream);
+  cudaSetDevice(d->device);
   delete d;
   return ASUNA_OK;
 }

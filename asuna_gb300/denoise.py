@@ -22,6 +22,26 @@ from . import _abi as A
 from ._abi import check, lib
 
 DEFAULT_CHANNELS = (32, 48, 64, 96, 128)
+IN_CHANNELS = 16  # log1p(radiance), albedo, normal, zero padding
+HEAD_CHANNELS = 16  # outputs 0..2 used
+
+
+def layer_table(channels=DEFAULT_CHANNELS):
+    """(cin, cout, level) of every convolution in parameter order: encoder
+    levels 0..L-1 (two each), decoder levels L-2..0 (two each), head."""
+    L = len(channels)
+    t = []
+    for l in range(L):
+        t += [(IN_CHANNELS if l == 0 else channels[l - 1], channels[l], l), (channels[l], channels[l], l)]
+    for l in range(L - 2, -1, -1):
+        t += [(channels[l + 1] + channels[l], channels[l], l), (channels[l], channels[l], l)]
+    t.append((channels[0], HEAD_CHANNELS, 0))
+    return t
+
+
+def forward_flops(channels, hp, wp):
+    """FLOPs (2 per multiply-add) of one forward pass at a padded hp x wp image."""
+    return sum(2.0 * 9 * cin * cout * (hp >> l) * (wp >> l) for cin, cout, l in layer_table(channels))
 
 
 def _torch():
@@ -133,27 +153,34 @@ class Denoiser:
 
 
 def render_pairs(ctx, seeds, width, height, spp_in=4, spp_target=256, level=4, max_depth=8):
-    """Renders each training scene twice with independent sample streams:
-    `spp_in` frames (network input, with the albedo / normal channels) and
-    `spp_target` frames (target).  Returns host arrays [n, h, w, 4] float32:
-    (radiance, albedo, normal, target)."""
+    """Renders each training scene with two independent sample streams: the
+    network input after each count of `spp_in` (an int or an increasing
+    tuple; one progressive render, with the albedo / normal channels) and
+    a `spp_target` render (the target).  Returns host arrays [n, h, w, 4]
+    float32 (radiance, albedo, normal, target), one entry per scene and
+    input count."""
     from . import scenes
 
+    levels = (spp_in,) if np.isscalar(spp_in) else tuple(spp_in)
     out = {k: [] for k in ("rad", "alb", "nrm", "tgt")}
     for s in seeds:
-        b, shot = scenes.training_scene(int(s), width, height, frames=spp_in, max_depth=max_depth, level=level)
+        b, shot = scenes.training_scene(int(s), width, height, frames=levels[0], max_depth=max_depth, level=level)
         scene = ctx.create_scene(b.desc())
+        g = ctx.create_film(width, height)
+        shot.frame0, shot.frames, shot.seed = 0, spp_target, 2 * int(s) + 1
+        ctx.render(scene, shot, g)
+        tgt = g.read(0)
         f = ctx.create_film(width, height)
         shot.seed = 2 * int(s)
-        ctx.render(scene, shot, f)
-        out["rad"].append(f.read(0))
-        out["alb"].append(f.read(1))
-        out["nrm"].append(f.read(2))
-        g = ctx.create_film(width, height)
-        shot.frames = spp_target
-        shot.seed = 2 * int(s) + 1
-        ctx.render(scene, shot, g)
-        out["tgt"].append(g.read(0))
+        done = 0
+        for spp in levels:
+            shot.frame0, shot.frames = done, spp - done
+            ctx.render(scene, shot, f)
+            done = spp
+            out["rad"].append(f.read(0))
+            out["alb"].append(f.read(1))
+            out["nrm"].append(f.read(2))
+            out["tgt"].append(tgt)
         f.close()
         g.close()
         del scene

@@ -278,6 +278,8 @@ def run(args):
                                                            ("frames", "trace_blocks_per_sm", "shade_blocks_per_sm")}},
         "msamples_per_s": tot["paths"] * world / (ms * 1e-3) / 1e6 if world == 1 else None,
         "rays_per_step": rays / args.steps,
+        "instrumented_step": {"extend_rays": cst["extend_rays"], "shadow_rays": cst["shadow_rays"],
+                              "nodes_visited": cst["nodes_visited"], "tris_tested": cst["tris_tested"]},
         "e2e": {"value": e2e_rays / e2e_s / 1e6, "unit": METRIC, "h2d_bytes_per_step": C_SHOT_BYTES,
                 "d2h_bytes_per_step": int(host.nbytes)},
         "gpu_launches": launches,
@@ -295,6 +297,135 @@ def run(args):
     print(json.dumps(line), flush=True)
     if torch_dist:
         torch_dist.destroy_process_group()
+    return 0
+
+
+def run_denoise_rmse(args):
+    """Time to image RMSE 0.01 against the FP64 reference (a seeded 1,024-pixel
+    subset of the 1080p workload at 262,144 spp, tests/golden) for the plain
+    wavefront path and for the denoised path.
+
+    Plain: progressive doubling of the sample count; RMSE on the subset with
+    the reference's own variance subtracted; the time at RMSE 0.01 is
+    interpolated on the 1/sqrt(spp) law from the first count that reaches it.
+    Denoised: two progressive films A and B on disjoint frames; the output is
+    the denoised A, judged by B (asuna_denoise_estimate): when the estimate
+    exceeds the target, the plain average is the output instead.  Its time
+    counts every render and every estimate.  The network is trained first,
+    on the GPU, on pairs the renderer makes of other seeded scenes of the
+    same recipe (4/16/64-spp input, 1024-spp target)."""
+    import torch
+
+    import asuna_gb300 as ag
+    from asuna_gb300 import denoise as dn
+
+    target = args.rmse_target
+    ref = np.load(os.path.join(ROOT, "tests", "golden", "rmse_ref_mixed_1080p.npz"))
+    px, mean, refvar = ref["pixels"], ref["mean"], float(ref["var"].mean())
+
+    def rmse(img):
+        v = img.reshape(-1, 4)[px, :3].astype(np.float64)
+        return float(np.sqrt(max(0.0, np.mean((v - mean) ** 2) - refvar)))
+
+    ctx = ag.Context(0)
+    stream = dn.ctx_stream(ctx)
+    out = {"metric": f"time to RMSE {target} vs FP64 reference (s)", "unit": "s", "higher_is_better": False,
+           "config": {**CONFIG, "reference": f"{len(px)} seeded pixels x {int(ref['spp'])} spp FP64 CPU oracle",
+                      "reference_rms_noise": float(np.sqrt(refvar))}}
+    # 1. train the denoiser on renderer-made pairs
+    t0 = time.time()
+    data = dn.render_pairs(ctx, range(1000, 1000 + args.train_scenes), args.train_size, args.train_size,
+                           spp_in=(4, 16, 64), spp_target=args.train_target_spp, level=5)
+    gen_s = time.time() - t0
+    den = dn.Denoiser(ctx, seed=0, max_pixels=args.train_batch * args.train_crop ** 2, training=True)
+    t1 = time.time()
+    losses = dn.train(den, data, steps=args.train_steps, batch=args.train_batch, crop=args.train_crop, lr=1e-3)
+    train_s = time.time() - t1
+    out["training"] = {"scenes": args.train_scenes, "size": args.train_size, "input_spp": [4, 16, 64],
+                       "target_spp": args.train_target_spp, "steps": args.train_steps, "batch": args.train_batch,
+                       "crop": args.train_crop, "data_seconds": gen_s, "train_seconds": train_s,
+                       "loss_first": float(np.mean(losses[:20])), "loss_last": float(np.mean(losses[-50:]))}
+    del data
+    # 2. the workload
+    b, shot = build_workload(args, verbose=False)
+    scene = ctx.create_scene(b.desc())
+    W, H = shot.width, shot.height
+    inf = dn.Denoiser(ctx, max_pixels=((H + 15) // 16 * 16) * ((W + 15) // 16 * 16))
+    inf.set_params(den.get_params())
+    del den
+    ctx.set_path_budget(16 * W * H * 196)
+    chunk = 16
+
+    def render_frames(film, first, count, seed):
+        ms = 0.0
+        f = first
+        while f < first + count:
+            k = min(chunk, first + count - f)
+            shot.frame0, shot.frames, shot.seed = f, k, seed
+            ms += ctx.render(scene, shot, film, stats=True)["ms_total"]
+            f += k
+        return ms
+
+    # 2a. plain path
+    film = ctx.create_film(W, H)
+    plain, spp, ms = [], 0, 0.0
+    while spp < args.plain_max_spp:
+        nxt = max(16, 2 * spp)
+        ms += render_frames(film, spp, nxt - spp, 0)
+        spp = nxt
+        e = rmse(film.read(0))
+        plain.append({"spp": spp, "seconds": ms / 1e3, "rmse": e})
+        if e <= target:
+            break
+    last = plain[-1]
+    spp_star = last["spp"] * (last["rmse"] / target) ** 2  # 1/sqrt(spp) law
+    t_plain = last["seconds"] / last["spp"] * spp_star
+    out["plain"] = {"ladder": plain, "spp_at_target": spp_star, "seconds_at_target": t_plain,
+                    "reached": last["rmse"] <= target}
+    # 2b. denoised path with the error-estimate fallback
+    fa, fb = ctx.create_film(W, H), ctx.create_film(W, H)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dres, half, ms = [], 0, 0.0
+    t_den = None
+    while 2 * half < args.denoise_max_spp:
+        nh = max(2, 2 * half)
+        ms += render_frames(fa, half, nh - half, 0)
+        ms += render_frames(fb, half, nh - half, 7)
+        half = nh
+        with torch.cuda.stream(stream):
+            ev0.record()
+            img, err_d, err_p = inf.estimate(fa, fb)
+            ev1.record()
+        ev1.synchronize()
+        est_ms = ev0.elapsed_time(ev1)
+        ms += est_ms
+        used = "denoised" if err_d <= target and err_d <= err_p else "plain"
+        if used == "denoised":
+            e = rmse(img.cpu().numpy())
+        else:
+            e = rmse(0.5 * (fa.read(0) + fb.read(0)))
+        dres.append({"spp": 2 * half, "seconds": ms / 1e3, "estimate_ms": est_ms, "err_estimate": err_d,
+                     "err_plain_estimate": err_p, "output": used, "rmse": e,
+                     "rmse_denoised": rmse(img.cpu().numpy())})
+        if e <= target:
+            t_den = ms / 1e3
+            break
+    out["denoised"] = {"ladder": dres, "seconds_at_target": t_den, "reached": t_den is not None}
+    # denoiser forward throughput at 1080p
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            inf.denoise(fa)
+        ev0.record()
+        for _ in range(10):
+            inf.denoise(fa)
+        ev1.record()
+    ev1.synchronize()
+    fwd_ms = ev0.elapsed_time(ev1) / 10
+    fl = dn.forward_flops(dn.DEFAULT_CHANNELS, (H + 15) // 16 * 16, (W + 15) // 16 * 16)
+    out["denoiser_forward"] = {"ms": fwd_ms, "tflops": fl / (fwd_ms * 1e-3) / 1e12, "flop": fl}
+    out["value"] = t_den
+    out["speedup"] = (t_plain / t_den) if t_den else None
+    print(json.dumps(out), flush=True)
     return 0
 
 
@@ -316,10 +447,23 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--verbose", action="store_true")
+    ap.add_argument("--denoise-rmse", action="store_true",
+                    help="time to RMSE 0.01 vs the FP64 reference, plain vs denoised path")
+    ap.add_argument("--rmse-target", type=float, default=0.01)
+    ap.add_argument("--plain-max-spp", type=int, default=32768)
+    ap.add_argument("--denoise-max-spp", type=int, default=4096)
+    ap.add_argument("--train-scenes", type=int, default=96)
+    ap.add_argument("--train-size", type=int, default=256)
+    ap.add_argument("--train-target-spp", type=int, default=1024)
+    ap.add_argument("--train-steps", type=int, default=3000)
+    ap.add_argument("--train-batch", type=int, default=16)
+    ap.add_argument("--train-crop", type=int, default=128)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.denoise_rmse:
+        return run_denoise_rmse(args)
     return run(args)
 
 

@@ -75,3 +75,12 @@ def test_init_layout_and_scale():
         assert abs(w.std() / np.sqrt(2.0 / (9 * cin)) - 1.0) < 0.1
     assert np.array_equal(p, U.he_init(ch, 11))
     assert not np.array_equal(p, U.he_init(ch, 12))
+
+
+def test_package_layer_table_matches_reference():
+    from asuna_gb300 import denoise as dn
+
+    ch = dn.DEFAULT_CHANNELS
+    assert [(a, b) for a, b, _ in dn.layer_table(ch)] == U.layer_shapes(list(ch))
+    # 0.40 TFLOP per forward of a padded 1088 x 1920 image
+    assert abs(dn.forward_flops(ch, 1088, 1920) / 1e12 - 0.4019) < 1e-3
