@@ -99,37 +99,47 @@ __device__ __forceinline__ void xformRay(const float4* w, float3 o, float3 d, fl
 }
 
 constexpr float kFarScale = 1.00000095367431640625f;  // 1 + 2^-20
+constexpr int32_t kDone = INT32_MIN + 1;               // stack empty: traversal over
+constexpr int32_t kNoLeaf = INT32_MIN + 2;             // no postponed leaf
+constexpr uint32_t kTraceSpinCap = 1u << 20;           // inner steps of one warp pass
+constexpr uint32_t kTraceRayCap = 1u << 16;            // leaves + transitions of one ray
+
+__device__ __forceinline__ bool isLeafRef(int32_t r) { return r < 0 && r != kStackSentinel && r != kDone; }
 
 struct HitOut {
   float t, u, v;
   uint32_t prim, inst;
 };
 
-// Traversal state of one ray.  step() walks the two-level BVH until it has
-// tested the triangles of one BLAS leaf or the traversal is over, so a warp
-// can hand finished lanes new rays between steps.
+// Traversal state of one ray (while-while traversal with postponed leaves,
+// after Aila and Laine, "Understanding the efficiency of ray traversal on
+// GPUs", HPG 2009).  innerStep() visits one inner node; a BLAS leaf met
+// there is postponed and, when `speculate`, the lane goes on visiting inner
+// nodes while other lanes of the warp still look for a leaf.  leafOrMove()
+// then tests the triangles of one leaf, or makes one TLAS/BLAS transition.
 struct Trav {
-  float3 wo, wd;  // world-space ray
-  float3 o, d, id;  // ray in the current space (world or instance object space)
+  float3 wo, wd, wid;  // world-space ray and its inverse direction
+  float3 o, id;        // ray origin / inverse direction in the current space
   WT wt;
   float tmin, best;
   uint32_t curInst;
   int sp;
-  int32_t ref;
+  int32_t ref, leaf;
   bool found, inBlas;
   HitOut h;
 
   __device__ __forceinline__ void init(const SceneDev& S, float3 ro, float3 rd, float t0, float t1) {
     wo = ro;
     wd = rd;
+    wid = safeInv(rd);
     o = ro;
-    d = rd;
-    id = safeInv(rd);
+    id = wid;
     tmin = t0;
     best = t1;
     curInst = 0;
     sp = 0;
     ref = S.tlasRoot;
+    leaf = kNoLeaf;
     found = false;
     inBlas = false;
   }
@@ -147,153 +157,143 @@ struct Trav {
     }
     ++sp;
   }
-  __device__ __forceinline__ int32_t pop(const int32_t* sh, const int32_t* loc) {
+  __device__ __forceinline__ int32_t popOrDone(const int32_t* sh, const int32_t* loc) {
+    if (sp == 0) return kDone;
     --sp;
     return sp < kSharedStack ? sh[sp * kTraceThreads] : loc[sp - kSharedStack];
   }
 
-  // Returns true when the traversal is finished.
-  template <bool ANY, bool COUNT>
-  __device__ __forceinline__ bool step(const SceneDev& S, int32_t* sh, int32_t* loc, uint32_t& nNodes,
-                                       uint32_t& nTris, bool& ovf) {
-    for (;;) {
-      if (ref >= 0) {
-        const BvhNode* n = S.nodes + ref;
-        const float4 xs = __ldg(&n->xs), ys = __ldg(&n->ys), zs = __ldg(&n->zs);
-        const int4 rr = __ldg(&n->ref);
-        if (COUNT) ++nNodes;
-        const float tx0 = (xs.x - o.x) * id.x, tx1 = (xs.y - o.x) * id.x;
-        const float ty0 = (ys.x - o.y) * id.y, ty1 = (ys.y - o.y) * id.y;
-        const float tz0 = (zs.x - o.z) * id.z, tz1 = (zs.y - o.z) * id.z;
-        const float ux0 = (xs.z - o.x) * id.x, ux1 = (xs.w - o.x) * id.x;
-        const float uy0 = (ys.z - o.y) * id.y, uy1 = (ys.w - o.y) * id.y;
-        const float uz0 = (zs.z - o.z) * id.z, uz1 = (zs.w - o.z) * id.z;
-        const float a0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-        const float a1 = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), best)) * kFarScale;
-        const float b0 = fmaxf(fmaxf(fminf(ux0, ux1), fminf(uy0, uy1)), fmaxf(fminf(uz0, uz1), tmin));
-        const float b1 = fminf(fminf(fmaxf(ux0, ux1), fmaxf(uy0, uy1)), fminf(fmaxf(uz0, uz1), best)) * kFarScale;
-        const bool h0 = a0 <= a1, h1 = b0 <= b1;
-        if (h0 && h1) {
-          const bool swap = b0 < a0;
-          push(sh, loc, swap ? rr.x : rr.y, ovf);
-          ref = swap ? rr.y : rr.x;
-          continue;
-        }
-        if (h0 || h1) {
-          ref = h0 ? rr.x : rr.y;
-          continue;
-        }
-      } else if (ref != kStackSentinel) {
-        if (!inBlas) {
-          // TLAS leaf: enter the instance's BLAS in object space
-          curInst = leafFirst(ref);
-          const InstDev* in = S.inst + curInst;
-          const int32_t root = __ldg(&in->blasRoot);
-          if (root >= 0 && sp < kStackDepth) {
-            xformRay(in->w2o, wo, wd, o, d);
-            id = safeInv(d);
-            wt = wtPre(d);
-            inBlas = true;
-            push(sh, loc, kStackSentinel, ovf);
-            ref = root;
-            continue;
-          }
-          if (root >= 0) ovf = true;
-        } else {
-          const uint32_t first = leafFirst(ref), cnt = leafCount(ref);
-          for (uint32_t k = 0; k < cnt; ++k) {
-            const TriDev* tr = S.tris + first + k;
-            const float4 p0 = __ldg(&tr->v0), p1 = __ldg(&tr->v1), p2 = __ldg(&tr->v2);
-            if (COUNT) ++nTris;
-            float t, b1, b2;
-            if (wtTri(wt, o, p0, p1, p2, tmin, best, t, b1, b2)) {
-              if (ANY) {
-                found = true;
-                return true;
-              }
-              const uint32_t prim = __float_as_uint(p0.w);
-              // exact ties resolve to the lowest (instance, primitive), so
-              // the result does not depend on traversal order
-              if (!found || t < best || (curInst < h.inst || (curInst == h.inst && prim < h.prim))) {
-                found = true;
-                best = t;
-                h.t = t;
-                h.u = b1;
-                h.v = b2;
-                h.prim = prim;
-                h.inst = curInst;
-              }
-            }
-          }
-          if (sp == 0) return true;
-          ref = pop(sh, loc);
-          return false;  // a leaf was processed: let the warp refill idle lanes
-        }
-      } else {
-        // leaving a BLAS: back to the world-space ray
-        inBlas = false;
-        o = wo;
-        d = wd;
-        id = safeInv(wd);
-      }
-      if (sp == 0) return true;
-      ref = pop(sh, loc);
+  template <bool COUNT>
+  __device__ __forceinline__ void innerStep(const SceneDev& S, int32_t* sh, int32_t* loc, uint32_t& nNodes,
+                                            bool& ovf) {
+    const BvhNode* n = S.nodes + ref;
+    const float4 xs = __ldg(&n->xs), ys = __ldg(&n->ys), zs = __ldg(&n->zs);
+    const int4 rr = __ldg(&n->ref);
+    if (COUNT) ++nNodes;
+    const float tx0 = (xs.x - o.x) * id.x, tx1 = (xs.y - o.x) * id.x;
+    const float ty0 = (ys.x - o.y) * id.y, ty1 = (ys.y - o.y) * id.y;
+    const float tz0 = (zs.x - o.z) * id.z, tz1 = (zs.y - o.z) * id.z;
+    const float ux0 = (xs.z - o.x) * id.x, ux1 = (xs.w - o.x) * id.x;
+    const float uy0 = (ys.z - o.y) * id.y, uy1 = (ys.w - o.y) * id.y;
+    const float uz0 = (zs.z - o.z) * id.z, uz1 = (zs.w - o.z) * id.z;
+    const float a0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+    const float a1 = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), best)) * kFarScale;
+    const float b0 = fmaxf(fmaxf(fminf(ux0, ux1), fminf(uy0, uy1)), fmaxf(fminf(uz0, uz1), tmin));
+    const float b1 = fminf(fminf(fmaxf(ux0, ux1), fmaxf(uy0, uy1)), fminf(fmaxf(uz0, uz1), best)) * kFarScale;
+    const bool h0 = a0 <= a1, h1 = b0 <= b1;
+    if (h0 && h1) {
+      const bool swap = b0 < a0;
+      push(sh, loc, swap ? rr.x : rr.y, ovf);
+      ref = swap ? rr.y : rr.x;
+    } else if (h0 || h1) {
+      ref = h0 ? rr.x : rr.y;
+    } else {
+      ref = popOrDone(sh, loc);
     }
+    if (inBlas && leaf == kNoLeaf && isLeafRef(ref)) {
+      leaf = ref;  // postpone: test it together with the other lanes' leaves
+      ref = popOrDone(sh, loc);
+    }
+  }
+
+  // Returns true when the traversal is over.
+  template <bool ANY, bool COUNT>
+  __device__ __forceinline__ bool leafOrMove(const SceneDev& S, int32_t* sh, int32_t* loc, uint32_t& nTris,
+                                             bool& ovf) {
+    int32_t L = kNoLeaf;
+    if (leaf != kNoLeaf) {
+      L = leaf;
+      leaf = kNoLeaf;
+    } else if (inBlas && isLeafRef(ref)) {
+      L = ref;
+      ref = popOrDone(sh, loc);
+    }
+    if (L != kNoLeaf) {
+      const uint32_t first = leafFirst(L), cnt = leafCount(L);
+      for (uint32_t k = 0; k < cnt; ++k) {
+        const TriDev* tr = S.tris + first + k;
+        const float4 p0 = __ldg(&tr->v0), p1 = __ldg(&tr->v1), p2 = __ldg(&tr->v2);
+        if (COUNT) ++nTris;
+        float t, b1, b2;
+        if (wtTri(wt, o, p0, p1, p2, tmin, best, t, b1, b2)) {
+          if (ANY) {
+            found = true;
+            return true;
+          }
+          const uint32_t prim = __float_as_uint(p0.w);
+          // exact ties resolve to the lowest (instance, primitive), so the
+          // result does not depend on traversal order
+          if (!found || t < best || (curInst < h.inst || (curInst == h.inst && prim < h.prim))) {
+            found = true;
+            best = t;
+            h.t = t;
+            h.u = b1;
+            h.v = b2;
+            h.prim = prim;
+            h.inst = curInst;
+          }
+        }
+      }
+      return false;
+    }
+    if (ref == kDone) return true;
+    if (ref == kStackSentinel) {
+      // leaving a BLAS: back to the world-space ray
+      inBlas = false;
+      o = wo;
+      id = wid;
+      ref = popOrDone(sh, loc);
+      return false;
+    }
+    // TLAS leaf: enter the instance's BLAS in object space
+    curInst = leafFirst(ref);
+    const InstDev* in = S.inst + curInst;
+    const int32_t root = __ldg(&in->blasRoot);
+    if (root >= 0 && sp < kStackDepth) {
+      float3 d;
+      xformRay(in->w2o, wo, wd, o, d);
+      id = safeInv(d);
+      wt = wtPre(d);
+      inBlas = true;
+      push(sh, loc, kStackSentinel, ovf);
+      ref = root;
+      return false;
+    }
+    if (root >= 0) ovf = true;
+    ref = popOrDone(sh, loc);
+    return false;
   }
 };
 
-// Persistent warps over a ray queue.  Lanes whose ray is finished take the
-// next rays of the queue (one atomic per refill, per warp) while the other
-// lanes keep traversing.
-template <bool ANY, bool COUNT>
-__global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_trace(KParams P) {
-  __shared__ int32_t sstack[kSharedStack * kTraceThreads];
-  int32_t lstack[kStackDepth - kSharedStack];
-  int32_t* sh = sstack + threadIdx.x;
-  const WaveDev& W = P.W;
-  const SceneDev& S = P.S;
-  const int cur = P.cur;
-  uint32_t* countPtr = ANY ? &W.cnt->c[kCntShadow] : &W.cnt->c[kCntExtend0 + cur];
-  uint32_t* fetch = ANY ? &W.cnt->c[kCntFetchShadow] : &W.cnt->c[kCntFetchExtend];
-  const uint32_t count = *countPtr;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    if (ANY) {
-      W.cnt->shadowRays += count;
-      W.cnt->c[kCntFetchExtend] = 0;  // the next extend pass fetches from 0
-    } else {
-      W.cnt->extendRays += count;
-      W.cnt->c[kCntExtend0 + (cur ^ 1)] = 0;  // shade appends into the other queue
-      W.cnt->c[kCntShadow] = 0;
-    }
-  }
-  const float4* rO = ANY ? W.shO : W.rayO[cur];
-  const float4* rD = ANY ? W.shD : W.rayD[cur];
+// Persistent warp over a ray source.  Lanes whose ray is finished take the
+// next rays of the source (one fetch per refill, per warp) while the other
+// lanes keep traversing.  Src supplies count, fetch(n) -> first index (called
+// by one lane), commit(first, n) (called by every lane), load(i, tr) and
+// finish(i, tr).
+template <bool ANY, bool COUNT, bool SPEC, class Src>
+__device__ __forceinline__ void traceWarp(const SceneDev& S, Src& src, int32_t* sh, int32_t* loc, uint32_t& nNodes,
+                                          uint32_t& nTris, bool& ovf) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lanesBelow = (1u << lane) - 1u;
-  uint32_t nNodes = 0, nTris = 0;
-  bool ovf = false;
   bool active = false, drained = false;
-  uint32_t idx = 0;
+  uint32_t idx = 0, events = 0;
   Trav tr;
   for (;;) {
     const unsigned idle = __ballot_sync(0xffffffffu, !active);
     if (idle && !drained && (__popc(idle) >= kRefillLanes || idle == 0xffffffffu)) {
       const int leader = __ffs(idle) - 1;
       uint32_t base = 0;
-      if (int(lane) == leader) base = atomicAdd(fetch, uint32_t(__popc(idle)));
+      if (int(lane) == leader) base = src.fetch(uint32_t(__popc(idle)));
       base = __shfl_sync(0xffffffffu, base, leader);
-      drained = base + uint32_t(__popc(idle)) >= count;
+      src.commit(base, uint32_t(__popc(idle)));
+      drained = base + uint32_t(__popc(idle)) >= src.count;
       if (!active) {
         const uint32_t r = base + uint32_t(__popc(idle & lanesBelow));
-        if (r < count) {
+        if (r < src.count) {
           idx = r;
           active = true;
-          const float4 o4 = __ldg(&rO[r]);
-          const float4 d4 = __ldg(&rD[r]);
-          if (ANY)
-            tr.init(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), 0.0f, o4.w);
-          else
-            tr.init(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), 0.00001f, 10000000000.0f);
+          events = 0;
+          src.load(S, r, tr);
         }
       }
     }
@@ -301,30 +301,104 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_trace(KParam
       if (drained) break;
       continue;
     }
-    if (active && tr.template step<ANY, COUNT>(S, sh, lstack, nNodes, nTris, ovf)) {
+    // inner nodes until every lane holds a leaf (or waits at a transition)
+    // (lanes without a leaf make progress every iteration, so the loop ends;
+    // with SPEC the others walk on speculatively meanwhile).  Both loops
+    // carry a bound far above any real traversal: past it the warp stops
+    // and reports the error instead of running on.
+    uint32_t spin = 0;
+    for (;;) {
+      const bool stepping = active && tr.ref >= 0;
+      const bool needy = stepping && tr.leaf == kNoLeaf;
+      if (!__any_sync(0xffffffffu, needy)) break;
+      if (++spin > kTraceSpinCap) break;
+      if (SPEC ? stepping : needy) tr.template innerStep<COUNT>(S, sh, loc, nNodes, ovf);
+    }
+    if (spin > kTraceSpinCap) {
+      ovf = true;
+      break;
+    }
+    if (active && (tr.template leafOrMove<ANY, COUNT>(S, sh, loc, nTris, ovf) || ++events > kTraceRayCap)) {
+      if (events > kTraceRayCap) ovf = true;
       active = false;
-      if (ANY) {
-        if (!tr.found) {
-          const uint32_t p = __float_as_uint(__ldg(&rD[idx].w));
-          const float4 c = __ldg(&W.shC[idx]);
-          float4 r = W.rad[p];
-          r.x = r.x + c.x;
-          r.y = r.y + c.y;
-          r.z = r.z + c.z;
-          W.rad[p] = r;
-          if (P.records) W.rec[p].y |= 1u << (P.depth - 1u);
-        }
-      } else if (tr.found) {
-        W.hit[idx] = make_float4(tr.h.t, tr.h.u, tr.h.v, __uint_as_float(tr.h.prim));
-        W.hitInst[idx] = tr.h.inst;
-      } else {
-        W.hit[idx] = make_float4(-1.0f, 0.0f, 0.0f, 0.0f);
-        W.hitInst[idx] = 0xffffffffu;
-      }
+      src.finish(idx, tr);
     }
   }
+}
+
+// Ray queue of a wavefront pass.
+template <bool ANY>
+struct QueueSrc {
+  const WaveDev* W;
+  const KParams* P;
+  const float4 *rO, *rD;
+  uint32_t* fetchCtr;
+  uint32_t count;
+  __device__ __forceinline__ uint32_t fetch(uint32_t n) { return atomicAdd(fetchCtr, n); }
+  __device__ __forceinline__ void commit(uint32_t, uint32_t) {}
+  __device__ __forceinline__ void load(const SceneDev& S, uint32_t r, Trav& tr) {
+    const float4 o4 = __ldg(&rO[r]);
+    const float4 d4 = __ldg(&rD[r]);
+    if (ANY)
+      tr.init(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), 0.0f, o4.w);
+    else
+      tr.init(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), 0.00001f, 10000000000.0f);
+  }
+  __device__ __forceinline__ void finish(uint32_t i, const Trav& tr) {
+    if (ANY) {
+      if (!tr.found) {
+        const uint32_t p = __float_as_uint(__ldg(&rD[i].w));
+        const float4 c = __ldg(&W->shC[i]);
+        float4 r = W->rad[p];
+        r.x = r.x + c.x;
+        r.y = r.y + c.y;
+        r.z = r.z + c.z;
+        W->rad[p] = r;
+        if (P->records) W->rec[p].y |= 1u << (P->depth - 1u);
+      }
+    } else if (tr.found) {
+      W->hit[i] = make_float4(tr.h.t, tr.h.u, tr.h.v, __uint_as_float(tr.h.prim));
+      W->hitInst[i] = tr.h.inst;
+    } else {
+      W->hit[i] = make_float4(-1.0f, 0.0f, 0.0f, 0.0f);
+      W->hitInst[i] = 0xffffffffu;
+    }
+  }
+};
+
+template <bool ANY, bool COUNT>
+__global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_trace(KParams P) {
+  __shared__ int32_t sstack[kSharedStack * kTraceThreads];
+  int32_t lstack[kStackDepth - kSharedStack];
+  int32_t* sh = sstack + threadIdx.x;
+  const WaveDev& W = P.W;
+  const int cur = P.cur;
+  uint32_t* countPtr = ANY ? &W.cnt->c[kCntShadow] : &W.cnt->c[kCntExtend0 + cur];
+  QueueSrc<ANY> src;
+  src.W = &P.W;
+  src.P = &P;
+  src.fetchCtr = ANY ? &W.cnt->c[kCntFetchShadow] : &W.cnt->c[kCntFetchExtend];
+  src.count = *countPtr;
+  src.rO = ANY ? W.shO : W.rayO[cur];
+  src.rD = ANY ? W.shD : W.rayD[cur];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (ANY) {
+      W.cnt->shadowRays += src.count;
+      W.cnt->c[kCntFetchExtend] = 0;  // the next extend pass fetches from 0
+    } else {
+      W.cnt->extendRays += src.count;
+      W.cnt->c[kCntExtend0 + (cur ^ 1)] = 0;  // shade appends into the other queue
+      W.cnt->c[kCntShadow] = 0;
+    }
+  }
+  uint32_t nNodes = 0, nTris = 0;
+  bool ovf = false;
+  // the instrumented variant walks without speculation, so its node counts
+  // are those of the ordered traversal
+  traceWarp<ANY, COUNT, !COUNT>(P.S, src, sh, lstack, nNodes, nTris, ovf);
   if (ovf) atomicAdd(&W.cnt->stackOverflow, 1ull);
   if (COUNT) {
+    const unsigned lane = threadIdx.x & 31u;
     unsigned long long a = nNodes, b = nTris;
     for (int off = 16; off; off >>= 1) {
       a += __shfl_down_sync(0xffffffffu, a, off);
@@ -337,24 +411,22 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_trace(KParam
   }
 }
 
-__global__ void __launch_bounds__(kTraceThreads) k_query(SceneDev S, const float4* o, const float4* d, uint32_t n,
-                                                         int anyHit, float4* hit, uint32_t* inst) {
-  __shared__ int32_t sstack[kSharedStack * kTraceThreads];
-  int32_t lstack[kStackDepth - kSharedStack];
-  int32_t* sh = sstack + threadIdx.x;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float4 o4 = o[i], d4 = d[i];
-    Trav tr;
+// Rays given as arrays (asuna_scene_trace): each warp walks its own
+// contiguous slice of the rays with the same warp loop.
+struct ArraySrc {
+  const float4 *o, *d;
+  float4* hit;
+  uint32_t* inst;
+  uint32_t cursor, count;
+  int anyHit;
+  __device__ __forceinline__ uint32_t fetch(uint32_t) { return cursor; }
+  // every lane of the warp advances its copy of the cursor alike
+  __device__ __forceinline__ void commit(uint32_t base, uint32_t n) { cursor = base + n; }
+  __device__ __forceinline__ void load(const SceneDev& S, uint32_t r, Trav& tr) {
+    const float4 o4 = o[r], d4 = d[r];
     tr.init(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), o4.w, d4.w);
-    uint32_t a = 0, b = 0;
-    bool ovf = false;
-    if (anyHit) {
-      while (!tr.template step<true, false>(S, sh, lstack, a, b, ovf)) {
-      }
-    } else {
-      while (!tr.template step<false, false>(S, sh, lstack, a, b, ovf)) {
-      }
-    }
+  }
+  __device__ __forceinline__ void finish(uint32_t i, const Trav& tr) {
     if (tr.found) {
       hit[i] = anyHit ? make_float4(1.0f, 0.0f, 0.0f, 0.0f)
                       : make_float4(tr.h.t, tr.h.u, tr.h.v, __uint_as_float(tr.h.prim));
@@ -364,6 +436,25 @@ __global__ void __launch_bounds__(kTraceThreads) k_query(SceneDev S, const float
       inst[i] = 0xffffffffu;
     }
   }
+};
+
+__global__ void __launch_bounds__(kTraceThreads) k_query(SceneDev S, const float4* o, const float4* d, uint32_t n,
+                                                         int anyHit, float4* hit, uint32_t* inst) {
+  __shared__ int32_t sstack[kSharedStack * kTraceThreads];
+  int32_t lstack[kStackDepth - kSharedStack];
+  int32_t* sh = sstack + threadIdx.x;
+  const uint32_t warps = gridDim.x * (blockDim.x / 32u);
+  const uint32_t w = blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u;
+  const uint32_t per = (n + warps - 1) / warps;
+  const uint32_t lo = min(n, w * per), hi = min(n, lo + per);
+  // indices are relative to the slice
+  ArraySrc src{o + lo, d + lo, hit + lo, inst + lo, 0u, hi - lo, anyHit};
+  uint32_t a = 0, b = 0;
+  bool ovf = false;
+  if (anyHit)
+    traceWarp<true, false, true>(S, src, sh, lstack, a, b, ovf);
+  else
+    traceWarp<false, false, true>(S, src, sh, lstack, a, b, ovf);
 }
 
 }  // namespace

@@ -211,12 +211,18 @@ def mixed_scene(width=1920, height=1080, frames=64, max_depth=12, n_spheres=64, 
                                                    np.float32))
         if verbose and k % 16 == 15:
             print(f"mixed_scene: {k + 1}/{n_spheres} spheres", flush=True)
+    return b, mixed_shot(b, width, height, frames, max_depth, rr_depth, channels, eye, at)
+
+
+def mixed_shot(b, width, height, frames, max_depth=12, rr_depth=3, channels=("albedo", "normal", "depth"),
+               eye=(0.0, 4.0, 30.0), at=(0.0, -2.0, 0.0), seed=0):
+    """A shot of a mixed-recipe scene `b` (thin lens focused on `at`) at any
+    resolution and sample count, without rebuilding the geometry."""
     state, depth = b.state(spp=frames, max_path_depth=max_depth, channels=channels)
     eye, at = np.asarray(eye, np.float64), np.asarray(at, np.float64)
     cam = perspective_camera(eye, at, (0, 1, 0), 50.0, width, height, aperture=0.05,
                              focal_distance=float(np.linalg.norm(eye - at)))
-    shot = make_shot(cam, state, width, height, frames, seed=0, depth_channel=depth, rr_depth=rr_depth)
-    return b, shot
+    return make_shot(cam, state, width, height, frames, seed=seed, depth_channel=depth, rr_depth=rr_depth)
 
 
 def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=False, seed=11,

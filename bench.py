@@ -429,6 +429,54 @@ def run_denoise_rmse(args):
     return 0
 
 
+SERVE_SCENES = [(4, 7), (16, 6), (16, 7), (24, 7), (32, 7), (48, 7), (64, 6), (64, 7)]  # (spheres, level): 1.3M-21M triangles
+
+
+def run_serve(args):
+    """Serving loop: requests arrive as a Poisson process (wall clock) at
+    --serve-rate per second; each picks a resident scene of the mixed recipe
+    (4-64 spheres, 1.3-21M triangles), a resolution from {512x512, 1280x720,
+    1920x1080} and a sample count from {4, 16, 64}, with a seeded camera.
+    Reports latency percentiles (arrival to finish), Msamples/s and the
+    rejection / queueing rates under the 150 GB admission budget."""
+    from asuna_gb300 import scenes
+    from asuna_gb300.serving import Server, poisson_load
+
+    rng = np.random.default_rng(7)
+    srv = Server(slots=args.serve_slots, frames_per_chunk=args.serve_chunk, max_batch=8,
+                 max_queue=args.serve_max_queue, memory_budget=150 << 30)
+    t0 = time.time()
+    pool = []
+    for k, (n, lvl) in enumerate(SERVE_SCENES):
+        b, _ = scenes.mixed_scene(64, 64, frames=1, n_spheres=n, level=lvl, seed=3000 + k)
+        pool.append((srv.add_scene(b.desc()), b, n * 20 * 4 ** lvl))
+    build_s = time.time() - t0
+    res = [(512, 512), (1280, 720), (1920, 1080)]
+    reqs = []
+    for i in range(args.serve_requests):
+        sid, b, _ = pool[int(rng.integers(len(pool)))]
+        w, h = res[int(rng.integers(3))]
+        spp = int((4, 16, 64)[int(rng.integers(3))])
+        ang = float(rng.uniform(0, 2 * np.pi))
+        eye = (30.0 * np.sin(ang), float(rng.uniform(0.0, 10.0)), 30.0 * np.cos(ang))
+        reqs.append((sid, scenes.mixed_shot(b, w, h, spp, eye=eye, seed=i)))
+    out = poisson_load(srv, reqs, rate_hz=args.serve_rate, seed=11)
+    st = srv.stats()
+    srv.close()
+    out.pop("films")
+    line = {"metric": "serving latency p99 (s)", "value": out["p99_s"], "unit": "s", "higher_is_better": False,
+            "n_gpus": 1, "data": "synthetic (seeded procedural scenes)",
+            "config": {"workload": f"Poisson {args.serve_rate} req/s, {args.serve_requests} requests, "
+                                   f"{len(pool)} resident scenes of 1.3-21M triangles, "
+                                   "512^2 / 1280x720 / 1920x1080, 4 / 16 / 64 spp, depth 12",
+                       "slots": args.serve_slots, "frames_per_chunk": args.serve_chunk,
+                       "max_queue": args.serve_max_queue, "memory_budget_gb": 150,
+                       "scene_triangles": [p[2] for p in pool], "scene_build_s": build_s},
+            **out, "server_stats": st}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 C_SHOT_BYTES = 340  # sizeof(asuna_shot): the only host->device input of a step
 
 
@@ -458,12 +506,20 @@ def main():
     ap.add_argument("--train-steps", type=int, default=3000)
     ap.add_argument("--train-batch", type=int, default=16)
     ap.add_argument("--train-crop", type=int, default=128)
+    ap.add_argument("--serve", action="store_true", help="serving loop: Poisson arrivals, latency percentiles")
+    ap.add_argument("--serve-rate", type=float, default=20.0)
+    ap.add_argument("--serve-requests", type=int, default=600)
+    ap.add_argument("--serve-slots", type=int, default=2)
+    ap.add_argument("--serve-chunk", type=int, default=4)
+    ap.add_argument("--serve-max-queue", type=int, default=256)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
     if args.denoise_rmse:
         return run_denoise_rmse(args)
+    if args.serve:
+        return run_serve(args)
     return run(args)
 
 
