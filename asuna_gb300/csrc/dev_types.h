@@ -5,7 +5,9 @@
 // with 128-bit loads.
 #pragma once
 #include <cstdint>
+#include <cstring>
 
+#include <vector_functions.h>
 #include <vector_types.h>
 
 #include "../../include/asuna_rt.h"
@@ -23,6 +25,27 @@ struct __align__(16) BvhNode {
   int4 ref;   // c0, c1, unused, unused
 };
 static_assert(sizeof(BvhNode) == 64, "BvhNode is 64 bytes");
+
+// 4-wide BVH node, 128 B = one cache line: four 32-B child records, each
+// (lo.x, lo.y, lo.z, hi.x), (hi.y, hi.z, ref bits, unused) so a child's box
+// test needs only its own two 128-bit loads.  Child references use the
+// BvhNode encoding; an empty slot has a degenerate box at 1e30 and ref
+// kStackSentinel, so no box test ever selects it.  The traversal kernels
+// walk these nodes; they are collapsed from the binary builder's tree.
+struct __align__(16) Bvh4Child {
+  float4 a;  // lo.x, lo.y, lo.z, hi.x
+  float4 b;  // hi.y, hi.z, ref (int bits), 0
+};
+struct __align__(128) Bvh4Node {
+  Bvh4Child c[4];
+};
+inline int32_t bvh4Ref(const Bvh4Node& n, int k) {
+  int32_t r;
+  std::memcpy(&r, &n.c[k].b.z, 4);
+  return r;
+}
+inline void setBvh4Ref(Bvh4Node& n, int k, int32_t r) { std::memcpy(&n.c[k].b.z, &r, 4); }
+static_assert(sizeof(Bvh4Node) == 128, "Bvh4Node is 128 bytes");
 
 constexpr int kMaxLeafTris = 8;
 constexpr int32_t kStackSentinel = INT32_MIN;  // "leave the BLAS" marker
@@ -78,7 +101,7 @@ struct __align__(16) LightDev {
 
 // Device view of one uploaded scene.
 struct SceneDev {
-  const BvhNode* nodes;  // all BLAS nodes, then the TLAS nodes
+  const Bvh4Node* nodes;  // all BLAS nodes, then the TLAS nodes (4-wide)
   const TriDev* tris;
   const VtxDev* vtx;
   const uint4* idx;  // mesh-local vertex indices (x, y, z), w unused
@@ -124,7 +147,20 @@ enum CounterSlot {
   kCntShadow = 2,   // rays in the shadow queue
   kCntFetchExtend = 3,
   kCntFetchShadow = 4,
-  kCntNum32 = 8
+  kCntCls0 = 5,  // rays per shading class (kNumShadeClasses slots)
+  kCntNum32 = 12
+};
+
+// Shading classes: the hits of an extend pass are split by what shades them,
+// so every shading kernel runs one material's code with full warps.
+enum ShadeClass {
+  kClsTerminal = 0,    // miss, light hit, emissive surface: the path ends
+  kClsLambertian = 1,
+  kClsRoughPlastic = 2,
+  kClsDielectric = 3,
+  kClsPlastic = 4,
+  kClsMirror = 5,
+  kNumShadeClasses = 6
 };
 struct DevCounters {
   uint32_t c[kCntNum32];
@@ -155,6 +191,7 @@ struct WaveDev {
   float4* rad;  // radiance.xyz, filter weight
   uint4* info;  // seed, last BSDF lobe flags, range index, local index
   uint4* rec;   // parity records: signature, unoccluded bits, shadow bits, depth
+  uint32_t* cls[kNumShadeClasses];  // extend-queue indices of each shading class
   DevCounters* cnt;
   const RangeDev* ranges;
   const ShotDev* shots;

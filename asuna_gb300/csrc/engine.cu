@@ -31,7 +31,7 @@ using namespace asuna;
 
 namespace {
 
-constexpr uint64_t kBytesPerPath = 2 * 32 + 16 + 4 + 48 + 48 + 16;
+constexpr uint64_t kBytesPerPath = 2 * 32 + 16 + 4 + 48 + 48 + 16 + 4 * kNumShadeClasses;
 
 template <class T>
 int devUpload(asuna_scene* s, const T* host, size_t n, const T** out) {
@@ -71,6 +71,11 @@ int ensureWave(asuna_ctx* c, uint64_t paths) {
   uint64_t o_rad = off; off += pad(paths * 16);
   uint64_t o_info = off; off += pad(paths * 16);
   uint64_t o_rec = off; off += pad(paths * 16);
+  uint64_t o_cls[kNumShadeClasses];
+  for (int k = 0; k < kNumShadeClasses; ++k) {
+    o_cls[k] = off;
+    off += pad(paths * 4);
+  }
   void* base = nullptr;
   ASUNA_CUDA_TRY(cudaMalloc(&base, off));
   char* b = static_cast<char*>(base);
@@ -88,6 +93,7 @@ int ensureWave(asuna_ctx* c, uint64_t paths) {
   v.rad = reinterpret_cast<float4*>(b + o_rad);
   v.info = reinterpret_cast<uint4*>(b + o_info);
   v.rec = reinterpret_cast<uint4*>(b + o_rec);
+  for (int k = 0; k < kNumShadeClasses; ++k) v.cls[k] = reinterpret_cast<uint32_t*>(b + o_cls[k]);
   v.cnt = c->cnt;
   c->wave.base = base;
   c->wave.capacity = paths;
@@ -233,6 +239,7 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
   }
   if (triBase[nm] > kMaxLeafFirst) return fail(ASUNA_ERR_UNSUPPORTED, "scene has more than 2^28 triangles");
   std::vector<BvhBuildOut> blas(nm);
+  std::vector<Bvh4Out> blas4(nm);
   std::vector<int> okMesh(nm, 1);
   {
     std::atomic<uint32_t> next{0};
@@ -255,6 +262,7 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
             }
           }
           okMesh[m] = buildBvh(boxes, cen, 4, triBase[m], blas[m]) ? 1 : 0;
+          if (okMesh[m]) collapseBvh4(blas[m].nodes, blas4[m]);
         }
       });
     for (auto& t : th) t.join();
@@ -262,19 +270,21 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
   for (uint32_t m = 0; m < nm; ++m)
     if (!okMesh[m]) return fail(ASUNA_ERR_UNSUPPORTED, "mesh %u: BVH cannot be encoded", m);
   std::vector<uint32_t> nodeBase(nm + 1, 0);
-  uint32_t blasDepth = 0;
+  uint32_t blasPush = 0;
   for (uint32_t m = 0; m < nm; ++m) {
-    nodeBase[m + 1] = nodeBase[m] + uint32_t(blas[m].nodes.size());
-    blasDepth = std::max(blasDepth, blas[m].maxDepth);
+    nodeBase[m + 1] = nodeBase[m] + uint32_t(blas4[m].nodes.size());
+    blasPush = std::max(blasPush, blas4[m].maxPush);
   }
-  std::vector<BvhNode> nodes;
-  nodes.reserve(nodeBase[nm] + 2 * d->num_instances + 2);
+  std::vector<Bvh4Node> nodes;
+  nodes.reserve(nodeBase[nm] + d->num_instances + 2);
   std::vector<TriDev> tris(triBase[nm]);
   for (uint32_t m = 0; m < nm; ++m) {
     const asuna_mesh_desc& md = d->meshes[m];
-    for (BvhNode n : blas[m].nodes) {
-      if (n.ref.x >= 0) n.ref.x += int32_t(nodeBase[m]);
-      if (n.ref.y >= 0) n.ref.y += int32_t(nodeBase[m]);
+    for (Bvh4Node n : blas4[m].nodes) {
+      for (int k = 0; k < 4; ++k) {
+        const int32_t r = bvh4Ref(n, k);
+        if (r >= 0) setBvh4Ref(n, k, r + int32_t(nodeBase[m]));
+      }
       nodes.push_back(n);
     }
     for (uint32_t i = 0; i < md.num_triangles; ++i) {
@@ -348,21 +358,21 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
   }
   BvhBuildOut tlas;
   if (!buildBvh(iboxes, icen, 1, 0, tlas)) return fail(ASUNA_ERR_UNSUPPORTED, "TLAS cannot be encoded");
+  Bvh4Out tlas4;
+  collapseBvh4(tlas.nodes, tlas4);
   const uint32_t tlasBase = uint32_t(nodes.size());
-  for (BvhNode n : tlas.nodes) {
-    for (int side = 0; side < 2; ++side) {
-      int32_t& ref = side == 0 ? n.ref.x : n.ref.y;
+  for (Bvh4Node n : tlas4.nodes) {
+    for (int k = 0; k < 4; ++k) {
+      const int32_t ref = bvh4Ref(n, k);
       if (ref == kStackSentinel) continue;
-      if (ref >= 0)
-        ref += int32_t(tlasBase);
-      else
-        ref = encodeLeaf(ids[tlas.order[leafFirst(ref)]], 1);
+      setBvh4Ref(n, k, ref >= 0 ? ref + int32_t(tlasBase) : encodeLeaf(ids[tlas.order[leafFirst(ref)]], 1));
     }
     nodes.push_back(n);
   }
-  if (tlas.maxDepth + blasDepth + 1 > uint32_t(kStackDepth))
-    return fail(ASUNA_ERR_UNSUPPORTED, "BVH too deep for the traversal stack (TLAS %u + BLAS %u levels, limit %d)",
-                tlas.maxDepth, blasDepth, kStackDepth - 1);
+  // worst case of the traversal stack: TLAS pushes, the BLAS sentinel, BLAS pushes
+  if (tlas4.maxPush + 1 + blasPush > uint32_t(kStackDepth))
+    return fail(ASUNA_ERR_UNSUPPORTED, "BVH too deep for the traversal stack (TLAS %u + BLAS %u entries, limit %d)",
+                tlas4.maxPush, blasPush, kStackDepth - 1);
   // ---- shading data ----
   std::vector<VtxDev> vtx(vtxBase[nm]);
   std::vector<uint4> idx(triBase[nm]);
@@ -428,7 +438,7 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
   s->stats.triangles = triBase[nm];
   s->stats.instances = ni;
   s->stats.blas_nodes = nodeBase[nm];
-  s->stats.tlas_nodes = tlas.nodes.size();
+  s->stats.tlas_nodes = tlas4.nodes.size();
   s->stats.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   *out = guard.release();
   return ASUNA_OK;

@@ -61,7 +61,7 @@ int validateSceneDesc(const asuna_scene_desc* d) {
   for (uint32_t i = 0; i < d->num_materials; ++i) {
     uint32_t t = d->materials[i].type;
     if (t != ASUNA_MAT_LAMBERTIAN && t != ASUNA_MAT_ROUGH_PLASTIC && t != ASUNA_MAT_DIELECTRIC &&
-        t != ASUNA_MAT_EMISSIVE)
+        t != ASUNA_MAT_EMISSIVE && t != ASUNA_MAT_PLASTIC && t != ASUNA_MAT_MIRROR)
       return fail(ASUNA_ERR_UNSUPPORTED, "material %u: type %u is not implemented", i, t);
     const asuna_material& m = d->materials[i];
     if (m.diffuse_texture_id >= 0 || m.normal_texture_id >= 0 || m.roughness_texture_id >= 0 ||
@@ -962,6 +962,20 @@ int addMaterial(LoadCtx& L, const Json& mj) {
     if (mj.has("alpha")) REQUIRE(vecN(mj["alpha"], 2, m.aniso_alpha), "bad alpha");
     if ((rc = tex("alpha_texture", m.roughness_texture_id))) return rc;
     m.radiance[0] = asuna_diffuse_fresnel(m.ior, 1000);
+  } else if (t == "brdf_plastic") {
+    // src/loader/material.cpp:197-210
+    m.type = ASUNA_MAT_PLASTIC;
+    if (mj.has("ior")) m.ior = float(mj["ior"].num);
+    if (mj.has("diffuse_reflectance")) REQUIRE(vecN(mj["diffuse_reflectance"], 3, m.diffuse), "bad diffuse_reflectance");
+    if ((rc = tex("diffuse_texture", m.diffuse_texture_id)) || (rc = tex("normal_texture", m.normal_texture_id)))
+      return rc;
+    m.radiance[0] = asuna_diffuse_fresnel(m.ior, 1000);
+  } else if (t == "brdf_mirror") {
+    // src/loader/material.cpp:233-243
+    m.type = ASUNA_MAT_MIRROR;
+    if (mj.has("diffuse_reflectance")) REQUIRE(vecN(mj["diffuse_reflectance"], 3, m.diffuse), "bad diffuse_reflectance");
+    if ((rc = tex("diffuse_texture", m.diffuse_texture_id)) || (rc = tex("normal_texture", m.normal_texture_id)))
+      return rc;
   } else if (t == "brdf_emissive") {
     // src/loader/material.cpp:145-155
     m.type = ASUNA_MAT_EMISSIVE;
@@ -969,8 +983,8 @@ int addMaterial(LoadCtx& L, const Json& mj) {
     if (mj.has("radiance_factor")) REQUIRE(vecN(mj["radiance_factor"], 3, m.radiance_factor), "bad radiance_factor");
     if ((rc = tex("radiance_texture", m.radiance_texture_id))) return rc;
   } else {
-    static const char* known[] = {"brdf_pbr_metalness_roughness", "brdf_kang18", "brdf_plastic",
-                                  "brdf_mirror", "brdf_conductor", "brdf_rough_conductor", "brdf_disney", "brdf_phong"};
+    static const char* known[] = {"brdf_pbr_metalness_roughness", "brdf_kang18", "brdf_conductor",
+                                  "brdf_rough_conductor", "brdf_disney", "brdf_phong"};
     for (const char* k : known)
       if (t == k) return fail(ASUNA_ERR_UNSUPPORTED, "material type [%s] is not implemented", t.c_str());
     return fail(ASUNA_ERR_PARSE, "unrecognized material type [%s]", t.c_str());

@@ -17,7 +17,7 @@ struct KParams {
 
 constexpr int kTraceThreads = 128;
 constexpr int kTraceMinBlocks = 8;   // resident blocks per SM the traversal kernels are compiled for
-constexpr int kStackDepth = 64;      // traversal stack entries per ray
+constexpr int kStackDepth = 96;      // traversal stack entries per ray
 constexpr int kSharedStack = 24;     // of which in shared memory (the rest in local memory)
 constexpr int kRefillLanes = 8;      // idle lanes of a warp that trigger a queue fetch
 constexpr int kShadeMinBlocks = 3;   // resident 256-thread blocks per SM the shading kernel is compiled for

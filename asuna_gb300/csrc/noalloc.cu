@@ -11,7 +11,7 @@
 // stream.
 //
 // The array holds kNoAllocMaxPaths path slots (ASUNA_NOALLOC_MAX_PATHS =
-// 262,144, 196 bytes each, about 49 MiB in all); every GPU that loads this
+// 262,144, 220 bytes each, about 55 MiB in all); every GPU that loads this
 // library keeps it until the process exits.  A frame of more pixels than
 // that is rejected with ASUNA_ERR_INVALID.
 //
@@ -41,10 +41,11 @@ constexpr uint64_t kNoAllocMaxPaths = ASUNA_NOALLOC_MAX_PATHS;
 constexpr uint64_t kNoAllocMaxRanges = 64;
 
 constexpr uint64_t pad256(uint64_t b) { return (b + 255) / 256 * 256; }
-// scratch layout: 13 per-path arrays (12 x 16 B + 1 x 4 B), counters, shot, ranges
+// scratch layout: 19 per-path arrays (12 x 16 B, hit instances and the
+// shading-class lists 7 x 4 B), counters, shot, ranges
 constexpr uint64_t kPerPath16 = pad256(kNoAllocMaxPaths * 16);
 constexpr uint64_t kPerPath4 = pad256(kNoAllocMaxPaths * 4);
-constexpr uint64_t kOffCounters = 12 * kPerPath16 + kPerPath4;
+constexpr uint64_t kOffCounters = 12 * kPerPath16 + (1 + kNumShadeClasses) * kPerPath4;
 constexpr uint64_t kOffShot = kOffCounters + pad256(sizeof(DevCounters));
 constexpr uint64_t kOffRanges = kOffShot + pad256(sizeof(ShotDev));
 constexpr uint64_t kScratchBytes = kOffRanges + pad256(kNoAllocMaxRanges * sizeof(RangeDev));
@@ -126,6 +127,8 @@ int renderNoAlloc(const asuna_scene* s, const asuna_shot* shot, asuna_film* film
   W.info = reinterpret_cast<uint4*>(f16[10]);
   W.rec = reinterpret_cast<uint4*>(f16[11]);
   W.hitInst = reinterpret_cast<uint32_t*>(base + 12 * kPerPath16);
+  for (int k = 0; k < kNumShadeClasses; ++k)
+    W.cls[k] = reinterpret_cast<uint32_t*>(base + 12 * kPerPath16 + uint64_t(1 + k) * kPerPath4);
   W.cnt = reinterpret_cast<DevCounters*>(base + kOffCounters);
   ShotDev* dShot = reinterpret_cast<ShotDev*>(base + kOffShot);
   RangeDev* dRanges = reinterpret_cast<RangeDev*>(base + kOffRanges);

@@ -247,6 +247,33 @@ __device__ __forceinline__ void nextEvent(const SceneDev& S, const ShotDev& sh, 
       // (.., ax, ay, eta, ..); kept as written.
       w = rpEval(lRec.d, st.V, st.ffN, st.X, st.Y, kd, splat(1.0f), eta, fdrInt, ax, ay, invEta2, EArea);
       bpdf = rpPdf(lRec.d, st.V, st.ffN, st.X, st.Y, eta, ax, ay, ssw, lRec.flags);
+    } else if (type == ASUNA_MAT_PLASTIC) {
+      // brdf_plastic.rchit:43-61 eval with EArea, 63-84 pdf with lRec.flags
+      const float eta = m.b.z, fdrInt = m.b.w, invEta2 = 1.0f / (eta * eta);
+      const f3 kd = ld3(m.a);
+      const float dAvg = luminance(kd), sAvg = luminance(splat(1.0f));
+      const float ssw = sAvg / (dAvg + sAvg);
+      const f3 L = lRec.d, V = st.V, N = st.ffN;
+      const float NdotL = dot(L, N), NdotV = dot(V, N);
+      if (!(NdotL < 0.0f || NdotV < 0.0f)) {
+        float c0;
+        const float Fo = fresnelDielectricExt(NdotV, c0, eta);
+        float c1;
+        const float Fi = fresnelDielectricExt(NdotL, c1, eta);
+        f3 diff = kd;
+        diff = diff / (splat(1.0f) - diff * fdrInt);
+        w = (1.0f - Fi) * (1.0f - Fo) * diff * invEta2 * INV_PI * NdotL;
+        const float probSpecular = (Fo * ssw) / (Fo * ssw + (1.0f - Fo) * (1.0f - ssw));
+        if (lRec.flags & EDelta) {
+          if (fabsf(dot(reflect(-V, N), L) - 1.0f) < EPS) bpdf = probSpecular;
+        } else if (lRec.flags & EArea) {
+          bpdf = NdotL * (1.0f - probSpecular);  // no 1/pi, as in the reference
+        }
+      }
+    } else if (type == ASUNA_MAT_MIRROR) {
+      // brdf_mirror.rchit:12-26: eval is zero for area samples; pdf 1 on the
+      // mirror direction of a delta light
+      if ((lRec.flags & EDelta) && fabsf(dot(reflect(-st.V, st.ffN), lRec.d) - 1.0f) < EPS) bpdf = 1.0f;
     } else if (type == ASUNA_MAT_DIELECTRIC) {
       // eval() with EArea returns 0 (bsdf_dielectric.rchit:26-38); pdf 41-52
       const float ior = m.b.z;
@@ -274,7 +301,7 @@ __device__ __forceinline__ void nextEvent(const SceneDev& S, const ShotDev& sh, 
 }
 
 // BSDF sampling of the continuation ray: brdf_lambertian.rchit:31-42,136-151
-__device__ __noinline__ void sampleLambertian(PathIO& io, const HitSt& st, f3 kd) {
+__device__ __forceinline__ void sampleLambertian(PathIO& io, const HitSt& st, f3 kd) {
   f2 u = rnd2(io.seed);
   f3 wi = cosineSampleHemisphere(u);
   float pdf = cosineHemispherePdf(wi.z);
@@ -292,7 +319,7 @@ __device__ __noinline__ void sampleLambertian(PathIO& io, const HitSt& st, f3 kd
 }
 
 // brdf_rough_plastic.rchit:138-189,252-269
-__device__ __noinline__ void sampleRoughPlastic(PathIO& io, const HitSt& st, const MatDev& m) {
+__device__ __forceinline__ void sampleRoughPlastic(PathIO& io, const HitSt& st, const MatDev& m) {
   const float eta = m.b.z;
   const float fdrInt = m.b.w;
   const float invEta2 = 1.0f / (eta * eta);
@@ -355,8 +382,67 @@ __device__ __noinline__ void sampleRoughPlastic(PathIO& io, const HitSt& st, con
   io.thp = io.thp * (weight / (bpdf + EPS));
 }
 
+// brdf_plastic.rchit:86-120,187-205
+__device__ __forceinline__ void samplePlastic(PathIO& io, const HitSt& st, const MatDev& m) {
+  const float eta = m.b.z, fdrInt = m.b.w, invEta2 = 1.0f / (eta * eta);
+  const f3 kd = ld3(m.a);
+  const float dAvg = luminance(kd), sAvg = luminance(splat(1.0f));
+  const float ssw = sAvg / (dAvg + sAvg);
+  f2 u = rnd2(io.seed);
+  const f3 V = st.V, N = st.ffN, X = st.X, Y = st.Y;
+  f3 weight = splat(0.0f), bd = splat(0.0f);
+  float bpdf = 0.0f;
+  uint32_t bflags = EBsdfNull;
+  const float NdotV = dot(V, N);
+  if (NdotV > 0.0f) {
+    float c0;
+    const float Fo = fresnelDielectricExt(NdotV, c0, eta);
+    const float probSpecular = (Fo * ssw) / (Fo * ssw + (1.0f - Fo) * (1.0f - ssw));
+    if (u.x < probSpecular) {
+      bd = makeNormal(reflect(-V, N));
+      bflags = ESpecularReflection;
+      bpdf = probSpecular;
+      weight = splat(1.0f) * Fo;
+    } else {
+      u.x = (u.x - probSpecular) / (1.0f + EPS - probSpecular);
+      const f3 wi = cosineSampleHemisphere(u);
+      float c1;
+      const float Fi = fresnelDielectricExt(wi.z, c1, eta);
+      f3 diff = kd;
+      diff = diff / (splat(1.0f) - diff * fdrInt);
+      bpdf = (1.0f - probSpecular) * cosineHemispherePdf(wi.z);
+      bd = toWorld(X, Y, N, wi);
+      bflags = EDiffuseReflection;
+      weight = (1.0f - Fi) * (1.0f - Fo) * invEta2 * diff * INV_PI * fabsf(wi.z);
+    }
+  }
+  if (bpdf <= 0.0f || length(weight) == 0.0f) {
+    io.stop = true;
+    return;
+  }
+  io.bflags = bflags;
+  io.bpdf = bpdf;
+  io.nro = offsetPositionAlongNormal(st.pos, st.ffN);
+  io.nrd = bd;
+  io.thp = io.thp * (weight / (bpdf + EPS));
+}
+
+// brdf_mirror.rchit:28-37,88-106
+__device__ __forceinline__ void sampleMirror(PathIO& io, const HitSt& st, const MatDev& m) {
+  const f3 weight = ld3(m.a);
+  if (length(weight) == 0.0f) {
+    io.stop = true;
+    return;
+  }
+  io.bflags = ESpecularReflection;
+  io.bpdf = 1.0f;
+  io.nro = offsetPositionAlongNormal(st.pos, st.ffN);
+  io.nrd = reflect(-st.V, st.ffN);
+  io.thp = io.thp * (weight / 1.0f);
+}
+
 // bsdf_dielectric.rchit:54-72,273-289
-__device__ __noinline__ void sampleDielectric(PathIO& io, const HitSt& st, const MatDev& m) {
+__device__ __forceinline__ void sampleDielectric(PathIO& io, const HitSt& st, const MatDev& m) {
   const float ior = m.b.z;
   const float eta = dot(st.V, st.N) > 0.0f ? (1.0f / ior) : ior;
   float u = rnd(io.seed);
@@ -390,11 +476,13 @@ __device__ __noinline__ void sampleDielectric(PathIO& io, const HitSt& st, const
 }  // namespace
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256, kShadeMinBlocks) k_shade(KParams P) {
+// Splits the hits of the extend queue into the shading classes (material
+// sort): one warp-aggregated append per class and warp.  Classes that no hit
+// of a pass uses cost one empty launch.
+__global__ void __launch_bounds__(256) k_classify(KParams P) {
   const WaveDev& W = P.W;
   const SceneDev& S = P.S;
-  const int cur = P.cur, nxt = cur ^ 1;
-  const uint32_t n = W.cnt->c[kCntExtend0 + cur];
+  const uint32_t n = W.cnt->c[kCntExtend0 + P.cur];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     // the connect kernel that follows fetches shadow rays from 0
     W.cnt->c[kCntFetchShadow] = 0;
@@ -402,7 +490,45 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shade(KParams P) {
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
     const uint32_t i = i0 + threadIdx.x;
-    const bool valid = i < n;
+    int cls = -1;
+    if (i < n) {
+      const uint32_t inst = W.hitInst[i];
+      cls = kClsTerminal;
+      if (inst != 0xffffffffu) {
+        const InstDev& in = S.inst[inst];
+        if (__ldg(&in.lightId) < 0) {
+          const uint32_t type = __ldg(&in.matType);
+          cls = type == ASUNA_MAT_ROUGH_PLASTIC ? kClsRoughPlastic
+                : type == ASUNA_MAT_DIELECTRIC  ? kClsDielectric
+                : type == ASUNA_MAT_PLASTIC     ? kClsPlastic
+                : type == ASUNA_MAT_MIRROR      ? kClsMirror
+                : type == ASUNA_MAT_EMISSIVE    ? kClsTerminal
+                                                : kClsLambertian;
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kNumShadeClasses; ++k) {
+      const uint32_t slot = warpAppend(cls == k, &W.cnt->c[kCntCls0 + k]);
+      if (cls == k) W.cls[k][slot] = i;
+    }
+  }
+}
+
+// Shades the rays of one class: the miss shader, the light / emissive hit
+// shaders (class kClsTerminal), or one material's hit shader with its
+// next-event estimation and BSDF sampling.
+template <int CLS>
+__global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) {
+  const WaveDev& W = P.W;
+  const SceneDev& S = P.S;
+  const int cur = P.cur, nxt = cur ^ 1;
+  const uint32_t n = W.cnt->c[kCntCls0 + CLS];
+  const uint32_t* list = W.cls[CLS];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+    const bool valid = i0 + threadIdx.x < n;
+    const uint32_t i = valid ? list[i0 + threadIdx.x] : 0u;
     bool wantNext = false, wantShadow = false;
     PathIO io;
     uint32_t p = 0;
@@ -431,7 +557,7 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shade(KParams P) {
       io.stop = false;
       io.dskip = true;
       io.drad = splat(0.0f);
-      if (inst == 0xffffffffu) {
+      if (CLS == kClsTerminal && inst == 0xffffffffu) {
         // raytrace.default.rmiss:24-56
         io.stop = true;
         f3 env = (sh.state.has_env_map == 1u) ? evalEnvmap(S, sh, rd) : ld3(sh.state.bg_color);
@@ -447,7 +573,7 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shade(KParams P) {
         const uint32_t prim = __float_as_uint(h4.w);
         rc.x = sigMix(rc.x, (inst << 20) ^ prim);
         const HitSt st = hitState(S, in, prim, h4.y, h4.z, rd, sh.state.use_face_normal);
-        if (in.lightId >= 0) {
+        if (CLS == kClsTerminal && in.lightId >= 0) {
           // brdf_lambertian.rchit:44-68 (hitLight)
           const LightDev l = S.lights[in.lightId];
           f3 ldir = makeNormal(rd);
@@ -466,8 +592,7 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shade(KParams P) {
           }
         } else {
           const MatDev m = S.mats[in.matId];
-          const uint32_t type = in.matType;
-          if (depth == 1u && frame == 0u && sh.state.n_multi_channel > 0u && type == ASUNA_MAT_LAMBERTIAN) {
+          if (CLS == kClsLambertian && depth == 1u && frame == 0u && sh.state.n_multi_channel > 0u) {
             // brdf_lambertian.rchit:93-108
             const asuna_rt_state& ps = sh.state;
             float4* ch = sh.filmCh;
@@ -483,16 +608,25 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shade(KParams P) {
             put(ps.position_out_channel, st.pos);
             put(ps.uv_out_channel, f3{st.u, st.v, 1.0f});
           }
-          if (type == ASUNA_MAT_EMISSIVE) {
+          if (CLS == kClsTerminal) {
             // brdf_emissive.rchit:12-27: add the emitted radiance and stop
             io.stop = true;
             if (sh.state.ignore_emissive == 0u) io.rad = io.rad + ld3(m.a) * io.thp;
           } else {
+            constexpr uint32_t type = CLS == kClsRoughPlastic ? ASUNA_MAT_ROUGH_PLASTIC
+                                      : CLS == kClsDielectric ? ASUNA_MAT_DIELECTRIC
+                                      : CLS == kClsPlastic    ? ASUNA_MAT_PLASTIC
+                                      : CLS == kClsMirror     ? ASUNA_MAT_MIRROR
+                                                              : ASUNA_MAT_LAMBERTIAN;
             nextEvent(S, sh, io, st, m, type, rd);
-            if (type == ASUNA_MAT_ROUGH_PLASTIC)
+            if (CLS == kClsRoughPlastic)
               sampleRoughPlastic(io, st, m);
-            else if (type == ASUNA_MAT_DIELECTRIC)
+            else if (CLS == kClsDielectric)
               sampleDielectric(io, st, m);
+            else if (CLS == kClsPlastic)
+              samplePlastic(io, st, m);
+            else if (CLS == kClsMirror)
+              sampleMirror(io, st, m);
             else
               sampleLambertian(io, st, ld3(m.a));
           }
@@ -505,7 +639,7 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shade(KParams P) {
       }
       wantShadow = !io.dskip;
       bool alive = !io.stop && depth < uint32_t(sh.state.max_path_depth);
-      if (alive && (sh.flags & ASUNA_SHOT_RR) && depth >= sh.rrDepth) {
+      if (CLS != kClsTerminal && alive && (sh.flags & ASUNA_SHOT_RR) && depth >= sh.rrDepth) {
         // Russian roulette (extension; off for the reference's streams)
         float q = gmin(0.95f, gmax(io.thp.x, gmax(io.thp.y, io.thp.z)));
         float u = rnd(io.seed);
@@ -526,17 +660,19 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shade(KParams P) {
       if (P.records) W.rec[p] = rc;
     }
     __syncwarp();
-    const uint32_t sslot = warpAppend(wantShadow, &W.cnt->c[kCntShadow]);
-    const uint32_t nslot = warpAppend(wantNext, &W.cnt->c[kCntExtend0 + nxt]);
-    if (wantShadow) {
-      float maxDist = io.ddist - 2.0f * EPS;
-      W.shO[sslot] = make_float4(io.dro.x, io.dro.y, io.dro.z, maxDist);
-      W.shD[sslot] = make_float4(io.drd.x, io.drd.y, io.drd.z, __uint_as_float(p));
-      W.shC[sslot] = make_float4(io.drad.x, io.drad.y, io.drad.z, 0.0f);
-    }
-    if (wantNext) {
-      W.rayO[nxt][nslot] = make_float4(io.nro.x, io.nro.y, io.nro.z, INF);
-      W.rayD[nxt][nslot] = make_float4(io.nrd.x, io.nrd.y, io.nrd.z, __uint_as_float(p));
+    if (CLS != kClsTerminal) {  // terminal paths append nothing
+      const uint32_t sslot = warpAppend(wantShadow, &W.cnt->c[kCntShadow]);
+      const uint32_t nslot = warpAppend(wantNext, &W.cnt->c[kCntExtend0 + nxt]);
+      if (wantShadow) {
+        float maxDist = io.ddist - 2.0f * EPS;
+        W.shO[sslot] = make_float4(io.dro.x, io.dro.y, io.dro.z, maxDist);
+        W.shD[sslot] = make_float4(io.drd.x, io.drd.y, io.drd.z, __uint_as_float(p));
+        W.shC[sslot] = make_float4(io.drad.x, io.drad.y, io.drad.z, 0.0f);
+      }
+      if (wantNext) {
+        W.rayO[nxt][nslot] = make_float4(io.nro.x, io.nro.y, io.nro.z, INF);
+        W.rayD[nxt][nslot] = make_float4(io.nrd.x, io.nrd.y, io.nrd.z, __uint_as_float(p));
+      }
     }
   }
 }
@@ -593,10 +729,20 @@ __global__ void __launch_bounds__(256) k_records(KParams P, asuna_path_record* o
 
 // ---------------------------------------------------------------------------
 void launchRaygen(const KParams& P, int grid, cudaStream_t s) { k_raygen<<<grid, 256, 0, s>>>(P); }
-void launchShade(const KParams& P, int grid, cudaStream_t s) { k_shade<<<grid, 256, 0, s>>>(P); }
+// classify, then one kernel per shading class (each a persistent grid over
+// its own list)
+void launchShade(const KParams& P, int grid, cudaStream_t s) {
+  k_classify<<<grid, 256, 0, s>>>(P);
+  k_shadeClass<kClsTerminal><<<grid, 256, 0, s>>>(P);
+  k_shadeClass<kClsLambertian><<<grid, 256, 0, s>>>(P);
+  k_shadeClass<kClsRoughPlastic><<<grid, 256, 0, s>>>(P);
+  k_shadeClass<kClsDielectric><<<grid, 256, 0, s>>>(P);
+  k_shadeClass<kClsPlastic><<<grid, 256, 0, s>>>(P);
+  k_shadeClass<kClsMirror><<<grid, 256, 0, s>>>(P);
+}
 int shadeBlocksPerSm() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shade, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shadeClass<kClsRoughPlastic>, 256, 0);
   return n > 0 ? n : 1;
 }
 void launchAccumulate(const KParams& P, uint32_t maxPix, uint32_t nranges, cudaStream_t s) {

@@ -103,6 +103,7 @@ constexpr int32_t kDone = INT32_MIN + 1;               // stack empty: traversal
 constexpr int32_t kNoLeaf = INT32_MIN + 2;             // no postponed leaf
 constexpr uint32_t kTraceSpinCap = 1u << 20;           // inner steps of one warp pass
 constexpr uint32_t kTraceRayCap = 1u << 16;            // leaves + transitions of one ray
+constexpr float kMissT = 3.0e38f;                      // entry distance of a missed child
 
 __device__ __forceinline__ bool isLeafRef(int32_t r) { return r < 0 && r != kStackSentinel && r != kDone; }
 
@@ -163,32 +164,52 @@ struct Trav {
     return sp < kSharedStack ? sh[sp * kTraceThreads] : loc[sp - kSharedStack];
   }
 
+  // One 4-wide node: the four slab tests, the hit children sorted by entry
+  // distance (a 5-comparator network; misses sort last), the nearest one
+  // taken next and the others pushed far to near.
   template <bool COUNT>
   __device__ __forceinline__ void innerStep(const SceneDev& S, int32_t* sh, int32_t* loc, uint32_t& nNodes,
                                             bool& ovf) {
-    const BvhNode* n = S.nodes + ref;
-    const float4 xs = __ldg(&n->xs), ys = __ldg(&n->ys), zs = __ldg(&n->zs);
-    const int4 rr = __ldg(&n->ref);
+    const Bvh4Child* cc = S.nodes[ref].c;
     if (COUNT) ++nNodes;
-    const float tx0 = (xs.x - o.x) * id.x, tx1 = (xs.y - o.x) * id.x;
-    const float ty0 = (ys.x - o.y) * id.y, ty1 = (ys.y - o.y) * id.y;
-    const float tz0 = (zs.x - o.z) * id.z, tz1 = (zs.y - o.z) * id.z;
-    const float ux0 = (xs.z - o.x) * id.x, ux1 = (xs.w - o.x) * id.x;
-    const float uy0 = (ys.z - o.y) * id.y, uy1 = (ys.w - o.y) * id.y;
-    const float uz0 = (zs.z - o.z) * id.z, uz1 = (zs.w - o.z) * id.z;
-    const float a0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-    const float a1 = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), best)) * kFarScale;
-    const float b0 = fmaxf(fmaxf(fminf(ux0, ux1), fminf(uy0, uy1)), fmaxf(fminf(uz0, uz1), tmin));
-    const float b1 = fminf(fminf(fmaxf(ux0, ux1), fmaxf(uy0, uy1)), fminf(fmaxf(uz0, uz1), best)) * kFarScale;
-    const bool h0 = a0 <= a1, h1 = b0 <= b1;
-    if (h0 && h1) {
-      const bool swap = b0 < a0;
-      push(sh, loc, swap ? rr.x : rr.y, ovf);
-      ref = swap ? rr.y : rr.x;
-    } else if (h0 || h1) {
-      ref = h0 ? rr.x : rr.y;
-    } else {
+    // child k's box test; its reference comes back in r
+    auto slab = [&](int k, int32_t& r) {
+      const float4 a = __ldg(&cc[k].a), b = __ldg(&cc[k].b);
+      r = __float_as_int(b.z);
+      const float tx0 = (a.x - o.x) * id.x, tx1 = (a.w - o.x) * id.x;
+      const float ty0 = (a.y - o.y) * id.y, ty1 = (b.x - o.y) * id.y;
+      const float tz0 = (a.z - o.z) * id.z, tz1 = (b.y - o.z) * id.z;
+      const float a0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+      const float a1 = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), best)) * kFarScale;
+      return a0 <= a1 ? a0 : kMissT;
+    };
+    int32_t r0, r1, r2, r3;
+    float t0 = slab(0, r0);
+    float t1 = slab(1, r1);
+    float t2 = slab(2, r2);
+    float t3 = slab(3, r3);
+    auto cswap = [](float& ta, int32_t& ra, float& tb, int32_t& rb) {
+      if (tb < ta) {
+        const float t = ta;
+        ta = tb;
+        tb = t;
+        const int32_t r = ra;
+        ra = rb;
+        rb = r;
+      }
+    };
+    cswap(t0, r0, t1, r1);
+    cswap(t2, r2, t3, r3);
+    cswap(t0, r0, t2, r2);
+    cswap(t1, r1, t3, r3);
+    cswap(t1, r1, t2, r2);
+    if (t0 == kMissT) {
       ref = popOrDone(sh, loc);
+    } else {
+      if (t3 != kMissT) push(sh, loc, r3, ovf);
+      if (t2 != kMissT) push(sh, loc, r2, ovf);
+      if (t1 != kMissT) push(sh, loc, r1, ovf);
+      ref = r0;
     }
     if (inBlas && leaf == kNoLeaf && isLeafRef(ref)) {
       leaf = ref;  // postpone: test it together with the other lanes' leaves
@@ -389,6 +410,7 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_trace(KParam
       W.cnt->extendRays += src.count;
       W.cnt->c[kCntExtend0 + (cur ^ 1)] = 0;  // shade appends into the other queue
       W.cnt->c[kCntShadow] = 0;
+      for (int k = 0; k < kNumShadeClasses; ++k) W.cnt->c[kCntCls0 + k] = 0;  // classify appends
     }
   }
   uint32_t nNodes = 0, nTris = 0;

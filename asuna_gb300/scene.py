@@ -104,6 +104,22 @@ class SceneBuilder:
         m.radiance[0] = lib().asuna_diffuse_fresnel(C.c_float(ior), 1000)
         return self._add_material(name, m)
 
+    def add_plastic(self, name, diffuse, ior=1.5):
+        """brdf_plastic (src/loader/material.cpp:197-210): smooth coating over a diffuse base."""
+        m = default_material()
+        m.type = A.MAT_PLASTIC
+        m.diffuse = A.f3(*diffuse)
+        m.ior = ior
+        m.radiance[0] = lib().asuna_diffuse_fresnel(C.c_float(ior), 1000)
+        return self._add_material(name, m)
+
+    def add_mirror(self, name, reflectance=(1.0, 1.0, 1.0)):
+        """brdf_mirror (src/loader/material.cpp:233-243)."""
+        m = default_material()
+        m.type = A.MAT_MIRROR
+        m.diffuse = A.f3(*reflectance)
+        return self._add_material(name, m)
+
     def add_dielectric(self, name, ior=1.5):
         m = default_material()
         m.type = A.MAT_DIELECTRIC

@@ -228,7 +228,8 @@ def mixed_shot(b, width, height, frames, max_depth=12, rr_depth=3, channels=("al
 def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=False, seed=11,
                  channels=("albedo", "normal", "depth", "position", "uv", "tangent", "roughness")):
     """Every implemented plugin in one small scene: Lambertian, anisotropic
-    rough plastic and dielectric spheres on a ground quad; a single-sided rect
+    rough plastic, dielectric, smooth plastic and mirror spheres and an
+    emissive cuboid on a ground quad; a single-sided rect
     light, a double-sided JSON "triangle" light (rect with half area), a mesh
     triangle light, a point light and a distant light; an optional lognormal
     environment map (else a background colour); a thin-lens perspective or an
@@ -248,6 +249,8 @@ def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=Fa
     rp = b.add_rough_plastic("plastic", (0.2, 0.4, 0.8), (0.2, 0.5), 1.5)
     di = b.add_dielectric("glass", 1.5)
     em = b.add_emissive("lamp", (3.0, 1.5, 0.5))
+    sp = b.add_plastic("smooth_plastic", (0.7, 0.65, 0.1), 1.6)
+    mi = b.add_mirror("mirror", (0.9, 0.9, 0.95))
     v, i = cuboid_mesh(0.15, 0.15, 0.15)
     b.add_mesh("lamp", v, i)
     b.add_instance("lamp", em, rot_y(30.0, (0.6, -0.85, 1.2)))
@@ -258,9 +261,10 @@ def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=Fa
     b.add_instance("ground", g)
     base_v, faces = icosphere(3)
     idx = faces.astype(np.uint32).reshape(-1)
-    for k, (mat, pos) in enumerate([(lam, (-1.3, -0.2, 0.0)), (rp, (0.0, -0.1, -0.6)), (di, (1.2, -0.2, 0.3))]):
+    spheres = [(lam, (-1.3, -0.2, 0.0), 0.8), (rp, (0.0, -0.1, -0.6), 0.8), (di, (1.2, -0.2, 0.3), 0.8),
+               (sp, (-0.4, -0.6, 1.1), 0.4), (mi, (0.75, -0.62, 1.3), 0.38)]
+    for k, (mat, pos, s) in enumerate(spheres):
         b.add_mesh(f"s{k}", displaced_sphere(base_v, faces, seed + k, amplitude=0.05), idx)
-        s = 0.8
         b.add_instance(f"s{k}", mat, np.array([[s, 0, 0, pos[0]], [0, s, 0, pos[1]], [0, 0, s, pos[2]]], np.float32))
     state, depth = b.state(spp=frames, max_path_depth=max_depth, channels=channels, bg_color=(0.2, 0.25, 0.3))
     eye, at = (0.0, 1.0, 5.0), (0.0, -0.3, 0.0)

@@ -12,7 +12,7 @@ Metric: Mrays/s = (camera + continuation + occlusion rays traced) / time.
 `value` is device time of K steps (CUDA events on the library's stream);
 `e2e` is wall time of the same steps through the C ABI with the film read
 back to pinned host memory every step.  `roofline` is the closest-hit
-traversal kernel: algorithmic bytes = BVH nodes x 64 B + triangles x 48 B per
+traversal kernel: algorithmic bytes = 4-wide BVH nodes x 128 B + triangles x 48 B per
 ray (counted by a separate instrumented frame), over its event-timed
 duration, against the measured HBM copy bandwidth.
 
@@ -192,7 +192,7 @@ def run(args):
         if rank == 0 and args.verbose:
             print(f"autotune: {tuned}", file=sys.stderr, flush=True)
     else:
-        ctx.set_path_budget(args.frames_per_step * shot.width * shot.height * 196)
+        ctx.set_path_budget(args.frames_per_step * shot.width * shot.height * BYTES_PER_PATH)
     # per-rank frames: replicas render disjoint frames of the same shot
     from asuna_gb300 import replicas
 
@@ -208,8 +208,8 @@ def run(args):
     ctx.set_counters(True)
     cst = step(0)
     ctx.set_counters(False)
-    bytes_per_ext = (cst["nodes_visited"] * 64 + cst["tris_tested"] * 48) / max(cst["extend_rays"], 1)
-    bytes_per_sh = (cst["shadow_nodes_visited"] * 64 + cst["shadow_tris_tested"] * 48) / max(cst["shadow_rays"], 1)
+    bytes_per_ext = (cst["nodes_visited"] * NODE_BYTES + cst["tris_tested"] * 48) / max(cst["extend_rays"], 1)
+    bytes_per_sh = (cst["shadow_nodes_visited"] * NODE_BYTES + cst["shadow_tris_tested"] * 48) / max(cst["shadow_rays"], 1)
     for i in range(args.warmup):
         step(1 + i)
     if torch_dist:
@@ -265,9 +265,10 @@ def run(args):
         with open(tpath) as f:
             tj = json.load(f)
         traffic = tj.get("dram_bytes_per_ray", 0) * tot["extend_rays"] / max(tot["extend_launches"], 1)
-    # per wavefront: raygen + accumulate, and extend + shade + connect per depth
-    # (one wavefront per step: the path budget holds frames_per_step frames)
-    launches = int(tot["extend_launches"] * 2 + tot["connect_launches"] + 2 * args.steps)
+    # per wavefront: raygen + accumulate; per depth: extend, classify, four
+    # shading-class kernels, connect (one wavefront per step: the path budget
+    # holds frames_per_step frames)
+    launches = int(tot["extend_launches"] * 6 + tot["connect_launches"] + 2 * args.steps)
     line = {
         "metric": METRIC, "value": rays / (ms * 1e-3) / 1e6, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -353,7 +354,7 @@ def run_denoise_rmse(args):
     inf = dn.Denoiser(ctx, max_pixels=((H + 15) // 16 * 16) * ((W + 15) // 16 * 16))
     inf.set_params(den.get_params())
     del den
-    ctx.set_path_budget(16 * W * H * 196)
+    ctx.set_path_budget(16 * W * H * BYTES_PER_PATH)
     chunk = 16
 
     def render_frames(film, first, count, seed):
@@ -477,7 +478,69 @@ def run_serve(args):
     return 0
 
 
+def run_batch(args):
+    """Batched shots: 32 shots of the mixed recipe with 8 instances (2.6M
+    triangles) on a sphere of radius 15 around the origin, resolutions from
+    {256^2, 512^2, 1280x720, 1920x1080} and sample counts from {1, 4, 16, 64}
+    (seeded), depth 12; all shots in one asuna_render_batch call (one
+    wavefront per path budget, replayed as a CUDA graph) against the same
+    shots as 32 sequential asuna_render calls.  Device time of each, after
+    warm-up; Msamples/s and Mrays/s."""
+    import asuna_gb300 as ag
+    from asuna_gb300 import scenes
+
+    rng = np.random.default_rng(5)
+    b, _ = scenes.mixed_scene(64, 64, frames=1, n_spheres=8, level=7, seed=4321)
+    ctx = ag.Context(0)
+    scene = ctx.create_scene(b.desc())
+    res = [(256, 256), (512, 512), (1280, 720), (1920, 1080)]
+    shots, films = [], []
+    for k in range(32):
+        w, h = res[int(rng.integers(4))]
+        spp = int((1, 4, 16, 64)[int(rng.integers(4))])
+        z = float(rng.uniform(-1.0, 1.0))
+        a = float(rng.uniform(0.0, 2.0 * np.pi))
+        r = np.sqrt(1.0 - z * z)
+        eye = (15.0 * r * np.cos(a), 15.0 * z, 15.0 * r * np.sin(a))
+        shots.append(scenes.mixed_shot(b, w, h, spp, eye=eye, at=(0.0, 0.0, 0.0), seed=k))
+        films.append(ctx.create_film(w, h))
+    samples = sum(s.width * s.height * s.frames for s in shots)
+
+    def batched():
+        return ctx.render_batch(scene, shots, films, stats=True)
+
+    def sequential():
+        tot = {"ms_total": 0.0, "extend_rays": 0, "shadow_rays": 0}
+        for s, f in zip(shots, films):
+            st = ctx.render(scene, s, f, stats=True)
+            for k in tot:
+                tot[k] += st[k]
+        return tot
+
+    out = {}
+    for name, fn in (("sequential", sequential), ("batched", batched)):
+        for _ in range(args.warmup):
+            fn()
+        ms, rays = [], 0
+        for _ in range(args.steps):
+            st = fn()
+            ms.append(st["ms_total"])
+            rays = st["extend_rays"] + st["shadow_rays"]
+        m = float(np.median(ms))
+        out[name] = {"ms": m, "msamples_per_s": samples / (m * 1e-3) / 1e6, "mrays_per_s": rays / (m * 1e-3) / 1e6}
+    line = {"metric": "batched shots speed-up", "value": out["sequential"]["ms"] / out["batched"]["ms"],
+            "unit": "x", "higher_is_better": True, "n_gpus": 1, "data": "synthetic (seeded procedural scene)",
+            "config": {"workload": "32 shots, mixed recipe with 8 level-7 instances (2.6M triangles), radius-15 "
+                                   "sphere of cameras, 256^2..1920x1080, 1..64 spp, depth 12",
+                       "samples_per_call": samples, "steps": args.steps, "warmup": args.warmup},
+            **out}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 C_SHOT_BYTES = 340  # sizeof(asuna_shot): the only host->device input of a step
+NODE_BYTES = 128  # one 4-wide BVH node (a cache line)
+BYTES_PER_PATH = 220  # wavefront state per path slot (asuna_gb300/csrc/engine.cu)
 
 
 def main():
@@ -507,6 +570,7 @@ def main():
     ap.add_argument("--train-batch", type=int, default=16)
     ap.add_argument("--train-crop", type=int, default=128)
     ap.add_argument("--serve", action="store_true", help="serving loop: Poisson arrivals, latency percentiles")
+    ap.add_argument("--batch", action="store_true", help="32 batched shots vs 32 sequential calls")
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-requests", type=int, default=600)
     ap.add_argument("--serve-slots", type=int, default=2)
@@ -520,6 +584,8 @@ def main():
         return run_denoise_rmse(args)
     if args.serve:
         return run_serve(args)
+    if args.batch:
+        return run_batch(args)
     return run(args)
 
 

@@ -66,18 +66,18 @@ enum {
   ASUNA_LIGHT_POINT = 3,
   ASUNA_LIGHT_UNDEFINED = 4
 };
-/* MaterialType, src/shared/material.h:7-21 (the four marked (*) are
+/* MaterialType, src/shared/material.h:7-21 (the six marked (*) are
  * implemented; others are rejected with ASUNA_ERR_UNSUPPORTED) */
 enum {
   ASUNA_MAT_LAMBERTIAN = 0, /* (*) brdf_lambertian   */
   ASUNA_MAT_KANG18 = 1,
   ASUNA_MAT_EMISSIVE = 2, /* (*) brdf_emissive      */
   ASUNA_MAT_PBR_METALNESS_ROUGHNESS = 3,
-  ASUNA_MAT_PLASTIC = 4,
+  ASUNA_MAT_PLASTIC = 4, /* (*) brdf_plastic       */
   ASUNA_MAT_ROUGH_PLASTIC = 5, /* (*) brdf_rough_plastic */
   ASUNA_MAT_CONDUCTOR = 6,
   ASUNA_MAT_ROUGH_CONDUCTOR = 7,
-  ASUNA_MAT_MIRROR = 8,
+  ASUNA_MAT_MIRROR = 8, /* (*) brdf_mirror        */
   ASUNA_MAT_DISNEY = 9,
   ASUNA_MAT_DIELECTRIC = 10, /* (*) bsdf_dielectric    */
   ASUNA_MAT_PHONG = 11,
@@ -362,7 +362,7 @@ int asuna_scene_trace(asuna_ctx* ctx, const asuna_scene* scene, const float* ray
  * the allocator): renders shot->frames frames of one shot into `film` like
  * asuna_render, on `stream` (a cudaStream_t; NULL = default stream), with
  * all scratch in one fixed device array compiled into the library.  The
- * array holds ASUNA_NOALLOC_MAX_PATHS path slots (about 49 MiB, kept by
+ * array holds ASUNA_NOALLOC_MAX_PATHS path slots (about 55 MiB, kept by
  * every GPU that loads the library until exit); a frame with more pixels is
  * rejected with ASUNA_ERR_INVALID.  The array's address is set up on a
  * device by the first call there: make that call before any stream capture.

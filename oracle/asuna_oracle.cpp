@@ -1135,6 +1135,139 @@ template <class R> void shadeDielectric(const Scene& s, const asuna_shot& sh, Pa
   p.throughput = p.throughput * (weight / (bpdf + K<R>::EPS));
 }
 
+// brdf_plastic.rchit:43-61 (eval; the same fresnelDielectricExt as rough plastic)
+template <class R>
+V3<R> plEval(V3<R> L, V3<R> V, V3<R> N, V3<R> kd, R eta, R fdrInt, R invEta2, uint32_t flags) {
+  V3<R> weight = splat(R(0));
+  R NdotL = dot(L, N), NdotV = dot(V, N);
+  if (NdotL < R(0) || NdotV < R(0)) return weight;
+  R c0;
+  R Fo = fresnelDielectricExt(NdotV, c0, eta);
+  const bool hasSpecular = (flags & EDelta) != 0, hasDiffuse = (flags & EArea) != 0;
+  if (hasSpecular) {
+    if (std::fabs(dot(reflect(-V, N), L) - R(1)) < K<R>::EPS) weight = Fo * splat(R(1));
+  } else if (hasDiffuse) {
+    R c1;
+    R Fi = fresnelDielectricExt(NdotL, c1, eta);
+    V3<R> diff = kd;
+    diff = diff / (splat(R(1)) - diff * fdrInt);
+    weight = (R(1) - Fi) * (R(1) - Fo) * diff * invEta2 * K<R>::INV_PI * NdotL;
+  }
+  return weight;
+}
+// 63-84
+template <class R> R plPdf(V3<R> L, V3<R> V, V3<R> N, R eta, R ssw, uint32_t flags) {
+  R pdf = R(0);
+  R NdotL = dot(L, N), NdotV = dot(V, N);
+  if (NdotL < R(0) || NdotV < R(0)) return pdf;
+  R c0;
+  R Fo = fresnelDielectricExt(NdotV, c0, eta);
+  const bool hasSpecular = (flags & EDelta) != 0, hasDiffuse = (flags & EArea) != 0;
+  R probSpecular = (Fo * ssw) / (Fo * ssw + (R(1) - Fo) * (R(1) - ssw));
+  if (hasSpecular) {
+    if (std::fabs(dot(reflect(-V, N), L) - R(1)) < K<R>::EPS) pdf = probSpecular;
+  } else if (hasDiffuse) {
+    pdf = NdotL * (R(1) - probSpecular);  // no 1/pi, as in the reference
+  }
+  return pdf;
+}
+
+// brdf_plastic.rchit:122-205 (main) with sampleBsdf 86-120
+template <class R> void shadePlastic(const Scene& s, const asuna_shot& sh, PathState<R>& p, HitState<R>& st) {
+  R eta = R(st.mat.ior);
+  R fdrInt = R(st.mat.radiance[0]);
+  V3<R> kd = L3<R>(st.mat.diffuse);
+  R dAvg = luminance(kd), sAvg = luminance(splat(R(1)));
+  R ssw = sAvg / (dAvg + sAvg);
+  R invEta2 = R(1) / (eta * eta);
+  {
+    bool visible;
+    LRec<R> lRec;
+    V3<R> Ld = splat(R(0));
+    V3<R> rad = sampleLights<R>(s, sh, p, st.pos, st.ffN, visible, lRec);
+    if (visible) {
+      V3<R> w = plEval<R>(lRec.d, st.V, st.ffN, kd, eta, fdrInt, invEta2, EArea);
+      R bpdf = plPdf<R>(lRec.d, st.V, st.ffN, eta, ssw, lRec.flags);
+      R mis = powerHeuristic(lRec.pdf, bpdf);
+      Ld = Ld + mis * w * rad * p.throughput / (lRec.pdf + K<R>::EPS);
+    }
+    p.drad = Ld;
+    p.dskip = !visible;
+  }
+  V2<R> u = rnd2<R>(p.seed);
+  V3<R> V = st.V, N = st.ffN, X = st.X, Y = st.Y;
+  V3<R> weight = splat(R(0));
+  R bpdf = R(0);
+  uint32_t bflags = EBsdfNull;
+  V3<R> bd = splat(R(0));
+  R NdotV = dot(V, N);
+  if (NdotV > R(0)) {
+    R c0;
+    R Fo = fresnelDielectricExt(NdotV, c0, eta);
+    R probSpecular = (Fo * ssw) / (Fo * ssw + (R(1) - Fo) * (R(1) - ssw));
+    if (u.x < probSpecular) {
+      bd = makeNormal(reflect(-V, N));
+      bflags = ESpecularReflection;
+      bpdf = probSpecular;
+      weight = splat(R(1)) * Fo;
+    } else {
+      u.x = (u.x - probSpecular) / (R(1) + K<R>::EPS - probSpecular);
+      V3<R> wi = cosineSampleHemisphere(u);
+      R c1;
+      R Fi = fresnelDielectricExt(wi.z, c1, eta);
+      V3<R> diff = kd;
+      diff = diff / (splat(R(1)) - diff * fdrInt);
+      bpdf = (R(1) - probSpecular) * cosineHemispherePdf(wi.z);
+      bd = toWorld(X, Y, N, wi);
+      bflags = EDiffuseReflection;
+      weight = (R(1) - Fi) * (R(1) - Fo) * invEta2 * diff * K<R>::INV_PI * std::fabs(wi.z);
+    }
+  }
+  if (bpdf <= R(0) || length(weight) == R(0)) {
+    p.stop = true;
+    return;
+  }
+  p.bflags = bflags;
+  p.bpdf = bpdf;
+  p.ro = offsetPositionAlongNormal(st.pos, st.ffN);
+  p.rd = bd;
+  p.throughput = p.throughput * (weight / (bpdf + K<R>::EPS));
+}
+
+// brdf_mirror.rchit:40-106 (main): eval (12-19) is zero for area samples,
+// pdf (21-26) is 1 on the mirror direction of a delta light; sampleBsdf 28-37.
+template <class R> void shadeMirror(const Scene& s, const asuna_shot& sh, PathState<R>& p, HitState<R>& st) {
+  V3<R> kd = L3<R>(st.mat.diffuse);
+  {
+    bool visible;
+    LRec<R> lRec;
+    V3<R> Ld = splat(R(0));
+    V3<R> rad = sampleLights<R>(s, sh, p, st.pos, st.ffN, visible, lRec);
+    if (visible) {
+      V3<R> w = splat(R(0));
+      R bpdf = R(0);
+      if ((lRec.flags & EDelta) != 0 && std::fabs(dot(reflect(-st.V, st.ffN), lRec.d) - R(1)) < K<R>::EPS)
+        bpdf = R(1);
+      R mis = powerHeuristic(lRec.pdf, bpdf);
+      Ld = Ld + mis * w * rad * p.throughput / (lRec.pdf + K<R>::EPS);
+    }
+    p.drad = Ld;
+    p.dskip = !visible;
+  }
+  const R bpdf = R(1);
+  const V3<R> bd = reflect(-st.V, st.ffN);
+  const V3<R> weight = kd;
+  if (bpdf <= R(0) || length(weight) == R(0)) {
+    p.stop = true;
+    return;
+  }
+  p.bflags = ESpecularReflection;
+  p.bpdf = bpdf;
+  p.ro = offsetPositionAlongNormal(st.pos, st.ffN);
+  p.rd = bd;
+  p.throughput = p.throughput * (weight / bpdf);
+}
+
 struct PathOut {
   float rad[3];
   float fw;
@@ -1228,6 +1361,10 @@ void tracePath(const Scene& s, const asuna_shot& sh, uint32_t x, uint32_t y, uin
           shadeRoughPlastic<R>(s, sh, p, hs);
         else if (type == ASUNA_MAT_DIELECTRIC)
           shadeDielectric<R>(s, sh, p, hs);
+        else if (type == ASUNA_MAT_PLASTIC)
+          shadePlastic<R>(s, sh, p, hs);
+        else if (type == ASUNA_MAT_MIRROR)
+          shadeMirror<R>(s, sh, p, hs);
         else
           shadeLambertian<R>(s, sh, p, hs);
         p.sig = sigMix(p.sig, p.stop ? 0xfffu : p.bflags);

@@ -45,6 +45,8 @@ SHADERS = {
     "bxdf/raytrace.brdf_rough_plastic.rchit": "stage_rough_plastic",
     "bxdf/raytrace.bsdf_dielectric.rchit": "stage_dielectric",
     "bxdf/raytrace.brdf_emissive.rchit": "stage_emissive",
+    "bxdf/raytrace.brdf_plastic.rchit": "stage_plastic",
+    "bxdf/raytrace.brdf_mirror.rchit": "stage_mirror",
 }
 
 FLOAT_LIT = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")

@@ -90,6 +90,8 @@ static thread_local RayPayload payload;
 #include "raytrace.brdf_rough_plastic.rchit.h"
 #include "raytrace.bsdf_dielectric.rchit.h"
 #include "raytrace.brdf_emissive.rchit.h"
+#include "raytrace.brdf_plastic.rchit.h"
+#include "raytrace.brdf_mirror.rchit.h"
 }  // namespace glslx
 
 namespace {
@@ -159,6 +161,12 @@ void traceRayEXT(accelerationStructureEXT, uint, uint, uint, uint, uint, vec3 or
       break;
     case MaterialTypeBrdfEmissive:
       stage_emissive::main();
+      break;
+    case MaterialTypeBrdfPlastic:
+      stage_plastic::main();
+      break;
+    case MaterialTypeBrdfMirror:
+      stage_mirror::main();
       break;
     default:
       stage_lambertian::main();
