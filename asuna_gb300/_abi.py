@@ -17,6 +17,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_IO, ERR_PARSE, ERR_TIMEOUT, ERR_UNSUPPOR
 CAMERA_PERSPECTIVE, CAMERA_OPENCV = 0, 1
 LIGHT_DIRECTIONAL, LIGHT_RECT, LIGHT_TRIANGLE, LIGHT_POINT = 0, 1, 2, 3
 MAT_LAMBERTIAN, MAT_EMISSIVE, MAT_PLASTIC, MAT_ROUGH_PLASTIC, MAT_MIRROR, MAT_DIELECTRIC = 0, 2, 4, 5, 8, 10
+MAT_CONDUCTOR, MAT_ROUGH_CONDUCTOR = 6, 7
 CH_DIFFUSE, CH_NORMAL, CH_SPECULAR, CH_TANGENT, CH_ROUGHNESS, CH_POSITION, CH_UV, CH_DEPTH = range(8)
 SHOT_RR = 1
 NUM_OUTPUT_IMAGES = 9
@@ -130,6 +131,7 @@ SIGNATURES = [
     ("asuna_ctx_set_path_budget", C.c_int, [P, C.c_uint64]),
     ("asuna_ctx_set_launch", C.c_int, [P, C.c_int, C.c_int]),
     ("asuna_ctx_set_graphs", C.c_int, [P, C.c_int]),
+    ("asuna_ctx_set_traversal", C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int]),
     ("asuna_scene_create", C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(P)]),
     ("asuna_scene_destroy", C.c_int, [P]),
     ("asuna_scene_get_stats", C.c_int, [P, C.POINTER(SceneStats)]),
@@ -154,6 +156,7 @@ SIGNATURES = [
     ("asuna_camera_opencv", C.c_int, [C.POINTER(C.c_float)] * 4 + [C.POINTER(Camera)]),
     ("asuna_envmap_tables", C.c_int, [C.c_uint32, C.c_uint32, P, P, P]),
     ("asuna_diffuse_fresnel", C.c_float, [C.c_float, C.c_int]),
+    ("asuna_complex_ior", C.c_int, [C.c_char_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     ("asuna_tracer_run_offline", C.c_int, [P, C.c_char_p, C.c_char_p]),
     ("asuna_image_write", C.c_int, [C.c_char_p, C.c_uint32, C.c_uint32, P]),
     ("asuna_image_read", C.c_int, [C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), P, C.c_uint64]),

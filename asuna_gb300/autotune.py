@@ -9,19 +9,24 @@ caller's, so they never touch its sample streams.
 """
 import itertools
 
-BYTES_PER_PATH = 220  # wavefront state per path slot (asuna_gb300/csrc/engine.cu)
+BYTES_PER_PATH = 228  # wavefront state per path slot (asuna_gb300/csrc/engine.cu)
 
 
-def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16), trace_options=(0, 4, 6),
-         shade_options=(0, 2), memory_bytes=16 << 30, reps=2, frame_base=1 << 20):
-    """Returns {"frames": f, "trace_blocks_per_sm": t, "shade_blocks_per_sm": s, "mrays": best, "trials": [...]}
-    and leaves the context configured with the best choice."""
+def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32), trace_options=(0, 6),
+         shade_options=(0, 2), refill_options=(4, 8, 16), memory_bytes=24 << 30, reps=2, frame_base=1 << 20):
+    """Returns {"frames": f, "trace_blocks_per_sm": t, "shade_blocks_per_sm": s, "traversal": (refill
+    extend, refill shadow, speculate extend, speculate shadow), "mrays": best, "trials": [...]} and leaves
+    the context configured with the best choice.  Coordinate search: frames, then grids, then the
+    traversal refill thresholds and speculation of each pass."""
     npix = shot.width * shot.height
     saved = (shot.frame0, shot.frames)
     trials = []
     best = None
 
+    trav = [8, 8, 1, 1]
+
     def run(frames, t, s):
+        ctx.set_traversal(*trav)
         ctx.set_launch(t, s)
         ctx.set_path_budget(max(frames * npix * BYTES_PER_PATH, 1))
         shot.frames = frames
@@ -47,8 +52,19 @@ def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16), trace_options=
             trials.append({"frames": best["frames"], "trace": t, "shade": s, "mrays": v})
             if v > best["mrays"]:
                 best = {**best, "trace_blocks_per_sm": t, "shade_blocks_per_sm": s, "mrays": v}
+        best["traversal"] = tuple(trav)
+        # traversal: refill threshold, then speculation, of each pass in turn
+        for k in (1, 0):
+            for opt in [(k, r) for r in refill_options if r != 8] + [(k + 2, 0)]:
+                trav = list(best["traversal"])
+                trav[opt[0]] = opt[1]
+                v = run(best["frames"], best["trace_blocks_per_sm"], best["shade_blocks_per_sm"])
+                trials.append({"frames": best["frames"], "traversal": tuple(trav), "mrays": v})
+                if v > best["mrays"]:
+                    best = {**best, "traversal": tuple(trav), "mrays": v}
     finally:
         shot.frame0, shot.frames = saved
+    ctx.set_traversal(*best["traversal"])
     ctx.set_launch(best["trace_blocks_per_sm"], best["shade_blocks_per_sm"])
     ctx.set_path_budget(best["frames"] * npix * BYTES_PER_PATH)
     film.clear()

@@ -11,7 +11,6 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
-#include <cstring>
 
 namespace asuna {
 namespace {
@@ -234,89 +233,6 @@ bool buildBvh(const std::vector<Aabb>& boxes, const std::vector<float>& centroid
     stack.push_back({idx, 0, t.begin, m, t.depth + 1});
   }
   return true;
-}
-
-namespace {
-
-struct Child4 {
-  int32_t ref;
-  float lo[3], hi[3];
-};
-
-void binChild(const BvhNode& n, int side, Child4& c) {
-  c.ref = side == 0 ? n.ref.x : n.ref.y;
-  c.lo[0] = side == 0 ? n.xs.x : n.xs.z;
-  c.hi[0] = side == 0 ? n.xs.y : n.xs.w;
-  c.lo[1] = side == 0 ? n.ys.x : n.ys.z;
-  c.hi[1] = side == 0 ? n.ys.y : n.ys.w;
-  c.lo[2] = side == 0 ? n.zs.x : n.zs.z;
-  c.hi[2] = side == 0 ? n.zs.y : n.zs.w;
-}
-
-float halfArea(const Child4& c) {
-  const float dx = c.hi[0] - c.lo[0], dy = c.hi[1] - c.lo[1], dz = c.hi[2] - c.lo[2];
-  return dx * dy + dy * dz + dz * dx;
-}
-
-void setSlot(Bvh4Node& n, int k, const float lo[3], const float hi[3], int32_t ref) {
-  float rf;
-  std::memcpy(&rf, &ref, 4);
-  n.c[k].a = make_float4(lo[0], lo[1], lo[2], hi[0]);
-  n.c[k].b = make_float4(hi[1], hi[2], rf, 0.0f);
-}
-
-}  // namespace
-
-void collapseBvh4(const std::vector<BvhNode>& bin, Bvh4Out& out) {
-  out.nodes.clear();
-  out.maxPush = 0;
-  struct Work {
-    uint32_t src, dst, pushes;
-  };
-  std::vector<Work> stack;
-  out.nodes.emplace_back();
-  stack.push_back({0u, 0u, 0u});
-  while (!stack.empty()) {
-    const Work w = stack.back();
-    stack.pop_back();
-    Child4 kids[4];
-    int nk = 0;
-    const BvhNode& n = bin[w.src];
-    binChild(n, 0, kids[nk++]);
-    if (n.ref.y != kStackSentinel) binChild(n, 1, kids[nk++]);
-    while (nk < 4) {
-      int best = -1;
-      float bestA = -1.0f;
-      for (int i = 0; i < nk; ++i)
-        if (kids[i].ref >= 0 && halfArea(kids[i]) > bestA) {
-          bestA = halfArea(kids[i]);
-          best = i;
-        }
-      if (best < 0) break;
-      const BvhNode& m = bin[uint32_t(kids[best].ref)];
-      const bool two = m.ref.y != kStackSentinel;
-      binChild(m, 0, kids[best]);
-      if (two) binChild(m, 1, kids[nk++]);
-    }
-    out.maxPush = std::max(out.maxPush, w.pushes + uint32_t(nk - 1));
-    Bvh4Node node{};
-    const float far[3] = {1e30f, 1e30f, 1e30f};
-    for (int k = 0; k < 4; ++k) {
-      if (k >= nk) {
-        setSlot(node, k, far, far, kStackSentinel);
-        continue;
-      }
-      int32_t ref = kids[k].ref;
-      if (ref >= 0) {
-        const uint32_t idx = uint32_t(out.nodes.size());
-        out.nodes.emplace_back();
-        stack.push_back({uint32_t(kids[k].ref), idx, w.pushes + uint32_t(nk - 1)});
-        ref = int32_t(idx);
-      }
-      setSlot(node, k, kids[k].lo, kids[k].hi, ref);
-    }
-    out.nodes[w.dst] = node;
-  }
 }
 
 }  // namespace asuna

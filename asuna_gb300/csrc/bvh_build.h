@@ -26,15 +26,5 @@ struct BvhBuildOut {
 bool buildBvh(const std::vector<Aabb>& boxes, const std::vector<float>& centroids, int maxLeaf, uint32_t firstBase,
               BvhBuildOut& out);
 
-struct Bvh4Out {
-  std::vector<Bvh4Node> nodes;  // node 0 is the root; inner refs index `nodes`
-  uint32_t maxPush = 0;         // most stack entries one root-to-leaf walk can push
-};
-
-// Collapses a binary BVH (node 0 = root) into a 4-wide one: every 4-wide
-// node takes a binary node's children and keeps opening the inner child of
-// largest surface area until it holds four children or only leaves.  Leaf
-// refs are copied unchanged.
-void collapseBvh4(const std::vector<BvhNode>& bin, Bvh4Out& out);
 
 }  // namespace asuna

@@ -341,6 +341,26 @@ __device__ __forceinline__ float fresnelDielectricExt(float cosThetaI_, float& c
   return 0.5f * (Rs * Rs + Rp * Rp);
 }
 __device__ __forceinline__ float sqr(float x) { return x * x; }
+// Conductor Fresnel reflectance (P. Shirley, "Physically based lighting
+// calculations for computer graphics", 1991), brdf_conductor.rchit:14-36
+__device__ __forceinline__ float conductorReflectance(float eta, float k, float cosThetaI) {
+  const float cosThetaISq = cosThetaI * cosThetaI;
+  const float sinThetaISq = fmaxf(1.0f - cosThetaISq, 0.0f);
+  const float sinThetaIQu = sinThetaISq * sinThetaISq;
+  const float innerTerm = eta * eta - k * k - sinThetaISq;
+  const float aSqPlusBSq = sqrtf(fmaxf(innerTerm * innerTerm + 4.0f * eta * eta * k * k, 0.0f));
+  const float a = sqrtf(fmaxf((aSqPlusBSq + innerTerm) * 0.5f, 0.0f));
+  const float Rs = ((aSqPlusBSq + cosThetaISq) - (2.0f * a * cosThetaI)) /
+                   ((aSqPlusBSq + cosThetaISq) + (2.0f * a * cosThetaI));
+  const float Rp = ((cosThetaISq * aSqPlusBSq + sinThetaIQu) - (2.0f * a * cosThetaI * sinThetaISq)) /
+                   ((cosThetaISq * aSqPlusBSq + sinThetaIQu) + (2.0f * a * cosThetaI * sinThetaISq));
+  return 0.5f * (Rs + Rs * Rp);
+}
+__device__ __forceinline__ f3 conductorReflectance3(f3 eta, f3 k, float cosThetaI) {
+  return {conductorReflectance(eta.x, k.x, cosThetaI), conductorReflectance(eta.y, k.y, cosThetaI),
+          conductorReflectance(eta.z, k.z, cosThetaI)};
+}
+
 __device__ __forceinline__ float dAnisoGGX(float HdotN, float HdotX, float HdotY, float ax, float ay) {
   return 1.0f / (PI * ax * ay * sqr(sqr(HdotX / ax) + sqr(HdotY / ay) + sqr(HdotN)) + EPS);
 }

@@ -5,9 +5,7 @@
 // with 128-bit loads.
 #pragma once
 #include <cstdint>
-#include <cstring>
 
-#include <vector_functions.h>
 #include <vector_types.h>
 
 #include "../../include/asuna_rt.h"
@@ -25,27 +23,6 @@ struct __align__(16) BvhNode {
   int4 ref;   // c0, c1, unused, unused
 };
 static_assert(sizeof(BvhNode) == 64, "BvhNode is 64 bytes");
-
-// 4-wide BVH node, 128 B = one cache line: four 32-B child records, each
-// (lo.x, lo.y, lo.z, hi.x), (hi.y, hi.z, ref bits, unused) so a child's box
-// test needs only its own two 128-bit loads.  Child references use the
-// BvhNode encoding; an empty slot has a degenerate box at 1e30 and ref
-// kStackSentinel, so no box test ever selects it.  The traversal kernels
-// walk these nodes; they are collapsed from the binary builder's tree.
-struct __align__(16) Bvh4Child {
-  float4 a;  // lo.x, lo.y, lo.z, hi.x
-  float4 b;  // hi.y, hi.z, ref (int bits), 0
-};
-struct __align__(128) Bvh4Node {
-  Bvh4Child c[4];
-};
-inline int32_t bvh4Ref(const Bvh4Node& n, int k) {
-  int32_t r;
-  std::memcpy(&r, &n.c[k].b.z, 4);
-  return r;
-}
-inline void setBvh4Ref(Bvh4Node& n, int k, int32_t r) { std::memcpy(&n.c[k].b.z, &r, 4); }
-static_assert(sizeof(Bvh4Node) == 128, "Bvh4Node is 128 bytes");
 
 constexpr int kMaxLeafTris = 8;
 constexpr int32_t kStackSentinel = INT32_MIN;  // "leave the BLAS" marker
@@ -82,11 +59,15 @@ struct __align__(16) InstDev {
 };
 static_assert(sizeof(InstDev) == 128, "InstDev is 128 bytes");
 
-// Packed material, 32 B: (diffuse.xyz, type bits), (alpha.x, alpha.y, ior, fdrInt);
-// an emissive material holds its radiance in place of the diffuse albedo.
+// Packed material, 64 B: (diffuse.xyz, type bits), (alpha.x, alpha.y, ior,
+// fdrInt), (radiance.xyz, 0), (radiance_factor.xyz, 0); an emissive material
+// holds its radiance in place of the diffuse albedo; conductors keep eta in
+// radiance and k in radiance_factor, as the reference's loader does.
 struct __align__(16) MatDev {
   float4 a;
   float4 b;
+  float4 c;
+  float4 d;
 };
 
 // Packed light, 80 B: (position, type bits), (direction, radius),
@@ -101,7 +82,7 @@ struct __align__(16) LightDev {
 
 // Device view of one uploaded scene.
 struct SceneDev {
-  const Bvh4Node* nodes;  // all BLAS nodes, then the TLAS nodes (4-wide)
+  const BvhNode* nodes;  // all BLAS nodes, then the TLAS nodes
   const TriDev* tris;
   const VtxDev* vtx;
   const uint4* idx;  // mesh-local vertex indices (x, y, z), w unused
@@ -148,7 +129,7 @@ enum CounterSlot {
   kCntFetchExtend = 3,
   kCntFetchShadow = 4,
   kCntCls0 = 5,  // rays per shading class (kNumShadeClasses slots)
-  kCntNum32 = 12
+  kCntNum32 = 16
 };
 
 // Shading classes: the hits of an extend pass are split by what shades them,
@@ -160,7 +141,9 @@ enum ShadeClass {
   kClsDielectric = 3,
   kClsPlastic = 4,
   kClsMirror = 5,
-  kNumShadeClasses = 6
+  kClsConductor = 6,
+  kClsRoughConductor = 7,
+  kNumShadeClasses = 8
 };
 struct DevCounters {
   uint32_t c[kCntNum32];

@@ -195,6 +195,19 @@ int asuna_ctx_set_counters(asuna_ctx* c, int enable) {
   return ASUNA_OK;
 }
 
+int asuna_ctx_set_traversal(asuna_ctx* c, int refillExtend, int refillShadow, int specExtend, int specShadow) {
+  clearError();
+  if (!c) return fail(ASUNA_ERR_INVALID, "null context");
+  const int r[2] = {refillExtend, refillShadow}, sp[2] = {specExtend, specShadow};
+  for (int k = 0; k < 2; ++k) {
+    if (r[k] < 0 || r[k] > 32) return fail(ASUNA_ERR_INVALID, "refill lanes %d not in [0, 32]", r[k]);
+    if (sp[k] < -1 || sp[k] > 1) return fail(ASUNA_ERR_INVALID, "speculate %d not in {-1, 0, 1}", sp[k]);
+    c->refill[k] = r[k] == 0 ? uint32_t(kRefillLanes) : uint32_t(r[k]);
+    c->speculate[k] = sp[k] < 0 ? 1 : sp[k];
+  }
+  return ASUNA_OK;
+}
+
 int asuna_ctx_set_launch(asuna_ctx* c, int traceBlocks, int shadeBlocks) {
   if (!c) return fail(ASUNA_ERR_INVALID, "null context");
   const int tmax = traceBlocksPerSm(), smax = shadeBlocksPerSm();
@@ -239,7 +252,6 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
   }
   if (triBase[nm] > kMaxLeafFirst) return fail(ASUNA_ERR_UNSUPPORTED, "scene has more than 2^28 triangles");
   std::vector<BvhBuildOut> blas(nm);
-  std::vector<Bvh4Out> blas4(nm);
   std::vector<int> okMesh(nm, 1);
   {
     std::atomic<uint32_t> next{0};
@@ -262,7 +274,6 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
             }
           }
           okMesh[m] = buildBvh(boxes, cen, 4, triBase[m], blas[m]) ? 1 : 0;
-          if (okMesh[m]) collapseBvh4(blas[m].nodes, blas4[m]);
         }
       });
     for (auto& t : th) t.join();
@@ -270,21 +281,19 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
   for (uint32_t m = 0; m < nm; ++m)
     if (!okMesh[m]) return fail(ASUNA_ERR_UNSUPPORTED, "mesh %u: BVH cannot be encoded", m);
   std::vector<uint32_t> nodeBase(nm + 1, 0);
-  uint32_t blasPush = 0;
+  uint32_t blasDepth = 0;
   for (uint32_t m = 0; m < nm; ++m) {
-    nodeBase[m + 1] = nodeBase[m] + uint32_t(blas4[m].nodes.size());
-    blasPush = std::max(blasPush, blas4[m].maxPush);
+    nodeBase[m + 1] = nodeBase[m] + uint32_t(blas[m].nodes.size());
+    blasDepth = std::max(blasDepth, blas[m].maxDepth);
   }
-  std::vector<Bvh4Node> nodes;
-  nodes.reserve(nodeBase[nm] + d->num_instances + 2);
+  std::vector<BvhNode> nodes;
+  nodes.reserve(nodeBase[nm] + 2 * d->num_instances + 2);
   std::vector<TriDev> tris(triBase[nm]);
   for (uint32_t m = 0; m < nm; ++m) {
     const asuna_mesh_desc& md = d->meshes[m];
-    for (Bvh4Node n : blas4[m].nodes) {
-      for (int k = 0; k < 4; ++k) {
-        const int32_t r = bvh4Ref(n, k);
-        if (r >= 0) setBvh4Ref(n, k, r + int32_t(nodeBase[m]));
-      }
+    for (BvhNode n : blas[m].nodes) {
+      if (n.ref.x >= 0) n.ref.x += int32_t(nodeBase[m]);
+      if (n.ref.y >= 0) n.ref.y += int32_t(nodeBase[m]);
       nodes.push_back(n);
     }
     for (uint32_t i = 0; i < md.num_triangles; ++i) {
@@ -358,21 +367,21 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
   }
   BvhBuildOut tlas;
   if (!buildBvh(iboxes, icen, 1, 0, tlas)) return fail(ASUNA_ERR_UNSUPPORTED, "TLAS cannot be encoded");
-  Bvh4Out tlas4;
-  collapseBvh4(tlas.nodes, tlas4);
   const uint32_t tlasBase = uint32_t(nodes.size());
-  for (Bvh4Node n : tlas4.nodes) {
-    for (int k = 0; k < 4; ++k) {
-      const int32_t ref = bvh4Ref(n, k);
+  for (BvhNode n : tlas.nodes) {
+    for (int side = 0; side < 2; ++side) {
+      int32_t& ref = side == 0 ? n.ref.x : n.ref.y;
       if (ref == kStackSentinel) continue;
-      setBvh4Ref(n, k, ref >= 0 ? ref + int32_t(tlasBase) : encodeLeaf(ids[tlas.order[leafFirst(ref)]], 1));
+      if (ref >= 0)
+        ref += int32_t(tlasBase);
+      else
+        ref = encodeLeaf(ids[tlas.order[leafFirst(ref)]], 1);
     }
     nodes.push_back(n);
   }
-  // worst case of the traversal stack: TLAS pushes, the BLAS sentinel, BLAS pushes
-  if (tlas4.maxPush + 1 + blasPush > uint32_t(kStackDepth))
-    return fail(ASUNA_ERR_UNSUPPORTED, "BVH too deep for the traversal stack (TLAS %u + BLAS %u entries, limit %d)",
-                tlas4.maxPush, blasPush, kStackDepth - 1);
+  if (tlas.maxDepth + blasDepth + 1 > uint32_t(kStackDepth))
+    return fail(ASUNA_ERR_UNSUPPORTED, "BVH too deep for the traversal stack (TLAS %u + BLAS %u levels, limit %d)",
+                tlas.maxDepth, blasDepth, kStackDepth - 1);
   // ---- shading data ----
   std::vector<VtxDev> vtx(vtxBase[nm]);
   std::vector<uint4> idx(triBase[nm]);
@@ -395,6 +404,8 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
     const float* rgb = m.type == ASUNA_MAT_EMISSIVE ? m.radiance : m.diffuse;
     mats[i].a = make_float4(rgb[0], rgb[1], rgb[2], tb);
     mats[i].b = make_float4(m.aniso_alpha[0], m.aniso_alpha[1], m.ior, m.radiance[0]);
+    mats[i].c = make_float4(m.radiance[0], m.radiance[1], m.radiance[2], 0.0f);
+    mats[i].d = make_float4(m.radiance_factor[0], m.radiance_factor[1], m.radiance_factor[2], 0.0f);
   }
   std::vector<LightDev> lights(std::max(1u, d->num_lights));
   for (uint32_t i = 0; i < d->num_lights; ++i) {
@@ -438,7 +449,7 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
   s->stats.triangles = triBase[nm];
   s->stats.instances = ni;
   s->stats.blas_nodes = nodeBase[nm];
-  s->stats.tlas_nodes = tlas4.nodes.size();
+  s->stats.tlas_nodes = tlas.nodes.size();
   s->stats.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   *out = guard.release();
   return ASUNA_OK;
@@ -639,7 +650,8 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
     std::memcpy(key.data(), &s->view, sizeof(SceneDev));  // every scene pointer and size
     key.insert(key.end(), {uint64_t(uintptr_t(c->wave.base)), c->wave.capacity,
            uint64_t(uintptr_t(dShots)), uint64_t(uintptr_t(dRanges)), uint64_t(c->traceGrid), uint64_t(c->shadeGrid),
-           uint64_t(c->raygenGrid), uint64_t(c->counters), uint64_t(stats ? 1 : 0)});
+           uint64_t(c->raygenGrid), uint64_t(c->counters), uint64_t(stats ? 1 : 0), uint64_t(c->refill[0]),
+           uint64_t(c->refill[1]), uint64_t(c->speculate[0]), uint64_t(c->speculate[1])});
     for (const Batch& b : batches)
       key.insert(key.end(), {b.rangeBegin, b.rangeEnd, b.paths, b.maxPix, uint64_t(b.maxDepth)});
     for (auto& g : c->gcache)
@@ -683,8 +695,12 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
           evi += 2;
         }
       };
+      P.refillLanes = c->refill[0];
+      P.speculate = c->speculate[0];
       timedLaunch(0, [&] { launchExtend(P, c->traceGrid, c->stream); });
       timedLaunch(1, [&] { launchShade(P, c->shadeGrid, c->stream); });
+      P.refillLanes = c->refill[1];
+      P.speculate = c->speculate[1];
       timedLaunch(2, [&] { launchConnect(P, c->traceGrid, c->stream); });
       P.cur ^= 1;
     }

@@ -39,6 +39,9 @@ struct asuna_ctx {
   asuna::RangeDev* dRanges = nullptr;
   size_t rangesCap = 0;
   int graphs = 1;
+  // traversal settings of the extend [0] and connect [1] passes
+  uint32_t refill[2] = {8, 8};
+  int32_t speculate[2] = {1, 1};
   uint64_t useClock = 0;
   std::vector<GraphEntry> gcache;
 };

@@ -13,13 +13,15 @@ struct KParams {
   int32_t cur;     // extend queue holding this bounce's rays (0/1)
   int32_t records; // write per-path parity records
   int32_t counters;
+  uint32_t refillLanes;  // traversal: idle lanes of a warp that trigger a queue fetch
+  int32_t speculate;     // traversal: postponed leaves walk on speculatively
 };
 
 constexpr int kTraceThreads = 128;
 constexpr int kTraceMinBlocks = 8;   // resident blocks per SM the traversal kernels are compiled for
-constexpr int kStackDepth = 96;      // traversal stack entries per ray
+constexpr int kStackDepth = 64;      // traversal stack entries per ray
 constexpr int kSharedStack = 24;     // of which in shared memory (the rest in local memory)
-constexpr int kRefillLanes = 8;      // idle lanes of a warp that trigger a queue fetch
+constexpr int kRefillLanes = 8;      // default idle lanes of a warp that trigger a queue fetch
 constexpr int kShadeMinBlocks = 3;   // resident 256-thread blocks per SM the shading kernel is compiled for
 
 void launchRaygen(const KParams& P, int grid, cudaStream_t s);

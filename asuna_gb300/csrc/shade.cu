@@ -270,6 +270,30 @@ __device__ __forceinline__ void nextEvent(const SceneDev& S, const ShotDev& sh, 
           bpdf = NdotL * (1.0f - probSpecular);  // no 1/pi, as in the reference
         }
       }
+    } else if (type == ASUNA_MAT_CONDUCTOR) {
+      // brdf_conductor.rchit:38-63: eval is zero for area samples; pdf 1 on the
+      // mirror direction of a delta light (front side only)
+      const float NdotL = dot(lRec.d, st.ffN), NdotV = dot(st.V, st.ffN);
+      if (!(NdotL < 0.0f || NdotV < 0.0f) && (lRec.flags & EDelta) &&
+          fabsf(dot(reflect(-st.V, st.ffN), lRec.d) - 1.0f) < EPS)
+        bpdf = 1.0f;
+    } else if (type == ASUNA_MAT_ROUGH_CONDUCTOR) {
+      // brdf_rough_conductor.rchit:72-101 (Fresnel at N.L, as the reference)
+      const float ax = gmax(EPS, m.b.x), ay = gmax(EPS, m.b.y);
+      const f3 L = lRec.d, V = st.V, N = st.ffN, X = st.X, Y = st.Y;
+      const float NdotL = dot(L, N), NdotV = dot(V, N);
+      if (!(NdotL < 0.0f || NdotV < 0.0f)) {
+        const f3 H = makeNormal(L + V);
+        const f3 Fs = conductorReflectance3(ld3(m.c), ld3(m.d), NdotL);
+        float Gs = g1SmithAnisoGGX(NdotV, dot(V, X), dot(V, Y), ax, ay);
+        Gs = Gs * g1SmithAnisoGGX(NdotL, dot(L, X), dot(L, Y), ax, ay);
+        const float Ds = dAnisoGGX(dot(H, N), dot(H, X), dot(H, Y), ax, ay);
+        w = ld3(m.a) * Fs * Gs * Ds * NdotL;
+        if (lRec.flags & EArea) {
+          const f3 wi = toLocal(X, Y, N, L), wo = toLocal(X, Y, N, V);
+          bpdf = importanceAnisoGGXPdf(makeNormal(wi + wo), wo, ax, ay);
+        }
+      }
     } else if (type == ASUNA_MAT_MIRROR) {
       // brdf_mirror.rchit:12-26: eval is zero for area samples; pdf 1 on the
       // mirror direction of a delta light
@@ -427,6 +451,61 @@ __device__ __forceinline__ void samplePlastic(PathIO& io, const HitSt& st, const
   io.thp = io.thp * (weight / (bpdf + EPS));
 }
 
+// brdf_conductor.rchit:65-80,141-163: the direction sample ignores its two
+// random numbers but draws them
+__device__ __forceinline__ void sampleConductor(PathIO& io, const HitSt& st, const MatDev& m) {
+  rnd2(io.seed);
+  const f3 V = st.V, N = st.ffN;
+  if (!(dot(V, N) > 0.0f)) {
+    io.stop = true;
+    return;
+  }
+  const f3 bd = reflect(-V, N);
+  const f3 weight = ld3(m.a) * conductorReflectance3(ld3(m.c), ld3(m.d), dot(N, bd));
+  if (length(weight) == 0.0f) {
+    io.stop = true;
+    return;
+  }
+  io.bflags = ESpecularReflection;
+  io.bpdf = 1.0f;
+  io.nro = offsetPositionAlongNormal(st.pos, st.ffN);
+  io.nrd = bd;
+  io.thp = io.thp * (weight / (1.0f + EPS));
+}
+
+// brdf_rough_conductor.rchit:103-131,187-206
+__device__ __forceinline__ void sampleRoughConductor(PathIO& io, const HitSt& st, const MatDev& m) {
+  const float ax = gmax(EPS, m.b.x), ay = gmax(EPS, m.b.y);
+  f2 u = rnd2(io.seed);
+  const f3 V = st.V, N = st.ffN, X = st.X, Y = st.Y;
+  const float NdotV = dot(V, N);
+  if (NdotV <= 0.0f) {
+    io.stop = true;
+    return;
+  }
+  const f3 wo = toLocal(X, Y, N, V);
+  const f3 wi = importanceSampleAnisoGGX(u, wo, ax, ay);
+  const f3 L = toWorld(X, Y, N, wi);
+  const f3 H = makeNormal(V + L);
+  const f3 wh = makeNormal(wi + wo);
+  const float NdotL = dot(N, L);
+  const f3 Fs = conductorReflectance3(ld3(m.c), ld3(m.d), NdotL);
+  float Gs = g1SmithAnisoGGX(NdotV, dot(V, X), dot(V, Y), ax, ay);
+  Gs = Gs * g1SmithAnisoGGX(NdotL, dot(L, X), dot(L, Y), ax, ay);
+  const float Ds = dAnisoGGX(dot(H, N), dot(H, X), dot(H, Y), ax, ay);
+  const float bpdf = importanceAnisoGGXPdf(wh, wo, ax, ay);
+  const f3 weight = ld3(m.a) * Fs * Gs * Ds * NdotL;
+  if (bpdf <= 0.0f || length(weight) == 0.0f) {
+    io.stop = true;
+    return;
+  }
+  io.bflags = EGlossyReflection;
+  io.bpdf = bpdf;
+  io.nro = offsetPositionAlongNormal(st.pos, st.ffN);
+  io.nrd = L;
+  io.thp = io.thp * (weight / (bpdf + EPS));
+}
+
 // brdf_mirror.rchit:28-37,88-106
 __device__ __forceinline__ void sampleMirror(PathIO& io, const HitSt& st, const MatDev& m) {
   const f3 weight = ld3(m.a);
@@ -502,6 +581,8 @@ __global__ void __launch_bounds__(256) k_classify(KParams P) {
                 : type == ASUNA_MAT_DIELECTRIC  ? kClsDielectric
                 : type == ASUNA_MAT_PLASTIC     ? kClsPlastic
                 : type == ASUNA_MAT_MIRROR      ? kClsMirror
+                : type == ASUNA_MAT_CONDUCTOR   ? kClsConductor
+                : type == ASUNA_MAT_ROUGH_CONDUCTOR ? kClsRoughConductor
                 : type == ASUNA_MAT_EMISSIVE    ? kClsTerminal
                                                 : kClsLambertian;
         }
@@ -617,6 +698,8 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
                                       : CLS == kClsDielectric ? ASUNA_MAT_DIELECTRIC
                                       : CLS == kClsPlastic    ? ASUNA_MAT_PLASTIC
                                       : CLS == kClsMirror     ? ASUNA_MAT_MIRROR
+                                      : CLS == kClsConductor  ? ASUNA_MAT_CONDUCTOR
+                                      : CLS == kClsRoughConductor ? ASUNA_MAT_ROUGH_CONDUCTOR
                                                               : ASUNA_MAT_LAMBERTIAN;
             nextEvent(S, sh, io, st, m, type, rd);
             if (CLS == kClsRoughPlastic)
@@ -627,6 +710,10 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
               samplePlastic(io, st, m);
             else if (CLS == kClsMirror)
               sampleMirror(io, st, m);
+            else if (CLS == kClsConductor)
+              sampleConductor(io, st, m);
+            else if (CLS == kClsRoughConductor)
+              sampleRoughConductor(io, st, m);
             else
               sampleLambertian(io, st, ld3(m.a));
           }
@@ -739,6 +826,8 @@ void launchShade(const KParams& P, int grid, cudaStream_t s) {
   k_shadeClass<kClsDielectric><<<grid, 256, 0, s>>>(P);
   k_shadeClass<kClsPlastic><<<grid, 256, 0, s>>>(P);
   k_shadeClass<kClsMirror><<<grid, 256, 0, s>>>(P);
+  k_shadeClass<kClsConductor><<<grid, 256, 0, s>>>(P);
+  k_shadeClass<kClsRoughConductor><<<grid, 256, 0, s>>>(P);
 }
 int shadeBlocksPerSm() {
   int n = 0;

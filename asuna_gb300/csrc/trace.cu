@@ -83,6 +83,19 @@ __device__ __forceinline__ bool wtTri(const WT& w, float3 o, float4 p0, float4 p
   return true;
 }
 
+// Three-input min / max (one instruction each on sm_100 and later; exact,
+// like fminf / fmaxf, for the finite values the slab test produces).
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 __device__ __forceinline__ float3 safeInv(float3 d) {
   auto inv = [](float x) { return 1.0f / (fabsf(x) > 1e-30f ? x : copysignf(1e-30f, x)); };
   return make_float3(inv(d.x), inv(d.y), inv(d.z));
@@ -103,7 +116,6 @@ constexpr int32_t kDone = INT32_MIN + 1;               // stack empty: traversal
 constexpr int32_t kNoLeaf = INT32_MIN + 2;             // no postponed leaf
 constexpr uint32_t kTraceSpinCap = 1u << 20;           // inner steps of one warp pass
 constexpr uint32_t kTraceRayCap = 1u << 16;            // leaves + transitions of one ray
-constexpr float kMissT = 3.0e38f;                      // entry distance of a missed child
 
 __device__ __forceinline__ bool isLeafRef(int32_t r) { return r < 0 && r != kStackSentinel && r != kDone; }
 
@@ -164,52 +176,32 @@ struct Trav {
     return sp < kSharedStack ? sh[sp * kTraceThreads] : loc[sp - kSharedStack];
   }
 
-  // One 4-wide node: the four slab tests, the hit children sorted by entry
-  // distance (a 5-comparator network; misses sort last), the nearest one
-  // taken next and the others pushed far to near.
   template <bool COUNT>
   __device__ __forceinline__ void innerStep(const SceneDev& S, int32_t* sh, int32_t* loc, uint32_t& nNodes,
                                             bool& ovf) {
-    const Bvh4Child* cc = S.nodes[ref].c;
+    const BvhNode* n = S.nodes + ref;
+    const float4 xs = __ldg(&n->xs), ys = __ldg(&n->ys), zs = __ldg(&n->zs);
+    const int4 rr = __ldg(&n->ref);
     if (COUNT) ++nNodes;
-    // child k's box test; its reference comes back in r
-    auto slab = [&](int k, int32_t& r) {
-      const float4 a = __ldg(&cc[k].a), b = __ldg(&cc[k].b);
-      r = __float_as_int(b.z);
-      const float tx0 = (a.x - o.x) * id.x, tx1 = (a.w - o.x) * id.x;
-      const float ty0 = (a.y - o.y) * id.y, ty1 = (b.x - o.y) * id.y;
-      const float tz0 = (a.z - o.z) * id.z, tz1 = (b.y - o.z) * id.z;
-      const float a0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-      const float a1 = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), best)) * kFarScale;
-      return a0 <= a1 ? a0 : kMissT;
-    };
-    int32_t r0, r1, r2, r3;
-    float t0 = slab(0, r0);
-    float t1 = slab(1, r1);
-    float t2 = slab(2, r2);
-    float t3 = slab(3, r3);
-    auto cswap = [](float& ta, int32_t& ra, float& tb, int32_t& rb) {
-      if (tb < ta) {
-        const float t = ta;
-        ta = tb;
-        tb = t;
-        const int32_t r = ra;
-        ra = rb;
-        rb = r;
-      }
-    };
-    cswap(t0, r0, t1, r1);
-    cswap(t2, r2, t3, r3);
-    cswap(t0, r0, t2, r2);
-    cswap(t1, r1, t3, r3);
-    cswap(t1, r1, t2, r2);
-    if (t0 == kMissT) {
-      ref = popOrDone(sh, loc);
+    const float tx0 = (xs.x - o.x) * id.x, tx1 = (xs.y - o.x) * id.x;
+    const float ty0 = (ys.x - o.y) * id.y, ty1 = (ys.y - o.y) * id.y;
+    const float tz0 = (zs.x - o.z) * id.z, tz1 = (zs.y - o.z) * id.z;
+    const float ux0 = (xs.z - o.x) * id.x, ux1 = (xs.w - o.x) * id.x;
+    const float uy0 = (ys.z - o.y) * id.y, uy1 = (ys.w - o.y) * id.y;
+    const float uz0 = (zs.z - o.z) * id.z, uz1 = (zs.w - o.z) * id.z;
+    const float a0 = fmax3(fminf(tx0, tx1), fminf(ty0, ty1), fmaxf(fminf(tz0, tz1), tmin));
+    const float a1 = fmin3(fmaxf(tx0, tx1), fmaxf(ty0, ty1), fminf(fmaxf(tz0, tz1), best)) * kFarScale;
+    const float b0 = fmax3(fminf(ux0, ux1), fminf(uy0, uy1), fmaxf(fminf(uz0, uz1), tmin));
+    const float b1 = fmin3(fmaxf(ux0, ux1), fmaxf(uy0, uy1), fminf(fmaxf(uz0, uz1), best)) * kFarScale;
+    const bool h0 = a0 <= a1, h1 = b0 <= b1;
+    if (h0 && h1) {
+      const bool swap = b0 < a0;
+      push(sh, loc, swap ? rr.x : rr.y, ovf);
+      ref = swap ? rr.y : rr.x;
+    } else if (h0 || h1) {
+      ref = h0 ? rr.x : rr.y;
     } else {
-      if (t3 != kMissT) push(sh, loc, r3, ovf);
-      if (t2 != kMissT) push(sh, loc, r2, ovf);
-      if (t1 != kMissT) push(sh, loc, r1, ovf);
-      ref = r0;
+      ref = popOrDone(sh, loc);
     }
     if (inBlas && leaf == kNoLeaf && isLeafRef(ref)) {
       leaf = ref;  // postpone: test it together with the other lanes' leaves
@@ -292,8 +284,8 @@ struct Trav {
 // by one lane), commit(first, n) (called by every lane), load(i, tr) and
 // finish(i, tr).
 template <bool ANY, bool COUNT, bool SPEC, class Src>
-__device__ __forceinline__ void traceWarp(const SceneDev& S, Src& src, int32_t* sh, int32_t* loc, uint32_t& nNodes,
-                                          uint32_t& nTris, bool& ovf) {
+__device__ __forceinline__ void traceWarp(const SceneDev& S, Src& src, int32_t* sh, int32_t* loc, uint32_t refill,
+                                          uint32_t& nNodes, uint32_t& nTris, bool& ovf) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lanesBelow = (1u << lane) - 1u;
   bool active = false, drained = false;
@@ -301,7 +293,7 @@ __device__ __forceinline__ void traceWarp(const SceneDev& S, Src& src, int32_t* 
   Trav tr;
   for (;;) {
     const unsigned idle = __ballot_sync(0xffffffffu, !active);
-    if (idle && !drained && (__popc(idle) >= kRefillLanes || idle == 0xffffffffu)) {
+    if (idle && !drained && (uint32_t(__popc(idle)) >= refill || idle == 0xffffffffu)) {
       const int leader = __ffs(idle) - 1;
       uint32_t base = 0;
       if (int(lane) == leader) base = src.fetch(uint32_t(__popc(idle)));
@@ -387,7 +379,7 @@ struct QueueSrc {
   }
 };
 
-template <bool ANY, bool COUNT>
+template <bool ANY, bool COUNT, bool SPEC>
 __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_trace(KParams P) {
   __shared__ int32_t sstack[kSharedStack * kTraceThreads];
   int32_t lstack[kStackDepth - kSharedStack];
@@ -415,9 +407,9 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_trace(KParam
   }
   uint32_t nNodes = 0, nTris = 0;
   bool ovf = false;
-  // the instrumented variant walks without speculation, so its node counts
-  // are those of the ordered traversal
-  traceWarp<ANY, COUNT, !COUNT>(P.S, src, sh, lstack, nNodes, nTris, ovf);
+  // (the instrumented variant walks without speculation, so its node counts
+  // are those of the ordered traversal)
+  traceWarp<ANY, COUNT, SPEC>(P.S, src, sh, lstack, P.refillLanes, nNodes, nTris, ovf);
   if (ovf) atomicAdd(&W.cnt->stackOverflow, 1ull);
   if (COUNT) {
     const unsigned lane = threadIdx.x & 31u;
@@ -474,28 +466,32 @@ __global__ void __launch_bounds__(kTraceThreads) k_query(SceneDev S, const float
   uint32_t a = 0, b = 0;
   bool ovf = false;
   if (anyHit)
-    traceWarp<true, false, true>(S, src, sh, lstack, a, b, ovf);
+    traceWarp<true, false, true>(S, src, sh, lstack, kRefillLanes, a, b, ovf);
   else
-    traceWarp<false, false, true>(S, src, sh, lstack, a, b, ovf);
+    traceWarp<false, false, true>(S, src, sh, lstack, kRefillLanes, a, b, ovf);
 }
 
 }  // namespace
 
 void launchExtend(const KParams& P, int grid, cudaStream_t s) {
   if (P.counters)
-    k_trace<false, true><<<grid, kTraceThreads, 0, s>>>(P);
+    k_trace<false, true, false><<<grid, kTraceThreads, 0, s>>>(P);
+  else if (P.speculate)
+    k_trace<false, false, true><<<grid, kTraceThreads, 0, s>>>(P);
   else
-    k_trace<false, false><<<grid, kTraceThreads, 0, s>>>(P);
+    k_trace<false, false, false><<<grid, kTraceThreads, 0, s>>>(P);
 }
 void launchConnect(const KParams& P, int grid, cudaStream_t s) {
   if (P.counters)
-    k_trace<true, true><<<grid, kTraceThreads, 0, s>>>(P);
+    k_trace<true, true, false><<<grid, kTraceThreads, 0, s>>>(P);
+  else if (P.speculate)
+    k_trace<true, false, true><<<grid, kTraceThreads, 0, s>>>(P);
   else
-    k_trace<true, false><<<grid, kTraceThreads, 0, s>>>(P);
+    k_trace<true, false, false><<<grid, kTraceThreads, 0, s>>>(P);
 }
 int traceBlocksPerSm() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace<false, false>, kTraceThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace<false, false, true>, kTraceThreads, 0);
   return n > 0 ? n : 1;
 }
 void launchTraceQuery(const SceneDev& S, const float4* o, const float4* d, uint32_t n, int anyHit, float4* hit,

@@ -120,6 +120,19 @@ class SceneBuilder:
         m.diffuse = A.f3(*reflectance)
         return self._add_material(name, m)
 
+    def add_conductor(self, name, metal="Cu", reflectance=(0.0, 0.0, 0.0), alpha=None):
+        """brdf_conductor, or brdf_rough_conductor with `alpha` (src/loader/material.cpp:306-347):
+        the complex index of refraction of the named metal in radiance / radiance_factor.
+        The reflectance scale defaults to the reference's default albedo, 0
+        (a scene file without diffuse_reflectance renders the metal black)."""
+        m = default_material()
+        m.type = A.MAT_CONDUCTOR if alpha is None else A.MAT_ROUGH_CONDUCTOR
+        m.diffuse = A.f3(*reflectance)
+        check(lib().asuna_complex_ior(metal.encode(), m.radiance, m.radiance_factor))
+        if alpha is not None:
+            m.aniso_alpha = (C.c_float * 2)(*alpha)
+        return self._add_material(name, m)
+
     def add_dielectric(self, name, ior=1.5):
         m = default_material()
         m.type = A.MAT_DIELECTRIC
@@ -398,6 +411,10 @@ class Context:
 
     def set_graphs(self, on):
         check(lib().asuna_ctx_set_graphs(self.handle, 1 if on else 0))
+
+    def set_traversal(self, refill_extend=0, refill_shadow=0, speculate_extend=-1, speculate_shadow=-1):
+        check(lib().asuna_ctx_set_traversal(self.handle, int(refill_extend), int(refill_shadow),
+                                            int(speculate_extend), int(speculate_shadow)))
 
     def set_launch(self, trace_blocks_per_sm=0, shade_blocks_per_sm=0):
         check(lib().asuna_ctx_set_launch(self.handle, int(trace_blocks_per_sm), int(shade_blocks_per_sm)))

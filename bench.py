@@ -12,7 +12,7 @@ Metric: Mrays/s = (camera + continuation + occlusion rays traced) / time.
 `value` is device time of K steps (CUDA events on the library's stream);
 `e2e` is wall time of the same steps through the C ABI with the film read
 back to pinned host memory every step.  `roofline` is the closest-hit
-traversal kernel: algorithmic bytes = 4-wide BVH nodes x 128 B + triangles x 48 B per
+traversal kernel: algorithmic bytes = BVH nodes x 64 B + triangles x 48 B per
 ray (counted by a separate instrumented frame), over its event-timed
 duration, against the measured HBM copy bandwidth.
 
@@ -276,7 +276,8 @@ def run(args):
         "config": {**CONFIG, "width": shot.width, "height": shot.height, "parallelism": f"replicas{world}",
                    "frames_per_step": args.frames_per_step,
                    "autotune": None if tuned is None else {k: tuned[k] for k in
-                                                           ("frames", "trace_blocks_per_sm", "shade_blocks_per_sm")}},
+                                                           ("frames", "trace_blocks_per_sm", "shade_blocks_per_sm",
+                                                            "traversal")}},
         "msamples_per_s": tot["paths"] * world / (ms * 1e-3) / 1e6 if world == 1 else None,
         "rays_per_step": rays / args.steps,
         "instrumented_step": {"extend_rays": cst["extend_rays"], "shadow_rays": cst["shadow_rays"],
@@ -539,8 +540,8 @@ def run_batch(args):
 
 
 C_SHOT_BYTES = 340  # sizeof(asuna_shot): the only host->device input of a step
-NODE_BYTES = 128  # one 4-wide BVH node (a cache line)
-BYTES_PER_PATH = 220  # wavefront state per path slot (asuna_gb300/csrc/engine.cu)
+NODE_BYTES = 64  # one binary BVH node
+BYTES_PER_PATH = 228  # wavefront state per path slot (asuna_gb300/csrc/engine.cu)
 
 
 def main():

@@ -66,7 +66,7 @@ enum {
   ASUNA_LIGHT_POINT = 3,
   ASUNA_LIGHT_UNDEFINED = 4
 };
-/* MaterialType, src/shared/material.h:7-21 (the six marked (*) are
+/* MaterialType, src/shared/material.h:7-21 (the eight marked (*) are
  * implemented; others are rejected with ASUNA_ERR_UNSUPPORTED) */
 enum {
   ASUNA_MAT_LAMBERTIAN = 0, /* (*) brdf_lambertian   */
@@ -75,8 +75,8 @@ enum {
   ASUNA_MAT_PBR_METALNESS_ROUGHNESS = 3,
   ASUNA_MAT_PLASTIC = 4, /* (*) brdf_plastic       */
   ASUNA_MAT_ROUGH_PLASTIC = 5, /* (*) brdf_rough_plastic */
-  ASUNA_MAT_CONDUCTOR = 6,
-  ASUNA_MAT_ROUGH_CONDUCTOR = 7,
+  ASUNA_MAT_CONDUCTOR = 6, /* (*) brdf_conductor     */
+  ASUNA_MAT_ROUGH_CONDUCTOR = 7, /* (*) brdf_rough_conductor */
   ASUNA_MAT_MIRROR = 8, /* (*) brdf_mirror        */
   ASUNA_MAT_DISNEY = 9,
   ASUNA_MAT_DIELECTRIC = 10, /* (*) bsdf_dielectric    */
@@ -319,6 +319,12 @@ int asuna_ctx_set_graphs(asuna_ctx* ctx, int enable);
 /* Persistent-grid sizes in resident blocks per SM of the traversal and
  * shading kernels (0 = default, capped at the occupancy limit). */
 int asuna_ctx_set_launch(asuna_ctx* ctx, int trace_blocks_per_sm, int shade_blocks_per_sm);
+/* Traversal settings of the closest-hit (extend) and occlusion (shadow)
+ * passes: idle lanes of a warp that trigger a refill from the ray queue
+ * (1..32, 0 = default 8) and speculative walking past a postponed leaf
+ * (1 on, 0 off, -1 default on).  Results do not depend on them. */
+int asuna_ctx_set_traversal(asuna_ctx* ctx, int refill_extend, int refill_shadow, int speculate_extend,
+                            int speculate_shadow);
 
 /* ---- scene: upload + acceleration-structure build ------------------------ */
 /* Replaces Scene::submit + BLAS/TLAS build.  Host arrays are deep-copied; the
@@ -362,7 +368,7 @@ int asuna_scene_trace(asuna_ctx* ctx, const asuna_scene* scene, const float* ray
  * the allocator): renders shot->frames frames of one shot into `film` like
  * asuna_render, on `stream` (a cudaStream_t; NULL = default stream), with
  * all scratch in one fixed device array compiled into the library.  The
- * array holds ASUNA_NOALLOC_MAX_PATHS path slots (about 55 MiB, kept by
+ * array holds ASUNA_NOALLOC_MAX_PATHS path slots (about 57 MiB, kept by
  * every GPU that loads the library until exit); a frame with more pixels is
  * rejected with ASUNA_ERR_INVALID.  The array's address is set up on a
  * device by the first call there: make that call before any stream capture.
@@ -401,6 +407,10 @@ int asuna_envmap_tables(uint32_t width, uint32_t height, const float* rgba, floa
                         float* conditional_xy);
 /* Diffuse Fresnel reflectance fdrInt (src/loader/material.cpp:25-37). */
 float asuna_diffuse_fresnel(float ior, int sample_count);
+/* Complex index of refraction (eta, k at R, G, B) of a named conductor, as
+ * brdf_conductor / brdf_rough_conductor select it (complexIorListLookup,
+ * src/loader/material.cpp:290-300); ASUNA_ERR_PARSE for an unknown name. */
+int asuna_complex_ior(const char* name, float* eta, float* k);
 
 /* ---- render server (continuous batching) -------------------------------------
  * No counterpart in the reference (an addition for serving).  Requests on

@@ -1268,6 +1268,131 @@ template <class R> void shadeMirror(const Scene& s, const asuna_shot& sh, PathSt
   p.throughput = p.throughput * (weight / bpdf);
 }
 
+// brdf_conductor.rchit:14-36 (P. Shirley's conductor Fresnel)
+template <class R> R conductorReflectance(R eta, R k, R cosThetaI) {
+  R cosThetaISq = cosThetaI * cosThetaI;
+  R sinThetaISq = gmax(R(1) - cosThetaISq, R(0));
+  R sinThetaIQu = sinThetaISq * sinThetaISq;
+  R innerTerm = eta * eta - k * k - sinThetaISq;
+  R aSqPlusBSq = std::sqrt(gmax(innerTerm * innerTerm + R(4) * eta * eta * k * k, R(0)));
+  R a = std::sqrt(gmax((aSqPlusBSq + innerTerm) * R(0.5), R(0)));
+  R Rs = ((aSqPlusBSq + cosThetaISq) - (R(2) * a * cosThetaI)) / ((aSqPlusBSq + cosThetaISq) + (R(2) * a * cosThetaI));
+  R Rp = ((cosThetaISq * aSqPlusBSq + sinThetaIQu) - (R(2) * a * cosThetaI * sinThetaISq)) /
+         ((cosThetaISq * aSqPlusBSq + sinThetaIQu) + (R(2) * a * cosThetaI * sinThetaISq));
+  return R(0.5) * (Rs + Rs * Rp);
+}
+template <class R> V3<R> conductorReflectance3(V3<R> eta, V3<R> k, R c) {
+  return V3<R>{conductorReflectance(eta.x, k.x, c), conductorReflectance(eta.y, k.y, c),
+               conductorReflectance(eta.z, k.z, c)};
+}
+
+// brdf_conductor.rchit:83-164 (main), eval 38-51, pdf 53-63, sampleBsdf 65-80
+template <class R> void shadeConductor(const Scene& s, const asuna_shot& sh, PathState<R>& p, HitState<R>& st) {
+  V3<R> kd = L3<R>(st.mat.diffuse), eta = L3<R>(st.mat.radiance), k = L3<R>(st.mat.radiance_factor);
+  {
+    bool visible;
+    LRec<R> lRec;
+    V3<R> Ld = splat(R(0));
+    V3<R> rad = sampleLights<R>(s, sh, p, st.pos, st.ffN, visible, lRec);
+    if (visible) {
+      V3<R> w = splat(R(0));  // eval with EArea is zero
+      R bpdf = R(0);
+      R NdotL = dot(lRec.d, st.ffN), NdotV = dot(st.V, st.ffN);
+      if (!(NdotL < R(0) || NdotV < R(0) || ((lRec.flags & EDelta) == 0)))
+        if (std::fabs(dot(reflect(-st.V, st.ffN), lRec.d) - R(1)) < K<R>::EPS) bpdf = R(1);
+      R mis = powerHeuristic(lRec.pdf, bpdf);
+      Ld = Ld + mis * w * rad * p.throughput / (lRec.pdf + K<R>::EPS);
+    }
+    p.drad = Ld;
+    p.dskip = !visible;
+  }
+  rnd2<R>(p.seed);  // drawn and unused (sampleBsdf ignores u)
+  V3<R> weight = splat(R(0));
+  R bpdf = R(0);
+  V3<R> bd = splat(R(0));
+  if (dot(st.V, st.ffN) > R(0)) {
+    bd = reflect(-st.V, st.ffN);
+    bpdf = R(1);
+    weight = kd * conductorReflectance3(eta, k, dot(st.ffN, bd));
+  }
+  if (bpdf <= R(0) || length(weight) == R(0)) {
+    p.stop = true;
+    return;
+  }
+  p.bflags = ESpecularReflection;
+  p.bpdf = bpdf;
+  p.ro = offsetPositionAlongNormal(st.pos, st.ffN);
+  p.rd = bd;
+  p.throughput = p.throughput * (weight / (bpdf + K<R>::EPS));
+}
+
+// brdf_rough_conductor.rchit:133-206 (main), eval 72-88, pdf 90-101,
+// sampleBsdf 103-131; the Fresnel term is taken at N.L, as written there
+template <class R> void shadeRoughConductor(const Scene& s, const asuna_shot& sh, PathState<R>& p, HitState<R>& st) {
+  V3<R> kd = L3<R>(st.mat.diffuse), eta = L3<R>(st.mat.radiance), k = L3<R>(st.mat.radiance_factor);
+  R ax = gmax(R(st.mat.aniso_alpha[0]), K<R>::EPS);
+  R ay = gmax(R(st.mat.aniso_alpha[1]), K<R>::EPS);
+  V3<R> V = st.V, N = st.ffN, X = st.X, Y = st.Y;
+  {
+    bool visible;
+    LRec<R> lRec;
+    V3<R> Ld = splat(R(0));
+    V3<R> rad = sampleLights<R>(s, sh, p, st.pos, st.ffN, visible, lRec);
+    if (visible) {
+      V3<R> L = lRec.d;
+      V3<R> w = splat(R(0));
+      R NdotL = dot(L, N), NdotV = dot(V, N);
+      if (!(NdotL < R(0) || NdotV < R(0))) {
+        V3<R> H = makeNormal(L + V);
+        V3<R> Fs = conductorReflectance3(eta, k, NdotL);
+        R Gs = g1SmithAnisoGGX(NdotV, dot(V, X), dot(V, Y), ax, ay);
+        Gs = Gs * g1SmithAnisoGGX(NdotL, dot(L, X), dot(L, Y), ax, ay);
+        R Ds = dAnisoGGX(dot(H, N), dot(H, X), dot(H, Y), ax, ay);
+        w = w + kd * Fs * Gs * Ds * NdotL;
+      }
+      R bpdf = R(0);
+      if (!(NdotL < R(0) || NdotV < R(0) || ((lRec.flags & EArea) == 0))) {
+        V3<R> wi = toLocal(X, Y, N, L), wo = toLocal(X, Y, N, V);
+        V3<R> wh = makeNormal(wi + wo);
+        bpdf = importanceAnisoGGXPdf(wh, wo, ax, ay);
+      }
+      R mis = powerHeuristic(lRec.pdf, bpdf);
+      Ld = Ld + mis * w * rad * p.throughput / (lRec.pdf + K<R>::EPS);
+    }
+    p.drad = Ld;
+    p.dskip = !visible;
+  }
+  V2<R> u = rnd2<R>(p.seed);
+  V3<R> weight = splat(R(0));
+  R bpdf = R(0);
+  V3<R> bd = splat(R(0));
+  R NdotV = dot(V, N);
+  if (NdotV > R(0)) {
+    V3<R> wo = toLocal(X, Y, N, V);
+    V3<R> wi = importanceSampleAnisoGGX(u, wo, ax, ay);
+    V3<R> L = toWorld(X, Y, N, wi);
+    bd = L;
+    V3<R> H = makeNormal(V + L);
+    V3<R> wh = makeNormal(wi + wo);
+    R NdotL = dot(N, L);
+    V3<R> Fs = conductorReflectance3(eta, k, NdotL);
+    R Gs = g1SmithAnisoGGX(NdotV, dot(V, X), dot(V, Y), ax, ay);
+    Gs = Gs * g1SmithAnisoGGX(NdotL, dot(L, X), dot(L, Y), ax, ay);
+    R Ds = dAnisoGGX(dot(H, N), dot(H, X), dot(H, Y), ax, ay);
+    bpdf = importanceAnisoGGXPdf(wh, wo, ax, ay);
+    weight = kd * Fs * Gs * Ds * NdotL;
+  }
+  if (bpdf <= R(0) || length(weight) == R(0)) {
+    p.stop = true;
+    return;
+  }
+  p.bflags = EGlossyReflection;
+  p.bpdf = bpdf;
+  p.ro = offsetPositionAlongNormal(st.pos, st.ffN);
+  p.rd = bd;
+  p.throughput = p.throughput * (weight / (bpdf + K<R>::EPS));
+}
+
 struct PathOut {
   float rad[3];
   float fw;
@@ -1365,6 +1490,10 @@ void tracePath(const Scene& s, const asuna_shot& sh, uint32_t x, uint32_t y, uin
           shadePlastic<R>(s, sh, p, hs);
         else if (type == ASUNA_MAT_MIRROR)
           shadeMirror<R>(s, sh, p, hs);
+        else if (type == ASUNA_MAT_CONDUCTOR)
+          shadeConductor<R>(s, sh, p, hs);
+        else if (type == ASUNA_MAT_ROUGH_CONDUCTOR)
+          shadeRoughConductor<R>(s, sh, p, hs);
         else
           shadeLambertian<R>(s, sh, p, hs);
         p.sig = sigMix(p.sig, p.stop ? 0xfffu : p.bflags);

@@ -47,6 +47,8 @@ SHADERS = {
     "bxdf/raytrace.brdf_emissive.rchit": "stage_emissive",
     "bxdf/raytrace.brdf_plastic.rchit": "stage_plastic",
     "bxdf/raytrace.brdf_mirror.rchit": "stage_mirror",
+    "bxdf/raytrace.brdf_conductor.rchit": "stage_conductor",
+    "bxdf/raytrace.brdf_rough_conductor.rchit": "stage_rough_conductor",
 }
 
 FLOAT_LIT = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")

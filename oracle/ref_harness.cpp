@@ -92,6 +92,8 @@ static thread_local RayPayload payload;
 #include "raytrace.brdf_emissive.rchit.h"
 #include "raytrace.brdf_plastic.rchit.h"
 #include "raytrace.brdf_mirror.rchit.h"
+#include "raytrace.brdf_conductor.rchit.h"
+#include "raytrace.brdf_rough_conductor.rchit.h"
 }  // namespace glslx
 
 namespace {
@@ -167,6 +169,12 @@ void traceRayEXT(accelerationStructureEXT, uint, uint, uint, uint, uint, vec3 or
       break;
     case MaterialTypeBrdfMirror:
       stage_mirror::main();
+      break;
+    case MaterialTypeBrdfConductor:
+      stage_conductor::main();
+      break;
+    case MaterialTypeBrdfRoughConductor:
+      stage_rough_conductor::main();
       break;
     default:
       stage_lambertian::main();

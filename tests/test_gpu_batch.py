@@ -75,3 +75,20 @@ def test_graph_replay_equals_direct_launches(ctx):
         films.append(np.stack([f.read(i) for i in range(9)]))
     ctx.set_graphs(True)
     assert np.array_equal(films[0], films[1])
+
+
+def test_traversal_settings_do_not_change_results(ctx):
+    """Refill thresholds and speculative walking change the visiting order
+    only: closest hits (ties to the lowest instance / primitive) and
+    occlusion answers are the same, so films are bit-identical."""
+    b, shot = scenes.plugin_scene(64, 48, frames=2, max_depth=6)
+    scene = ctx.create_scene(b.desc())
+    films = []
+    for trav in ((8, 8, 1, 1), (1, 32, 0, 0), (32, 1, 1, 0), (4, 16, 0, 1)):
+        ctx.set_traversal(*trav)
+        f = ctx.create_film(64, 48)
+        ctx.render(scene, shot, f)
+        films.append(np.stack([f.read(i) for i in range(9)]))
+    ctx.set_traversal()
+    for f in films[1:]:
+        assert np.array_equal(films[0], f)

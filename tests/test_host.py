@@ -360,3 +360,38 @@ def test_hdr_envmap_reader(tmp_path):
     A.check(A.lib().asuna_image_read(str(tmp_path / "e.hdr").encode(), C.byref(ww), C.byref(hh), out.ctypes.data,
                                      out.size))
     assert np.allclose(out[..., :3], np.array([128, 64, 32]) * 2.0 ** (129 - 136))
+
+
+def test_json_material_plugins_match_builder():
+    """brdf_plastic, brdf_mirror, brdf_conductor and brdf_rough_conductor
+    parse into the same device structs as the builder (src/loader/material.cpp:
+    197-210, 233-243, 306-347); an unknown metal is a parse error."""
+    base = {"state": {}, "camera": {"type": "perspective", "film": {"resolution": [8, 8]}}, "meshes": [],
+            "instances": []}
+    mats = [{"type": "brdf_plastic", "name": "p", "diffuse_reflectance": [0.7, 0.65, 0.1], "ior": 1.6},
+            {"type": "brdf_mirror", "name": "m", "diffuse_reflectance": [0.9, 0.9, 0.95]},
+            {"type": "brdf_conductor", "name": "au", "material": "Au"},
+            {"type": "brdf_rough_conductor", "name": "al", "material": "Al", "diffuse_reflectance": [0.9, 0.9, 0.9],
+             "alpha": [0.15, 0.3]},
+            {"type": "brdf_conductor", "name": "cu"}]
+    js = ag.JsonScene(text=json.dumps({**base, "materials": mats}), base_dir=".")
+    d = js.desc().desc
+    b = ag.SceneBuilder()
+    b.add_plastic("p", (0.7, 0.65, 0.1), 1.6)
+    b.add_mirror("m", (0.9, 0.9, 0.95))
+    b.add_conductor("au", "Au")
+    b.add_conductor("al", "Al", (0.9, 0.9, 0.9), alpha=(0.15, 0.3))
+    b.add_conductor("cu")
+    assert d.num_materials == len(b.materials)
+    for k in range(1, d.num_materials):
+        assert bytes(d.materials[k]) == bytes(b.materials[k]), k
+    assert d.materials[1].type == A.MAT_PLASTIC and d.materials[1].radiance[0] == pytest.approx(
+        float(_np_fdr(1.6, 1000)), abs=0)
+    assert d.materials[3].type == A.MAT_CONDUCTOR and d.materials[4].type == A.MAT_ROUGH_CONDUCTOR
+    # gold: eta (0.1431, 0.3750, 1.4425), k (3.9832, 2.3857, 1.6032)
+    assert np.allclose(list(d.materials[3].radiance), [0.1431189557, 0.3749570432, 1.4424785571])
+    assert np.allclose(list(d.materials[3].radiance_factor), [3.9831604247, 2.3857207478, 1.6032152899])
+    with pytest.raises(ag.AsunaError) as e:
+        ag.JsonScene(text=json.dumps({**base, "materials": [{"type": "brdf_conductor", "name": "x",
+                                                             "material": "Unobtainium"}]}), base_dir=".")
+    assert e.value.code == A.ERR_PARSE
