@@ -7,5 +7,6 @@ assembly, cameras, shots, films and render calls.  There is no CPU fallback:
 without the native library or a CUDA device the calls raise ``AsunaError``.
 """
 from ._abi import AsunaError, lib  # noqa: F401
-from .scene import (Context, DeviceScene, Film, JsonScene, SceneBuilder, default_material, default_state,  # noqa: F401
+from .scene import (Context, DeviceScene, Film, JsonScene, SceneBuilder, default_material, default_post,  # noqa: F401
+                    default_state,
                     envmap_tables, make_shot, opencv_camera, perspective_camera, set_channels)

@@ -105,6 +105,17 @@ class RenderStats(C.Structure):
                 ("extend_launches", C.c_uint64), ("connect_launches", C.c_uint64)]
 
 
+class PostState(C.Structure):
+    """asuna_post_state = GpuPushConstantPost (src/shared/pushconstant.h:50-62)."""
+    _fields_ = [("brightness", C.c_float), ("contrast", C.c_float), ("saturation", C.c_float),
+                ("vignette", C.c_float), ("avg_lum", C.c_float), ("zoom", C.c_float),
+                ("rendering_ratio", C.c_float * 2), ("auto_exposure", C.c_int32), ("y_white", C.c_float),
+                ("key", C.c_float), ("tm_type", C.c_uint32)]
+
+
+TONEMAP_NONE, TONEMAP_GAMMA, TONEMAP_REINHARD, TONEMAP_ACES, TONEMAP_FILMIC, TONEMAP_PBRT, TONEMAP_CUSTOM = range(7)
+
+
 class DenoiserOpts(C.Structure):
     _fields_ = [("levels", C.c_uint32), ("channels", C.c_uint32 * 6), ("seed", C.c_uint64),
                 ("max_pixels", C.c_uint64), ("training", C.c_uint32), ("reserved", C.c_uint32)]
@@ -158,6 +169,9 @@ SIGNATURES = [
     ("asuna_diffuse_fresnel", C.c_float, [C.c_float, C.c_int]),
     ("asuna_complex_ior", C.c_int, [C.c_char_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     ("asuna_tracer_run_offline", C.c_int, [P, C.c_char_p, C.c_char_p]),
+    ("asuna_post_default", None, [C.POINTER(PostState)]),
+    ("asuna_tonemap", C.c_int, [P, P, C.c_int, C.POINTER(PostState), P]),
+    ("asuna_json_post_state", C.c_int, [P, C.POINTER(PostState)]),
     ("asuna_image_write", C.c_int, [C.c_char_p, C.c_uint32, C.c_uint32, P]),
     ("asuna_image_read", C.c_int, [C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), P, C.c_uint64]),
     # include/asuna_denoise.h
@@ -167,8 +181,8 @@ SIGNATURES = [
     ("asuna_denoiser_get_params", C.c_int, [P, P, C.c_uint64]),
     ("asuna_denoiser_set_params", C.c_int, [P, P, C.c_uint64]),
     ("asuna_denoiser_get_grads", C.c_int, [P, P, C.c_uint64]),
-    ("asuna_denoiser_forward", C.c_int, [P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, P]),
-    ("asuna_denoiser_loss_grad", C.c_int, [P, P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32,
+    ("asuna_denoiser_forward", C.c_int, [P, P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, P]),
+    ("asuna_denoiser_loss_grad", C.c_int, [P, P, P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32,
                                             C.POINTER(C.c_float)]),
     ("asuna_denoiser_adam", C.c_int, [P, C.c_float, C.c_float, C.c_float, C.c_float]),
     ("asuna_denoise", C.c_int, [P, P, P, C.c_int, C.c_int, P]),

@@ -367,12 +367,15 @@ __global__ void k_copy_channels(const __nv_bfloat16* src, int Csrc, int sOff, __
 
 // Network input: log1p(radiance), albedo, normal, zeros up to C; pixels
 // outside the h x w image (padding up to hp x wp) are zero.
-__global__ void k_prep_input(const float4* rad, const float4* alb, const float4* nrm, __nv_bfloat16* out, int n,
-                             int h, int w, int hp, int wp, int C) {
+// Network input: log1p(radiance), albedo, normal, log2(1 + filter-weight
+// sum) / 16 (the sample count: how much noise there is to remove), zeros up
+// to C; pixels outside the h x w image (padding up to hp x wp) are zero.
+__global__ void k_prep_input(const float4* rad, const float4* alb, const float4* nrm, const float4* wsum,
+                             __nv_bfloat16* out, int n, int h, int w, int hp, int wp, int C) {
   const size_t P = size_t(n) * hp * wp;
   for (size_t q = blockIdx.x * size_t(blockDim.x) + threadIdx.x; q < P; q += size_t(gridDim.x) * blockDim.x) {
     const int x = int(q % wp), y = int((q / wp) % hp), b = int(q / (size_t(wp) * hp));
-    float v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    float v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (y < h && x < w) {
       const size_t p = (size_t(b) * h + y) * w + x;
       const float4 r = rad[p];
@@ -391,10 +394,11 @@ __global__ void k_prep_input(const float4* rad, const float4* alb, const float4*
         v[7] = m.y;
         v[8] = m.z;
       }
+      if (wsum) v[9] = log2f(1.0f + fmaxf(wsum[p].x, 0.0f)) * 0.0625f;
     }
     __nv_bfloat162* o = reinterpret_cast<__nv_bfloat162*>(out + q * C);
     for (int c = 0; c < C; c += 2)
-      o[c / 2] = __floats2bfloat162_rn(c < 9 ? v[c] : 0.0f, c + 1 < 9 ? v[c + 1] : 0.0f);
+      o[c / 2] = __floats2bfloat162_rn(c < 10 ? v[c] : 0.0f, c + 1 < 10 ? v[c + 1] : 0.0f);
   }
 }
 
@@ -722,13 +726,14 @@ int dims(const asuna_denoiser* d, uint32_t n, uint32_t h, uint32_t w, Dims& o) {
   return ASUNA_OK;
 }
 
-int forward(asuna_denoiser* d, const float* rad, const float* alb, const float* nrm, const Dims& D) {
+int forward(asuna_denoiser* d, const float* rad, const float* alb, const float* nrm, const float* wsum,
+            const Dims& D) {
   const int L = d->L;
   cudaStream_t s = d->stream();
   const size_t P0 = size_t(D.n) * D.hp * D.wp;
   k_prep_input<<<grid1d(P0), 256, 0, s>>>(reinterpret_cast<const float4*>(rad), reinterpret_cast<const float4*>(alb),
-                                          reinterpret_cast<const float4*>(nrm), d->lv[0].X, D.n, D.h, D.w, D.hp, D.wp,
-                                          kInC);
+                                          reinterpret_cast<const float4*>(nrm), reinterpret_cast<const float4*>(wsum),
+                                          d->lv[0].X, D.n, D.h, D.w, D.hp, D.wp, kInC);
   ASUNA_CUDA_TRY(cudaGetLastError());
   for (int l = 0; l < L; ++l) {
     const int hl = D.hp >> l, wl = D.wp >> l;
@@ -952,13 +957,13 @@ int asuna_denoiser_get_grads(asuna_denoiser* d, float* host, uint64_t n) {
 }
 
 int asuna_denoiser_forward(asuna_denoiser* d, const float* radiance, const float* albedo, const float* normal,
-                           uint32_t n, uint32_t h, uint32_t w, float* out) {
+                           const float* weight, uint32_t n, uint32_t h, uint32_t w, float* out) {
   clearError();
   if (!d || !radiance || !out) return fail(ASUNA_ERR_INVALID, "asuna_denoiser_forward: null argument");
   Dims D;
   NN_TRY(dims(d, n, h, w, D));
   ASUNA_CUDA_TRY(cudaSetDevice(d->ctx->device));
-  NN_TRY(forward(d, radiance, albedo, normal, D));
+  NN_TRY(forward(d, radiance, albedo, normal, weight, D));
   k_output<<<grid1d(size_t(n) * h * w), 256, 0, d->stream()>>>(d->head, kHeadC,
                                                                reinterpret_cast<const float4*>(radiance),
                                                                reinterpret_cast<float4*>(out), D.n, D.h, D.w, D.hp,
@@ -968,7 +973,8 @@ int asuna_denoiser_forward(asuna_denoiser* d, const float* radiance, const float
 }
 
 int asuna_denoiser_loss_grad(asuna_denoiser* d, const float* radiance, const float* albedo, const float* normal,
-                             const float* target, uint32_t n, uint32_t h, uint32_t w, float* loss) {
+                             const float* weight, const float* target, uint32_t n, uint32_t h, uint32_t w,
+                             float* loss) {
   clearError();
   if (!d || !radiance || !target) return fail(ASUNA_ERR_INVALID, "asuna_denoiser_loss_grad: null argument");
   if (!d->training) return fail(ASUNA_ERR_INVALID, "denoiser was created without training state");
@@ -978,7 +984,7 @@ int asuna_denoiser_loss_grad(asuna_denoiser* d, const float* radiance, const flo
   cudaStream_t s = d->stream();
   ASUNA_CUDA_TRY(cudaMemsetAsync(d->grad, 0, d->nParams * sizeof(float), s));
   ASUNA_CUDA_TRY(cudaMemsetAsync(d->dLoss, 0, sizeof(float), s));
-  NN_TRY(forward(d, radiance, albedo, normal, D));
+  NN_TRY(forward(d, radiance, albedo, normal, weight, D));
   const size_t P0 = size_t(D.n) * D.hp * D.wp;
   k_l1_loss<<<grid1d(P0), 256, 0, s>>>(d->head, kHeadC, reinterpret_cast<const float4*>(radiance),
                                        reinterpret_cast<const float4*>(target), d->gHead, D.n, D.h, D.w, D.hp, D.wp,
@@ -1012,7 +1018,7 @@ int asuna_denoise(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* film, int albed
   if (albedo_image > 7 || normal_image > 7 || albedo_image == 0 || normal_image == 0)
     return fail(ASUNA_ERR_INVALID, "asuna_denoise: guide images must be channels 1..7 or -1");
   return asuna_denoiser_forward(d, filmImage(film, 0), filmImage(film, albedo_image), filmImage(film, normal_image),
-                                1, film->height, film->width, out);
+                                filmImage(film, 8), 1, film->height, film->width, out);
 }
 
 int asuna_denoise_estimate(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asuna_film* b, int albedo_image,

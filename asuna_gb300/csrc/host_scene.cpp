@@ -21,6 +21,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+
+#include <cuda_runtime.h>
 #include <fstream>
 #include <sstream>
 
@@ -1456,6 +1458,13 @@ int asuna_json_get_shot(const asuna_json_scene* js, uint32_t index, asuna_shot* 
   return js->scene.shot(index, out);
 }
 
+int asuna_json_post_state(const asuna_json_scene* js, asuna_post_state* out) {
+  if (!js || !out) return fail(ASUNA_ERR_INVALID, "null argument");
+  asuna_post_default(out);
+  out->tm_type = js->scene.state.toneMapping;
+  return ASUNA_OK;
+}
+
 int asuna_json_channels(const asuna_json_scene* js, uint32_t* n, int32_t* kinds) {
   if (!js || !n) return fail(ASUNA_ERR_INVALID, "null argument");
   const auto& k = js->scene.state.channelKinds;
@@ -1494,10 +1503,27 @@ int asuna_tracer_run_offline(asuna_ctx* ctx, const char* scene_json, const char*
     if ((rc = asuna_render(ctx, scene, &shot, film, nullptr))) return rc;
     if (!S.state.outputRenderResult) continue;
     char name[64];
-    std::snprintf(name, sizeof(name), "_shot_%04u.exr", i);
-    if ((rc = asuna_film_read(ctx, film, 0, px.data())) || (rc = writeExr(out_prefix + std::string(name), S.width,
-                                                                          S.height, px.data())))
-      return rc;
+    if (S.state.outputHdr) {
+      std::snprintf(name, sizeof(name), "_shot_%04u.exr", i);
+      if ((rc = asuna_film_read(ctx, film, 0, px.data())) ||
+          (rc = writeExr(out_prefix + std::string(name), S.width, S.height, px.data())))
+        return rc;
+    } else {
+      // the post pass's LDR color (tone mapping of the scene file)
+      asuna_post_state post;
+      if ((rc = asuna_json_post_state(js, &post))) return rc;
+      float* dev = nullptr;
+      if (cudaMalloc(&dev, px.size() * sizeof(float)) != cudaSuccess)
+        return fail(ASUNA_ERR_OOM, "offline output: device allocation failed");
+      std::unique_ptr<float, cudaError_t (*)(void*)> gd(dev, cudaFree);
+      if ((rc = asuna_tonemap(ctx, film, 0, &post, dev))) return rc;
+      cudaStream_t stream = static_cast<cudaStream_t>(asuna_ctx_stream(ctx));
+      if (cudaMemcpyAsync(px.data(), dev, px.size() * sizeof(float), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+          cudaStreamSynchronize(stream) != cudaSuccess)
+        return fail(ASUNA_ERR_CUDA, "offline output: read-back of the tone-mapped image failed");
+      std::snprintf(name, sizeof(name), "_shot_%04u.png", i);
+      if ((rc = writePng(out_prefix + std::string(name), S.width, S.height, px.data()))) return rc;
+    }
     for (uint32_t c = 0; c < S.state.rtx.n_multi_channel; ++c) {
       const bool ldr = c < S.state.channelLdr.size() && S.state.channelLdr[c];
       std::snprintf(name, sizeof(name), "_shot_%04u_channel_%04u.%s", i, c, ldr ? "png" : "exr");

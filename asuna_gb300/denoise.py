@@ -106,20 +106,22 @@ class Denoiser:
         return d
 
     # compute -----------------------------------------------------------
-    def forward(self, rad, alb=None, nrm=None, out=None):
-        """rad/alb/nrm: CUDA float32 [n, h, w, 4]; returns the denoised radiance."""
+    def forward(self, rad, alb=None, nrm=None, wsum=None, out=None):
+        """rad/alb/nrm/wsum (film images 0, albedo, normal, 8): CUDA float32
+        [n, h, w, 4]; returns the denoised radiance."""
         torch = _torch()
         n, h, w, _ = rad.shape
         if out is None:
             out = torch.empty_like(rad)
-        check(lib().asuna_denoiser_forward(self.handle, _ptr(rad), _ptr(alb), _ptr(nrm), n, h, w, _ptr(out)))
+        check(lib().asuna_denoiser_forward(self.handle, _ptr(rad), _ptr(alb), _ptr(nrm), _ptr(wsum), n, h, w,
+                                           _ptr(out)))
         return out
 
-    def loss_grad(self, rad, alb, nrm, target):
+    def loss_grad(self, rad, alb, nrm, wsum, target):
         n, h, w, _ = rad.shape
         loss = C.c_float()
-        check(lib().asuna_denoiser_loss_grad(self.handle, _ptr(rad), _ptr(alb), _ptr(nrm), _ptr(target), n, h, w,
-                                             C.byref(loss)))
+        check(lib().asuna_denoiser_loss_grad(self.handle, _ptr(rad), _ptr(alb), _ptr(nrm), _ptr(wsum),
+                                             _ptr(target), n, h, w, C.byref(loss)))
         return loss.value
 
     def adam(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
@@ -157,12 +159,12 @@ def render_pairs(ctx, seeds, width, height, spp_in=4, spp_target=256, level=4, m
     network input after each count of `spp_in` (an int or an increasing
     tuple; one progressive render, with the albedo / normal channels) and
     a `spp_target` render (the target).  Returns host arrays [n, h, w, 4]
-    float32 (radiance, albedo, normal, target), one entry per scene and
-    input count."""
+    float32 (radiance, albedo, normal, filter-weight sum, target), one entry
+    per scene and input count."""
     from . import scenes
 
     levels = (spp_in,) if np.isscalar(spp_in) else tuple(spp_in)
-    out = {k: [] for k in ("rad", "alb", "nrm", "tgt")}
+    out = {k: [] for k in ("rad", "alb", "nrm", "wsum", "tgt")}
     for s in seeds:
         b, shot = scenes.training_scene(int(s), width, height, frames=levels[0], max_depth=max_depth, level=level)
         scene = ctx.create_scene(b.desc())
@@ -180,16 +182,17 @@ def render_pairs(ctx, seeds, width, height, spp_in=4, spp_target=256, level=4, m
             out["rad"].append(f.read(0))
             out["alb"].append(f.read(1))
             out["nrm"].append(f.read(2))
+            out["wsum"].append(f.read(8))
             out["tgt"].append(tgt)
         f.close()
         g.close()
         del scene
-    return tuple(np.stack(out[k]) for k in ("rad", "alb", "nrm", "tgt"))
+    return tuple(np.stack(out[k]) for k in ("rad", "alb", "nrm", "wsum", "tgt"))
 
 
 def train(den, data, steps, batch=8, crop=64, lr=1e-3, seed=0, log_every=0):
     """Adam on random crops of the training pairs.  `data` = (rad, alb, nrm,
-    tgt) host arrays [n, h, w, 4]; returns the loss history."""
+    wsum, tgt) host arrays [n, h, w, 4]; returns the loss history."""
     torch = _torch()
     rng = np.random.default_rng(seed)
     dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in data]

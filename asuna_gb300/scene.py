@@ -27,6 +27,15 @@ def default_material():
     return m
 
 
+def default_post(tm_type=None):
+    """PipelineState's post-pass defaults (src/core/state.h:46-58)."""
+    p = A.PostState()
+    lib().asuna_post_default(C.byref(p))
+    if tm_type is not None:
+        p.tm_type = tm_type
+    return p
+
+
 def default_state():
     """State() of src/core/state.h:15-63 (ray-tracing part)."""
     s = A.RtState()
@@ -402,6 +411,7 @@ class Context:
         h = C.c_void_p()
         check(lib().asuna_ctx_create(device, C.byref(h)))
         self.handle = h
+        self.device = device
 
     def set_counters(self, on):
         check(lib().asuna_ctx_set_counters(self.handle, 1 if on else 0))
@@ -446,6 +456,18 @@ class Context:
 
     def sync(self):
         check(lib().asuna_ctx_sync(self.handle))
+
+    def tonemap(self, film, image=0, post=None):
+        """Post pass (tone mapping) of a film image; returns host RGBA float32."""
+        import torch
+
+        if post is None:
+            post = default_post()
+        out = torch.empty((film.height, film.width, 4), dtype=torch.float32, device=f"cuda:{self.device}")
+        torch.cuda.synchronize()
+        check(lib().asuna_tonemap(self.handle, film.handle, image, C.byref(post), C.c_void_p(out.data_ptr())))
+        self.sync()
+        return out.cpu().numpy()
 
     def run_offline(self, scene_json, out_prefix):
         check(lib().asuna_tracer_run_offline(self.handle, scene_json.encode(), out_prefix.encode()))

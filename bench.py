@@ -315,7 +315,7 @@ def run_denoise_rmse(args):
     exceeds the target, the plain average is the output instead.  Its time
     counts every render and every estimate.  The network is trained first,
     on the GPU, on pairs the renderer makes of other seeded scenes of the
-    same recipe (4/16/64-spp input, 1024-spp target)."""
+    same recipe (inputs at several sample counts, a high-count target)."""
     import torch
 
     import asuna_gb300 as ag
@@ -336,14 +336,16 @@ def run_denoise_rmse(args):
                       "reference_rms_noise": float(np.sqrt(refvar))}}
     # 1. train the denoiser on renderer-made pairs
     t0 = time.time()
+    spp_in = tuple(int(x) for x in args.train_spp_in.split(","))
     data = dn.render_pairs(ctx, range(1000, 1000 + args.train_scenes), args.train_size, args.train_size,
-                           spp_in=(4, 16, 64), spp_target=args.train_target_spp, level=5)
+                           spp_in=spp_in, spp_target=args.train_target_spp, level=args.train_level)
     gen_s = time.time() - t0
     den = dn.Denoiser(ctx, seed=0, max_pixels=args.train_batch * args.train_crop ** 2, training=True)
     t1 = time.time()
     losses = dn.train(den, data, steps=args.train_steps, batch=args.train_batch, crop=args.train_crop, lr=1e-3)
     train_s = time.time() - t1
-    out["training"] = {"scenes": args.train_scenes, "size": args.train_size, "input_spp": [4, 16, 64],
+    out["training"] = {"scenes": args.train_scenes, "size": args.train_size, "input_spp": list(spp_in),
+                       "level": args.train_level,
                        "target_spp": args.train_target_spp, "steps": args.train_steps, "batch": args.train_batch,
                        "crop": args.train_crop, "data_seconds": gen_s, "train_seconds": train_s,
                        "loss_first": float(np.mean(losses[:20])), "loss_last": float(np.mean(losses[-50:]))}
@@ -564,10 +566,12 @@ def main():
     ap.add_argument("--rmse-target", type=float, default=0.01)
     ap.add_argument("--plain-max-spp", type=int, default=32768)
     ap.add_argument("--denoise-max-spp", type=int, default=4096)
-    ap.add_argument("--train-scenes", type=int, default=96)
+    ap.add_argument("--train-scenes", type=int, default=64)
     ap.add_argument("--train-size", type=int, default=256)
-    ap.add_argument("--train-target-spp", type=int, default=1024)
-    ap.add_argument("--train-steps", type=int, default=3000)
+    ap.add_argument("--train-spp-in", default="4,16,64,256,1024")
+    ap.add_argument("--train-target-spp", type=int, default=16384)
+    ap.add_argument("--train-level", type=int, default=6)
+    ap.add_argument("--train-steps", type=int, default=6000)
     ap.add_argument("--train-batch", type=int, default=16)
     ap.add_argument("--train-crop", type=int, default=128)
     ap.add_argument("--serve", action="store_true", help="serving loop: Poisson arrivals, latency percentiles")

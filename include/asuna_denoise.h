@@ -13,7 +13,7 @@
  * pooling; decoder level l: nearest x2 upsampling, concatenation with the
  * encoder output of level l, two 3x3 conv + ReLU; a 3x3 head gives a residual
  * added to log1p(radiance).  Input channels (padded to 16): log1p(radiance),
- * albedo, normal.  Activations NHWC bf16; images are padded to multiples of
+ * albedo, normal, log2(1 + filter-weight sum) / 16.  Activations NHWC bf16; images are padded to multiples of
  * 2^(L-1) internally.
  *
  * Parameter layout (asuna_denoiser_get_params / set_params / get_grads): for
@@ -57,14 +57,17 @@ int asuna_denoiser_get_params(asuna_denoiser* d, float* host, uint64_t n);
 int asuna_denoiser_set_params(asuna_denoiser* d, const float* host, uint64_t n);
 int asuna_denoiser_get_grads(asuna_denoiser* d, float* host, uint64_t n);
 
-/* Forward pass: out = expm1(log1p(radiance) + head), clamped at 0 (RGBA, alpha 1). */
+/* Forward pass: out = expm1(log1p(radiance) + head), clamped at 0 (RGBA, alpha 1).
+ * `weight` is the film's filter-weight sum image (image 8; NULL = unknown):
+ * it tells the network how many samples the radiance holds. */
 int asuna_denoiser_forward(asuna_denoiser* d, const float* radiance, const float* albedo, const float* normal,
-                           uint32_t n, uint32_t h, uint32_t w, float* out);
+                           const float* weight, uint32_t n, uint32_t h, uint32_t w, float* out);
 /* Zeroes the gradients, runs forward, the L1 loss on log1p radiance against
  * `target` (mean over valid pixels and 3 channels) and the backward pass.
  * *loss (host) receives the loss; the call synchronises the stream. */
 int asuna_denoiser_loss_grad(asuna_denoiser* d, const float* radiance, const float* albedo, const float* normal,
-                             const float* target, uint32_t n, uint32_t h, uint32_t w, float* loss);
+                             const float* weight, const float* target, uint32_t n, uint32_t h, uint32_t w,
+                             float* loss);
 /* One Adam step (bias-corrected) on the gradients of the last loss_grad. */
 int asuna_denoiser_adam(asuna_denoiser* d, float lr, float beta1, float beta2, float eps);
 

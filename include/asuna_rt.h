@@ -391,6 +391,9 @@ int asuna_json_num_shots(const asuna_json_scene* js, uint32_t* out);
 int asuna_json_get_shot(const asuna_json_scene* js, uint32_t index, asuna_shot* out);
 /* Channel kinds of the scene's multi_channel list (ASUNA_CH_*), count in *n. */
 int asuna_json_channels(const asuna_json_scene* js, uint32_t* n, int32_t* kinds);
+struct asuna_post_state;
+/* The post-pass state of the scene file ("post_processing.tone_mapping"). */
+int asuna_json_post_state(const asuna_json_scene* js, struct asuna_post_state* out);
 
 /* ---- host side: camera helpers (src/core/camera.cpp:28-99) ---------------- */
 /* Fills a perspective GpuCamera from look-at parameters; fov in degrees is
@@ -466,9 +469,37 @@ int asuna_server_destroy(asuna_server* server);
 int asuna_image_write(const char* path, uint32_t width, uint32_t height, const float* rgba);
 int asuna_image_read(const char* path, uint32_t* width, uint32_t* height, float* rgba, uint64_t capacity);
 
+/* ---- post pass: tone mapping --------------------------------------------------
+ * GpuPushConstantPost (src/shared/pushconstant.h:50-62) and the operators of
+ * ToneMappingType (:37-46) as src/shaders/post.idle.frag:71-133 applies them. */
+enum {
+  ASUNA_TONEMAP_NONE = 0,
+  ASUNA_TONEMAP_GAMMA = 1,
+  ASUNA_TONEMAP_REINHARD = 2,
+  ASUNA_TONEMAP_ACES = 3,
+  ASUNA_TONEMAP_FILMIC = 4,
+  ASUNA_TONEMAP_PBRT = 5,
+  ASUNA_TONEMAP_CUSTOM = 6,
+  ASUNA_TONEMAP_NUM = 7
+};
+typedef struct asuna_post_state {
+  float brightness, contrast, saturation, vignette;
+  float avg_lum, zoom;
+  float rendering_ratio[2];
+  int32_t auto_exposure; /* bit 0: exposure from the mean luminance, bit 1: local */
+  float y_white, key;
+  uint32_t tm_type;      /* ASUNA_TONEMAP_* */
+} asuna_post_state;
+/* The defaults of PipelineState (src/core/state.h:46-58): filmic. */
+void asuna_post_default(asuna_post_state* post);
+/* Tone-maps film image `image` into `out` (device, width*height RGBA32F):
+ * the LDR color of the offline output before its 8-bit conversion. */
+int asuna_tonemap(asuna_ctx* ctx, asuna_film* film, int image, const asuna_post_state* post, float* out);
+
 /* ---- offline tracer ------------------------------------------------------- */
 /* Renders every shot of a scene file and writes <out_prefix>_shot_%04d.exr
- * (+ _channel_%04d.exr/.png per AOV), the offline mode of Tracer::runOffline. */
+ * (output_hdr) or the tone-mapped _shot_%04d.png, + _channel_%04d.exr/.png
+ * per AOV: the offline mode of Tracer::runOffline. */
 int asuna_tracer_run_offline(asuna_ctx* ctx, const char* scene_json, const char* out_prefix);
 
 #ifdef __cplusplus

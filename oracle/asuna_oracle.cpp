@@ -1555,6 +1555,69 @@ struct oracle_scene {
   Scene s;
 };
 
+
+// ---- post pass (src/shaders/post.idle.frag:71-133, utils/tonemapping.glsl) --
+namespace post {
+struct F3 {
+  float x, y, z;
+};
+inline F3 op(F3 a, F3 b, float (*f)(float, float)) { return {f(a.x, b.x), f(a.y, b.y), f(a.z, b.z)}; }
+inline F3 add(F3 a, F3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline F3 sub(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline F3 mul(F3 a, F3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+inline F3 div(F3 a, F3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
+inline F3 s3(float v) { return {v, v, v}; }
+inline F3 pw(F3 a, float e) { return {std::pow(a.x, e), std::pow(a.y, e), std::pow(a.z, e)}; }
+inline F3 lin2s(F3 c) { return pw(c, 1.0f / 2.2f); }
+inline F3 s2lin(F3 c) { return pw(c, 2.2f); }
+inline float lum709(F3 c) { return c.x * 0.2126f + c.y * 0.7152f + c.z * 0.0722f; }
+inline F3 unch(F3 c) {
+  const float A = 0.15f, B = 0.50f, C = 0.10f, D = 0.20f, E = 0.02f, F = 0.30f;
+  F3 num = add(mul(c, add(mul(c, s3(A)), s3(C * B))), s3(D * E));
+  F3 den = add(mul(c, add(mul(c, s3(A)), s3(B))), s3(D * F));
+  return sub(div(num, den), s3(E / F));
+}
+inline F3 hejl(F3 c) {
+  c = {std::max(c.x - 0.004f, 0.0f), std::max(c.y - 0.004f, 0.0f), std::max(c.z - 0.004f, 0.0f)};
+  return div(mul(c, add(mul(c, s3(6.2f)), s3(0.5f))), add(mul(c, add(mul(c, s3(6.2f)), s3(1.7f))), s3(0.06f)));
+}
+inline float clamp01(float v) { return std::min(std::max(v, 0.0f), 1.0f); }
+inline float srgb(float c) { return c < 0.0031308f ? 12.92f * c : 1.055f * std::pow(c, 1.0f / 2.4f) - 0.055f; }
+struct Lv {
+  std::vector<float> p;
+  int w, h;
+};
+inline F3 sample(const Lv& L, float u, float v, float* alpha = nullptr) {
+  const float x = u * float(L.w) - 0.5f, y = v * float(L.h) - 0.5f;
+  const float fx = std::floor(x), fy = std::floor(y), tx = x - fx, ty = y - fy;
+  auto at = [&](int i, int j, int c) {
+    i = std::min(std::max(i, 0), L.w - 1);
+    j = std::min(std::max(j, 0), L.h - 1);
+    return L.p[(size_t(j) * L.w + i) * 4 + c];
+  };
+  const int i0 = int(fx), j0 = int(fy);
+  float r[4];
+  for (int c = 0; c < 4; ++c) {
+    float a = at(i0, j0, c), b = at(i0 + 1, j0, c), cc = at(i0, j0 + 1, c), d = at(i0 + 1, j0 + 1, c);
+    float p = a + (b - a) * tx, q = cc + (d - cc) * tx;
+    r[c] = p + (q - p) * ty;
+  }
+  if (alpha) *alpha = r[3];
+  return {r[0], r[1], r[2]};
+}
+inline uint32_t pcg3dc(uint32_t v[3]) {
+  for (int k = 0; k < 3; ++k) v[k] = v[k] * 1664525u + 1013904223u;
+  v[0] += v[1] * v[2];
+  v[1] += v[2] * v[0];
+  v[2] += v[0] * v[1];
+  for (int k = 0; k < 3; ++k) v[k] ^= v[k] >> 16u;
+  v[0] += v[1] * v[2];
+  v[1] += v[2] * v[0];
+  v[2] += v[0] * v[1];
+  return 0;
+}
+}  // namespace post
+
 extern "C" {
 
 uint32_t oracle_xxhash32(uint32_t x, uint32_t y, uint32_t z) { return xxhash32(x, y, z); }
@@ -1570,6 +1633,141 @@ float oracle_math(int which, float x, float y) {
 }
 uint32_t oracle_pcg(uint32_t* state) { return pcg(*state); }
 float oracle_rand(uint32_t* state) { return rnd<float>(*state); }
+
+
+// Post pass of one image (rgba w*h) into out, as the GPU's k_tonemap
+// (the same box mip pyramid and exact mean for Custom's exposure).
+int oracle_tonemap(const float* rgba, uint32_t w, uint32_t h, const asuna_post_state* tm, float* out) {
+  using namespace post;
+  if (!rgba || !tm || !out || !w || !h) return ASUNA_ERR_INVALID;
+  std::vector<Lv> pyr;
+  pyr.push_back({std::vector<float>(rgba, rgba + size_t(w) * h * 4), int(w), int(h)});
+  float avgLum2 = 1.0f;
+  if (tm->tm_type == ASUNA_TONEMAP_CUSTOM && (tm->auto_exposure & 1)) {
+    double s[3] = {0, 0, 0};
+    for (size_t i = 0; i < size_t(w) * h; ++i)
+      for (int c = 0; c < 3; ++c) s[c] += rgba[i * 4 + c];
+    const float m[3] = {float(s[0] / double(size_t(w) * h)), float(s[1] / double(size_t(w) * h)),
+                        float(s[2] / double(size_t(w) * h))};
+    avgLum2 = m[0] * 0.2126f + m[1] * 0.7152f + m[2] * 0.0722f;
+    if ((tm->auto_exposure >> 1) & 1)
+      while (pyr.size() < 9 && !(pyr.back().w == 1 && pyr.back().h == 1)) {
+        const Lv& p = pyr.back();
+        Lv q{{}, std::max(1, p.w / 2), std::max(1, p.h / 2)};
+        q.p.resize(size_t(q.w) * q.h * 4);
+        for (int y = 0; y < q.h; ++y)
+          for (int x = 0; x < q.w; ++x) {
+            const int x0 = std::min(2 * x, p.w - 1), x1 = std::min(2 * x + 1, p.w - 1);
+            const int y0 = std::min(2 * y, p.h - 1), y1 = std::min(2 * y + 1, p.h - 1);
+            for (int c = 0; c < 4; ++c)
+              q.p[(size_t(y) * q.w + x) * 4 + c] =
+                  0.25f * (p.p[(size_t(y0) * p.w + x0) * 4 + c] + p.p[(size_t(y0) * p.w + x1) * 4 + c] +
+                           p.p[(size_t(y1) * p.w + x0) * 4 + c] + p.p[(size_t(y1) * p.w + x1) * 4 + c]);
+          }
+        pyr.push_back(std::move(q));
+      }
+  }
+  for (uint32_t y = 0; y < h; ++y)
+    for (uint32_t x = 0; x < w; ++x) {
+      const float u = (float(x) + 0.5f) / float(w) * tm->zoom, v = (float(y) + 0.5f) / float(h) * tm->zoom;
+      float alpha;
+      F3 hdr;
+      if (tm->zoom == 1.0f) {
+        const float* p = rgba + (size_t(y) * w + x) * 4;
+        hdr = {p[0], p[1], p[2]};
+        alpha = p[3];
+      } else {
+        hdr = sample(pyr[0], u, v, &alpha);
+      }
+      F3 c = hdr;
+      switch (tm->tm_type) {
+        case ASUNA_TONEMAP_NONE:
+          break;
+        case ASUNA_TONEMAP_GAMMA:
+          c = lin2s(div(hdr, add(div(hdr, s3(1.5f)), s3(1.0f))));
+          break;
+        case ASUNA_TONEMAP_REINHARD:
+        case ASUNA_TONEMAP_FILMIC:
+          c = hejl(hdr);
+          break;
+        case ASUNA_TONEMAP_ACES: {
+          const float A = 2.51f, B = 0.03f, C = 2.43f, D = 0.59f, E = 0.14f;
+          F3 t = div(mul(hdr, add(mul(hdr, s3(A)), s3(B))), add(mul(hdr, add(mul(hdr, s3(C)), s3(D))), s3(E)));
+          c = lin2s({clamp01(t.x), clamp01(t.y), clamp01(t.z)});
+          break;
+        }
+        case ASUNA_TONEMAP_PBRT:
+          c = {srgb(hdr.x), srgb(hdr.y), srgb(hdr.z)};
+          break;
+        default: {
+          F3 hh = hdr;
+          if (tm->auto_exposure & 1) {
+            const float XYZy = 0.3575761f * hh.x + 0.7151522f * hh.y + 0.1191920f * hh.z;
+            const float factor = tm->key / avgLum2, Y = factor * XYZy;
+            if ((tm->auto_exposure >> 1) & 1) {
+              const float scale[7] = {1, 2, 4, 8, 16, 32, 64};
+              float La = 0.0f;
+              for (int i = 0; i < 7; ++i) {
+                const Lv& a = pyr[std::min<size_t>(i, pyr.size() - 1)];
+                const Lv& b = pyr[std::min<size_t>(i + 1, pyr.size() - 1)];
+                const float v1 = lum709(sample(a, u, v)) * factor, v2 = lum709(sample(b, u, v)) * factor;
+                if (std::fabs(v1 - v2) / ((tm->key * std::pow(2.0f, 2.0f) / (scale[i] * scale[i])) + v1) > 0.05f) {
+                  La = v1;
+                  break;
+                }
+                La = v2;
+              }
+              const float k = Y / (1.0f + La);
+              hh = mul(div(hh, s3(XYZy)), s3(k));
+            } else {
+              const float Yd = (Y * (1.0f + Y / (tm->y_white * tm->y_white))) / (1.0f + Y);
+              hh = mul(div(hh, s3(XYZy)), s3(Yd));
+            }
+          }
+          F3 col = mul(hh, s3(tm->avg_lum));
+          {
+            const F3 cu = unch(mul(col, s3(2.0f))), white = unch(s3(11.2f));
+            col = lin2s(mul(cu, div(s3(1.0f), white)));
+          }
+          uint32_t r[3] = {x, y, 0u};
+          pcg3dc(r);
+          float noise[3];
+          for (int k = 0; k < 3; ++k) {
+            uint32_t bits = 0x3f800000u | (r[k] >> 9);
+            float f;
+            std::memcpy(&f, &bits, 4);
+            noise[k] = f - 1.0f;
+          }
+          {
+            const float quant = 1.0f / 255.0f;
+            const F3 lin = s2lin(col), sv = lin2s(lin);
+            const F3 c0 = {std::floor(sv.x / quant) * quant, std::floor(sv.y / quant) * quant,
+                           std::floor(sv.z / quant) * quant};
+            const F3 c1 = add(c0, s3(quant));
+            const F3 l0 = s2lin(c0), l1 = s2lin(c1);
+            const F3 discr = {l0.x + (l1.x - l0.x) * noise[0], l0.y + (l1.y - l0.y) * noise[1],
+                              l0.z + (l1.z - l0.z) * noise[2]};
+            col = {discr.x < lin.x ? c1.x : c0.x, discr.y < lin.y ? c1.y : c0.y, discr.z < lin.z ? c1.z : c0.z};
+          }
+          col = {clamp01(0.5f + (col.x - 0.5f) * tm->contrast), clamp01(0.5f + (col.y - 0.5f) * tm->contrast),
+                 clamp01(0.5f + (col.z - 0.5f) * tm->contrast)};
+          col = pw(col, 1.0f / tm->brightness);
+          const float g = col.x * 0.299f + col.y * 0.587f + col.z * 0.114f;
+          col = {g + (col.x - g) * tm->saturation, g + (col.y - g) * tm->saturation, g + (col.z - g) * tm->saturation};
+          const float vx = ((float(x) + 0.5f) / float(w) * tm->rendering_ratio[0] - 0.5f) * 2.0f;
+          const float vy = ((float(y) + 0.5f) / float(h) * tm->rendering_ratio[1] - 0.5f) * 2.0f;
+          const float vg = 1.0f - (vx * vx + vy * vy) * tm->vignette;
+          c = {col.x * vg, col.y * vg, col.z * vg};
+        }
+      }
+      float* o = out + (size_t(y) * w + x) * 4;
+      o[0] = c.x;
+      o[1] = c.y;
+      o[2] = c.z;
+      o[3] = alpha;
+    }
+  return ASUNA_OK;
+}
 
 int oracle_envmap_tables(uint32_t w, uint32_t h, const float* rgba, float* marg, float* cond) {
   if (!w || !h || !rgba || !marg || !cond) return ASUNA_ERR_INVALID;

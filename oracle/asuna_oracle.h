@@ -74,6 +74,8 @@ void oracle_invert3x4(const float* m12, float* out12);
 float oracle_math(int which, float x, float y);
 /* Env tables (marginal/conditional .xy per texel). */
 int oracle_envmap_tables(uint32_t w, uint32_t h, const float* rgba, float* marg_xy, float* cond_xy);
+/* Post pass (tone mapping) of one RGBA image, as the library's asuna_tonemap. */
+int oracle_tonemap(const float* rgba, uint32_t w, uint32_t h, const asuna_post_state* post, float* out);
 
 #ifdef __cplusplus
 }

@@ -52,6 +52,7 @@ def port():
         L.oracle_math.restype = C.c_float
         L.oracle_math.argtypes = [C.c_int, C.c_float, C.c_float]
         L.oracle_envmap_tables.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_tonemap.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]
         _port = L
     return _port
 

@@ -115,8 +115,9 @@ def upsample2_bwd(g):
     return g.reshape(n, h // 2, 2, w // 2, 2, c).sum(axis=(2, 4))
 
 
-def prep_input(rad, alb, nrm, hp, wp):
-    """[N,H,W,4] images -> padded [N,hp,wp,16] network input."""
+def prep_input(rad, alb, nrm, hp, wp, wsum=None):
+    """[N,H,W,4] images -> padded [N,hp,wp,16] network input (channel 9:
+    log2(1 + filter-weight sum) / 16)."""
     n, h, w, _ = rad.shape
     x = np.zeros((n, hp, wp, IN_C))
     x[:, :h, :w, 0:3] = np.log1p(np.maximum(rad[..., :3], 0.0))
@@ -124,6 +125,8 @@ def prep_input(rad, alb, nrm, hp, wp):
         x[:, :h, :w, 3:6] = alb[..., :3]
     if nrm is not None:
         x[:, :h, :w, 6:9] = nrm[..., :3]
+    if wsum is not None:
+        x[:, :h, :w, 9] = np.log2(1.0 + np.maximum(wsum[..., 0], 0.0)) / 16.0
     return x
 
 
@@ -147,7 +150,7 @@ class UNetRef:
     def dec(self, l, k):
         return 2 * self.L + 2 * (self.L - 2 - l) + k
 
-    def forward(self, rad, alb, nrm):
+    def forward(self, rad, alb, nrm, wsum=None):
         L = self.L
         n, h, w, _ = rad.shape
         a = 1 << (L - 1)
@@ -159,7 +162,7 @@ class UNetRef:
         U = [None] * L
         B = [None] * L
         D = [None] * L
-        X[0] = self.r(prep_input(rad, alb, nrm, hp, wp))
+        X[0] = self.r(prep_input(rad, alb, nrm, hp, wp, wsum))
         for l in range(L):
             if l > 0:
                 X[l] = self.r(avgpool2(S[l - 1]))
@@ -182,16 +185,16 @@ class UNetRef:
         self.cache = c
         return head
 
-    def output(self, rad, alb, nrm):
-        head = self.forward(rad, alb, nrm)
+    def output(self, rad, alb, nrm, wsum=None):
+        head = self.forward(rad, alb, nrm, wsum)
         n, h, w, _ = rad.shape
         y = head[:, :h, :w, :3] + np.log1p(np.maximum(rad[..., :3], 0.0))
         return np.maximum(np.expm1(y), 0.0)
 
-    def loss_grad(self, rad, alb, nrm, target):
+    def loss_grad(self, rad, alb, nrm, target, wsum=None):
         """Returns (loss, flat gradient) in the parameter layout."""
         L = self.L
-        head = self.forward(rad, alb, nrm)
+        head = self.forward(rad, alb, nrm, wsum)
         c = self.cache
         n, h, w = rad.shape[:3]
         count = 3.0 * n * h * w
@@ -239,8 +242,8 @@ class UNetRef:
         flat = np.concatenate([np.concatenate([gw.ravel(), gb.ravel()]) for gw, gb in grads])
         return loss, flat
 
-    def loss(self, rad, alb, nrm, target):
-        head = self.forward(rad, alb, nrm)
+    def loss(self, rad, alb, nrm, target, wsum=None):
+        head = self.forward(rad, alb, nrm, wsum)
         n, h, w = rad.shape[:3]
         d = head[:, :h, :w, :3] + np.log1p(np.maximum(rad[..., :3], 0.0)) - np.log1p(np.maximum(target[..., :3], 0.0))
         return np.abs(d).sum() / (3.0 * n * h * w)

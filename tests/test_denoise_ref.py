@@ -14,6 +14,13 @@ def _images(rng, n, h, w):
     return rad, alb, nrm, tgt
 
 
+def test_sample_count_channel():
+    rad = np.ones((1, 4, 4, 4))
+    w = np.full((1, 4, 4, 4), 255.0)
+    x = U.prep_input(rad, None, None, 16, 16, w)
+    assert np.allclose(x[0, :4, :4, 9], 0.5) and not x[0, 4:, :, 9].any()
+
+
 def test_backward_matches_finite_differences():
     rng = np.random.default_rng(3)
     ch = [4, 6, 8]

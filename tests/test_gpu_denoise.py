@@ -141,31 +141,32 @@ def _net_inputs(rng, n, h, w):
     rad = rng.gamma(1.2, 0.5, (n, h, w, 4)).astype(np.float32)
     alb = rng.uniform(0, 1, (n, h, w, 4)).astype(np.float32)
     nrm = rng.normal(size=(n, h, w, 4)).astype(np.float32)
+    wsum = np.repeat(rng.uniform(1.0, 600.0, (n, h, w, 1)), 4, axis=3).astype(np.float32)
     tgt = (rad * rng.uniform(0.5, 1.5, rad.shape)).astype(np.float32)
-    return rad, alb, nrm, tgt
+    return rad, alb, nrm, wsum, tgt
 
 
 def test_network_forward_loss_and_gradients(dctx):
     ch = dn.DEFAULT_CHANNELS
     rng = np.random.default_rng(5)
     n, h, w = 2, 37, 45  # padded to 48 x 48
-    rad, alb, nrm, tgt = _net_inputs(rng, n, h, w)
+    rad, alb, nrm, wsum, tgt = _net_inputs(rng, n, h, w)
     d = dn.Denoiser(dctx, ch, seed=3, max_pixels=n * 48 * 48, training=True)
     p = U.he_init(ch, 3)
     assert np.allclose(d.get_params(), p, rtol=1e-6, atol=1e-9)
     p = (p + rng.normal(0, 0.02, p.size)).astype(np.float32)  # non-zero biases, active head
     d.set_params(p)
     ref = U.UNetRef(ch, p, bf16=True)
-    drad, dalb, dnrm, dtgt = f32(rad), f32(alb), f32(nrm), f32(tgt)
+    drad, dalb, dnrm, dw, dtgt = f32(rad), f32(alb), f32(nrm), f32(wsum), f32(tgt)
     torch.cuda.synchronize()
-    out = d.forward(drad, dalb, dnrm)
+    out = d.forward(drad, dalb, dnrm, dw)
     dctx.sync()
-    ro = ref.output(rad.astype(np.float64), alb, nrm)
+    ro = ref.output(rad.astype(np.float64), alb, nrm, wsum)
     got = out.cpu().numpy()[..., :3]
     med = np.median(np.abs(got - ro) / (np.abs(ro) + 1e-3))
     mx = np.abs(got - ro).max() / np.abs(ro).max()
-    loss = d.loss_grad(drad, dalb, dnrm, dtgt)
-    rl, rg = ref.loss_grad(rad.astype(np.float64), alb, nrm, tgt.astype(np.float64))
+    loss = d.loss_grad(drad, dalb, dnrm, dw, dtgt)
+    rl, rg = ref.loss_grad(rad.astype(np.float64), alb, nrm, tgt.astype(np.float64), wsum)
     g = d.get_grads().astype(np.float64)
     print(f"\nforward: median rel {med:.2e}, max/scale {mx:.2e}; loss {loss:.6f} vs {rl:.6f}")
     off, rows = 0, []
@@ -197,10 +198,10 @@ def test_training_gain_over_noisy_input(dctx):
     assert np.mean(losses[-50:]) < 0.8 * np.mean(losses[:10])
     e = dn.Denoiser(dctx, max_pixels=4 * 96 * 96)
     e.set_params(d.get_params())
-    rad, alb, nrm, tgt = test
-    drad, dalb, dnrm = f32(rad), f32(alb), f32(nrm)
+    rad, alb, nrm, wsum, tgt = test
+    drad, dalb, dnrm, dw = f32(rad), f32(alb), f32(nrm), f32(wsum)
     torch.cuda.synchronize()
-    out = e.forward(drad, dalb, dnrm)
+    out = e.forward(drad, dalb, dnrm, dw)
     dctx.sync()
     den = out.cpu().numpy()
     noisy_err = dn.rmse(rad, tgt)

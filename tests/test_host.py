@@ -22,7 +22,8 @@ def test_library_exports_every_declared_symbol():
     declared = set()
     for name in sorted(os.listdir(os.path.join(ROOT, "include"))):
         text = open(os.path.join(ROOT, "include", name)).read()
-        declared |= set(re.findall(r"^\s*(?:int|float|uint64_t|void\*|const char\*)\s+(asuna_\w+)\s*\(", text, re.M))
+        declared |= set(re.findall(r"^\s*(?:int|float|uint64_t|void\*|void|const char\*)\s+(asuna_\w+)\s*\(", text,
+                                   re.M))
     assert len(declared) >= 60
     assert "asuna_denoise" in declared and "asuna_server_submit" in declared
     L = C.CDLL(A.LIB_PATH)
@@ -395,3 +396,41 @@ def test_json_material_plugins_match_builder():
         ag.JsonScene(text=json.dumps({**base, "materials": [{"type": "brdf_conductor", "name": "x",
                                                              "material": "Unobtainium"}]}), base_dir=".")
     assert e.value.code == A.ERR_PARSE
+
+
+def test_post_state_layout_defaults_and_json():
+    # GpuPushConstantPost (src/shared/pushconstant.h:50-62): 48 bytes
+    assert C.sizeof(A.PostState) == 48
+    assert A.PostState.rendering_ratio.offset == 24 and A.PostState.tm_type.offset == 44
+    p = ag.default_post()
+    assert (p.brightness, p.contrast, p.saturation, p.vignette, p.avg_lum, p.zoom) == (1, 1, 1, 0, 1, 1)
+    assert (p.y_white, p.key, p.auto_exposure, p.tm_type) == (0.5, 0.5, 0, A.TONEMAP_FILMIC)
+    base = {"camera": {"type": "perspective", "film": {"resolution": [8, 8]}}, "meshes": [], "instances": []}
+    for name, t in [("none", 0), ("gamma", 1), ("reinhard", 2), ("Aces", 3), ("filmic", 4), ("pbrt", 5),
+                    ("custom", 6)]:
+        js = ag.JsonScene(text=json.dumps({**base, "state": {"post_processing": {"tone_mapping": name}}}),
+                          base_dir=".")
+        q = A.PostState()
+        A.check(A.lib().asuna_json_post_state(js.handle, C.byref(q)))
+        assert q.tm_type == t
+
+
+def test_oracle_tonemap_closed_forms():
+    L = oracle_py.port()
+    rng = np.random.default_rng(4)
+    img = rng.gamma(1.0, 0.6, (6, 10, 4)).astype(np.float32)
+    out = np.zeros_like(img)
+
+    def run(t):
+        p = ag.default_post(t)
+        assert L.oracle_tonemap(img.ctypes.data, 10, 6, C.byref(p), out.ctypes.data) == 0
+        return out.copy()
+
+    assert np.array_equal(run(A.TONEMAP_NONE), img)
+    x = np.maximum(img[..., :3] - np.float32(0.004), np.float32(0))
+    hejl = (x * (x * np.float32(6.2) + np.float32(0.5))) / (x * (x * np.float32(6.2) + np.float32(1.7)) + np.float32(0.06))
+    assert np.allclose(run(A.TONEMAP_FILMIC)[..., :3], hejl, rtol=1e-6, atol=1e-7)
+    c = img[..., :3].astype(np.float64)
+    srgb = np.where(c < 0.0031308, 12.92 * c, 1.055 * c ** (1 / 2.4) - 0.055)
+    assert np.allclose(run(A.TONEMAP_PBRT)[..., :3], srgb, rtol=1e-5, atol=1e-6)
+    assert np.allclose(run(A.TONEMAP_GAMMA)[..., :3], (c / (1 + c / 1.5)) ** (1 / 2.2), rtol=1e-5)
