@@ -118,7 +118,7 @@ TONEMAP_NONE, TONEMAP_GAMMA, TONEMAP_REINHARD, TONEMAP_ACES, TONEMAP_FILMIC, TON
 
 class DenoiserOpts(C.Structure):
     _fields_ = [("levels", C.c_uint32), ("channels", C.c_uint32 * 6), ("seed", C.c_uint64),
-                ("max_pixels", C.c_uint64), ("training", C.c_uint32), ("reserved", C.c_uint32)]
+                ("max_pixels", C.c_uint64), ("training", C.c_uint32), ("tensor_memory", C.c_uint32)]
 
 
 class SceneStats(C.Structure):
@@ -142,7 +142,7 @@ SIGNATURES = [
     ("asuna_ctx_set_path_budget", C.c_int, [P, C.c_uint64]),
     ("asuna_ctx_set_launch", C.c_int, [P, C.c_int, C.c_int]),
     ("asuna_ctx_set_graphs", C.c_int, [P, C.c_int]),
-    ("asuna_ctx_set_traversal", C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int]),
+    ("asuna_ctx_set_traversal", C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     ("asuna_scene_create", C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(P)]),
     ("asuna_scene_destroy", C.c_int, [P]),
     ("asuna_scene_get_stats", C.c_int, [P, C.POINTER(SceneStats)]),
@@ -200,6 +200,10 @@ SIGNATURES = [
     ("asuna_nn_copy_channels", C.c_int, [P, P, C.c_int, C.c_int, P, C.c_int, C.c_int, C.c_int, C.c_uint64,
                                           C.c_int]),
     ("asuna_nn_relu_mask", C.c_int, [P, P, P, C.c_uint64]),
+    ("asuna_nn_weights_tc", C.c_int, [P, P, P, C.c_int, C.c_int]),
+    ("asuna_nn_conv3x3_tc", C.c_int, [P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, C.c_int, C.c_int, P, P,
+                                       C.c_int]),
+    ("asuna_nn_tc_status", C.c_int, [C.POINTER(C.c_int)]),
     ("asuna_nn_f32_to_bf16", C.c_int, [P, P, P, C.c_uint64]),
 ]
 

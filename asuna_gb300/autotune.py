@@ -13,17 +13,19 @@ BYTES_PER_PATH = 228  # wavefront state per path slot (asuna_gb300/csrc/engine.c
 
 
 def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64), trace_options=(0, 6),
-         shade_options=(0, 2), refill_options=(4, 8, 16, 24), memory_bytes=48 << 30, reps=2, frame_base=1 << 20):
+         shade_options=(0, 2), refill_options=(4, 8, 16, 24), occupancy_options=(8, 10, 12), memory_bytes=48 << 30,
+         reps=2, frame_base=1 << 20):
     """Returns {"frames": f, "trace_blocks_per_sm": t, "shade_blocks_per_sm": s, "traversal": (refill
-    extend, refill shadow, speculate extend, speculate shadow), "mrays": best, "trials": [...]} and leaves
-    the context configured with the best choice.  Coordinate search: frames, then grids, then the
-    traversal refill thresholds and speculation of each pass."""
+    extend, refill shadow, speculate extend, speculate shadow, traversal blocks per SM), "mrays": best,
+    "trials": [...]} and leaves the context configured with the best choice.  Coordinate search: frames,
+    then grids, then the traversal kernel variant and the refill thresholds and speculation of each
+    pass."""
     npix = shot.width * shot.height
     saved = (shot.frame0, shot.frames)
     trials = []
     best = None
 
-    trav = [8, 8, 1, 1]
+    trav = [8, 8, 1, 1, 8]
 
     def run(frames, t, s):
         ctx.set_traversal(*trav)
@@ -53,15 +55,17 @@ def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64), trace_
             if v > best["mrays"]:
                 best = {**best, "trace_blocks_per_sm": t, "shade_blocks_per_sm": s, "mrays": v}
         best["traversal"] = tuple(trav)
-        # traversal: refill threshold, then speculation, of each pass in turn
+        # traversal: kernel occupancy, then refill threshold and speculation of each pass
+        steps = [(4, o) for o in occupancy_options if o != 8]
         for k in (1, 0):
-            for opt in [(k, r) for r in refill_options if r != 8] + [(k + 2, 0)]:
-                trav = list(best["traversal"])
-                trav[opt[0]] = opt[1]
-                v = run(best["frames"], best["trace_blocks_per_sm"], best["shade_blocks_per_sm"])
-                trials.append({"frames": best["frames"], "traversal": tuple(trav), "mrays": v})
-                if v > best["mrays"]:
-                    best = {**best, "traversal": tuple(trav), "mrays": v}
+            steps += [(k, r) for r in refill_options if r != 8] + [(k + 2, 0)]
+        for index, value in steps:
+            trav = list(best["traversal"])
+            trav[index] = value
+            v = run(best["frames"], best["trace_blocks_per_sm"], best["shade_blocks_per_sm"])
+            trials.append({"frames": best["frames"], "traversal": tuple(trav), "mrays": v})
+            if v > best["mrays"]:
+                best = {**best, "traversal": tuple(trav), "mrays": v}
     finally:
         shot.frame0, shot.frames = saved
     ctx.set_traversal(*best["traversal"])

@@ -1,0 +1,374 @@
+// conv_tc.cu — 3x3 convolution (stride 1, zero padding 1) on the
+// fifth-generation tensor cores: tcgen05.mma with the accumulator in tensor
+// memory, operands staged in shared memory by TMA.
+//
+// One CTA computes a 16 x 8 pixel tile (M = 128) for all output channels
+// (N = cout <= 256, a multiple of 16).  The input channels are consumed in
+// groups of 16 (K = 16 per MMA):
+//   * activations: for each 8-channel chunk, one TMA tiled load of the
+//     18 x 10 halo of the tile from the NHWC tensor (zero fill outside the
+//     image) lands as [row][col][8] bf16 (blocks 2,944 B apart, 128-byte
+//     aligned); for tap (dy, dx) the A operand is the view starting at
+//     pixel (dy, dx) of that halo: 8-row core matrices are 8 consecutive
+//     pixels of one image row, image rows are 160 B apart (stride
+//     dimension), the second 8-channel chunk is one block further (leading
+//     dimension) — K-major, no swizzle;
+//   * weights: pre-arranged as [cin/16][tap][chunk][cout][8] so one group's
+//     nine taps are one contiguous bulk copy, B = [chunk][cout][8] per tap;
+//   * nine MMAs per group accumulate into TMEM (fp32, lane = pixel,
+//     column = output channel); a 3-stage ring of shared-memory buffers is
+//     refilled as tcgen05.commit reports each stage's MMAs done.
+// One elected thread issues the copies and the MMAs; after the last group
+// the four warps read their 32 TMEM lanes each (tcgen05.ld), apply bias,
+// ReLU and the ReLU mask and store bf16 (or fp32).  Every mbarrier wait is
+// bounded: on expiry the CTA records an error, skips its output and still
+// frees its tensor memory.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/asuna_denoise.h"
+#include "common.h"
+
+namespace asuna {
+namespace tc {
+namespace {
+
+constexpr int kTileH = 16, kTileW = 8;                         // pixels per CTA (M = 128)
+constexpr int kHaloH = kTileH + 2, kHaloW = kTileW + 2;
+constexpr int kBoxBytes = kHaloH * kHaloW * 16;  // bytes one TMA box of 8 channels transfers: 2,880
+constexpr int kChunkBytes = 2944;                  // its shared-memory slot, padded to 128 B
+constexpr int kActStage = 2 * kChunkBytes;  // 16 channels
+constexpr int kStages = 3;
+constexpr int kThreads = 128;
+constexpr int kPadBytes = 48 * 1024;                           // slack past the operands
+constexpr uint32_t kWaitLimit = 1u << 26;                      // try_wait rounds before giving up
+
+__device__ int g_tcError;  // set when a wait expired; read and cleared by asuna_nn_tc_status
+
+__device__ __forceinline__ uint32_t smem(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void mbarInit(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void mbarExpectTx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// bounded wait for phase `parity` of the barrier; false when it expired
+__device__ __forceinline__ bool mbarWait(uint32_t bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kWaitLimit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tmaLoad4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                          uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(dst),
+      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void bulkLoad(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+// shared-memory matrix descriptor: start, leading (K) and stride (M/N)
+// byte offsets, fixed bits 46-48 = 0b001, no swizzle
+__device__ __forceinline__ uint64_t matDesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return uint64_t((addr >> 4) & 0x3FFFu) | (uint64_t((lbo >> 4) & 0x3FFFu) << 16) |
+         (uint64_t((sbo >> 4) & 0x3FFFu) << 32) | (uint64_t(1) << 46);
+}
+// instruction descriptor of kind::f16: D fp32, A and B bf16, both K-major
+__device__ __forceinline__ uint32_t instrDesc(uint32_t n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+}
+__device__ __forceinline__ void mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void fenceBefore() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fenceAfter() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct TcArgs {
+  const __nv_bfloat16* wt;    // [cin/16][9][2][cout][8]
+  const float* bias;          // [cout] or null
+  const __nv_bfloat16* mask;  // [P][cout] or null
+  void* out;                  // [P][cout]
+  int n, h, w, cin, cout;
+  int tilesX, tilesY;
+  int relu, outF32;
+  uint32_t tmemCols;
+  uint32_t wStageBytes;  // 9 * 2 * cout * 16
+};
+
+__global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__ CUtensorMap act, TcArgs a) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  // [0, 128): barriers and the TMEM address; then activation stages, weight stages, slack
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm);
+  uint64_t* empty = full + kStages;
+  uint64_t* done = empty + kStages;
+  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(done + 1);
+  int* abortFlag = reinterpret_cast<int*>(tmemSlot + 1);
+  unsigned char* actBase = sm + 128;
+  unsigned char* wBase = actBase + kStages * kActStage;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  int t = blockIdx.x;
+  const int tx = t % a.tilesX;
+  t /= a.tilesX;
+  const int ty = t % a.tilesY;
+  const int img = t / a.tilesY;
+  const int x0 = tx * kTileW, y0 = ty * kTileH;
+
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbarInit(smem(&full[s]), 1);
+      mbarInit(smem(&empty[s]), 1);
+    }
+    mbarInit(smem(done), 1);
+    *abortFlag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem(tmemSlot)),
+                 "r"(a.tmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fenceBefore();
+  __syncthreads();
+  fenceAfter();
+  const uint32_t tmem = *tmemSlot;
+
+  const int groups = a.cin / 16;
+  if (tid == 0) {
+    const uint32_t idesc = instrDesc(uint32_t(a.cout));
+    auto issue = [&](int s, int g) {
+      const uint32_t bar = smem(&full[s]);
+      mbarExpectTx(bar, uint32_t(2 * kBoxBytes) + a.wStageBytes);
+      const uint32_t dstA = smem(actBase + s * kActStage);
+      tmaLoad4d(dstA, &act, g * 16, x0 - 1, y0 - 1, img, bar);
+      tmaLoad4d(dstA + kChunkBytes, &act, g * 16 + 8, x0 - 1, y0 - 1, img, bar);
+      bulkLoad(smem(wBase + size_t(s) * a.wStageBytes), a.wt + size_t(g) * (a.wStageBytes / 2), a.wStageBytes, bar);
+    };
+    bool ok = true;
+    for (int g = 0; g < groups && g < kStages; ++g) issue(g, g);
+    for (int g = 0; g < groups && ok; ++g) {
+      const int s = g % kStages;
+      const uint32_t use = uint32_t(g / kStages);
+      if (!mbarWait(smem(&full[s]), use & 1u)) {
+        ok = false;
+        break;
+      }
+      const uint32_t aBase = smem(actBase + s * kActStage);
+      const uint32_t bBase = smem(wBase + size_t(s) * a.wStageBytes);
+      const uint32_t bTap = uint32_t(2 * a.cout * 16);
+#pragma unroll 1
+      for (int tap = 0; tap < 9; ++tap) {
+        const int dy = tap / 3, dx = tap % 3;
+        const uint64_t da = matDesc(aBase + uint32_t(dy * kHaloW + dx) * 16u, kChunkBytes, kHaloW * 16);
+        const uint64_t db = matDesc(bBase + uint32_t(tap) * bTap, uint32_t(a.cout * 16), 128u);
+        mma(tmem, da, db, idesc, (g > 0 || tap > 0) ? 1u : 0u);
+      }
+      commit(smem(&empty[s]));
+      const int gn = g + kStages;
+      if (gn < groups) {
+        if (!mbarWait(smem(&empty[s]), use & 1u)) {
+          ok = false;
+          break;
+        }
+        issue(s, gn);
+      }
+    }
+    if (ok) {
+      commit(smem(done));
+      ok = mbarWait(smem(done), 0u);
+    }
+    if (!ok) {
+      *abortFlag = 1;
+      atomicExch(&g_tcError, 1);
+    }
+  }
+  fenceBefore();
+  __syncthreads();
+  fenceAfter();
+  if (!*abortFlag) {
+    // epilogue: warp w owns TMEM lanes 32w..32w+31 = tile pixels 32w..32w+31
+    const int m = warp * 32 + lane;
+    const int py = y0 + m / kTileW, px = x0 + m % kTileW;
+    const bool inside = py < a.h && px < a.w;
+    const size_t p = (size_t(img) * a.h + py) * a.w + px;
+    const uint32_t laneBase = tmem + (uint32_t(warp * 32) << 16);
+    for (int c0 = 0; c0 < a.cout; c0 += 16) {
+      float v[16];
+      ld16(laneBase + uint32_t(c0), v);
+      if (!inside) continue;
+#pragma unroll
+      for (int i = 0; i < 16; i += 2) {
+        const int co = c0 + i;
+        float v0 = v[i], v1 = v[i + 1];
+        if (a.bias) {
+          v0 += a.bias[co];
+          v1 += a.bias[co + 1];
+        }
+        if (a.relu) {
+          v0 = fmaxf(v0, 0.0f);
+          v1 = fmaxf(v1, 0.0f);
+        }
+        if (a.mask) {
+          const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162*>(a.mask + p * a.cout + co);
+          if (!(__bfloat162float(mk.x) > 0.0f)) v0 = 0.0f;
+          if (!(__bfloat162float(mk.y) > 0.0f)) v1 = 0.0f;
+        }
+        if (a.outF32)
+          *reinterpret_cast<float2*>(static_cast<float*>(a.out) + p * a.cout + co) = make_float2(v0, v1);
+        else
+          *reinterpret_cast<__nv_bfloat162*>(static_cast<__nv_bfloat16*>(a.out) + p * a.cout + co) =
+              __floats2bfloat162_rn(v0, v1);
+      }
+    }
+  }
+  fenceBefore();
+  __syncthreads();
+  if (warp == 0) {
+    fenceAfter();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmemCols) : "memory");
+  }
+}
+
+// [cout][9][cin] -> [cin/16][9][2][cout][8]
+__global__ void k_weights_tc(const __nv_bfloat16* w, __nv_bfloat16* o, int cout, int cin) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cout * 9 * cin) return;
+  const int ci = i % cin, tap = (i / cin) % 9, co = i / (9 * cin);
+  const int g = ci / 16, c = (ci / 8) & 1, e = ci & 7;
+  o[((((size_t(g) * 9 + tap) * 2 + c) * cout + co) * 8) + e] = w[i];
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encodeFn() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+}  // namespace
+}  // namespace tc
+}  // namespace asuna
+
+using namespace asuna;
+using namespace asuna::tc;
+
+extern "C" {
+
+int asuna_nn_weights_tc(void* stream, const void* w, void* wtc, int cout, int cin) {
+  if (!w || !wtc || cin % 16 || cout % 16) return fail(ASUNA_ERR_INVALID, "asuna_nn_weights_tc: bad argument");
+  const int n = cout * 9 * cin;
+  k_weights_tc<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      static_cast<const __nv_bfloat16*>(w), static_cast<__nv_bfloat16*>(wtc), cout, cin);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? ASUNA_OK : fail(ASUNA_ERR_CUDA, "asuna_nn_weights_tc: %s", cudaGetErrorString(e));
+}
+
+int asuna_nn_conv3x3_tc(void* stream, const void* in, int n, int h, int w, int cin, const void* weight_tc,
+                        const float* bias, int cout, int relu, const void* mask, void* out, int out_f32) {
+  if (!in || !weight_tc || !out || n <= 0 || h <= 0 || w <= 0)
+    return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: bad argument");
+  if (cin % 16 || cout % 16 || cout > 256)
+    return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: cin %% 16, cout %% 16 and cout <= 256 required");
+  if (reinterpret_cast<uintptr_t>(in) % 16 || reinterpret_cast<uintptr_t>(weight_tc) % 16)
+    return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: operands must be 16-byte aligned");
+  EncodeTiledFn enc = encodeFn();
+  if (!enc) return fail(ASUNA_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+  // NHWC bf16 as a 4-D tensor (C, W, H, N); box = 8 channels x halo
+  CUtensorMap map;
+  const cuuint64_t dims[4] = {cuuint64_t(cin), cuuint64_t(w), cuuint64_t(h), cuuint64_t(n)};
+  const cuuint64_t strides[3] = {cuuint64_t(cin) * 2, cuuint64_t(w) * cin * 2, cuuint64_t(h) * w * cin * 2};
+  const cuuint32_t box[4] = {8, kHaloW, kHaloH, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(in), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: tensor map encoding failed (%d)", int(r));
+  TcArgs a{};
+  a.wt = static_cast<const __nv_bfloat16*>(weight_tc);
+  a.bias = bias;
+  a.mask = static_cast<const __nv_bfloat16*>(mask);
+  a.out = out;
+  a.n = n;
+  a.h = h;
+  a.w = w;
+  a.cin = cin;
+  a.cout = cout;
+  a.tilesX = (w + kTileW - 1) / kTileW;
+  a.tilesY = (h + kTileH - 1) / kTileH;
+  a.relu = relu;
+  a.outF32 = out_f32;
+  a.tmemCols = cout <= 32 ? 32u : cout <= 64 ? 64u : cout <= 128 ? 128u : 256u;
+  a.wStageBytes = uint32_t(9 * 2 * cout * 16);
+  const size_t smemBytes = 128 + size_t(kStages) * (kActStage + a.wStageBytes) + kPadBytes;
+  static std::once_flag attr;
+  std::call_once(attr, [] {
+    cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  });
+  if (smemBytes > 227 * 1024) return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: cout %d needs too much shared memory", cout);
+  const long long blocks = (long long)a.tilesX * a.tilesY * n;
+  if (blocks > (1ll << 31) - 1) return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: too many tiles");
+  k_conv_tc<<<unsigned(blocks), kThreads, smemBytes, static_cast<cudaStream_t>(stream)>>>(map, a);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? ASUNA_OK : fail(ASUNA_ERR_CUDA, "asuna_nn_conv3x3_tc: %s", cudaGetErrorString(e));
+}
+
+int asuna_nn_tc_status(int* expired) {
+  if (!expired) return fail(ASUNA_ERR_INVALID, "null argument");
+  int zero = 0;
+  if (cudaMemcpyFromSymbol(expired, g_tcError, sizeof(int)) != cudaSuccess ||
+      cudaMemcpyToSymbol(g_tcError, &zero, sizeof(int)) != cudaSuccess)
+    return fail(ASUNA_ERR_CUDA, "asuna_nn_tc_status: %s", cudaGetErrorString(cudaGetLastError()));
+  return ASUNA_OK;
+}
+
+}  // extern "C"

@@ -641,6 +641,8 @@ struct asuna_denoiser {
   size_t nParams = 0, nFlip = 0;
   float *p32 = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
   __nv_bfloat16 *pbf = nullptr, *wt = nullptr;
+  bool useTc = false;                                // convolutions on tcgen05
+  __nv_bfloat16 *wtc = nullptr, *wtcT = nullptr;     // their weight layouts (forward, input gradient)
   float* dLoss = nullptr;
   double* dSums = nullptr;
   float* head = nullptr;
@@ -683,6 +685,9 @@ int dalloc(asuna_denoiser* d, T** p, size_t count) {
 
 int convFwd(asuna_denoiser* d, int li, const __nv_bfloat16* in, int n, int h, int w, bool relu, void* out, bool f32) {
   const ConvLayer& c = d->layers[li];
+  if (d->useTc)
+    return asuna_nn_conv3x3_tc(d->stream(), in, n, h, w, c.cin, d->wtc + c.wtOff, d->p32 + c.bOff, c.cout,
+                               relu ? 1 : 0, nullptr, out, f32 ? 1 : 0);
   return asuna_nn_conv3x3(d->stream(), in, n, h, w, c.cin, d->pbf + c.wOff, d->p32 + c.bOff, c.cout, relu ? 1 : 0,
                           nullptr, out, f32 ? 1 : 0);
 }
@@ -691,6 +696,8 @@ int convFwd(asuna_denoiser* d, int li, const __nv_bfloat16* in, int n, int h, in
 int convDx(asuna_denoiser* d, int li, const __nv_bfloat16* dz, int n, int h, int w, const __nv_bfloat16* mask,
            __nv_bfloat16* dx) {
   const ConvLayer& c = d->layers[li];
+  if (d->useTc)
+    return asuna_nn_conv3x3_tc(d->stream(), dz, n, h, w, c.cout, d->wtcT + c.wtOff, nullptr, c.cin, 0, mask, dx, 0);
   return asuna_nn_conv3x3(d->stream(), dz, n, h, w, c.cout, d->wt + c.wtOff, nullptr, c.cin, 0, mask, dx, 0);
 }
 
@@ -700,10 +707,17 @@ int convDw(asuna_denoiser* d, int li, const __nv_bfloat16* dz, const __nv_bfloat
   return asuna_nn_bias_grad(d->stream(), dz, n * h * w, c.cout, d->grad + c.bOff);
 }
 
+// weights derived from the bf16 copy: flipped (input gradient) and, for the
+// tcgen05 kernels, both in their operand layout
 int flipAll(asuna_denoiser* d) {
   if (d->flipped) return ASUNA_OK;
-  for (const ConvLayer& c : d->layers)
+  for (const ConvLayer& c : d->layers) {
     NN_TRY(asuna_nn_flip_weights(d->stream(), d->pbf + c.wOff, d->wt + c.wtOff, c.cout, c.cin));
+    if (d->useTc) {
+      NN_TRY(asuna_nn_weights_tc(d->stream(), d->pbf + c.wOff, d->wtc + c.wtOff, c.cout, c.cin));
+      NN_TRY(asuna_nn_weights_tc(d->stream(), d->wt + c.wtOff, d->wtcT + c.wtOff, c.cin, c.cout));
+    }
+  }
   d->flipped = true;
   return ASUNA_OK;
 }
@@ -730,6 +744,7 @@ int forward(asuna_denoiser* d, const float* rad, const float* alb, const float* 
             const Dims& D) {
   const int L = d->L;
   cudaStream_t s = d->stream();
+  if (d->useTc) NN_TRY(flipAll(d));
   const size_t P0 = size_t(D.n) * D.hp * D.wp;
   k_prep_input<<<grid1d(P0), 256, 0, s>>>(reinterpret_cast<const float4*>(rad), reinterpret_cast<const float4*>(alb),
                                           reinterpret_cast<const float4*>(nrm), reinterpret_cast<const float4*>(wsum),
@@ -824,6 +839,7 @@ int asuna_denoiser_create(asuna_ctx* ctx, const asuna_denoiser_opts* o, asuna_de
   d->L = L;
   for (int l = 0; l < L; ++l) d->ch[l] = int(o->channels[l]);
   d->training = o->training != 0;
+  d->useTc = o->tensor_memory != 0;
   d->maxPixels = o->max_pixels;
   // layers in parameter order
   auto add = [&](int cin, int cout) {
@@ -854,6 +870,10 @@ int asuna_denoiser_create(asuna_ctx* ctx, const asuna_denoiser_opts* o, asuna_de
   A(&d->p32, d->nParams);
   A(&d->pbf, d->nParams);
   A(&d->wt, d->nFlip);
+  if (d->useTc) {
+    A(&d->wtc, d->nFlip);
+    A(&d->wtcT, d->nFlip);
+  }
   A(&d->dLoss, 1);
   A(&d->dSums, 2);
   if (d->training) {

@@ -195,9 +195,17 @@ int asuna_ctx_set_counters(asuna_ctx* c, int enable) {
   return ASUNA_OK;
 }
 
-int asuna_ctx_set_traversal(asuna_ctx* c, int refillExtend, int refillShadow, int specExtend, int specShadow) {
+int asuna_ctx_set_traversal(asuna_ctx* c, int refillExtend, int refillShadow, int specExtend, int specShadow,
+                            int blocksPerSm) {
   clearError();
   if (!c) return fail(ASUNA_ERR_INVALID, "null context");
+  if (blocksPerSm != 0 && blocksPerSm != 8 && blocksPerSm != 10 && blocksPerSm != 12)
+    return fail(ASUNA_ERR_INVALID, "traversal blocks per SM %d not in {0, 8, 10, 12}", blocksPerSm);
+  const int occ = blocksPerSm == 0 ? kTraceMinBlocks : blocksPerSm;
+  if (occ != c->occupancy) {
+    c->occupancy = occ;
+    c->traceGrid = c->numSMs * traceBlocksPerSm(occ);
+  }
   const int r[2] = {refillExtend, refillShadow}, sp[2] = {specExtend, specShadow};
   for (int k = 0; k < 2; ++k) {
     if (r[k] < 0 || r[k] > 32) return fail(ASUNA_ERR_INVALID, "refill lanes %d not in [0, 32]", r[k]);
@@ -210,7 +218,7 @@ int asuna_ctx_set_traversal(asuna_ctx* c, int refillExtend, int refillShadow, in
 
 int asuna_ctx_set_launch(asuna_ctx* c, int traceBlocks, int shadeBlocks) {
   if (!c) return fail(ASUNA_ERR_INVALID, "null context");
-  const int tmax = traceBlocksPerSm(), smax = shadeBlocksPerSm();
+  const int tmax = traceBlocksPerSm(c->occupancy), smax = shadeBlocksPerSm();
   const int t = traceBlocks <= 0 ? tmax : std::min(traceBlocks, tmax);
   const int sh = shadeBlocks <= 0 ? smax : std::min(shadeBlocks, smax);
   c->traceGrid = c->numSMs * t;
@@ -651,7 +659,7 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
     key.insert(key.end(), {uint64_t(uintptr_t(c->wave.base)), c->wave.capacity,
            uint64_t(uintptr_t(dShots)), uint64_t(uintptr_t(dRanges)), uint64_t(c->traceGrid), uint64_t(c->shadeGrid),
            uint64_t(c->raygenGrid), uint64_t(c->counters), uint64_t(stats ? 1 : 0), uint64_t(c->refill[0]),
-           uint64_t(c->refill[1]), uint64_t(c->speculate[0]), uint64_t(c->speculate[1])});
+           uint64_t(c->refill[1]), uint64_t(c->speculate[0]), uint64_t(c->speculate[1]), uint64_t(c->occupancy)});
     for (const Batch& b : batches)
       key.insert(key.end(), {b.rangeBegin, b.rangeEnd, b.paths, b.maxPix, uint64_t(b.maxDepth)});
     for (auto& g : c->gcache)
@@ -695,6 +703,7 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
           evi += 2;
         }
       };
+      P.occupancy = c->occupancy;
       P.refillLanes = c->refill[0];
       P.speculate = c->speculate[0];
       timedLaunch(0, [&] { launchExtend(P, c->traceGrid, c->stream); });

@@ -42,6 +42,7 @@ struct asuna_ctx {
   // traversal settings of the extend [0] and connect [1] passes
   uint32_t refill[2] = {8, 8};
   int32_t speculate[2] = {1, 1};
+  int32_t occupancy = 8;  // traversal kernel variant: resident blocks per SM
   uint64_t useClock = 0;
   std::vector<GraphEntry> gcache;
 };

@@ -15,6 +15,7 @@ struct KParams {
   int32_t counters;
   uint32_t refillLanes;  // traversal: idle lanes of a warp that trigger a queue fetch
   int32_t speculate;     // traversal: postponed leaves walk on speculatively
+  int32_t occupancy;     // traversal: resident blocks per SM of the kernel variant (8, 10 or 12)
 };
 
 constexpr int kTraceThreads = 128;
@@ -30,7 +31,7 @@ void launchAccumulate(const KParams& P, uint32_t maxPix, uint32_t nranges, cudaS
 void launchRecords(const KParams& P, asuna_path_record* out, int grid, cudaStream_t s);
 void launchExtend(const KParams& P, int grid, cudaStream_t s);
 void launchConnect(const KParams& P, int grid, cudaStream_t s);
-int traceBlocksPerSm();
+int traceBlocksPerSm(int occupancy = kTraceMinBlocks);
 int shadeBlocksPerSm();
 
 // Standalone ray queries (tests): rays are (o.xyz, tmin), (d.xyz, tmax).

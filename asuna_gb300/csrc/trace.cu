@@ -379,8 +379,9 @@ struct QueueSrc {
   }
 };
 
-template <bool ANY, bool COUNT, bool SPEC>
-__global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_trace(KParams P) {
+// OCC: resident blocks per SM the variant is compiled for (its register cap)
+template <bool ANY, bool COUNT, bool SPEC, int OCC>
+__global__ void __launch_bounds__(kTraceThreads, OCC) k_trace(KParams P) {
   __shared__ int32_t sstack[kSharedStack * kTraceThreads];
   int32_t lstack[kStackDepth - kSharedStack];
   int32_t* sh = sstack + threadIdx.x;
@@ -473,25 +474,38 @@ __global__ void __launch_bounds__(kTraceThreads) k_query(SceneDev S, const float
 
 }  // namespace
 
-void launchExtend(const KParams& P, int grid, cudaStream_t s) {
-  if (P.counters)
-    k_trace<false, true, false><<<grid, kTraceThreads, 0, s>>>(P);
-  else if (P.speculate)
-    k_trace<false, false, true><<<grid, kTraceThreads, 0, s>>>(P);
+namespace {
+template <bool ANY, int OCC>
+void launchTraceOcc(const KParams& P, int grid, cudaStream_t s) {
+  if (P.speculate)
+    k_trace<ANY, false, true, OCC><<<grid, kTraceThreads, 0, s>>>(P);
   else
-    k_trace<false, false, false><<<grid, kTraceThreads, 0, s>>>(P);
+    k_trace<ANY, false, false, OCC><<<grid, kTraceThreads, 0, s>>>(P);
 }
-void launchConnect(const KParams& P, int grid, cudaStream_t s) {
+template <bool ANY>
+void launchTrace(const KParams& P, int grid, cudaStream_t s) {
   if (P.counters)
-    k_trace<true, true, false><<<grid, kTraceThreads, 0, s>>>(P);
-  else if (P.speculate)
-    k_trace<true, false, true><<<grid, kTraceThreads, 0, s>>>(P);
+    k_trace<ANY, true, false, kTraceMinBlocks><<<grid, kTraceThreads, 0, s>>>(P);
+  else if (P.occupancy >= 12)
+    launchTraceOcc<ANY, 12>(P, grid, s);
+  else if (P.occupancy >= 10)
+    launchTraceOcc<ANY, 10>(P, grid, s);
   else
-    k_trace<true, false, false><<<grid, kTraceThreads, 0, s>>>(P);
+    launchTraceOcc<ANY, kTraceMinBlocks>(P, grid, s);
 }
-int traceBlocksPerSm() {
+}  // namespace
+
+void launchExtend(const KParams& P, int grid, cudaStream_t s) { launchTrace<false>(P, grid, s); }
+void launchConnect(const KParams& P, int grid, cudaStream_t s) { launchTrace<true>(P, grid, s); }
+int traceBlocksPerSm(int occupancy) {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace<false, false, true>, kTraceThreads, 0);
+  if (occupancy >= 12)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace<false, false, true, 12>, kTraceThreads, 0);
+  else if (occupancy >= 10)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace<false, false, true, 10>, kTraceThreads, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace<false, false, true, kTraceMinBlocks>, kTraceThreads,
+                                                  0);
   return n > 0 ? n : 1;
 }
 void launchTraceQuery(const SceneDev& S, const float4* o, const float4* d, uint32_t n, int anyHit, float4* hit,

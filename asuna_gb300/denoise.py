@@ -64,7 +64,8 @@ def ctx_stream(ctx):
 
 
 class Denoiser:
-    def __init__(self, ctx, channels=DEFAULT_CHANNELS, seed=0, max_pixels=1 << 20, training=False):
+    def __init__(self, ctx, channels=DEFAULT_CHANNELS, seed=0, max_pixels=1 << 20, training=False,
+                 tensor_memory=False):
         self.ctx = ctx
         self.channels = tuple(int(c) for c in channels)
         o = A.DenoiserOpts()
@@ -74,6 +75,7 @@ class Denoiser:
         o.seed = seed
         o.max_pixels = int(max_pixels)
         o.training = 1 if training else 0
+        o.tensor_memory = 1 if tensor_memory else 0
         h = C.c_void_p()
         check(lib().asuna_denoiser_create(ctx.handle, C.byref(o), C.byref(h)))
         self.handle = h

@@ -422,9 +422,10 @@ class Context:
     def set_graphs(self, on):
         check(lib().asuna_ctx_set_graphs(self.handle, 1 if on else 0))
 
-    def set_traversal(self, refill_extend=0, refill_shadow=0, speculate_extend=-1, speculate_shadow=-1):
+    def set_traversal(self, refill_extend=0, refill_shadow=0, speculate_extend=-1, speculate_shadow=-1,
+                      blocks_per_sm=0):
         check(lib().asuna_ctx_set_traversal(self.handle, int(refill_extend), int(refill_shadow),
-                                            int(speculate_extend), int(speculate_shadow)))
+                                            int(speculate_extend), int(speculate_shadow), int(blocks_per_sm)))
 
     def set_launch(self, trace_blocks_per_sm=0, shade_blocks_per_sm=0):
         check(lib().asuna_ctx_set_launch(self.handle, int(trace_blocks_per_sm), int(shade_blocks_per_sm)))

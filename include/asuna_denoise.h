@@ -45,7 +45,7 @@ typedef struct asuna_denoiser_opts {
   uint64_t seed;                                 /* He-normal initialisation */
   uint64_t max_pixels;                           /* n*h*w of the largest call (padded) */
   uint32_t training;                             /* 1: allocate gradient and Adam state */
-  uint32_t reserved;
+  uint32_t tensor_memory;                        /* 1: convolutions on tcgen05 (TMEM accumulators, TMA) */
 } asuna_denoiser_opts;
 
 typedef struct asuna_denoiser asuna_denoiser;
@@ -103,6 +103,16 @@ int asuna_nn_upsample2_bwd(void* stream, const void* dout, void* din, int n, int
 int asuna_nn_copy_channels(void* stream, const void* src, int csrc, int soff, void* dst, int cdst, int doff, int c,
                            uint64_t pixels, int accumulate);
 int asuna_nn_relu_mask(void* stream, void* grad, const void* y, uint64_t count);
+/* The same convolution on the fifth-generation tensor cores: tcgen05.mma
+ * with the accumulator in tensor memory, TMA-staged operands, weights in
+ * the layout asuna_nn_weights_tc makes ([cin/16][9][2][cout][8]);
+ * cin % 16 == 0, cout % 16 == 0, cout <= 256, 16-byte aligned operands.
+ * A CTA whose bounded waits expire writes nothing and sets the flag that
+ * asuna_nn_tc_status reports (and clears). */
+int asuna_nn_weights_tc(void* stream, const void* w, void* wtc, int cout, int cin);
+int asuna_nn_conv3x3_tc(void* stream, const void* in, int n, int h, int w, int cin, const void* weight_tc,
+                        const float* bias, int cout, int relu, const void* mask, void* out, int out_f32);
+int asuna_nn_tc_status(int* expired);
 int asuna_nn_f32_to_bf16(void* stream, const float* a, void* b, uint64_t n);
 
 #ifdef __cplusplus

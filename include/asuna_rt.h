@@ -321,10 +321,12 @@ int asuna_ctx_set_graphs(asuna_ctx* ctx, int enable);
 int asuna_ctx_set_launch(asuna_ctx* ctx, int trace_blocks_per_sm, int shade_blocks_per_sm);
 /* Traversal settings of the closest-hit (extend) and occlusion (shadow)
  * passes: idle lanes of a warp that trigger a refill from the ray queue
- * (1..32, 0 = default 8) and speculative walking past a postponed leaf
- * (1 on, 0 off, -1 default on).  Results do not depend on them. */
+ * (1..32, 0 = default 8), speculative walking past a postponed leaf (1 on,
+ * 0 off, -1 default on) and the kernel variant's resident blocks per SM
+ * (8, 10 or 12 — fewer registers, more warps; 0 = default 8).  Results do
+ * not depend on them. */
 int asuna_ctx_set_traversal(asuna_ctx* ctx, int refill_extend, int refill_shadow, int speculate_extend,
-                            int speculate_shadow);
+                            int speculate_shadow, int blocks_per_sm);
 
 /* ---- scene: upload + acceleration-structure build ------------------------ */
 /* Replaces Scene::submit + BLAS/TLAS build.  Host arrays are deep-copied; the

@@ -84,7 +84,7 @@ def test_traversal_settings_do_not_change_results(ctx):
     b, shot = scenes.plugin_scene(64, 48, frames=2, max_depth=6)
     scene = ctx.create_scene(b.desc())
     films = []
-    for trav in ((8, 8, 1, 1), (1, 32, 0, 0), (32, 1, 1, 0), (4, 16, 0, 1)):
+    for trav in ((8, 8, 1, 1, 8), (1, 32, 0, 0, 10), (32, 1, 1, 0, 12), (4, 16, 0, 1, 10)):
         ctx.set_traversal(*trav)
         f = ctx.create_film(64, 48)
         ctx.render(scene, shot, f)

@@ -88,6 +88,65 @@ def test_conv3x3_input_gradient_with_mask(lib):
     assert np.abs(host(out) - ref).max() <= 2e-5 * np.abs(ref).max()
 
 
+@pytest.mark.parametrize("shape", [(1, 16, 8, 16, 16), (2, 20, 24, 32, 48), (1, 33, 70, 224, 96),
+                                   (1, 40, 37, 48, 128), (3, 9, 13, 16, 32), (1, 24, 16, 96, 64)])
+def test_conv3x3_tcgen05(lib, shape):
+    """The tcgen05 / TMEM / TMA convolution against the float64 reference:
+    edge tiles (sizes not multiples of 16 x 8), batches, 16..224 input and
+    16..128 output channels; bias, ReLU, mask and fp32 / bf16 outputs."""
+    n, h, w, cin, cout = shape
+    rng = np.random.default_rng(cin * 7 + cout)
+    x = U.round_bf16(rng.normal(size=(n, h, w, cin)))
+    wt = U.round_bf16(rng.normal(0, 0.2, (cout, 9, cin)))
+    b = rng.normal(0, 0.1, cout).astype(np.float32)
+    mask = U.round_bf16(rng.normal(size=(n, h, w, cout)))
+    dx, dwt, db, dmask = bf16(x), bf16(wt), f32(b), bf16(mask)
+    wtc = torch.empty(cout * 9 * cin, dtype=torch.bfloat16, device="cuda")
+    run(lib, "asuna_nn_weights_tc", ptr(dwt), ptr(wtc), cout, cin)
+    out = torch.full((n, h, w, cout), float("nan"), dtype=torch.float32, device="cuda")
+    run(lib, "asuna_nn_conv3x3_tc", ptr(dx), n, h, w, cin, ptr(wtc), ptr(db), cout, 0, None, ptr(out), 1)
+    expired = C.c_int(-1)
+    A.check(lib.asuna_nn_tc_status(C.byref(expired)))
+    assert expired.value == 0
+    ref = U.conv3x3(x, wt, b.astype(np.float64))
+    got = host(out)
+    assert np.isfinite(got).all()
+    assert np.abs(got - ref).max() <= 2e-5 * np.abs(ref).max()
+    outb = torch.empty((n, h, w, cout), dtype=torch.bfloat16, device="cuda")
+    run(lib, "asuna_nn_conv3x3_tc", ptr(dx), n, h, w, cin, ptr(wtc), ptr(db), cout, 1, ptr(dmask), ptr(outb), 0)
+    rr = U.round_bf16(np.maximum(ref, 0) * (mask > 0))
+    gb = host(outb)
+    assert np.all(np.abs(gb - rr) <= np.abs(rr) * 2.0 ** -7 + 2e-5 * np.abs(ref).max())
+    A.check(lib.asuna_nn_tc_status(C.byref(expired)))
+    assert expired.value == 0
+
+
+def test_network_on_tcgen05_matches_mma_sync(dctx):
+    """The whole denoiser (forward, loss, gradients) with every forward and
+    input-gradient convolution on tcgen05 equals the mma.sync network up to
+    accumulation order."""
+    rng = np.random.default_rng(8)
+    n, h, w = 2, 40, 56
+    rad, alb, nrm, wsum, tgt = _net_inputs(rng, n, h, w)
+    p = U.he_init(dn.DEFAULT_CHANNELS, 4)
+    p = (p + rng.normal(0, 0.02, p.size)).astype(np.float32)
+    res = []
+    for tm in (False, True):
+        d = dn.Denoiser(dctx, seed=4, max_pixels=n * 48 * 64, training=True, tensor_memory=tm)
+        d.set_params(p)
+        drad, dalb, dnrm, dw, dtgt = f32(rad), f32(alb), f32(nrm), f32(wsum), f32(tgt)
+        torch.cuda.synchronize()
+        out = d.forward(drad, dalb, dnrm, dw)
+        dctx.sync()
+        loss = d.loss_grad(drad, dalb, dnrm, dw, dtgt)
+        res.append((out.cpu().numpy(), loss, d.get_grads().astype(np.float64)))
+    (o0, l0, g0), (o1, l1, g1) = res
+    assert np.median(np.abs(o1 - o0) / (np.abs(o0) + 1e-3)) < 2e-3
+    assert abs(l1 - l0) <= 1e-3 * l0
+    rel = np.linalg.norm(g1 - g0) / np.linalg.norm(g0)
+    assert rel < 0.03, rel
+
+
 @pytest.mark.parametrize("shape", [(2, 40, 64, 32, 48), (1, 16, 16, 16, 16), (3, 23, 37, 112, 48)])
 def test_conv3x3_weight_gradient(lib, shape):
     n, h, w, cin, cout = shape  # > 2048 pixels: several split-K blocks
