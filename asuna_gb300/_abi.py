@@ -17,7 +17,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_IO, ERR_PARSE, ERR_TIMEOUT, ERR_UNSUPPOR
 CAMERA_PERSPECTIVE, CAMERA_OPENCV = 0, 1
 LIGHT_DIRECTIONAL, LIGHT_RECT, LIGHT_TRIANGLE, LIGHT_POINT = 0, 1, 2, 3
 MAT_LAMBERTIAN, MAT_EMISSIVE, MAT_PLASTIC, MAT_ROUGH_PLASTIC, MAT_MIRROR, MAT_DIELECTRIC = 0, 2, 4, 5, 8, 10
-MAT_CONDUCTOR, MAT_ROUGH_CONDUCTOR = 6, 7
+MAT_CONDUCTOR, MAT_ROUGH_CONDUCTOR, MAT_PHONG = 6, 7, 11
 CH_DIFFUSE, CH_NORMAL, CH_SPECULAR, CH_TANGENT, CH_ROUGHNESS, CH_POSITION, CH_UV, CH_DEPTH = range(8)
 SHOT_RR = 1
 NUM_OUTPUT_IMAGES = 9
@@ -102,7 +102,8 @@ class RenderStats(C.Structure):
                 ("nodes_visited", C.c_uint64), ("tris_tested", C.c_uint64),
                 ("shadow_nodes_visited", C.c_uint64), ("shadow_tris_tested", C.c_uint64), ("ms_total", C.c_double),
                 ("ms_extend", C.c_double), ("ms_connect", C.c_double), ("ms_shade", C.c_double),
-                ("extend_launches", C.c_uint64), ("connect_launches", C.c_uint64)]
+                ("extend_launches", C.c_uint64), ("connect_launches", C.c_uint64),
+                ("kernel_launches", C.c_uint64)]
 
 
 class PostState(C.Structure):

@@ -2,9 +2,12 @@
 // fifth-generation tensor cores: tcgen05.mma with the accumulator in tensor
 // memory, operands staged in shared memory by TMA.
 //
-// One CTA computes a 16 x 8 pixel tile (M = 128) for all output channels
-// (N = cout <= 256, a multiple of 16).  The input channels are consumed in
-// groups of 16 (K = 16 per MMA):
+// One CTA computes a 16 x 8 pixel tile (M = 128) for one slice of nt output
+// channels (N = nt, a multiple of 16, at most 256 and small enough that three
+// weight stages fit shared memory; cout is split into cout / nt slices, the
+// slice index varying fastest across the grid so the CTAs that read one
+// activation tile run together and share it in L2).  The input channels are
+// consumed in groups of 16 (K = 16 per MMA):
 //   * activations: for each 8-channel chunk, one TMA tiled load of the
 //     18 x 10 halo of the tile from the NHWC tensor (zero fill outside the
 //     image) lands as [row][col][8] bf16 (blocks 2,944 B apart, 128-byte
@@ -13,8 +16,9 @@
 //     pixels of one image row, image rows are 160 B apart (stride
 //     dimension), the second 8-channel chunk is one block further (leading
 //     dimension) — K-major, no swizzle;
-//   * weights: pre-arranged as [cin/16][tap][chunk][cout][8] so one group's
-//     nine taps are one contiguous bulk copy, B = [chunk][cout][8] per tap;
+//   * weights: pre-arranged as [slice][cin/16][tap][chunk][nt][8] so one
+//     group's nine taps are one contiguous bulk copy, B = [chunk][nt][8] per
+//     tap;
 //   * nine MMAs per group accumulate into TMEM (fp32, lane = pixel,
 //     column = output channel); a 3-stage ring of shared-memory buffers is
 //     refilled as tcgen05.commit reports each stage's MMAs done.
@@ -46,9 +50,21 @@ constexpr int kActStage = 2 * kChunkBytes;  // 16 channels
 constexpr int kStages = 3;
 constexpr int kThreads = 128;
 constexpr int kPadBytes = 48 * 1024;                           // slack past the operands
-constexpr uint32_t kWaitLimit = 1u << 26;                      // try_wait rounds before giving up
+constexpr uint32_t kWaitLimit = 1u << 20;                      // try_wait rounds before giving up
 
 __device__ int g_tcError;  // set when a wait expired; read and cleared by asuna_nn_tc_status
+
+constexpr size_t kSmemLimit = 227 * 1024;
+size_t smemFor(int nt) { return 128 + size_t(kStages) * (kActStage + size_t(9 * 2 * nt * 16)) + kPadBytes; }
+// Output channels per CTA: the widest slice (fewest slices) that divides cout
+// into multiples of 16 and whose stages fit shared memory.
+int sliceWidth(int cout) {
+  for (int s = 1; s <= cout / 16; ++s) {
+    const int nt = cout / s;
+    if (cout % s == 0 && nt % 16 == 0 && nt <= 256 && smemFor(nt) <= kSmemLimit) return nt;
+  }
+  return 16;
+}
 
 __device__ __forceinline__ uint32_t smem(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
 
@@ -121,15 +137,16 @@ __device__ __forceinline__ void ld16(uint32_t taddr, float* v) {
 }
 
 struct TcArgs {
-  const __nv_bfloat16* wt;    // [cin/16][9][2][cout][8]
+  const __nv_bfloat16* wt;    // [cout/nt][cin/16][9][2][nt][8]
   const float* bias;          // [cout] or null
   const __nv_bfloat16* mask;  // [P][cout] or null
   void* out;                  // [P][cout]
   int n, h, w, cin, cout;
+  int nt, slices;             // output channels per CTA, cout / nt
   int tilesX, tilesY;
   int relu, outF32;
   uint32_t tmemCols;
-  uint32_t wStageBytes;  // 9 * 2 * cout * 16
+  uint32_t wStageBytes;  // 9 * 2 * nt * 16
 };
 
 __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__ CUtensorMap act, TcArgs a) {
@@ -145,6 +162,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   int t = blockIdx.x;
+  const int slice = t % a.slices;
+  t /= a.slices;
+  const int n0 = slice * a.nt;
+  const __nv_bfloat16* wt = a.wt + size_t(slice) * size_t(a.cin / 16) * (a.wStageBytes / 2);
   const int tx = t % a.tilesX;
   t /= a.tilesX;
   const int ty = t % a.tilesY;
@@ -173,15 +194,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
   const uint32_t tmem = *tmemSlot;
 
   const int groups = a.cin / 16;
-  if (tid == 0) {
-    const uint32_t idesc = instrDesc(uint32_t(a.cout));
+  // a CTA that finds an expired wait recorded skips its work: one failure
+  // costs one timeout, not one per CTA
+  if (tid == 0 && *reinterpret_cast<volatile int*>(&g_tcError)) *abortFlag = 1;
+  if (tid == 0 && !*abortFlag) {
+    const uint32_t idesc = instrDesc(uint32_t(a.nt));
     auto issue = [&](int s, int g) {
       const uint32_t bar = smem(&full[s]);
       mbarExpectTx(bar, uint32_t(2 * kBoxBytes) + a.wStageBytes);
       const uint32_t dstA = smem(actBase + s * kActStage);
       tmaLoad4d(dstA, &act, g * 16, x0 - 1, y0 - 1, img, bar);
       tmaLoad4d(dstA + kChunkBytes, &act, g * 16 + 8, x0 - 1, y0 - 1, img, bar);
-      bulkLoad(smem(wBase + size_t(s) * a.wStageBytes), a.wt + size_t(g) * (a.wStageBytes / 2), a.wStageBytes, bar);
+      bulkLoad(smem(wBase + size_t(s) * a.wStageBytes), wt + size_t(g) * (a.wStageBytes / 2), a.wStageBytes, bar);
     };
     bool ok = true;
     for (int g = 0; g < groups && g < kStages; ++g) issue(g, g);
@@ -194,12 +218,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
       }
       const uint32_t aBase = smem(actBase + s * kActStage);
       const uint32_t bBase = smem(wBase + size_t(s) * a.wStageBytes);
-      const uint32_t bTap = uint32_t(2 * a.cout * 16);
+      const uint32_t bTap = uint32_t(2 * a.nt * 16);
 #pragma unroll 1
       for (int tap = 0; tap < 9; ++tap) {
         const int dy = tap / 3, dx = tap % 3;
         const uint64_t da = matDesc(aBase + uint32_t(dy * kHaloW + dx) * 16u, kChunkBytes, kHaloW * 16);
-        const uint64_t db = matDesc(bBase + uint32_t(tap) * bTap, uint32_t(a.cout * 16), 128u);
+        const uint64_t db = matDesc(bBase + uint32_t(tap) * bTap, uint32_t(a.nt * 16), 128u);
         mma(tmem, da, db, idesc, (g > 0 || tap > 0) ? 1u : 0u);
       }
       commit(smem(&empty[s]));
@@ -231,13 +255,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
     const bool inside = py < a.h && px < a.w;
     const size_t p = (size_t(img) * a.h + py) * a.w + px;
     const uint32_t laneBase = tmem + (uint32_t(warp * 32) << 16);
-    for (int c0 = 0; c0 < a.cout; c0 += 16) {
+    for (int c0 = 0; c0 < a.nt; c0 += 16) {
       float v[16];
       ld16(laneBase + uint32_t(c0), v);
       if (!inside) continue;
 #pragma unroll
       for (int i = 0; i < 16; i += 2) {
-        const int co = c0 + i;
+        const int co = n0 + c0 + i;
         float v0 = v[i], v1 = v[i + 1];
         if (a.bias) {
           v0 += a.bias[co];
@@ -268,13 +292,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
   }
 }
 
-// [cout][9][cin] -> [cin/16][9][2][cout][8]
-__global__ void k_weights_tc(const __nv_bfloat16* w, __nv_bfloat16* o, int cout, int cin) {
+// [cout][9][cin] -> [cout/nt][cin/16][9][2][nt][8]
+__global__ void k_weights_tc(const __nv_bfloat16* w, __nv_bfloat16* o, int cout, int cin, int nt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= cout * 9 * cin) return;
   const int ci = i % cin, tap = (i / cin) % 9, co = i / (9 * cin);
   const int g = ci / 16, c = (ci / 8) & 1, e = ci & 7;
-  o[((((size_t(g) * 9 + tap) * 2 + c) * cout + co) * 8) + e] = w[i];
+  const int slice = co / nt, cl = co % nt;
+  o[(((((size_t(slice) * (cin / 16) + g) * 9 + tap) * 2 + c) * nt + cl) * 8) + e] = w[i];
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -308,7 +333,7 @@ int asuna_nn_weights_tc(void* stream, const void* w, void* wtc, int cout, int ci
   if (!w || !wtc || cin % 16 || cout % 16) return fail(ASUNA_ERR_INVALID, "asuna_nn_weights_tc: bad argument");
   const int n = cout * 9 * cin;
   k_weights_tc<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      static_cast<const __nv_bfloat16*>(w), static_cast<__nv_bfloat16*>(wtc), cout, cin);
+      static_cast<const __nv_bfloat16*>(w), static_cast<__nv_bfloat16*>(wtc), cout, cin, sliceWidth(cout));
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? ASUNA_OK : fail(ASUNA_ERR_CUDA, "asuna_nn_weights_tc: %s", cudaGetErrorString(e));
 }
@@ -317,8 +342,8 @@ int asuna_nn_conv3x3_tc(void* stream, const void* in, int n, int h, int w, int c
                         const float* bias, int cout, int relu, const void* mask, void* out, int out_f32) {
   if (!in || !weight_tc || !out || n <= 0 || h <= 0 || w <= 0)
     return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: bad argument");
-  if (cin % 16 || cout % 16 || cout > 256)
-    return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: cin %% 16, cout %% 16 and cout <= 256 required");
+  if (cin % 16 || cout % 16)
+    return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: cin %% 16 and cout %% 16 required");
   if (reinterpret_cast<uintptr_t>(in) % 16 || reinterpret_cast<uintptr_t>(weight_tc) % 16)
     return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: operands must be 16-byte aligned");
   EncodeTiledFn enc = encodeFn();
@@ -347,15 +372,17 @@ int asuna_nn_conv3x3_tc(void* stream, const void* in, int n, int h, int w, int c
   a.tilesY = (h + kTileH - 1) / kTileH;
   a.relu = relu;
   a.outF32 = out_f32;
-  a.tmemCols = cout <= 32 ? 32u : cout <= 64 ? 64u : cout <= 128 ? 128u : 256u;
-  a.wStageBytes = uint32_t(9 * 2 * cout * 16);
-  const size_t smemBytes = 128 + size_t(kStages) * (kActStage + a.wStageBytes) + kPadBytes;
+  a.nt = sliceWidth(cout);
+  a.slices = cout / a.nt;
+  a.tmemCols = a.nt <= 32 ? 32u : a.nt <= 64 ? 64u : a.nt <= 128 ? 128u : 256u;
+  a.wStageBytes = uint32_t(9 * 2 * a.nt * 16);
+  const size_t smemBytes = smemFor(a.nt);
   static std::once_flag attr;
   std::call_once(attr, [] {
-    cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemLimit));
   });
-  if (smemBytes > 227 * 1024) return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: cout %d needs too much shared memory", cout);
-  const long long blocks = (long long)a.tilesX * a.tilesY * n;
+  if (smemBytes > kSmemLimit) return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: cout %d needs too much shared memory", cout);
+  const long long blocks = (long long)a.tilesX * a.tilesY * n * a.slices;
   if (blocks > (1ll << 31) - 1) return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: too many tiles");
   k_conv_tc<<<unsigned(blocks), kThreads, smemBytes, static_cast<cudaStream_t>(stream)>>>(map, a);
   const cudaError_t e = cudaGetLastError();

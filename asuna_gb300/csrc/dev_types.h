@@ -95,6 +95,7 @@ struct SceneDev {
   int32_t tlasRoot;
   int32_t envW, envH;
   int32_t numInst;
+  uint32_t classMask;  // shading classes some instance can reach (bit k = class k)
 };
 
 // ---- shots, films, batches ----------------------------------------------------
@@ -143,8 +144,26 @@ enum ShadeClass {
   kClsMirror = 5,
   kClsConductor = 6,
   kClsRoughConductor = 7,
-  kNumShadeClasses = 8
+  kClsPhong = 8,
+  kNumShadeClasses = 9
 };
+// The class that shades a hit on a surface of material `type` (not a light).
+#if defined(__CUDACC__)
+__host__ __device__
+#endif
+inline int shadeClassOf(uint32_t type) {
+  switch (type) {
+    case ASUNA_MAT_ROUGH_PLASTIC: return kClsRoughPlastic;
+    case ASUNA_MAT_DIELECTRIC: return kClsDielectric;
+    case ASUNA_MAT_PLASTIC: return kClsPlastic;
+    case ASUNA_MAT_MIRROR: return kClsMirror;
+    case ASUNA_MAT_CONDUCTOR: return kClsConductor;
+    case ASUNA_MAT_ROUGH_CONDUCTOR: return kClsRoughConductor;
+    case ASUNA_MAT_PHONG: return kClsPhong;
+    case ASUNA_MAT_EMISSIVE: return kClsTerminal;
+    default: return kClsLambertian;
+  }
+}
 struct DevCounters {
   uint32_t c[kCntNum32];
   unsigned long long extendRays;

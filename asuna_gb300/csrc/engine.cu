@@ -343,6 +343,7 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
     I.matId = id.light_id >= 0 ? -1 : id.material_id;
     I.lightId = id.light_id;
     I.matType = id.light_id >= 0 ? 0u : d->materials[id.material_id].type;
+    s->view.classMask |= 1u << (id.light_id >= 0 ? int(kClsTerminal) : shadeClassOf(I.matType));
     if (empty) continue;
     // world box of the BLAS root's children
     const BvhNode& r = blas[m].nodes[0];
@@ -412,7 +413,9 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
     const float* rgb = m.type == ASUNA_MAT_EMISSIVE ? m.radiance : m.diffuse;
     mats[i].a = make_float4(rgb[0], rgb[1], rgb[2], tb);
     mats[i].b = make_float4(m.aniso_alpha[0], m.aniso_alpha[1], m.ior, m.radiance[0]);
-    mats[i].c = make_float4(m.radiance[0], m.radiance[1], m.radiance[2], 0.0f);
+    // Phong: specular reflectance and exponent (rhoSpec, specular); others: radiance
+    mats[i].c = m.type == ASUNA_MAT_PHONG ? make_float4(m.rho_spec[0], m.rho_spec[1], m.rho_spec[2], m.specular)
+                                          : make_float4(m.radiance[0], m.radiance[1], m.radiance[2], 0.0f);
     mats[i].d = make_float4(m.radiance_factor[0], m.radiance_factor[1], m.radiance_factor[2], 0.0f);
   }
   std::vector<LightDev> lights(std::max(1u, d->num_lights));
@@ -761,6 +764,9 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
     stats->tris_tested = c->hostCnt->tris;
     stats->shadow_nodes_visited = c->hostCnt->shNodes;
     stats->shadow_tris_tested = c->hostCnt->shTris;
+    // raygen + accumulate (+ records) per wave; extend, shading, connect per depth
+    for (const Batch& b : batches)
+      stats->kernel_launches += 2 + (hostRecords ? 1 : 0) + uint64_t(b.maxDepth) * (2 + shadeLaunches(s->view.classMask));
     float ms = 0;
     ASUNA_CUDA_TRY(cudaEventElapsedTime(&ms, c->events[0], c->events[1]));
     stats->ms_total = ms;

@@ -64,7 +64,7 @@ int validateSceneDesc(const asuna_scene_desc* d) {
     uint32_t t = d->materials[i].type;
     if (t != ASUNA_MAT_LAMBERTIAN && t != ASUNA_MAT_ROUGH_PLASTIC && t != ASUNA_MAT_DIELECTRIC &&
         t != ASUNA_MAT_EMISSIVE && t != ASUNA_MAT_PLASTIC && t != ASUNA_MAT_MIRROR && t != ASUNA_MAT_CONDUCTOR &&
-        t != ASUNA_MAT_ROUGH_CONDUCTOR)
+        t != ASUNA_MAT_ROUGH_CONDUCTOR && t != ASUNA_MAT_PHONG)
       return fail(ASUNA_ERR_UNSUPPORTED, "material %u: type %u is not implemented", i, t);
     const asuna_material& m = d->materials[i];
     if (m.diffuse_texture_id >= 0 || m.normal_texture_id >= 0 || m.roughness_texture_id >= 0 ||
@@ -993,6 +993,16 @@ int addMaterial(LoadCtx& L, const Json& mj) {
       if (mj.has("alpha")) REQUIRE(vecN(mj["alpha"], 2, m.aniso_alpha), "bad alpha");
       if ((rc = tex("alpha_texture", m.roughness_texture_id))) return rc;
     }
+  } else if (t == "brdf_phong") {
+    // src/loader/material.cpp:391-405: specular reflectance in rho_spec, the
+    // exponent in specular
+    m.type = ASUNA_MAT_PHONG;
+    if ((rc = tex("normal_texture", m.normal_texture_id))) return rc;
+    if (mj.has("diffuse_reflectance")) REQUIRE(vecN(mj["diffuse_reflectance"], 3, m.diffuse), "bad diffuse_reflectance");
+    if ((rc = tex("diffuse_texture", m.diffuse_texture_id))) return rc;
+    if (mj.has("specular_reflectance"))
+      REQUIRE(vecN(mj["specular_reflectance"], 3, m.rho_spec), "bad specular_reflectance");
+    if (mj.has("shininess")) m.specular = float(mj["shininess"].num);
   } else if (t == "brdf_emissive") {
     // src/loader/material.cpp:145-155
     m.type = ASUNA_MAT_EMISSIVE;
@@ -1000,7 +1010,7 @@ int addMaterial(LoadCtx& L, const Json& mj) {
     if (mj.has("radiance_factor")) REQUIRE(vecN(mj["radiance_factor"], 3, m.radiance_factor), "bad radiance_factor");
     if ((rc = tex("radiance_texture", m.radiance_texture_id))) return rc;
   } else {
-    static const char* known[] = {"brdf_pbr_metalness_roughness", "brdf_kang18", "brdf_disney", "brdf_phong"};
+    static const char* known[] = {"brdf_pbr_metalness_roughness", "brdf_kang18", "brdf_disney"};
     for (const char* k : known)
       if (t == k) return fail(ASUNA_ERR_UNSUPPORTED, "material type [%s] is not implemented", t.c_str());
     return fail(ASUNA_ERR_PARSE, "unrecognized material type [%s]", t.c_str());

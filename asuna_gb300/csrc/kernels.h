@@ -27,6 +27,8 @@ constexpr int kShadeMinBlocks = 3;   // resident 256-thread blocks per SM the sh
 
 void launchRaygen(const KParams& P, int grid, cudaStream_t s);
 void launchShade(const KParams& P, int grid, cudaStream_t s);
+// kernels launchShade issues for a scene's class mask (classify included)
+int shadeLaunches(uint32_t classMask);
 void launchAccumulate(const KParams& P, uint32_t maxPix, uint32_t nranges, cudaStream_t s);
 void launchRecords(const KParams& P, asuna_path_record* out, int grid, cudaStream_t s);
 void launchExtend(const KParams& P, int grid, cudaStream_t s);

@@ -13,7 +13,9 @@
 //   shade/miss  raytrace.default.rmiss:24-56
 //   shade/hit   rchit_layouts.glsl:61-167, brdf_lambertian.rchit:12-151,
 //               brdf_rough_plastic.rchit:191-269, bsdf_dielectric.rchit:74-139,
-//               brdf_emissive.rchit:12-27
+//               brdf_emissive.rchit:12-27, brdf_plastic.rchit:43-205,
+//               brdf_mirror.rchit:12-106, brdf_conductor.rchit:14-164,
+//               brdf_rough_conductor.rchit, brdf_phong.rchit:12-194
 //   accumulate  raytrace.projective.rgen:134-179
 //
 // Compiled with -fmad=false: the float arithmetic rounds operation by
@@ -223,6 +225,25 @@ __device__ __forceinline__ f3 sampleLights(const SceneDev& S, const ShotDev& sh,
 }
 
 // Next-event estimation of a material hit.  The three material hit shaders
+// brdf_phong.rchit:12-30 (flag EArea): normalised Phong lobe mixed with the
+// Lambertian lobe by the luminances of the two reflectances.
+__device__ __forceinline__ f3 phongEval(f3 L, f3 V, f3 N, f3 kd, f3 ks, float n) {
+  const float NdotL = dot(N, L), NdotV = dot(N, V);
+  if (NdotL < 0.0f || NdotV < 0.0f) return splat(0.0f);
+  const f3 H = normalize(L + V);
+  const f3 diffuseLobe = kd * INV_PI;
+  const f3 specularLobe = ks * mpow(gmax(dot(H, N), 0.0f), n) * (n + 2.0f) * INV_2PI;
+  const float db = luminance(kd), sb = luminance(ks);
+  const float dw = db / (db + sb), sw = 1.0f - dw;
+  return (dw * diffuseLobe + sw * specularLobe) * NdotL;
+}
+// brdf_phong.rchit:32-37
+__device__ __forceinline__ float phongLobePdf(f3 L, f3 V, f3 N, float n) {
+  const f3 H = normalize(L + V);
+  const float NdotH = gmax(dot(H, N), 0.0f), VdotH = gmax(dot(H, V), 0.0f);
+  return (n + 1.0f) * INV_2PI * mpow(NdotH, n) * 0.25f / (VdotH + EPS);
+}
+
 // (brdf_lambertian.rchit:110-134, brdf_rough_plastic.rchit:224-250,
 // bsdf_dielectric.rchit:248-271) all start with sampleLights(pos, ffN) and
 // differ only in the BSDF eval/pdf pair, so light sampling runs once here and
@@ -310,6 +331,15 @@ __device__ __forceinline__ void nextEvent(const SceneDev& S, const ShotDev& sh, 
         } else {
           if (fabsf(dot(refract(-V, N, eta), L) - 1.0f) < EPS) bpdf = 1.0f - F;
         }
+      }
+    } else if (type == ASUNA_MAT_PHONG) {
+      // brdf_phong.rchit:12-30 eval with EArea, 39-52 pdf with lRec.flags
+      const f3 kd = ld3(m.a), ks = ld3(m.c);
+      w = phongEval(lRec.d, st.V, st.ffN, kd, ks, m.c.w);
+      if (lRec.flags & EArea) {
+        const float db = luminance(kd), sb = luminance(ks);
+        const float dw = db / (db + sb), sw = 1.0f - dw;
+        bpdf = dw * cosineHemispherePdf(dot(st.ffN, lRec.d)) + sw * phongLobePdf(lRec.d, st.V, st.ffN, m.c.w);
       }
     } else {
       // Lambertian eval 12-21 (flag EArea), pdf 23-29 (lRec.flags)
@@ -451,6 +481,47 @@ __device__ __forceinline__ void samplePlastic(PathIO& io, const HitSt& st, const
   io.thp = io.thp * (weight / (bpdf + EPS));
 }
 
+// brdf_phong.rchit:54-84,178-193: lobe chosen by the diffuse weight; the
+// Phong lobe samples the half vector (cos^(1/(n+1))) and reflects V about it
+__device__ __forceinline__ void samplePhong(PathIO& io, const HitSt& st, const MatDev& m) {
+  const f3 kd = ld3(m.a), ks = ld3(m.c);
+  const float n = m.c.w;
+  f2 u = rnd2(io.seed);
+  const f3 V = st.V, N = st.ffN, X = st.X, Y = st.Y;
+  const float db = luminance(kd), sb = luminance(ks);
+  const float dw = db / (db + sb), sw = 1.0f - dw;
+  f3 bd;
+  float bpdf;
+  uint32_t bflags;
+  if (u.x < dw) {
+    u.x = u.x / dw;
+    const f3 wi = cosineSampleHemisphere(u);
+    bpdf = cosineHemispherePdf(wi.z);
+    bd = toWorld(X, Y, N, wi);
+    bflags = EDiffuseReflection;
+  } else {
+    u.x = (u.x - dw) / sw;
+    const float cosTheta = mpow(u.x, 1.0f / (n + 1.0f));
+    const float phi = TWO_PI * u.y;
+    const float sinTheta = sqrtf(gmax(0.0f, 1.0f - cosTheta * cosTheta));
+    const f3 wh = f3{sinTheta * msin(phi), sinTheta * mcos(phi), cosTheta};
+    const f3 H = toWorld(X, Y, N, wh);
+    bd = reflect(-V, H);
+    bpdf = phongLobePdf(bd, V, N, n);
+    bflags = EGlossyReflection;
+  }
+  const f3 weight = phongEval(bd, V, N, kd, ks, n);
+  if (bpdf <= 0.0f || length(weight) == 0.0f) {
+    io.stop = true;
+    return;
+  }
+  io.bflags = bflags;
+  io.bpdf = bpdf;
+  io.nro = offsetPositionAlongNormal(st.pos, st.ffN);
+  io.nrd = bd;
+  io.thp = io.thp * (weight / bpdf);
+}
+
 // brdf_conductor.rchit:65-80,141-163: the direction sample ignores its two
 // random numbers but draws them
 __device__ __forceinline__ void sampleConductor(PathIO& io, const HitSt& st, const MatDev& m) {
@@ -576,15 +647,7 @@ __global__ void __launch_bounds__(256) k_classify(KParams P) {
       if (inst != 0xffffffffu) {
         const InstDev& in = S.inst[inst];
         if (__ldg(&in.lightId) < 0) {
-          const uint32_t type = __ldg(&in.matType);
-          cls = type == ASUNA_MAT_ROUGH_PLASTIC ? kClsRoughPlastic
-                : type == ASUNA_MAT_DIELECTRIC  ? kClsDielectric
-                : type == ASUNA_MAT_PLASTIC     ? kClsPlastic
-                : type == ASUNA_MAT_MIRROR      ? kClsMirror
-                : type == ASUNA_MAT_CONDUCTOR   ? kClsConductor
-                : type == ASUNA_MAT_ROUGH_CONDUCTOR ? kClsRoughConductor
-                : type == ASUNA_MAT_EMISSIVE    ? kClsTerminal
-                                                : kClsLambertian;
+          cls = shadeClassOf(__ldg(&in.matType));
         }
       }
     }
@@ -673,8 +736,10 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
           }
         } else {
           const MatDev m = S.mats[in.matId];
-          if (CLS == kClsLambertian && depth == 1u && frame == 0u && sh.state.n_multi_channel > 0u) {
-            // brdf_lambertian.rchit:93-108
+          if ((CLS == kClsLambertian || CLS == kClsPhong) && depth == 1u && frame == 0u &&
+              sh.state.n_multi_channel > 0u) {
+            // brdf_lambertian.rchit:93-108; brdf_phong.rchit:135-150 writes
+            // the face-forward normal and its specular reflectance
             const asuna_rt_state& ps = sh.state;
             float4* ch = sh.filmCh;
             const size_t npx = size_t(sh.width) * sh.height;
@@ -682,8 +747,8 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
               if (slot >= 0 && slot < ASUNA_MAX_CHANNELS) ch[size_t(slot) * npx + pix] = make_float4(v.x, v.y, v.z, 1.0f);
             };
             put(ps.diffuse_out_channel, ld3(m.a));
-            put(ps.normal_out_channel, st.N);
-            put(ps.specular_out_channel, splat(0.0f));
+            put(ps.normal_out_channel, CLS == kClsPhong ? st.ffN : st.N);
+            put(ps.specular_out_channel, CLS == kClsPhong ? ld3(m.c) : splat(0.0f));
             put(ps.tangent_out_channel, st.X);
             put(ps.roughness_out_channel, f3{1.0f, 1.0f, 0.0f});
             put(ps.position_out_channel, st.pos);
@@ -700,6 +765,7 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
                                       : CLS == kClsMirror     ? ASUNA_MAT_MIRROR
                                       : CLS == kClsConductor  ? ASUNA_MAT_CONDUCTOR
                                       : CLS == kClsRoughConductor ? ASUNA_MAT_ROUGH_CONDUCTOR
+                                      : CLS == kClsPhong      ? ASUNA_MAT_PHONG
                                                               : ASUNA_MAT_LAMBERTIAN;
             nextEvent(S, sh, io, st, m, type, rd);
             if (CLS == kClsRoughPlastic)
@@ -714,6 +780,8 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
               sampleConductor(io, st, m);
             else if (CLS == kClsRoughConductor)
               sampleRoughConductor(io, st, m);
+            else if (CLS == kClsPhong)
+              samplePhong(io, st, m);
             else
               sampleLambertian(io, st, ld3(m.a));
           }
@@ -816,19 +884,22 @@ __global__ void __launch_bounds__(256) k_records(KParams P, asuna_path_record* o
 
 // ---------------------------------------------------------------------------
 void launchRaygen(const KParams& P, int grid, cudaStream_t s) { k_raygen<<<grid, 256, 0, s>>>(P); }
-// classify, then one kernel per shading class (each a persistent grid over
-// its own list)
+// classify, then one kernel per shading class the scene's materials can
+// reach (each a persistent grid over its own list)
 void launchShade(const KParams& P, int grid, cudaStream_t s) {
   k_classify<<<grid, 256, 0, s>>>(P);
-  k_shadeClass<kClsTerminal><<<grid, 256, 0, s>>>(P);
-  k_shadeClass<kClsLambertian><<<grid, 256, 0, s>>>(P);
-  k_shadeClass<kClsRoughPlastic><<<grid, 256, 0, s>>>(P);
-  k_shadeClass<kClsDielectric><<<grid, 256, 0, s>>>(P);
-  k_shadeClass<kClsPlastic><<<grid, 256, 0, s>>>(P);
-  k_shadeClass<kClsMirror><<<grid, 256, 0, s>>>(P);
-  k_shadeClass<kClsConductor><<<grid, 256, 0, s>>>(P);
-  k_shadeClass<kClsRoughConductor><<<grid, 256, 0, s>>>(P);
+  const uint32_t m = P.S.classMask | (1u << kClsTerminal);
+  if (m & (1u << kClsTerminal)) k_shadeClass<kClsTerminal><<<grid, 256, 0, s>>>(P);
+  if (m & (1u << kClsLambertian)) k_shadeClass<kClsLambertian><<<grid, 256, 0, s>>>(P);
+  if (m & (1u << kClsRoughPlastic)) k_shadeClass<kClsRoughPlastic><<<grid, 256, 0, s>>>(P);
+  if (m & (1u << kClsDielectric)) k_shadeClass<kClsDielectric><<<grid, 256, 0, s>>>(P);
+  if (m & (1u << kClsPlastic)) k_shadeClass<kClsPlastic><<<grid, 256, 0, s>>>(P);
+  if (m & (1u << kClsMirror)) k_shadeClass<kClsMirror><<<grid, 256, 0, s>>>(P);
+  if (m & (1u << kClsConductor)) k_shadeClass<kClsConductor><<<grid, 256, 0, s>>>(P);
+  if (m & (1u << kClsRoughConductor)) k_shadeClass<kClsRoughConductor><<<grid, 256, 0, s>>>(P);
+  if (m & (1u << kClsPhong)) k_shadeClass<kClsPhong><<<grid, 256, 0, s>>>(P);
 }
+int shadeLaunches(uint32_t classMask) { return 1 + __builtin_popcount(classMask | (1u << kClsTerminal)); }
 int shadeBlocksPerSm() {
   int n = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shadeClass<kClsRoughPlastic>, 256, 0);

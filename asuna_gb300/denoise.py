@@ -65,7 +65,7 @@ def ctx_stream(ctx):
 
 class Denoiser:
     def __init__(self, ctx, channels=DEFAULT_CHANNELS, seed=0, max_pixels=1 << 20, training=False,
-                 tensor_memory=False):
+                 tensor_memory=True):
         self.ctx = ctx
         self.channels = tuple(int(c) for c in channels)
         o = A.DenoiserOpts()

@@ -142,6 +142,17 @@ class SceneBuilder:
             m.aniso_alpha = (C.c_float * 2)(*alpha)
         return self._add_material(name, m)
 
+    def add_phong(self, name, diffuse, specular, shininess):
+        """brdf_phong (src/loader/material.cpp:391-405): a Lambertian lobe and a
+        normalised Phong lobe (reflectance `specular`, exponent `shininess`),
+        mixed by the luminances of the two reflectances."""
+        m = default_material()
+        m.type = A.MAT_PHONG
+        m.diffuse = A.f3(*diffuse)
+        m.rho_spec = A.f3(*specular)
+        m.specular = float(shininess)
+        return self._add_material(name, m)
+
     def add_dielectric(self, name, ior=1.5):
         m = default_material()
         m.type = A.MAT_DIELECTRIC

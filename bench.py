@@ -216,7 +216,7 @@ def run(args):
         torch_dist.barrier()
     ctx.sync()
     tot = {k: 0.0 for k in ("extend_rays", "shadow_rays", "paths", "ms_total", "ms_extend", "ms_connect",
-                            "ms_shade", "extend_launches", "connect_launches")}
+                            "ms_shade", "extend_launches", "connect_launches", "kernel_launches")}
     with ClockSampler(local) as clk:
         for i in range(args.steps):
             st = step(1 + args.warmup + i)
@@ -265,10 +265,9 @@ def run(args):
         with open(tpath) as f:
             tj = json.load(f)
         traffic = tj.get("dram_bytes_per_ray", 0) * tot["extend_rays"] / max(tot["extend_launches"], 1)
-    # per wavefront: raygen + accumulate; per depth: extend, classify, four
-    # shading-class kernels, connect (one wavefront per step: the path budget
-    # holds frames_per_step frames)
-    launches = int(tot["extend_launches"] * 6 + tot["connect_launches"] + 2 * args.steps)
+    # counted by the engine: per wavefront raygen + accumulate; per depth
+    # extend, classify, one kernel per shading class the scene uses, connect
+    launches = int(tot["kernel_launches"])
     line = {
         "metric": METRIC, "value": rays / (ms * 1e-3) / 1e6, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -543,7 +542,7 @@ def run_batch(args):
 
 C_SHOT_BYTES = 340  # sizeof(asuna_shot): the only host->device input of a step
 NODE_BYTES = 64  # one binary BVH node
-BYTES_PER_PATH = 228  # wavefront state per path slot (asuna_gb300/csrc/engine.cu)
+BYTES_PER_PATH = 232  # wavefront state per path slot (asuna_gb300/csrc/engine.cu)
 
 
 def main():

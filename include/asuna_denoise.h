@@ -45,7 +45,8 @@ typedef struct asuna_denoiser_opts {
   uint64_t seed;                                 /* He-normal initialisation */
   uint64_t max_pixels;                           /* n*h*w of the largest call (padded) */
   uint32_t training;                             /* 1: allocate gradient and Adam state */
-  uint32_t tensor_memory;                        /* 1: convolutions on tcgen05 (TMEM accumulators, TMA) */
+  uint32_t tensor_memory;                        /* 1: forward and input-gradient convolutions on tcgen05
+                                                    (TMEM accumulators, TMA; the faster path); 0: mma.sync */
 } asuna_denoiser_opts;
 
 typedef struct asuna_denoiser asuna_denoiser;
@@ -105,8 +106,10 @@ int asuna_nn_copy_channels(void* stream, const void* src, int csrc, int soff, vo
 int asuna_nn_relu_mask(void* stream, void* grad, const void* y, uint64_t count);
 /* The same convolution on the fifth-generation tensor cores: tcgen05.mma
  * with the accumulator in tensor memory, TMA-staged operands, weights in
- * the layout asuna_nn_weights_tc makes ([cin/16][9][2][cout][8]);
- * cin % 16 == 0, cout % 16 == 0, cout <= 256, 16-byte aligned operands.
+ * the layout asuna_nn_weights_tc makes ([cout/nt][cin/16][9][2][nt][8],
+ * nt = the output channels one CTA computes: the widest multiple of 16
+ * dividing cout whose weight stages fit shared memory, e.g. 224 -> 112);
+ * cin % 16 == 0, cout % 16 == 0, 16-byte aligned operands.
  * A CTA whose bounded waits expire writes nothing and sets the flag that
  * asuna_nn_tc_status reports (and clears). */
 int asuna_nn_weights_tc(void* stream, const void* w, void* wtc, int cout, int cin);

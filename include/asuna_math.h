@@ -15,8 +15,13 @@
  *         Cephes library's atanf (S. L. Moshier, "Methods and Programs for
  *         Mathematical Functions", 1989), with IEEE quadrant handling.
  *   acos  acos(x) = atan2(sqrt((1 - x)(1 + x)), x).
- * Errors: sin, cos, exp within 1 ulp; atan2, acos within 3 ulp over the
- * ranges the path tracer uses (tested against double-precision results).
+ *   log2  x = m 2^e with m in [sqrt(1/2), sqrt(2)); ln m = 2 atanh(s),
+ *         s = (m - 1) / (m + 1), odd series to s^9; times log2(e).
+ *   exp2  t = n + r, |r| <= 1/2: the exp polynomial at r ln 2, times 2^n.
+ *   pow   exp2(y log2 x) (x > 0; GLSL leaves x < 0 undefined: NaN here).
+ * Errors: sin, cos, exp within 1 ulp; atan2, acos, log2 within 3 ulp; exp2
+ * within 2 ulp; pow within 2 ulp plus |y log2 x| ulp of the exponent,
+ * over the ranges the path tracer uses (tested against double precision).
  */
 #ifndef ASUNA_MATH_H
 #define ASUNA_MATH_H
@@ -170,6 +175,58 @@ ASUNA_MATH_FN float atan2f_(float y, float x) {
 ASUNA_MATH_FN float acosf_(float x) {
   if (fl_isnan(x) || x > 1.0f || x < -1.0f) return bits_to_float(0x7fc00000u);
   return atan2f_(fl_sqrt((1.0f - x) * (1.0f + x)), x);
+}
+
+ASUNA_MATH_FN float log2f_(float x) {
+  if (fl_isnan(x) || x < 0.0f) return bits_to_float(0x7fc00000u);
+  if (x == 0.0f) return bits_to_float(0xff800000u);
+  if (x == bits_to_float(0x7f800000u)) return x;
+  int e = 0;
+  uint32_t b = float_to_bits(x);
+  if ((b >> 23) == 0) {  // subnormal: scale by 2^23 first
+    b = float_to_bits(x * 8388608.0f);
+    e = -23;
+  }
+  e += int(b >> 23) - 127;
+  float m = bits_to_float((b & 0x007fffffu) | 0x3f800000u);  // [1, 2)
+  if (m > 1.41421356f) {
+    m = m * 0.5f;
+    e += 1;
+  }
+  const float s = (m - 1.0f) / (m + 1.0f);
+  const float s2 = s * s;
+  float p = 1.0f / 9.0f;
+  p = p * s2 + 1.0f / 7.0f;
+  p = p * s2 + 1.0f / 5.0f;
+  p = p * s2 + 1.0f / 3.0f;
+  p = p * s2 + 1.0f;
+  const float ln = 2.0f * s * p;
+  return float(e) + ln * 0x1.715476p+0f;
+}
+
+ASUNA_MATH_FN float exp2f_(float t) {
+  if (fl_isnan(t)) return t;
+  if (t >= 128.0f) return bits_to_float(0x7f800000u);
+  if (t < -150.0f) return 0.0f;
+  const float n = fl_floor(t + 0.5f);
+  const float r = (t - n) * 0x1.62e430p-1f;  // (t - n) is exact; times ln 2
+  float p = 1.0f / 5040.0f;
+  p = p * r + 1.0f / 720.0f;
+  p = p * r + 1.0f / 120.0f;
+  p = p * r + 1.0f / 24.0f;
+  p = p * r + 1.0f / 6.0f;
+  p = p * r + 0.5f;
+  p = p * r + 1.0f;
+  p = p * r + 1.0f;
+  return p * pow2i((int)n);
+}
+
+ASUNA_MATH_FN float powf_(float x, float y) {
+  if (fl_isnan(x) || fl_isnan(y)) return bits_to_float(0x7fc00000u);
+  if (y == 0.0f) return 1.0f;
+  if (x == 0.0f) return y > 0.0f ? 0.0f : bits_to_float(0x7f800000u);
+  if (x < 0.0f) return bits_to_float(0x7fc00000u);
+  return exp2f_(y * log2f_(x));
 }
 
 }  // namespace asuna_math

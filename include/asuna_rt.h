@@ -80,7 +80,7 @@ enum {
   ASUNA_MAT_MIRROR = 8, /* (*) brdf_mirror        */
   ASUNA_MAT_DISNEY = 9,
   ASUNA_MAT_DIELECTRIC = 10, /* (*) bsdf_dielectric    */
-  ASUNA_MAT_PHONG = 11,
+  ASUNA_MAT_PHONG = 11, /* (*) brdf_phong         */
   ASUNA_MAT_NUM = 12
 };
 
@@ -279,6 +279,7 @@ typedef struct asuna_render_stats {
   double ms_shade;         /* device time of shading kernels                */
   uint64_t extend_launches;
   uint64_t connect_launches;
+  uint64_t kernel_launches; /* every kernel the call launched (all waves)   */
 } asuna_render_stats;
 
 typedef struct asuna_scene_stats {
@@ -370,7 +371,7 @@ int asuna_scene_trace(asuna_ctx* ctx, const asuna_scene* scene, const float* ray
  * the allocator): renders shot->frames frames of one shot into `film` like
  * asuna_render, on `stream` (a cudaStream_t; NULL = default stream), with
  * all scratch in one fixed device array compiled into the library.  The
- * array holds ASUNA_NOALLOC_MAX_PATHS path slots (about 57 MiB, kept by
+ * array holds ASUNA_NOALLOC_MAX_PATHS path slots (about 58 MiB, kept by
  * every GPU that loads the library until exit); a frame with more pixels is
  * rejected with ASUNA_ERR_INVALID.  The array's address is set up on a
  * device by the first call there: make that call before any stream capture.

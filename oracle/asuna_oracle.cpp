@@ -43,6 +43,8 @@ inline double msin(double x) { return std::sin(x); }
 inline double mcos(double x) { return std::cos(x); }
 inline double macos(double x) { return std::acos(x); }
 inline double matan2(double y, double x) { return std::atan2(y, x); }
+inline float mpow(float x, float y) { return asuna_math::powf_(x, y); }
+inline double mpow(double x, double y) { return std::pow(x, y); }
 inline double mexp(double x) { return std::exp(x); }
 
 template <class R> inline V3<R> mk(R a, R b, R c) { return V3<R>{a, b, c}; }
@@ -1268,6 +1270,98 @@ template <class R> void shadeMirror(const Scene& s, const asuna_shot& sh, PathSt
   p.throughput = p.throughput * (weight / bpdf);
 }
 
+// brdf_phong.rchit:12-30 (flag is EArea at every call site)
+template <class R> V3<R> phEval(V3<R> L, V3<R> V, V3<R> N, V3<R> kd, V3<R> ks, R n, uint32_t flags) {
+  V3<R> weight = splat(R(0));
+  if ((flags & EArea) == 0) return weight;
+  R NdotL = dot(N, L), NdotV = dot(N, V);
+  if (NdotL < R(0) || NdotV < R(0)) return weight;
+  V3<R> H = normalize(L + V);
+  V3<R> diffuseLobe = kd * K<R>::INV_PI;
+  V3<R> specularLobe = ks * mpow(gmax(dot(H, N), R(0)), n) * (n + R(2)) * K<R>::INV_2PI;
+  R db = luminance(kd), sb = luminance(ks);
+  R dw = db / (db + sb), sw = R(1) - dw;
+  return (dw * diffuseLobe + sw * specularLobe) * NdotL;
+}
+// 32-37
+template <class R> R phLobePdf(V3<R> L, V3<R> V, V3<R> N, R n) {
+  V3<R> H = normalize(L + V);
+  R NdotH = gmax(dot(H, N), R(0)), VdotH = gmax(dot(H, V), R(0));
+  return (n + R(1)) * K<R>::INV_2PI * mpow(NdotH, n) * R(0.25) / (VdotH + K<R>::EPS);
+}
+// 39-52
+template <class R> R phPdf(V3<R> L, V3<R> V, V3<R> N, V3<R> kd, V3<R> ks, R n, uint32_t flags) {
+  if ((flags & EArea) == 0) return R(0);
+  R db = luminance(kd), sb = luminance(ks);
+  R dw = db / (db + sb), sw = R(1) - dw;
+  return dw * cosineHemispherePdf(dot(N, L)) + sw * phLobePdf(L, V, N, n);
+}
+
+// brdf_phong.rchit:112-194 (main) with sampleBsdf 54-84; AOVs at depth 1
+// (135-150) carry the shading-side normal and the specular reflectance.
+template <class R> void shadePhong(const Scene& s, const asuna_shot& sh, PathState<R>& p, HitState<R>& st) {
+  const asuna_rt_state& ps = sh.state;
+  V3<R> kd = L3<R>(st.mat.diffuse), ks = L3<R>(st.mat.rho_spec);
+  R n = R(st.mat.specular);
+  if (p.depth == 1) {
+    if (ps.diffuse_out_channel >= 0) p.ch[ps.diffuse_out_channel] = kd;
+    if (ps.normal_out_channel >= 0) p.ch[ps.normal_out_channel] = st.ffN;
+    if (ps.specular_out_channel >= 0) p.ch[ps.specular_out_channel] = ks;
+    if (ps.tangent_out_channel >= 0) p.ch[ps.tangent_out_channel] = st.X;
+    if (ps.roughness_out_channel >= 0) p.ch[ps.roughness_out_channel] = V3<R>{R(1), R(1), R(0)};
+    if (ps.position_out_channel >= 0) p.ch[ps.position_out_channel] = st.pos;
+    if (ps.uv_out_channel >= 0) p.ch[ps.uv_out_channel] = V3<R>{st.uv.x, st.uv.y, R(1)};
+  }
+  {
+    bool visible;
+    LRec<R> lRec;
+    V3<R> Ld = splat(R(0));
+    V3<R> rad = sampleLights<R>(s, sh, p, st.pos, st.ffN, visible, lRec);
+    if (visible) {
+      V3<R> w = phEval<R>(lRec.d, st.V, st.ffN, kd, ks, n, EArea);
+      R bpdf = phPdf<R>(lRec.d, st.V, st.ffN, kd, ks, n, lRec.flags);
+      R mis = powerHeuristic(lRec.pdf, bpdf);
+      Ld = Ld + mis * w * rad * p.throughput / (lRec.pdf + K<R>::EPS);
+    }
+    p.drad = Ld;
+    p.dskip = !visible;
+  }
+  V2<R> u = rnd2<R>(p.seed);
+  V3<R> V = st.V, N = st.ffN, X = st.X, Y = st.Y;
+  R db = luminance(kd), sb = luminance(ks);
+  R dw = db / (db + sb), sw = R(1) - dw;
+  V3<R> bd;
+  R bpdf;
+  uint32_t bflags;
+  if (u.x < dw) {
+    u.x = u.x / dw;
+    V3<R> wi = cosineSampleHemisphere(u);
+    bpdf = cosineHemispherePdf(wi.z);
+    bd = toWorld(X, Y, N, wi);
+    bflags = EDiffuseReflection;
+  } else {
+    u.x = (u.x - dw) / sw;
+    R cosTheta = mpow(u.x, R(1) / (n + R(1)));
+    R phi = K<R>::TWO_PI * u.y;
+    R sinTheta = std::sqrt(gmax(R(0), R(1) - cosTheta * cosTheta));
+    V3<R> wh{sinTheta * msin(phi), sinTheta * mcos(phi), cosTheta};
+    V3<R> H = toWorld(X, Y, N, wh);
+    bd = reflect(-V, H);
+    bpdf = phLobePdf(bd, V, N, n);
+    bflags = EGlossyReflection;
+  }
+  V3<R> weight = phEval<R>(bd, V, N, kd, ks, n, EArea);
+  if (bpdf <= R(0) || length(weight) == R(0)) {
+    p.stop = true;
+    return;
+  }
+  p.bflags = bflags;
+  p.bpdf = bpdf;
+  p.ro = offsetPositionAlongNormal(st.pos, st.ffN);
+  p.rd = bd;
+  p.throughput = p.throughput * (weight / bpdf);
+}
+
 // brdf_conductor.rchit:14-36 (P. Shirley's conductor Fresnel)
 template <class R> R conductorReflectance(R eta, R k, R cosThetaI) {
   R cosThetaISq = cosThetaI * cosThetaI;
@@ -1494,6 +1588,8 @@ void tracePath(const Scene& s, const asuna_shot& sh, uint32_t x, uint32_t y, uin
           shadeConductor<R>(s, sh, p, hs);
         else if (type == ASUNA_MAT_ROUGH_CONDUCTOR)
           shadeRoughConductor<R>(s, sh, p, hs);
+        else if (type == ASUNA_MAT_PHONG)
+          shadePhong<R>(s, sh, p, hs);
         else
           shadeLambertian<R>(s, sh, p, hs);
         p.sig = sigMix(p.sig, p.stop ? 0xfffu : p.bflags);
@@ -1628,6 +1724,9 @@ float oracle_math(int which, float x, float y) {
     case 1: return mcos(x);
     case 2: return mexp(x);
     case 3: return macos(x);
+    case 5: return asuna_math::log2f_(x);
+    case 6: return asuna_math::exp2f_(x);
+    case 7: return asuna_math::powf_(x, y);
     default: return matan2(x, y);
   }
 }

@@ -49,6 +49,7 @@ SHADERS = {
     "bxdf/raytrace.brdf_mirror.rchit": "stage_mirror",
     "bxdf/raytrace.brdf_conductor.rchit": "stage_conductor",
     "bxdf/raytrace.brdf_rough_conductor.rchit": "stage_rough_conductor",
+    "bxdf/raytrace.brdf_phong.rchit": "stage_phong",
 }
 
 FLOAT_LIT = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")

@@ -162,6 +162,7 @@ inline float sin(float x) { return asuna_math::sinf_(x); }
 inline float cos(float x) { return asuna_math::cosf_(x); }
 inline float acos(float x) { return asuna_math::acosf_(x); }
 inline float atan(float y, float x) { return asuna_math::atan2f_(y, x); }
+inline float pow(float x, float y) { return asuna_math::powf_(x, y); }
 inline float sign(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
 inline bool isnan(float x) { return std::isnan(x); }
 inline bool isinf(float x) { return std::isinf(x); }

@@ -94,6 +94,7 @@ static thread_local RayPayload payload;
 #include "raytrace.brdf_mirror.rchit.h"
 #include "raytrace.brdf_conductor.rchit.h"
 #include "raytrace.brdf_rough_conductor.rchit.h"
+#include "raytrace.brdf_phong.rchit.h"
 }  // namespace glslx
 
 namespace {
@@ -175,6 +176,9 @@ void traceRayEXT(accelerationStructureEXT, uint, uint, uint, uint, uint, vec3 or
       break;
     case MaterialTypeBrdfRoughConductor:
       stage_rough_conductor::main();
+      break;
+    case MaterialTypeBrdfPhong:
+      stage_phong::main();
       break;
     default:
       stage_lambertian::main();

@@ -89,11 +89,13 @@ def test_conv3x3_input_gradient_with_mask(lib):
 
 
 @pytest.mark.parametrize("shape", [(1, 16, 8, 16, 16), (2, 20, 24, 32, 48), (1, 33, 70, 224, 96),
-                                   (1, 40, 37, 48, 128), (3, 9, 13, 16, 32), (1, 24, 16, 96, 64)])
+                                   (1, 40, 37, 48, 128), (3, 9, 13, 16, 32), (1, 24, 16, 96, 64),
+                                   (1, 20, 30, 32, 224), (2, 12, 20, 16, 256), (1, 17, 19, 48, 192)])
 def test_conv3x3_tcgen05(lib, shape):
     """The tcgen05 / TMEM / TMA convolution against the float64 reference:
     edge tiles (sizes not multiples of 16 x 8), batches, 16..224 input and
-    16..128 output channels; bias, ReLU, mask and fp32 / bf16 outputs."""
+    16..256 output channels (192, 224 and 256 split over two CTAs per tile);
+    bias, ReLU, mask and fp32 / bf16 outputs."""
     n, h, w, cin, cout = shape
     rng = np.random.default_rng(cin * 7 + cout)
     x = U.round_bf16(rng.normal(size=(n, h, w, cin)))

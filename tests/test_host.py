@@ -364,9 +364,10 @@ def test_hdr_envmap_reader(tmp_path):
 
 
 def test_json_material_plugins_match_builder():
-    """brdf_plastic, brdf_mirror, brdf_conductor and brdf_rough_conductor
-    parse into the same device structs as the builder (src/loader/material.cpp:
-    197-210, 233-243, 306-347); an unknown metal is a parse error."""
+    """brdf_plastic, brdf_mirror, brdf_conductor, brdf_rough_conductor and
+    brdf_phong parse into the same device structs as the builder
+    (src/loader/material.cpp:197-210, 233-243, 306-347, 391-405); an unknown
+    metal is a parse error."""
     base = {"state": {}, "camera": {"type": "perspective", "film": {"resolution": [8, 8]}}, "meshes": [],
             "instances": []}
     mats = [{"type": "brdf_plastic", "name": "p", "diffuse_reflectance": [0.7, 0.65, 0.1], "ior": 1.6},
@@ -374,7 +375,9 @@ def test_json_material_plugins_match_builder():
             {"type": "brdf_conductor", "name": "au", "material": "Au"},
             {"type": "brdf_rough_conductor", "name": "al", "material": "Al", "diffuse_reflectance": [0.9, 0.9, 0.9],
              "alpha": [0.15, 0.3]},
-            {"type": "brdf_conductor", "name": "cu"}]
+            {"type": "brdf_conductor", "name": "cu"},
+            {"type": "brdf_phong", "name": "ph", "diffuse_reflectance": [0.3, 0.5, 0.2],
+             "specular_reflectance": [0.5, 0.5, 0.45], "shininess": 40}]
     js = ag.JsonScene(text=json.dumps({**base, "materials": mats}), base_dir=".")
     d = js.desc().desc
     b = ag.SceneBuilder()
@@ -383,12 +386,15 @@ def test_json_material_plugins_match_builder():
     b.add_conductor("au", "Au")
     b.add_conductor("al", "Al", (0.9, 0.9, 0.9), alpha=(0.15, 0.3))
     b.add_conductor("cu")
+    b.add_phong("ph", (0.3, 0.5, 0.2), (0.5, 0.5, 0.45), 40.0)
     assert d.num_materials == len(b.materials)
     for k in range(1, d.num_materials):
         assert bytes(d.materials[k]) == bytes(b.materials[k]), k
     assert d.materials[1].type == A.MAT_PLASTIC and d.materials[1].radiance[0] == pytest.approx(
         float(_np_fdr(1.6, 1000)), abs=0)
     assert d.materials[3].type == A.MAT_CONDUCTOR and d.materials[4].type == A.MAT_ROUGH_CONDUCTOR
+    assert d.materials[6].type == A.MAT_PHONG and d.materials[6].specular == 40.0
+    assert list(d.materials[6].rho_spec) == pytest.approx([0.5, 0.5, 0.45])
     # gold: eta (0.1431, 0.3750, 1.4425), k (3.9832, 2.3857, 1.6032)
     assert np.allclose(list(d.materials[3].radiance), [0.1431189557, 0.3749570432, 1.4424785571])
     assert np.allclose(list(d.materials[3].radiance_factor), [3.9831604247, 2.3857207478, 1.6032152899])

@@ -74,15 +74,24 @@ def test_oracle_double_precision_close_to_float():
 
 
 @pytest.mark.parametrize("which,fn,lo,hi,ulps", [(0, np.sin, -7, 7, 1), (1, np.cos, -7, 7, 1), (2, np.exp, -20, 1, 1),
-                                                 (3, np.arccos, -1, 1, 3), (4, None, -3, 3, 3)])
+                                                 (3, np.arccos, -1, 1, 3), (4, None, -3, 3, 3),
+                                                 (5, np.log2, 1e-6, 40, 3), (6, np.exp2, -30, 30, 2),
+                                                 (7, "pow", 0.0, 1.0, 80)])
 def test_shared_math_accuracy(which, fn, lo, hi, ulps):
     """include/asuna_math.h (used by the CUDA kernels and the oracle) against
-    double precision, in ulps of the float result."""
+    double precision, in ulps of the float result (pow: bases in (0, 1],
+    exponents 1..40)."""
     L = oracle_py.port()
     rng = np.random.default_rng(which)
     x = rng.uniform(lo, hi, 20000).astype(np.float32)
     y = rng.uniform(-3, 3, 20000).astype(np.float32)
+    if fn == "pow":
+        x = np.maximum(x, np.float32(0.3))
+        y = rng.uniform(1, 40, 20000).astype(np.float32)
     got = np.array([L.oracle_math(which, float(a), float(b)) for a, b in zip(x, y)], np.float32)
-    ref = np.arctan2(x.astype(np.float64), y.astype(np.float64)) if fn is None else fn(x.astype(np.float64))
+    if fn == "pow":
+        ref = np.power(x.astype(np.float64), y.astype(np.float64))
+    else:
+        ref = np.arctan2(x.astype(np.float64), y.astype(np.float64)) if fn is None else fn(x.astype(np.float64))
     d = np.abs(got.view(np.int32).astype(np.int64) - ref.astype(np.float32).view(np.int32).astype(np.int64))
     assert d.max() <= ulps
