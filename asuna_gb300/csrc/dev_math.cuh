@@ -60,6 +60,7 @@ __device__ __forceinline__ float msin(float x) { return asuna_math::sinf_(x); }
 __device__ __forceinline__ float mcos(float x) { return asuna_math::cosf_(x); }
 __device__ __forceinline__ float macos(float x) { return asuna_math::acosf_(x); }
 __device__ __forceinline__ float mpow(float x, float y) { return asuna_math::powf_(x, y); }
+__device__ __forceinline__ float mlog(float x) { return asuna_math::logf_(x); }
 __device__ __forceinline__ float matan2(float y, float x) { return asuna_math::atan2f_(y, x); }
 __device__ __forceinline__ float mexp(float x) { return asuna_math::expf_(x); }
 

@@ -145,8 +145,11 @@ enum ShadeClass {
   kClsConductor = 6,
   kClsRoughConductor = 7,
   kClsPhong = 8,
-  kNumShadeClasses = 9
+  kClsPbr = 9,  // brdf_pbr_metalness_roughness
+  kClsDisney = 10,
+  kNumShadeClasses = 11
 };
+static_assert(kCntCls0 + kNumShadeClasses <= kCntNum32, "class counters exceed the counter page's slots");
 // The class that shades a hit on a surface of material `type` (not a light).
 #if defined(__CUDACC__)
 __host__ __device__
@@ -160,6 +163,8 @@ inline int shadeClassOf(uint32_t type) {
     case ASUNA_MAT_CONDUCTOR: return kClsConductor;
     case ASUNA_MAT_ROUGH_CONDUCTOR: return kClsRoughConductor;
     case ASUNA_MAT_PHONG: return kClsPhong;
+    case ASUNA_MAT_PBR_METALNESS_ROUGHNESS: return kClsPbr;
+    case ASUNA_MAT_DISNEY: return kClsDisney;
     case ASUNA_MAT_EMISSIVE: return kClsTerminal;
     default: return kClsLambertian;
   }

@@ -412,11 +412,21 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
     // emissive materials carry their radiance where the others carry the albedo
     const float* rgb = m.type == ASUNA_MAT_EMISSIVE ? m.radiance : m.diffuse;
     mats[i].a = make_float4(rgb[0], rgb[1], rgb[2], tb);
-    mats[i].b = make_float4(m.aniso_alpha[0], m.aniso_alpha[1], m.ior, m.radiance[0]);
-    // Phong: specular reflectance and exponent (rhoSpec, specular); others: radiance
+    // Disney: (anisotropic, opacity, ior, -); others: (alpha x, alpha y, ior, fdrInt)
+    mats[i].b = m.type == ASUNA_MAT_DISNEY ? make_float4(m.anisotropic, m.rho_spec[0], m.ior, 0.0f)
+                                           : make_float4(m.aniso_alpha[0], m.aniso_alpha[1], m.ior, m.radiance[0]);
+    // Phong: specular reflectance and exponent (rhoSpec, specular); PBR:
+    // roughness, metalness, opacity (specular); Disney: metalness, roughness,
+    // subsurface, specular tint; others: radiance
     mats[i].c = m.type == ASUNA_MAT_PHONG ? make_float4(m.rho_spec[0], m.rho_spec[1], m.rho_spec[2], m.specular)
-                                          : make_float4(m.radiance[0], m.radiance[1], m.radiance[2], 0.0f);
-    mats[i].d = make_float4(m.radiance_factor[0], m.radiance_factor[1], m.radiance_factor[2], 0.0f);
+                : m.type == ASUNA_MAT_PBR_METALNESS_ROUGHNESS
+                    ? make_float4(m.roughness, m.metalness, m.specular, 0.0f)
+                : m.type == ASUNA_MAT_DISNEY ? make_float4(m.metalness, m.roughness, m.subsurface, m.specular_tint)
+                                             : make_float4(m.radiance[0], m.radiance[1], m.radiance[2], 0.0f);
+    // Disney: sheen, sheen tint, clearcoat, clearcoat gloss; others: radiance factor
+    mats[i].d = m.type == ASUNA_MAT_DISNEY
+                    ? make_float4(m.sheen, m.sheen_tint, m.clearcoat, m.clearcoat_gloss)
+                    : make_float4(m.radiance_factor[0], m.radiance_factor[1], m.radiance_factor[2], 0.0f);
   }
   std::vector<LightDev> lights(std::max(1u, d->num_lights));
   for (uint32_t i = 0; i < d->num_lights; ++i) {

@@ -64,12 +64,22 @@ int validateSceneDesc(const asuna_scene_desc* d) {
     uint32_t t = d->materials[i].type;
     if (t != ASUNA_MAT_LAMBERTIAN && t != ASUNA_MAT_ROUGH_PLASTIC && t != ASUNA_MAT_DIELECTRIC &&
         t != ASUNA_MAT_EMISSIVE && t != ASUNA_MAT_PLASTIC && t != ASUNA_MAT_MIRROR && t != ASUNA_MAT_CONDUCTOR &&
-        t != ASUNA_MAT_ROUGH_CONDUCTOR && t != ASUNA_MAT_PHONG)
+        t != ASUNA_MAT_ROUGH_CONDUCTOR && t != ASUNA_MAT_PHONG && t != ASUNA_MAT_PBR_METALNESS_ROUGHNESS &&
+        t != ASUNA_MAT_DISNEY)
       return fail(ASUNA_ERR_UNSUPPORTED, "material %u: type %u is not implemented", i, t);
     const asuna_material& m = d->materials[i];
     if (m.diffuse_texture_id >= 0 || m.normal_texture_id >= 0 || m.roughness_texture_id >= 0 ||
-        (t == ASUNA_MAT_EMISSIVE && m.radiance_texture_id >= 0))
+        (t == ASUNA_MAT_EMISSIVE && m.radiance_texture_id >= 0) ||
+        ((t == ASUNA_MAT_PBR_METALNESS_ROUGHNESS || t == ASUNA_MAT_DISNEY) &&
+         (m.metalness_texture_id >= 0 || m.opacity_texture_id >= 0)))
       return fail(ASUNA_ERR_UNSUPPORTED, "material %u: textures are not implemented", i);
+    // brdf_pbr_metalness_roughness.rchit:152-160 and brdf_disney.rchit:409-417:
+    // an opacity above 0 (PBR: the specular field, which the JSON loader
+    // always sets to 0; Disney: rho_spec[0], JSON "opacity") lets rays pass
+    // through without counting a bounce
+    if ((t == ASUNA_MAT_PBR_METALNESS_ROUGHNESS && m.specular != 0.0f) ||
+        (t == ASUNA_MAT_DISNEY && m.rho_spec[0] != 0.0f))
+      return fail(ASUNA_ERR_UNSUPPORTED, "material %u: opacity pass-through is not implemented", i);
   }
   for (uint32_t i = 0; i < d->num_instances; ++i) {
     const asuna_instance_desc& in = d->instances[i];
@@ -1003,6 +1013,32 @@ int addMaterial(LoadCtx& L, const Json& mj) {
     if (mj.has("specular_reflectance"))
       REQUIRE(vecN(mj["specular_reflectance"], 3, m.rho_spec), "bad specular_reflectance");
     if (mj.has("shininess")) m.specular = float(mj["shininess"].num);
+  } else if (t == "brdf_pbr_metalness_roughness") {
+    // src/loader/material.cpp:116-143: opacity (specular) is always 0
+    m.type = ASUNA_MAT_PBR_METALNESS_ROUGHNESS;
+    if ((rc = tex("normal_texture", m.normal_texture_id))) return rc;
+    if (mj.has("diffuse_reflectance")) REQUIRE(vecN(mj["diffuse_reflectance"], 3, m.diffuse), "bad diffuse_reflectance");
+    if ((rc = tex("diffuse_texture", m.diffuse_texture_id))) return rc;
+    if (mj.has("metalness")) m.metalness = float(mj["metalness"].num);
+    if ((rc = tex("metalness_texture", m.metalness_texture_id))) return rc;
+    if (mj.has("roughness")) m.roughness = float(mj["roughness"].num);
+    if ((rc = tex("roughness_texture", m.roughness_texture_id))) return rc;
+    m.specular = 0.0f;
+    if ((rc = tex("opacity_texture", m.opacity_texture_id))) return rc;
+  } else if (t == "brdf_disney") {
+    // src/loader/material.cpp:359-389: opacity in rho_spec[0]; the other
+    // Disney parameters keep their defaults (0) on this path
+    m.type = ASUNA_MAT_DISNEY;
+    if ((rc = tex("normal_texture", m.normal_texture_id))) return rc;
+    if (mj.has("diffuse_reflectance")) REQUIRE(vecN(mj["diffuse_reflectance"], 3, m.diffuse), "bad diffuse_reflectance");
+    if ((rc = tex("diffuse_texture", m.diffuse_texture_id))) return rc;
+    if (mj.has("metallic")) m.metalness = float(mj["metallic"].num);
+    if ((rc = tex("metallic_texture", m.metalness_texture_id))) return rc;
+    if (mj.has("roughness")) m.roughness = float(mj["roughness"].num);
+    if ((rc = tex("roughness_texture", m.roughness_texture_id))) return rc;
+    m.rho_spec[0] = 0.0f;
+    if (mj.has("opacity")) m.rho_spec[0] = float(mj["opacity"].num);
+    if ((rc = tex("opacity_texture", m.opacity_texture_id))) return rc;
   } else if (t == "brdf_emissive") {
     // src/loader/material.cpp:145-155
     m.type = ASUNA_MAT_EMISSIVE;
@@ -1010,7 +1046,7 @@ int addMaterial(LoadCtx& L, const Json& mj) {
     if (mj.has("radiance_factor")) REQUIRE(vecN(mj["radiance_factor"], 3, m.radiance_factor), "bad radiance_factor");
     if ((rc = tex("radiance_texture", m.radiance_texture_id))) return rc;
   } else {
-    static const char* known[] = {"brdf_pbr_metalness_roughness", "brdf_kang18", "brdf_disney"};
+    static const char* known[] = {"brdf_kang18"};
     for (const char* k : known)
       if (t == k) return fail(ASUNA_ERR_UNSUPPORTED, "material type [%s] is not implemented", t.c_str());
     return fail(ASUNA_ERR_PARSE, "unrecognized material type [%s]", t.c_str());
@@ -1283,6 +1319,12 @@ const NamedIor kConductorIors[] = {
 extern "C" {
 
 int asuna_abi_version(void) { return ASUNA_ABI_VERSION; }
+
+int asuna_scene_validate(const asuna_scene_desc* desc) {
+  clearError();
+  if (!desc) return fail(ASUNA_ERR_INVALID, "null argument");
+  return validateSceneDesc(desc);
+}
 const char* asuna_last_error(void) { return gLastError.c_str(); }
 
 int asuna_camera_perspective(const float eye[3], const float lookat[3], const float up[3], float fov_deg,

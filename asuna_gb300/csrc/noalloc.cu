@@ -11,7 +11,7 @@
 // stream.
 //
 // The array holds kNoAllocMaxPaths path slots (ASUNA_NOALLOC_MAX_PATHS =
-// 262,144, 232 bytes each, about 58 MiB in all); every GPU that loads this
+// 262,144, 240 bytes each, about 60 MiB in all); every GPU that loads this
 // library keeps it until the process exits.  A frame of more pixels than
 // that is rejected with ASUNA_ERR_INVALID.
 //

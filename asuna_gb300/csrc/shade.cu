@@ -15,7 +15,9 @@
 //               brdf_rough_plastic.rchit:191-269, bsdf_dielectric.rchit:74-139,
 //               brdf_emissive.rchit:12-27, brdf_plastic.rchit:43-205,
 //               brdf_mirror.rchit:12-106, brdf_conductor.rchit:14-164,
-//               brdf_rough_conductor.rchit, brdf_phong.rchit:12-194
+//               brdf_rough_conductor.rchit, brdf_phong.rchit:12-194,
+//               brdf_pbr_metalness_roughness.rchit:12-219,
+//               brdf_disney.rchit:31-477
 //   accumulate  raytrace.projective.rgen:134-179
 //
 // Compiled with -fmad=false: the float arithmetic rounds operation by
@@ -244,6 +246,212 @@ __device__ __forceinline__ float phongLobePdf(f3 L, f3 V, f3 N, float n) {
   return (n + 1.0f) * INV_2PI * mpow(NdotH, n) * 0.25f / (VdotH + EPS);
 }
 
+// brdf_pbr_metalness_roughness.rchit:14-16, 57-86 (flags unused): GGX with
+// Schlick Fresnel (f0 = mix(F0(eta), albedo, metalness)) plus the Lambertian
+// base weighted by 1 - metalness
+__device__ __forceinline__ f3 pbrEval(f3 L, f3 V, f3 N, f3 X, f3 Y, f3 albedo, float a, float metalness, float eta) {
+  const float NdotL = dot(N, L), NdotV = dot(N, V);
+  if (NdotL <= 0.0f || NdotV <= 0.0f) return splat(0.0f);
+  const f3 H = makeNormal(L + V);
+  const float HdotN = dot(H, N), HdotX = dot(H, X), HdotY = dot(H, Y), HdotV = dot(H, V);
+  const float F0 = sqr((eta - 1.0f) / (eta + 1.0f));
+  const f3 f0 = splat(F0) * (1.0f - metalness) + albedo * metalness;
+  const f3 Fs = f0 + (splat(1.0f) - f0) * mpow(gclamp(1.0f - HdotV, 0.0f, 1.0f), 5.0f);
+  const float Ds = dAnisoGGX(HdotN, HdotX, HdotY, a, a);
+  float Gs = g1SmithAnisoGGX(NdotV, dot(V, X), dot(V, Y), a, a);
+  Gs = Gs * g1SmithAnisoGGX(NdotL, dot(L, X), dot(L, Y), a, a);
+  const f3 diffuse = albedo * (1.0f - metalness) * INV_PI;
+  const f3 specular = Fs * Ds * Gs;
+  return (diffuse + specular) * NdotL;
+}
+// 88-105: fixed 0.2 / 0.8 mixture of the cosine and GGX pdfs (EArea only)
+__device__ __forceinline__ float pbrPdf(f3 L, f3 V, f3 N, f3 X, f3 Y, float a) {
+  const float NdotL = dot(N, L), NdotV = dot(N, V);
+  if (NdotL <= 0.0f || NdotV <= 0.0f) return 0.0f;
+  const f3 H = makeNormal(L + V);
+  const f3 wh = makeNormal(toLocal(X, Y, N, H)), wo = makeNormal(toLocal(X, Y, N, V)),
+           wi = makeNormal(toLocal(X, Y, N, L));
+  return 0.2f * cosineHemispherePdf(wi.z) + (1.0f - 0.2f) * importanceAnisoGGXPdf(wh, wo, a, a);
+}
+
+// ---- brdf_disney.rchit (float restatement; expressions in source order) ----
+namespace disney {
+struct Mat {  // DisneyMaterial (31-48) without the unused fields
+  f3 baseColor;
+  float metallic, roughness, subsurface, specularTint, sheen, sheenTint, clearcoat, clearcoatRoughness, ax, ay;
+};
+__device__ __forceinline__ float mix1(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+__device__ __forceinline__ f3 mix3(f3 x, f3 y, float a) { return x * (1.0f - a) + y * a; }
+__device__ __forceinline__ float lum(f3 c) { return 0.212671f * c.x + 0.715160f * c.y + 0.072169f * c.z; }
+// 54-59
+__device__ __forceinline__ float GTR1(float NDotH, float a) {
+  if (a >= 1.0f) return INV_PI;
+  const float a2 = a * a;
+  const float t = 1.0f + (a2 - 1.0f) * NDotH * NDotH;
+  return (a2 - 1.0f) / (PI * mlog(a2) * t);
+}
+// 61-74 (r1 drives both angles; r2 unused, as written)
+__device__ __forceinline__ f3 SampleGTR1(float rgh, float r1) {
+  const float a = gmax(0.001f, rgh);
+  const float a2 = a * a;
+  const float phi = r1 * TWO_PI;
+  const float cosTheta = sqrtf((1.0f - mpow(a2, 1.0f - r1)) / (1.0f - a2));
+  const float sinTheta = gclamp(sqrtf(1.0f - (cosTheta * cosTheta)), 0.0f, 1.0f);
+  return f3{sinTheta * mcos(phi), sinTheta * msin(phi), cosTheta};
+}
+// 95-114
+__device__ __forceinline__ f3 SampleGGXVNDF(f3 V, float ax, float ay, float r1, float r2) {
+  const f3 Vh = normalize(f3{ax * V.x, ay * V.y, V.z});
+  const float lensq = Vh.x * Vh.x + Vh.y * Vh.y;
+  const f3 T1 = lensq > 0.0f ? f3{-Vh.y, Vh.x, 0.0f} * (1.0f / sqrtf(lensq)) : f3{1.0f, 0.0f, 0.0f};
+  const f3 T2 = cross(Vh, T1);
+  const float r = sqrtf(r1);
+  const float phi = 2.0f * PI * r2;
+  const float t1 = r * mcos(phi);
+  float t2 = r * msin(phi);
+  const float sv = 0.5f * (1.0f + Vh.z);
+  t2 = (1.0f - sv) * sqrtf(1.0f - t1 * t1) + sv * t2;
+  const f3 Nh = t1 * T1 + t2 * T2 + sqrtf(gmax(0.0f, 1.0f - t1 * t1 - t2 * t2)) * Vh;
+  return normalize(f3{ax * Nh.x, ay * Nh.y, gmax(0.0f, Nh.z)});
+}
+// 116-121
+__device__ __forceinline__ float GTR2Aniso(float NDotH, float HDotX, float HDotY, float ax, float ay) {
+  const float a = HDotX / ax, b = HDotY / ay;
+  const float c = a * a + b * b + NDotH * NDotH;
+  return 1.0f / (PI * ax * ay * c * c);
+}
+// 133-144
+__device__ __forceinline__ float SmithG(float NDotV, float alphaG) {
+  const float a = alphaG * alphaG, b = NDotV * NDotV;
+  return (2.0f * NDotV) / (NDotV + sqrtf(a + b - a * b));
+}
+__device__ __forceinline__ float SmithGAniso(float NDotV, float VDotX, float VDotY, float ax, float ay) {
+  const float a = VDotX * ax, b = VDotY * ay, c = NDotV;
+  return (2.0f * NDotV) / (NDotV + sqrtf(a * a + b * b + c * c));
+}
+// 146-170
+__device__ __forceinline__ float SchlickFresnel(float u) {
+  const float m = gclamp(1.0f - u, 0.0f, 1.0f);
+  const float m2 = m * m;
+  return m2 * m2 * m;
+}
+__device__ __forceinline__ float DielectricFresnel(float cosThetaI, float eta) {
+  const float sinThetaTSq = eta * eta * (1.0f - cosThetaI * cosThetaI);
+  if (sinThetaTSq > 1.0f) return 1.0f;
+  const float cosThetaT = sqrtf(gmax(1.0f - sinThetaTSq, 0.0f));
+  const float rs = (eta * cosThetaT - cosThetaI) / (eta * cosThetaT + cosThetaI);
+  const float rp = (eta * cosThetaI - cosThetaT) / (eta * cosThetaI + cosThetaT);
+  return 0.5f * (rs * rs + rp * rp);
+}
+__device__ __forceinline__ float Fresnel(float metallic, float eta, float LDotH, float VDotH) {
+  return mix1(DielectricFresnel(fabsf(VDotH), eta), SchlickFresnel(LDotH), metallic);
+}
+// 172-195
+__device__ __forceinline__ f3 EvalDiffuse(const Mat& mat, f3 Csheen, f3 V, f3 L, f3 H, float& pdf) {
+  pdf = 0.0f;
+  if (L.z <= 0.0f) return splat(0.0f);
+  const float FL = SchlickFresnel(L.z), FV = SchlickFresnel(V.z), FH = SchlickFresnel(dot(L, H));
+  const float Fd90 = 0.5f + 2.0f * dot(L, H) * dot(L, H) * mat.roughness;
+  const float Fd = mix1(1.0f, Fd90, FL) * mix1(1.0f, Fd90, FV);
+  const float Fss90 = dot(L, H) * dot(L, H) * mat.roughness;
+  const float Fss = mix1(1.0f, Fss90, FL) * mix1(1.0f, Fss90, FV);
+  const float ss = 1.25f * (Fss * (1.0f / (L.z + V.z) - 0.5f) + 0.5f);
+  const f3 Fsheen = FH * mat.sheen * Csheen;
+  pdf = L.z * INV_PI;
+  return (1.0f - mat.metallic) * (INV_PI * mix1(Fd, ss, mat.subsurface) * mat.baseColor + Fsheen);
+}
+// 197-211
+__device__ __forceinline__ f3 EvalSpecReflection(const Mat& mat, float eta, f3 specCol, f3 V, f3 L, f3 H,
+                                                 float& pdf) {
+  pdf = 0.0f;
+  if (L.z <= 0.0f) return splat(0.0f);
+  const float FM = Fresnel(mat.metallic, eta, dot(L, H), dot(V, H));
+  const f3 F = mix3(specCol, splat(1.0f), FM);
+  const float D = GTR2Aniso(H.z, H.x, H.y, mat.ax, mat.ay);
+  const float G1 = SmithGAniso(fabsf(V.z), V.x, V.y, mat.ax, mat.ay);
+  const float G2 = G1 * SmithGAniso(fabsf(L.z), L.x, L.y, mat.ax, mat.ay);
+  pdf = G1 * D / (4.0f * V.z);
+  return F * D * G2 / (4.0f * L.z * V.z);
+}
+// 213-226
+__device__ __forceinline__ f3 EvalClearcoat(const Mat& mat, f3 V, f3 L, f3 H, float& pdf) {
+  pdf = 0.0f;
+  if (L.z <= 0.0f) return splat(0.0f);
+  const float FH = DielectricFresnel(dot(V, H), 1.0f / 1.5f);
+  const float F = mix1(0.04f, 1.0f, FH);
+  const float D = GTR1(H.z, mat.clearcoatRoughness);
+  const float G = SmithG(L.z, 0.25f) * SmithG(V.z, 0.25f);
+  const float jacobian = 1.0f / (4.0f * dot(V, H));
+  pdf = D * H.z * jacobian;
+  return splat(0.25f) * mat.clearcoat * F * D * G / (4.0f * L.z * V.z);
+}
+// 228-250
+__device__ __forceinline__ void SpecColor(const Mat& mat, float eta, f3& specCol, f3& sheenCol) {
+  const float l = lum(mat.baseColor);
+  const f3 ctint = l > 0.0f ? mat.baseColor / l : splat(1.0f);
+  const float F0 = (1.0f - eta) / (1.0f + eta);
+  specCol = mix3(F0 * F0 * mix3(splat(1.0f), ctint, mat.specularTint), mat.baseColor, mat.metallic);
+  sheenCol = mix3(splat(1.0f), ctint, mat.sheenTint);
+}
+__device__ __forceinline__ void LobeProbabilities(const Mat& mat, f3 specCol, float approxFresnel, float& diffuseWt,
+                                                  float& specReflectWt, float& clearcoatWt) {
+  diffuseWt = lum(mat.baseColor) * (1.0f - mat.metallic);
+  specReflectWt = lum(mix3(specCol, splat(1.0f), approxFresnel));
+  clearcoatWt = 0.25f * mat.clearcoat * (1.0f - mat.metallic);
+  const float totalWt = diffuseWt + specReflectWt + clearcoatWt;
+  diffuseWt = diffuseWt / totalWt;
+  specReflectWt = specReflectWt / totalWt;
+  clearcoatWt = clearcoatWt / totalWt;
+}
+// 252-300 (EArea at every call site)
+__device__ __forceinline__ f3 eval(f3 L, f3 V, f3 N, f3 X, f3 Y, const Mat& mat, float eta, float& bsdfPdf) {
+  f3 weight = splat(0.0f);
+  bsdfPdf = 0.0f;
+  V = toLocal(X, Y, N, V);
+  L = toLocal(X, Y, N, L);
+  if (L.z <= 0.0f || V.z <= 0.0f) return weight;
+  f3 H = normalize(L + V);
+  if (H.z < 0.0f) H = -H;
+  f3 specCol, sheenCol;
+  SpecColor(mat, eta, specCol, sheenCol);
+  float diffuseWt, specReflectWt, clearcoatWt;
+  LobeProbabilities(mat, specCol, Fresnel(mat.metallic, eta, dot(L, H), dot(V, H)), diffuseWt, specReflectWt,
+                    clearcoatWt);
+  float pdf = 0.0f;
+  if (diffuseWt > 0.0f && L.z > 0.0f) {
+    weight = weight + EvalDiffuse(mat, sheenCol, V, L, H, pdf);
+    bsdfPdf = bsdfPdf + pdf * diffuseWt;
+  }
+  if (specReflectWt > 0.0f && L.z > 0.0f && V.z > 0.0f) {
+    weight = weight + EvalSpecReflection(mat, eta, specCol, V, L, H, pdf);
+    bsdfPdf = bsdfPdf + pdf * specReflectWt;
+  }
+  if (clearcoatWt > 0.0f && L.z > 0.0f && V.z > 0.0f) {
+    weight = weight + EvalClearcoat(mat, V, L, H, pdf);
+    bsdfPdf = bsdfPdf + pdf * clearcoatWt;
+  }
+  return weight * L.z;
+}
+// main 419-439: the material as the shader derives it
+__device__ __forceinline__ Mat fromDev(const MatDev& m) {
+  Mat d;
+  const float rough = m.c.y;
+  const float aspect = sqrtf(1.0f - m.b.x * 0.9f);
+  d.ax = gmax(0.001f, rough * rough / aspect);
+  d.ay = gmax(0.001f, rough * rough * aspect);
+  d.baseColor = ld3(m.a);
+  d.metallic = m.c.x;
+  d.roughness = gmax(rough * rough, 0.001f);
+  d.subsurface = m.c.z;
+  d.specularTint = m.c.w;
+  d.sheen = m.d.x;
+  d.sheenTint = m.d.y;
+  d.clearcoat = m.d.z;
+  d.clearcoatRoughness = mix1(0.1f, 0.001f, m.d.w);
+  return d;
+}
+}  // namespace disney
+
 // (brdf_lambertian.rchit:110-134, brdf_rough_plastic.rchit:224-250,
 // bsdf_dielectric.rchit:248-271) all start with sampleLights(pos, ffN) and
 // differ only in the BSDF eval/pdf pair, so light sampling runs once here and
@@ -332,6 +540,16 @@ __device__ __forceinline__ void nextEvent(const SceneDev& S, const ShotDev& sh, 
           if (fabsf(dot(refract(-V, N, eta), L) - 1.0f) < EPS) bpdf = 1.0f - F;
         }
       }
+    } else if (type == ASUNA_MAT_PBR_METALNESS_ROUGHNESS) {
+      // brdf_pbr_metalness_roughness.rchit:184-195
+      const float a = gmax(sqr(m.c.x), 0.001f);
+      w = pbrEval(lRec.d, st.V, st.ffN, st.X, st.Y, ld3(m.a), a, m.c.y, m.b.z);
+      if (lRec.flags & EArea) bpdf = pbrPdf(lRec.d, st.V, st.ffN, st.X, st.Y, a);
+    } else if (type == ASUNA_MAT_DISNEY) {
+      // brdf_disney.rchit:450-466: eval (and its pdf) with EArea for every light
+      const disney::Mat dm = disney::fromDev(m);
+      const float eta = dot(st.V, st.N) > 0.0f ? (1.0f / m.b.z) : m.b.z;
+      w = disney::eval(lRec.d, st.V, st.ffN, st.X, st.Y, dm, eta, bpdf);
     } else if (type == ASUNA_MAT_PHONG) {
       // brdf_phong.rchit:12-30 eval with EArea, 39-52 pdf with lRec.flags
       const f3 kd = ld3(m.a), ks = ld3(m.c);
@@ -520,6 +738,99 @@ __device__ __forceinline__ void samplePhong(PathIO& io, const HitSt& st, const M
   io.nro = offsetPositionAlongNormal(st.pos, st.ffN);
   io.nrd = bd;
   io.thp = io.thp * (weight / bpdf);
+}
+
+// brdf_pbr_metalness_roughness.rchit:107-129,203-219: the direction pair is
+// drawn before the lobe choice; the pdf is the chosen lobe's alone and the
+// weight carries a second |cos| (as the reference writes them)
+__device__ __forceinline__ void samplePbr(PathIO& io, const HitSt& st, const MatDev& m) {
+  const float a = gmax(sqr(m.c.x), 0.001f);
+  f2 u = rnd2(io.seed);
+  const f3 V = st.V, N = st.ffN, X = st.X, Y = st.Y;
+  const f3 wo = makeNormal(toLocal(X, Y, N, V));
+  f3 wi;
+  float bpdf;
+  uint32_t bflags;
+  if (rnd(io.seed) < 0.2f) {
+    wi = cosineSampleHemisphere(u);
+    bflags = EDiffuseReflection;
+    bpdf = cosineHemispherePdf(wi.z);
+  } else {
+    wi = importanceSampleAnisoGGX(u, wo, a, a);
+    const f3 wh = makeNormal(wi + wo);
+    bpdf = importanceAnisoGGXPdf(wh, wo, a, a);
+    bflags = EGlossyReflection;
+  }
+  const f3 bd = toWorld(X, Y, N, wi);
+  const f3 weight = pbrEval(bd, V, N, X, Y, ld3(m.a), a, m.c.y, m.b.z) * fabsf(wi.z);
+  if (bpdf <= 0.0f || length(weight) == 0.0f) {
+    io.stop = true;
+    return;
+  }
+  io.bflags = bflags;
+  io.bpdf = bpdf;
+  io.nro = offsetPositionAlongNormal(st.pos, st.ffN);
+  io.nrd = bd;
+  io.thp = io.thp * (weight / (bpdf + EPS));
+}
+
+// brdf_disney.rchit:302-378,469-477: lobe CDF (diffuse, clearcoat, specular)
+// from an approximate Fresnel at N; the weight is scaled by |dot(N, L)| with
+// N in world and L in the local frame (as the reference writes it)
+__device__ __forceinline__ void sampleDisney(PathIO& io, const HitSt& st, const MatDev& m) {
+  using namespace disney;
+  const Mat mat = fromDev(m);
+  const float eta = dot(st.V, st.N) > 0.0f ? (1.0f / m.b.z) : m.b.z;
+  const f2 u = rnd2(io.seed);
+  float pdf = 0.0f;
+  f3 f = splat(0.0f);
+  float r1 = u.x;
+  const float r2 = u.y;
+  const f3 N = st.ffN, X = st.X, Y = st.Y;
+  const f3 V = toLocal(X, Y, N, st.V);
+  f3 L;
+  f3 specCol, sheenCol;
+  SpecColor(mat, eta, specCol, sheenCol);
+  float diffuseWt, specReflectWt, clearcoatWt;
+  LobeProbabilities(mat, specCol, Fresnel(mat.metallic, eta, V.z, V.z), diffuseWt, specReflectWt, clearcoatWt);
+  const float cdf0 = diffuseWt;
+  const float cdf1 = cdf0 + clearcoatWt;
+  uint32_t bflags;
+  if (r1 < cdf0) {
+    r1 = r1 / cdf0;
+    L = cosineSampleHemisphere(f2{r1, r2});
+    const f3 H = normalize(L + V);
+    f = EvalDiffuse(mat, sheenCol, V, L, H, pdf);
+    pdf = pdf * diffuseWt;
+    bflags = EDiffuseReflection;
+  } else if (r1 < cdf1) {
+    r1 = (r1 - cdf0) / (cdf1 - cdf0);
+    f3 H = SampleGTR1(mat.clearcoatRoughness, r1);
+    if (H.z < 0.0f) H = -H;
+    L = normalize(reflect(-V, H));
+    f = EvalClearcoat(mat, V, L, H, pdf);
+    pdf = pdf * clearcoatWt;
+    bflags = EGlossyReflection;
+  } else {
+    r1 = (r1 - cdf1) / (1.0f - cdf1);
+    f3 H = SampleGGXVNDF(V, mat.ax, mat.ay, r1, r2);
+    if (H.z < 0.0f) H = -H;
+    L = normalize(reflect(-V, H));
+    f = EvalSpecReflection(mat, eta, specCol, V, L, H, pdf);
+    pdf = pdf * specReflectWt;
+    bflags = EGlossyReflection;
+  }
+  const f3 bd = toWorld(X, Y, N, L);
+  const f3 weight = f * fabsf(dot(N, L));
+  if (pdf <= 0.0f || length(weight) == 0.0f) {
+    io.stop = true;
+    return;
+  }
+  io.bflags = bflags;
+  io.bpdf = pdf;
+  io.nro = offsetPositionAlongNormal(st.pos, st.ffN);
+  io.nrd = bd;
+  io.thp = io.thp * (weight / pdf);
 }
 
 // brdf_conductor.rchit:65-80,141-163: the direction sample ignores its two
@@ -736,6 +1047,19 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
           }
         } else {
           const MatDev m = S.mats[in.matId];
+          // brdf_pbr_metalness_roughness.rchit:156: the opacity test's draw
+          // comes first (pass-through, opacity > 0, is rejected at validation)
+          // brdf_disney.rchit:413 likewise (opacity in rho_spec[0])
+          if (CLS == kClsPbr || CLS == kClsDisney) rnd(io.seed);
+          if (CLS == kClsPbr && depth == 1u && frame == 0u && sh.state.n_multi_channel > 0u) {
+            // 169-174: albedo and the face-forward normal only
+            const asuna_rt_state& ps = sh.state;
+            const size_t npx = size_t(sh.width) * sh.height;
+            if (ps.diffuse_out_channel >= 0 && ps.diffuse_out_channel < ASUNA_MAX_CHANNELS)
+              sh.filmCh[size_t(ps.diffuse_out_channel) * npx + pix] = make_float4(m.a.x, m.a.y, m.a.z, 1.0f);
+            if (ps.normal_out_channel >= 0 && ps.normal_out_channel < ASUNA_MAX_CHANNELS)
+              sh.filmCh[size_t(ps.normal_out_channel) * npx + pix] = make_float4(st.ffN.x, st.ffN.y, st.ffN.z, 1.0f);
+          }
           if ((CLS == kClsLambertian || CLS == kClsPhong) && depth == 1u && frame == 0u &&
               sh.state.n_multi_channel > 0u) {
             // brdf_lambertian.rchit:93-108; brdf_phong.rchit:135-150 writes
@@ -766,6 +1090,8 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
                                       : CLS == kClsConductor  ? ASUNA_MAT_CONDUCTOR
                                       : CLS == kClsRoughConductor ? ASUNA_MAT_ROUGH_CONDUCTOR
                                       : CLS == kClsPhong      ? ASUNA_MAT_PHONG
+                                      : CLS == kClsPbr        ? ASUNA_MAT_PBR_METALNESS_ROUGHNESS
+                                      : CLS == kClsDisney     ? ASUNA_MAT_DISNEY
                                                               : ASUNA_MAT_LAMBERTIAN;
             nextEvent(S, sh, io, st, m, type, rd);
             if (CLS == kClsRoughPlastic)
@@ -782,6 +1108,10 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
               sampleRoughConductor(io, st, m);
             else if (CLS == kClsPhong)
               samplePhong(io, st, m);
+            else if (CLS == kClsPbr)
+              samplePbr(io, st, m);
+            else if (CLS == kClsDisney)
+              sampleDisney(io, st, m);
             else
               sampleLambertian(io, st, ld3(m.a));
           }
@@ -898,6 +1228,8 @@ void launchShade(const KParams& P, int grid, cudaStream_t s) {
   if (m & (1u << kClsConductor)) k_shadeClass<kClsConductor><<<grid, 256, 0, s>>>(P);
   if (m & (1u << kClsRoughConductor)) k_shadeClass<kClsRoughConductor><<<grid, 256, 0, s>>>(P);
   if (m & (1u << kClsPhong)) k_shadeClass<kClsPhong><<<grid, 256, 0, s>>>(P);
+  if (m & (1u << kClsPbr)) k_shadeClass<kClsPbr><<<grid, 256, 0, s>>>(P);
+  if (m & (1u << kClsDisney)) k_shadeClass<kClsDisney><<<grid, 256, 0, s>>>(P);
 }
 int shadeLaunches(uint32_t classMask) { return 1 + __builtin_popcount(classMask | (1u << kClsTerminal)); }
 int shadeBlocksPerSm() {

@@ -153,6 +153,39 @@ class SceneBuilder:
         m.specular = float(shininess)
         return self._add_material(name, m)
 
+    def add_pbr(self, name, albedo, metalness=0.0, roughness=0.5, ior=1.5):
+        """brdf_pbr_metalness_roughness (src/loader/material.cpp:116-143):
+        GGX specular with Schlick Fresnel (f0 from ior, tinted by albedo with
+        metalness) over a Lambertian base weighted by 1 - metalness."""
+        m = default_material()
+        m.type = A.MAT_PBR_METALNESS_ROUGHNESS
+        m.diffuse = A.f3(*albedo)
+        m.metalness = float(metalness)
+        m.roughness = float(roughness)
+        m.ior = float(ior)
+        return self._add_material(name, m)
+
+    def add_disney(self, name, base_color, metallic=0.0, roughness=0.5, subsurface=0.0, specular_tint=0.0,
+                   sheen=0.0, sheen_tint=0.0, clearcoat=0.0, clearcoat_gloss=0.0, anisotropic=0.0, ior=1.5):
+        """brdf_disney (src/loader/material.cpp:359-389; the JSON path sets
+        base colour, metallic and roughness, the others stay 0): diffuse with
+        retro-reflection, fake subsurface and sheen, anisotropic GGX
+        specular and a GTR1 clearcoat."""
+        m = default_material()
+        m.type = A.MAT_DISNEY
+        m.diffuse = A.f3(*base_color)
+        m.metalness = float(metallic)
+        m.roughness = float(roughness)
+        m.subsurface = float(subsurface)
+        m.specular_tint = float(specular_tint)
+        m.sheen = float(sheen)
+        m.sheen_tint = float(sheen_tint)
+        m.clearcoat = float(clearcoat)
+        m.clearcoat_gloss = float(clearcoat_gloss)
+        m.anisotropic = float(anisotropic)
+        m.ior = float(ior)
+        return self._add_material(name, m)
+
     def add_dielectric(self, name, ior=1.5):
         m = default_material()
         m.type = A.MAT_DIELECTRIC

@@ -1,7 +1,7 @@
 /*
  * asuna_math.h — the float transcendental functions of the path tracer.
  *
- * The reference's GLSL leaves sin, cos, acos, atan and exp to the driver
+ * The reference's GLSL leaves sin, cos, acos, atan, exp, log and pow to the driver
  * (GLSL 4.60 only bounds their error), so the reference's own sample streams
  * are defined up to those functions.  This library fixes them with one
  * implementation shared by the CUDA kernels and the CPU oracle, so a path
@@ -17,9 +17,10 @@
  *   acos  acos(x) = atan2(sqrt((1 - x)(1 + x)), x).
  *   log2  x = m 2^e with m in [sqrt(1/2), sqrt(2)); ln m = 2 atanh(s),
  *         s = (m - 1) / (m + 1), odd series to s^9; times log2(e).
+ *   log   the same ln m plus e ln 2 (ln 2 split in two parts).
  *   exp2  t = n + r, |r| <= 1/2: the exp polynomial at r ln 2, times 2^n.
  *   pow   exp2(y log2 x) (x > 0; GLSL leaves x < 0 undefined: NaN here).
- * Errors: sin, cos, exp within 1 ulp; atan2, acos, log2 within 3 ulp; exp2
+ * Errors: sin, cos, exp within 1 ulp; atan2, acos, log2, log within 3 ulp; exp2
  * within 2 ulp; pow within 2 ulp plus |y log2 x| ulp of the exponent,
  * over the ranges the path tracer uses (tested against double precision).
  */
@@ -177,10 +178,8 @@ ASUNA_MATH_FN float acosf_(float x) {
   return atan2f_(fl_sqrt((1.0f - x) * (1.0f + x)), x);
 }
 
-ASUNA_MATH_FN float log2f_(float x) {
-  if (fl_isnan(x) || x < 0.0f) return bits_to_float(0x7fc00000u);
-  if (x == 0.0f) return bits_to_float(0xff800000u);
-  if (x == bits_to_float(0x7f800000u)) return x;
+// x = 2^e m, m in [sqrt(1/2), sqrt(2)): returns ln m (x finite, > 0)
+ASUNA_MATH_FN float log_reduce(float x, int* eo) {
   int e = 0;
   uint32_t b = float_to_bits(x);
   if ((b >> 23) == 0) {  // subnormal: scale by 2^23 first
@@ -200,8 +199,28 @@ ASUNA_MATH_FN float log2f_(float x) {
   p = p * s2 + 1.0f / 5.0f;
   p = p * s2 + 1.0f / 3.0f;
   p = p * s2 + 1.0f;
-  const float ln = 2.0f * s * p;
+  *eo = e;
+  return 2.0f * s * p;
+}
+
+ASUNA_MATH_FN float log2f_(float x) {
+  if (fl_isnan(x) || x < 0.0f) return bits_to_float(0x7fc00000u);
+  if (x == 0.0f) return bits_to_float(0xff800000u);
+  if (x == bits_to_float(0x7f800000u)) return x;
+  int e;
+  const float ln = log_reduce(x, &e);
   return float(e) + ln * 0x1.715476p+0f;
+}
+
+// natural logarithm: e ln 2 (two-part constant) + ln m
+ASUNA_MATH_FN float logf_(float x) {
+  if (fl_isnan(x) || x < 0.0f) return bits_to_float(0x7fc00000u);
+  if (x == 0.0f) return bits_to_float(0xff800000u);
+  if (x == bits_to_float(0x7f800000u)) return x;
+  int e;
+  const float ln = log_reduce(x, &e);
+  const float fe = float(e);
+  return fe * 0x1.62e400p-1f + (ln + fe * 0x1.7f7d1cp-20f);
 }
 
 ASUNA_MATH_FN float exp2f_(float t) {

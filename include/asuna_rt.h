@@ -72,13 +72,13 @@ enum {
   ASUNA_MAT_LAMBERTIAN = 0, /* (*) brdf_lambertian   */
   ASUNA_MAT_KANG18 = 1,
   ASUNA_MAT_EMISSIVE = 2, /* (*) brdf_emissive      */
-  ASUNA_MAT_PBR_METALNESS_ROUGHNESS = 3,
+  ASUNA_MAT_PBR_METALNESS_ROUGHNESS = 3, /* (*) brdf_pbr_metalness_roughness */
   ASUNA_MAT_PLASTIC = 4, /* (*) brdf_plastic       */
   ASUNA_MAT_ROUGH_PLASTIC = 5, /* (*) brdf_rough_plastic */
   ASUNA_MAT_CONDUCTOR = 6, /* (*) brdf_conductor     */
   ASUNA_MAT_ROUGH_CONDUCTOR = 7, /* (*) brdf_rough_conductor */
   ASUNA_MAT_MIRROR = 8, /* (*) brdf_mirror        */
-  ASUNA_MAT_DISNEY = 9,
+  ASUNA_MAT_DISNEY = 9, /* (*) brdf_disney        */
   ASUNA_MAT_DIELECTRIC = 10, /* (*) bsdf_dielectric    */
   ASUNA_MAT_PHONG = 11, /* (*) brdf_phong         */
   ASUNA_MAT_NUM = 12
@@ -336,6 +336,9 @@ int asuna_ctx_set_traversal(asuna_ctx* ctx, int refill_extend, int refill_shadow
 int asuna_scene_create(asuna_ctx* ctx, const asuna_scene_desc* desc, asuna_scene** out);
 int asuna_scene_destroy(asuna_scene* scene);
 int asuna_scene_get_stats(const asuna_scene* scene, asuna_scene_stats* out);
+/* The checks asuna_scene_create runs before any upload (indices in range,
+ * implemented material types and features, lights), on the host alone. */
+int asuna_scene_validate(const asuna_scene_desc* desc);
 
 /* ---- film: the 9 RGBA32F output images ---------------------------------- */
 int asuna_film_create(asuna_ctx* ctx, uint32_t width, uint32_t height, asuna_film** out);
@@ -371,7 +374,7 @@ int asuna_scene_trace(asuna_ctx* ctx, const asuna_scene* scene, const float* ray
  * the allocator): renders shot->frames frames of one shot into `film` like
  * asuna_render, on `stream` (a cudaStream_t; NULL = default stream), with
  * all scratch in one fixed device array compiled into the library.  The
- * array holds ASUNA_NOALLOC_MAX_PATHS path slots (about 58 MiB, kept by
+ * array holds ASUNA_NOALLOC_MAX_PATHS path slots (about 60 MiB, kept by
  * every GPU that loads the library until exit); a frame with more pixels is
  * rejected with ASUNA_ERR_INVALID.  The array's address is set up on a
  * device by the first call there: make that call before any stream capture.

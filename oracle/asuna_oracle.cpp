@@ -45,6 +45,8 @@ inline double macos(double x) { return std::acos(x); }
 inline double matan2(double y, double x) { return std::atan2(y, x); }
 inline float mpow(float x, float y) { return asuna_math::powf_(x, y); }
 inline double mpow(double x, double y) { return std::pow(x, y); }
+inline float mlog(float x) { return asuna_math::logf_(x); }
+inline double mlog(double x) { return std::log(x); }
 inline double mexp(double x) { return std::exp(x); }
 
 template <class R> inline V3<R> mk(R a, R b, R c) { return V3<R>{a, b, c}; }
@@ -1362,6 +1364,374 @@ template <class R> void shadePhong(const Scene& s, const asuna_shot& sh, PathSta
   p.throughput = p.throughput * (weight / bpdf);
 }
 
+// brdf_pbr_metalness_roughness.rchit:14-16 (GLSL mix: x (1 - a) + y a)
+template <class R> V3<R> fresnelSchlick(R cosThetaI, V3<R> f0) {
+  return f0 + (splat(R(1)) - f0) * mpow(gclamp(R(1) - cosThetaI, R(0), R(1)), R(5));
+}
+// 57-86 (the flags argument is unused: its test is commented out)
+template <class R> V3<R> pbrEval(V3<R> L, V3<R> V, V3<R> N, V3<R> X, V3<R> Y, V3<R> albedo, R ax, R ay, R metalness,
+                                 R eta) {
+  V3<R> weight = splat(R(0));
+  R NdotL = dot(N, L), NdotV = dot(N, V);
+  if (NdotL <= R(0) || NdotV <= R(0)) return weight;
+  V3<R> H = makeNormal(L + V);
+  R HdotN = dot(H, N), HdotX = dot(H, X), HdotY = dot(H, Y), HdotV = dot(H, V);
+  R F0 = sqr((eta - R(1)) / (eta + R(1)));
+  V3<R> f0 = splat(F0) * (R(1) - metalness) + albedo * metalness;
+  V3<R> Fs = fresnelSchlick(HdotV, f0);
+  R Ds = dAnisoGGX(HdotN, HdotX, HdotY, ax, ay);
+  R Gs = g1SmithAnisoGGX(NdotV, dot(V, X), dot(V, Y), ax, ay);
+  Gs = Gs * g1SmithAnisoGGX(NdotL, dot(L, X), dot(L, Y), ax, ay);
+  V3<R> diffuse = albedo * (R(1) - metalness) * K<R>::INV_PI;
+  V3<R> specular = Fs * Ds * Gs;
+  weight = weight + diffuse;
+  weight = weight + specular;
+  weight = weight * NdotL;
+  return weight;
+}
+// 88-105: a fixed 0.2 / 0.8 mixture of the cosine and GGX pdfs
+template <class R> R pbrPdf(V3<R> L, V3<R> V, V3<R> N, V3<R> X, V3<R> Y, R ax, R ay, uint32_t flags) {
+  R pdf = R(0);
+  if ((flags & EArea) == 0) return pdf;
+  R NdotL = dot(N, L), NdotV = dot(N, V);
+  if (NdotL <= R(0) || NdotV <= R(0)) return pdf;
+  V3<R> H = makeNormal(L + V);
+  V3<R> wh = makeNormal(toLocal(X, Y, N, H)), wo = makeNormal(toLocal(X, Y, N, V)),
+        wi = makeNormal(toLocal(X, Y, N, L));
+  pdf = pdf + R(0.2f) * cosineHemispherePdf(wi.z);
+  pdf = pdf + (R(1) - R(0.2f)) * importanceAnisoGGXPdf(wh, wo, ax, ay);
+  return pdf;
+}
+
+// brdf_pbr_metalness_roughness.rchit:131-219 (main) with sampleBsdf 107-129.
+// Random numbers in order: the opacity test, the light sample, the direction
+// pair, then the lobe choice.  The sampled direction's pdf is that of the
+// chosen lobe alone and its weight carries a second |cos| (as written).
+// AOVs at depth 1: albedo and the face-forward normal only.
+template <class R> void shadePbr(const Scene& s, const asuna_shot& sh, PathState<R>& p, HitState<R>& st) {
+  const asuna_rt_state& ps = sh.state;
+  V3<R> albedo = L3<R>(st.mat.diffuse);
+  R metalness = R(st.mat.metalness), roughness = R(st.mat.roughness);
+  R opacity = R(st.mat.specular);
+  // 156-160: the pass-through branch (opacity > 0) is rejected at scene
+  // validation; the draw is kept
+  (void)(rnd<R>(p.seed) < opacity);
+  R ax = gmax(sqr(roughness), R(0.001f)), ay = ax;
+  R eta = R(st.mat.ior);
+  if (p.depth == 1) {
+    if (ps.diffuse_out_channel >= 0) p.ch[ps.diffuse_out_channel] = albedo;
+    if (ps.normal_out_channel >= 0) p.ch[ps.normal_out_channel] = st.ffN;
+  }
+  {
+    bool visible;
+    LRec<R> lRec;
+    V3<R> Ld = splat(R(0));
+    V3<R> rad = sampleLights<R>(s, sh, p, st.pos, st.ffN, visible, lRec);
+    if (visible) {
+      V3<R> w = pbrEval<R>(lRec.d, st.V, st.ffN, st.X, st.Y, albedo, ax, ay, metalness, eta);
+      R bpdf = pbrPdf<R>(lRec.d, st.V, st.ffN, st.X, st.Y, ax, ay, lRec.flags);
+      R mis = powerHeuristic(lRec.pdf, bpdf);
+      Ld = mis * w * rad * p.throughput / (lRec.pdf + K<R>::EPS);
+    }
+    p.drad = Ld;
+    p.dskip = !visible;
+  }
+  V2<R> u = rnd2<R>(p.seed);
+  V3<R> V = st.V, N = st.ffN, X = st.X, Y = st.Y;
+  V3<R> wo = makeNormal(toLocal(X, Y, N, V));
+  V3<R> wi;
+  R bpdf = R(0);
+  uint32_t bflags;
+  if (rnd<R>(p.seed) < R(0.2f)) {
+    wi = cosineSampleHemisphere(u);
+    bflags = EDiffuseReflection;
+    bpdf = cosineHemispherePdf(wi.z);
+  } else {
+    wi = importanceSampleAnisoGGX(u, wo, ax, ay);
+    V3<R> wh = makeNormal(wi + wo);
+    bpdf = importanceAnisoGGXPdf(wh, wo, ax, ay);
+    bflags = EGlossyReflection;
+  }
+  V3<R> bd = toWorld(X, Y, N, wi);
+  V3<R> weight = pbrEval<R>(bd, V, N, X, Y, albedo, ax, ay, metalness, eta) * std::fabs(wi.z);
+  if (bpdf <= R(0) || length(weight) == R(0)) {
+    p.stop = true;
+    return;
+  }
+  p.bflags = bflags;
+  p.bpdf = bpdf;
+  p.ro = offsetPositionAlongNormal(st.pos, st.ffN);
+  p.rd = bd;
+  p.throughput = p.throughput * (weight / (bpdf + K<R>::EPS));
+}
+
+// ---- brdf_disney.rchit -------------------------------------------------------
+// GLSL mix of scalars: x (1 - a) + y a
+template <class R> inline R gmix(R x, R y, R a) { return x * (R(1) - a) + y * a; }
+template <class R> inline V3<R> gmix3(V3<R> x, V3<R> y, R a) { return x * (R(1) - a) + y * a; }
+// 31-48
+template <class R> struct DisneyMat {
+  V3<R> baseColor;
+  R anisotropic, metallic, roughness, subsurface, specularTint, sheen, sheenTint, clearcoat, clearcoatRoughness, ior,
+      opacity, ax, ay;
+};
+// 50-52
+template <class R> R dLuminance(V3<R> c) { return R(0.212671f) * c.x + R(0.715160f) * c.y + R(0.072169f) * c.z; }
+// 54-59
+template <class R> R GTR1(R NDotH, R a) {
+  if (a >= R(1)) return K<R>::INV_PI;
+  R a2 = a * a;
+  R t = R(1) + (a2 - R(1)) * NDotH * NDotH;
+  return (a2 - R(1)) / (K<R>::PI * mlog(a2) * t);
+}
+// 61-74: the polar angle uses r1 as well (r2 is unused, as written)
+template <class R> V3<R> SampleGTR1(R rgh, R r1, R r2) {
+  (void)r2;
+  R a = gmax(R(0.001f), rgh);
+  R a2 = a * a;
+  R phi = r1 * K<R>::TWO_PI;
+  R cosTheta = std::sqrt((R(1) - mpow(a2, R(1) - r1)) / (R(1) - a2));
+  R sinTheta = gclamp(std::sqrt(R(1) - (cosTheta * cosTheta)), R(0), R(1));
+  R sinPhi = msin(phi), cosPhi = mcos(phi);
+  return V3<R>{sinTheta * cosPhi, sinTheta * sinPhi, cosTheta};
+}
+// 95-114 (Heitz 2018, visible normals)
+template <class R> V3<R> SampleGGXVNDF(V3<R> V, R ax, R ay, R r1, R r2) {
+  V3<R> Vh = normalize(V3<R>{ax * V.x, ay * V.y, V.z});
+  R lensq = Vh.x * Vh.x + Vh.y * Vh.y;
+  V3<R> T1 = lensq > R(0) ? V3<R>{-Vh.y, Vh.x, R(0)} * (R(1) / std::sqrt(lensq)) : V3<R>{R(1), R(0), R(0)};
+  V3<R> T2 = cross(Vh, T1);
+  R r = std::sqrt(r1);
+  R phi = R(2.0f * 3.14159265358979323846f) * r2;
+  R t1 = r * mcos(phi);
+  R t2 = r * msin(phi);
+  R sv = R(0.5f) * (R(1) + Vh.z);
+  t2 = (R(1) - sv) * std::sqrt(R(1) - t1 * t1) + sv * t2;
+  V3<R> Nh = t1 * T1 + t2 * T2 + std::sqrt(gmax(R(0), R(1) - t1 * t1 - t2 * t2)) * Vh;
+  return normalize(V3<R>{ax * Nh.x, ay * Nh.y, gmax(R(0), Nh.z)});
+}
+// 116-121
+template <class R> R GTR2Aniso(R NDotH, R HDotX, R HDotY, R ax, R ay) {
+  R a = HDotX / ax, b = HDotY / ay;
+  R c = a * a + b * b + NDotH * NDotH;
+  return R(1) / (K<R>::PI * ax * ay * c * c);
+}
+// 133-137
+template <class R> R SmithG(R NDotV, R alphaG) {
+  R a = alphaG * alphaG, b = NDotV * NDotV;
+  return (R(2) * NDotV) / (NDotV + std::sqrt(a + b - a * b));
+}
+// 139-144
+template <class R> R SmithGAniso(R NDotV, R VDotX, R VDotY, R ax, R ay) {
+  R a = VDotX * ax, b = VDotY * ay, c = NDotV;
+  return (R(2) * NDotV) / (NDotV + std::sqrt(a * a + b * b + c * c));
+}
+// 146-150
+template <class R> R SchlickFresnel(R u) {
+  R m = gclamp(R(1) - u, R(0), R(1));
+  R m2 = m * m;
+  return m2 * m2 * m;
+}
+// 152-164
+template <class R> R DisneyDielectricFresnel(R cosThetaI, R eta) {
+  R sinThetaTSq = eta * eta * (R(1) - cosThetaI * cosThetaI);
+  if (sinThetaTSq > R(1)) return R(1);
+  R cosThetaT = std::sqrt(gmax(R(1) - sinThetaTSq, R(0)));
+  R rs = (eta * cosThetaT - cosThetaI) / (eta * cosThetaT + cosThetaI);
+  R rp = (eta * cosThetaI - cosThetaT) / (eta * cosThetaI + cosThetaT);
+  return R(0.5f) * (rs * rs + rp * rp);
+}
+// 166-170
+template <class R> R DisneyFresnel(R metallic, R eta, R LDotH, R VDotH) {
+  R metallicFresnel = SchlickFresnel(LDotH);
+  R dielectricFresnel = DisneyDielectricFresnel(std::fabs(VDotH), eta);
+  return gmix(dielectricFresnel, metallicFresnel, metallic);
+}
+// 172-195
+template <class R> V3<R> EvalDiffuse(const DisneyMat<R>& mat, V3<R> Csheen, V3<R> V, V3<R> L, V3<R> H, R& pdf) {
+  pdf = R(0);
+  if (L.z <= R(0)) return splat(R(0));
+  R FL = SchlickFresnel(L.z), FV = SchlickFresnel(V.z), FH = SchlickFresnel(dot(L, H));
+  R Fd90 = R(0.5f) + R(2) * dot(L, H) * dot(L, H) * mat.roughness;
+  R Fd = gmix(R(1), Fd90, FL) * gmix(R(1), Fd90, FV);
+  R Fss90 = dot(L, H) * dot(L, H) * mat.roughness;
+  R Fss = gmix(R(1), Fss90, FL) * gmix(R(1), Fss90, FV);
+  R ss = R(1.25f) * (Fss * (R(1) / (L.z + V.z) - R(0.5f)) + R(0.5f));
+  V3<R> Fsheen = FH * mat.sheen * Csheen;
+  pdf = L.z * K<R>::INV_PI;
+  return (R(1) - mat.metallic) * (K<R>::INV_PI * gmix(Fd, ss, mat.subsurface) * mat.baseColor + Fsheen);
+}
+// 197-211
+template <class R>
+V3<R> EvalSpecReflection(const DisneyMat<R>& mat, R eta, V3<R> specCol, V3<R> V, V3<R> L, V3<R> H, R& pdf) {
+  pdf = R(0);
+  if (L.z <= R(0)) return splat(R(0));
+  R FM = DisneyFresnel(mat.metallic, eta, dot(L, H), dot(V, H));
+  V3<R> F = gmix3(specCol, splat(R(1)), FM);
+  R D = GTR2Aniso(H.z, H.x, H.y, mat.ax, mat.ay);
+  R G1 = SmithGAniso(std::fabs(V.z), V.x, V.y, mat.ax, mat.ay);
+  R G2 = G1 * SmithGAniso(std::fabs(L.z), L.x, L.y, mat.ax, mat.ay);
+  pdf = G1 * D / (R(4) * V.z);
+  return F * D * G2 / (R(4) * L.z * V.z);
+}
+// 213-226
+template <class R> V3<R> EvalClearcoat(const DisneyMat<R>& mat, V3<R> V, V3<R> L, V3<R> H, R& pdf) {
+  pdf = R(0);
+  if (L.z <= R(0)) return splat(R(0));
+  R FH = DisneyDielectricFresnel(dot(V, H), R(1.0f / 1.5f));
+  R F = gmix(R(0.04f), R(1), FH);
+  R D = GTR1(H.z, mat.clearcoatRoughness);
+  R G = SmithG(L.z, R(0.25f)) * SmithG(V.z, R(0.25f));
+  R jacobian = R(1) / (R(4) * dot(V, H));
+  pdf = D * H.z * jacobian;
+  return splat(R(0.25f)) * mat.clearcoat * F * D * G / (R(4) * L.z * V.z);
+}
+// 228-236
+template <class R> void GetSpecColor(const DisneyMat<R>& mat, R eta, V3<R>& specCol, V3<R>& sheenCol) {
+  R lum = dLuminance(mat.baseColor);
+  V3<R> ctint = lum > R(0) ? mat.baseColor / lum : splat(R(1));
+  R F0 = (R(1) - eta) / (R(1) + eta);
+  specCol = gmix3(F0 * F0 * gmix3(splat(R(1)), ctint, mat.specularTint), mat.baseColor, mat.metallic);
+  sheenCol = gmix3(splat(R(1)), ctint, mat.sheenTint);
+}
+// 238-250
+template <class R>
+void GetLobeProbabilities(const DisneyMat<R>& mat, V3<R> specCol, R approxFresnel, R& diffuseWt, R& specReflectWt,
+                          R& clearcoatWt) {
+  diffuseWt = dLuminance(mat.baseColor) * (R(1) - mat.metallic);
+  specReflectWt = dLuminance(gmix3(specCol, splat(R(1)), approxFresnel));
+  clearcoatWt = R(0.25f) * mat.clearcoat * (R(1) - mat.metallic);
+  R totalWt = diffuseWt + specReflectWt + clearcoatWt;
+  diffuseWt = diffuseWt / totalWt;
+  specReflectWt = specReflectWt / totalWt;
+  clearcoatWt = clearcoatWt / totalWt;
+}
+// 252-300 (flags is EArea at both call sites)
+template <class R>
+V3<R> disneyEval(V3<R> L, V3<R> V, V3<R> N, V3<R> X, V3<R> Y, const DisneyMat<R>& mat, R eta, R& bsdfPdf) {
+  V3<R> weight = splat(R(0));
+  bsdfPdf = R(0);
+  V = toLocal(X, Y, N, V);
+  L = toLocal(X, Y, N, L);
+  if (L.z <= R(0) || V.z <= R(0)) return weight;
+  V3<R> H = normalize(L + V);
+  if (H.z < R(0)) H = -H;
+  V3<R> specCol, sheenCol;
+  GetSpecColor(mat, eta, specCol, sheenCol);
+  R diffuseWt, specReflectWt, clearcoatWt;
+  R fresnel = DisneyFresnel(mat.metallic, eta, dot(L, H), dot(V, H));
+  GetLobeProbabilities(mat, specCol, fresnel, diffuseWt, specReflectWt, clearcoatWt);
+  R pdf = R(0);
+  if (diffuseWt > R(0) && L.z > R(0)) {
+    weight = weight + EvalDiffuse(mat, sheenCol, V, L, H, pdf);
+    bsdfPdf = bsdfPdf + pdf * diffuseWt;
+  }
+  if (specReflectWt > R(0) && L.z > R(0) && V.z > R(0)) {
+    weight = weight + EvalSpecReflection(mat, eta, specCol, V, L, H, pdf);
+    bsdfPdf = bsdfPdf + pdf * specReflectWt;
+  }
+  if (clearcoatWt > R(0) && L.z > R(0) && V.z > R(0)) {
+    weight = weight + EvalClearcoat(mat, V, L, H, pdf);
+    bsdfPdf = bsdfPdf + pdf * clearcoatWt;
+  }
+  return weight * L.z;
+}
+
+// brdf_disney.rchit:380-477 (main) with sampleBsdf 302-378.  Random numbers:
+// the opacity test, the light sample, the direction pair.  No AOVs (the
+// depth-1 block is commented out).  The sampled weight is scaled by
+// |dot(N, L)| with N in world and L in the local frame, as written.
+template <class R> void shadeDisney(const Scene& s, const asuna_shot& sh, PathState<R>& p, HitState<R>& st) {
+  const asuna_material& m = st.mat;
+  R opacity = R(m.rho_spec[0]);
+  // 413-417: pass-through (opacity > 0) is rejected at scene validation
+  (void)(rnd<R>(p.seed) < opacity);
+  DisneyMat<R> mat;
+  {
+    R rough = R(m.roughness);
+    R aspect = std::sqrt(R(1) - R(m.anisotropic) * R(0.9f));
+    mat.ax = gmax(R(0.001f), rough * rough / aspect);
+    mat.ay = gmax(R(0.001f), rough * rough * aspect);
+    mat.baseColor = L3<R>(m.diffuse);
+    mat.anisotropic = R(m.anisotropic);
+    mat.metallic = R(m.metalness);
+    mat.roughness = gmax(rough * rough, R(0.001f));
+    mat.subsurface = R(m.subsurface);
+    mat.specularTint = R(m.specular_tint);
+    mat.sheen = R(m.sheen);
+    mat.sheenTint = R(m.sheen_tint);
+    mat.clearcoat = R(m.clearcoat);
+    mat.clearcoatRoughness = gmix(R(0.1f), R(0.001f), R(m.clearcoat_gloss));
+    mat.ior = R(m.ior);
+    mat.opacity = opacity;
+  }
+  R eta = dot(st.V, st.N) > R(0) ? (R(1) / mat.ior) : mat.ior;
+  {
+    bool visible;
+    LRec<R> lRec;
+    V3<R> Ld = splat(R(0));
+    V3<R> rad = sampleLights<R>(s, sh, p, st.pos, st.ffN, visible, lRec);
+    if (visible) {
+      R bpdf;
+      V3<R> w = disneyEval<R>(lRec.d, st.V, st.ffN, st.X, st.Y, mat, eta, bpdf);
+      R mis = powerHeuristic(lRec.pdf, bpdf);
+      Ld = Ld + mis * w * rad * p.throughput / (lRec.pdf + K<R>::EPS);
+    }
+    p.drad = Ld;
+    p.dskip = !visible;
+  }
+  V2<R> u = rnd2<R>(p.seed);
+  R pdf = R(0);
+  V3<R> f = splat(R(0));
+  R r1 = u.x, r2 = u.y;
+  V3<R> N = st.ffN, X = st.X, Y = st.Y;
+  V3<R> V = toLocal(X, Y, N, st.V);
+  V3<R> L;
+  V3<R> specCol, sheenCol;
+  GetSpecColor(mat, eta, specCol, sheenCol);
+  R diffuseWt, specReflectWt, clearcoatWt;
+  R approxFresnel = DisneyFresnel(mat.metallic, eta, V.z, V.z);
+  GetLobeProbabilities(mat, specCol, approxFresnel, diffuseWt, specReflectWt, clearcoatWt);
+  R cdf0 = diffuseWt;
+  R cdf1 = cdf0 + clearcoatWt;
+  uint32_t bflags;
+  if (r1 < cdf0) {
+    r1 = r1 / cdf0;
+    L = cosineSampleHemisphere(V2<R>{r1, r2});
+    V3<R> H = normalize(L + V);
+    f = EvalDiffuse(mat, sheenCol, V, L, H, pdf);
+    pdf = pdf * diffuseWt;
+    bflags = EDiffuseReflection;
+  } else if (r1 < cdf1) {
+    r1 = (r1 - cdf0) / (cdf1 - cdf0);
+    V3<R> H = SampleGTR1(mat.clearcoatRoughness, r1, r2);
+    if (H.z < R(0)) H = -H;
+    L = normalize(reflect(-V, H));
+    f = EvalClearcoat(mat, V, L, H, pdf);
+    pdf = pdf * clearcoatWt;
+    bflags = EGlossyReflection;
+  } else {
+    r1 = (r1 - cdf1) / (R(1) - cdf1);
+    V3<R> H = SampleGGXVNDF(V, mat.ax, mat.ay, r1, r2);
+    if (H.z < R(0)) H = -H;
+    L = normalize(reflect(-V, H));
+    f = EvalSpecReflection(mat, eta, specCol, V, L, H, pdf);
+    pdf = pdf * specReflectWt;
+    bflags = EGlossyReflection;
+  }
+  V3<R> bd = toWorld(X, Y, N, L);
+  V3<R> weight = f * std::fabs(dot(N, L));
+  if (pdf <= R(0) || length(weight) == R(0)) {
+    p.stop = true;
+    return;
+  }
+  p.bflags = bflags;
+  p.bpdf = pdf;
+  p.ro = offsetPositionAlongNormal(st.pos, st.ffN);
+  p.rd = bd;
+  p.throughput = p.throughput * (weight / pdf);
+}
+
 // brdf_conductor.rchit:14-36 (P. Shirley's conductor Fresnel)
 template <class R> R conductorReflectance(R eta, R k, R cosThetaI) {
   R cosThetaISq = cosThetaI * cosThetaI;
@@ -1590,6 +1960,10 @@ void tracePath(const Scene& s, const asuna_shot& sh, uint32_t x, uint32_t y, uin
           shadeRoughConductor<R>(s, sh, p, hs);
         else if (type == ASUNA_MAT_PHONG)
           shadePhong<R>(s, sh, p, hs);
+        else if (type == ASUNA_MAT_PBR_METALNESS_ROUGHNESS)
+          shadePbr<R>(s, sh, p, hs);
+        else if (type == ASUNA_MAT_DISNEY)
+          shadeDisney<R>(s, sh, p, hs);
         else
           shadeLambertian<R>(s, sh, p, hs);
         p.sig = sigMix(p.sig, p.stop ? 0xfffu : p.bflags);
@@ -1727,6 +2101,7 @@ float oracle_math(int which, float x, float y) {
     case 5: return asuna_math::log2f_(x);
     case 6: return asuna_math::exp2f_(x);
     case 7: return asuna_math::powf_(x, y);
+    case 8: return asuna_math::logf_(x);
     default: return matan2(x, y);
   }
 }

@@ -13,7 +13,7 @@ Rewrites (all mechanical, no logic changes):
   * ``#include`` of a GLSL file -> the translated file; of ``shared/*.h`` ->
     dropped (the harness includes them at global scope);
   * ``inout T x`` / ``out T x`` -> ``T& x``; ``in T x`` -> ``T x``;
-  * rvalue swizzles ``.xy .xyz .rg .rgb .rgba`` -> accessor calls;
+  * rvalue swizzles ``.xy .xyz .rg .rgb .rgba .r`` -> accessor calls;
   * unsuffixed floating literals get an ``f`` suffix (GLSL literals are float);
   * the macro ``INFINITY`` is renamed (it clashes with C's);
   * ``vec2(rand(s), rand(s))`` -> brace initialisation, because C++ does not
@@ -50,10 +50,12 @@ SHADERS = {
     "bxdf/raytrace.brdf_conductor.rchit": "stage_conductor",
     "bxdf/raytrace.brdf_rough_conductor.rchit": "stage_rough_conductor",
     "bxdf/raytrace.brdf_phong.rchit": "stage_phong",
+    "bxdf/raytrace.brdf_pbr_metalness_roughness.rchit": "stage_pbr",
+    "bxdf/raytrace.brdf_disney.rchit": "stage_disney",
 }
 
 FLOAT_LIT = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")
-SWIZZLE = re.compile(r"\.(xyz|xy|rgba|rgb|rg)\b")
+SWIZZLE = re.compile(r"\.(xyz|xy|rgba|rgb|rg|r)\b")
 DROP_LINE = re.compile(r"^\s*(#version|#extension|layout\s*\(|hitAttributeEXT)")
 
 

@@ -61,6 +61,7 @@ struct vec4 {
   vec4(vec3 v, B b) : x(v.x), y(v.y), z(v.z), w(float(b)) {}
   vec3 xyz() const { return vec3(x, y, z); }
   vec3 rgb() const { return vec3(x, y, z); }
+  float r() const { return x; }
   vec2 xy() const { return vec2(x, y); }
   vec2 rg() const { return vec2(x, y); }
   vec4 rgba() const { return *this; }
@@ -163,6 +164,8 @@ inline float cos(float x) { return asuna_math::cosf_(x); }
 inline float acos(float x) { return asuna_math::acosf_(x); }
 inline float atan(float y, float x) { return asuna_math::atan2f_(y, x); }
 inline float pow(float x, float y) { return asuna_math::powf_(x, y); }
+inline float log(float x) { return asuna_math::logf_(x); }
+inline float inversesqrt(float x) { return 1.0f / std::sqrt(x); }
 inline float sign(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
 inline bool isnan(float x) { return std::isnan(x); }
 inline bool isinf(float x) { return std::isinf(x); }
@@ -197,6 +200,12 @@ inline float clamp(A x, B lo, C hi) {
 template <class B, class C>
 inline vec3 clamp(vec3 v, B lo, C hi) {
   return vec3(clamp(v.x, lo, hi), clamp(v.y, lo, hi), clamp(v.z, lo, hi));
+}
+// GLSL mix as the specification writes it: x * (1 - a) + y * a
+inline vec3 mix(vec3 x, vec3 y, float a) { return x * (1.0f - a) + y * a; }
+template <class A, class B, class T, class = std::enable_if_t<is_num<A> && is_num<B>>>
+inline float mix(A x, B y, T a) {
+  return float(x) * (1.0f - float(a)) + float(y) * float(a);
 }
 
 // ---- geometric built-ins ----------------------------------------------------

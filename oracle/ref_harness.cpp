@@ -95,6 +95,8 @@ static thread_local RayPayload payload;
 #include "raytrace.brdf_conductor.rchit.h"
 #include "raytrace.brdf_rough_conductor.rchit.h"
 #include "raytrace.brdf_phong.rchit.h"
+#include "raytrace.brdf_pbr_metalness_roughness.rchit.h"
+#include "raytrace.brdf_disney.rchit.h"
 }  // namespace glslx
 
 namespace {
@@ -179,6 +181,12 @@ void traceRayEXT(accelerationStructureEXT, uint, uint, uint, uint, uint, vec3 or
       break;
     case MaterialTypeBrdfPhong:
       stage_phong::main();
+      break;
+    case MaterialTypeBrdfPbrMetalnessRoughness:
+      stage_pbr::main();
+      break;
+    case MaterialTypeBrdfDisney:
+      stage_disney::main();
       break;
     default:
       stage_lambertian::main();

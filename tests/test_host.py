@@ -255,7 +255,7 @@ def test_json_scene_renders_like_builder_on_oracle(tmp_path):
     ('{"state": {}, "camera": {"type": "fisheye", "film": {"resolution": [8, 8]}}, "meshes": [], "instances": []}',
      A.ERR_PARSE),
     ('{"state": {}, "camera": {"type": "perspective", "film": {"resolution": [8, 8]}}, "meshes": [], '
-     '"instances": [], "materials": [{"type": "brdf_disney", "name": "d"}]}', A.ERR_UNSUPPORTED),
+     '"instances": [], "materials": [{"type": "brdf_kang18", "name": "d"}]}', A.ERR_UNSUPPORTED),
     ('{"state": {}, "camera": {"type": "perspective", "film": {"resolution": [8, 8]}}, '
      '"meshes": [{"name": "m", "path": "missing.obj"}], "instances": []}', A.ERR_IO),
     ('{"state": {"path_tracing": {"multi_channel": ["a","b","c","d","e","f","g","h"]}}, '
@@ -364,10 +364,11 @@ def test_hdr_envmap_reader(tmp_path):
 
 
 def test_json_material_plugins_match_builder():
-    """brdf_plastic, brdf_mirror, brdf_conductor, brdf_rough_conductor and
-    brdf_phong parse into the same device structs as the builder
-    (src/loader/material.cpp:197-210, 233-243, 306-347, 391-405); an unknown
-    metal is a parse error."""
+    """brdf_plastic, brdf_mirror, brdf_conductor, brdf_rough_conductor,
+    brdf_phong, brdf_pbr_metalness_roughness and brdf_disney parse into the
+    same device structs as the builder (src/loader/material.cpp:116-143,
+    197-210, 233-243, 306-347, 359-405); an unknown metal is a parse error;
+    PBR and Disney opacity (pass-through) is rejected as unsupported."""
     base = {"state": {}, "camera": {"type": "perspective", "film": {"resolution": [8, 8]}}, "meshes": [],
             "instances": []}
     mats = [{"type": "brdf_plastic", "name": "p", "diffuse_reflectance": [0.7, 0.65, 0.1], "ior": 1.6},
@@ -377,7 +378,11 @@ def test_json_material_plugins_match_builder():
              "alpha": [0.15, 0.3]},
             {"type": "brdf_conductor", "name": "cu"},
             {"type": "brdf_phong", "name": "ph", "diffuse_reflectance": [0.3, 0.5, 0.2],
-             "specular_reflectance": [0.5, 0.5, 0.45], "shininess": 40}]
+             "specular_reflectance": [0.5, 0.5, 0.45], "shininess": 40},
+            {"type": "brdf_pbr_metalness_roughness", "name": "pb", "diffuse_reflectance": [0.9, 0.6, 0.3],
+             "metalness": 0.7, "roughness": 0.35},
+            {"type": "brdf_disney", "name": "dn", "diffuse_reflectance": [0.25, 0.45, 0.85], "metallic": 0.3,
+             "roughness": 0.4}]
     js = ag.JsonScene(text=json.dumps({**base, "materials": mats}), base_dir=".")
     d = js.desc().desc
     b = ag.SceneBuilder()
@@ -387,6 +392,8 @@ def test_json_material_plugins_match_builder():
     b.add_conductor("al", "Al", (0.9, 0.9, 0.9), alpha=(0.15, 0.3))
     b.add_conductor("cu")
     b.add_phong("ph", (0.3, 0.5, 0.2), (0.5, 0.5, 0.45), 40.0)
+    b.add_pbr("pb", (0.9, 0.6, 0.3), metalness=0.7, roughness=0.35)
+    b.add_disney("dn", (0.25, 0.45, 0.85), metallic=0.3, roughness=0.4)
     assert d.num_materials == len(b.materials)
     for k in range(1, d.num_materials):
         assert bytes(d.materials[k]) == bytes(b.materials[k]), k
@@ -402,6 +409,21 @@ def test_json_material_plugins_match_builder():
         ag.JsonScene(text=json.dumps({**base, "materials": [{"type": "brdf_conductor", "name": "x",
                                                              "material": "Unobtainium"}]}), base_dir=".")
     assert e.value.code == A.ERR_PARSE
+    b2 = ag.SceneBuilder()
+    k = b2.add_pbr("glassy", (0.5, 0.5, 0.5))
+    b2.materials[k].specular = 0.5
+    with pytest.raises(ag.AsunaError) as e:
+        A.check(A.lib().asuna_scene_validate(b2.desc().ptr))
+    assert e.value.code == A.ERR_UNSUPPORTED
+    b2.materials[k].specular = 0.0
+    A.check(A.lib().asuna_scene_validate(b2.desc().ptr))
+    # Disney's JSON "opacity" lands in rho_spec[0]: parsed, then rejected
+    js = ag.JsonScene(text=json.dumps({**base, "materials": [{"type": "brdf_disney", "name": "x", "opacity": 0.5}]}),
+                      base_dir=".")
+    assert js.desc().desc.materials[1].rho_spec[0] == 0.5
+    with pytest.raises(ag.AsunaError) as e:
+        A.check(A.lib().asuna_scene_validate(js.desc().ptr))
+    assert e.value.code == A.ERR_UNSUPPORTED
 
 
 def test_post_state_layout_defaults_and_json():

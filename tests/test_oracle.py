@@ -76,7 +76,7 @@ def test_oracle_double_precision_close_to_float():
 @pytest.mark.parametrize("which,fn,lo,hi,ulps", [(0, np.sin, -7, 7, 1), (1, np.cos, -7, 7, 1), (2, np.exp, -20, 1, 1),
                                                  (3, np.arccos, -1, 1, 3), (4, None, -3, 3, 3),
                                                  (5, np.log2, 1e-6, 40, 3), (6, np.exp2, -30, 30, 2),
-                                                 (7, "pow", 0.0, 1.0, 80)])
+                                                 (7, "pow", 0.0, 1.0, 80), (8, np.log, 1e-6, 40, 3)])
 def test_shared_math_accuracy(which, fn, lo, hi, ulps):
     """include/asuna_math.h (used by the CUDA kernels and the oracle) against
     double precision, in ulps of the float result (pow: bases in (0, 1],
