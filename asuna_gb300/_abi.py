@@ -17,7 +17,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_IO, ERR_PARSE, ERR_TIMEOUT, ERR_UNSUPPOR
 CAMERA_PERSPECTIVE, CAMERA_OPENCV = 0, 1
 LIGHT_DIRECTIONAL, LIGHT_RECT, LIGHT_TRIANGLE, LIGHT_POINT = 0, 1, 2, 3
 MAT_LAMBERTIAN, MAT_EMISSIVE, MAT_PLASTIC, MAT_ROUGH_PLASTIC, MAT_MIRROR, MAT_DIELECTRIC = 0, 2, 4, 5, 8, 10
-MAT_CONDUCTOR, MAT_ROUGH_CONDUCTOR, MAT_PHONG, MAT_PBR_METALNESS_ROUGHNESS, MAT_DISNEY = 6, 7, 11, 3, 9
+MAT_CONDUCTOR, MAT_ROUGH_CONDUCTOR, MAT_PHONG, MAT_PBR_METALNESS_ROUGHNESS, MAT_DISNEY, MAT_KANG18 = 6, 7, 11, 3, 9, 1
 CH_DIFFUSE, CH_NORMAL, CH_SPECULAR, CH_TANGENT, CH_ROUGHNESS, CH_POSITION, CH_UV, CH_DEPTH = range(8)
 SHOT_RR = 1
 NUM_OUTPUT_IMAGES = 9

@@ -9,7 +9,7 @@ caller's, so they never touch its sample streams.
 """
 import itertools
 
-BYTES_PER_PATH = 240  # wavefront state per path slot (asuna_gb300/csrc/engine.cu)
+BYTES_PER_PATH = 244  # wavefront state per path slot (asuna_gb300/csrc/engine.cu)
 
 
 def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64), trace_options=(0, 6),

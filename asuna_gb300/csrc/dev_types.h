@@ -122,7 +122,7 @@ struct __align__(16) RangeDev {
   uint32_t pad[3];
 };
 
-// Counters in device memory (one 4 KB page).
+// Counters in device memory.
 enum CounterSlot {
   kCntExtend0 = 0,  // rays in extend queue 0
   kCntExtend1 = 1,  // rays in extend queue 1
@@ -130,7 +130,7 @@ enum CounterSlot {
   kCntFetchExtend = 3,
   kCntFetchShadow = 4,
   kCntCls0 = 5,  // rays per shading class (kNumShadeClasses slots)
-  kCntNum32 = 16
+  kCntNum32 = 24
 };
 
 // Shading classes: the hits of an extend pass are split by what shades them,
@@ -147,7 +147,8 @@ enum ShadeClass {
   kClsPhong = 8,
   kClsPbr = 9,  // brdf_pbr_metalness_roughness
   kClsDisney = 10,
-  kNumShadeClasses = 11
+  kClsKang18 = 11,
+  kNumShadeClasses = 12
 };
 static_assert(kCntCls0 + kNumShadeClasses <= kCntNum32, "class counters exceed the counter page's slots");
 // The class that shades a hit on a surface of material `type` (not a light).
@@ -165,6 +166,7 @@ inline int shadeClassOf(uint32_t type) {
     case ASUNA_MAT_PHONG: return kClsPhong;
     case ASUNA_MAT_PBR_METALNESS_ROUGHNESS: return kClsPbr;
     case ASUNA_MAT_DISNEY: return kClsDisney;
+    case ASUNA_MAT_KANG18: return kClsKang18;
     case ASUNA_MAT_EMISSIVE: return kClsTerminal;
     default: return kClsLambertian;
   }

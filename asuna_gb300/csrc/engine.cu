@@ -415,10 +415,11 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
     // Disney: (anisotropic, opacity, ior, -); others: (alpha x, alpha y, ior, fdrInt)
     mats[i].b = m.type == ASUNA_MAT_DISNEY ? make_float4(m.anisotropic, m.rho_spec[0], m.ior, 0.0f)
                                            : make_float4(m.aniso_alpha[0], m.aniso_alpha[1], m.ior, m.radiance[0]);
-    // Phong: specular reflectance and exponent (rhoSpec, specular); PBR:
+    // Phong, kang18: specular reflectance (rhoSpec) and Phong's exponent; PBR:
     // roughness, metalness, opacity (specular); Disney: metalness, roughness,
     // subsurface, specular tint; others: radiance
-    mats[i].c = m.type == ASUNA_MAT_PHONG ? make_float4(m.rho_spec[0], m.rho_spec[1], m.rho_spec[2], m.specular)
+    mats[i].c = (m.type == ASUNA_MAT_PHONG || m.type == ASUNA_MAT_KANG18)
+                    ? make_float4(m.rho_spec[0], m.rho_spec[1], m.rho_spec[2], m.specular)
                 : m.type == ASUNA_MAT_PBR_METALNESS_ROUGHNESS
                     ? make_float4(m.roughness, m.metalness, m.specular, 0.0f)
                 : m.type == ASUNA_MAT_DISNEY ? make_float4(m.metalness, m.roughness, m.subsurface, m.specular_tint)

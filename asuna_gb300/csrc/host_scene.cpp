@@ -65,20 +65,20 @@ int validateSceneDesc(const asuna_scene_desc* d) {
     if (t != ASUNA_MAT_LAMBERTIAN && t != ASUNA_MAT_ROUGH_PLASTIC && t != ASUNA_MAT_DIELECTRIC &&
         t != ASUNA_MAT_EMISSIVE && t != ASUNA_MAT_PLASTIC && t != ASUNA_MAT_MIRROR && t != ASUNA_MAT_CONDUCTOR &&
         t != ASUNA_MAT_ROUGH_CONDUCTOR && t != ASUNA_MAT_PHONG && t != ASUNA_MAT_PBR_METALNESS_ROUGHNESS &&
-        t != ASUNA_MAT_DISNEY)
+        t != ASUNA_MAT_DISNEY && t != ASUNA_MAT_KANG18)
       return fail(ASUNA_ERR_UNSUPPORTED, "material %u: type %u is not implemented", i, t);
     const asuna_material& m = d->materials[i];
     if (m.diffuse_texture_id >= 0 || m.normal_texture_id >= 0 || m.roughness_texture_id >= 0 ||
         (t == ASUNA_MAT_EMISSIVE && m.radiance_texture_id >= 0) ||
-        ((t == ASUNA_MAT_PBR_METALNESS_ROUGHNESS || t == ASUNA_MAT_DISNEY) &&
-         (m.metalness_texture_id >= 0 || m.opacity_texture_id >= 0)))
+        ((t == ASUNA_MAT_PBR_METALNESS_ROUGHNESS || t == ASUNA_MAT_DISNEY || t == ASUNA_MAT_KANG18) &&
+         (m.metalness_texture_id >= 0 || m.opacity_texture_id >= 0 || m.tangent_texture_id >= 0)))
       return fail(ASUNA_ERR_UNSUPPORTED, "material %u: textures are not implemented", i);
-    // brdf_pbr_metalness_roughness.rchit:152-160 and brdf_disney.rchit:409-417:
-    // an opacity above 0 (PBR: the specular field, which the JSON loader
-    // always sets to 0; Disney: rho_spec[0], JSON "opacity") lets rays pass
-    // through without counting a bounce
+    // brdf_pbr_metalness_roughness.rchit:152-160, brdf_disney.rchit:409-417,
+    // brdf_kang18.rchit:150-187: an opacity above 0 (PBR: the specular field
+    // and kang18: metalness, both always 0 from the JSON loader; Disney:
+    // rho_spec[0], JSON "opacity") lets rays pass through without a bounce
     if ((t == ASUNA_MAT_PBR_METALNESS_ROUGHNESS && m.specular != 0.0f) ||
-        (t == ASUNA_MAT_DISNEY && m.rho_spec[0] != 0.0f))
+        (t == ASUNA_MAT_DISNEY && m.rho_spec[0] != 0.0f) || (t == ASUNA_MAT_KANG18 && m.metalness != 0.0f))
       return fail(ASUNA_ERR_UNSUPPORTED, "material %u: opacity pass-through is not implemented", i);
   }
   for (uint32_t i = 0; i < d->num_instances; ++i) {
@@ -1039,6 +1039,32 @@ int addMaterial(LoadCtx& L, const Json& mj) {
     m.rho_spec[0] = 0.0f;
     if (mj.has("opacity")) m.rho_spec[0] = float(mj["opacity"].num);
     if ((rc = tex("opacity_texture", m.opacity_texture_id))) return rc;
+  } else if (t == "brdf_kang18") {
+    // src/loader/material.cpp:156-187: each of diffuse, specular and alpha
+    // comes from its texture or else its (required) value; specular in
+    // rho_spec, alpha in aniso_alpha, opacity (metalness) 0
+    m.type = ASUNA_MAT_KANG18;
+    if ((rc = tex("normal_texture", m.normal_texture_id)) || (rc = tex("tangent_texture", m.tangent_texture_id)))
+      return rc;
+    if (mj.has("diffuse_texture")) {
+      if ((rc = tex("diffuse_texture", m.diffuse_texture_id))) return rc;
+    } else {
+      REQUIRE(mj.has("diffuse_reflectance") && vecN(mj["diffuse_reflectance"], 3, m.diffuse),
+              "brdf_kang18 needs diffuse_reflectance or diffuse_texture");
+    }
+    if (mj.has("specular_texture")) {
+      if ((rc = tex("specular_texture", m.metalness_texture_id))) return rc;
+    } else {
+      REQUIRE(mj.has("specular_reflectance") && vecN(mj["specular_reflectance"], 3, m.rho_spec),
+              "brdf_kang18 needs specular_reflectance or specular_texture");
+    }
+    if (mj.has("alpha_texture")) {
+      if ((rc = tex("alpha_texture", m.roughness_texture_id))) return rc;
+    } else {
+      REQUIRE(mj.has("alpha") && vecN(mj["alpha"], 2, m.aniso_alpha), "brdf_kang18 needs alpha or alpha_texture");
+    }
+    m.metalness = 0.0f;
+    if ((rc = tex("opacity_texture", m.opacity_texture_id))) return rc;
   } else if (t == "brdf_emissive") {
     // src/loader/material.cpp:145-155
     m.type = ASUNA_MAT_EMISSIVE;
@@ -1046,9 +1072,6 @@ int addMaterial(LoadCtx& L, const Json& mj) {
     if (mj.has("radiance_factor")) REQUIRE(vecN(mj["radiance_factor"], 3, m.radiance_factor), "bad radiance_factor");
     if ((rc = tex("radiance_texture", m.radiance_texture_id))) return rc;
   } else {
-    static const char* known[] = {"brdf_kang18"};
-    for (const char* k : known)
-      if (t == k) return fail(ASUNA_ERR_UNSUPPORTED, "material type [%s] is not implemented", t.c_str());
     return fail(ASUNA_ERR_PARSE, "unrecognized material type [%s]", t.c_str());
   }
   L.S.materialNames.push_back(name);

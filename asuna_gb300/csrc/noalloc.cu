@@ -11,7 +11,7 @@
 // stream.
 //
 // The array holds kNoAllocMaxPaths path slots (ASUNA_NOALLOC_MAX_PATHS =
-// 262,144, 240 bytes each, about 60 MiB in all); every GPU that loads this
+// 262,144, 244 bytes each, about 61 MiB in all); every GPU that loads this
 // library keeps it until the process exits.  A frame of more pixels than
 // that is rejected with ASUNA_ERR_INVALID.
 //
@@ -41,8 +41,8 @@ constexpr uint64_t kNoAllocMaxPaths = ASUNA_NOALLOC_MAX_PATHS;
 constexpr uint64_t kNoAllocMaxRanges = 64;
 
 constexpr uint64_t pad256(uint64_t b) { return (b + 255) / 256 * 256; }
-// scratch layout: 21 per-path arrays (12 x 16 B, hit instances and the
-// shading-class lists 9 x 4 B), counters, shot, ranges
+// scratch layout: per-path arrays (12 x 16 B; 4 B each for the hit
+// instances and every shading-class list), counters, shot, ranges
 constexpr uint64_t kPerPath16 = pad256(kNoAllocMaxPaths * 16);
 constexpr uint64_t kPerPath4 = pad256(kNoAllocMaxPaths * 4);
 constexpr uint64_t kOffCounters = 12 * kPerPath16 + (1 + kNumShadeClasses) * kPerPath4;

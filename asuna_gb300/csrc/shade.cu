@@ -17,7 +17,7 @@
 //               brdf_mirror.rchit:12-106, brdf_conductor.rchit:14-164,
 //               brdf_rough_conductor.rchit, brdf_phong.rchit:12-194,
 //               brdf_pbr_metalness_roughness.rchit:12-219,
-//               brdf_disney.rchit:31-477
+//               brdf_disney.rchit:31-477, brdf_kang18.rchit:11-249
 //   accumulate  raytrace.projective.rgen:134-179
 //
 // Compiled with -fmad=false: the float arithmetic rounds operation by
@@ -272,6 +272,37 @@ __device__ __forceinline__ float pbrPdf(f3 L, f3 V, f3 N, f3 X, f3 Y, float a) {
   const f3 wh = makeNormal(toLocal(X, Y, N, H)), wo = makeNormal(toLocal(X, Y, N, V)),
            wi = makeNormal(toLocal(X, Y, N, L));
   return 0.2f * cosineHemispherePdf(wi.z) + (1.0f - 0.2f) * importanceAnisoGGXPdf(wh, wo, a, a);
+}
+
+// brdf_kang18.rchit:57-111: anisotropic GGX with scalar Schlick Fresnel over
+// a Lambertian base; lobe probability from the two luminances
+__device__ __forceinline__ f3 kangEval(f3 L, f3 V, f3 N, f3 X, f3 Y, f3 kd, f3 ks, float ax, float ay, float eta) {
+  const float NdotL = dot(N, L), NdotV = dot(N, V);
+  if (NdotL <= 0.0f || NdotV <= 0.0f) return splat(0.0f);
+  const f3 H = makeNormal(L + V);
+  const float HdotN = dot(H, N), HdotX = dot(H, X), HdotY = dot(H, Y), HdotV = dot(H, V);
+  const float F0 = sqr((eta - 1.0f) / (eta + 1.0f));
+  const float Fs = F0 + (1.0f - F0) * mpow(gclamp(1.0f - HdotV, 0.0f, 1.0f), 5.0f);
+  const float Ds = dAnisoGGX(HdotN, HdotX, HdotY, ax, ay);
+  float Gs = g1SmithAnisoGGX(NdotV, dot(V, X), dot(V, Y), ax, ay);
+  Gs = Gs * g1SmithAnisoGGX(NdotL, dot(L, X), dot(L, Y), ax, ay);
+  const f3 diffuse = kd * INV_PI;
+  const f3 specular = ks * Fs * Ds * Gs;
+  return (diffuse + specular) * NdotL;
+}
+__device__ __forceinline__ float kangDiffuseProb(f3 kd, f3 ks) {
+  const float pd = 0.212671f * kd.x + 0.715160f * kd.y + 0.072169f * kd.z;
+  const float ps = 0.212671f * ks.x + 0.715160f * ks.y + 0.072169f * ks.z;
+  return pd / (pd + ps + EPS);
+}
+__device__ __forceinline__ float kangPdf(f3 L, f3 V, f3 N, f3 X, f3 Y, float ax, float ay, f3 kd, f3 ks) {
+  const float NdotL = dot(N, L), NdotV = dot(N, V);
+  if (NdotL <= 0.0f || NdotV <= 0.0f) return 0.0f;
+  const f3 H = makeNormal(L + V);
+  const f3 wh = makeNormal(toLocal(X, Y, N, H)), wo = makeNormal(toLocal(X, Y, N, V)),
+           wi = makeNormal(toLocal(X, Y, N, L));
+  const float dp = kangDiffuseProb(kd, ks);
+  return dp * cosineHemispherePdf(wi.z) + (1.0f - dp) * importanceAnisoGGXPdf(wh, wo, ax, ay);
 }
 
 // ---- brdf_disney.rchit (float restatement; expressions in source order) ----
@@ -545,6 +576,12 @@ __device__ __forceinline__ void nextEvent(const SceneDev& S, const ShotDev& sh, 
       const float a = gmax(sqr(m.c.x), 0.001f);
       w = pbrEval(lRec.d, st.V, st.ffN, st.X, st.Y, ld3(m.a), a, m.c.y, m.b.z);
       if (lRec.flags & EArea) bpdf = pbrPdf(lRec.d, st.V, st.ffN, st.X, st.Y, a);
+    } else if (type == ASUNA_MAT_KANG18) {
+      // brdf_kang18.rchit:198-221 (eval ignores the flags, pdf does not)
+      const float ax = gmax(m.b.x, EPS), ay = gmax(m.b.y, EPS);
+      const f3 kd = ld3(m.a), ks = ld3(m.c);
+      w = kangEval(lRec.d, st.V, st.ffN, st.X, st.Y, kd, ks, ax, ay, m.b.z);
+      if (lRec.flags & EArea) bpdf = kangPdf(lRec.d, st.V, st.ffN, st.X, st.Y, ax, ay, kd, ks);
     } else if (type == ASUNA_MAT_DISNEY) {
       // brdf_disney.rchit:450-466: eval (and its pdf) with EArea for every light
       const disney::Mat dm = disney::fromDev(m);
@@ -763,6 +800,41 @@ __device__ __forceinline__ void samplePbr(PathIO& io, const HitSt& st, const Mat
   }
   const f3 bd = toWorld(X, Y, N, wi);
   const f3 weight = pbrEval(bd, V, N, X, Y, ld3(m.a), a, m.c.y, m.b.z) * fabsf(wi.z);
+  if (bpdf <= 0.0f || length(weight) == 0.0f) {
+    io.stop = true;
+    return;
+  }
+  io.bflags = bflags;
+  io.bpdf = bpdf;
+  io.nro = offsetPositionAlongNormal(st.pos, st.ffN);
+  io.nrd = bd;
+  io.thp = io.thp * (weight / (bpdf + EPS));
+}
+
+// brdf_kang18.rchit:113-135,223-249: direction pair, then the lobe choice;
+// the pdf is the chosen lobe's alone
+__device__ __forceinline__ void sampleKang18(PathIO& io, const HitSt& st, const MatDev& m) {
+  const float ax = gmax(m.b.x, EPS), ay = gmax(m.b.y, EPS);
+  const f3 kd = ld3(m.a), ks = ld3(m.c);
+  const f2 u = rnd2(io.seed);
+  const f3 V = st.V, N = st.ffN, X = st.X, Y = st.Y;
+  const f3 wo = makeNormal(toLocal(X, Y, N, V));
+  const float dp = kangDiffuseProb(kd, ks);
+  f3 wi;
+  float bpdf;
+  uint32_t bflags;
+  if (rnd(io.seed) < dp) {
+    wi = cosineSampleHemisphere(u);
+    bflags = EDiffuseReflection;
+    bpdf = cosineHemispherePdf(wi.z);
+  } else {
+    wi = importanceSampleAnisoGGX(u, wo, ax, ay);
+    const f3 wh = makeNormal(wi + wo);
+    bpdf = importanceAnisoGGXPdf(wh, wo, ax, ay);
+    bflags = EGlossyReflection;
+  }
+  const f3 bd = toWorld(X, Y, N, wi);
+  const f3 weight = kangEval(bd, V, N, X, Y, kd, ks, ax, ay, m.b.z);
   if (bpdf <= 0.0f || length(weight) == 0.0f) {
     io.stop = true;
     return;
@@ -1027,7 +1099,13 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
         const InstDev& in = S.inst[inst];
         const uint32_t prim = __float_as_uint(h4.w);
         rc.x = sigMix(rc.x, (inst << 20) ^ prim);
-        const HitSt st = hitState(S, in, prim, h4.y, h4.z, rd, sh.state.use_face_normal);
+        HitSt st = hitState(S, in, prim, h4.y, h4.z, rd, sh.state.use_face_normal);
+        if (CLS == kClsKang18) {
+          // brdf_kang18.rchit:178-181: the tangent frame is rebuilt from N and X
+          st.Y = makeNormal(cross(st.N, st.X));
+          st.X = makeNormal(cross(st.Y, st.N));
+          st.ffN = dot(st.N, st.V) > 0.0f ? st.N : -st.N;
+        }
         if (CLS == kClsTerminal && in.lightId >= 0) {
           // brdf_lambertian.rchit:44-68 (hitLight)
           const LightDev l = S.lights[in.lightId];
@@ -1049,8 +1127,8 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
           const MatDev m = S.mats[in.matId];
           // brdf_pbr_metalness_roughness.rchit:156: the opacity test's draw
           // comes first (pass-through, opacity > 0, is rejected at validation)
-          // brdf_disney.rchit:413 likewise (opacity in rho_spec[0])
-          if (CLS == kClsPbr || CLS == kClsDisney) rnd(io.seed);
+          // brdf_disney.rchit:413 and brdf_kang18.rchit:183 likewise
+          if (CLS == kClsPbr || CLS == kClsDisney || CLS == kClsKang18) rnd(io.seed);
           if (CLS == kClsPbr && depth == 1u && frame == 0u && sh.state.n_multi_channel > 0u) {
             // 169-174: albedo and the face-forward normal only
             const asuna_rt_state& ps = sh.state;
@@ -1060,10 +1138,11 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
             if (ps.normal_out_channel >= 0 && ps.normal_out_channel < ASUNA_MAX_CHANNELS)
               sh.filmCh[size_t(ps.normal_out_channel) * npx + pix] = make_float4(st.ffN.x, st.ffN.y, st.ffN.z, 1.0f);
           }
-          if ((CLS == kClsLambertian || CLS == kClsPhong) && depth == 1u && frame == 0u &&
+          if ((CLS == kClsLambertian || CLS == kClsPhong || CLS == kClsKang18) && depth == 1u && frame == 0u &&
               sh.state.n_multi_channel > 0u) {
-            // brdf_lambertian.rchit:93-108; brdf_phong.rchit:135-150 writes
-            // the face-forward normal and its specular reflectance
+            // brdf_lambertian.rchit:93-108; brdf_phong.rchit:135-150 and
+            // brdf_kang18.rchit:194-211 write the face-forward normal and the
+            // specular reflectance (kang18: the rebuilt tangent, (ax, ay, 0))
             const asuna_rt_state& ps = sh.state;
             float4* ch = sh.filmCh;
             const size_t npx = size_t(sh.width) * sh.height;
@@ -1071,10 +1150,11 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
               if (slot >= 0 && slot < ASUNA_MAX_CHANNELS) ch[size_t(slot) * npx + pix] = make_float4(v.x, v.y, v.z, 1.0f);
             };
             put(ps.diffuse_out_channel, ld3(m.a));
-            put(ps.normal_out_channel, CLS == kClsPhong ? st.ffN : st.N);
-            put(ps.specular_out_channel, CLS == kClsPhong ? ld3(m.c) : splat(0.0f));
+            put(ps.normal_out_channel, CLS == kClsLambertian ? st.N : st.ffN);
+            put(ps.specular_out_channel, CLS == kClsLambertian ? splat(0.0f) : ld3(m.c));
             put(ps.tangent_out_channel, st.X);
-            put(ps.roughness_out_channel, f3{1.0f, 1.0f, 0.0f});
+            put(ps.roughness_out_channel, CLS == kClsKang18 ? f3{gmax(m.b.x, EPS), gmax(m.b.y, EPS), 0.0f}
+                                                            : f3{1.0f, 1.0f, 0.0f});
             put(ps.position_out_channel, st.pos);
             put(ps.uv_out_channel, f3{st.u, st.v, 1.0f});
           }
@@ -1092,6 +1172,7 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
                                       : CLS == kClsPhong      ? ASUNA_MAT_PHONG
                                       : CLS == kClsPbr        ? ASUNA_MAT_PBR_METALNESS_ROUGHNESS
                                       : CLS == kClsDisney     ? ASUNA_MAT_DISNEY
+                                      : CLS == kClsKang18     ? ASUNA_MAT_KANG18
                                                               : ASUNA_MAT_LAMBERTIAN;
             nextEvent(S, sh, io, st, m, type, rd);
             if (CLS == kClsRoughPlastic)
@@ -1112,6 +1193,8 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
               samplePbr(io, st, m);
             else if (CLS == kClsDisney)
               sampleDisney(io, st, m);
+            else if (CLS == kClsKang18)
+              sampleKang18(io, st, m);
             else
               sampleLambertian(io, st, ld3(m.a));
           }
@@ -1230,6 +1313,7 @@ void launchShade(const KParams& P, int grid, cudaStream_t s) {
   if (m & (1u << kClsPhong)) k_shadeClass<kClsPhong><<<grid, 256, 0, s>>>(P);
   if (m & (1u << kClsPbr)) k_shadeClass<kClsPbr><<<grid, 256, 0, s>>>(P);
   if (m & (1u << kClsDisney)) k_shadeClass<kClsDisney><<<grid, 256, 0, s>>>(P);
+  if (m & (1u << kClsKang18)) k_shadeClass<kClsKang18><<<grid, 256, 0, s>>>(P);
 }
 int shadeLaunches(uint32_t classMask) { return 1 + __builtin_popcount(classMask | (1u << kClsTerminal)); }
 int shadeBlocksPerSm() {

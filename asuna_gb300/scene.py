@@ -186,6 +186,18 @@ class SceneBuilder:
         m.ior = float(ior)
         return self._add_material(name, m)
 
+    def add_kang18(self, name, diffuse, specular, alpha, ior=1.5):
+        """brdf_kang18 (src/loader/material.cpp:156-187): anisotropic GGX
+        (alpha = (ax, ay)) with Schlick Fresnel over a Lambertian base; the
+        shading frame is rebuilt from the normal and the tangent."""
+        m = default_material()
+        m.type = A.MAT_KANG18
+        m.diffuse = A.f3(*diffuse)
+        m.rho_spec = A.f3(*specular)
+        m.aniso_alpha = (C.c_float * 2)(*alpha)
+        m.ior = float(ior)
+        return self._add_material(name, m)
+
     def add_dielectric(self, name, ior=1.5):
         m = default_material()
         m.type = A.MAT_DIELECTRIC

@@ -229,8 +229,8 @@ def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=Fa
                  channels=("albedo", "normal", "depth", "position", "uv", "tangent", "roughness")):
     """Every implemented plugin in one small scene: Lambertian, anisotropic
     rough plastic, dielectric, smooth plastic, mirror, conductor, rough
-    conductor, Phong, PBR metalness-roughness and Disney (every lobe on)
-    spheres and an emissive cuboid on a ground quad; a single-sided rect
+    conductor, Phong, PBR metalness-roughness, Disney (every lobe on) and
+    kang18 spheres and an emissive cuboid on a ground quad; a single-sided rect
     light, a double-sided JSON "triangle" light (rect with half area), a mesh
     triangle light, a point light and a distant light; an optional lognormal
     environment map (else a background colour); a thin-lens perspective or an
@@ -258,6 +258,7 @@ def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=Fa
     pb = b.add_pbr("pbr_metal", (0.9, 0.6, 0.3), metalness=0.7, roughness=0.35)
     dn = b.add_disney("disney", (0.25, 0.45, 0.85), metallic=0.3, roughness=0.4, subsurface=0.5, specular_tint=0.3,
                       sheen=0.6, sheen_tint=0.5, clearcoat=0.8, clearcoat_gloss=0.7, anisotropic=0.5)
+    kg = b.add_kang18("kang18", (0.5, 0.3, 0.3), (0.4, 0.4, 0.5), (0.1, 0.3))
     v, i = cuboid_mesh(0.15, 0.15, 0.15)
     b.add_mesh("lamp", v, i)
     b.add_instance("lamp", em, rot_y(30.0, (0.6, -0.85, 1.2)))
@@ -271,7 +272,7 @@ def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=Fa
     spheres = [(lam, (-1.3, -0.2, 0.0), 0.8), (rp, (0.0, -0.1, -0.6), 0.8), (di, (1.2, -0.2, 0.3), 0.8),
                (sp, (-0.4, -0.6, 1.1), 0.4), (mi, (0.75, -0.62, 1.3), 0.38), (au, (-1.6, -0.65, 1.4), 0.35),
                (al, (1.75, -0.6, 1.2), 0.4), (ph, (0.2, -0.7, 2.0), 0.3), (pb, (-0.9, -0.72, 2.1), 0.28),
-               (dn, (1.0, -0.7, 2.2), 0.3)]
+               (dn, (1.0, -0.7, 2.2), 0.3), (kg, (-0.3, -0.75, 2.6), 0.25)]
     for k, (mat, pos, s) in enumerate(spheres):
         b.add_mesh(f"s{k}", displaced_sphere(base_v, faces, seed + k, amplitude=0.05), idx)
         b.add_instance(f"s{k}", mat, np.array([[s, 0, 0, pos[0]], [0, s, 0, pos[1]], [0, 0, s, pos[2]]], np.float32))

@@ -542,7 +542,7 @@ def run_batch(args):
 
 C_SHOT_BYTES = 340  # sizeof(asuna_shot): the only host->device input of a step
 NODE_BYTES = 64  # one binary BVH node
-BYTES_PER_PATH = 240  # wavefront state per path slot (asuna_gb300/csrc/engine.cu)
+BYTES_PER_PATH = 244  # wavefront state per path slot (asuna_gb300/csrc/engine.cu)
 
 
 def main():

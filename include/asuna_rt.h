@@ -70,7 +70,7 @@ enum {
  * implemented; others are rejected with ASUNA_ERR_UNSUPPORTED) */
 enum {
   ASUNA_MAT_LAMBERTIAN = 0, /* (*) brdf_lambertian   */
-  ASUNA_MAT_KANG18 = 1,
+  ASUNA_MAT_KANG18 = 1, /* (*) brdf_kang18        */
   ASUNA_MAT_EMISSIVE = 2, /* (*) brdf_emissive      */
   ASUNA_MAT_PBR_METALNESS_ROUGHNESS = 3, /* (*) brdf_pbr_metalness_roughness */
   ASUNA_MAT_PLASTIC = 4, /* (*) brdf_plastic       */
@@ -374,7 +374,7 @@ int asuna_scene_trace(asuna_ctx* ctx, const asuna_scene* scene, const float* ray
  * the allocator): renders shot->frames frames of one shot into `film` like
  * asuna_render, on `stream` (a cudaStream_t; NULL = default stream), with
  * all scratch in one fixed device array compiled into the library.  The
- * array holds ASUNA_NOALLOC_MAX_PATHS path slots (about 60 MiB, kept by
+ * array holds ASUNA_NOALLOC_MAX_PATHS path slots (about 61 MiB, kept by
  * every GPU that loads the library until exit); a frame with more pixels is
  * rejected with ASUNA_ERR_INVALID.  The array's address is set up on a
  * device by the first call there: make that call before any stream capture.

@@ -1732,6 +1732,115 @@ template <class R> void shadeDisney(const Scene& s, const asuna_shot& sh, PathSt
   p.throughput = p.throughput * (weight / pdf);
 }
 
+// ---- brdf_kang18.rchit ------------------------------------------------------
+// 57-86 (flags unused): anisotropic GGX with Schlick Fresnel plus Lambertian
+template <class R>
+V3<R> kangEval(V3<R> L, V3<R> V, V3<R> N, V3<R> X, V3<R> Y, V3<R> kd, V3<R> ks, R ax, R ay, R eta) {
+  V3<R> weight = splat(R(0));
+  R NdotL = dot(N, L), NdotV = dot(N, V);
+  if (NdotL <= R(0) || NdotV <= R(0)) return weight;
+  V3<R> H = makeNormal(L + V);
+  R HdotN = dot(H, N), HdotX = dot(H, X), HdotY = dot(H, Y), HdotV = dot(H, V);
+  R F0 = sqr((eta - R(1)) / (eta + R(1)));
+  R Fs = F0 + (R(1) - F0) * mpow(gclamp(R(1) - HdotV, R(0), R(1)), R(5));
+  R Ds = dAnisoGGX(HdotN, HdotX, HdotY, ax, ay);
+  R Gs = g1SmithAnisoGGX(NdotV, dot(V, X), dot(V, Y), ax, ay);
+  Gs = Gs * g1SmithAnisoGGX(NdotL, dot(L, X), dot(L, Y), ax, ay);
+  V3<R> diffuse = kd * K<R>::INV_PI;
+  V3<R> specular = ks * Fs * Ds * Gs;
+  weight = weight + diffuse;
+  weight = weight + specular;
+  weight = weight * NdotL;
+  return weight;
+}
+// 88-111: lobe probability pd / (pd + ps + EPS) from the two luminances
+template <class R> R kangDiffuseProb(V3<R> kd, V3<R> ks) {
+  R pd = dLuminance(kd), ps = dLuminance(ks);
+  return pd / (pd + ps + K<R>::EPS);
+}
+template <class R>
+R kangPdf(V3<R> L, V3<R> V, V3<R> N, V3<R> X, V3<R> Y, R ax, R ay, V3<R> kd, V3<R> ks, uint32_t flags) {
+  R pdf = R(0);
+  if ((flags & EArea) == 0) return pdf;
+  R NdotL = dot(N, L), NdotV = dot(N, V);
+  if (NdotL <= R(0) || NdotV <= R(0)) return pdf;
+  V3<R> H = makeNormal(L + V);
+  V3<R> wh = makeNormal(toLocal(X, Y, N, H)), wo = makeNormal(toLocal(X, Y, N, V)),
+        wi = makeNormal(toLocal(X, Y, N, L));
+  R dp = kangDiffuseProb(kd, ks);
+  pdf = pdf + dp * cosineHemispherePdf(wi.z);
+  pdf = pdf + (R(1) - dp) * importanceAnisoGGXPdf(wh, wo, ax, ay);
+  return pdf;
+}
+
+// brdf_kang18.rchit:137-249 (main) with sampleBsdf 113-135.  The tangent
+// frame is rebuilt from N and X before anything else (178-181); random
+// numbers: the opacity test, the light sample, the direction pair, the lobe
+// choice; the sampled pdf is that of the chosen lobe.
+template <class R> void shadeKang18(const Scene& s, const asuna_shot& sh, PathState<R>& p, HitState<R>& st) {
+  const asuna_rt_state& ps = sh.state;
+  V3<R> kd = L3<R>(st.mat.diffuse), ks = L3<R>(st.mat.rho_spec);
+  R opacity = R(st.mat.metalness);
+  st.Y = makeNormal(cross(st.N, st.X));
+  st.X = makeNormal(cross(st.Y, st.N));
+  st.ffN = dot(st.N, st.V) > R(0) ? st.N : -st.N;
+  // 183-187: pass-through (opacity > 0) is rejected at scene validation
+  (void)(rnd<R>(p.seed) < opacity);
+  R ax = gmax(R(st.mat.aniso_alpha[0]), K<R>::EPS), ay = gmax(R(st.mat.aniso_alpha[1]), K<R>::EPS);
+  R eta = R(st.mat.ior);
+  if (p.depth == 1) {
+    if (ps.diffuse_out_channel >= 0) p.ch[ps.diffuse_out_channel] = kd;
+    if (ps.normal_out_channel >= 0) p.ch[ps.normal_out_channel] = st.ffN;
+    if (ps.specular_out_channel >= 0) p.ch[ps.specular_out_channel] = ks;
+    if (ps.tangent_out_channel >= 0) p.ch[ps.tangent_out_channel] = st.X;
+    if (ps.roughness_out_channel >= 0) p.ch[ps.roughness_out_channel] = V3<R>{ax, ay, R(0)};
+    if (ps.position_out_channel >= 0) p.ch[ps.position_out_channel] = st.pos;
+    if (ps.uv_out_channel >= 0) p.ch[ps.uv_out_channel] = V3<R>{st.uv.x, st.uv.y, R(1)};
+  }
+  {
+    bool visible;
+    LRec<R> lRec;
+    V3<R> Ld = splat(R(0));
+    V3<R> rad = sampleLights<R>(s, sh, p, st.pos, st.ffN, visible, lRec);
+    if (visible) {
+      V3<R> w = kangEval<R>(lRec.d, st.V, st.ffN, st.X, st.Y, kd, ks, ax, ay, eta);
+      R bpdf = kangPdf<R>(lRec.d, st.V, st.ffN, st.X, st.Y, ax, ay, kd, ks, lRec.flags);
+      R mis = powerHeuristic(lRec.pdf, bpdf);
+      Ld = mis * w * rad * p.throughput / (lRec.pdf + K<R>::EPS);
+    }
+    p.drad = Ld;
+    p.dskip = !visible;
+  }
+  V2<R> u = rnd2<R>(p.seed);
+  V3<R> V = st.V, N = st.ffN, X = st.X, Y = st.Y;
+  V3<R> wo = makeNormal(toLocal(X, Y, N, V));
+  R dp = kangDiffuseProb(kd, ks);
+  V3<R> wi;
+  R bpdf = R(0);
+  uint32_t bflags;
+  if (rnd<R>(p.seed) < dp) {
+    wi = cosineSampleHemisphere(u);
+    bflags = EDiffuseReflection;
+    bpdf = cosineHemispherePdf(wi.z);
+  } else {
+    wi = importanceSampleAnisoGGX(u, wo, ax, ay);
+    V3<R> wh = makeNormal(wi + wo);
+    bpdf = importanceAnisoGGXPdf(wh, wo, ax, ay);
+    bflags = EGlossyReflection;
+  }
+  V3<R> bd = toWorld(X, Y, N, wi);
+  V3<R> weight = kangEval<R>(bd, V, N, X, Y, kd, ks, ax, ay, eta);
+  if (bpdf <= R(0) || length(weight) == R(0)) {
+    p.stop = true;
+    return;
+  }
+  p.bflags = bflags;
+  p.bpdf = bpdf;
+  p.ro = offsetPositionAlongNormal(st.pos, st.ffN);
+  p.rd = bd;
+  p.throughput = p.throughput * (weight / (bpdf + K<R>::EPS));
+}
+
 // brdf_conductor.rchit:14-36 (P. Shirley's conductor Fresnel)
 template <class R> R conductorReflectance(R eta, R k, R cosThetaI) {
   R cosThetaISq = cosThetaI * cosThetaI;
@@ -1964,6 +2073,8 @@ void tracePath(const Scene& s, const asuna_shot& sh, uint32_t x, uint32_t y, uin
           shadePbr<R>(s, sh, p, hs);
         else if (type == ASUNA_MAT_DISNEY)
           shadeDisney<R>(s, sh, p, hs);
+        else if (type == ASUNA_MAT_KANG18)
+          shadeKang18<R>(s, sh, p, hs);
         else
           shadeLambertian<R>(s, sh, p, hs);
         p.sig = sigMix(p.sig, p.stop ? 0xfffu : p.bflags);

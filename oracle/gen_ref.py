@@ -52,6 +52,7 @@ SHADERS = {
     "bxdf/raytrace.brdf_phong.rchit": "stage_phong",
     "bxdf/raytrace.brdf_pbr_metalness_roughness.rchit": "stage_pbr",
     "bxdf/raytrace.brdf_disney.rchit": "stage_disney",
+    "bxdf/raytrace.brdf_kang18.rchit": "stage_kang18",
 }
 
 FLOAT_LIT = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")

@@ -97,6 +97,7 @@ static thread_local RayPayload payload;
 #include "raytrace.brdf_phong.rchit.h"
 #include "raytrace.brdf_pbr_metalness_roughness.rchit.h"
 #include "raytrace.brdf_disney.rchit.h"
+#include "raytrace.brdf_kang18.rchit.h"
 }  // namespace glslx
 
 namespace {
@@ -187,6 +188,9 @@ void traceRayEXT(accelerationStructureEXT, uint, uint, uint, uint, uint, vec3 or
       break;
     case MaterialTypeBrdfDisney:
       stage_disney::main();
+      break;
+    case MaterialTypeBrdfKang18:
+      stage_kang18::main();
       break;
     default:
       stage_lambertian::main();

@@ -255,7 +255,9 @@ def test_json_scene_renders_like_builder_on_oracle(tmp_path):
     ('{"state": {}, "camera": {"type": "fisheye", "film": {"resolution": [8, 8]}}, "meshes": [], "instances": []}',
      A.ERR_PARSE),
     ('{"state": {}, "camera": {"type": "perspective", "film": {"resolution": [8, 8]}}, "meshes": [], '
-     '"instances": [], "materials": [{"type": "brdf_kang18", "name": "d"}]}', A.ERR_UNSUPPORTED),
+     '"instances": [], "materials": [{"type": "brdf_kang18", "name": "d"}]}', A.ERR_PARSE),
+    ('{"state": {}, "camera": {"type": "perspective", "film": {"resolution": [8, 8]}}, "meshes": [], '
+     '"instances": [], "materials": [{"type": "brdf_velvet", "name": "d"}]}', A.ERR_PARSE),
     ('{"state": {}, "camera": {"type": "perspective", "film": {"resolution": [8, 8]}}, '
      '"meshes": [{"name": "m", "path": "missing.obj"}], "instances": []}', A.ERR_IO),
     ('{"state": {"path_tracing": {"multi_channel": ["a","b","c","d","e","f","g","h"]}}, '
@@ -365,10 +367,11 @@ def test_hdr_envmap_reader(tmp_path):
 
 def test_json_material_plugins_match_builder():
     """brdf_plastic, brdf_mirror, brdf_conductor, brdf_rough_conductor,
-    brdf_phong, brdf_pbr_metalness_roughness and brdf_disney parse into the
-    same device structs as the builder (src/loader/material.cpp:116-143,
-    197-210, 233-243, 306-347, 359-405); an unknown metal is a parse error;
-    PBR and Disney opacity (pass-through) is rejected as unsupported."""
+    brdf_phong, brdf_pbr_metalness_roughness, brdf_disney and brdf_kang18
+    parse into the same device structs as the builder
+    (src/loader/material.cpp:116-143, 156-187, 197-210, 233-243, 306-347,
+    359-405); an unknown metal is a parse error; PBR and Disney opacity
+    (pass-through) is rejected as unsupported."""
     base = {"state": {}, "camera": {"type": "perspective", "film": {"resolution": [8, 8]}}, "meshes": [],
             "instances": []}
     mats = [{"type": "brdf_plastic", "name": "p", "diffuse_reflectance": [0.7, 0.65, 0.1], "ior": 1.6},
@@ -382,7 +385,9 @@ def test_json_material_plugins_match_builder():
             {"type": "brdf_pbr_metalness_roughness", "name": "pb", "diffuse_reflectance": [0.9, 0.6, 0.3],
              "metalness": 0.7, "roughness": 0.35},
             {"type": "brdf_disney", "name": "dn", "diffuse_reflectance": [0.25, 0.45, 0.85], "metallic": 0.3,
-             "roughness": 0.4}]
+             "roughness": 0.4},
+            {"type": "brdf_kang18", "name": "kg", "diffuse_reflectance": [0.5, 0.3, 0.3],
+             "specular_reflectance": [0.4, 0.4, 0.5], "alpha": [0.1, 0.3]}]
     js = ag.JsonScene(text=json.dumps({**base, "materials": mats}), base_dir=".")
     d = js.desc().desc
     b = ag.SceneBuilder()
@@ -394,6 +399,7 @@ def test_json_material_plugins_match_builder():
     b.add_phong("ph", (0.3, 0.5, 0.2), (0.5, 0.5, 0.45), 40.0)
     b.add_pbr("pb", (0.9, 0.6, 0.3), metalness=0.7, roughness=0.35)
     b.add_disney("dn", (0.25, 0.45, 0.85), metallic=0.3, roughness=0.4)
+    b.add_kang18("kg", (0.5, 0.3, 0.3), (0.4, 0.4, 0.5), (0.1, 0.3))
     assert d.num_materials == len(b.materials)
     for k in range(1, d.num_materials):
         assert bytes(d.materials[k]) == bytes(b.materials[k]), k
