@@ -84,11 +84,15 @@ class EnvmapDesc(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("rgba", C.c_void_p)]
 
 
+class TextureDesc(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("rgba", C.c_void_p)]
+
+
 class SceneDesc(C.Structure):
     _fields_ = [("num_meshes", C.c_uint32), ("meshes", C.POINTER(MeshDesc)), ("num_instances", C.c_uint32),
                 ("instances", C.POINTER(InstanceDesc)), ("num_materials", C.c_uint32),
                 ("materials", C.POINTER(Material)), ("num_lights", C.c_uint32), ("lights", C.POINTER(Light)),
-                ("envmap", EnvmapDesc)]
+                ("envmap", EnvmapDesc), ("num_textures", C.c_uint32), ("textures", C.POINTER(TextureDesc))]
 
 
 class Shot(C.Structure):
@@ -119,7 +123,11 @@ TONEMAP_NONE, TONEMAP_GAMMA, TONEMAP_REINHARD, TONEMAP_ACES, TONEMAP_FILMIC, TON
 
 class DenoiserOpts(C.Structure):
     _fields_ = [("levels", C.c_uint32), ("channels", C.c_uint32 * 6), ("seed", C.c_uint64),
-                ("max_pixels", C.c_uint64), ("training", C.c_uint32), ("tensor_memory", C.c_uint32)]
+                ("max_pixels", C.c_uint64), ("training", C.c_uint32), ("tensor_memory", C.c_uint32),
+                ("loss", C.c_uint32)]
+
+
+DENOISER_LOSS_L1_LOG, DENOISER_LOSS_RELMSE = 0, 1
 
 
 class SceneStats(C.Structure):

@@ -431,6 +431,41 @@ __global__ void k_l1_loss(const float* head, int C, const float4* rad, const flo
   if ((threadIdx.x & 31) == 0) atomicAdd(loss, s);
 }
 
+// Relative squared error on radiance with the denominator held fixed (the
+// "relMSE" of Lehtinen et al., Noise2Noise, ICML 2018, section 3.4):
+// L = mean (o - t)^2 / (sg(o) + 0.01)^2, o = max(expm1(head + log1p(r)), 0).
+// Its minimiser is the target's mean, so noisy targets add no bias (an L1
+// loss converges to the median, which sits below the mean of right-skewed
+// radiance noise).  dL/dhead = 2 (o - t) (o + 1) / (o + 0.01)^2 where o > 0.
+__global__ void k_relmse_loss(const float* head, int C, const float4* rad, const float4* target,
+                              __nv_bfloat16* grad, int n, int h, int w, int hp, int wp, float invCount, float* loss) {
+  const size_t P = size_t(n) * hp * wp;
+  float s = 0.0f;
+  for (size_t q = blockIdx.x * size_t(blockDim.x) + threadIdx.x; q < P; q += size_t(gridDim.x) * blockDim.x) {
+    const int x = int(q % wp), y = int((q / wp) % hp), b = int(q / (size_t(wp) * hp));
+    float g[3] = {0.0f, 0.0f, 0.0f};
+    if (y < h && x < w) {
+      const size_t p = (size_t(b) * h + y) * w + x;
+      const float4 r = rad[p], t = target[p];
+      const float rr[3] = {r.x, r.y, r.z}, tt[3] = {t.x, t.y, t.z};
+      for (int c = 0; c < 3; ++c) {
+        const float e = expm1f(head[q * C + c] + log1pf(fmaxf(rr[c], 0.0f)));
+        const float o = fmaxf(e, 0.0f);
+        const float den = 1.0f / ((o + 0.01f) * (o + 0.01f));
+        const float d = o - fmaxf(tt[c], 0.0f);
+        s += d * d * den;
+        g[c] = e > 0.0f ? 2.0f * d * (e + 1.0f) * den * invCount : 0.0f;
+      }
+    }
+    __nv_bfloat162* o = reinterpret_cast<__nv_bfloat162*>(grad + q * C);
+    o[0] = __floats2bfloat162_rn(g[0], g[1]);
+    o[1] = __floats2bfloat162_rn(g[2], 0.0f);
+    for (int c = 4; c < C; c += 2) o[c / 2] = __floats2bfloat162_rn(0.0f, 0.0f);
+  }
+  for (int off = 16; off; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, s);
+}
+
 // radiance = max(expm1(head + log1p(rad)), 0), alpha 1
 __global__ void k_output(const float* head, int C, const float4* rad, float4* out, int n, int h, int w, int hp,
                          int wp) {
@@ -636,6 +671,7 @@ struct asuna_denoiser {
   int L = 0;
   int ch[ASUNA_DENOISER_MAX_LEVELS] = {};
   bool training = false;
+  uint32_t loss = ASUNA_DENOISER_LOSS_L1_LOG;
   uint64_t maxPixels = 0;
   std::vector<ConvLayer> layers;
   size_t nParams = 0, nFlip = 0;
@@ -831,6 +867,8 @@ int asuna_denoiser_create(asuna_ctx* ctx, const asuna_denoiser_opts* o, asuna_de
                   o->channels[l]);
   if (o->max_pixels == 0 || o->max_pixels > (1ull << 31))
     return fail(ASUNA_ERR_INVALID, "denoiser: max_pixels %llu out of range", (unsigned long long)o->max_pixels);
+  if (o->loss != ASUNA_DENOISER_LOSS_L1_LOG && o->loss != ASUNA_DENOISER_LOSS_RELMSE)
+    return fail(ASUNA_ERR_INVALID, "denoiser: unknown loss %u", o->loss);
   ASUNA_CUDA_TRY(cudaSetDevice(ctx->device));
   asuna_denoiser* d = new (std::nothrow) asuna_denoiser;
   if (!d) return fail(ASUNA_ERR_OOM, "host allocation failed");
@@ -840,6 +878,7 @@ int asuna_denoiser_create(asuna_ctx* ctx, const asuna_denoiser_opts* o, asuna_de
   for (int l = 0; l < L; ++l) d->ch[l] = int(o->channels[l]);
   d->training = o->training != 0;
   d->useTc = o->tensor_memory != 0;
+  d->loss = o->loss;
   d->maxPixels = o->max_pixels;
   // layers in parameter order
   auto add = [&](int cin, int cout) {
@@ -1006,9 +1045,15 @@ int asuna_denoiser_loss_grad(asuna_denoiser* d, const float* radiance, const flo
   ASUNA_CUDA_TRY(cudaMemsetAsync(d->dLoss, 0, sizeof(float), s));
   NN_TRY(forward(d, radiance, albedo, normal, weight, D));
   const size_t P0 = size_t(D.n) * D.hp * D.wp;
-  k_l1_loss<<<grid1d(P0), 256, 0, s>>>(d->head, kHeadC, reinterpret_cast<const float4*>(radiance),
-                                       reinterpret_cast<const float4*>(target), d->gHead, D.n, D.h, D.w, D.hp, D.wp,
-                                       float(1.0 / (3.0 * double(n) * h * w)), d->dLoss);
+  const float invCount = float(1.0 / (3.0 * double(n) * h * w));
+  if (d->loss == ASUNA_DENOISER_LOSS_RELMSE)
+    k_relmse_loss<<<grid1d(P0), 256, 0, s>>>(d->head, kHeadC, reinterpret_cast<const float4*>(radiance),
+                                             reinterpret_cast<const float4*>(target), d->gHead, D.n, D.h, D.w, D.hp,
+                                             D.wp, invCount, d->dLoss);
+  else
+    k_l1_loss<<<grid1d(P0), 256, 0, s>>>(d->head, kHeadC, reinterpret_cast<const float4*>(radiance),
+                                         reinterpret_cast<const float4*>(target), d->gHead, D.n, D.h, D.w, D.hp, D.wp,
+                                         invCount, d->dLoss);
   ASUNA_CUDA_TRY(cudaGetLastError());
   NN_TRY(backward(d, D));
   float l = 0.0f;

@@ -59,15 +59,20 @@ struct __align__(16) InstDev {
 };
 static_assert(sizeof(InstDev) == 128, "InstDev is 128 bytes");
 
-// Packed material, 64 B: (diffuse.xyz, type bits), (alpha.x, alpha.y, ior,
+// Packed material, 96 B: (diffuse.xyz, type bits), (alpha.x, alpha.y, ior,
 // fdrInt), (radiance.xyz, 0), (radiance_factor.xyz, 0); an emissive material
 // holds its radiance in place of the diffuse albedo; conductors keep eta in
-// radiance and k in radiance_factor, as the reference's loader does.
+// radiance and k in radiance_factor, as the reference's loader does (other
+// types pack their own fields into b, c, d: see the upload).  Texture ids
+// (-1 = none): t0 = (diffuse, normal, roughness, metalness), t1 = (radiance,
+// tangent, opacity, -).
 struct __align__(16) MatDev {
   float4 a;
   float4 b;
   float4 c;
   float4 d;
+  int4 t0;
+  int4 t1;
 };
 
 // Packed light, 80 B: (position, type bits), (direction, radius),
@@ -92,6 +97,8 @@ struct SceneDev {
   const float4* env;    // W*H rgba
   const float2* marg;   // W*H (.x inverse CDF, .y pdf)
   const float2* cond;   // W*H
+  const float4* texels;  // every material texture, one after another
+  const int4* texInfo;   // per texture: (first texel, width, height, 0)
   int32_t tlasRoot;
   int32_t envW, envH;
   int32_t numInst;

@@ -425,6 +425,8 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
                 : m.type == ASUNA_MAT_DISNEY ? make_float4(m.metalness, m.roughness, m.subsurface, m.specular_tint)
                                              : make_float4(m.radiance[0], m.radiance[1], m.radiance[2], 0.0f);
     // Disney: sheen, sheen tint, clearcoat, clearcoat gloss; others: radiance factor
+    mats[i].t0 = make_int4(m.diffuse_texture_id, m.normal_texture_id, m.roughness_texture_id, m.metalness_texture_id);
+    mats[i].t1 = make_int4(m.radiance_texture_id, m.tangent_texture_id, m.opacity_texture_id, -1);
     mats[i].d = m.type == ASUNA_MAT_DISNEY
                     ? make_float4(m.sheen, m.sheen_tint, m.clearcoat, m.clearcoat_gloss)
                     : make_float4(m.radiance_factor[0], m.radiance_factor[1], m.radiance_factor[2], 0.0f);
@@ -442,6 +444,21 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
     lights[i].v = make_float4(l.v[0], l.v[1], l.v[2], db);
   }
   uint32_t ew = 1, eh = 1;
+  // material textures: one texel pool and a (first, w, h) table
+  std::vector<int4> texInfo(std::max(1u, d->num_textures), make_int4(0, 1, 1, 0));
+  uint64_t nTexels = 0;
+  for (uint32_t i = 0; i < d->num_textures; ++i) nTexels += uint64_t(d->textures[i].width) * d->textures[i].height;
+  std::vector<float4> texels(std::max<uint64_t>(nTexels, 1), make_float4(0, 0, 0, 0));
+  {
+    uint64_t off = 0;
+    for (uint32_t i = 0; i < d->num_textures; ++i) {
+      const asuna_texture_desc& t = d->textures[i];
+      const uint64_t n = uint64_t(t.width) * t.height;
+      texInfo[i] = make_int4(int32_t(uint32_t(off)), int32_t(t.width), int32_t(t.height), 0);
+      std::memcpy(&texels[off], t.rgba, n * sizeof(float4));
+      off += n;
+    }
+  }
   std::vector<float4> env(1, make_float4(0, 0, 0, 0));
   std::vector<float2> marg(1, make_float2(0, 0)), cond(1, make_float2(0, 0));
   if (d->envmap.rgba && d->envmap.width && d->envmap.height) {
@@ -462,7 +479,9 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
       (rc = devUpload(s, mats.data(), mats.size(), &v.mats)) ||
       (rc = devUpload(s, lights.data(), lights.size(), &v.lights)) ||
       (rc = devUpload(s, env.data(), env.size(), &v.env)) || (rc = devUpload(s, marg.data(), marg.size(), &v.marg)) ||
-      (rc = devUpload(s, cond.data(), cond.size(), &v.cond)))
+      (rc = devUpload(s, cond.data(), cond.size(), &v.cond)) ||
+      (rc = devUpload(s, texels.data(), texels.size(), &v.texels)) ||
+      (rc = devUpload(s, texInfo.data(), texInfo.size(), &v.texInfo)))
     return rc;
   v.tlasRoot = int32_t(tlasBase);
   v.envW = int32_t(ew);

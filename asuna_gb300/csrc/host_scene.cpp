@@ -68,11 +68,16 @@ int validateSceneDesc(const asuna_scene_desc* d) {
         t != ASUNA_MAT_DISNEY && t != ASUNA_MAT_KANG18)
       return fail(ASUNA_ERR_UNSUPPORTED, "material %u: type %u is not implemented", i, t);
     const asuna_material& m = d->materials[i];
-    if (m.diffuse_texture_id >= 0 || m.normal_texture_id >= 0 || m.roughness_texture_id >= 0 ||
-        (t == ASUNA_MAT_EMISSIVE && m.radiance_texture_id >= 0) ||
-        ((t == ASUNA_MAT_PBR_METALNESS_ROUGHNESS || t == ASUNA_MAT_DISNEY || t == ASUNA_MAT_KANG18) &&
-         (m.metalness_texture_id >= 0 || m.opacity_texture_id >= 0 || m.tangent_texture_id >= 0)))
-      return fail(ASUNA_ERR_UNSUPPORTED, "material %u: textures are not implemented", i);
+    const int32_t ids[7] = {m.diffuse_texture_id,  m.roughness_texture_id, m.metalness_texture_id,
+                            m.radiance_texture_id, m.normal_texture_id,    m.tangent_texture_id,
+                            m.opacity_texture_id};
+    for (int32_t id : ids)
+      if (id >= int32_t(d->num_textures))
+        return fail(ASUNA_ERR_INVALID, "material %u: texture %d out of range (%u textures)", i, id, d->num_textures);
+    // an opacity texture drives the pass-through below, per texel
+    if ((t == ASUNA_MAT_PBR_METALNESS_ROUGHNESS || t == ASUNA_MAT_DISNEY || t == ASUNA_MAT_KANG18) &&
+        m.opacity_texture_id >= 0)
+      return fail(ASUNA_ERR_UNSUPPORTED, "material %u: opacity textures (pass-through) are not implemented", i);
     // brdf_pbr_metalness_roughness.rchit:152-160, brdf_disney.rchit:409-417,
     // brdf_kang18.rchit:150-187: an opacity above 0 (PBR: the specular field
     // and kang18: metalness, both always 0 from the JSON loader; Disney:
@@ -96,6 +101,16 @@ int validateSceneDesc(const asuna_scene_desc* d) {
       return fail(ASUNA_ERR_UNSUPPORTED, "light %u: type %d", i, d->lights[i].type);
   if (d->envmap.rgba && (!d->envmap.width || !d->envmap.height))
     return fail(ASUNA_ERR_INVALID, "envmap has zero size");
+  if (d->num_textures && !d->textures) return fail(ASUNA_ERR_INVALID, "textures is NULL");
+  uint64_t texels = 0;
+  for (uint32_t i = 0; i < d->num_textures; ++i) {
+    const asuna_texture_desc& t = d->textures[i];
+    if (!t.rgba || !t.width || !t.height || t.width > 65536 || t.height > 65536)
+      return fail(ASUNA_ERR_INVALID, "texture %u: bad size %u x %u or no texels", i, t.width, t.height);
+    texels += uint64_t(t.width) * t.height;
+  }
+  if (texels >= (1ull << 32)) return fail(ASUNA_ERR_INVALID, "textures hold %llu texels (limit 2^32)",
+                                          (unsigned long long)texels);
   return ASUNA_OK;
 }
 
@@ -255,7 +270,10 @@ static asuna_material defaultMaterial() {
 
 void HostScene::reset() {
   *this = HostScene();
+  // src/scene/scene.cpp:87-130: a 1 x 1 dummy texture (its texels are left
+  // unset there; zero here)
   textureNames.push_back("add_by_default_dummy_texture");
+  textures.push_back(Texture{1, 1, std::vector<float>(4, 0.0f)});
   materialNames.push_back("add_by_default_dummy_material");
   materials.push_back(defaultMaterial());
   asuna_light d;
@@ -395,6 +413,9 @@ void HostScene::submit() {
     meshDescs[i].vertices = meshes[i].v.data();
     meshDescs[i].indices = meshes[i].idx.data();
   }
+  texDescs.resize(textures.size());
+  for (size_t i = 0; i < textures.size(); ++i)
+    texDescs[i] = asuna_texture_desc{textures[i].w, textures[i].h, textures[i].rgba.data()};
 }
 
 void HostScene::desc(asuna_scene_desc* o) const {
@@ -412,6 +433,8 @@ void HostScene::desc(asuna_scene_desc* o) const {
     o->envmap.height = envH;
     o->envmap.rgba = env.data();
   }
+  o->num_textures = uint32_t(texDescs.size());
+  o->textures = texDescs.data();
 }
 
 int HostScene::shot(uint32_t i, asuna_shot* out) const {
@@ -1196,10 +1219,17 @@ int loadSceneJson(const std::string& text, const std::string& baseDir, HostScene
     return fail(ASUNA_ERR_PARSE, "unrecognized camera type [%s]", cj["type"].str.c_str());
   }
   if (root.has("textures")) {
+    // src/loader/loader.cpp:334-347.  Decoding image files is not this
+    // library's job: .hdr and .pfm are read; other formats are reported
+    // (callers can pass decoded RGBA32F through asuna_scene_desc.textures).
+    // "gamma" applies only to 8-bit formats, none of which is read here.
     for (size_t i = 0; i < root["textures"].size(); ++i) {
       const Json& tj = root["textures"][i];
       if ((rc = checkKeys(tj, {"name", "path"}, "texture"))) return rc;
+      HostScene::Texture t;
+      if ((rc = loadImageRGBA(joinPath(baseDir, tj["path"].str), t.w, t.h, t.rgba))) return rc;
       S.textureNames.push_back(tj["name"].str);
+      S.textures.push_back(std::move(t));
     }
   }
   if (root.has("materials"))

@@ -53,8 +53,14 @@ struct HostScene {
   std::vector<HostShot> shots;
   uint32_t envW = 0, envH = 0;
   std::vector<float> env;
+  struct Texture {
+    uint32_t w = 1, h = 1;
+    std::vector<float> rgba;
+  };
+  std::vector<Texture> textures;  // parallel to textureNames
   // views for asuna_scene_desc
   std::vector<asuna_mesh_desc> meshDescs;
+  std::vector<asuna_texture_desc> texDescs;
 
   void reset();
   int addLight(const asuna_light& l);

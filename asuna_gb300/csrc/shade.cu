@@ -168,6 +168,73 @@ __device__ __forceinline__ HitSt hitState(const SceneDev& S, const InstDev& in, 
   return st;
 }
 
+// textureEval (rchit_layouts.glsl:169-171), .rgb
+__device__ __forceinline__ f3 texRGB(const SceneDev& S, int id, float u, float v) {
+  const int4 ti = __ldg(&S.texInfo[id]);
+  return tex4rgb(S.texels + uint32_t(ti.x), ti.y, ti.z, u, v);
+}
+// a normal-map texel (2c - 1) times the instance's world-to-object matrix
+// as a row vector: how the reference moves object-space normals to world
+__device__ __forceinline__ f3 objectToWorldNormal(const InstDev& in, f3 n) {
+  const float4 w0 = in.w2o[0], w1 = in.w2o[1], w2 = in.w2o[2];
+  return f3{n.x * w0.x + n.y * w1.x + n.z * w2.x, n.x * w0.y + n.y * w1.y + n.z * w2.y,
+            n.x * w0.z + n.y * w1.z + n.z * w2.z};
+}
+
+// The "Fetch textures" block at the top of each material's hit shader:
+// brdf_lambertian.rchit:80-90 (diffuse, tangent-space normal), the same in
+// brdf_plastic/mirror/conductor/phong; brdf_rough_plastic.rchit:196-208 and
+// brdf_rough_conductor.rchit:152-164 add alpha (.rg); bsdf_dielectric.rchit:
+// 79-86 normal only; brdf_pbr_metalness_roughness.rchit:136-149 and
+// brdf_disney.rchit:380-391 add metalness and roughness (.r);
+// brdf_kang18.rchit:140-175 specular (.rgb), alpha (.rg), object-space normal
+// and tangent maps; brdf_emissive.rchit:20-23 radiance = factor * texel.
+// A normal map is followed by configureShadingFrame, which with
+// use_face_normal puts the geometric normal back: the map then has no effect.
+template <int CLS>
+__device__ __forceinline__ void applyTextures(const SceneDev& S, const InstDev& in, MatDev& m, HitSt& st,
+                                              uint32_t useFaceNormal) {
+  if (CLS == kClsTerminal) {
+    if (m.t1.x >= 0) {
+      const f3 r = ld3(m.d) * texRGB(S, m.t1.x, st.u, st.v);
+      m.a = make_float4(r.x, r.y, r.z, m.a.w);
+    }
+    return;
+  }
+  if (CLS != kClsDielectric && m.t0.x >= 0) {
+    const f3 c = texRGB(S, m.t0.x, st.u, st.v);
+    m.a = make_float4(c.x, c.y, c.z, m.a.w);
+  }
+  if ((CLS == kClsRoughPlastic || CLS == kClsRoughConductor || CLS == kClsKang18) && m.t0.z >= 0) {
+    const f3 c = texRGB(S, m.t0.z, st.u, st.v);
+    m.b.x = c.x;
+    m.b.y = c.y;
+  }
+  if (CLS == kClsPbr) {
+    if (m.t0.w >= 0) m.c.y = texRGB(S, m.t0.w, st.u, st.v).x;
+    if (m.t0.z >= 0) m.c.x = texRGB(S, m.t0.z, st.u, st.v).x;
+  }
+  if (CLS == kClsDisney) {
+    if (m.t0.w >= 0) m.c.x = texRGB(S, m.t0.w, st.u, st.v).x;
+    if (m.t0.z >= 0) m.c.y = texRGB(S, m.t0.z, st.u, st.v).x;
+  }
+  if (CLS == kClsKang18 && m.t0.w >= 0) {
+    const f3 c = texRGB(S, m.t0.w, st.u, st.v);
+    m.c = make_float4(c.x, c.y, c.z, m.c.w);
+  }
+  if (m.t0.y >= 0 && useFaceNormal != 1u) {
+    const f3 c = texRGB(S, m.t0.y, st.u, st.v);
+    const f3 n = f3{2.0f * c.x - 1.0f, 2.0f * c.y - 1.0f, 2.0f * c.z - 1.0f};
+    st.N = makeNormal(CLS == kClsKang18 ? objectToWorldNormal(in, n) : toWorld(st.X, st.Y, st.N, n));
+    basis(st.N, st.X, st.Y);
+    st.ffN = dot(st.N, st.V) > 0.0f ? st.N : -st.N;
+  }
+  if (CLS == kClsKang18 && m.t1.y >= 0) {
+    const f3 c = texRGB(S, m.t1.y, st.u, st.v);
+    st.X = makeNormal(objectToWorldNormal(in, f3{2.0f * c.x - 1.0f, 2.0f * c.y - 1.0f, 2.0f * c.z - 1.0f}));
+  }
+}
+
 struct PathIO {
   uint32_t seed;
   uint32_t bflags;
@@ -1100,12 +1167,6 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
         const uint32_t prim = __float_as_uint(h4.w);
         rc.x = sigMix(rc.x, (inst << 20) ^ prim);
         HitSt st = hitState(S, in, prim, h4.y, h4.z, rd, sh.state.use_face_normal);
-        if (CLS == kClsKang18) {
-          // brdf_kang18.rchit:178-181: the tangent frame is rebuilt from N and X
-          st.Y = makeNormal(cross(st.N, st.X));
-          st.X = makeNormal(cross(st.Y, st.N));
-          st.ffN = dot(st.N, st.V) > 0.0f ? st.N : -st.N;
-        }
         if (CLS == kClsTerminal && in.lightId >= 0) {
           // brdf_lambertian.rchit:44-68 (hitLight)
           const LightDev l = S.lights[in.lightId];
@@ -1124,7 +1185,14 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
             io.rad = io.rad + io.thp * ld3(l.rad) * mis;
           }
         } else {
-          const MatDev m = S.mats[in.matId];
+          MatDev m = S.mats[in.matId];
+          applyTextures<CLS>(S, in, m, st, sh.state.use_face_normal);
+          if (CLS == kClsKang18) {
+            // brdf_kang18.rchit:178-181: the tangent frame is rebuilt from N and X
+            st.Y = makeNormal(cross(st.N, st.X));
+            st.X = makeNormal(cross(st.Y, st.N));
+            st.ffN = dot(st.N, st.V) > 0.0f ? st.N : -st.N;
+          }
           // brdf_pbr_metalness_roughness.rchit:156: the opacity test's draw
           // comes first (pass-through, opacity > 0, is rejected at validation)
           // brdf_disney.rchit:413 and brdf_kang18.rchit:183 likewise

@@ -64,8 +64,10 @@ def ctx_stream(ctx):
 
 
 class Denoiser:
+    LOSSES = {"l1log": A.DENOISER_LOSS_L1_LOG, "relmse": A.DENOISER_LOSS_RELMSE}
+
     def __init__(self, ctx, channels=DEFAULT_CHANNELS, seed=0, max_pixels=1 << 20, training=False,
-                 tensor_memory=True):
+                 tensor_memory=True, loss="l1log"):
         self.ctx = ctx
         self.channels = tuple(int(c) for c in channels)
         o = A.DenoiserOpts()
@@ -76,6 +78,7 @@ class Denoiser:
         o.max_pixels = int(max_pixels)
         o.training = 1 if training else 0
         o.tensor_memory = 1 if tensor_memory else 0
+        o.loss = self.LOSSES[loss]
         h = C.c_void_p()
         check(lib().asuna_denoiser_create(ctx.handle, C.byref(o), C.byref(h)))
         self.handle = h

@@ -92,10 +92,28 @@ class SceneBuilder:
         self.lights = []
         self.instances = []  # (transform 3x4, mesh, material, light)
         self.env = None
+        # textures[0] is the reference's dummy texture (src/scene/scene.cpp:87-130)
+        self.textures = [np.zeros((1, 1, 4), np.float32)]
+        self.texture_names = ["add_by_default_dummy_texture"]
         dummy = A.Light()
         dummy.type = A.LIGHT_DIRECTIONAL
         dummy.double_side = 1
         self.lights.append(dummy)
+
+    # -- textures (src/loader/loader.cpp:334-347; decoded RGBA32F) --
+    def add_texture(self, name, rgba):
+        """An [h, w, 3|4] float image (row 0 = v 0); returns its texture id
+        for the materials' *_texture_id fields."""
+        a = np.asarray(rgba, np.float32)
+        if a.ndim != 3 or a.shape[2] not in (3, 4):
+            raise ValueError("texture must be [h, w, 3] or [h, w, 4]")
+        if a.shape[2] == 3:
+            a = np.concatenate([a, np.ones(a.shape[:2] + (1,), np.float32)], 2)
+        if name in self.texture_names:
+            raise ValueError(f"texture [{name}] defined twice")
+        self.textures.append(np.ascontiguousarray(a))
+        self.texture_names.append(name)
+        return len(self.textures) - 1
 
     # -- materials (src/loader/material.cpp:104-231) --
     def add_lambertian(self, name, diffuse):
@@ -359,6 +377,12 @@ class SceneDescHandle:
             d.envmap.height = b.env.shape[0]
             d.envmap.rgba = b.env.ctypes.data
             self._keep.append(b.env)
+        self.textures = (A.TextureDesc * len(b.textures))()
+        for k, t in enumerate(b.textures):
+            self.textures[k] = A.TextureDesc(t.shape[1], t.shape[0], t.ctypes.data)
+            self._keep.append(t)
+        d.num_textures = len(b.textures)
+        d.textures = self.textures
         self.desc = d
 
     @property

@@ -225,8 +225,40 @@ def mixed_shot(b, width, height, frames, max_depth=12, rr_depth=3, channels=("al
     return make_shot(cam, state, width, height, frames, seed=seed, depth_channel=depth, rr_depth=rr_depth)
 
 
+def _spherical_uv(v):
+    """u = longitude, v = colatitude of each vertex (in place)."""
+    p = v["pos"].astype(np.float64)
+    r = np.maximum(np.linalg.norm(p, axis=1), 1e-12)
+    v["uv"][:, 0] = np.arctan2(p[:, 2], p[:, 0]) / (2 * np.pi) + 0.5
+    v["uv"][:, 1] = np.arccos(np.clip(p[:, 1] / r, -1, 1)) / np.pi
+    return v
+
+
+def _plugin_textures(b, rng):
+    """Procedural textures for every slot a material shader reads; returns
+    their ids by role."""
+    yy, xx = np.mgrid[0:32, 0:64].astype(np.float32)
+    chk = ((xx // 8 + yy // 8) % 2)[..., None]
+    smooth = 0.5 + 0.5 * np.sin(xx / 5.0)[..., None] * np.cos(yy / 3.0)[..., None]
+    diffuse = (chk * np.array([0.8, 0.55, 0.2]) + (1 - chk) * np.array([0.15, 0.35, 0.7])) * (0.6 + 0.4 * smooth)
+    bump = np.stack([0.35 * np.sin(xx / 3.0), 0.35 * np.cos(yy / 2.5), np.ones_like(xx)], -1)
+    bump /= np.linalg.norm(bump, axis=-1, keepdims=True)
+    obj_n = np.stack([np.sin(xx / 10.0), np.cos(yy / 6.0), 0.5 + 0.5 * np.sin(xx / 4.0)], -1)
+    obj_n /= np.linalg.norm(obj_n, axis=-1, keepdims=True)
+    tangent = np.stack([np.cos(xx / 9.0), 0.3 * np.sin(yy / 4.0), np.sin(xx / 9.0)], -1)
+    tangent /= np.linalg.norm(tangent, axis=-1, keepdims=True)
+    alpha = np.stack([0.05 + 0.5 * smooth[..., 0], 0.05 + 0.4 * chk[..., 0], np.zeros_like(xx)], -1)
+    metal = np.stack([smooth[..., 0], 0.2 + 0.6 * chk[..., 0], 0.3 + 0.2 * smooth[..., 0]], -1)
+    glow = np.stack([2.0 + 2.0 * smooth[..., 0], 1.0 + chk[..., 0], 0.5 * np.ones_like(xx)], -1)
+    noise = rng.uniform(0.0, 0.05, (32, 64, 3))
+    return {"diffuse": b.add_texture("checker", diffuse + noise), "normal": b.add_texture("bumps", 0.5 * bump + 0.5),
+            "object_normal": b.add_texture("object_normals", 0.5 * obj_n + 0.5),
+            "tangent": b.add_texture("tangents", 0.5 * tangent + 0.5), "alpha": b.add_texture("alpha", alpha),
+            "metal": b.add_texture("metal", metal), "glow": b.add_texture("glow", glow)}
+
+
 def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=False, seed=11,
-                 channels=("albedo", "normal", "depth", "position", "uv", "tangent", "roughness")):
+                 channels=("albedo", "normal", "depth", "position", "uv", "tangent", "roughness"), textured=False):
     """Every implemented plugin in one small scene: Lambertian, anisotropic
     rough plastic, dielectric, smooth plastic, mirror, conductor, rough
     conductor, Phong, PBR metalness-roughness, Disney (every lobe on) and
@@ -234,7 +266,10 @@ def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=Fa
     light, a double-sided JSON "triangle" light (rect with half area), a mesh
     triangle light, a point light and a distant light; an optional lognormal
     environment map (else a background colour); a thin-lens perspective or an
-    OpenCV pinhole camera."""
+    OpenCV pinhole camera.  `textured`: spherical UVs on the spheres and a
+    texture in every slot the shaders read (diffuse, alpha, metalness and
+    roughness, specular, tangent-space and object-space normal maps, tangent
+    map, emissive radiance)."""
     rng = np.random.default_rng(seed)
     b = SceneBuilder()
     b.add_rect_light((-1.0, 3.0, -1.0), (0.0, 3.0, -1.0), (-1.0, 3.0, 0.0), (6.0, 5.0, 4.0))
@@ -259,6 +294,26 @@ def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=Fa
     dn = b.add_disney("disney", (0.25, 0.45, 0.85), metallic=0.3, roughness=0.4, subsurface=0.5, specular_tint=0.3,
                       sheen=0.6, sheen_tint=0.5, clearcoat=0.8, clearcoat_gloss=0.7, anisotropic=0.5)
     kg = b.add_kang18("kang18", (0.5, 0.3, 0.3), (0.4, 0.4, 0.5), (0.1, 0.3))
+    if textured:
+        tx = _plugin_textures(b, rng)
+        M = b.materials
+        M[g].diffuse_texture_id = tx["diffuse"]
+        M[lam].diffuse_texture_id, M[lam].normal_texture_id = tx["diffuse"], tx["normal"]
+        M[rp].diffuse_texture_id, M[rp].roughness_texture_id, M[rp].normal_texture_id = (tx["diffuse"], tx["alpha"],
+                                                                                         tx["normal"])
+        M[di].normal_texture_id = tx["normal"]
+        M[em].radiance_texture_id = tx["glow"]
+        M[sp].normal_texture_id = tx["normal"]
+        M[mi].diffuse_texture_id = tx["diffuse"]
+        M[au].normal_texture_id = tx["normal"]
+        M[al].roughness_texture_id = tx["alpha"]
+        M[ph].diffuse_texture_id, M[ph].normal_texture_id = tx["diffuse"], tx["normal"]
+        M[pb].metalness_texture_id, M[pb].roughness_texture_id, M[pb].normal_texture_id = (tx["metal"], tx["alpha"],
+                                                                                           tx["normal"])
+        M[dn].metalness_texture_id, M[dn].roughness_texture_id, M[dn].diffuse_texture_id = (tx["metal"], tx["alpha"],
+                                                                                            tx["diffuse"])
+        M[kg].metalness_texture_id, M[kg].roughness_texture_id = tx["metal"], tx["alpha"]
+        M[kg].normal_texture_id, M[kg].tangent_texture_id = tx["object_normal"], tx["tangent"]
     v, i = cuboid_mesh(0.15, 0.15, 0.15)
     b.add_mesh("lamp", v, i)
     b.add_instance("lamp", em, rot_y(30.0, (0.6, -0.85, 1.2)))
@@ -274,7 +329,8 @@ def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=Fa
                (al, (1.75, -0.6, 1.2), 0.4), (ph, (0.2, -0.7, 2.0), 0.3), (pb, (-0.9, -0.72, 2.1), 0.28),
                (dn, (1.0, -0.7, 2.2), 0.3), (kg, (-0.3, -0.75, 2.6), 0.25)]
     for k, (mat, pos, s) in enumerate(spheres):
-        b.add_mesh(f"s{k}", displaced_sphere(base_v, faces, seed + k, amplitude=0.05), idx)
+        sv = displaced_sphere(base_v, faces, seed + k, amplitude=0.05)
+        b.add_mesh(f"s{k}", _spherical_uv(sv) if textured else sv, idx)
         b.add_instance(f"s{k}", mat, np.array([[s, 0, 0, pos[0]], [0, s, 0, pos[1]], [0, 0, s, pos[2]]], np.float32))
     state, depth = b.state(spp=frames, max_path_depth=max_depth, channels=channels, bg_color=(0.2, 0.25, 0.3))
     eye, at = (0.0, 1.0, 5.0), (0.0, -0.3, 0.0)

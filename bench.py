@@ -339,11 +339,13 @@ def run_denoise_rmse(args):
     data = dn.render_pairs(ctx, range(1000, 1000 + args.train_scenes), args.train_size, args.train_size,
                            spp_in=spp_in, spp_target=args.train_target_spp, level=args.train_level)
     gen_s = time.time() - t0
-    den = dn.Denoiser(ctx, seed=0, max_pixels=args.train_batch * args.train_crop ** 2, training=True)
+    den = dn.Denoiser(ctx, seed=0, max_pixels=args.train_batch * args.train_crop ** 2, training=True,
+                      loss=args.train_loss)
     t1 = time.time()
     losses = dn.train(den, data, steps=args.train_steps, batch=args.train_batch, crop=args.train_crop, lr=1e-3)
     train_s = time.time() - t1
-    out["training"] = {"scenes": args.train_scenes, "size": args.train_size, "input_spp": list(spp_in),
+    out["training"] = {"loss": args.train_loss, "scenes": args.train_scenes, "size": args.train_size,
+                       "input_spp": list(spp_in),
                        "level": args.train_level,
                        "target_spp": args.train_target_spp, "steps": args.train_steps, "batch": args.train_batch,
                        "crop": args.train_crop, "data_seconds": gen_s, "train_seconds": train_s,
@@ -573,6 +575,8 @@ def main():
     ap.add_argument("--train-steps", type=int, default=6000)
     ap.add_argument("--train-batch", type=int, default=16)
     ap.add_argument("--train-crop", type=int, default=128)
+    ap.add_argument("--train-loss", default="l1log", choices=("l1log", "relmse"),
+                    help="L1 on log radiance, or relative MSE (unbiased with noisy targets)")
     ap.add_argument("--serve", action="store_true", help="serving loop: Poisson arrivals, latency percentiles")
     ap.add_argument("--batch", action="store_true", help="32 batched shots vs 32 sequential calls")
     ap.add_argument("--serve-rate", type=float, default=20.0)

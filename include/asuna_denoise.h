@@ -39,6 +39,13 @@ extern "C" {
 
 #define ASUNA_DENOISER_MAX_LEVELS 6
 
+/* Training losses (asuna_denoiser_opts.loss). */
+enum {
+  ASUNA_DENOISER_LOSS_L1_LOG = 0, /* mean |log1p(out) - log1p(target)| */
+  ASUNA_DENOISER_LOSS_RELMSE = 1  /* mean (out - target)^2 / (out + 0.01)^2, the
+                                     denominator held fixed: unbiased with noisy targets */
+};
+
 typedef struct asuna_denoiser_opts {
   uint32_t levels;                               /* 2..6, default 5 */
   uint32_t channels[ASUNA_DENOISER_MAX_LEVELS];  /* multiples of 16 */
@@ -47,6 +54,7 @@ typedef struct asuna_denoiser_opts {
   uint32_t training;                             /* 1: allocate gradient and Adam state */
   uint32_t tensor_memory;                        /* 1: forward and input-gradient convolutions on tcgen05
                                                     (TMEM accumulators, TMA; the faster path); 0: mma.sync */
+  uint32_t loss;                                 /* ASUNA_DENOISER_LOSS_*, used by asuna_denoiser_loss_grad */
 } asuna_denoiser_opts;
 
 typedef struct asuna_denoiser asuna_denoiser;
@@ -63,7 +71,7 @@ int asuna_denoiser_get_grads(asuna_denoiser* d, float* host, uint64_t n);
  * it tells the network how many samples the radiance holds. */
 int asuna_denoiser_forward(asuna_denoiser* d, const float* radiance, const float* albedo, const float* normal,
                            const float* weight, uint32_t n, uint32_t h, uint32_t w, float* out);
-/* Zeroes the gradients, runs forward, the L1 loss on log1p radiance against
+/* Zeroes the gradients, runs forward, the loss chosen at creation against
  * `target` (mean over valid pixels and 3 channels) and the backward pass.
  * *loss (host) receives the loss; the call synchronises the stream. */
 int asuna_denoiser_loss_grad(asuna_denoiser* d, const float* radiance, const float* albedo, const float* normal,

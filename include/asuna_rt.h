@@ -219,6 +219,15 @@ typedef struct asuna_envmap_desc {
   const float* rgba; /* width*height*4 floats, row-major, NULL = none */
 } asuna_envmap_desc;
 
+/* A material texture: width x height RGBA32F texels, row 0 first (v = 0),
+ * sampled as the reference's texture(): bilinear, REPEAT, base level
+ * (src/core/texture.cpp:99-129, rchit_layouts.glsl:169-171). */
+typedef struct asuna_texture_desc {
+  uint32_t width;
+  uint32_t height;
+  const float* rgba;
+} asuna_texture_desc;
+
 typedef struct asuna_scene_desc {
   uint32_t num_meshes;
   const asuna_mesh_desc* meshes;
@@ -229,6 +238,8 @@ typedef struct asuna_scene_desc {
   uint32_t num_lights; /* lights[0] is the reference's dummy light   */
   const asuna_light* lights;
   asuna_envmap_desc envmap;
+  uint32_t num_textures; /* the materials' *_texture_id index this list; */
+  const asuna_texture_desc* textures; /* textures[0] is the dummy texture */
 } asuna_scene_desc;
 
 /* ---- shots ----------------------------------------------------------------

@@ -355,6 +355,7 @@ struct Scene {
   std::vector<asuna_light> lights;
   bool hasEnv = false;
   Tex env, marg, cond;
+  std::vector<Tex> texs;  // material textures (RGBA)
 };
 
 static void buildBvh(Mesh& m) {
@@ -786,6 +787,7 @@ struct HitState {
   V2<R> uv;
   V3<R> pos, V, N, geoN, ffN, X, Y;
   asuna_material mat;
+  const float* w2o;  // the instance's world-to-object rows
 };
 
 // rchit_layouts.glsl:61-95
@@ -806,6 +808,7 @@ template <class R> HitState<R> getHitState(const Scene& s, const asuna_shot& sh,
                  R(o[4]) * po.x + R(o[5]) * po.y + R(o[6]) * po.z + R(o[7]),
                  R(o[8]) * po.x + R(o[9]) * po.y + R(o[10]) * po.z + R(o[11])};
   const float* w = in.w2o;
+  st.w2o = w;
   auto nxf = [&](V3<R> n) {
     return makeNormal(V3<R>{n.x * R(w[0]) + n.y * R(w[4]) + n.z * R(w[8]),
                             n.x * R(w[1]) + n.y * R(w[5]) + n.z * R(w[9]),
@@ -823,6 +826,64 @@ template <class R> HitState<R> getHitState(const Scene& s, const asuna_shot& sh,
   basis(st.N, st.X, st.Y);
   st.ffN = dot(st.N, st.V) > R(0) ? st.N : -st.N;
   return st;
+}
+
+// The "Fetch textures" block of each material's hit shader (textureEval,
+// rchit_layouts.glsl:169-171, bilinear REPEAT at the base level):
+// brdf_lambertian.rchit:80-90 diffuse + tangent-space normal map (likewise
+// plastic, mirror, conductor, Phong); brdf_rough_plastic.rchit:196-208 and
+// brdf_rough_conductor.rchit:152-164 add alpha (.rg); bsdf_dielectric.rchit:
+// 79-86 normal only; brdf_pbr_metalness_roughness.rchit:136-149 and
+// brdf_disney.rchit:380-391 add metalness and roughness (.r);
+// brdf_kang18.rchit:140-175 specular (.rgb), alpha (.rg), object-space
+// normal and tangent maps; brdf_emissive.rchit:20-23 radiance = factor * texel.
+template <class R> V3<R> texRGB(const Scene& s, int id, V2<R> uv) {
+  R o[4];
+  texFetch(s.texs[size_t(id)], uv.x, uv.y, o);
+  return V3<R>{o[0], o[1], o[2]};
+}
+template <class R> void applyTextures(const Scene& s, const asuna_shot& sh, HitState<R>& st) {
+  asuna_material& m = st.mat;
+  const uint32_t t = m.type;
+  auto put3 = [](float* f, V3<R> v) {
+    f[0] = float(v.x);
+    f[1] = float(v.y);
+    f[2] = float(v.z);
+  };
+  if (t == ASUNA_MAT_EMISSIVE) {
+    if (m.radiance_texture_id >= 0) put3(m.radiance, L3<R>(m.radiance_factor) * texRGB(s, m.radiance_texture_id, st.uv));
+    return;
+  }
+  if (t != ASUNA_MAT_DIELECTRIC && m.diffuse_texture_id >= 0) put3(m.diffuse, texRGB(s, m.diffuse_texture_id, st.uv));
+  if (t == ASUNA_MAT_PBR_METALNESS_ROUGHNESS || t == ASUNA_MAT_DISNEY) {
+    if (m.metalness_texture_id >= 0) m.metalness = float(texRGB(s, m.metalness_texture_id, st.uv).x);
+    if (m.roughness_texture_id >= 0) m.roughness = float(texRGB(s, m.roughness_texture_id, st.uv).x);
+  }
+  if (t == ASUNA_MAT_KANG18 && m.metalness_texture_id >= 0) put3(m.rho_spec, texRGB(s, m.metalness_texture_id, st.uv));
+  if ((t == ASUNA_MAT_ROUGH_PLASTIC || t == ASUNA_MAT_ROUGH_CONDUCTOR || t == ASUNA_MAT_KANG18) &&
+      m.roughness_texture_id >= 0) {
+    V3<R> c = texRGB(s, m.roughness_texture_id, st.uv);
+    m.aniso_alpha[0] = float(c.x);
+    m.aniso_alpha[1] = float(c.y);
+  }
+  auto objToWorld = [&](V3<R> n) {
+    const float* w = st.w2o;
+    return V3<R>{n.x * R(w[0]) + n.y * R(w[4]) + n.z * R(w[8]), n.x * R(w[1]) + n.y * R(w[5]) + n.z * R(w[9]),
+                 n.x * R(w[2]) + n.y * R(w[6]) + n.z * R(w[10])};
+  };
+  if (m.normal_texture_id >= 0) {
+    V3<R> c = texRGB(s, m.normal_texture_id, st.uv);
+    V3<R> n{R(2) * c.x - R(1), R(2) * c.y - R(1), R(2) * c.z - R(1)};
+    st.N = makeNormal(t == ASUNA_MAT_KANG18 ? objToWorld(n) : toWorld(st.X, st.Y, st.N, n));
+    // configureShadingFrame, rchit_layouts.glsl:61-65
+    if (sh.state.use_face_normal == 1) st.N = st.geoN;
+    basis(st.N, st.X, st.Y);
+    st.ffN = dot(st.N, st.V) > R(0) ? st.N : -st.N;
+  }
+  if (t == ASUNA_MAT_KANG18 && m.tangent_texture_id >= 0) {
+    V3<R> c = texRGB(s, m.tangent_texture_id, st.uv);
+    st.X = makeNormal(objToWorld(V3<R>{R(2) * c.x - R(1), R(2) * c.y - R(1), R(2) * c.z - R(1)}));
+  }
 }
 
 // brdf_lambertian.rchit:44-68
@@ -2050,6 +2111,7 @@ void tracePath(const Scene& s, const asuna_shot& sh, uint32_t x, uint32_t y, uin
       if (hs.lightId >= 0) {
         hitLight<R>(s, p, hs.lightId, hs.pos);
       } else {
+        applyTextures<R>(s, sh, hs);
         uint32_t type = hs.mat.type;
         if (type == ASUNA_MAT_EMISSIVE) {
           // brdf_emissive.rchit:12-27
@@ -2399,6 +2461,14 @@ int oracle_scene_create(const asuna_scene_desc* d, oracle_scene** out) {
   }
   s.mats.assign(d->materials, d->materials + d->num_materials);
   s.lights.assign(d->lights, d->lights + d->num_lights);
+  s.texs.resize(d->num_textures);
+  for (uint32_t i = 0; i < d->num_textures; ++i) {
+    const asuna_texture_desc& t = d->textures[i];
+    s.texs[i].w = int(t.width);
+    s.texs[i].h = int(t.height);
+    s.texs[i].c = 4;
+    s.texs[i].d.assign(t.rgba, t.rgba + size_t(t.width) * t.height * 4);
+  }
   if (d->envmap.rgba && d->envmap.width && d->envmap.height) {
     int w = int(d->envmap.width), h = int(d->envmap.height);
     s.hasEnv = true;

@@ -63,7 +63,7 @@ static image2D images[NUM_OUTPUT_IMAGES];
 static GpuCamera cameraInfo;
 static GpuSunAndSky sunAndSky;
 static sampler2D envmapSamplers[3];
-static sampler2D textureSamplers[1];
+static std::vector<sampler2D> textureSamplers(1);
 static InstancesBuf instances;
 static LightsBuf lights;
 static thread_local GpuPushConstantRaytrace pc;
@@ -257,6 +257,9 @@ int ref_render(const asuna_scene_desc* d, const asuna_shot* shot, float* film, a
   S.cond.assign(size_t(ew) * eh * 2, 0.0f);
   if (d->envmap.rgba && d->envmap.width) oracle_envmap_tables(ew, eh, S.env.data(), S.marg.data(), S.cond.data());
   gS = &S;
+  textureSamplers.assign(std::max(1u, d->num_textures), sampler2D{});
+  for (uint32_t i = 0; i < d->num_textures; ++i)
+    textureSamplers[i] = sampler2D{int(d->textures[i].width), int(d->textures[i].height), 4, d->textures[i].rgba};
   envmapSamplers[0] = sampler2D{int(ew), int(eh), 4, S.env.data()};
   envmapSamplers[1] = sampler2D{int(ew), int(eh), 2, S.marg.data()};
   envmapSamplers[2] = sampler2D{int(ew), int(eh), 2, S.cond.data()};

@@ -2,7 +2,8 @@
 
 A numpy float64 restatement of the U-Net that ``asuna_gb300/csrc/denoise.cu``
 runs on the GPU: the same parameter layout, padding, residual on
-log1p(radiance), L1 loss and backward pass.  With ``bf16=True`` values are
+log1p(radiance), the training losses (L1 on log radiance, relative MSE) and
+backward pass.  With ``bf16=True`` values are
 rounded to bfloat16 (round to nearest even) at exactly the points where the
 GPU stores bf16 tensors, so GPU and CPU differ only by accumulation order;
 with ``bf16=False`` the network is plain float64 and is the one checked
@@ -191,17 +192,33 @@ class UNetRef:
         y = head[:, :h, :w, :3] + np.log1p(np.maximum(rad[..., :3], 0.0))
         return np.maximum(np.expm1(y), 0.0)
 
-    def loss_grad(self, rad, alb, nrm, target, wsum=None):
+    @staticmethod
+    def head_loss(head3, rad, target, loss="l1log", den=None):
+        """(loss, d loss / d head) of the valid head channels.  "l1log":
+        mean |head + log1p(r) - log1p(t)|; "relmse": mean (o - t)^2 /
+        (o + 0.01)^2 with o = max(expm1(head + log1p(r)), 0) and the
+        denominator treated as a constant (or taken from `den`)."""
+        count = head3.size
+        y = head3 + np.log1p(np.maximum(rad[..., :3], 0.0))
+        if loss == "l1log":
+            d = y - np.log1p(np.maximum(target[..., :3], 0.0))
+            return np.abs(d).sum() / count, np.sign(d) / count
+        e = np.expm1(y)
+        o = np.maximum(e, 0.0)
+        inv = 1.0 / (o + 0.01) ** 2 if den is None else den
+        d = o - np.maximum(target[..., :3], 0.0)
+        return (d * d * inv).sum() / count, np.where(e > 0, 2.0 * d * (e + 1.0) * inv, 0.0) / count
+
+    def loss_grad(self, rad, alb, nrm, target, wsum=None, loss="l1log"):
         """Returns (loss, flat gradient) in the parameter layout."""
         L = self.L
         head = self.forward(rad, alb, nrm, wsum)
         c = self.cache
         n, h, w = rad.shape[:3]
-        count = 3.0 * n * h * w
-        d = head[:, :h, :w, :3] + np.log1p(np.maximum(rad[..., :3], 0.0)) - np.log1p(np.maximum(target[..., :3], 0.0))
-        loss = np.abs(d).sum() / count
+        lv, gh = self.head_loss(head[:, :h, :w, :3], rad, target, loss)
+        loss = lv
         gHead = np.zeros_like(head)
-        gHead[:, :h, :w, :3] = np.sign(d) / count
+        gHead[:, :h, :w, :3] = gh
         gHead = self.r(gHead)
         grads = [None] * len(self.layers)
 
@@ -242,11 +259,10 @@ class UNetRef:
         flat = np.concatenate([np.concatenate([gw.ravel(), gb.ravel()]) for gw, gb in grads])
         return loss, flat
 
-    def loss(self, rad, alb, nrm, target, wsum=None):
+    def loss(self, rad, alb, nrm, target, wsum=None, loss="l1log", den=None):
         head = self.forward(rad, alb, nrm, wsum)
         n, h, w = rad.shape[:3]
-        d = head[:, :h, :w, :3] + np.log1p(np.maximum(rad[..., :3], 0.0)) - np.log1p(np.maximum(target[..., :3], 0.0))
-        return np.abs(d).sum() / (3.0 * n * h * w)
+        return self.head_loss(head[:, :h, :w, :3], rad, target, loss, den)[0]
 
 
 def he_init(channels, seed):

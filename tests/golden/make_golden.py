@@ -24,6 +24,9 @@ CASES = {
                                                                  "roughness", "specular")),
     "plugins_bg_opencv_32x24x2": lambda: scenes.plugin_scene(32, 24, frames=2, env=False, opencv=True,
                                                              channels=("albedo", "normal")),
+    "plugins_textured_40x28x2": lambda: scenes.plugin_scene(40, 28, frames=2, env=True, textured=True,
+                                                            channels=("albedo", "normal", "tangent", "roughness",
+                                                                      "specular", "uv")),
 }
 
 

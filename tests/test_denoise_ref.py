@@ -2,6 +2,7 @@
 central finite differences, bf16 rounding is round-to-nearest-even, and the
 initial parameters follow the library's seeded He-normal recipe."""
 import numpy as np
+import pytest
 
 from oracle import unet_ref as U
 
@@ -21,15 +22,21 @@ def test_sample_count_channel():
     assert np.allclose(x[0, :4, :4, 9], 0.5) and not x[0, 4:, :, 9].any()
 
 
-def test_backward_matches_finite_differences():
+@pytest.mark.parametrize("loss_kind", ["l1log", "relmse"])
+def test_backward_matches_finite_differences(loss_kind):
+    """Central differences of the float64 network; relmse's denominator is
+    held at the unperturbed output, as the gradient treats it."""
     rng = np.random.default_rng(3)
     ch = [4, 6, 8]
     params = U.he_init(ch, 5).astype(np.float64)
     params += rng.normal(0, 0.05, params.size)  # non-zero biases too
     rad, alb, nrm, tgt = _images(rng, 2, 7, 9)  # padded to 8 x 12
     net = U.UNetRef(ch, params, bf16=False)
-    loss, g = net.loss_grad(rad, alb, nrm, tgt)
-    assert np.isclose(loss, net.loss(rad, alb, nrm, tgt))
+    loss, g = net.loss_grad(rad, alb, nrm, tgt, loss=loss_kind)
+    den = None
+    if loss_kind == "relmse":
+        den = 1.0 / (net.output(rad, alb, nrm)[..., :3] + 0.01) ** 2
+    assert np.isclose(loss, net.loss(rad, alb, nrm, tgt, loss=loss_kind, den=den))
     # central differences on the largest-gradient parameters of every layer
     off, picks = 0, []
     for cin, cout in U.layer_shapes(ch):
@@ -42,8 +49,8 @@ def test_backward_matches_finite_differences():
         p1, p2 = params.copy(), params.copy()
         p1[i] += eps
         p2[i] -= eps
-        fd = (U.UNetRef(ch, p1, bf16=False).loss(rad, alb, nrm, tgt) -
-              U.UNetRef(ch, p2, bf16=False).loss(rad, alb, nrm, tgt)) / (2 * eps)
+        fd = (U.UNetRef(ch, p1, bf16=False).loss(rad, alb, nrm, tgt, loss=loss_kind, den=den) -
+              U.UNetRef(ch, p2, bf16=False).loss(rad, alb, nrm, tgt, loss=loss_kind, den=den)) / (2 * eps)
         assert abs(fd - g[i]) <= 1e-7 + 2e-4 * abs(fd), (i, fd, g[i])
 
 

@@ -207,12 +207,13 @@ def _net_inputs(rng, n, h, w):
     return rad, alb, nrm, wsum, tgt
 
 
-def test_network_forward_loss_and_gradients(dctx):
+@pytest.mark.parametrize("loss_kind", ["l1log", "relmse"])
+def test_network_forward_loss_and_gradients(dctx, loss_kind):
     ch = dn.DEFAULT_CHANNELS
     rng = np.random.default_rng(5)
     n, h, w = 2, 37, 45  # padded to 48 x 48
     rad, alb, nrm, wsum, tgt = _net_inputs(rng, n, h, w)
-    d = dn.Denoiser(dctx, ch, seed=3, max_pixels=n * 48 * 48, training=True)
+    d = dn.Denoiser(dctx, ch, seed=3, max_pixels=n * 48 * 48, training=True, loss=loss_kind)
     p = U.he_init(ch, 3)
     assert np.allclose(d.get_params(), p, rtol=1e-6, atol=1e-9)
     p = (p + rng.normal(0, 0.02, p.size)).astype(np.float32)  # non-zero biases, active head
@@ -227,7 +228,7 @@ def test_network_forward_loss_and_gradients(dctx):
     med = np.median(np.abs(got - ro) / (np.abs(ro) + 1e-3))
     mx = np.abs(got - ro).max() / np.abs(ro).max()
     loss = d.loss_grad(drad, dalb, dnrm, dw, dtgt)
-    rl, rg = ref.loss_grad(rad.astype(np.float64), alb, nrm, tgt.astype(np.float64), wsum)
+    rl, rg = ref.loss_grad(rad.astype(np.float64), alb, nrm, tgt.astype(np.float64), wsum, loss=loss_kind)
     g = d.get_grads().astype(np.float64)
     print(f"\nforward: median rel {med:.2e}, max/scale {mx:.2e}; loss {loss:.6f} vs {rl:.6f}")
     off, rows = 0, []

@@ -62,6 +62,19 @@ def test_every_plugin(ctx, env, opencv):
     _check(rec, orec, imgs, ofilm, film_tol=5e-3)
 
 
+@pytest.mark.parametrize("face_normal", [0, 1])
+def test_every_plugin_textured(ctx, face_normal):
+    """Every texture slot the shaders read (diffuse, alpha, metalness and
+    roughness, specular, tangent- and object-space normal maps, tangent map,
+    emissive radiance); with use_face_normal the normal maps must have no
+    effect, as configureShadingFrame puts the geometric normal back."""
+    b, shot = scenes.plugin_scene(96, 64, frames=4, max_depth=8, env=True, textured=True,
+                                  channels=("albedo", "normal", "tangent", "roughness", "specular", "uv"))
+    shot.state.use_face_normal = face_normal
+    rec, orec, imgs, ofilm = _run(ctx, b, shot)
+    _check(rec, orec, imgs, ofilm, film_tol=5e-3)
+
+
 def test_mixed_scene_small(ctx):
     b, shot = scenes.mixed_scene(160, 90, frames=2, max_depth=12, n_spheres=12, level=4, seed=3, rr_depth=3,
                                  env_size=(128, 64))

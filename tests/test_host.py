@@ -365,6 +365,41 @@ def test_hdr_envmap_reader(tmp_path):
     assert np.allclose(out[..., :3], np.array([128, 64, 32]) * 2.0 ** (129 - 136))
 
 
+def test_json_textures(tmp_path):
+    """"textures" (src/loader/loader.cpp:334-347) load into the scene's
+    texture list after the dummy texture; materials reference them by name.
+    .hdr / .pfm are read; other image formats are reported as unsupported."""
+    rng = np.random.default_rng(2)
+    img = rng.uniform(0, 2, (3, 5, 4)).astype(np.float32)
+    img[..., 3] = 1.0
+    A.check(A.lib().asuna_image_write(str(tmp_path / "t.pfm").encode(), 5, 3, img.ctypes.data))
+    base = {"state": {}, "camera": {"type": "perspective", "film": {"resolution": [8, 8]}}, "meshes": [],
+            "instances": []}
+    scene = {**base, "textures": [{"name": "t", "path": "t.pfm", "gamma": 2.2}],
+             "materials": [{"type": "brdf_lambertian", "name": "m", "diffuse_texture": "t", "normal_texture": "t"}]}
+    js = ag.JsonScene(text=json.dumps(scene), base_dir=str(tmp_path))
+    d = js.desc().desc
+    assert d.num_textures == 2 and (d.textures[0].width, d.textures[0].height) == (1, 1)
+    t = d.textures[1]
+    assert (t.width, t.height) == (5, 3)
+    got = np.ctypeslib.as_array(C.cast(t.rgba, C.POINTER(C.c_float)), shape=(3, 5, 4))
+    assert np.array_equal(got[..., :3], img[..., :3])
+    assert d.materials[1].diffuse_texture_id == 1 and d.materials[1].normal_texture_id == 1
+    A.check(A.lib().asuna_scene_validate(js.desc().ptr))
+    # a texture id past the list is invalid
+    b = ag.SceneBuilder()
+    k = b.add_lambertian("m", (0.5, 0.5, 0.5))
+    b.materials[k].diffuse_texture_id = 7
+    with pytest.raises(ag.AsunaError) as e:
+        A.check(A.lib().asuna_scene_validate(b.desc().ptr))
+    assert e.value.code == A.ERR_INVALID
+    (tmp_path / "p.png").write_bytes(b"not decoded")
+    bad = {**base, "textures": [{"name": "p", "path": "p.png"}]}
+    with pytest.raises(ag.AsunaError) as e:
+        ag.JsonScene(text=json.dumps(bad), base_dir=str(tmp_path))
+    assert e.value.code == A.ERR_UNSUPPORTED
+
+
 def test_json_material_plugins_match_builder():
     """brdf_plastic, brdf_mirror, brdf_conductor, brdf_rough_conductor,
     brdf_phong, brdf_pbr_metalness_roughness, brdf_disney and brdf_kang18
