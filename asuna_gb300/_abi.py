@@ -159,6 +159,7 @@ SIGNATURES = [
     ("asuna_film_create", C.c_int, [P, C.c_uint32, C.c_uint32, C.POINTER(P)]),
     ("asuna_film_destroy", C.c_int, [P]),
     ("asuna_film_read", C.c_int, [P, P, C.c_int, P]),
+    ("asuna_film_image", C.c_int, [P, C.c_int, C.POINTER(C.c_void_p)]),
     ("asuna_film_clear", C.c_int, [P, P]),
     ("asuna_render", C.c_int, [P, P, C.POINTER(Shot), P, C.POINTER(RenderStats)]),
     ("asuna_render_batch", C.c_int, [P, P, C.POINTER(Shot), C.POINTER(P), C.c_uint32, C.POINTER(RenderStats)]),

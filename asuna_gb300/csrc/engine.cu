@@ -563,6 +563,15 @@ int asuna_film_read(asuna_ctx* c, asuna_film* f, int image, float* host) {
   return ASUNA_OK;
 }
 
+int asuna_film_image(asuna_film* f, int image, float** out) {
+  if (!f || !out) return fail(ASUNA_ERR_INVALID, "null argument");
+  if (image < 0 || image >= ASUNA_NUM_OUTPUT_IMAGES) return fail(ASUNA_ERR_INVALID, "image %d out of range", image);
+  const size_t np = size_t(f->width) * f->height;
+  float4* p = image == 0 ? f->rad : (image == 8 ? f->w : f->ch + size_t(image - 1) * np);
+  *out = reinterpret_cast<float*>(p);
+  return ASUNA_OK;
+}
+
 // ---------------------------------------------------------------------------
 static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shots, asuna_film* const* films,
                       uint32_t n, asuna_render_stats* stats, asuna_path_record* hostRecords) {

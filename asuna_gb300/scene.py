@@ -436,6 +436,20 @@ class Film:
         check(lib().asuna_film_read(self.ctx.handle, self.handle, image, out.ctypes.data))
         return out
 
+    def tensor(self, image=0):
+        """Film image `image` as a CUDA [h, w, 4] float32 tensor sharing the
+        film's memory (no copy; valid while the film lives)."""
+        import torch
+
+        ptr = C.c_void_p()
+        check(lib().asuna_film_image(self.handle, int(image), C.byref(ptr)))
+
+        class _View:
+            __cuda_array_interface__ = {"shape": (self.height, self.width, 4), "typestr": "<f4",
+                                        "data": (int(ptr.value), False), "version": 2, "strides": None}
+
+        return torch.as_tensor(_View(), device=f"cuda:{self.ctx.device}")
+
     def clear(self):
         check(lib().asuna_film_clear(self.ctx.handle, self.handle))
 
@@ -504,6 +518,9 @@ class Context:
 
     def set_traversal(self, refill_extend=0, refill_shadow=0, speculate_extend=-1, speculate_shadow=-1,
                       blocks_per_sm=0):
+        """Traversal settings (results do not depend on them): refill thresholds,
+        speculative walking (-1 default on) and the kernel variant's resident
+        blocks per SM."""
         check(lib().asuna_ctx_set_traversal(self.handle, int(refill_extend), int(refill_shadow),
                                             int(speculate_extend), int(speculate_shadow), int(blocks_per_sm)))
 

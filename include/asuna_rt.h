@@ -357,6 +357,9 @@ int asuna_film_destroy(asuna_film* film);
 /* image: 0 radiance, 1..7 AOV channels, 8 filter-weight sum.  Copies
  * width*height*4 floats into host memory (pinned or pageable). */
 int asuna_film_read(asuna_ctx* ctx, asuna_film* film, int image, float* host_rgba);
+/* Device address of film image `image` (0..8; width x height RGBA32F,
+ * valid while the film lives) for zero-copy use on the context's stream. */
+int asuna_film_image(asuna_film* film, int image, float** device_rgba);
 int asuna_film_clear(asuna_ctx* ctx, asuna_film* film);
 
 /* ---- render --------------------------------------------------------------- */

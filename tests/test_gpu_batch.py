@@ -78,13 +78,14 @@ def test_graph_replay_equals_direct_launches(ctx):
 
 
 def test_traversal_settings_do_not_change_results(ctx):
-    """Refill thresholds and speculative walking change the visiting order
-    only: closest hits (ties to the lowest instance / primitive) and
-    occlusion answers are the same, so films are bit-identical."""
+    """Refill thresholds, speculative walking and the kernel variant change the
+    visiting order only: closest hits (ties to the lowest instance /
+    primitive) and occlusion answers are the same, so films are
+    bit-identical."""
     b, shot = scenes.plugin_scene(64, 48, frames=2, max_depth=6)
     scene = ctx.create_scene(b.desc())
     films = []
-    for trav in ((8, 8, 1, 1, 8), (1, 32, 0, 0, 10), (32, 1, 1, 0, 12), (4, 16, 0, 1, 10)):
+    for trav in ((8, 8, 1, 1, 8), (1, 32, 0, 0, 10), (32, 1, 1, 0, 12), (4, 16, 0, 1, 10), (24, 8, 1, 1, 10)):
         ctx.set_traversal(*trav)
         f = ctx.create_film(64, 48)
         ctx.render(scene, shot, f)
@@ -92,3 +93,16 @@ def test_traversal_settings_do_not_change_results(ctx):
     ctx.set_traversal()
     for f in films[1:]:
         assert np.array_equal(films[0], f)
+
+
+def test_film_image_tensor_is_the_film(ctx):
+    """asuna_film_image: a zero-copy device view equal to what film_read copies out."""
+    b, shot = scenes.box_scene(40, 24, frames=2, max_depth=4, channels=("albedo", "normal"))
+    scene = ctx.create_scene(b.desc())
+    f = ctx.create_film(40, 24)
+    ctx.render(scene, shot, f)
+    ctx.sync()
+    for k in (0, 1, 2, 8):
+        t = f.tensor(k)
+        assert t.shape == (24, 40, 4) and t.is_cuda
+        assert np.array_equal(t.cpu().numpy(), f.read(k))
