@@ -103,7 +103,15 @@ struct SceneDev {
   int32_t envW, envH;
   int32_t numInst;
   uint32_t classMask;  // shading classes some instance can reach (bit k = class k)
+  uint32_t passThrough;  // 1: some material can pass rays through (opacity)
 };
+// Wavefront passes of a batch: one per bounce, plus the pass-through reserve.
+inline int wavefrontPasses(int maxDepth, const SceneDev& S) {
+  return maxDepth + (S.passThrough ? ASUNA_MAX_PASS_THROUGH : 0);
+}
+// Path info word y: lobe flags in the low 16 bits, pass-throughs so far above.
+constexpr uint32_t kFlagsMask = 0xffffu;
+constexpr int kPassShift = 16;
 
 // ---- shots, films, batches ----------------------------------------------------
 struct __align__(16) ShotDev {

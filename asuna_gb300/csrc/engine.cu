@@ -415,16 +415,23 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
     // Disney: (anisotropic, opacity, ior, -); others: (alpha x, alpha y, ior, fdrInt)
     mats[i].b = m.type == ASUNA_MAT_DISNEY ? make_float4(m.anisotropic, m.rho_spec[0], m.ior, 0.0f)
                                            : make_float4(m.aniso_alpha[0], m.aniso_alpha[1], m.ior, m.radiance[0]);
-    // Phong, kang18: specular reflectance (rhoSpec) and Phong's exponent; PBR:
+    // Phong: specular reflectance (rhoSpec) and exponent; kang18: rhoSpec and
+    // opacity (metalness); PBR:
     // roughness, metalness, opacity (specular); Disney: metalness, roughness,
     // subsurface, specular tint; others: radiance
-    mats[i].c = (m.type == ASUNA_MAT_PHONG || m.type == ASUNA_MAT_KANG18)
-                    ? make_float4(m.rho_spec[0], m.rho_spec[1], m.rho_spec[2], m.specular)
+    mats[i].c = m.type == ASUNA_MAT_PHONG    ? make_float4(m.rho_spec[0], m.rho_spec[1], m.rho_spec[2], m.specular)
+                : m.type == ASUNA_MAT_KANG18 ? make_float4(m.rho_spec[0], m.rho_spec[1], m.rho_spec[2], m.metalness)
                 : m.type == ASUNA_MAT_PBR_METALNESS_ROUGHNESS
                     ? make_float4(m.roughness, m.metalness, m.specular, 0.0f)
                 : m.type == ASUNA_MAT_DISNEY ? make_float4(m.metalness, m.roughness, m.subsurface, m.specular_tint)
                                              : make_float4(m.radiance[0], m.radiance[1], m.radiance[2], 0.0f);
     // Disney: sheen, sheen tint, clearcoat, clearcoat gloss; others: radiance factor
+    // brdf_pbr_metalness_roughness.rchit:152-160, brdf_disney.rchit:409-417,
+    // brdf_kang18.rchit:150-187: opacity in specular / rho_spec[0] / metalness
+    if (m.opacity_texture_id >= 0 || (m.type == ASUNA_MAT_PBR_METALNESS_ROUGHNESS && m.specular != 0.0f) ||
+        (m.type == ASUNA_MAT_DISNEY && m.rho_spec[0] != 0.0f) || (m.type == ASUNA_MAT_KANG18 && m.metalness != 0.0f))
+      if (m.type == ASUNA_MAT_PBR_METALNESS_ROUGHNESS || m.type == ASUNA_MAT_DISNEY || m.type == ASUNA_MAT_KANG18)
+        s->view.passThrough = 1;
     mats[i].t0 = make_int4(m.diffuse_texture_id, m.normal_texture_id, m.roughness_texture_id, m.metalness_texture_id);
     mats[i].t1 = make_int4(m.radiance_texture_id, m.tangent_texture_id, m.opacity_texture_id, -1);
     mats[i].d = m.type == ASUNA_MAT_DISNEY
@@ -680,7 +687,7 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
   if (stats) ASUNA_CUDA_TRY(cudaMemsetAsync(c->cnt, 0, sizeof(DevCounters), c->stream));
   // timing events: [begin, end] + one pair per extend / shade / connect launch
   size_t evNeed = 2;
-  for (auto& b : batches) evNeed += size_t(b.maxDepth) * 6;
+  for (auto& b : batches) evNeed += size_t(wavefrontPasses(b.maxDepth, s->view)) * 6;
   if (stats) {
     while (c->events.size() < evNeed) {
       cudaEvent_t ev;
@@ -728,7 +735,8 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
     P.cur = 0;
     int rg = int(std::min<uint64_t>((b.paths + 255) / 256, uint64_t(c->raygenGrid)));
     launchRaygen(P, std::max(rg, 1), c->stream);
-    for (int depth = 1; depth <= b.maxDepth; ++depth) {
+    const int passes = wavefrontPasses(b.maxDepth, s->view);
+    for (int depth = 1; depth <= passes; ++depth) {
       P.depth = uint32_t(depth);
       // inside a capture the events become event-record nodes of the graph,
       // so every replay records them again
@@ -805,7 +813,8 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
     stats->shadow_tris_tested = c->hostCnt->shTris;
     // raygen + accumulate (+ records) per wave; extend, shading, connect per depth
     for (const Batch& b : batches)
-      stats->kernel_launches += 2 + (hostRecords ? 1 : 0) + uint64_t(b.maxDepth) * (2 + shadeLaunches(s->view.classMask));
+      stats->kernel_launches += 2 + (hostRecords ? 1 : 0) +
+                                uint64_t(wavefrontPasses(b.maxDepth, s->view)) * (2 + shadeLaunches(s->view.classMask));
     float ms = 0;
     ASUNA_CUDA_TRY(cudaEventElapsedTime(&ms, c->events[0], c->events[1]));
     stats->ms_total = ms;

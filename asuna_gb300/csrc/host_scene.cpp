@@ -74,17 +74,6 @@ int validateSceneDesc(const asuna_scene_desc* d) {
     for (int32_t id : ids)
       if (id >= int32_t(d->num_textures))
         return fail(ASUNA_ERR_INVALID, "material %u: texture %d out of range (%u textures)", i, id, d->num_textures);
-    // an opacity texture drives the pass-through below, per texel
-    if ((t == ASUNA_MAT_PBR_METALNESS_ROUGHNESS || t == ASUNA_MAT_DISNEY || t == ASUNA_MAT_KANG18) &&
-        m.opacity_texture_id >= 0)
-      return fail(ASUNA_ERR_UNSUPPORTED, "material %u: opacity textures (pass-through) are not implemented", i);
-    // brdf_pbr_metalness_roughness.rchit:152-160, brdf_disney.rchit:409-417,
-    // brdf_kang18.rchit:150-187: an opacity above 0 (PBR: the specular field
-    // and kang18: metalness, both always 0 from the JSON loader; Disney:
-    // rho_spec[0], JSON "opacity") lets rays pass through without a bounce
-    if ((t == ASUNA_MAT_PBR_METALNESS_ROUGHNESS && m.specular != 0.0f) ||
-        (t == ASUNA_MAT_DISNEY && m.rho_spec[0] != 0.0f) || (t == ASUNA_MAT_KANG18 && m.metalness != 0.0f))
-      return fail(ASUNA_ERR_UNSUPPORTED, "material %u: opacity pass-through is not implemented", i);
   }
   for (uint32_t i = 0; i < d->num_instances; ++i) {
     const asuna_instance_desc& in = d->instances[i];

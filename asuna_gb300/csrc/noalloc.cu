@@ -179,7 +179,7 @@ int renderNoAlloc(const asuna_scene* s, const asuna_shot* shot, asuna_film* film
       P.depth = 0;
       const int rg = int(std::min<uint64_t>((W.numPaths + 255) / 256, uint64_t(raygenGrid)));
       launchRaygen(P, std::max(rg, 1), stream);
-      for (int depth = 1; depth <= maxDepth; ++depth) {
+      for (int depth = 1; depth <= wavefrontPasses(maxDepth, s->view); ++depth) {
         P.depth = uint32_t(depth);
         launchExtend(P, traceGrid, stream);
         launchShade(P, shadeGrid, stream);

@@ -1142,9 +1142,13 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
       const ShotDev& sh = W.shots[R.shot];
       const uint32_t frame = R.frameBegin + inf.w / R.npix;
       const uint32_t pix = inf.w % R.npix;
-      const uint32_t depth = P.depth;
+      // a path that passed through surfaces without a bounce is that many
+      // passes behind the wavefront: its own depth is what the shaders see
+      uint32_t passes = inf.y >> kPassShift;
+      const uint32_t depth = P.depth - passes;
+      bool passThrough = false;
       io.seed = inf.x;
-      io.bflags = inf.y;
+      io.bflags = inf.y & kFlagsMask;
       io.bpdf = t4.w;
       io.thp = ld3(t4);
       io.rad = ld3(r4);
@@ -1193,11 +1197,19 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
             st.X = makeNormal(cross(st.Y, st.N));
             st.ffN = dot(st.N, st.V) > 0.0f ? st.N : -st.N;
           }
-          // brdf_pbr_metalness_roughness.rchit:156: the opacity test's draw
-          // comes first (pass-through, opacity > 0, is rejected at validation)
-          // brdf_disney.rchit:413 and brdf_kang18.rchit:183 likewise
-          if (CLS == kClsPbr || CLS == kClsDisney || CLS == kClsKang18) rnd(io.seed);
-          if (CLS == kClsPbr && depth == 1u && frame == 0u && sh.state.n_multi_channel > 0u) {
+          if (CLS == kClsPbr || CLS == kClsDisney || CLS == kClsKang18) {
+            // brdf_pbr_metalness_roughness.rchit:151-160, brdf_disney.rchit:
+            // 408-417, brdf_kang18.rchit:150-187: with probability opacity
+            // the ray goes on from the far side of the surface, same
+            // direction, no bounce counted (depth--), no light sample
+            float opacity = CLS == kClsPbr ? m.c.z : (CLS == kClsDisney ? m.b.y : m.c.w);
+            if (m.t1.z >= 0) opacity = texRGB(S, m.t1.z, st.u, st.v).x;
+            passThrough = rnd(io.seed) < opacity;
+          }
+          if (passThrough) {
+            io.nro = offsetPositionAlongNormal(st.pos, -st.ffN);
+            io.nrd = rd;
+          } else if (CLS == kClsPbr && depth == 1u && frame == 0u && sh.state.n_multi_channel > 0u) {
             // 169-174: albedo and the face-forward normal only
             const asuna_rt_state& ps = sh.state;
             const size_t npx = size_t(sh.width) * sh.height;
@@ -1206,8 +1218,8 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
             if (ps.normal_out_channel >= 0 && ps.normal_out_channel < ASUNA_MAX_CHANNELS)
               sh.filmCh[size_t(ps.normal_out_channel) * npx + pix] = make_float4(st.ffN.x, st.ffN.y, st.ffN.z, 1.0f);
           }
-          if ((CLS == kClsLambertian || CLS == kClsPhong || CLS == kClsKang18) && depth == 1u && frame == 0u &&
-              sh.state.n_multi_channel > 0u) {
+          if ((CLS == kClsLambertian || CLS == kClsPhong || CLS == kClsKang18) && !passThrough && depth == 1u &&
+              frame == 0u && sh.state.n_multi_channel > 0u) {
             // brdf_lambertian.rchit:93-108; brdf_phong.rchit:135-150 and
             // brdf_kang18.rchit:194-211 write the face-forward normal and the
             // specular reflectance (kang18: the rebuilt tangent, (ax, ay, 0))
@@ -1230,7 +1242,7 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
             // brdf_emissive.rchit:12-27: add the emitted radiance and stop
             io.stop = true;
             if (sh.state.ignore_emissive == 0u) io.rad = io.rad + ld3(m.a) * io.thp;
-          } else {
+          } else if (!passThrough) {
             constexpr uint32_t type = CLS == kClsRoughPlastic ? ASUNA_MAT_ROUGH_PLASTIC
                                       : CLS == kClsDielectric ? ASUNA_MAT_DIELECTRIC
                                       : CLS == kClsPlastic    ? ASUNA_MAT_PLASTIC
@@ -1274,8 +1286,10 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
         }
       }
       wantShadow = !io.dskip;
-      bool alive = !io.stop && depth < uint32_t(sh.state.max_path_depth);
-      if (CLS != kClsTerminal && alive && (sh.flags & ASUNA_SHOT_RR) && depth >= sh.rrDepth) {
+      // rgen:101-133: a pass-through leaves depth unchanged, so the loop goes on
+      bool alive = passThrough || (!io.stop && depth < uint32_t(sh.state.max_path_depth));
+      if (passThrough) ++passes;
+      if (CLS != kClsTerminal && alive && !passThrough && (sh.flags & ASUNA_SHOT_RR) && depth >= sh.rrDepth) {
         // Russian roulette (extension; off for the reference's streams)
         float q = gmin(0.95f, gmax(io.thp.x, gmax(io.thp.y, io.thp.z)));
         float u = rnd(io.seed);
@@ -1292,7 +1306,7 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
       // path state
       W.thp[p] = make_float4(io.thp.x, io.thp.y, io.thp.z, io.bpdf);
       W.rad[p] = make_float4(io.rad.x, io.rad.y, io.rad.z, r4.w);
-      W.info[p] = make_uint4(io.seed, io.bflags, inf.z, inf.w);
+      W.info[p] = make_uint4(io.seed, io.bflags | (passes << kPassShift), inf.z, inf.w);
       if (P.records) W.rec[p] = rc;
     }
     __syncwarp();

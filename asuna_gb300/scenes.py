@@ -258,7 +258,8 @@ def _plugin_textures(b, rng):
 
 
 def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=False, seed=11,
-                 channels=("albedo", "normal", "depth", "position", "uv", "tangent", "roughness"), textured=False):
+                 channels=("albedo", "normal", "depth", "position", "uv", "tangent", "roughness"), textured=False,
+                 opacity=False):
     """Every implemented plugin in one small scene: Lambertian, anisotropic
     rough plastic, dielectric, smooth plastic, mirror, conductor, rough
     conductor, Phong, PBR metalness-roughness, Disney (every lobe on) and
@@ -269,7 +270,9 @@ def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=Fa
     OpenCV pinhole camera.  `textured`: spherical UVs on the spheres and a
     texture in every slot the shaders read (diffuse, alpha, metalness and
     roughness, specular, tangent-space and object-space normal maps, tangent
-    map, emissive radiance)."""
+    map, emissive radiance).  `opacity`: the PBR, Disney and kang18 spheres
+    let rays pass through (opacity 0.35 / 0.5 / 0.3; Disney's from a mask
+    texture when `textured`)."""
     rng = np.random.default_rng(seed)
     b = SceneBuilder()
     b.add_rect_light((-1.0, 3.0, -1.0), (0.0, 3.0, -1.0), (-1.0, 3.0, 0.0), (6.0, 5.0, 4.0))
@@ -314,6 +317,14 @@ def plugin_scene(width=48, height=32, frames=3, max_depth=8, env=True, opencv=Fa
                                                                                             tx["diffuse"])
         M[kg].metalness_texture_id, M[kg].roughness_texture_id = tx["metal"], tx["alpha"]
         M[kg].normal_texture_id, M[kg].tangent_texture_id = tx["object_normal"], tx["tangent"]
+    if opacity:
+        b.materials[pb].specular = 0.35
+        b.materials[dn].rho_spec[0] = 0.5
+        b.materials[kg].metalness = 0.3
+        if textured:
+            yy, xx = np.mgrid[0:16, 0:32]
+            mask = np.repeat(((xx // 4 + yy // 4) % 2).astype(np.float32)[..., None], 3, 2) * 0.9
+            b.materials[dn].opacity_texture_id = b.add_texture("mask", mask)
     v, i = cuboid_mesh(0.15, 0.15, 0.15)
     b.add_mesh("lamp", v, i)
     b.add_instance("lamp", em, rot_y(30.0, (0.6, -0.85, 1.2)))

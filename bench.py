@@ -193,6 +193,8 @@ def run(args):
             print(f"autotune: {tuned}", file=sys.stderr, flush=True)
     else:
         ctx.set_path_budget(args.frames_per_step * shot.width * shot.height * BYTES_PER_PATH)
+        if args.traversal:
+            ctx.set_traversal(*(int(x) for x in args.traversal.split(",")))
     # per-rank frames: replicas render disjoint frames of the same shot
     from asuna_gb300 import replicas
 
@@ -436,6 +438,55 @@ def run_denoise_rmse(args):
     return 0
 
 
+def run_denoise_forward(args):
+    """Denoiser forward pass at the workload resolution (padded to 16):
+    device time per call on the context stream, tcgen05 and mma.sync
+    convolutions, against the measured dense bf16 peak."""
+    import torch
+
+    import asuna_gb300 as ag
+    from asuna_gb300 import denoise as dn
+
+    ctx = ag.Context(0)
+    stream = dn.ctx_stream(ctx)
+    H, W = args.height, args.width
+    rng = np.random.default_rng(0)
+    imgs = [torch.from_numpy(rng.uniform(0, 1, (1, H, W, 4)).astype(np.float32)).cuda() for _ in range(4)]
+    hp, wp = (H + 15) // 16 * 16, (W + 15) // 16 * 16
+    fl = dn.forward_flops(dn.DEFAULT_CHANNELS, hp, wp)
+    peak, kind = 1900.0, "fallback"
+    pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pp):
+        with open(pp) as f:
+            peak, kind = float(json.load(f)["bf16_tflops"]), "measured"
+    torch.cuda.synchronize()
+    res = {}
+    for tm in (True, False):
+        d = dn.Denoiser(ctx, seed=1, max_pixels=hp * wp, tensor_memory=tm)
+        out = torch.empty_like(imgs[0])
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                d.forward(*imgs, out=out)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(args.steps):
+                d.forward(*imgs, out=out)
+            e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        res["tcgen05" if tm else "mma_sync"] = {"ms": ms, "tflops": fl / (ms * 1e-3) / 1e12}
+        d.close()
+    tc = res["tcgen05"]
+    print(json.dumps({"metric": "denoiser forward TFLOP/s", "value": tc["tflops"], "unit": "TFLOP/s",
+                      "higher_is_better": True, "steps": args.steps, "warmup": args.warmup, "ms_per_step": tc["ms"],
+                      "config": {"workload": f"U-Net 32/48/64/96/128, 1 x {hp} x {wp}, bf16 NHWC, fp32 accumulation",
+                                 "flop": fl},
+                      "roofline": {"bound": "tensor", "achieved": tc["tflops"], "peak": peak, "unit": "TFLOP/s",
+                                   "frac": tc["tflops"] / peak, "peak_kind": kind},
+                      "variants": res}), flush=True)
+    return 0
+
+
 SERVE_SCENES = [(4, 7), (16, 6), (16, 7), (24, 7), (32, 7), (48, 7), (64, 6), (64, 7)]  # (spheres, level): 1.3M-21M triangles
 
 
@@ -560,6 +611,9 @@ def main():
     ap.add_argument("--spheres", type=int, default=64)
     ap.add_argument("--level", type=int, default=7)
     ap.add_argument("--frames-per-step", type=int, default=0, help="0 = autotune")
+    ap.add_argument("--traversal", default="",
+                    help="with --frames-per-step: refill extend,refill shadow,speculate extend,speculate shadow,"
+                         "blocks per SM (the autotuner's traversal tuple)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -579,6 +633,7 @@ def main():
     ap.add_argument("--train-crop", type=int, default=128)
     ap.add_argument("--train-loss", default="l1log", choices=("l1log", "relmse"),
                     help="L1 on log radiance, or relative MSE (unbiased with noisy targets)")
+    ap.add_argument("--denoise-forward", action="store_true", help="denoiser forward pass at the workload size")
     ap.add_argument("--serve", action="store_true", help="serving loop: Poisson arrivals, latency percentiles")
     ap.add_argument("--batch", action="store_true", help="32 batched shots vs 32 sequential calls")
     ap.add_argument("--serve-rate", type=float, default=20.0)
@@ -592,6 +647,8 @@ def main():
         return run_reference(args)
     if args.denoise_rmse:
         return run_denoise_rmse(args)
+    if args.denoise_forward:
+        return run_denoise_forward(args)
     if args.serve:
         return run_serve(args)
     if args.batch:

@@ -88,6 +88,12 @@ enum {
  * 1..7 = multi-channel AOVs, 8 = filter-weight sum (src/shared/binding.h:70). */
 #define ASUNA_NUM_OUTPUT_IMAGES 9
 #define ASUNA_MAX_CHANNELS 7
+/* Opacity pass-throughs (brdf_pbr_metalness_roughness / brdf_disney /
+ * brdf_kang18: a ray that passes a surface without counting a bounce) a path
+ * may take in one render beyond its max_path_depth bounces; a path that needs
+ * more ends there.  Only scenes whose materials can pass rays run the extra
+ * wavefront passes. */
+#define ASUNA_MAX_PASS_THROUGH 24
 
 /* AOV channel kinds; "multi_channel" strings of src/loader/loader.cpp:177-183.
  * ASUNA_CH_DEPTH (primary-hit distance) is an addition of this library. */

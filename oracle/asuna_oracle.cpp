@@ -724,6 +724,7 @@ struct PathState {
   V3<R> radiance, throughput;
   uint32_t depth, seed;
   bool stop;
+  bool passed;  // this hit passed the ray through (opacity): no bounce counted
   uint32_t bflags;
   R bpdf;
   V3<R> ch[ASUNA_MAX_CHANNELS];
@@ -1425,6 +1426,19 @@ template <class R> void shadePhong(const Scene& s, const asuna_shot& sh, PathSta
   p.throughput = p.throughput * (weight / bpdf);
 }
 
+// brdf_pbr_metalness_roughness.rchit:151-160 (brdf_disney.rchit:408-417,
+// brdf_kang18.rchit:150-187 alike): with probability `opacity` the ray goes
+// on from the far side of the surface in the same direction and the bounce
+// is not counted (depth--); nothing else of the hit runs.
+template <class R> bool passThrough(const Scene& s, PathState<R>& p, HitState<R>& st, R opacity) {
+  if (st.mat.opacity_texture_id >= 0) opacity = texRGB(s, st.mat.opacity_texture_id, st.uv).x;
+  if (!(rnd<R>(p.seed) < opacity)) return false;
+  p.ro = offsetPositionAlongNormal(st.pos, -st.ffN);
+  p.depth--;
+  p.passed = true;
+  return true;
+}
+
 // brdf_pbr_metalness_roughness.rchit:14-16 (GLSL mix: x (1 - a) + y a)
 template <class R> V3<R> fresnelSchlick(R cosThetaI, V3<R> f0) {
   return f0 + (splat(R(1)) - f0) * mpow(gclamp(R(1) - cosThetaI, R(0), R(1)), R(5));
@@ -1474,9 +1488,7 @@ template <class R> void shadePbr(const Scene& s, const asuna_shot& sh, PathState
   V3<R> albedo = L3<R>(st.mat.diffuse);
   R metalness = R(st.mat.metalness), roughness = R(st.mat.roughness);
   R opacity = R(st.mat.specular);
-  // 156-160: the pass-through branch (opacity > 0) is rejected at scene
-  // validation; the draw is kept
-  (void)(rnd<R>(p.seed) < opacity);
+  if (passThrough(s, p, st, opacity)) return;
   R ax = gmax(sqr(roughness), R(0.001f)), ay = ax;
   R eta = R(st.mat.ior);
   if (p.depth == 1) {
@@ -1705,8 +1717,7 @@ V3<R> disneyEval(V3<R> L, V3<R> V, V3<R> N, V3<R> X, V3<R> Y, const DisneyMat<R>
 template <class R> void shadeDisney(const Scene& s, const asuna_shot& sh, PathState<R>& p, HitState<R>& st) {
   const asuna_material& m = st.mat;
   R opacity = R(m.rho_spec[0]);
-  // 413-417: pass-through (opacity > 0) is rejected at scene validation
-  (void)(rnd<R>(p.seed) < opacity);
+  if (passThrough(s, p, st, opacity)) return;
   DisneyMat<R> mat;
   {
     R rough = R(m.roughness);
@@ -1845,8 +1856,7 @@ template <class R> void shadeKang18(const Scene& s, const asuna_shot& sh, PathSt
   st.Y = makeNormal(cross(st.N, st.X));
   st.X = makeNormal(cross(st.Y, st.N));
   st.ffN = dot(st.N, st.V) > R(0) ? st.N : -st.N;
-  // 183-187: pass-through (opacity > 0) is rejected at scene validation
-  (void)(rnd<R>(p.seed) < opacity);
+  if (passThrough(s, p, st, opacity)) return;
   R ax = gmax(R(st.mat.aniso_alpha[0]), K<R>::EPS), ay = gmax(R(st.mat.aniso_alpha[1]), K<R>::EPS);
   R eta = R(st.mat.ior);
   if (p.depth == 1) {
@@ -2081,9 +2091,13 @@ void tracePath(const Scene& s, const asuna_shot& sh, uint32_t x, uint32_t y, uin
   uint32_t events = 0, shadows = 0;
   R t1 = R(0);  // primary-hit distance (depth channel, an extension)
   const bool rr = (sh.flags & ASUNA_SHOT_RR) != 0;
-  // rgen:102-132
+  // rgen:102-132; the wavefront runs at most max_path_depth +
+  // ASUNA_MAX_PASS_THROUGH passes, and so does this loop
+  uint32_t iters = 0;
   for (p.depth = 1; p.depth <= uint32_t(ps.max_path_depth);) {
+    if (++iters > uint32_t(ps.max_path_depth) + ASUNA_MAX_PASS_THROUGH) break;
     p.dskip = true;
+    p.passed = false;
     p.drad = splat(R(0));
     float of[3] = {float(p.ro.x), float(p.ro.y), float(p.ro.z)}, df[3] = {float(p.rd.x), float(p.rd.y), float(p.rd.z)};
     Hit h;
@@ -2157,7 +2171,7 @@ void tracePath(const Scene& s, const asuna_shot& sh, uint32_t x, uint32_t y, uin
     }
     if (p.stop) break;
     // Russian roulette (extension, off for the reference's streams).
-    if (rr && p.depth >= sh.rr_depth) {
+    if (rr && !p.passed && p.depth >= sh.rr_depth) {
       R q = gmin(R(0.95), gmax(p.throughput.x, gmax(p.throughput.y, p.throughput.z)));
       R u = rnd<R>(p.seed);
       if (!(u < q)) break;

@@ -27,6 +27,8 @@ CASES = {
     "plugins_textured_40x28x2": lambda: scenes.plugin_scene(40, 28, frames=2, env=True, textured=True,
                                                             channels=("albedo", "normal", "tangent", "roughness",
                                                                       "specular", "uv")),
+    "plugins_opacity_40x28x3": lambda: scenes.plugin_scene(40, 28, frames=3, env=True, textured=True, opacity=True,
+                                                           channels=("albedo", "normal", "depth")),
 }
 
 

@@ -62,13 +62,15 @@ def test_every_plugin(ctx, env, opencv):
     _check(rec, orec, imgs, ofilm, film_tol=5e-3)
 
 
-@pytest.mark.parametrize("face_normal", [0, 1])
-def test_every_plugin_textured(ctx, face_normal):
+@pytest.mark.parametrize("face_normal,opacity", [(0, False), (1, False), (0, True)])
+def test_every_plugin_textured(ctx, face_normal, opacity):
     """Every texture slot the shaders read (diffuse, alpha, metalness and
     roughness, specular, tangent- and object-space normal maps, tangent map,
     emissive radiance); with use_face_normal the normal maps must have no
-    effect, as configureShadingFrame puts the geometric normal back."""
-    b, shot = scenes.plugin_scene(96, 64, frames=4, max_depth=8, env=True, textured=True,
+    effect, as configureShadingFrame puts the geometric normal back.  With
+    `opacity`, PBR / Disney (mask texture) / kang18 pass rays through
+    without counting a bounce, which the wavefront tracks per path."""
+    b, shot = scenes.plugin_scene(96, 64, frames=4, max_depth=8, env=True, textured=True, opacity=opacity,
                                   channels=("albedo", "normal", "tangent", "roughness", "specular", "uv"))
     shot.state.use_face_normal = face_normal
     rec, orec, imgs, ofilm = _run(ctx, b, shot)
