@@ -412,14 +412,31 @@ def run_denoise_rmse(args):
         ms += est_ms
         used = "denoised" if err_d <= target and err_d <= err_p else "plain"
         e_full = rmse(full[0].cpu().numpy())
-        e = e_full if used == "denoised" else rmse(0.5 * (fa.read(0) + fb.read(0)))
+        e_avg = rmse(0.5 * (fa.read(0) + fb.read(0)))
+        e = e_full if used == "denoised" else e_avg
         dres.append({"spp": 2 * half, "seconds": ms / 1e3, "estimate_ms": est_ms, "err_estimate": err_d,
                      "err_plain_estimate": err_p, "output": used, "rmse": e,
-                     "rmse_denoised_half": rmse(img.cpu().numpy()), "rmse_denoised_all": e_full})
+                     "rmse_denoised_half": rmse(img.cpu().numpy()), "rmse_denoised_all": e_full,
+                     "rmse_plain_average": e_avg})
         if e <= target:
             t_den = ms / 1e3
             break
     out["denoised"] = {"ladder": dres, "seconds_at_target": t_den, "reached": t_den is not None}
+    # the same ladders at other targets: plain by the 1/sqrt(spp) law from its
+    # last rung; denoised = the first rung whose output (chosen by the error
+    # estimate for that target) is below it
+    rows = []
+    for tgt in (0.05, 0.03, 0.02, target):
+        tp = last["seconds"] / last["spp"] * last["spp"] * (last["rmse"] / tgt) ** 2
+        td = None
+        for r in dres:
+            den_ok = r["err_estimate"] <= tgt and r["err_estimate"] <= r["err_plain_estimate"]
+            if (r["rmse_denoised_all"] if den_ok else r["rmse_plain_average"]) <= tgt:
+                td = r["seconds"]
+                break
+        rows.append({"rmse": tgt, "plain_seconds": tp, "denoised_seconds": td,
+                     "speedup": (tp / td) if td else None})
+    out["targets"] = rows
     # denoiser forward throughput at 1080p
     with torch.cuda.stream(stream):
         for _ in range(3):
@@ -622,7 +639,7 @@ def main():
                     help="time to RMSE 0.01 vs the FP64 reference, plain vs denoised path")
     ap.add_argument("--rmse-target", type=float, default=0.01)
     ap.add_argument("--plain-max-spp", type=int, default=32768)
-    ap.add_argument("--denoise-max-spp", type=int, default=4096)
+    ap.add_argument("--denoise-max-spp", type=int, default=8192)
     ap.add_argument("--train-scenes", type=int, default=64)
     ap.add_argument("--train-size", type=int, default=256)
     ap.add_argument("--train-spp-in", default="4,16,64,256,1024")
