@@ -180,6 +180,7 @@ SIGNATURES = [
     ("asuna_diffuse_fresnel", C.c_float, [C.c_float, C.c_int]),
     ("asuna_complex_ior", C.c_int, [C.c_char_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     ("asuna_tracer_run_offline", C.c_int, [P, C.c_char_p, C.c_char_p]),
+    ("asuna_tracer_run_offline_scanline", C.c_int, [P, C.c_char_p, C.c_char_p, C.c_int]),
     ("asuna_post_default", None, [C.POINTER(PostState)]),
     ("asuna_tonemap", C.c_int, [P, P, C.c_int, C.POINTER(PostState), P]),
     ("asuna_json_post_state", C.c_int, [P, C.POINTER(PostState)]),

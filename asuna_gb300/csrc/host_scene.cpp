@@ -641,6 +641,27 @@ int loadImageRGBA(const std::string& path, uint32_t& w, uint32_t& h, std::vector
               ext.c_str());
 }
 
+// NumPy .npy, format 1.0: magic, little-endian header dict padded with
+// spaces to a 64-byte boundary, then the float32 rows (C order).
+int writeNpy(const std::string& path, uint64_t rows, uint32_t cols, const float* data) {
+  std::string hdr = "{'descr': '<f4', 'fortran_order': False, 'shape': (" + std::to_string(rows) + ", " +
+                    std::to_string(cols) + "), }";
+  const size_t pre = 10;  // magic (6) + version (2) + header length (2)
+  size_t total = pre + hdr.size() + 1;
+  hdr.append((64 - total % 64) % 64, ' ');
+  hdr.push_back('\n');
+  std::ofstream f(path, std::ios::binary);
+  if (!f) return fail(ASUNA_ERR_IO, "cannot write %s", path.c_str());
+  const unsigned char magic[8] = {0x93, 'N', 'U', 'M', 'P', 'Y', 1, 0};
+  f.write(reinterpret_cast<const char*>(magic), 8);
+  const uint16_t n = uint16_t(hdr.size());
+  const unsigned char len[2] = {static_cast<unsigned char>(n & 0xff), static_cast<unsigned char>(n >> 8)};
+  f.write(reinterpret_cast<const char*>(len), 2);
+  f.write(hdr.data(), std::streamsize(hdr.size()));
+  f.write(reinterpret_cast<const char*>(data), std::streamsize(rows * cols * sizeof(float)));
+  return f ? ASUNA_OK : fail(ASUNA_ERR_IO, "write failed: %s", path.c_str());
+}
+
 int writePfm(const std::string& path, uint32_t w, uint32_t h, const float* rgba) {
   std::ofstream f(path, std::ios::binary);
   if (!f) return fail(ASUNA_ERR_IO, "cannot write %s", path.c_str());
@@ -1575,6 +1596,11 @@ int asuna_json_channels(const asuna_json_scene* js, uint32_t* n, int32_t* kinds)
 // goes through its tonemapping post pass, which is outside this path, so the
 // radiance is always written as HDR.
 int asuna_tracer_run_offline(asuna_ctx* ctx, const char* scene_json, const char* out_prefix) {
+  return asuna_tracer_run_offline_scanline(ctx, scene_json, out_prefix, 0);
+}
+
+int asuna_tracer_run_offline_scanline(asuna_ctx* ctx, const char* scene_json, const char* out_prefix,
+                                      int output_scanline) {
   clearError();
   if (!ctx || !scene_json || !out_prefix) return fail(ASUNA_ERR_INVALID, "null argument");
   asuna_json_scene* js = nullptr;
@@ -1618,12 +1644,28 @@ int asuna_tracer_run_offline(asuna_ctx* ctx, const char* scene_json, const char*
       std::snprintf(name, sizeof(name), "_shot_%04u.png", i);
       if ((rc = writePng(out_prefix + std::string(name), S.width, S.height, px.data()))) return rc;
     }
+    std::vector<uint32_t> valid;  // scanline mode: pixels whose first channel has .z == 1
     for (uint32_t c = 0; c < S.state.rtx.n_multi_channel; ++c) {
       const bool ldr = c < S.state.channelLdr.size() && S.state.channelLdr[c];
       std::snprintf(name, sizeof(name), "_shot_%04u_channel_%04u.%s", i, c, ldr ? "png" : "exr");
       if ((rc = asuna_film_read(ctx, film, int(c + 1), px.data()))) return rc;
-      rc = ldr ? writePng(out_prefix + std::string(name), S.width, S.height, px.data())
-               : writeExr(out_prefix + std::string(name), S.width, S.height, px.data());
+      if (output_scanline) {
+        if (c == 0) {
+          valid.clear();
+          for (uint32_t k = 0; k < S.width * S.height; ++k)
+            if (px[size_t(k) * 4 + 2] == 1.0f) {
+              valid.push_back(k);
+              px[size_t(k) * 4 + 2] = float(k);
+            }
+        }
+        std::vector<float> rows(valid.size() * 3);
+        for (size_t k = 0; k < valid.size(); ++k)
+          for (int j = 0; j < 3; ++j) rows[k * 3 + j] = px[size_t(valid[k]) * 4 + j];
+        rc = writeNpy(out_prefix + std::string(name), uint64_t(valid.size()), 3, rows.data());
+      } else {
+        rc = ldr ? writePng(out_prefix + std::string(name), S.width, S.height, px.data())
+                 : writeExr(out_prefix + std::string(name), S.width, S.height, px.data());
+      }
       if (rc) return rc;
     }
   }

@@ -78,6 +78,7 @@ int loadImageRGBA(const std::string& path, uint32_t& w, uint32_t& h, std::vector
 int writePfm(const std::string& path, uint32_t w, uint32_t h, const float* rgba);
 int writeExr(const std::string& path, uint32_t w, uint32_t h, const float* rgba);
 int writePng(const std::string& path, uint32_t w, uint32_t h, const float* rgba);
+int writeNpy(const std::string& path, uint64_t rows, uint32_t cols, const float* data);
 
 // Scene-file loader (src/loader/loader.cpp:67-468, src/loader/material.cpp).
 int loadSceneJson(const std::string& text, const std::string& baseDir, HostScene& scene);

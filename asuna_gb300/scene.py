@@ -567,8 +567,11 @@ class Context:
         self.sync()
         return out.cpu().numpy()
 
-    def run_offline(self, scene_json, out_prefix):
-        check(lib().asuna_tracer_run_offline(self.handle, scene_json.encode(), out_prefix.encode()))
+    def run_offline(self, scene_json, out_prefix, output_scanline=False):
+        """The offline tracer on a scene file; `output_scanline` is the CLI's
+        --output_scanline (AOV channels as [n, 3] .npy arrays of hit pixels)."""
+        check(lib().asuna_tracer_run_offline_scanline(self.handle, scene_json.encode(), out_prefix.encode(),
+                                                      1 if output_scanline else 0))
 
     def close(self):
         if getattr(self, "handle", None):

@@ -527,6 +527,13 @@ int asuna_tonemap(asuna_ctx* ctx, asuna_film* film, int image, const asuna_post_
  * (output_hdr) or the tone-mapped _shot_%04d.png, + _channel_%04d.exr/.png
  * per AOV: the offline mode of Tracer::runOffline. */
 int asuna_tracer_run_offline(asuna_ctx* ctx, const char* scene_json, const char* out_prefix);
+/* The same with the CLI's --output_scanline (src/main.cpp:21,
+ * tracer.cpp:347-395): each AOV channel is written as a [n, 3] float32 NumPy
+ * array of the pixels whose channel-0 .z is 1 (a hit, for the uv channel),
+ * with that channel's .z replaced by the pixel index; the file keeps its
+ * _channel_%04d.exr / .png name, as the reference's does. */
+int asuna_tracer_run_offline_scanline(asuna_ctx* ctx, const char* scene_json, const char* out_prefix,
+                                      int output_scanline);
 
 #ifdef __cplusplus
 } /* extern "C" */

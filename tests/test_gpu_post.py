@@ -139,3 +139,40 @@ def test_offline_outputs(tmp_path, output_hdr):
     # AOV channels: albedo as PNG (multi_channel_ldr), normal as EXR
     assert np.array_equal(read_png(prefix + "_shot_0000_channel_0000.png"), to8(f.read(1)).astype(np.uint8))
     assert np.array_equal(read_exr(prefix + "_shot_0000_channel_0001.exr", 40, 32), f.read(2))
+
+
+def test_offline_scanline_outputs(tmp_path):
+    """--output_scanline (tracer.cpp:347-395): the AOV channels as [n, 3]
+    float32 .npy arrays (under their image names) of the pixels whose first
+    channel has .z == 1, the first channel's .z holding the pixel index."""
+    obj = tmp_path / "quad.obj"
+    obj.write_text("v -1 -1 0\nv 1 -1 0\nv 1 1 0\nv -1 1 0\nvn 0 0 1\nvt 0 0\nvt 1 0\nvt 1 1\nvt 0 1\n"
+                   "f 1/1/1 2/2/1 3/3/1\nf 1/1/1 3/3/1 4/4/1\n")
+    scene = {
+        "state": {"path_tracing": {"spp": 2, "max_path_depth": 3, "multi_channel": ["uv", "normal"]},
+                  "output_hdr": True},
+        "camera": {"type": "perspective", "fov": 45.0, "film": {"resolution": [40, 32]}},
+        "materials": [{"type": "brdf_lambertian", "name": "white", "diffuse_reflectance": [0.7, 0.6, 0.5]}],
+        "lights": [{"type": "point", "position": [0, 0, 2], "radiance": [4, 4, 4]}],
+        "meshes": [{"name": "quad", "path": "quad.obj"}],
+        "instances": [{"mesh": "quad", "material": "white"}],
+        "shots": [{"type": "lookat", "eye": [0, 0, 4], "lookat": [0, 0, 0], "up": [0, 1, 0]}],
+    }
+    path = tmp_path / "scene.json"
+    path.write_text(json.dumps(scene))
+    ctx = ag.Context(0)
+    prefix = str(tmp_path / "out")
+    ctx.run_offline(str(path), prefix, output_scanline=True)
+    js = ag.JsonScene(str(path))
+    f = ctx.create_film(40, 32)
+    ctx.render(ctx.create_scene(js.desc()), js.shots()[0], f)
+    uv, nrm = f.read(1).reshape(-1, 4), f.read(2).reshape(-1, 4)
+    valid = np.nonzero(uv[:, 2] == 1.0)[0]
+    assert 0 < valid.size < 40 * 32  # the quad covers part of the frame
+    a = np.load(prefix + "_shot_0000_channel_0000.exr")
+    b = np.load(prefix + "_shot_0000_channel_0001.exr")
+    assert a.dtype == np.float32 and a.shape == (valid.size, 3) and b.shape == (valid.size, 3)
+    assert np.array_equal(a[:, :2], uv[valid, :2]) and np.array_equal(a[:, 2], valid.astype(np.float32))
+    assert np.array_equal(b, nrm[valid, :3])
+    # the shot image itself stays an image
+    assert np.array_equal(read_exr(prefix + "_shot_0000.exr", 40, 32), f.read(0))
