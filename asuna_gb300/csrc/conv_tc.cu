@@ -2,26 +2,28 @@
 // fifth-generation tensor cores: tcgen05.mma with the accumulator in tensor
 // memory, operands staged in shared memory by TMA.
 //
-// One CTA computes a 16 x 8 pixel tile (M = 128) for one slice of nt output
-// channels (N = nt, a multiple of 16, at most 256 and small enough that three
-// weight stages fit shared memory; cout is split into cout / nt slices, the
-// slice index varying fastest across the grid so the CTAs that read one
-// activation tile run together and share it in L2).  The input channels are
-// consumed in groups of 16 (K = 16 per MMA):
+// One CTA computes T (up to 4) 16 x 8 pixel tiles side by side in x (M = 128
+// each, one TMEM accumulator per tile) for one slice of nt output channels
+// (N = nt, a multiple of 16, at most 256 and small enough that three weight
+// stages fit shared memory; cout is split into cout / nt slices, the slice
+// index varying fastest across the grid so the CTAs that read one activation
+// region run together and share it in L2).  The T tiles share every weight
+// stage, so weights are fetched once per 128 T pixels.  The input channels
+// are consumed in groups of 16 (K = 16 per MMA):
 //   * activations: for each 8-channel chunk, one TMA tiled load of the
-//     18 x 10 halo of the tile from the NHWC tensor (zero fill outside the
-//     image) lands as [row][col][8] bf16 (blocks 2,944 B apart, 128-byte
-//     aligned); for tap (dy, dx) the A operand is the view starting at
-//     pixel (dy, dx) of that halo: 8-row core matrices are 8 consecutive
-//     pixels of one image row, image rows are 160 B apart (stride
-//     dimension), the second 8-channel chunk is one block further (leading
+//     18 x (8T + 2) halo of the tiles from the NHWC tensor (zero fill outside
+//     the image) lands as [row][col][8] bf16 (slots padded to 128 B); for tap
+//     (dy, dx) and tile t the A operand is the view starting at pixel
+//     (dy, dx + 8t) of that halo: 8-row core matrices are 8 consecutive
+//     pixels of one image row, image rows are (8T + 2) * 16 B apart (stride
+//     dimension), the second 8-channel chunk is one slot further (leading
 //     dimension) — K-major, no swizzle;
 //   * weights: pre-arranged as [slice][cin/16][tap][chunk][nt][8] so one
 //     group's nine taps are one contiguous bulk copy, B = [chunk][nt][8] per
 //     tap;
-//   * nine MMAs per group accumulate into TMEM (fp32, lane = pixel,
-//     column = output channel); a 3-stage ring of shared-memory buffers is
-//     refilled as tcgen05.commit reports each stage's MMAs done.
+//   * 9 T MMAs per group accumulate into TMEM (fp32, lane = pixel of a tile,
+//     column = tile t * nt + output channel); a 3-stage ring of shared-memory
+//     buffers is refilled as tcgen05.commit reports each stage's MMAs done.
 // One elected thread issues the copies and the MMAs; after the last group
 // the four warps read their 32 TMEM lanes each (tcgen05.ld), apply bias,
 // ReLU and the ReLU mask and store bf16 (or fp32).  Every mbarrier wait is
@@ -42,28 +44,48 @@ namespace asuna {
 namespace tc {
 namespace {
 
-constexpr int kTileH = 16, kTileW = 8;                         // pixels per CTA (M = 128)
-constexpr int kHaloH = kTileH + 2, kHaloW = kTileW + 2;
-constexpr int kBoxBytes = kHaloH * kHaloW * 16;  // bytes one TMA box of 8 channels transfers: 2,880
-constexpr int kChunkBytes = 2944;                  // its shared-memory slot, padded to 128 B
-constexpr int kActStage = 2 * kChunkBytes;  // 16 channels
+constexpr int kTileH = 16, kTileW = 8;                         // pixels per MMA tile (M = 128)
+constexpr int kHaloH = kTileH + 2;
+constexpr int kMaxTiles = 4;                                   // tiles per CTA, side by side in x
 constexpr int kStages = 3;
+// One TMA box of 8 channels covers the halo of T tiles: 18 x (8T + 2) pixels
+// of 16 bytes; its shared-memory slot is padded to 128 bytes.
+__host__ __device__ constexpr int haloW(int T) { return kTileW * T + 2; }
+__host__ __device__ constexpr int boxBytes(int T) { return kHaloH * haloW(T) * 16; }
+__host__ __device__ constexpr int chunkBytes(int T) { return (boxBytes(T) + 127) / 128 * 128; }
+__host__ __device__ constexpr int actStage(int T) { return 2 * chunkBytes(T); }  // 16 channels
 constexpr int kThreads = 128;
-constexpr int kPadBytes = 48 * 1024;                           // slack past the operands
 constexpr uint32_t kWaitLimit = 1u << 20;                      // try_wait rounds before giving up
 
 __device__ int g_tcError;  // set when a wait expired; read and cleared by asuna_nn_tc_status
 
 constexpr size_t kSmemLimit = 227 * 1024;
-size_t smemFor(int nt) { return 128 + size_t(kStages) * (kActStage + size_t(9 * 2 * nt * 16)) + kPadBytes; }
+// Every MMA operand view stays inside its stage: the A view of tile T-1 at
+// tap (2, 2) ends at ((2 * haloW + 2 + 8 (T-1)) + 15 haloW + 8) * 16 bytes =
+// 17 haloW * 16 = boxBytes, the end of the halo box, and the second 8-channel
+// chunk's at chunkBytes + boxBytes <= actStage.
+size_t smemFor(int nt, int T) { return 128 + size_t(kStages) * (actStage(T) + size_t(9 * 2 * nt * 16)); }
+uint32_t pow2Cols(int n) {
+  uint32_t c = 32;
+  while (c < uint32_t(n)) c <<= 1;
+  return c;
+}
 // Output channels per CTA: the widest slice (fewest slices) that divides cout
-// into multiples of 16 and whose stages fit shared memory.
+// into multiples of 16 and whose one-tile stages fit shared memory.
 int sliceWidth(int cout) {
   for (int s = 1; s <= cout / 16; ++s) {
     const int nt = cout / s;
-    if (cout % s == 0 && nt % 16 == 0 && nt <= 256 && smemFor(nt) <= kSmemLimit) return nt;
+    if (cout % s == 0 && nt % 16 == 0 && nt <= 256 && smemFor(nt, 1) <= kSmemLimit) return nt;
   }
   return 16;
+}
+// Pixel tiles per CTA: as many (up to 4) as tensor memory (T accumulators of
+// nt columns in 512) and shared memory hold and the image width uses; the
+// tiles share every weight stage.
+int tilesPerCta(int nt, int w) {
+  int T = kMaxTiles;
+  while (T > 1 && (pow2Cols(T * nt) > 512 || smemFor(nt, T) > kSmemLimit || kTileW * (T - 1) >= w)) --T;
+  return T;
 }
 
 __device__ __forceinline__ uint32_t smem(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
@@ -143,7 +165,8 @@ struct TcArgs {
   void* out;                  // [P][cout]
   int n, h, w, cin, cout;
   int nt, slices;             // output channels per CTA, cout / nt
-  int tilesX, tilesY;
+  int tiles;                  // 16 x 8 pixel tiles per CTA, side by side in x
+  int tilesX, tilesY;         // CTA regions (16 x 8 tiles pixels) per image
   int relu, outF32;
   uint32_t tmemCols;
   uint32_t wStageBytes;  // 9 * 2 * nt * 16
@@ -151,14 +174,16 @@ struct TcArgs {
 
 __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__ CUtensorMap act, TcArgs a) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  // [0, 128): barriers and the TMEM address; then activation stages, weight stages, slack
+  // [0, 128): barriers and the TMEM address; then activation stages, weight stages
   uint64_t* full = reinterpret_cast<uint64_t*>(sm);
   uint64_t* empty = full + kStages;
   uint64_t* done = empty + kStages;
   uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(done + 1);
   int* abortFlag = reinterpret_cast<int*>(tmemSlot + 1);
+  const int T = a.tiles, hw = haloW(T);
+  const uint32_t chunk = uint32_t(chunkBytes(T)), stageA = uint32_t(actStage(T));
   unsigned char* actBase = sm + 128;
-  unsigned char* wBase = actBase + kStages * kActStage;
+  unsigned char* wBase = actBase + kStages * stageA;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   int t = blockIdx.x;
@@ -170,7 +195,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
   t /= a.tilesX;
   const int ty = t % a.tilesY;
   const int img = t / a.tilesY;
-  const int x0 = tx * kTileW, y0 = ty * kTileH;
+  const int x0 = tx * kTileW * T, y0 = ty * kTileH;
 
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -201,10 +226,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
     const uint32_t idesc = instrDesc(uint32_t(a.nt));
     auto issue = [&](int s, int g) {
       const uint32_t bar = smem(&full[s]);
-      mbarExpectTx(bar, uint32_t(2 * kBoxBytes) + a.wStageBytes);
-      const uint32_t dstA = smem(actBase + s * kActStage);
+      mbarExpectTx(bar, uint32_t(2 * boxBytes(T)) + a.wStageBytes);
+      const uint32_t dstA = smem(actBase + s * stageA);
       tmaLoad4d(dstA, &act, g * 16, x0 - 1, y0 - 1, img, bar);
-      tmaLoad4d(dstA + kChunkBytes, &act, g * 16 + 8, x0 - 1, y0 - 1, img, bar);
+      tmaLoad4d(dstA + chunk, &act, g * 16 + 8, x0 - 1, y0 - 1, img, bar);
       bulkLoad(smem(wBase + size_t(s) * a.wStageBytes), wt + size_t(g) * (a.wStageBytes / 2), a.wStageBytes, bar);
     };
     bool ok = true;
@@ -216,15 +241,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
         ok = false;
         break;
       }
-      const uint32_t aBase = smem(actBase + s * kActStage);
+      const uint32_t aBase = smem(actBase + s * stageA);
       const uint32_t bBase = smem(wBase + size_t(s) * a.wStageBytes);
       const uint32_t bTap = uint32_t(2 * a.nt * 16);
 #pragma unroll 1
       for (int tap = 0; tap < 9; ++tap) {
         const int dy = tap / 3, dx = tap % 3;
-        const uint64_t da = matDesc(aBase + uint32_t(dy * kHaloW + dx) * 16u, kChunkBytes, kHaloW * 16);
         const uint64_t db = matDesc(bBase + uint32_t(tap) * bTap, uint32_t(a.nt * 16), 128u);
-        mma(tmem, da, db, idesc, (g > 0 || tap > 0) ? 1u : 0u);
+        // tile t: the view starting 8 t pixels further along the halo rows;
+        // its accumulator is columns [t nt, (t + 1) nt) of tensor memory
+        for (int t2 = 0; t2 < T; ++t2) {
+          const uint64_t da = matDesc(aBase + uint32_t(dy * hw + dx + kTileW * t2) * 16u, chunk, uint32_t(hw * 16));
+          mma(tmem + uint32_t(t2 * a.nt), da, db, idesc, (g > 0 || tap > 0) ? 1u : 0u);
+        }
       }
       commit(smem(&empty[s]));
       const int gn = g + kStages;
@@ -249,15 +278,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
   __syncthreads();
   fenceAfter();
   if (!*abortFlag) {
-    // epilogue: warp w owns TMEM lanes 32w..32w+31 = tile pixels 32w..32w+31
+    // epilogue: warp w owns TMEM lanes 32w..32w+31 = pixels 32w..32w+31 of each tile
     const int m = warp * 32 + lane;
-    const int py = y0 + m / kTileW, px = x0 + m % kTileW;
-    const bool inside = py < a.h && px < a.w;
-    const size_t p = (size_t(img) * a.h + py) * a.w + px;
     const uint32_t laneBase = tmem + (uint32_t(warp * 32) << 16);
+    for (int t2 = 0; t2 < T; ++t2)
     for (int c0 = 0; c0 < a.nt; c0 += 16) {
+      const int py = y0 + m / kTileW, px = x0 + kTileW * t2 + m % kTileW;
+      const bool inside = py < a.h && px < a.w;
+      const size_t p = (size_t(img) * a.h + py) * a.w + px;
       float v[16];
-      ld16(laneBase + uint32_t(c0), v);
+      ld16(laneBase + uint32_t(t2 * a.nt + c0), v);
       if (!inside) continue;
 #pragma unroll
       for (int i = 0; i < 16; i += 2) {
@@ -348,11 +378,12 @@ int asuna_nn_conv3x3_tc(void* stream, const void* in, int n, int h, int w, int c
     return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: operands must be 16-byte aligned");
   EncodeTiledFn enc = encodeFn();
   if (!enc) return fail(ASUNA_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
-  // NHWC bf16 as a 4-D tensor (C, W, H, N); box = 8 channels x halo
+  const int nt = sliceWidth(cout), T = tilesPerCta(nt, w);
+  // NHWC bf16 as a 4-D tensor (C, W, H, N); box = 8 channels x the T tiles' halo
   CUtensorMap map;
   const cuuint64_t dims[4] = {cuuint64_t(cin), cuuint64_t(w), cuuint64_t(h), cuuint64_t(n)};
   const cuuint64_t strides[3] = {cuuint64_t(cin) * 2, cuuint64_t(w) * cin * 2, cuuint64_t(h) * w * cin * 2};
-  const cuuint32_t box[4] = {8, kHaloW, kHaloH, 1};
+  const cuuint32_t box[4] = {8, cuuint32_t(haloW(T)), kHaloH, 1};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   const CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(in), dims, strides, box, estr,
                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -368,15 +399,16 @@ int asuna_nn_conv3x3_tc(void* stream, const void* in, int n, int h, int w, int c
   a.w = w;
   a.cin = cin;
   a.cout = cout;
-  a.tilesX = (w + kTileW - 1) / kTileW;
+  a.tiles = T;
+  a.tilesX = (w + kTileW * T - 1) / (kTileW * T);
   a.tilesY = (h + kTileH - 1) / kTileH;
   a.relu = relu;
   a.outF32 = out_f32;
-  a.nt = sliceWidth(cout);
+  a.nt = nt;
   a.slices = cout / a.nt;
-  a.tmemCols = a.nt <= 32 ? 32u : a.nt <= 64 ? 64u : a.nt <= 128 ? 128u : 256u;
+  a.tmemCols = pow2Cols(T * nt);
   a.wStageBytes = uint32_t(9 * 2 * a.nt * 16);
-  const size_t smemBytes = smemFor(a.nt);
+  const size_t smemBytes = smemFor(a.nt, T);
   static std::once_flag attr;
   std::call_once(attr, [] {
     cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemLimit));
