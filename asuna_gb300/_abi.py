@@ -107,7 +107,7 @@ class RenderStats(C.Structure):
                 ("shadow_nodes_visited", C.c_uint64), ("shadow_tris_tested", C.c_uint64), ("ms_total", C.c_double),
                 ("ms_extend", C.c_double), ("ms_connect", C.c_double), ("ms_shade", C.c_double),
                 ("extend_launches", C.c_uint64), ("connect_launches", C.c_uint64),
-                ("kernel_launches", C.c_uint64)]
+                ("kernel_launches", C.c_uint64), ("ms_sort", C.c_double)]
 
 
 class PostState(C.Structure):
@@ -152,6 +152,7 @@ SIGNATURES = [
     ("asuna_ctx_set_launch", C.c_int, [P, C.c_int, C.c_int]),
     ("asuna_ctx_set_graphs", C.c_int, [P, C.c_int]),
     ("asuna_ctx_set_traversal", C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+    ("asuna_ctx_set_ray_sort", C.c_int, [P, C.c_int]),
     ("asuna_scene_create", C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(P)]),
     ("asuna_scene_validate", C.c_int, [C.POINTER(SceneDesc)]),
     ("asuna_scene_destroy", C.c_int, [P]),

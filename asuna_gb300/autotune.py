@@ -16,16 +16,17 @@ def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64), trace_
          shade_options=(0, 2), refill_options=(4, 8, 16, 24), occupancy_options=(8, 10, 12), memory_bytes=48 << 30,
          reps=2, frame_base=1 << 20):
     """Returns {"frames": f, "trace_blocks_per_sm": t, "shade_blocks_per_sm": s, "traversal": (refill
-    extend, refill shadow, speculate extend, speculate shadow, traversal blocks per SM), "mrays": best,
-    "trials": [...]} and leaves the context configured with the best choice.  Coordinate search: frames,
-    then grids, then the traversal kernel variant and the refill thresholds and speculation of each
-    pass."""
+    extend, refill shadow, speculate extend, speculate shadow, traversal blocks per SM), "ray_sort": 0 / 1 / 2,
+    "mrays": best, "trials": [...]} and leaves the context configured with the best choice.  Coordinate
+    search: frames, then grids, then the traversal kernel variant and the refill thresholds and
+    speculation of each pass, then extend-queue sorting."""
     npix = shot.width * shot.height
     saved = (shot.frame0, shot.frames)
     trials = []
     best = None
 
     trav = [8, 8, 1, 1, 8]
+    ctx.set_ray_sort(0)
 
     def run(frames, t, s):
         ctx.set_traversal(*trav)
@@ -66,6 +67,17 @@ def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64), trace_
             trials.append({"frames": best["frames"], "traversal": tuple(trav), "mrays": v})
             if v > best["mrays"]:
                 best = {**best, "traversal": tuple(trav), "mrays": v}
+        # extend-queue sorting before secondary passes (mode 1: 4^3 origin
+        # cells, 2: 8^3 in Morton order)
+        trav = list(best["traversal"])
+        best["ray_sort"] = 0
+        for mode in (1, 2):
+            ctx.set_ray_sort(mode)
+            v = run(best["frames"], best["trace_blocks_per_sm"], best["shade_blocks_per_sm"])
+            trials.append({"frames": best["frames"], "ray_sort": mode, "mrays": v})
+            if v > best["mrays"]:
+                best = {**best, "ray_sort": mode, "mrays": v}
+        ctx.set_ray_sort(best["ray_sort"])
     finally:
         shot.frame0, shot.frames = saved
     ctx.set_traversal(*best["traversal"])

@@ -99,6 +99,8 @@ struct SceneDev {
   const float2* cond;   // W*H
   const float4* texels;  // every material texture, one after another
   const int4* texInfo;   // per texture: (first texel, width, height, 0)
+  float4 boundLo;        // world bounds of the instances (xyz) ...
+  float4 cellScale;      // ... and 4 / extent per axis: the ray-sort origin cells
   int32_t tlasRoot;
   int32_t envW, envH;
   int32_t numInst;
@@ -186,8 +188,13 @@ inline int shadeClassOf(uint32_t type) {
     default: return kClsLambertian;
   }
 }
+// Ray-queue sort: key = direction octant (major) and an origin cell (up to
+// 8 x 8 x 8: 4,096 keys).
+constexpr int kSortKeys = 4096;
 struct DevCounters {
   uint32_t c[kCntNum32];
+  uint32_t sortHist[kSortKeys];    // rays per key (zeroed by the scan after use)
+  uint32_t sortCursor[kSortKeys];  // next slot per key while scattering
   unsigned long long extendRays;
   unsigned long long shadowRays;
   unsigned long long nodes;   // closest-hit traversal

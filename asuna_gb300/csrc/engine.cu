@@ -195,6 +195,14 @@ int asuna_ctx_set_counters(asuna_ctx* c, int enable) {
   return ASUNA_OK;
 }
 
+int asuna_ctx_set_ray_sort(asuna_ctx* c, int enable) {
+  clearError();
+  if (!c) return fail(ASUNA_ERR_INVALID, "null context");
+  if (enable < 0 || enable > 2) return fail(ASUNA_ERR_INVALID, "ray sort %d not in {0, 1, 2}", enable);
+  c->raySort = enable;
+  return ASUNA_OK;
+}
+
 int asuna_ctx_set_traversal(asuna_ctx* c, int refillExtend, int refillShadow, int specExtend, int specShadow,
                             int blocksPerSm) {
   clearError();
@@ -373,6 +381,22 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
     iboxes.push_back(wb);
     for (int k = 0; k < 3; ++k) icen.push_back(0.5f * (wb.lo[k] + wb.hi[k]));
     ids.push_back(i);
+  }
+  {
+    // world bounds for the ray-sort origin cells
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (const Aabb& b : iboxes)
+      for (int k = 0; k < 3; ++k) {
+        lo[k] = std::min(lo[k], b.lo[k]);
+        hi[k] = std::max(hi[k], b.hi[k]);
+      }
+    float sc[3];
+    for (int k = 0; k < 3; ++k) {
+      if (!(lo[k] <= hi[k])) lo[k] = hi[k] = 0.0f;
+      sc[k] = hi[k] > lo[k] ? 4.0f / (hi[k] - lo[k]) : 0.0f;
+    }
+    s->view.boundLo = make_float4(lo[0], lo[1], lo[2], 0.0f);
+    s->view.cellScale = make_float4(sc[0], sc[1], sc[2], 0.0f);
   }
   BvhBuildOut tlas;
   if (!buildBvh(iboxes, icen, 1, 0, tlas)) return fail(ASUNA_ERR_UNSUPPORTED, "TLAS cannot be encoded");
@@ -687,7 +711,7 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
   if (stats) ASUNA_CUDA_TRY(cudaMemsetAsync(c->cnt, 0, sizeof(DevCounters), c->stream));
   // timing events: [begin, end] + one pair per extend / shade / connect launch
   size_t evNeed = 2;
-  for (auto& b : batches) evNeed += size_t(wavefrontPasses(b.maxDepth, s->view)) * 6;
+  for (auto& b : batches) evNeed += size_t(wavefrontPasses(b.maxDepth, s->view)) * 8;
   if (stats) {
     while (c->events.size() < evNeed) {
       cudaEvent_t ev;
@@ -708,7 +732,8 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
     key.insert(key.end(), {uint64_t(uintptr_t(c->wave.base)), c->wave.capacity,
            uint64_t(uintptr_t(dShots)), uint64_t(uintptr_t(dRanges)), uint64_t(c->traceGrid), uint64_t(c->shadeGrid),
            uint64_t(c->raygenGrid), uint64_t(c->counters), uint64_t(stats ? 1 : 0), uint64_t(c->refill[0]),
-           uint64_t(c->refill[1]), uint64_t(c->speculate[0]), uint64_t(c->speculate[1]), uint64_t(c->occupancy)});
+           uint64_t(c->refill[1]), uint64_t(c->speculate[0]), uint64_t(c->speculate[1]), uint64_t(c->occupancy),
+           uint64_t(c->raySort)});
     for (const Batch& b : batches)
       key.insert(key.end(), {b.rangeBegin, b.rangeEnd, b.paths, b.maxPix, uint64_t(b.maxDepth)});
     for (auto& g : c->gcache)
@@ -753,6 +778,11 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
           evi += 2;
         }
       };
+      if (c->raySort && depth >= 2) {
+        // sorted into the idle queue, which this pass then runs on
+        timedLaunch(3, [&] { launchSortQueue(P, c->raySort, c->raygenGrid, c->stream); });
+        P.cur ^= 1;
+      }
       P.occupancy = c->occupancy;
       P.refillLanes = c->refill[0];
       P.speculate = c->speculate[0];
@@ -814,7 +844,8 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
     // raygen + accumulate (+ records) per wave; extend, shading, connect per depth
     for (const Batch& b : batches)
       stats->kernel_launches += 2 + (hostRecords ? 1 : 0) +
-                                uint64_t(wavefrontPasses(b.maxDepth, s->view)) * (2 + shadeLaunches(s->view.classMask));
+                                uint64_t(wavefrontPasses(b.maxDepth, s->view)) * (2 + shadeLaunches(s->view.classMask)) +
+                                (c->raySort ? 3 * uint64_t(wavefrontPasses(b.maxDepth, s->view) - 1) : 0);
     float ms = 0;
     ASUNA_CUDA_TRY(cudaEventElapsedTime(&ms, c->events[0], c->events[1]));
     stats->ms_total = ms;
@@ -826,6 +857,8 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
         stats->extend_launches++;
       } else if (t.first == 1) {
         stats->ms_shade += m;
+      } else if (t.first == 3) {
+        stats->ms_sort += m;
       } else {
         stats->ms_connect += m;
         stats->connect_launches++;

@@ -30,6 +30,9 @@ void launchShade(const KParams& P, int grid, cudaStream_t s);
 // kernels launchShade issues for a scene's class mask (classify included)
 int shadeLaunches(uint32_t classMask);
 void launchAccumulate(const KParams& P, uint32_t maxPix, uint32_t nranges, cudaStream_t s);
+// counting-sorts extend queue P.cur into queue P.cur ^ 1 (count, scan,
+// scatter); mode 1: octant + 4^3 origin cells, 2: octant + 8^3 (Morton)
+void launchSortQueue(const KParams& P, int mode, int grid, cudaStream_t s);
 void launchRecords(const KParams& P, asuna_path_record* out, int grid, cudaStream_t s);
 void launchExtend(const KParams& P, int grid, cudaStream_t s);
 void launchConnect(const KParams& P, int grid, cudaStream_t s);

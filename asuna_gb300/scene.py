@@ -524,6 +524,12 @@ class Context:
         check(lib().asuna_ctx_set_traversal(self.handle, int(refill_extend), int(refill_shadow),
                                             int(speculate_extend), int(speculate_shadow), int(blocks_per_sm)))
 
+    def set_ray_sort(self, mode=1):
+        """Sort the extend queue by direction octant and origin cell before
+        secondary passes: 0 off, 1 4^3 cells, 2 8^3 cells in Morton order
+        (True = 1).  Results do not depend on it."""
+        check(lib().asuna_ctx_set_ray_sort(self.handle, int(mode)))
+
     def set_launch(self, trace_blocks_per_sm=0, shade_blocks_per_sm=0):
         check(lib().asuna_ctx_set_launch(self.handle, int(trace_blocks_per_sm), int(shade_blocks_per_sm)))
 

@@ -195,6 +195,7 @@ def run(args):
         ctx.set_path_budget(args.frames_per_step * shot.width * shot.height * BYTES_PER_PATH)
         if args.traversal:
             ctx.set_traversal(*(int(x) for x in args.traversal.split(",")))
+        ctx.set_ray_sort(args.ray_sort)
     # per-rank frames: replicas render disjoint frames of the same shot
     from asuna_gb300 import replicas
 
@@ -218,7 +219,7 @@ def run(args):
         torch_dist.barrier()
     ctx.sync()
     tot = {k: 0.0 for k in ("extend_rays", "shadow_rays", "paths", "ms_total", "ms_extend", "ms_connect",
-                            "ms_shade", "extend_launches", "connect_launches", "kernel_launches")}
+                            "ms_shade", "ms_sort", "extend_launches", "connect_launches", "kernel_launches")}
     with ClockSampler(local) as clk:
         for i in range(args.steps):
             st = step(1 + args.warmup + i)
@@ -278,7 +279,7 @@ def run(args):
                    "frames_per_step": args.frames_per_step,
                    "autotune": None if tuned is None else {k: tuned[k] for k in
                                                            ("frames", "trace_blocks_per_sm", "shade_blocks_per_sm",
-                                                            "traversal")}},
+                                                            "traversal", "ray_sort")}},
         "msamples_per_s": tot["paths"] * world / (ms * 1e-3) / 1e6 if world == 1 else None,
         "rays_per_step": rays / args.steps,
         "instrumented_step": {"extend_rays": cst["extend_rays"], "shadow_rays": cst["shadow_rays"],
@@ -290,7 +291,8 @@ def run(args):
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": traffic, "bytes_per_ray": bytes_per_ext, "shadow_bytes_per_ray": bytes_per_sh,
                      "ms_per_launch": ext_ms_per_launch},
-        "kernel_ms": {"extend": tot["ms_extend"], "shade": tot["ms_shade"], "connect": tot["ms_connect"]},
+        "kernel_ms": {"extend": tot["ms_extend"], "shade": tot["ms_shade"], "connect": tot["ms_connect"],
+                      "sort": tot["ms_sort"]},
         "clocks": clk.summary(),
         "scene": {"triangles": sstats["triangles"], "device_bytes": sstats["device_bytes"],
                   "build_ms": sstats["build_ms"]},
@@ -628,6 +630,8 @@ def main():
     ap.add_argument("--spheres", type=int, default=64)
     ap.add_argument("--level", type=int, default=7)
     ap.add_argument("--frames-per-step", type=int, default=0, help="0 = autotune")
+    ap.add_argument("--ray-sort", type=int, default=0, choices=(0, 1, 2),
+                    help="with --frames-per-step: extend-queue sort mode")
     ap.add_argument("--traversal", default="",
                     help="with --frames-per-step: refill extend,refill shadow,speculate extend,speculate shadow,"
                          "blocks per SM (the autotuner's traversal tuple)")

@@ -106,3 +106,23 @@ def test_film_image_tensor_is_the_film(ctx):
         t = f.tensor(k)
         assert t.shape == (24, 40, 4) and t.is_cuda
         assert np.array_equal(t.cpu().numpy(), f.read(k))
+
+
+def test_ray_sort_does_not_change_results(ctx):
+    """Sorting the extend queue reorders rays only: films (and per-path
+    records) are bit-identical with and without it, including opacity
+    pass-through and textured materials."""
+    b, shot = scenes.plugin_scene(64, 48, frames=3, max_depth=8, textured=True, opacity=True)
+    scene = ctx.create_scene(b.desc())
+    out = []
+    for mode in (0, 1, 2):
+        ctx.set_ray_sort(mode)
+        f = ctx.create_film(64, 48)
+        rec = ctx.render_paths(scene, shot, f)
+        f2 = ctx.create_film(64, 48)
+        ctx.render(scene, shot, f2)
+        out.append((np.stack([f.read(i) for i in range(9)]), rec, np.stack([f2.read(i) for i in range(9)])))
+    ctx.set_ray_sort(0)
+    for imgs, rec, imgs2 in out[1:]:
+        assert np.array_equal(out[0][0], imgs) and np.array_equal(out[0][1], rec)
+        assert np.array_equal(out[0][2], imgs2)
