@@ -16,7 +16,7 @@ def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64), trace_
          shade_options=(0, 2), refill_options=(4, 8, 16, 24), occupancy_options=(8, 10, 12), memory_bytes=48 << 30,
          reps=2, frame_base=1 << 20):
     """Returns {"frames": f, "trace_blocks_per_sm": t, "shade_blocks_per_sm": s, "traversal": (refill
-    extend, refill shadow, speculate extend, speculate shadow, traversal blocks per SM), "ray_sort": 0 / 1 / 2,
+    extend, refill shadow, speculate extend, speculate shadow, traversal blocks per SM), "ray_sort": 0..3,
     "mrays": best, "trials": [...]} and leaves the context configured with the best choice.  Coordinate
     search: frames, then grids, then the traversal kernel variant and the refill thresholds and
     speculation of each pass, then extend-queue sorting."""
@@ -67,11 +67,11 @@ def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64), trace_
             trials.append({"frames": best["frames"], "traversal": tuple(trav), "mrays": v})
             if v > best["mrays"]:
                 best = {**best, "traversal": tuple(trav), "mrays": v}
-        # extend-queue sorting before secondary passes (mode 1: 4^3 origin
-        # cells, 2: 8^3 in Morton order)
+        # extend-queue sorting before secondary passes (mode 1: octant x 4^3
+        # origin cells, 2: octant x 8^3 in Morton order, 3: the same, origin major)
         trav = list(best["traversal"])
         best["ray_sort"] = 0
-        for mode in (1, 2):
+        for mode in (1, 2, 3):
             ctx.set_ray_sort(mode)
             v = run(best["frames"], best["trace_blocks_per_sm"], best["shade_blocks_per_sm"])
             trials.append({"frames": best["frames"], "ray_sort": mode, "mrays": v})

@@ -188,8 +188,8 @@ inline int shadeClassOf(uint32_t type) {
     default: return kClsLambertian;
   }
 }
-// Ray-queue sort: key = direction octant (major) and an origin cell (up to
-// 8 x 8 x 8: 4,096 keys).
+// Ray-queue sort: key = direction octant and an origin cell (at most 4,096
+// keys).
 constexpr int kSortKeys = 4096;
 struct DevCounters {
   uint32_t c[kCntNum32];

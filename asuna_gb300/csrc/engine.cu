@@ -198,7 +198,7 @@ int asuna_ctx_set_counters(asuna_ctx* c, int enable) {
 int asuna_ctx_set_ray_sort(asuna_ctx* c, int enable) {
   clearError();
   if (!c) return fail(ASUNA_ERR_INVALID, "null context");
-  if (enable < 0 || enable > 2) return fail(ASUNA_ERR_INVALID, "ray sort %d not in {0, 1, 2}", enable);
+  if (enable < 0 || enable > 3) return fail(ASUNA_ERR_INVALID, "ray sort %d not in {0, 1, 2, 3}", enable);
   c->raySort = enable;
   return ASUNA_OK;
 }

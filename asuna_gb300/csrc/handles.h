@@ -43,7 +43,7 @@ struct asuna_ctx {
   uint32_t refill[2] = {8, 8};
   int32_t speculate[2] = {1, 1};
   int32_t occupancy = 8;  // traversal kernel variant: resident blocks per SM
-  int32_t raySort = 0;    // sort the extend queue before secondary passes
+  int32_t raySort = 3;    // extend-queue sort mode before secondary passes (0 off)
   uint64_t useClock = 0;
   std::vector<GraphEntry> gcache;
 };

@@ -7,7 +7,8 @@
 // sorted by a 9-bit key: the direction octant (which fixes the near-child
 // order of every node) and a 4 x 4 x 4 cell of the origin in the scene
 // bounds (mode 1), or a 12-bit key: the octant and an 8 x 8 x 8 cell in
-// Morton order, so neighbouring cells stay neighbours (mode 2).  The sort
+// Morton order, so neighbouring cells stay neighbours (mode 2), or the same
+// two with the origin cell major (mode 3).  The sort
 // writes into the idle ping-pong queue; the pass then runs
 // on that queue.  Only the order changes: every ray carries its path index,
 // and closest hits break exact ties by (instance, primitive), so results do
@@ -44,6 +45,12 @@ __device__ __forceinline__ uint32_t sortKey(const SceneDev& S, float4 o, float4 
   if (MODE == 1)
     return (oct << 6) | (cellOf(o.x, S.boundLo.x, S.cellScale.x, 4.0f) << 4) |
            (cellOf(o.y, S.boundLo.y, S.cellScale.y, 4.0f) << 2) | cellOf(o.z, S.boundLo.z, S.cellScale.z, 4.0f);
+  if (MODE == 3)  // origin cell (8^3, Morton) major, octant minor
+    return (((spread3(cellOf(o.x, S.boundLo.x, S.cellScale.x, 8.0f)) << 2) |
+             (spread3(cellOf(o.y, S.boundLo.y, S.cellScale.y, 8.0f)) << 1) |
+             spread3(cellOf(o.z, S.boundLo.z, S.cellScale.z, 8.0f)))
+            << 3) |
+           oct;
   return (oct << 9) | (spread3(cellOf(o.x, S.boundLo.x, S.cellScale.x, 8.0f)) << 2) |
          (spread3(cellOf(o.y, S.boundLo.y, S.cellScale.y, 8.0f)) << 1) |
          spread3(cellOf(o.z, S.boundLo.z, S.cellScale.z, 8.0f));
@@ -67,17 +74,19 @@ __global__ void __launch_bounds__(kSortThreads) k_sortCount(KParams P) {
     if (h[k]) atomicAdd(&W.cnt->sortHist[k], h[k]);
 }
 
-// one block of 1024 threads, 4 consecutive keys each (512-key mode: the
-// upper keys are empty)
+// one block of 1024 threads, kSortKeys / 1024 consecutive keys each (the
+// keys a mode does not use are empty)
 constexpr int kScanThreads = 1024;
+constexpr int kKeysPerThread = kSortKeys / kScanThreads;
+static_assert(kSortKeys % kScanThreads == 0, "scan tiling");
 __global__ void __launch_bounds__(kScanThreads) k_sortScan(KParams P) {
   __shared__ uint32_t v[kScanThreads];
   const WaveDev& W = P.W;
   const int t = threadIdx.x;
-  uint32_t c[4], run = 0;
+  uint32_t c[kKeysPerThread], run = 0;
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    c[j] = W.cnt->sortHist[4 * t + j];
+  for (int j = 0; j < kKeysPerThread; ++j) {
+    c[j] = W.cnt->sortHist[kKeysPerThread * t + j];
     run += c[j];
   }
   v[t] = run;
@@ -91,9 +100,9 @@ __global__ void __launch_bounds__(kScanThreads) k_sortScan(KParams P) {
   }
   uint32_t start = v[t] - run;
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    W.cnt->sortCursor[4 * t + j] = start;
-    W.cnt->sortHist[4 * t + j] = 0u;
+  for (int j = 0; j < kKeysPerThread; ++j) {
+    W.cnt->sortCursor[kKeysPerThread * t + j] = start;
+    W.cnt->sortHist[kKeysPerThread * t + j] = 0u;
     start += c[j];
   }
   if (t == kScanThreads - 1) W.cnt->c[kCntExtend0 + (P.cur ^ 1)] = v[t];
@@ -148,10 +157,14 @@ void launchSortQueue(const KParams& P, int mode, int grid, cudaStream_t s) {
     k_sortCount<1><<<grid, kSortThreads, 0, s>>>(P);
     k_sortScan<<<1, kScanThreads, 0, s>>>(P);
     k_sortScatter<1><<<grid, kSortThreads, 0, s>>>(P);
-  } else {
+  } else if (mode == 2) {
     k_sortCount<2><<<grid, kSortThreads, 0, s>>>(P);
     k_sortScan<<<1, kScanThreads, 0, s>>>(P);
     k_sortScatter<2><<<grid, kSortThreads, 0, s>>>(P);
+  } else {
+    k_sortCount<3><<<grid, kSortThreads, 0, s>>>(P);
+    k_sortScan<<<1, kScanThreads, 0, s>>>(P);
+    k_sortScatter<3><<<grid, kSortThreads, 0, s>>>(P);
   }
 }
 

@@ -526,8 +526,9 @@ class Context:
 
     def set_ray_sort(self, mode=1):
         """Sort the extend queue by direction octant and origin cell before
-        secondary passes: 0 off, 1 4^3 cells, 2 8^3 cells in Morton order
-        (True = 1).  Results do not depend on it."""
+        secondary passes: 0 off, 1 octant x 4^3 cells, 2 octant x 8^3 cells
+        in Morton order, 3 the same with the origin cell major (True = 1).  Results
+        do not depend on it."""
         check(lib().asuna_ctx_set_ray_sort(self.handle, int(mode)))
 
     def set_launch(self, trace_blocks_per_sm=0, shade_blocks_per_sm=0):

@@ -630,7 +630,7 @@ def main():
     ap.add_argument("--spheres", type=int, default=64)
     ap.add_argument("--level", type=int, default=7)
     ap.add_argument("--frames-per-step", type=int, default=0, help="0 = autotune")
-    ap.add_argument("--ray-sort", type=int, default=0, choices=(0, 1, 2),
+    ap.add_argument("--ray-sort", type=int, default=3, choices=(0, 1, 2, 3),
                     help="with --frames-per-step: extend-queue sort mode")
     ap.add_argument("--traversal", default="",
                     help="with --frames-per-step: refill extend,refill shadow,speculate extend,speculate shadow,"

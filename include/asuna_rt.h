@@ -346,10 +346,10 @@ int asuna_ctx_set_launch(asuna_ctx* ctx, int trace_blocks_per_sm, int shade_bloc
  * not depend on them. */
 int asuna_ctx_set_traversal(asuna_ctx* ctx, int refill_extend, int refill_shadow, int speculate_extend,
                             int speculate_shadow, int blocks_per_sm);
-/* Reorders the extend queue before every secondary pass by direction octant
- * and origin cell so warps carry rays that walk alike: 0 off (the default),
- * 1 with 4 x 4 x 4 origin cells, 2 with 8 x 8 x 8 cells in Morton order.
- * Results do not depend on it. */
+/* Reorders the extend queue before every secondary pass by direction and
+ * origin so warps carry rays that walk alike: 0 off, 1 octant x 4 x 4 x 4
+ * origin cells, 2 octant x 8 x 8 x 8 cells in Morton order, 3 the same with
+ * the origin cell major (the default).  Results do not depend on it. */
 int asuna_ctx_set_ray_sort(asuna_ctx* ctx, int mode);
 
 /* ---- scene: upload + acceleration-structure build ------------------------ */

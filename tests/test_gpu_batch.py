@@ -115,7 +115,7 @@ def test_ray_sort_does_not_change_results(ctx):
     b, shot = scenes.plugin_scene(64, 48, frames=3, max_depth=8, textured=True, opacity=True)
     scene = ctx.create_scene(b.desc())
     out = []
-    for mode in (0, 1, 2):
+    for mode in (0, 1, 2, 3):
         ctx.set_ray_sort(mode)
         f = ctx.create_film(64, 48)
         rec = ctx.render_paths(scene, shot, f)
