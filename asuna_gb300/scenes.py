@@ -225,6 +225,38 @@ def mixed_shot(b, width, height, frames, max_depth=12, rr_depth=3, channels=("al
     return make_shot(cam, state, width, height, frames, seed=seed, depth_channel=depth, rr_depth=rr_depth)
 
 
+def furnace_scene(albedo=(1.0, 1.0, 1.0), width=24, height=24, frames=32, max_depth=8, background=(1.0, 1.0, 1.0)):
+    """A flat-shaded convex polyhedron (level-2 icosphere, use_face_normal)
+    of Lambertian `albedo` under a uniform background and no lights: every
+    camera ray that hits it converges to albedo x background (a white one
+    disappears), every other to the background.  Returns (builder, shot,
+    mask of the pixels whose samples all see the object, mask of those whose
+    samples all miss it)."""
+    b = SceneBuilder()
+    m = b.add_lambertian("grey", albedo)
+    vtx, faces = icosphere(2)
+    v = np.zeros(len(vtx), A.VERTEX_DTYPE)
+    v["pos"] = vtx
+    v["normal"] = vtx
+    b.add_mesh("ball", v, faces.astype(np.uint32).reshape(-1))
+    b.add_instance("ball", m)
+    state, depth = b.state(spp=frames, max_path_depth=max_depth, channels=(), bg_color=background)
+    state.use_face_normal = 1
+    eye, at = (0.0, 0.0, 3.2), (0.0, 0.0, 0.0)
+    cam = perspective_camera(eye, at, (0, 1, 0), 45.0, width, height)
+    shot = make_shot(cam, state, width, height, frames, seed=0, depth_channel=depth)
+    # pixel centres inside the object's silhouette (the inscribed radius of
+    # the polyhedron, in the image plane of a 45-degree horizontal fov)
+    ys, xs = np.mgrid[0:height, 0:width]
+    px = (xs + 0.5) / width * 2 - 1
+    py = ((ys + 0.5) / height * 2 - 1) * height / width
+    tan = math.tan(math.radians(45.0) / 2)
+    ang = np.arctan(np.hypot(px, py) * tan)
+    inside = np.sin(ang) * 3.2 < 0.9  # inscribed radius 0.98, less a pixel footprint
+    outside = np.sin(ang) * 3.2 > 1.1  # circumscribed radius 1, plus a pixel footprint
+    return b, shot, inside, outside
+
+
 def _spherical_uv(v):
     """u = longitude, v = colatitude of each vertex (in place)."""
     p = v["pos"].astype(np.float64)

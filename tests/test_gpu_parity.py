@@ -82,3 +82,22 @@ def test_mixed_scene_small(ctx):
                                  env_size=(128, 64))
     rec, orec, imgs, ofilm = _run(ctx, b, shot)
     _check(rec, orec, imgs, ofilm, film_tol=5e-2)
+
+
+@pytest.mark.parametrize("albedo", [(1.0, 1.0, 1.0), (0.5, 0.7, 0.9)])
+def test_furnace_closed_form(ctx, albedo):
+    """The GPU on the furnace of tests/test_oracle.py: hits converge to
+    albedo x (1 - ln 17 / 16) (the reference's estimator without a light
+    sample), background pixels are exactly the background, and the film
+    equals the oracle's within the parity tolerance."""
+    import math
+
+    b, shot, inside, outside = scenes.furnace_scene(albedo, 48, 48, frames=256)
+    rec, orec, imgs, ofilm = _run(ctx, b, shot)
+    _check(rec, orec, imgs, ofilm)
+    img = imgs[0][..., :3].astype(np.float64)
+    expect = np.array(albedo) * (1.0 - math.log(17.0) / 16.0)
+    got = img[inside].mean(0)
+    sigma = img[inside].std(0) / math.sqrt(inside.sum())
+    assert np.all(np.abs(got - expect) <= 4 * sigma + 1e-4), (got, expect, sigma)
+    assert np.all(img[outside] == 1.0)

@@ -3,6 +3,8 @@ reference's own shader code (tests/golden/make_golden.py) and, where the
 reference tree is present, a live comparison with it."""
 import os
 
+import math
+
 import numpy as np
 import pytest
 
@@ -95,3 +97,24 @@ def test_shared_math_accuracy(which, fn, lo, hi, ulps):
         ref = np.arctan2(x.astype(np.float64), y.astype(np.float64)) if fn is None else fn(x.astype(np.float64))
     d = np.abs(got.view(np.int32).astype(np.int64) - ref.astype(np.float32).view(np.int32).astype(np.int64))
     assert d.max() <= ulps
+
+
+@pytest.mark.parametrize("albedo", [(1.0, 1.0, 1.0), (0.5, 0.7, 0.9)])
+def test_furnace_closed_form(albedo):
+    """A convex Lambertian under a uniform background colour, no env map and
+    no lights: sampleLights takes no light sample (rchit_layouts.glsl:127-134,
+    case "no env & light"), while the miss shader still weights the BSDF
+    sample by the power heuristic against the uniform-sphere pdf
+    (raytrace.default.rmiss:41-50).  The expected radiance of a hit is then
+    albedo x background x 2 int_0^1 c^3 / (c^2 + 1/16) dc = albedo x
+    background x (1 - ln 17 / 16): the reference's estimator, not an
+    energy-conserving one.  Pixels that see only the background get it
+    exactly."""
+    b, shot, inside, outside = scenes.furnace_scene(albedo, 24, 24, frames=64)
+    film, _, _ = oracle_py.OracleScene(b.desc()).render(shot, records=False)
+    img = film[0][..., :3].astype(np.float64)
+    expect = np.array(albedo) * (1.0 - math.log(17.0) / 16.0)
+    got = img[inside].mean(0)
+    sigma = img[inside].std(0) / math.sqrt(inside.sum())
+    assert np.all(np.abs(got - expect) <= 4 * sigma + 1e-4), (got, expect, sigma)
+    assert np.all(img[outside] == 1.0)
