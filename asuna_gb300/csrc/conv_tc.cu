@@ -24,15 +24,19 @@
 //   * 9 T MMAs per group accumulate into TMEM (fp32, lane = pixel of a tile,
 //     column = tile t * nt + output channel); a 3-stage ring of shared-memory
 //     buffers is refilled as tcgen05.commit reports each stage's MMAs done.
-// One elected thread issues the copies and the MMAs; after the last group
-// the four warps read their 32 TMEM lanes each (tcgen05.ld), apply bias,
-// ReLU and the ReLU mask and store bf16 (or fp32).  Every mbarrier wait is
-// bounded: on expiry the CTA records an error, skips its output and still
-// frees its tensor memory.
+// The CTAs are persistent and warp-specialised: one elected thread of a
+// fifth warp issues the copies and the MMAs of a stream of units (the ring
+// runs ahead across unit boundaries, the MMAs alternate between two TMEM
+// accumulator buffers); the four epilogue warps read their 32 TMEM lanes
+// each (tcgen05.ld) of the finished buffer, apply bias, ReLU and the ReLU
+// mask, store bf16 (or fp32) and hand the buffer back, while the next unit's
+// MMAs run.  Every mbarrier wait is bounded: on expiry the CTA records an
+// error, stops its work and still frees its tensor memory.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -54,7 +58,6 @@ __host__ __device__ constexpr int haloW(int T) { return kTileW * T + 2; }
 __host__ __device__ constexpr int boxBytes(int T) { return kHaloH * haloW(T) * 16; }
 __host__ __device__ constexpr int chunkBytes(int T) { return (boxBytes(T) + 127) / 128 * 128; }
 __host__ __device__ constexpr int actStage(int T) { return 2 * chunkBytes(T); }  // 16 channels
-constexpr int kThreads = 128;
 constexpr uint32_t kWaitLimit = 1u << 20;                      // try_wait rounds before giving up
 
 __device__ int g_tcError;  // set when a wait expired; read and cleared by asuna_nn_tc_status
@@ -79,12 +82,12 @@ int sliceWidth(int cout) {
   }
   return 16;
 }
-// Pixel tiles per CTA: as many (up to 4) as tensor memory (T accumulators of
-// nt columns in 512) and shared memory hold and the image width uses; the
-// tiles share every weight stage.
+// Pixel tiles per unit: as many (up to 4) as tensor memory (two buffers of T
+// accumulators of nt columns in 512) and shared memory hold and the image
+// width uses; the tiles share every weight stage.
 int tilesPerCta(int nt, int w) {
   int T = kMaxTiles;
-  while (T > 1 && (pow2Cols(T * nt) > 512 || smemFor(nt, T) > kSmemLimit || kTileW * (T - 1) >= w)) --T;
+  while (T > 1 && (pow2Cols(2 * T * nt) > 512 || smemFor(nt, T) > kSmemLimit || kTileW * (T - 1) >= w)) --T;
   return T;
 }
 
@@ -165,45 +168,87 @@ struct TcArgs {
   void* out;                  // [P][cout]
   int n, h, w, cin, cout;
   int nt, slices;             // output channels per CTA, cout / nt
-  int tiles;                  // 16 x 8 pixel tiles per CTA, side by side in x
-  int tilesX, tilesY;         // CTA regions (16 x 8 tiles pixels) per image
+  int tiles;                  // 16 x 8 pixel tiles per unit, side by side in x
+  int tilesX, tilesY;         // units (16 x 8 tiles pixels) per image row / column
+  int units;                  // tilesX * tilesY * n * slices
   int relu, outF32;
-  uint32_t tmemCols;
-  uint32_t wStageBytes;  // 9 * 2 * nt * 16
+  uint32_t tmemCols;          // two accumulator buffers of tiles * nt columns
+  uint32_t wStageBytes;       // 9 * 2 * nt * 16
 };
+
+// a unit: slice (fastest), then tile column, tile row, image
+struct Unit {
+  int slice, img, x0, y0;
+};
+__device__ __forceinline__ Unit unitOf(const TcArgs& a, int u) {
+  Unit r;
+  r.slice = u % a.slices;
+  u /= a.slices;
+  const int tx = u % a.tilesX;
+  u /= a.tilesX;
+  const int ty = u % a.tilesY;
+  r.img = u / a.tilesY;
+  r.x0 = tx * kTileW * a.tiles;
+  r.y0 = ty * kTileH;
+  return r;
+}
+
+// bounded wait that also gives up once another role has recorded an abort
+__device__ __forceinline__ bool mbarWaitOr(uint32_t bar, uint32_t parity, const volatile int* abortFlag) {
+  for (uint32_t i = 0; i < kWaitLimit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((i & 255u) == 255u && *abortFlag) return false;
+  }
+  return false;
+}
+__device__ __forceinline__ void mbarArrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Persistent CTAs, warp-specialised: warps 0-3 are the epilogue (TMEM lane
+// quarter = warp), warp 4's first lane issues the TMA copies and the MMAs.
+// Units (T tiles of one channel slice) are taken round-robin; the copy ring
+// runs ahead across unit boundaries and the MMAs alternate between two
+// accumulator buffers, so one unit's epilogue overlaps the next unit's
+// MMAs.  Barriers: full / empty per ring stage (copies landed / MMAs done
+// reading), accFull / accEmpty per accumulator buffer.
+constexpr int kEpiWarps = 4;
+constexpr int kThreads = 32 * (kEpiWarps + 1);
 
 __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__ CUtensorMap act, TcArgs a) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  // [0, 128): barriers and the TMEM address; then activation stages, weight stages
+  // [0, 128): barriers, the TMEM address and the abort flag; then the
+  // activation stages and the weight stages
   uint64_t* full = reinterpret_cast<uint64_t*>(sm);
   uint64_t* empty = full + kStages;
-  uint64_t* done = empty + kStages;
-  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(done + 1);
-  int* abortFlag = reinterpret_cast<int*>(tmemSlot + 1);
+  uint64_t* accFull = empty + kStages;
+  uint64_t* accEmpty = accFull + 2;
+  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(accEmpty + 2);
+  volatile int* abortFlag = reinterpret_cast<volatile int*>(tmemSlot + 1);
   const int T = a.tiles, hw = haloW(T);
   const uint32_t chunk = uint32_t(chunkBytes(T)), stageA = uint32_t(actStage(T));
   unsigned char* actBase = sm + 128;
   unsigned char* wBase = actBase + kStages * stageA;
-
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  int t = blockIdx.x;
-  const int slice = t % a.slices;
-  t /= a.slices;
-  const int n0 = slice * a.nt;
-  const __nv_bfloat16* wt = a.wt + size_t(slice) * size_t(a.cin / 16) * (a.wStageBytes / 2);
-  const int tx = t % a.tilesX;
-  t /= a.tilesX;
-  const int ty = t % a.tilesY;
-  const int img = t / a.tilesY;
-  const int x0 = tx * kTileW * T, y0 = ty * kTileH;
 
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbarInit(smem(&full[s]), 1);
       mbarInit(smem(&empty[s]), 1);
     }
-    mbarInit(smem(done), 1);
-    *abortFlag = 0;
+    for (int b = 0; b < 2; ++b) {
+      mbarInit(smem(&accFull[b]), 1);
+      mbarInit(smem(&accEmpty[b]), kEpiWarps);
+    }
+    // a CTA that finds an expired wait recorded skips its work: one failure
+    // costs one timeout, not one per CTA
+    *abortFlag = *reinterpret_cast<volatile int*>(&g_tcError) ? 1 : 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -217,101 +262,117 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
   __syncthreads();
   fenceAfter();
   const uint32_t tmem = *tmemSlot;
-
   const int groups = a.cin / 16;
-  // a CTA that finds an expired wait recorded skips its work: one failure
-  // costs one timeout, not one per CTA
-  if (tid == 0 && *reinterpret_cast<volatile int*>(&g_tcError)) *abortFlag = 1;
-  if (tid == 0 && !*abortFlag) {
-    const uint32_t idesc = instrDesc(uint32_t(a.nt));
-    auto issue = [&](int s, int g) {
-      const uint32_t bar = smem(&full[s]);
-      mbarExpectTx(bar, uint32_t(2 * boxBytes(T)) + a.wStageBytes);
-      const uint32_t dstA = smem(actBase + s * stageA);
-      tmaLoad4d(dstA, &act, g * 16, x0 - 1, y0 - 1, img, bar);
-      tmaLoad4d(dstA + chunk, &act, g * 16 + 8, x0 - 1, y0 - 1, img, bar);
-      bulkLoad(smem(wBase + size_t(s) * a.wStageBytes), wt + size_t(g) * (a.wStageBytes / 2), a.wStageBytes, bar);
-    };
-    bool ok = true;
-    for (int g = 0; g < groups && g < kStages; ++g) issue(g, g);
-    for (int g = 0; g < groups && ok; ++g) {
-      const int s = g % kStages;
-      const uint32_t use = uint32_t(g / kStages);
-      if (!mbarWait(smem(&full[s]), use & 1u)) {
-        ok = false;
-        break;
-      }
-      const uint32_t aBase = smem(actBase + s * stageA);
-      const uint32_t bBase = smem(wBase + size_t(s) * a.wStageBytes);
-      const uint32_t bTap = uint32_t(2 * a.nt * 16);
+  const int myUnits = blockIdx.x < a.units ? (a.units - 1 - int(blockIdx.x)) / int(gridDim.x) + 1 : 0;
+  const uint32_t bufCols = uint32_t(T * a.nt);
+
+  if (warp == kEpiWarps) {
+    if (lane == 0 && !*abortFlag) {
+      const uint32_t idesc = instrDesc(uint32_t(a.nt));
+      const int total = myUnits * groups;
+      // stream position q = (unit k of this CTA, channel group g)
+      auto issue = [&](int q) {
+        const int k = q / groups, g = q % groups, s = q % kStages;
+        const Unit U = unitOf(a, int(blockIdx.x) + k * int(gridDim.x));
+        const __nv_bfloat16* wt = a.wt + size_t(U.slice) * size_t(groups) * (a.wStageBytes / 2);
+        const uint32_t bar = smem(&full[s]);
+        mbarExpectTx(bar, uint32_t(2 * boxBytes(T)) + a.wStageBytes);
+        const uint32_t dstA = smem(actBase + s * stageA);
+        tmaLoad4d(dstA, &act, g * 16, U.x0 - 1, U.y0 - 1, U.img, bar);
+        tmaLoad4d(dstA + chunk, &act, g * 16 + 8, U.x0 - 1, U.y0 - 1, U.img, bar);
+        bulkLoad(smem(wBase + size_t(s) * a.wStageBytes), wt + size_t(g) * (a.wStageBytes / 2), a.wStageBytes, bar);
+      };
+      bool ok = true;
+      for (int q = 0; q < total && q < kStages; ++q) issue(q);
+      for (int q = 0; q < total && ok; ++q) {
+        const int k = q / groups, g = q % groups, s = q % kStages;
+        const uint32_t use = uint32_t(q / kStages), buf = uint32_t(k & 1);
+        if (g == 0 && k >= 2) {
+          // the epilogue has read this buffer's previous unit out
+          if (!(ok = mbarWaitOr(smem(&accEmpty[buf]), uint32_t((k >> 1) - 1) & 1u, abortFlag))) break;
+          fenceAfter();
+        }
+        if (!(ok = mbarWaitOr(smem(&full[s]), use & 1u, abortFlag))) break;
+        const uint32_t aBase = smem(actBase + s * stageA);
+        const uint32_t bBase = smem(wBase + size_t(s) * a.wStageBytes);
+        const uint32_t bTap = uint32_t(2 * a.nt * 16);
+        const uint32_t acc = tmem + buf * bufCols;
 #pragma unroll 1
-      for (int tap = 0; tap < 9; ++tap) {
-        const int dy = tap / 3, dx = tap % 3;
-        const uint64_t db = matDesc(bBase + uint32_t(tap) * bTap, uint32_t(a.nt * 16), 128u);
-        // tile t: the view starting 8 t pixels further along the halo rows;
-        // its accumulator is columns [t nt, (t + 1) nt) of tensor memory
-        for (int t2 = 0; t2 < T; ++t2) {
-          const uint64_t da = matDesc(aBase + uint32_t(dy * hw + dx + kTileW * t2) * 16u, chunk, uint32_t(hw * 16));
-          mma(tmem + uint32_t(t2 * a.nt), da, db, idesc, (g > 0 || tap > 0) ? 1u : 0u);
+        for (int tap = 0; tap < 9; ++tap) {
+          const int dy = tap / 3, dx = tap % 3;
+          const uint64_t db = matDesc(bBase + uint32_t(tap) * bTap, uint32_t(a.nt * 16), 128u);
+          // tile t: the view starting 8 t pixels further along the halo
+          // rows; its accumulator is columns [t nt, (t + 1) nt) of the buffer
+          for (int t2 = 0; t2 < T; ++t2) {
+            const uint64_t da = matDesc(aBase + uint32_t(dy * hw + dx + kTileW * t2) * 16u, chunk, uint32_t(hw * 16));
+            mma(acc + uint32_t(t2 * a.nt), da, db, idesc, (g > 0 || tap > 0) ? 1u : 0u);
+          }
+        }
+        commit(smem(&empty[s]));
+        if (g == groups - 1) commit(smem(&accFull[buf]));
+        const int qn = q + kStages;
+        if (qn < total) {
+          if (!(ok = mbarWaitOr(smem(&empty[s]), use & 1u, abortFlag))) break;
+          issue(qn);
         }
       }
-      commit(smem(&empty[s]));
-      const int gn = g + kStages;
-      if (gn < groups) {
-        if (!mbarWait(smem(&empty[s]), use & 1u)) {
-          ok = false;
-          break;
-        }
-        issue(s, gn);
+      if (!ok) {
+        *abortFlag = 1;
+        atomicExch(&g_tcError, 1);
       }
     }
-    if (ok) {
-      commit(smem(done));
-      ok = mbarWait(smem(done), 0u);
-    }
-    if (!ok) {
-      *abortFlag = 1;
-      atomicExch(&g_tcError, 1);
-    }
-  }
-  fenceBefore();
-  __syncthreads();
-  fenceAfter();
-  if (!*abortFlag) {
+  } else {
     // epilogue: warp w owns TMEM lanes 32w..32w+31 = pixels 32w..32w+31 of each tile
     const int m = warp * 32 + lane;
-    const uint32_t laneBase = tmem + (uint32_t(warp * 32) << 16);
-    for (int t2 = 0; t2 < T; ++t2)
-    for (int c0 = 0; c0 < a.nt; c0 += 16) {
-      const int py = y0 + m / kTileW, px = x0 + kTileW * t2 + m % kTileW;
-      const bool inside = py < a.h && px < a.w;
-      const size_t p = (size_t(img) * a.h + py) * a.w + px;
-      float v[16];
-      ld16(laneBase + uint32_t(t2 * a.nt + c0), v);
-      if (!inside) continue;
-#pragma unroll
-      for (int i = 0; i < 16; i += 2) {
-        const int co = n0 + c0 + i;
-        float v0 = v[i], v1 = v[i + 1];
-        if (a.bias) {
-          v0 += a.bias[co];
-          v1 += a.bias[co + 1];
+    for (int k = 0; k < myUnits; ++k) {
+      const uint32_t buf = uint32_t(k & 1);
+      if (!mbarWaitOr(smem(&accFull[buf]), uint32_t(k >> 1) & 1u, abortFlag)) {
+        if (lane == 0) {
+          *abortFlag = 1;
+          atomicExch(&g_tcError, 1);
         }
-        if (a.relu) {
-          v0 = fmaxf(v0, 0.0f);
-          v1 = fmaxf(v1, 0.0f);
-        }
-        if (a.mask) {
-          const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162*>(a.mask + p * a.cout + co);
-          if (!(__bfloat162float(mk.x) > 0.0f)) v0 = 0.0f;
-          if (!(__bfloat162float(mk.y) > 0.0f)) v1 = 0.0f;
-        }
-        if (a.outF32)
-          *reinterpret_cast<float2*>(static_cast<float*>(a.out) + p * a.cout + co) = make_float2(v0, v1);
-        else
-          *reinterpret_cast<__nv_bfloat162*>(static_cast<__nv_bfloat16*>(a.out) + p * a.cout + co) =
-              __floats2bfloat162_rn(v0, v1);
+        break;
       }
+      fenceAfter();
+      const Unit U = unitOf(a, int(blockIdx.x) + k * int(gridDim.x));
+      const int n0 = U.slice * a.nt;
+      const uint32_t laneBase = tmem + (uint32_t(warp * 32) << 16) + buf * bufCols;
+      for (int t2 = 0; t2 < T; ++t2)
+        for (int c0 = 0; c0 < a.nt; c0 += 16) {
+          const int py = U.y0 + m / kTileW, px = U.x0 + kTileW * t2 + m % kTileW;
+          const bool inside = py < a.h && px < a.w;
+          const size_t p = (size_t(U.img) * a.h + py) * a.w + px;
+          float v[16];
+          ld16(laneBase + uint32_t(t2 * a.nt + c0), v);
+          if (!inside) continue;
+#pragma unroll
+          for (int i = 0; i < 16; i += 2) {
+            const int co = n0 + c0 + i;
+            float v0 = v[i], v1 = v[i + 1];
+            if (a.bias) {
+              v0 += a.bias[co];
+              v1 += a.bias[co + 1];
+            }
+            if (a.relu) {
+              v0 = fmaxf(v0, 0.0f);
+              v1 = fmaxf(v1, 0.0f);
+            }
+            if (a.mask) {
+              const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162*>(a.mask + p * a.cout + co);
+              if (!(__bfloat162float(mk.x) > 0.0f)) v0 = 0.0f;
+              if (!(__bfloat162float(mk.y) > 0.0f)) v1 = 0.0f;
+            }
+            if (a.outF32)
+              *reinterpret_cast<float2*>(static_cast<float*>(a.out) + p * a.cout + co) = make_float2(v0, v1);
+            else
+              *reinterpret_cast<__nv_bfloat162*>(static_cast<__nv_bfloat16*>(a.out) + p * a.cout + co) =
+                  __floats2bfloat162_rn(v0, v1);
+          }
+        }
+      // this warp's lanes of the buffer are read: hand it back to the MMAs
+      fenceBefore();
+      __syncwarp();
+      if (lane == 0) mbarArrive(smem(&accEmpty[buf]));
     }
   }
   fenceBefore();
@@ -406,7 +467,7 @@ int asuna_nn_conv3x3_tc(void* stream, const void* in, int n, int h, int w, int c
   a.outF32 = out_f32;
   a.nt = nt;
   a.slices = cout / a.nt;
-  a.tmemCols = pow2Cols(T * nt);
+  a.tmemCols = pow2Cols(2 * T * nt);
   a.wStageBytes = uint32_t(9 * 2 * a.nt * 16);
   const size_t smemBytes = smemFor(a.nt, T);
   static std::once_flag attr;
@@ -414,9 +475,19 @@ int asuna_nn_conv3x3_tc(void* stream, const void* in, int n, int h, int w, int c
     cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemLimit));
   });
   if (smemBytes > kSmemLimit) return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: cout %d needs too much shared memory", cout);
-  const long long blocks = (long long)a.tilesX * a.tilesY * n * a.slices;
-  if (blocks > (1ll << 31) - 1) return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: too many tiles");
-  k_conv_tc<<<unsigned(blocks), kThreads, smemBytes, static_cast<cudaStream_t>(stream)>>>(map, a);
+  const long long units = (long long)a.tilesX * a.tilesY * n * a.slices;
+  if (units > (1ll << 31) - 1) return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: too many tiles");
+  a.units = int(units);
+  // persistent grid: the CTAs that fit on the device at once (shared memory,
+  // and tensor memory: 512 columns per SM), or fewer when there is less work
+  int dev = 0, sms = 1, perSm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_conv_tc, kThreads, smemBytes);
+  perSm = std::max(1, std::min(perSm, int(512 / a.tmemCols)));
+  const long long grid = std::min<long long>(units, (long long)sms * perSm);
+  k_conv_tc<<<unsigned(std::max<long long>(grid, 1)), kThreads, smemBytes, static_cast<cudaStream_t>(stream)>>>(map,
+                                                                                                                 a);
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? ASUNA_OK : fail(ASUNA_ERR_CUDA, "asuna_nn_conv3x3_tc: %s", cudaGetErrorString(e));
 }
