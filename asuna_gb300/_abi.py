@@ -201,6 +201,8 @@ SIGNATURES = [
     ("asuna_denoise", C.c_int, [P, P, P, C.c_int, C.c_int, P]),
     ("asuna_denoise_estimate", C.c_int, [P, P, P, P, C.c_int, C.c_int, P, C.POINTER(C.c_double),
                                           C.POINTER(C.c_double)]),
+    ("asuna_denoise_combined", C.c_int, [P, P, P, P, C.c_int, C.c_int, P, C.POINTER(C.c_double),
+                                          C.POINTER(C.c_double)]),
     ("asuna_nn_conv3x3", C.c_int, [P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, C.c_int, C.c_int, P, P,
                                     C.c_int]),
     ("asuna_nn_conv3x3_wgrad", C.c_int, [P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P]),

@@ -504,6 +504,21 @@ __global__ void k_err_sums(const float4* d, const float4* a, const float4* b, si
   }
 }
 
+// sums of |D_A - D_B|^2 (two denoised halves) and the combined input of
+// both films: radiance (A + B) / 2, weight A + B
+__global__ void k_combine(const float4* da, const float4* db, const float4* a, const float4* b, const float4* wa,
+                          const float4* wb, float4* rad, float4* wsum, size_t P, double* sums) {
+  float s0 = 0.0f;
+  for (size_t p = blockIdx.x * size_t(blockDim.x) + threadIdx.x; p < P; p += size_t(gridDim.x) * blockDim.x) {
+    const float4 x = da[p], y = db[p], av = a[p], bv = b[p], w0 = wa[p], w1 = wb[p];
+    s0 += (x.x - y.x) * (x.x - y.x) + (x.y - y.y) * (x.y - y.y) + (x.z - y.z) * (x.z - y.z);
+    rad[p] = make_float4(0.5f * (av.x + bv.x), 0.5f * (av.y + bv.y), 0.5f * (av.z + bv.z), 1.0f);
+    wsum[p] = make_float4(w0.x + w1.x, w0.y + w1.y, w0.z + w1.z, w0.w + w1.w);
+  }
+  for (int off = 16; off; off >>= 1) s0 += __shfl_down_sync(0xffffffffu, s0, off);
+  if ((threadIdx.x & 31) == 0) atomicAdd(&sums[2], double(s0));
+}
+
 // Adam on fp32 master weights; writes the bf16 copy used by the kernels.
 __global__ void k_adam(float* w, float* m, float* v, const float* g, __nv_bfloat16* wb, size_t n, float lr, float b1,
                        float b2, float eps, float c1, float c2) {
@@ -914,7 +929,7 @@ int asuna_denoiser_create(asuna_ctx* ctx, const asuna_denoiser_opts* o, asuna_de
     A(&d->wtcT, d->nFlip);
   }
   A(&d->dLoss, 1);
-  A(&d->dSums, 2);
+  A(&d->dSums, 3);
   if (d->training) {
     A(&d->grad, d->nParams);
     A(&d->m, d->nParams);
@@ -1104,6 +1119,46 @@ int asuna_denoise_estimate(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asu
   const double mDB = h[0] / (3.0 * P), mAB = h[1] / (3.0 * P);
   if (err_denoised) *err_denoised = std::sqrt(std::max(0.0, mDB - 0.5 * mAB));
   if (err_plain) *err_plain = std::sqrt(0.25 * mAB);
+  return ASUNA_OK;
+}
+
+int asuna_denoise_combined(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asuna_film* b, int albedo_image,
+                           int normal_image, float* out, double* err_denoised, double* err_plain) {
+  clearError();
+  if (!ctx || !d || !a || !b || !out) return fail(ASUNA_ERR_INVALID, "asuna_denoise_combined: null argument");
+  if (a->width != b->width || a->height != b->height)
+    return fail(ASUNA_ERR_INVALID, "asuna_denoise_combined: films differ in size");
+  cudaStream_t s = ctx->stream;
+  const size_t P = size_t(a->width) * a->height;
+  float4 *db = nullptr, *rad = nullptr, *wsum = nullptr;
+  ASUNA_CUDA_TRY(cudaMallocAsync(&db, 3 * P * sizeof(float4), s));
+  rad = db + P;
+  wsum = rad + P;
+  struct Free {
+    float4* p;
+    cudaStream_t s;
+    ~Free() { cudaFreeAsync(p, s); }
+  } guard{db, s};
+  // D_A (into out) against film B, as asuna_denoise_estimate does
+  double eA = 0.0, eP = 0.0;
+  NN_TRY(asuna_denoise_estimate(ctx, d, a, b, albedo_image, normal_image, out, &eA, &eP));
+  NN_TRY(asuna_denoise(ctx, d, b, albedo_image, normal_image, reinterpret_cast<float*>(db)));
+  ASUNA_CUDA_TRY(cudaMemsetAsync(d->dSums + 2, 0, sizeof(double), s));
+  k_combine<<<grid1d(P), 256, 0, s>>>(reinterpret_cast<const float4*>(out), db, a->rad, b->rad, a->w, b->w, rad, wsum,
+                                      P, d->dSums);
+  ASUNA_CUDA_TRY(cudaGetLastError());
+  double h = 0.0;
+  ASUNA_CUDA_TRY(cudaMemcpyAsync(&h, d->dSums + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
+  NN_TRY(asuna_denoiser_forward(d, reinterpret_cast<const float*>(rad), filmImage(a, albedo_image),
+                                filmImage(a, normal_image), reinterpret_cast<const float*>(wsum), 1, a->height,
+                                a->width, out));
+  ASUNA_CUDA_TRY(cudaStreamSynchronize(s));
+  // the halves' denoised outputs differ by twice the output variance of a
+  // half; doubling the samples is taken to halve that variance and keep the
+  // bias: err^2(all) = err^2(half) - var(half) / 2
+  const double varHalf = 0.5 * h / (3.0 * P);
+  if (err_denoised) *err_denoised = std::sqrt(std::max(0.0, eA * eA - 0.5 * varHalf));
+  if (err_plain) *err_plain = eP;
   return ASUNA_OK;
 }
 

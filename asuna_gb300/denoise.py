@@ -151,6 +151,17 @@ class Denoiser:
                                            normal_image, _ptr(out), C.byref(ed), C.byref(ep)))
         return out, ed.value, ep.value
 
+    def combined(self, film_a, film_b, albedo_image=1, normal_image=2, out=None):
+        """Denoises all samples of two half renders and estimates the RMSE of
+        that output and of the plain average against the converged image."""
+        torch = _torch()
+        if out is None:
+            out = torch.empty((film_a.height, film_a.width, 4), dtype=torch.float32, device="cuda")
+        ed, ep = C.c_double(), C.c_double()
+        check(lib().asuna_denoise_combined(self.ctx.handle, self.handle, film_a.handle, film_b.handle, albedo_image,
+                                           normal_image, _ptr(out), C.byref(ed), C.byref(ep)))
+        return out, ed.value, ep.value
+
     def close(self):
         if getattr(self, "handle", None):
             lib().asuna_denoiser_destroy(self.handle)

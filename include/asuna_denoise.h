@@ -95,6 +95,14 @@ int asuna_denoise(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* film, int albed
  * err_plain.  Writes D into `out` (device, film-sized RGBA32F). */
 int asuna_denoise_estimate(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asuna_film* b, int albedo_image,
                            int normal_image, float* out, double* err_denoised, double* err_plain);
+/* Denoises all samples of the two half renders (radiance (a + b) / 2, weight
+ * a + b, guides of a) into `out` and estimates the RMSE of that output:
+ * with D_a, D_b the denoised halves, var = mean((D_a - D_b)^2) / 2 is the
+ * output variance of a half, and doubling the samples is taken to halve it
+ * and keep the bias, so err_denoised^2 = err^2(D_a) - var / 2 (err(D_a) as in
+ * asuna_denoise_estimate).  err_plain estimates the plain average of a, b. */
+int asuna_denoise_combined(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asuna_film* b, int albedo_image,
+                           int normal_image, float* out, double* err_denoised, double* err_plain);
 
 /* Device-side building blocks (raw device pointers, NHWC bf16, the context
  * stream as `stream`); exported for kernel-level tests.  cin % 16 == 0 and

@@ -299,6 +299,23 @@ def test_film_denoise_and_error_estimate(dctx):
     assert np.isclose(ep, np.sqrt(mab / 4), rtol=1e-4)
     mdb = np.mean((den.cpu().numpy()[..., :3].astype(np.float64) - bb[..., :3]) ** 2)
     assert np.isclose(ed, np.sqrt(max(0.0, mdb - mab / 2)), rtol=1e-3, atol=1e-6)
+    # all samples: the output is the denoiser on (A + B) / 2 with weight A + B;
+    # the estimate subtracts half the halves' output variance
+    full, ec, ep2 = d.combined(fa, fb)
+    dctx.sync()
+    db_ = d.denoise(fb).cpu().numpy()
+    dctx.sync()
+    import torch
+
+    comb = 0.5 * (a + bb)
+    comb[..., 3] = 1.0
+    ref = d.forward(torch.from_numpy(comb)[None].cuda(), fa.tensor(1)[None].contiguous(),
+                    fa.tensor(2)[None].contiguous(), (fa.tensor(8) + fb.tensor(8))[None])
+    dctx.sync()
+    assert np.allclose(full.cpu().numpy(), ref[0].cpu().numpy(), atol=1e-6)
+    var_half = 0.5 * np.mean((den.cpu().numpy()[..., :3].astype(np.float64) - db_[..., :3]) ** 2)
+    assert np.isclose(ec, np.sqrt(max(0.0, ed * ed - 0.5 * var_half)), rtol=1e-3, atol=1e-6)
+    assert ep2 == pytest.approx(ep)
     with pytest.raises(A.AsunaError):
         d.denoise(fa, albedo_image=0)
     big = dctx.create_film(256, 256)
