@@ -303,8 +303,9 @@ def test_film_denoise_and_error_estimate(dctx):
     # the estimate subtracts half the halves' output variance
     full, ec, ep2 = d.combined(fa, fb)
     dctx.sync()
-    db_ = d.denoise(fb).cpu().numpy()
-    dctx.sync()
+    db_ = d.denoise(fb)
+    dctx.sync()  # the library's stream, not torch's: wait before the copy
+    db_ = db_.cpu().numpy()
     import torch
 
     comb = 0.5 * (a + bb)
