@@ -37,6 +37,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -51,7 +52,8 @@ namespace {
 constexpr int kTileH = 16, kTileW = 8;                         // pixels per MMA tile (M = 128)
 constexpr int kHaloH = kTileH + 2;
 constexpr int kMaxTiles = 4;                                   // tiles per CTA, side by side in x
-constexpr int kStages = 3;
+constexpr int kMaxStages = 8;  // copy-ring depth, chosen per layer in [2, 8]
+constexpr int kHeader = 256;   // barriers, the TMEM address and the abort flag
 // One TMA box of 8 channels covers the halo of T tiles: 18 x (8T + 2) pixels
 // of 16 bytes; its shared-memory slot is padded to 128 bytes.
 __host__ __device__ constexpr int haloW(int T) { return kTileW * T + 2; }
@@ -67,7 +69,12 @@ constexpr size_t kSmemLimit = 227 * 1024;
 // tap (2, 2) ends at ((2 * haloW + 2 + 8 (T-1)) + 15 haloW + 8) * 16 bytes =
 // 17 haloW * 16 = boxBytes, the end of the halo box, and the second 8-channel
 // chunk's at chunkBytes + boxBytes <= actStage.
-size_t smemFor(int nt, int T) { return 128 + size_t(kStages) * (actStage(T) + size_t(9 * 2 * nt * 16)); }
+__host__ __device__ constexpr int wStage(int nt) { return 9 * 2 * nt * 16; }  // one 16-channel group
+// S ring stages of activations; weights either in the ring (a stage per
+// group) or resident (all `groups` of the layer, loaded once per CTA)
+size_t smemFor(int nt, int T, int S, bool resident, int groups) {
+  return kHeader + size_t(S) * actStage(T) + size_t(resident ? groups : S) * wStage(nt);
+}
 uint32_t pow2Cols(int n) {
   uint32_t c = 32;
   while (c < uint32_t(n)) c <<= 1;
@@ -78,17 +85,57 @@ uint32_t pow2Cols(int n) {
 int sliceWidth(int cout) {
   for (int s = 1; s <= cout / 16; ++s) {
     const int nt = cout / s;
-    if (cout % s == 0 && nt % 16 == 0 && nt <= 256 && smemFor(nt, 1) <= kSmemLimit) return nt;
+    if (cout % s == 0 && nt % 16 == 0 && nt <= 256 && smemFor(nt, 1, 3, false, 0) <= kSmemLimit) return nt;
   }
   return 16;
 }
-// Pixel tiles per unit: as many (up to 4) as tensor memory (two buffers of T
-// accumulators of nt columns in 512) and shared memory hold and the image
-// width uses; the tiles share every weight stage.
-int tilesPerCta(int nt, int w) {
-  int T = kMaxTiles;
-  while (T > 1 && (pow2Cols(2 * T * nt) > 512 || smemFor(nt, T) > kSmemLimit || kTileW * (T - 1) >= w)) --T;
-  return T;
+// Pixel tiles per unit (T), resident CTAs per SM, ring depth and weight
+// residency: the choice with the most tiles in flight per SM (T x CTAs),
+// where a CTA needs two accumulator buffers of T x nt tensor-memory columns
+// (512 per SM), its shared memory, and 192 threads of 72 registers (four
+// CTAs fit); then resident weights (single-slice layers whose weights fit:
+// read from L2 once per CTA instead of once per unit), then the deepest ring
+// the CTAs' shared memory holds; ties go to smaller T (more CTAs, rings that
+// run independently).  T stays within the image width.
+struct TileShape {
+  int T, perSm, stages;
+  bool resident;
+};
+int shapePolicy() {
+  static const int p = [] {
+    const char* e = std::getenv("ASUNA_TC_SHAPE_POLICY");
+    return e ? std::atoi(e) : 0;
+  }();
+  return p;
+}
+TileShape tileShape(int nt, int slices, int groups, int w, size_t smemSm, size_t reserve) {
+  const int policy = shapePolicy();
+  TileShape best{1, 1, 2, false};
+  long long bestKey = -1;
+  for (int T = 1; T <= kMaxTiles; ++T) {
+    if (T > 1 && kTileW * (T - 1) >= w) break;
+    const uint32_t cols = pow2Cols(2 * T * nt);
+    if (cols > 512) break;
+    for (int res = 0; res <= (slices == 1 ? 1 : 0); ++res) {
+      if (smemFor(nt, T, 2, res, groups) > kSmemLimit) continue;
+      // CTAs per SM at the shallowest ring, then the deepest ring they allow
+      const int per = std::max(
+          1, std::min({int(smemSm / (smemFor(nt, T, 2, res, groups) + reserve)), 4, int(512 / cols)}));
+      const size_t budget = std::min(kSmemLimit, smemSm / size_t(per) - reserve);
+      int S = 2;
+      while (S < kMaxStages && smemFor(nt, T, S + 1, res, groups) <= budget) ++S;
+      if (res && S < 3) continue;  // resident weights only beside a ring of 3 or more
+      // policy 0: tiles in flight, then CTAs, residency, ring depth;
+      // policy 1: tiles in flight, then residency, ring depth (fewer, deeper CTAs)
+      const long long key = policy == 0 ? (((long long)(per * T) * 8 + per) * 2 + res) * 16 + S
+                                        : (((long long)(per * T) * 2 + res) * 16 + S) * 8 + (8 - T);
+      if (key > bestKey) {
+        bestKey = key;
+        best = {T, per, S, res != 0};
+      }
+    }
+  }
+  return best;
 }
 
 __device__ __forceinline__ uint32_t smem(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
@@ -98,19 +145,6 @@ __device__ __forceinline__ void mbarInit(uint32_t bar, uint32_t count) {
 }
 __device__ __forceinline__ void mbarExpectTx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-// bounded wait for phase `parity` of the barrier; false when it expired
-__device__ __forceinline__ bool mbarWait(uint32_t bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kWaitLimit; ++i) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
 }
 __device__ __forceinline__ void tmaLoad4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
                                           uint32_t bar) {
@@ -174,6 +208,8 @@ struct TcArgs {
   int relu, outF32;
   uint32_t tmemCols;          // two accumulator buffers of tiles * nt columns
   uint32_t wStageBytes;       // 9 * 2 * nt * 16
+  int stages;                 // copy-ring depth
+  int resident;               // weights loaded once per CTA (one slice)
 };
 
 // a unit: slice (fastest), then tile column, tile row, image
@@ -193,7 +229,12 @@ __device__ __forceinline__ Unit unitOf(const TcArgs& a, int u) {
   return r;
 }
 
-// bounded wait that also gives up once another role has recorded an abort
+// an abort flag that is never set: for the drains, which wait out the
+// copies and MMAs in flight even after an abort
+__device__ const int kNeverAbort = 0;
+
+// bounded wait for phase `parity` of the barrier, false when it expired;
+// it also gives up once another role has recorded an abort
 __device__ __forceinline__ bool mbarWaitOr(uint32_t bar, uint32_t parity, const volatile int* abortFlag) {
   for (uint32_t i = 0; i < kWaitLimit; ++i) {
     uint32_t done;
@@ -212,40 +253,48 @@ __device__ __forceinline__ void mbarArrive(uint32_t bar) {
 }
 
 // Persistent CTAs, warp-specialised: warps 0-3 are the epilogue (TMEM lane
-// quarter = warp), warp 4's first lane issues the TMA copies and the MMAs.
-// Units (T tiles of one channel slice) are taken round-robin; the copy ring
-// runs ahead across unit boundaries and the MMAs alternate between two
+// quarter = warp), warp 4's first lane issues the TMA copies, warp 5's first
+// lane the MMAs.  Units (T tiles of one channel slice) are taken
+// round-robin; the copy ring runs ahead across unit boundaries, the MMA
+// thread never waits for its own MMAs, and the MMAs alternate between two
 // accumulator buffers, so one unit's epilogue overlaps the next unit's
 // MMAs.  Barriers: full / empty per ring stage (copies landed / MMAs done
-// reading), accFull / accEmpty per accumulator buffer.
+// reading), accFull / accEmpty per accumulator buffer, drain (every MMA of
+// the CTA done, before TMEM is freed).
 constexpr int kEpiWarps = 4;
-constexpr int kThreads = 32 * (kEpiWarps + 1);
+constexpr int kProducerWarp = kEpiWarps, kMmaWarp = kEpiWarps + 1;
+constexpr int kThreads = 32 * (kEpiWarps + 2);
 
 __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__ CUtensorMap act, TcArgs a) {
   extern __shared__ __align__(1024) unsigned char sm[];
   // [0, 128): barriers, the TMEM address and the abort flag; then the
   // activation stages and the weight stages
   uint64_t* full = reinterpret_cast<uint64_t*>(sm);
-  uint64_t* empty = full + kStages;
-  uint64_t* accFull = empty + kStages;
+  uint64_t* empty = full + kMaxStages;
+  uint64_t* accFull = empty + kMaxStages;
   uint64_t* accEmpty = accFull + 2;
-  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(accEmpty + 2);
+  uint64_t* drain = accEmpty + 2;
+  uint64_t* wFull = drain + 1;  // resident weights landed
+  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(wFull + 1);
   volatile int* abortFlag = reinterpret_cast<volatile int*>(tmemSlot + 1);
-  const int T = a.tiles, hw = haloW(T);
+  static_assert((2 * kMaxStages + 6) * 8 + 8 <= kHeader, "barrier header");
+  const int T = a.tiles, hw = haloW(T), S = a.stages;
   const uint32_t chunk = uint32_t(chunkBytes(T)), stageA = uint32_t(actStage(T));
-  unsigned char* actBase = sm + 128;
-  unsigned char* wBase = actBase + kStages * stageA;
+  unsigned char* actBase = sm + kHeader;
+  unsigned char* wBase = actBase + S * stageA;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) {
+    for (int s = 0; s < S; ++s) {
       mbarInit(smem(&full[s]), 1);
       mbarInit(smem(&empty[s]), 1);
     }
+    mbarInit(smem(wFull), 1);
     for (int b = 0; b < 2; ++b) {
       mbarInit(smem(&accFull[b]), 1);
       mbarInit(smem(&accEmpty[b]), kEpiWarps);
     }
+    mbarInit(smem(drain), 1);
     // a CTA that finds an expired wait recorded skips its work: one failure
     // costs one timeout, not one per CTA
     *abortFlag = *reinterpret_cast<volatile int*>(&g_tcError) ? 1 : 0;
@@ -264,62 +313,88 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
   const uint32_t tmem = *tmemSlot;
   const int groups = a.cin / 16;
   const int myUnits = blockIdx.x < a.units ? (a.units - 1 - int(blockIdx.x)) / int(gridDim.x) + 1 : 0;
+  const int total = myUnits * groups;  // stream position q = (unit k of this CTA, channel group g)
   const uint32_t bufCols = uint32_t(T * a.nt);
+  auto fail = [&]() {
+    *abortFlag = 1;
+    atomicExch(&g_tcError, 1);
+  };
 
-  if (warp == kEpiWarps) {
+  if (warp == kProducerWarp) {
     if (lane == 0 && !*abortFlag) {
-      const uint32_t idesc = instrDesc(uint32_t(a.nt));
-      const int total = myUnits * groups;
-      // stream position q = (unit k of this CTA, channel group g)
-      auto issue = [&](int q) {
-        const int k = q / groups, g = q % groups, s = q % kStages;
+      if (a.resident && total > 0) {
+        // the whole layer's weights (one slice), once
+        mbarExpectTx(smem(wFull), uint32_t(groups) * a.wStageBytes);
+        bulkLoad(smem(wBase), a.wt, uint32_t(groups) * a.wStageBytes, smem(wFull));
+      }
+      int q = 0;
+      for (; q < total; ++q) {
+        const int k = q / groups, g = q % groups, s = q % S;
+        const uint32_t use = uint32_t(q / S);
+        // the MMAs of this stage's previous use are done reading it
+        if (use > 0 && !mbarWaitOr(smem(&empty[s]), (use - 1) & 1u, abortFlag)) break;
         const Unit U = unitOf(a, int(blockIdx.x) + k * int(gridDim.x));
         const __nv_bfloat16* wt = a.wt + size_t(U.slice) * size_t(groups) * (a.wStageBytes / 2);
         const uint32_t bar = smem(&full[s]);
-        mbarExpectTx(bar, uint32_t(2 * boxBytes(T)) + a.wStageBytes);
+        mbarExpectTx(bar, uint32_t(2 * boxBytes(T)) + (a.resident ? 0u : a.wStageBytes));
         const uint32_t dstA = smem(actBase + s * stageA);
         tmaLoad4d(dstA, &act, g * 16, U.x0 - 1, U.y0 - 1, U.img, bar);
         tmaLoad4d(dstA + chunk, &act, g * 16 + 8, U.x0 - 1, U.y0 - 1, U.img, bar);
-        bulkLoad(smem(wBase + size_t(s) * a.wStageBytes), wt + size_t(g) * (a.wStageBytes / 2), a.wStageBytes, bar);
-      };
-      bool ok = true;
-      for (int q = 0; q < total && q < kStages; ++q) issue(q);
-      for (int q = 0; q < total && ok; ++q) {
-        const int k = q / groups, g = q % groups, s = q % kStages;
-        const uint32_t use = uint32_t(q / kStages), buf = uint32_t(k & 1);
-        if (g == 0 && k >= 2) {
-          // the epilogue has read this buffer's previous unit out
-          if (!(ok = mbarWaitOr(smem(&accEmpty[buf]), uint32_t((k >> 1) - 1) & 1u, abortFlag))) break;
-          fenceAfter();
-        }
-        if (!(ok = mbarWaitOr(smem(&full[s]), use & 1u, abortFlag))) break;
-        const uint32_t aBase = smem(actBase + s * stageA);
-        const uint32_t bBase = smem(wBase + size_t(s) * a.wStageBytes);
+        if (!a.resident)
+          bulkLoad(smem(wBase + size_t(s) * a.wStageBytes), wt + size_t(g) * (a.wStageBytes / 2), a.wStageBytes,
+                   bar);
+      }
+      if (q < total) fail();
+      // the last copies of each stage have landed before the CTA may exit
+      for (int r = q - 1; r >= 0 && r >= q - S; --r)
+        mbarWaitOr(smem(&full[r % S]), uint32_t(r / S) & 1u, &kNeverAbort);
+      if (a.resident && total > 0) mbarWaitOr(smem(wFull), 0u, &kNeverAbort);
+    }
+  } else if (warp == kMmaWarp) {
+    if (lane == 0) {
+      if (!*abortFlag) {
+        const uint32_t idesc = instrDesc(uint32_t(a.nt));
         const uint32_t bTap = uint32_t(2 * a.nt * 16);
-        const uint32_t acc = tmem + buf * bufCols;
-#pragma unroll 1
-        for (int tap = 0; tap < 9; ++tap) {
-          const int dy = tap / 3, dx = tap % 3;
-          const uint64_t db = matDesc(bBase + uint32_t(tap) * bTap, uint32_t(a.nt * 16), 128u);
-          // tile t: the view starting 8 t pixels further along the halo
-          // rows; its accumulator is columns [t nt, (t + 1) nt) of the buffer
-          for (int t2 = 0; t2 < T; ++t2) {
-            const uint64_t da = matDesc(aBase + uint32_t(dy * hw + dx + kTileW * t2) * 16u, chunk, uint32_t(hw * 16));
-            mma(acc + uint32_t(t2 * a.nt), da, db, idesc, (g > 0 || tap > 0) ? 1u : 0u);
+        bool ok = !a.resident || total == 0 || mbarWaitOr(smem(wFull), 0u, abortFlag);
+        if (!ok) fail();
+        for (int q = 0; q < total && ok; ++q) {
+          const int k = q / groups, g = q % groups, s = q % S;
+          const uint32_t use = uint32_t(q / S), buf = uint32_t(k & 1);
+          if (g == 0 && k >= 2) {
+            // the epilogue has read this buffer's previous unit out
+            if (!mbarWaitOr(smem(&accEmpty[buf]), uint32_t((k >> 1) - 1) & 1u, abortFlag)) {
+              fail();
+              break;
+            }
+            fenceAfter();
           }
-        }
-        commit(smem(&empty[s]));
-        if (g == groups - 1) commit(smem(&accFull[buf]));
-        const int qn = q + kStages;
-        if (qn < total) {
-          if (!(ok = mbarWaitOr(smem(&empty[s]), use & 1u, abortFlag))) break;
-          issue(qn);
+          if (!mbarWaitOr(smem(&full[s]), use & 1u, abortFlag)) {
+            fail();
+            break;
+          }
+          fenceAfter();
+          const uint32_t aBase = smem(actBase + s * stageA);
+          const uint32_t bBase = smem(wBase + size_t(a.resident ? g : s) * a.wStageBytes);
+          const uint32_t acc = tmem + buf * bufCols;
+#pragma unroll 1
+          for (int tap = 0; tap < 9; ++tap) {
+            const int dy = tap / 3, dx = tap % 3;
+            const uint64_t db = matDesc(bBase + uint32_t(tap) * bTap, uint32_t(a.nt * 16), 128u);
+            // tile t: the view starting 8 t pixels further along the halo
+            // rows; its accumulator is columns [t nt, (t + 1) nt) of the buffer
+            for (int t2 = 0; t2 < T; ++t2) {
+              const uint64_t da =
+                  matDesc(aBase + uint32_t(dy * hw + dx + kTileW * t2) * 16u, chunk, uint32_t(hw * 16));
+              mma(acc + uint32_t(t2 * a.nt), da, db, idesc, (g > 0 || tap > 0) ? 1u : 0u);
+            }
+          }
+          commit(smem(&empty[s]));
+          if (g == groups - 1) commit(smem(&accFull[buf]));
         }
       }
-      if (!ok) {
-        *abortFlag = 1;
-        atomicExch(&g_tcError, 1);
-      }
+      // every MMA issued by this thread has finished before TMEM is freed
+      commit(smem(drain));
+      mbarWaitOr(smem(drain), 0u, &kNeverAbort);
     }
   } else {
     // epilogue: warp w owns TMEM lanes 32w..32w+31 = pixels 32w..32w+31 of each tile
@@ -327,10 +402,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
     for (int k = 0; k < myUnits; ++k) {
       const uint32_t buf = uint32_t(k & 1);
       if (!mbarWaitOr(smem(&accFull[buf]), uint32_t(k >> 1) & 1u, abortFlag)) {
-        if (lane == 0) {
-          *abortFlag = 1;
-          atomicExch(&g_tcError, 1);
-        }
+        if (lane == 0) fail();
         break;
       }
       fenceAfter();
@@ -341,32 +413,47 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
         for (int c0 = 0; c0 < a.nt; c0 += 16) {
           const int py = U.y0 + m / kTileW, px = U.x0 + kTileW * t2 + m % kTileW;
           const bool inside = py < a.h && px < a.w;
-          const size_t p = (size_t(U.img) * a.h + py) * a.w + px;
+          // 16 consecutive channels of one pixel: 32 B (bf16) or 64 B (f32),
+          // aligned as cout and n0 + c0 are multiples of 16
+          const size_t e = ((size_t(U.img) * a.h + py) * a.w + px) * size_t(a.cout) + size_t(n0 + c0);
           float v[16];
           ld16(laneBase + uint32_t(t2 * a.nt + c0), v);
           if (!inside) continue;
+          if (a.bias) {
+            const float4* b4 = reinterpret_cast<const float4*>(a.bias + n0 + c0);
 #pragma unroll
-          for (int i = 0; i < 16; i += 2) {
-            const int co = n0 + c0 + i;
-            float v0 = v[i], v1 = v[i + 1];
-            if (a.bias) {
-              v0 += a.bias[co];
-              v1 += a.bias[co + 1];
+            for (int i = 0; i < 4; ++i) {
+              const float4 b = __ldg(&b4[i]);
+              v[4 * i] += b.x;
+              v[4 * i + 1] += b.y;
+              v[4 * i + 2] += b.z;
+              v[4 * i + 3] += b.w;
             }
-            if (a.relu) {
-              v0 = fmaxf(v0, 0.0f);
-              v1 = fmaxf(v1, 0.0f);
-            }
-            if (a.mask) {
-              const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162*>(a.mask + p * a.cout + co);
-              if (!(__bfloat162float(mk.x) > 0.0f)) v0 = 0.0f;
-              if (!(__bfloat162float(mk.y) > 0.0f)) v1 = 0.0f;
-            }
-            if (a.outF32)
-              *reinterpret_cast<float2*>(static_cast<float*>(a.out) + p * a.cout + co) = make_float2(v0, v1);
-            else
-              *reinterpret_cast<__nv_bfloat162*>(static_cast<__nv_bfloat16*>(a.out) + p * a.cout + co) =
-                  __floats2bfloat162_rn(v0, v1);
+          }
+          if (a.relu) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.0f);
+          }
+          if (a.mask) {
+            const uint4* m4 = reinterpret_cast<const uint4*>(a.mask + e);
+            const uint4 mm[2] = {m4[0], m4[1]};
+            const __nv_bfloat16* mk = reinterpret_cast<const __nv_bfloat16*>(mm);
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+              if (!(__bfloat162float(mk[i]) > 0.0f)) v[i] = 0.0f;
+          }
+          if (a.outF32) {
+            float4* o4 = reinterpret_cast<float4*>(static_cast<float*>(a.out) + e);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) o4[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+          } else {
+            uint4 pk[2];
+            __nv_bfloat162* h2 = reinterpret_cast<__nv_bfloat162*>(pk);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) h2[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+            uint4* o4 = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(a.out) + e);
+            o4[0] = pk[0];
+            o4[1] = pk[1];
           }
         }
       // this warp's lanes of the buffer are read: hand it back to the MMAs
@@ -435,11 +522,20 @@ int asuna_nn_conv3x3_tc(void* stream, const void* in, int n, int h, int w, int c
     return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: bad argument");
   if (cin % 16 || cout % 16)
     return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: cin %% 16 and cout %% 16 required");
-  if (reinterpret_cast<uintptr_t>(in) % 16 || reinterpret_cast<uintptr_t>(weight_tc) % 16)
+  // the copies and the epilogue's 16-byte loads and stores need 16-byte bases
+  if ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(weight_tc) | reinterpret_cast<uintptr_t>(bias) |
+       reinterpret_cast<uintptr_t>(mask) | reinterpret_cast<uintptr_t>(out)) % 16)
     return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: operands must be 16-byte aligned");
   EncodeTiledFn enc = encodeFn();
   if (!enc) return fail(ASUNA_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
-  const int nt = sliceWidth(cout), T = tilesPerCta(nt, w);
+  int dev = 0, sms = 1, smemSm = 0, reserve = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&smemSm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&reserve, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  const int nt = sliceWidth(cout);
+  const TileShape shape = tileShape(nt, cout / nt, cin / 16, w, size_t(smemSm), size_t(reserve));
+  const int T = shape.T;
   // NHWC bf16 as a 4-D tensor (C, W, H, N); box = 8 channels x the T tiles' halo
   CUtensorMap map;
   const cuuint64_t dims[4] = {cuuint64_t(cin), cuuint64_t(w), cuuint64_t(h), cuuint64_t(n)};
@@ -468,23 +564,24 @@ int asuna_nn_conv3x3_tc(void* stream, const void* in, int n, int h, int w, int c
   a.nt = nt;
   a.slices = cout / a.nt;
   a.tmemCols = pow2Cols(2 * T * nt);
-  a.wStageBytes = uint32_t(9 * 2 * a.nt * 16);
-  const size_t smemBytes = smemFor(a.nt, T);
+  a.wStageBytes = uint32_t(wStage(a.nt));
+  a.stages = shape.stages;
+  a.resident = shape.resident ? 1 : 0;
+  const size_t smemBytes = smemFor(a.nt, T, a.stages, shape.resident, cin / 16);
   static std::once_flag attr;
   std::call_once(attr, [] {
     cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemLimit));
+    // the whole unified L1 as shared memory, so two CTAs of ~87 KB share an
+    // SM (and the occupancy query below counts them)
+    cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   });
   if (smemBytes > kSmemLimit) return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: cout %d needs too much shared memory", cout);
   const long long units = (long long)a.tilesX * a.tilesY * n * a.slices;
   if (units > (1ll << 31) - 1) return fail(ASUNA_ERR_INVALID, "asuna_nn_conv3x3_tc: too many tiles");
   a.units = int(units);
-  // persistent grid: the CTAs that fit on the device at once (shared memory,
-  // and tensor memory: 512 columns per SM), or fewer when there is less work
-  int dev = 0, sms = 1, perSm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_conv_tc, kThreads, smemBytes);
-  perSm = std::max(1, std::min(perSm, int(512 / a.tmemCols)));
+  // persistent grid: the CTAs that fit on the device at once, or fewer
+  // when there is less work
+  const int perSm = shape.perSm;
   const long long grid = std::min<long long>(units, (long long)sms * perSm);
   k_conv_tc<<<unsigned(std::max<long long>(grid, 1)), kThreads, smemBytes, static_cast<cudaStream_t>(stream)>>>(map,
                                                                                                                  a);
