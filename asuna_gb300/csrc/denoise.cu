@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <initializer_list>
 #include <new>
 #include <vector>
 
@@ -365,6 +366,130 @@ __global__ void k_copy_channels(const __nv_bfloat16* src, int Csrc, int sOff, __
   }
 }
 
+// The same five layout operations on 8-channel (16-byte) chunks, for
+// channel counts and offsets that are multiples of 8 and 16-byte aligned
+// buffers; I is the index type (32-bit when every buffer has fewer than 2^32
+// chunks).  Per element they compute what the scalar kernels above do, in
+// the same order, with no contraction into fused multiply-adds.
+struct Bf8 {
+  float v[8];
+};
+__device__ __forceinline__ Bf8 unpack8(uint4 u) {
+  Bf8 r;
+  const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float2 f = __bfloat1622float2(h[i]);
+    r.v[2 * i] = f.x;
+    r.v[2 * i + 1] = f.y;
+  }
+  return r;
+}
+__device__ __forceinline__ uint4 pack8(const Bf8& r) {
+  uint4 u;
+  __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(&u);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(r.v[2 * i], r.v[2 * i + 1]);
+  return u;
+}
+
+template <typename I>
+__global__ void k_avgpool2_v(const uint4* in, uint4* out, I N, I H, I W, I C8) {
+  const I Ho = H / 2, Wo = W / 2, total = N * Ho * Wo * C8;
+  for (I i = I(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += I(gridDim.x) * blockDim.x) {
+    const I c = i % C8, q = i / C8, x = q % Wo, t = q / Wo, y = t % Ho, n = t / Ho;
+    const uint4* b = in + ((n * H + 2 * y) * W + 2 * x) * C8 + c;
+    const Bf8 a0 = unpack8(__ldg(b)), a1 = unpack8(__ldg(b + C8)), a2 = unpack8(__ldg(b + W * C8)),
+              a3 = unpack8(__ldg(b + W * C8 + C8));
+    Bf8 r;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) r.v[k] = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(a0.v[k], a1.v[k]), a2.v[k]), a3.v[k]));
+    out[i] = pack8(r);
+  }
+}
+
+template <typename I>
+__global__ void k_avgpool2_bwd_v(const uint4* dout, uint4* din, I N, I H, I W, I C8, int accumulate) {
+  const I total = N * H * W * C8;
+  for (I i = I(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += I(gridDim.x) * blockDim.x) {
+    const I c = i % C8, q = i / C8, x = q % W, t = q / W, y = t % H, n = t / H;
+    const Bf8 g = unpack8(__ldg(&dout[((n * (H / 2) + y / 2) * (W / 2) + x / 2) * C8 + c]));
+    Bf8 r;
+    if (accumulate) {
+      const Bf8 o = unpack8(din[i]);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) r.v[k] = __fadd_rn(o.v[k], __fmul_rn(0.25f, g.v[k]));
+    } else {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) r.v[k] = __fmul_rn(0.25f, g.v[k]);
+    }
+    din[i] = pack8(r);
+  }
+}
+
+template <typename I>
+__global__ void k_upsample2_v(const uint4* in, uint4* out, I N, I H, I W, I C8, I Ct8, I cOff8) {
+  const I total = N * H * W * C8;  // H, W of the output
+  for (I i = I(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += I(gridDim.x) * blockDim.x) {
+    const I c = i % C8, q = i / C8, x = q % W, t = q / W, y = t % H, n = t / H;
+    out[q * Ct8 + cOff8 + c] = __ldg(&in[((n * (H / 2) + y / 2) * (W / 2) + x / 2) * C8 + c]);
+  }
+}
+
+template <typename I>
+__global__ void k_upsample2_bwd_v(const uint4* dout, uint4* din, I N, I H, I W, I C8, I Ct8, I cOff8) {
+  const I total = N * H * W * C8;  // H, W of the (small) input
+  for (I i = I(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += I(gridDim.x) * blockDim.x) {
+    const I c = i % C8, q = i / C8, x = q % W, t = q / W, y = t % H, n = t / H;
+    const I W2 = 2 * W;
+    const uint4* b = dout + ((n * 2 * H + 2 * y) * W2 + 2 * x) * Ct8 + cOff8 + c;
+    const Bf8 a0 = unpack8(__ldg(b)), a1 = unpack8(__ldg(b + Ct8)), a2 = unpack8(__ldg(b + W2 * Ct8)),
+              a3 = unpack8(__ldg(b + W2 * Ct8 + Ct8));
+    Bf8 r;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) r.v[k] = __fadd_rn(__fadd_rn(__fadd_rn(a0.v[k], a1.v[k]), a2.v[k]), a3.v[k]);
+    din[i] = pack8(r);
+  }
+}
+
+template <typename I>
+__global__ void k_copy_channels_v(const uint4* src, I Cs8, I sOff8, uint4* dst, I Cd8, I dOff8, I C8, I P,
+                                  int accumulate) {
+  const I total = P * C8;
+  for (I i = I(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += I(gridDim.x) * blockDim.x) {
+    const I p = i / C8, c = i % C8;
+    const uint4 v = __ldg(&src[p * Cs8 + sOff8 + c]);
+    uint4& d = dst[p * Cd8 + dOff8 + c];
+    if (accumulate) {
+      const Bf8 a = unpack8(d), b = unpack8(v);
+      Bf8 r;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) r.v[k] = __fadd_rn(a.v[k], b.v[k]);
+      d = pack8(r);
+    } else {
+      d = v;
+    }
+  }
+}
+
+// decoder input in one pass: out[p] = (up2(low)[p] channels 0..Cu, skip[p]
+// channels 0..Cs); every chunk of out written once, in order
+template <typename I>
+__global__ void k_upsample_concat_v(const uint4* low, const uint4* skip, uint4* out, I N, I H, I W, I Cu8, I Cs8) {
+  const I Ct8 = Cu8 + Cs8, total = N * H * W * Ct8;
+  for (I i = I(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += I(gridDim.x) * blockDim.x) {
+    const I c = i % Ct8, q = i / Ct8;
+    uint4 v;
+    if (c < Cu8) {
+      const I x = q % W, t = q / W, y = t % H, n = t / H;
+      v = __ldg(&low[((n * (H / 2) + y / 2) * (W / 2) + x / 2) * Cu8 + c]);
+    } else {
+      v = __ldg(&skip[q * Cs8 + (c - Cu8)]);
+    }
+    out[i] = v;
+  }
+}
+
 // Network input: log1p(radiance), albedo, normal, zeros up to C; pixels
 // outside the h x w image (padding up to hp x wp) are zero.
 // Network input: log1p(radiance), albedo, normal, log2(1 + filter-weight
@@ -558,6 +683,27 @@ using namespace asuna::nn;
     return ASUNA_OK;                                                                               \
   } while (0)
 
+namespace {
+bool al16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+// the chunked kernels: channel counts and offsets multiples of 8, 16-byte
+// bases; chunks = the largest buffer's 16-byte count (32-bit indexing below 2^32)
+bool vec8(std::initializer_list<int> chans, std::initializer_list<const void*> ptrs) {
+  for (int c : chans)
+    if (c % 8) return false;
+  for (const void* p : ptrs)
+    if (!al16(p)) return false;
+  return true;
+}
+bool small32(size_t chunks) { return chunks < (size_t(1) << 32); }
+#define NN_LAUNCH_V(KERNEL, COUNT, CHUNKS, ...)                                                              \
+  do {                                                                                                      \
+    if (small32(CHUNKS))                                                                                    \
+      KERNEL<uint32_t><<<grid1d(COUNT), 256, 0, static_cast<cudaStream_t>(stream)>>>(__VA_ARGS__);         \
+    else                                                                                                    \
+      KERNEL<size_t><<<grid1d(COUNT), 256, 0, static_cast<cudaStream_t>(stream)>>>(__VA_ARGS__);           \
+  } while (0)
+}  // namespace
+
 extern "C" {
 
 int asuna_nn_conv3x3(void* stream, const void* in, int n, int h, int w, int cin, const void* weight, const float* bias,
@@ -600,25 +746,50 @@ int asuna_nn_flip_weights(void* stream, const void* w, void* wt, int cout, int c
   NN_CHECK_LAUNCH();
 }
 
+
 int asuna_nn_avgpool2(void* stream, const void* in, void* out, int n, int h, int w, int c) {
+  if (vec8({c}, {in, out})) {
+    const size_t chunks = size_t(n) * h * w * (c / 8);
+    NN_LAUNCH_V(k_avgpool2_v, chunks / 4, chunks, static_cast<const uint4*>(in), static_cast<uint4*>(out), n, h, w,
+                c / 8);
+    NN_CHECK_LAUNCH();
+  }
   k_avgpool2<<<grid1d(size_t(n) * h * w * c / 4), 256, 0, static_cast<cudaStream_t>(stream)>>>(
       static_cast<const __nv_bfloat16*>(in), static_cast<__nv_bfloat16*>(out), n, h, w, c);
   NN_CHECK_LAUNCH();
 }
 
 int asuna_nn_avgpool2_bwd(void* stream, const void* dout, void* din, int n, int h, int w, int c, int accumulate) {
+  if (vec8({c}, {dout, din})) {
+    const size_t chunks = size_t(n) * h * w * (c / 8);
+    NN_LAUNCH_V(k_avgpool2_bwd_v, chunks, chunks, static_cast<const uint4*>(dout), static_cast<uint4*>(din), n, h,
+                w, c / 8, accumulate);
+    NN_CHECK_LAUNCH();
+  }
   k_avgpool2_bwd<<<grid1d(size_t(n) * h * w * c), 256, 0, static_cast<cudaStream_t>(stream)>>>(
       static_cast<const __nv_bfloat16*>(dout), static_cast<__nv_bfloat16*>(din), n, h, w, c, accumulate);
   NN_CHECK_LAUNCH();
 }
 
 int asuna_nn_upsample2(void* stream, const void* in, void* out, int n, int h, int w, int c, int ctot, int coff) {
+  if (vec8({c, ctot, coff}, {in, out})) {
+    const size_t chunks = size_t(n) * h * w * (ctot / 8);
+    NN_LAUNCH_V(k_upsample2_v, size_t(n) * h * w * (c / 8), chunks, static_cast<const uint4*>(in),
+                static_cast<uint4*>(out), n, h, w, c / 8, ctot / 8, coff / 8);
+    NN_CHECK_LAUNCH();
+  }
   k_upsample2<<<grid1d(size_t(n) * h * w * c), 256, 0, static_cast<cudaStream_t>(stream)>>>(
       static_cast<const __nv_bfloat16*>(in), static_cast<__nv_bfloat16*>(out), n, h, w, c, ctot, coff);
   NN_CHECK_LAUNCH();
 }
 
 int asuna_nn_upsample2_bwd(void* stream, const void* dout, void* din, int n, int h, int w, int c, int ctot, int coff) {
+  if (vec8({c, ctot, coff}, {dout, din})) {
+    const size_t chunks = size_t(n) * 4 * h * w * (ctot / 8);
+    NN_LAUNCH_V(k_upsample2_bwd_v, size_t(n) * h * w * (c / 8), chunks, static_cast<const uint4*>(dout),
+                static_cast<uint4*>(din), n, h, w, c / 8, ctot / 8, coff / 8);
+    NN_CHECK_LAUNCH();
+  }
   k_upsample2_bwd<<<grid1d(size_t(n) * h * w * c), 256, 0, static_cast<cudaStream_t>(stream)>>>(
       static_cast<const __nv_bfloat16*>(dout), static_cast<__nv_bfloat16*>(din), n, h, w, c, ctot, coff);
   NN_CHECK_LAUNCH();
@@ -626,6 +797,12 @@ int asuna_nn_upsample2_bwd(void* stream, const void* dout, void* din, int n, int
 
 int asuna_nn_copy_channels(void* stream, const void* src, int csrc, int soff, void* dst, int cdst, int doff, int c,
                            uint64_t pixels, int accumulate) {
+  if (vec8({csrc, soff, cdst, doff, c}, {src, dst})) {
+    const size_t chunks = size_t(pixels) * (std::max(csrc, cdst) / 8);
+    NN_LAUNCH_V(k_copy_channels_v, size_t(pixels) * (c / 8), chunks, static_cast<const uint4*>(src), csrc / 8,
+                soff / 8, static_cast<uint4*>(dst), cdst / 8, doff / 8, c / 8, pixels, accumulate);
+    NN_CHECK_LAUNCH();
+  }
   k_copy_channels<<<grid1d(pixels * c), 256, 0, static_cast<cudaStream_t>(stream)>>>(
       static_cast<const __nv_bfloat16*>(src), csrc, soff, static_cast<__nv_bfloat16*>(dst), cdst, doff, c, pixels,
       accumulate);
@@ -791,6 +968,19 @@ int dims(const asuna_denoiser* d, uint32_t n, uint32_t h, uint32_t w, Dims& o) {
   return ASUNA_OK;
 }
 
+// decoder input: the upsampled lower level beside the skip connection
+int upsampleConcat(cudaStream_t stream, const __nv_bfloat16* low, const __nv_bfloat16* skip, __nv_bfloat16* out, int n,
+                   int h, int w, int cu, int cs, size_t P) {
+  if (vec8({cu, cs}, {low, skip, out})) {
+    const size_t chunks = P * ((cu + cs) / 8);
+    NN_LAUNCH_V(k_upsample_concat_v, chunks, chunks, reinterpret_cast<const uint4*>(low),
+                reinterpret_cast<const uint4*>(skip), reinterpret_cast<uint4*>(out), n, h, w, cu / 8, cs / 8);
+    NN_CHECK_LAUNCH();
+  }
+  NN_TRY(asuna_nn_upsample2(stream, low, out, n, h, w, cu, cu + cs, 0));
+  return asuna_nn_copy_channels(stream, skip, cs, 0, out, cu + cs, cu, cs, P, 0);
+}
+
 int forward(asuna_denoiser* d, const float* rad, const float* alb, const float* nrm, const float* wsum,
             const Dims& D) {
   const int L = d->L;
@@ -814,8 +1004,7 @@ int forward(asuna_denoiser* d, const float* rad, const float* alb, const float* 
     LevelBufs& b = d->lv[l];
     const __nv_bfloat16* src = (l == L - 2) ? d->lv[L - 1].S : d->lv[l + 1].D;
     const int cu = d->ch[l + 1], cs = d->ch[l], ct = cu + cs;
-    NN_TRY(asuna_nn_upsample2(s, src, b.U, D.n, hl, wl, cu, ct, 0));
-    NN_TRY(asuna_nn_copy_channels(s, b.S, cs, 0, b.U, ct, cu, cs, Pl, 0));
+    NN_TRY(upsampleConcat(s, src, b.S, b.U, D.n, hl, wl, cu, cs, Pl));
     NN_TRY(convFwd(d, d->dec(l, 0), b.U, D.n, hl, wl, true, b.B, false));
     NN_TRY(convFwd(d, d->dec(l, 1), b.B, D.n, hl, wl, true, b.D, false));
   }

@@ -191,6 +191,17 @@ def test_pool_upsample_copy_and_mask(lib):
     dst = torch.zeros((n, h, w, 16), dtype=torch.bfloat16, device="cuda")
     run(lib, "asuna_nn_copy_channels", ptr(big), 48, 10, ptr(dst), 16, 4, 8, n * h * w, 0)
     assert np.array_equal(host(dst)[..., 4:12], hb[..., 10:18])
+    # 8-channel-aligned offsets take the 16-byte kernels; accumulate adds in fp32
+    run(lib, "asuna_nn_copy_channels", ptr(big), 48, 8, ptr(dst), 16, 8, 8, n * h * w, 1)
+    want = host(dst)
+    assert np.array_equal(want[..., 8:12], U.round_bf16(hb[..., 14:18] + hb[..., 8:12]))
+    assert np.array_equal(want[..., 12:16], hb[..., 12:16]) and np.array_equal(want[..., 4:8], hb[..., 10:14])
+    # channel counts that are not multiples of 8 take the per-element kernels
+    x12 = U.round_bf16(rng.normal(size=(n, h, w, 12)))
+    o12 = torch.empty((n, h // 2, w // 2, 12), dtype=torch.bfloat16, device="cuda")
+    d12 = bf16(x12)
+    run(lib, "asuna_nn_avgpool2", ptr(d12), ptr(o12), n, h, w, 12)
+    assert np.abs(host(o12) - U.round_bf16(U.avgpool2(x12))).max() <= 2.0 ** -7 * np.abs(x12).max()
     m = bf16(x)
     y = U.round_bf16(rng.normal(size=x.shape))
     dy = bf16(y)
