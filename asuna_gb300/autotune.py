@@ -19,7 +19,7 @@ def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64), trace_
     extend, refill shadow, speculate extend, speculate shadow, traversal blocks per SM), "ray_sort": 0..3,
     "mrays": best, "trials": [...]} and leaves the context configured with the best choice.  Coordinate
     search: frames, then grids, then the traversal kernel variant and the refill thresholds and
-    speculation of each pass, then extend-queue sorting."""
+    speculation of each pass, then extend-queue sorting, then the refill thresholds again under it."""
     npix = shot.width * shot.height
     saved = (shot.frame0, shot.frames)
     trials = []
@@ -78,6 +78,18 @@ def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64), trace_
             if v > best["mrays"]:
                 best = {**best, "ray_sort": mode, "mrays": v}
         ctx.set_ray_sort(best["ray_sort"])
+        # sorted queues walk the BVH more coherently: the refill thresholds
+        # again, with the chosen sort
+        for index, value in [(0, r) for r in refill_options + (32,)] + [(1, r) for r in refill_options]:
+            trav = list(best["traversal"])
+            if trav[index] == value:
+                continue
+            trav[index] = value
+            v = run(best["frames"], best["trace_blocks_per_sm"], best["shade_blocks_per_sm"])
+            trials.append({"frames": best["frames"], "traversal": tuple(trav), "ray_sort": best["ray_sort"],
+                           "mrays": v})
+            if v > best["mrays"]:
+                best = {**best, "traversal": tuple(trav), "mrays": v}
     finally:
         shot.frame0, shot.frames = saved
     ctx.set_traversal(*best["traversal"])
