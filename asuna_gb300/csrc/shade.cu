@@ -1077,7 +1077,7 @@ __device__ __forceinline__ void sampleDielectric(PathIO& io, const HitSt& st, co
 
 // ---------------------------------------------------------------------------
 // Splits the hits of the extend queue into the shading classes (material
-// sort): one warp-aggregated append per class and warp.  Classes that no hit
+// sort): one warp-aggregated append per class present in a warp.  Classes that no hit
 // of a pass uses cost one empty launch.
 __global__ void __launch_bounds__(256) k_classify(KParams P) {
   const WaveDev& W = P.W;
@@ -1101,11 +1101,13 @@ __global__ void __launch_bounds__(256) k_classify(KParams P) {
         }
       }
     }
-#pragma unroll
-    for (int k = 0; k < kNumShadeClasses; ++k) {
-      const uint32_t slot = warpAppend(cls == k, &W.cnt->c[kCntCls0 + k]);
-      if (cls == k) W.cls[k][slot] = i;
-    }
+    // lanes grouped by class: one append per class present in the warp
+    const unsigned peers = __match_any_sync(0xffffffffu, cls);
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (int(laneId()) == leader && cls >= 0) base = atomicAdd(&W.cnt->c[kCntCls0 + cls], uint32_t(__popc(peers)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (cls >= 0) W.cls[cls][base + uint32_t(__popc(peers & ((1u << laneId()) - 1u)))] = i;
   }
 }
 
