@@ -56,7 +56,7 @@ def _bind():
 
 
 class Server:
-    def __init__(self, device=0, slots=2, frames_per_chunk=4, max_batch=8, max_queue=0, memory_budget=150 << 30,
+    def __init__(self, device=0, slots=3, frames_per_chunk=16, max_batch=8, max_queue=0, memory_budget=150 << 30,
                  path_budget=0):
         self.L = _bind()
         o = ServerOpts(device, slots, frames_per_chunk, max_batch, max_queue, 0, memory_budget, path_budget)

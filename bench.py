@@ -664,8 +664,8 @@ def main():
     ap.add_argument("--batch", action="store_true", help="32 batched shots vs 32 sequential calls")
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-requests", type=int, default=600)
-    ap.add_argument("--serve-slots", type=int, default=2)
-    ap.add_argument("--serve-chunk", type=int, default=4)
+    ap.add_argument("--serve-slots", type=int, default=3)
+    ap.add_argument("--serve-chunk", type=int, default=16)
     ap.add_argument("--serve-max-queue", type=int, default=256)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
