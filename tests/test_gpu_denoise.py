@@ -333,3 +333,5 @@ def test_film_denoise_and_error_estimate(dctx):
     big = dctx.create_film(256, 256)
     with pytest.raises(A.AsunaError):
         d.denoise(big)  # larger than max_pixels: rejected, not overrun
+    with pytest.raises(A.AsunaError):
+        d.combined(fa, big)  # the halves must have one size
