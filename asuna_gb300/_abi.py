@@ -203,6 +203,8 @@ SIGNATURES = [
                                           C.POINTER(C.c_double)]),
     ("asuna_denoise_combined", C.c_int, [P, P, P, P, C.c_int, C.c_int, P, C.POINTER(C.c_double),
                                           C.POINTER(C.c_double)]),
+    ("asuna_denoise_blended", C.c_int, [P, P, P, P, C.c_int, C.c_int, P, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double)]),
     ("asuna_nn_conv3x3", C.c_int, [P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, C.c_int, C.c_int, P, P,
                                     C.c_int]),
     ("asuna_nn_conv3x3_wgrad", C.c_int, [P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P]),

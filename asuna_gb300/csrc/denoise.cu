@@ -644,6 +644,47 @@ __global__ void k_combine(const float4* da, const float4* db, const float4* a, c
   if ((threadIdx.x & 31) == 0) atomicAdd(&sums[2], double(s0));
 }
 
+// Sums for the blend of the denoised and plain images (rgb, over pixels):
+// with da, db the denoised halves and a, b the halves' radiance,
+//   [3] (da - b)^2   [4] (da - b)(a - b)   [5] (a - b)^2
+//   [6] (da - db)^2  [7] (da - db)(a - b)
+// and the input of the all-sample denoise: radiance (a + b) / 2, weight a + b.
+__global__ void k_blend_sums(const float4* da, const float4* db, const float4* a, const float4* b, const float4* wa,
+                             const float4* wb, float4* rad, float4* wsum, size_t P, double* sums) {
+  float s[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+  for (size_t p = blockIdx.x * size_t(blockDim.x) + threadIdx.x; p < P; p += size_t(gridDim.x) * blockDim.x) {
+    const float4 x = da[p], y = db[p], av = a[p], bv = b[p], w0 = wa[p], w1 = wb[p];
+    const float xb[3] = {x.x - bv.x, x.y - bv.y, x.z - bv.z}, ab[3] = {av.x - bv.x, av.y - bv.y, av.z - bv.z};
+    const float xy[3] = {x.x - y.x, x.y - y.y, x.z - y.z};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      s[0] += xb[c] * xb[c];
+      s[1] += xb[c] * ab[c];
+      s[2] += ab[c] * ab[c];
+      s[3] += xy[c] * xy[c];
+      s[4] += xy[c] * ab[c];
+    }
+    rad[p] = make_float4(0.5f * (av.x + bv.x), 0.5f * (av.y + bv.y), 0.5f * (av.z + bv.z), 1.0f);
+    wsum[p] = make_float4(w0.x + w1.x, w0.y + w1.y, w0.z + w1.z, w0.w + w1.w);
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    float v = s[k];
+    for (int off = 16; off; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&sums[3 + k], double(v));
+  }
+}
+
+// out = w out + (1 - w) (a + b) / 2 on rgb; alpha 1
+__global__ void k_blend(float4* out, const float4* a, const float4* b, float w, size_t P) {
+  for (size_t p = blockIdx.x * size_t(blockDim.x) + threadIdx.x; p < P; p += size_t(gridDim.x) * blockDim.x) {
+    const float4 o = out[p], av = a[p], bv = b[p];
+    const float v = 1.0f - w;
+    out[p] = make_float4(w * o.x + v * (0.5f * (av.x + bv.x)), w * o.y + v * (0.5f * (av.y + bv.y)),
+                         w * o.z + v * (0.5f * (av.z + bv.z)), 1.0f);
+  }
+}
+
 // Adam on fp32 master weights; writes the bf16 copy used by the kernels.
 __global__ void k_adam(float* w, float* m, float* v, const float* g, __nv_bfloat16* wb, size_t n, float lr, float b1,
                        float b2, float eps, float c1, float c2) {
@@ -1118,7 +1159,7 @@ int asuna_denoiser_create(asuna_ctx* ctx, const asuna_denoiser_opts* o, asuna_de
     A(&d->wtcT, d->nFlip);
   }
   A(&d->dLoss, 1);
-  A(&d->dSums, 3);
+  A(&d->dSums, 8);
   if (d->training) {
     A(&d->grad, d->nParams);
     A(&d->m, d->nParams);
@@ -1348,6 +1389,57 @@ int asuna_denoise_combined(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asu
   const double varHalf = 0.5 * h / (3.0 * P);
   if (err_denoised) *err_denoised = std::sqrt(std::max(0.0, eA * eA - 0.5 * varHalf));
   if (err_plain) *err_plain = eP;
+  return ASUNA_OK;
+}
+
+
+int asuna_denoise_blended(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asuna_film* b, int albedo_image,
+                          int normal_image, float* out, double* err_out, double* err_plain, double* weight) {
+  clearError();
+  if (!ctx || !d || !a || !b || !out) return fail(ASUNA_ERR_INVALID, "asuna_denoise_blended: null argument");
+  if (a->width != b->width || a->height != b->height)
+    return fail(ASUNA_ERR_INVALID, "asuna_denoise_blended: films differ in size");
+  cudaStream_t s = ctx->stream;
+  const size_t P = size_t(a->width) * a->height;
+  float4* scratch = nullptr;
+  ASUNA_CUDA_TRY(cudaMallocAsync(&scratch, 4 * P * sizeof(float4), s));
+  struct Free {
+    float4* p;
+    cudaStream_t s;
+    ~Free() { cudaFreeAsync(p, s); }
+  } guard{scratch, s};
+  float4 *da = scratch, *db = da + P, *rad = db + P, *wsum = rad + P;
+  NN_TRY(asuna_denoise(ctx, d, a, albedo_image, normal_image, reinterpret_cast<float*>(da)));
+  NN_TRY(asuna_denoise(ctx, d, b, albedo_image, normal_image, reinterpret_cast<float*>(db)));
+  ASUNA_CUDA_TRY(cudaMemsetAsync(d->dSums + 3, 0, 5 * sizeof(double), s));
+  k_blend_sums<<<grid1d(P), 256, 0, s>>>(da, db, a->rad, b->rad, a->w, b->w, rad, wsum, P, d->dSums);
+  ASUNA_CUDA_TRY(cudaGetLastError());
+  double h[5];
+  ASUNA_CUDA_TRY(cudaMemcpyAsync(h, d->dSums + 3, sizeof(h), cudaMemcpyDeviceToHost, s));
+  NN_TRY(asuna_denoiser_forward(d, reinterpret_cast<const float*>(rad), filmImage(a, albedo_image),
+                                filmImage(a, normal_image), reinterpret_cast<const float*>(wsum), 1, a->height,
+                                a->width, out));
+  ASUNA_CUDA_TRY(cudaStreamSynchronize(s));
+  // X_half = w D_a + (1 - w) a, judged by b: err^2 = mean((X_half - b)^2) -
+  // mean((a - b)^2) / 2; all samples: minus a quarter of mean((X_a - X_b)^2).
+  // Both quadratic in w: f(w) = alpha w^2 + 2 beta w + gamma.
+  const double n = 3.0 * double(P);
+  const double Sdd = h[0] / n, Sda = h[1] / n, Saa = h[2] / n, Qdd = h[3] / n, Qda = h[4] / n;
+  const double alpha = (Sdd - 2.0 * Sda + Saa) - 0.25 * (Qdd - 2.0 * Qda + Saa);
+  const double beta = (Sda - Saa) - 0.25 * (Qda - Saa);
+  const double gamma = 0.25 * Saa;
+  auto f = [&](double w) { return alpha * w * w + 2.0 * beta * w + gamma; };
+  double w = f(1.0) < f(0.0) ? 1.0 : 0.0;
+  if (alpha > 0.0) {
+    const double ws = std::min(1.0, std::max(0.0, -beta / alpha));
+    if (f(ws) < f(w)) w = ws;
+  }
+  k_blend<<<grid1d(P), 256, 0, s>>>(reinterpret_cast<float4*>(out), a->rad, b->rad, float(w), P);
+  ASUNA_CUDA_TRY(cudaGetLastError());
+  ASUNA_CUDA_TRY(cudaStreamSynchronize(s));
+  if (err_out) *err_out = std::sqrt(std::max(0.0, f(w)));
+  if (err_plain) *err_plain = std::sqrt(std::max(0.0, gamma));
+  if (weight) *weight = w;
   return ASUNA_OK;
 }
 

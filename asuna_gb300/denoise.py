@@ -162,6 +162,18 @@ class Denoiser:
                                            normal_image, _ptr(out), C.byref(ed), C.byref(ep)))
         return out, ed.value, ep.value
 
+    def blended(self, film_a, film_b, albedo_image=1, normal_image=2, out=None):
+        """The all-sample denoise blended with the plain average of two half
+        renders at the weight that minimises the estimated RMSE; returns
+        (image, estimated RMSE, plain-average estimate, weight)."""
+        torch = _torch()
+        if out is None:
+            out = torch.empty((film_a.height, film_a.width, 4), dtype=torch.float32, device="cuda")
+        eo, ep, w = C.c_double(), C.c_double(), C.c_double()
+        check(lib().asuna_denoise_blended(self.ctx.handle, self.handle, film_a.handle, film_b.handle, albedo_image,
+                                          normal_image, _ptr(out), C.byref(eo), C.byref(ep), C.byref(w)))
+        return out, eo.value, ep.value, w.value
+
     def close(self):
         if getattr(self, "handle", None):
             lib().asuna_denoiser_destroy(self.handle)

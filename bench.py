@@ -314,9 +314,9 @@ def run_denoise_rmse(args):
     the reference's own variance subtracted; the time at RMSE 0.01 is
     interpolated on the 1/sqrt(spp) law from the first count that reaches it.
     Denoised: two progressive films A and B on disjoint frames; the output
-    denoises all their samples, its error estimated from the two denoised
-    halves (asuna_denoise_combined): when the estimate exceeds the target or
-    the plain average's estimate, the plain average is the output instead.  Its time
+    blends the denoise of all their samples with their plain average at the
+    weight that minimises the error estimated from the two halves
+    (asuna_denoise_blended; weight 0 is the plain path).  Its time
     counts every render and every estimate.  The network is trained first,
     on the GPU, on pairs the renderer makes of other seeded scenes of the
     same recipe (inputs at several sample counts, a high-count target)."""
@@ -392,13 +392,16 @@ def run_denoise_rmse(args):
     t_plain = last["seconds"] / last["spp"] * spp_star
     out["plain"] = {"ladder": plain, "spp_at_target": spp_star, "seconds_at_target": t_plain,
                     "reached": last["rmse"] <= target}
-    # 2b. denoised path with the error-estimate fallback; the denoiser's
-    # first calls (workspace, weight staging) run before the clock starts
+    # 2b. denoised path: the all-sample denoise blended with the plain
+    # average at the weight that minimises the error estimate (weight 0 is the
+    # plain path); the denoiser's first calls (workspace, weight staging) run
+    # before the clock starts
     fa, fb = ctx.create_film(W, H), ctx.create_film(W, H)
     render_frames(fa, 0, 1, 11)
     render_frames(fb, 0, 1, 12)
     with torch.cuda.stream(stream):
         for _ in range(2):
+            inf.blended(fa, fb)
             inf.combined(fa, fb)
     torch.cuda.synchronize()
     fa.clear()
@@ -413,34 +416,30 @@ def run_denoise_rmse(args):
         half = nh
         with torch.cuda.stream(stream):
             ev0.record()
-            full, err_d, err_p = inf.combined(fa, fb)
+            blend, err_b, err_p, wgt = inf.blended(fa, fb)
             ev1.record()
         ev1.synchronize()
         est_ms = ev0.elapsed_time(ev1)
         ms += est_ms
-        used = "denoised" if err_d <= target and err_d <= err_p else "plain"
+        e = rmse(blend.cpu().numpy())
+        # untimed, for the table: the all-sample denoise alone and its estimate
+        with torch.cuda.stream(stream):
+            full, err_d, _ = inf.combined(fa, fb)
         e_full = rmse(full.cpu().numpy())
         e_avg = rmse(0.5 * (fa.read(0) + fb.read(0)))
-        e = e_full if used == "denoised" else e_avg
-        dres.append({"spp": 2 * half, "seconds": ms / 1e3, "estimate_ms": est_ms, "err_estimate": err_d,
-                     "err_plain_estimate": err_p, "output": used, "rmse": e, "rmse_denoised_all": e_full,
-                     "rmse_plain_average": e_avg})
+        dres.append({"spp": 2 * half, "seconds": ms / 1e3, "estimate_ms": est_ms, "weight": wgt,
+                     "err_estimate": err_b, "err_plain_estimate": err_p, "err_denoised_estimate": err_d,
+                     "rmse": e, "rmse_denoised_all": e_full, "rmse_plain_average": e_avg})
         if e <= target:
             t_den = ms / 1e3
             break
     out["denoised"] = {"ladder": dres, "seconds_at_target": t_den, "reached": t_den is not None}
     # the same ladders at other targets: plain by the 1/sqrt(spp) law from its
-    # last rung; denoised = the first rung whose output (chosen by the error
-    # estimate for that target) is below it
+    # last rung; denoised = the first rung whose blended output is below it
     rows = []
     for tgt in (0.05, 0.03, 0.02, target):
         tp = last["seconds"] / last["spp"] * last["spp"] * (last["rmse"] / tgt) ** 2
-        td = None
-        for r in dres:
-            den_ok = r["err_estimate"] <= tgt and r["err_estimate"] <= r["err_plain_estimate"]
-            if (r["rmse_denoised_all"] if den_ok else r["rmse_plain_average"]) <= tgt:
-                td = r["seconds"]
-                break
+        td = next((r["seconds"] for r in dres if r["rmse"] <= tgt), None)
         rows.append({"rmse": tgt, "plain_seconds": tp, "denoised_seconds": td,
                      "speedup": (tp / td) if td else None})
     out["targets"] = rows

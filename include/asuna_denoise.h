@@ -103,6 +103,16 @@ int asuna_denoise_estimate(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asu
  * asuna_denoise_estimate).  err_plain estimates the plain average of a, b. */
 int asuna_denoise_combined(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asuna_film* b, int albedo_image,
                            int normal_image, float* out, double* err_denoised, double* err_plain);
+/* Blends the all-sample denoise with the plain average of the two half
+ * renders: out = w D(a + b) + (1 - w) (a + b) / 2 (rgb), with w in [0, 1]
+ * chosen to minimise the estimated RMSE against the converged image.  The
+ * estimate judges the half blend w D_a + (1 - w) a by b (its error^2 is the
+ * mean square difference less the variance of b, mean((a - b)^2) / 2) and
+ * takes a quarter of the halves' blend difference, mean((X_a - X_b)^2) / 4,
+ * off for doubling the samples; both are quadratic in w.  w = 0 is the plain
+ * average (err_plain); *err_out is the estimate at the chosen *weight. */
+int asuna_denoise_blended(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asuna_film* b, int albedo_image,
+                          int normal_image, float* out, double* err_out, double* err_plain, double* weight);
 
 /* Device-side building blocks (raw device pointers, NHWC bf16, the context
  * stream as `stream`); exported for kernel-level tests.  cin % 16 == 0 and

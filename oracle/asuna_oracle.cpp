@@ -2410,8 +2410,12 @@ int oracle_tonemap(const float* rgba, uint32_t w, uint32_t h, const asuna_post_s
                               l0.z + (l1.z - l0.z) * noise[2]};
             col = {discr.x < lin.x ? c1.x : c0.x, discr.y < lin.y ? c1.y : c0.y, discr.z < lin.z ? c1.z : c0.z};
           }
-          col = {clamp01(0.5f + (col.x - 0.5f) * tm->contrast), clamp01(0.5f + (col.y - 0.5f) * tm->contrast),
-                 clamp01(0.5f + (col.z - 0.5f) * tm->contrast)};
+          // GLSL clamp as NVIDIA hardware evaluates it (and fminf / fmaxf):
+          // IEEE 754 minNum / maxNum, so a NaN (0/0 on a black pixel under
+          // auto exposure, post.idle.frag:45,68) clamps to 0
+          auto clampNum = [](float v) { return std::fmin(std::fmax(v, 0.0f), 1.0f); };
+          col = {clampNum(0.5f + (col.x - 0.5f) * tm->contrast), clampNum(0.5f + (col.y - 0.5f) * tm->contrast),
+                 clampNum(0.5f + (col.z - 0.5f) * tm->contrast)};
           col = pw(col, 1.0f / tm->brightness);
           const float g = col.x * 0.299f + col.y * 0.587f + col.z * 0.114f;
           col = {g + (col.x - g) * tm->saturation, g + (col.y - g) * tm->saturation, g + (col.z - g) * tm->saturation};

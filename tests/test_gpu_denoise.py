@@ -328,6 +328,24 @@ def test_film_denoise_and_error_estimate(dctx):
     var_half = 0.5 * np.mean((den.cpu().numpy()[..., :3].astype(np.float64) - db_[..., :3]) ** 2)
     assert np.isclose(ec, np.sqrt(max(0.0, ed * ed - 0.5 * var_half)), rtol=1e-3, atol=1e-6)
     assert ep2 == pytest.approx(ep)
+    # the blend of that output with the plain average, at the weight that
+    # minimises the estimate (a quadratic in w)
+    bl, eo, ep3, wgt = d.blended(fa, fb)
+    dctx.sync()
+    assert 0.0 <= wgt <= 1.0 and ep3 == pytest.approx(ep)
+    plain = 0.5 * (a + bb)
+    want = wgt * full.cpu().numpy()[..., :3] + (1.0 - wgt) * plain[..., :3]
+    assert np.allclose(bl.cpu().numpy()[..., :3], want, rtol=1e-5, atol=1e-5)
+    da_, db2 = den.cpu().numpy()[..., :3].astype(np.float64), db_[..., :3]
+    a3, b3 = a[..., :3].astype(np.float64), bb[..., :3].astype(np.float64)
+
+    def est(w):
+        xa, xb = w * da_ + (1 - w) * a3, w * db2 + (1 - w) * b3
+        return np.mean((xa - b3) ** 2) - np.mean((a3 - b3) ** 2) / 2 - np.mean((xa - xb) ** 2) / 4
+
+    assert np.isclose(eo, np.sqrt(max(0.0, est(wgt))), rtol=1e-3, atol=1e-6)
+    assert all(est(wgt) <= est(w) + 1e-3 * est(0.0) for w in np.linspace(0, 1, 21))
+    assert eo <= min(ec, ep) * (1 + 1e-6)
     with pytest.raises(A.AsunaError):
         d.denoise(fa, albedo_image=0)
     big = dctx.create_film(256, 256)
@@ -335,3 +353,5 @@ def test_film_denoise_and_error_estimate(dctx):
         d.denoise(big)  # larger than max_pixels: rejected, not overrun
     with pytest.raises(A.AsunaError):
         d.combined(fa, big)  # the halves must have one size
+    with pytest.raises(A.AsunaError):
+        d.blended(big, fb)
