@@ -12,8 +12,8 @@ import itertools
 BYTES_PER_PATH = 244  # wavefront state per path slot (asuna_gb300/csrc/engine.cu)
 
 
-def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64), trace_options=(0, 6),
-         shade_options=(0, 2), refill_options=(4, 8, 16, 24), occupancy_options=(8, 10, 12), memory_bytes=48 << 30,
+def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64, 128), trace_options=(0, 6),
+         shade_options=(0, 2), refill_options=(4, 8, 16, 24), occupancy_options=(8, 10, 12), memory_bytes=80 << 30,
          reps=2, frame_base=1 << 20):
     """Returns {"frames": f, "trace_blocks_per_sm": t, "shade_blocks_per_sm": s, "traversal": (refill
     extend, refill shadow, speculate extend, speculate shadow, traversal blocks per SM), "ray_sort": 0..3,
