@@ -13,7 +13,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libasuna_rt.so")
 
 # ---- status codes and enums (asuna_rt.h) -----------------------------------
-OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_IO, ERR_PARSE, ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_NO_DEVICE, ERR_BUSY = range(10)
+OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_IO, ERR_PARSE, ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_NO_DEVICE, ERR_BUSY, \
+    ERR_TRAVERSAL = range(11)
 CAMERA_PERSPECTIVE, CAMERA_OPENCV = 0, 1
 LIGHT_DIRECTIONAL, LIGHT_RECT, LIGHT_TRIANGLE, LIGHT_POINT = 0, 1, 2, 3
 MAT_LAMBERTIAN, MAT_EMISSIVE, MAT_PLASTIC, MAT_ROUGH_PLASTIC, MAT_MIRROR, MAT_DIELECTRIC = 0, 2, 4, 5, 8, 10
@@ -153,6 +154,7 @@ SIGNATURES = [
     ("asuna_ctx_set_graphs", C.c_int, [P, C.c_int]),
     ("asuna_ctx_set_traversal", C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     ("asuna_ctx_set_ray_sort", C.c_int, [P, C.c_int]),
+    ("asuna_ctx_set_traversal_stack", C.c_int, [P, C.c_int]),
     ("asuna_scene_create", C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(P)]),
     ("asuna_scene_validate", C.c_int, [C.POINTER(SceneDesc)]),
     ("asuna_scene_destroy", C.c_int, [P]),

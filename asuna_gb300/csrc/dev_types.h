@@ -200,9 +200,12 @@ struct DevCounters {
   unsigned long long nodes;   // closest-hit traversal
   unsigned long long tris;
   unsigned long long paths;
-  unsigned long long stackOverflow;  // traversals cut short by a full stack (must stay 0)
   unsigned long long shNodes;  // occlusion traversal
   unsigned long long shTris;
+  // traversals cut short by a full stack or a loop bound (must stay 0);
+  // last, so the render statistics can be cleared without it: the count
+  // only grows, and the host reports each increase as a render error
+  unsigned long long stackOverflow;
 };
 
 // Wavefront buffers (structure of arrays, indexed by queue slot or path).

@@ -15,6 +15,7 @@
 #include <memory>
 #include <chrono>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <new>
 #include <thread>
@@ -118,6 +119,23 @@ void dropGraphs(asuna_ctx* c) {
   c->gcache.clear();
 }
 
+// Reports the traversals cut short on the device since the last report, once
+// the copy of the count queued after the latest render has landed (waits for
+// it: call only where the stream is waited for anyway).
+int reportTraversal(asuna_ctx* c) {
+  if (!c->errPending) return ASUNA_OK;
+  ASUNA_CUDA_TRY(cudaEventSynchronize(c->errEvent));
+  c->errPending = false;
+  const unsigned long long now = *c->hostErr;
+  if (now <= c->errSeen) return ASUNA_OK;
+  const unsigned long long d = now - c->errSeen;
+  c->errSeen = now;
+  return fail(ASUNA_ERR_TRAVERSAL,
+              "traversal cut short (stack of %d entries full, or a loop bound reached) in %llu warps or rays: "
+              "the image is wrong",
+              c->stackLimit > 0 ? c->stackLimit : kStackDepth, d);
+}
+
 struct Batch {
   uint32_t rangeBegin, rangeEnd;
   uint32_t paths;
@@ -152,11 +170,18 @@ int asuna_ctx_create(int device_ordinal, asuna_ctx** out) {
     return fail(ASUNA_ERR_CUDA, "cudaStreamCreate failed");
   }
   if (cudaMalloc(&c->cnt, sizeof(DevCounters)) != cudaSuccess ||
-      cudaMallocHost(&c->hostCnt, sizeof(DevCounters)) != cudaSuccess) {
+      cudaMallocHost(&c->hostCnt, sizeof(DevCounters)) != cudaSuccess ||
+      cudaMallocHost(&c->hostErr, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->errEvent, cudaEventDisableTiming) != cudaSuccess) {
+    cudaFree(c->cnt);
+    cudaFreeHost(c->hostCnt);
+    cudaFreeHost(c->hostErr);
+    if (c->errEvent) cudaEventDestroy(c->errEvent);
     cudaStreamDestroy(c->stream);
     delete c;
     return fail(ASUNA_ERR_OOM, "counter allocation failed");
   }
+  *c->hostErr = 0;
   cudaMemset(c->cnt, 0, sizeof(DevCounters));
   c->traceGrid = c->numSMs * traceBlocksPerSm();
   c->shadeGrid = c->numSMs * shadeBlocksPerSm();
@@ -176,15 +201,18 @@ int asuna_ctx_destroy(asuna_ctx* c) {
   if (c->wave.base) cudaFree(c->wave.base);
   if (c->cnt) cudaFree(c->cnt);
   if (c->hostCnt) cudaFreeHost(c->hostCnt);
+  if (c->hostErr) cudaFreeHost(c->hostErr);
+  if (c->errEvent) cudaEventDestroy(c->errEvent);
   cudaStreamDestroy(c->stream);
   delete c;
   return ASUNA_OK;
 }
 
 int asuna_ctx_sync(asuna_ctx* c) {
+  clearError();
   if (!c) return fail(ASUNA_ERR_INVALID, "null context");
   ASUNA_CUDA_TRY(cudaStreamSynchronize(c->stream));
-  return ASUNA_OK;
+  return reportTraversal(c);
 }
 
 void* asuna_ctx_stream(asuna_ctx* c) { return c ? static_cast<void*>(c->stream) : nullptr; }
@@ -221,6 +249,15 @@ int asuna_ctx_set_traversal(asuna_ctx* c, int refillExtend, int refillShadow, in
     c->refill[k] = r[k] == 0 ? uint32_t(kRefillLanes) : uint32_t(r[k]);
     c->speculate[k] = sp[k] < 0 ? 1 : sp[k];
   }
+  return ASUNA_OK;
+}
+
+int asuna_ctx_set_traversal_stack(asuna_ctx* c, int entries) {
+  clearError();
+  if (!c) return fail(ASUNA_ERR_INVALID, "null context");
+  if (entries < 0 || entries > kStackDepth)
+    return fail(ASUNA_ERR_INVALID, "traversal stack of %d entries not in [0, %d]", entries, kStackDepth);
+  c->stackLimit = entries == kStackDepth ? 0 : entries;
   return ASUNA_OK;
 }
 
@@ -591,7 +628,7 @@ int asuna_film_read(asuna_ctx* c, asuna_film* f, int image, float* host) {
   const float4* src = image == 0 ? f->rad : (image == 8 ? f->w : f->ch + size_t(image - 1) * np);
   ASUNA_CUDA_TRY(cudaMemcpyAsync(host, src, np * 16, cudaMemcpyDeviceToHost, c->stream));
   ASUNA_CUDA_TRY(cudaStreamSynchronize(c->stream));
-  return ASUNA_OK;
+  return reportTraversal(c);
 }
 
 int asuna_film_image(asuna_film* f, int image, float** out) {
@@ -708,7 +745,8 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
   uint64_t totalPaths = 0;
   for (auto& b : batches) totalPaths += b.paths;
   if (hostRecords) ASUNA_CUDA_TRY(cudaMallocAsync(&dRec, totalPaths * sizeof(asuna_path_record), c->stream));
-  if (stats) ASUNA_CUDA_TRY(cudaMemsetAsync(c->cnt, 0, sizeof(DevCounters), c->stream));
+  // the statistics start at zero; the cut-short count (last) is cumulative
+  if (stats) ASUNA_CUDA_TRY(cudaMemsetAsync(c->cnt, 0, offsetof(DevCounters, stackOverflow), c->stream));
   // timing events: [begin, end] + one pair per extend / shade / connect launch
   size_t evNeed = 2;
   for (auto& b : batches) evNeed += size_t(wavefrontPasses(b.maxDepth, s->view)) * 8;
@@ -733,7 +771,7 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
            uint64_t(uintptr_t(dShots)), uint64_t(uintptr_t(dRanges)), uint64_t(c->traceGrid), uint64_t(c->shadeGrid),
            uint64_t(c->raygenGrid), uint64_t(c->counters), uint64_t(stats ? 1 : 0), uint64_t(c->refill[0]),
            uint64_t(c->refill[1]), uint64_t(c->speculate[0]), uint64_t(c->speculate[1]), uint64_t(c->occupancy),
-           uint64_t(c->raySort)});
+           uint64_t(c->raySort), uint64_t(c->stackLimit)});
     for (const Batch& b : batches)
       key.insert(key.end(), {b.rangeBegin, b.rangeEnd, b.paths, b.maxPix, uint64_t(b.maxDepth)});
     for (auto& g : c->gcache)
@@ -752,6 +790,7 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
   P.W.shots = dShots;
   P.records = hostRecords ? 1 : 0;
   P.counters = c->counters;
+  P.stackLimit = c->stackLimit;
   for (const Batch& b : batches) {
     P.W.ranges = dRanges + b.rangeBegin;
     P.W.numRanges = b.rangeEnd - b.rangeBegin;
@@ -824,11 +863,17 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
   }
   ASUNA_CUDA_TRY(cudaGetLastError());
   if (stats) ASUNA_CUDA_TRY(cudaEventRecord(c->events[1], c->stream));
+  // every render queues the copy of the cut-short count (8 bytes, pinned)
+  ASUNA_CUDA_TRY(cudaMemcpyAsync(c->hostErr, &c->cnt->stackOverflow, sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, c->stream));
+  ASUNA_CUDA_TRY(cudaEventRecord(c->errEvent, c->stream));
+  c->errPending = true;
   if (hostRecords) {
     ASUNA_CUDA_TRY(cudaMemcpyAsync(hostRecords, dRec, totalPaths * sizeof(asuna_path_record), cudaMemcpyDeviceToHost,
                                    c->stream));
     ASUNA_CUDA_TRY(cudaFreeAsync(dRec, c->stream));
     ASUNA_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if ((rc = reportTraversal(c))) return rc;
   }
   if (stats) {
     ASUNA_CUDA_TRY(cudaMemcpyAsync(c->hostCnt, c->cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, c->stream));
@@ -864,9 +909,7 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
         stats->connect_launches++;
       }
     }
-    if (c->hostCnt->stackOverflow)
-      return fail(ASUNA_ERR_INVALID, "traversal stack overflow or runaway traversal in %llu warps or rays",
-                  c->hostCnt->stackOverflow);
+    if ((rc = reportTraversal(c))) return rc;
   }
   return ASUNA_OK;
 }

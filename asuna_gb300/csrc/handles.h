@@ -44,6 +44,14 @@ struct asuna_ctx {
   int32_t speculate[2] = {1, 1};
   int32_t occupancy = 8;  // traversal kernel variant: resident blocks per SM
   int32_t raySort = 3;    // extend-queue sort mode before secondary passes (0 off)
+  int32_t stackLimit = 0; // traversal stack entries a ray may use (0 = the compiled capacity)
+  // traversals cut short on the device: the cumulative device count is
+  // copied to hostErr after every render (errEvent marks the copy); the
+  // host reports each increase over errSeen as ASUNA_ERR_TRAVERSAL
+  unsigned long long* hostErr = nullptr;
+  cudaEvent_t errEvent = nullptr;
+  bool errPending = false;
+  unsigned long long errSeen = 0;
   uint64_t useClock = 0;
   std::vector<GraphEntry> gcache;
 };

@@ -1418,7 +1418,12 @@ int asuna_camera_opencv(const float eye[3], const float lookat[3], const float u
   return ASUNA_OK;
 }
 
-// src/core/texture.cpp:144-226, with its double literals and float storage
+// Environment-map importance tables, following EnvMap::EnvMap
+// (src/core/texture.cpp:144-226) step for step: texel weights 0.3 r + 0.6 g
+// + 0.1 b, per-row conditional and marginal pdf/cdf with the 1e-7 guards,
+// and the inverse-CDF lookup by lower bound, with its double literals and
+// float storage.  The tables must equal the reference's
+// bit for bit, or the environment samples of the two diverge.
 int asuna_envmap_tables(uint32_t width, uint32_t height, const float* px, float* marg, float* cond) {
   if (!width || !height || !px || !marg || !cond) return fail(ASUNA_ERR_INVALID, "envmap tables: bad argument");
   const int W = int(width), H = int(height);

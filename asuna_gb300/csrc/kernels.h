@@ -16,6 +16,7 @@ struct KParams {
   uint32_t refillLanes;  // traversal: idle lanes of a warp that trigger a queue fetch
   int32_t speculate;     // traversal: postponed leaves walk on speculatively
   int32_t occupancy;     // traversal: resident blocks per SM of the kernel variant (8, 10 or 12)
+  int32_t stackLimit;    // traversal: stack entries a ray may use (<= kStackDepth)
 };
 
 constexpr int kTraceThreads = 128;

@@ -18,10 +18,18 @@
 // The device address of the array is looked up once per device, the first
 // time the entry point runs on it (cudaGetSymbolAddress with that device
 // current); make that first call before any stream capture.  Every call
-// shares the one array and it keeps the previous call's contents: the
-// kernels reset the counters they rely on at the start of each wavefront.
-// Calls whose work overlaps on the GPU (different streams, or different host
-// threads without ordering) race on the array.
+// shares the one array and it keeps the previous call's contents: the call
+// writes its shot and batch records and clears its error count in the array
+// with small kernels queued ahead of the render (their values travel as
+// kernel parameters), and the kernels reset the queue counters they rely on
+// at the start of each wavefront.  Calls whose work overlaps on the GPU
+// (different streams, or different host threads without ordering) race on
+// the array.
+//
+// The call waits for its work on the stream to finish, then reads the
+// array's count of traversals cut short: a nonzero count is returned as
+// ASUNA_ERR_TRAVERSAL.  Because it waits, it does not run on a stream that
+// is being captured (ASUNA_ERR_UNSUPPORTED, before any work is queued).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,19 +46,33 @@ using namespace asuna;
 namespace {
 
 constexpr uint64_t kNoAllocMaxPaths = ASUNA_NOALLOC_MAX_PATHS;
-constexpr uint64_t kNoAllocMaxRanges = 64;
 
 constexpr uint64_t pad256(uint64_t b) { return (b + 255) / 256 * 256; }
 // scratch layout: per-path arrays (12 x 16 B; 4 B each for the hit
-// instances and every shading-class list), counters, shot, ranges
+// instances and every shading-class list), counters, shot, the current
+// batch's range record
 constexpr uint64_t kPerPath16 = pad256(kNoAllocMaxPaths * 16);
 constexpr uint64_t kPerPath4 = pad256(kNoAllocMaxPaths * 4);
 constexpr uint64_t kOffCounters = 12 * kPerPath16 + (1 + kNumShadeClasses) * kPerPath4;
 constexpr uint64_t kOffShot = kOffCounters + pad256(sizeof(DevCounters));
 constexpr uint64_t kOffRanges = kOffShot + pad256(sizeof(ShotDev));
-constexpr uint64_t kScratchBytes = kOffRanges + pad256(kNoAllocMaxRanges * sizeof(RangeDev));
+constexpr uint64_t kScratchBytes = kOffRanges + pad256(sizeof(RangeDev));
 
 __device__ __align__(256) unsigned char g_noallocScratch[kScratchBytes];
+
+// Start of a call: the shot record, and a zero error count.
+__global__ void k_noallocBegin(ShotDev* dst, ShotDev shot, DevCounters* cnt) {
+  if (threadIdx.x == 0) {
+    *dst = shot;
+    cnt->stackOverflow = 0;
+  }
+}
+
+// Start of a batch: its range record (ordered after the previous batch's
+// kernels by the stream).
+__global__ void k_noallocRange(RangeDev* dst, RangeDev range) {
+  if (threadIdx.x == 0) *dst = range;
+}
 
 constexpr int kMaxDevices = 64;
 std::mutex gSetupMutex;
@@ -103,6 +125,12 @@ int renderNoAlloc(const asuna_scene* s, const asuna_shot* shot, asuna_film* film
       if (dev != prev) cudaSetDevice(prev);
     }
   } restore{s->device, prev};
+  cudaGetLastError();  // a non-sticky error left by the caller's own CUDA calls is not this call's failure
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  ASUNA_CUDA_TRY(cudaStreamIsCapturing(stream, &capture));
+  if (capture != cudaStreamCaptureStatusNone)
+    return fail(ASUNA_ERR_UNSUPPORTED,
+                "asuna_render_noalloc waits for its work to finish and cannot run on a stream being captured");
   unsigned char* base = nullptr;
   int rc = scratchAddress(s->device, &base);
   if (rc) return rc;
@@ -150,49 +178,47 @@ int renderNoAlloc(const asuna_scene* s, const asuna_shot* shot, asuna_film* film
   sd.filmRad = film->rad;
   sd.filmW = film->w;
   sd.filmCh = film->ch;
-  ASUNA_CUDA_TRY(cudaMemcpyAsync(dShot, &sd, sizeof(sd), cudaMemcpyHostToDevice, stream));
+  k_noallocBegin<<<1, 32, 0, stream>>>(dShot, sd, W.cnt);
 
-  // batches of whole frames, up to kNoAllocMaxRanges of them staged per upload
+  // batches of whole frames, each with its range record written in order
   const int traceGrid = numSMs * traceBlocksPerSm(), shadeGrid = numSMs * 8, raygenGrid = numSMs * 16;
   const int maxDepth = shot->state.max_path_depth;
-  uint32_t f = 0;
-  while (f < shot->frames) {
-    RangeDev staged[kNoAllocMaxRanges];
-    uint32_t nr = 0;
-    for (uint32_t g = f; g < shot->frames && nr < kNoAllocMaxRanges; ++nr) {
-      uint32_t k = uint32_t(std::min<uint64_t>(framesPerBatch, shot->frames - g));
-      RangeDev& r = staged[nr];
-      std::memset(&r, 0, sizeof(r));
-      r.pathBegin = 0;
-      r.shot = 0;
-      r.frameBegin = shot->frame0 + g;
-      r.nframes = k;
-      r.npix = uint32_t(npix);
-      g += k;
+  W.ranges = dRanges;
+  W.numRanges = 1;
+  for (uint32_t f = 0; f < shot->frames;) {
+    RangeDev r;
+    std::memset(&r, 0, sizeof(r));
+    r.pathBegin = 0;
+    r.shot = 0;
+    r.frameBegin = shot->frame0 + f;
+    r.nframes = uint32_t(std::min<uint64_t>(framesPerBatch, shot->frames - f));
+    r.npix = uint32_t(npix);
+    k_noallocRange<<<1, 32, 0, stream>>>(dRanges, r);
+    W.numPaths = r.nframes * uint32_t(npix);
+    P.cur = 0;
+    P.depth = 0;
+    const int rg = int(std::min<uint64_t>((W.numPaths + 255) / 256, uint64_t(raygenGrid)));
+    launchRaygen(P, std::max(rg, 1), stream);
+    for (int depth = 1; depth <= wavefrontPasses(maxDepth, s->view); ++depth) {
+      P.depth = uint32_t(depth);
+      launchExtend(P, traceGrid, stream);
+      launchShade(P, shadeGrid, stream);
+      launchConnect(P, traceGrid, stream);
+      P.cur ^= 1;
     }
-    ASUNA_CUDA_TRY(cudaMemcpyAsync(dRanges, staged, nr * sizeof(RangeDev), cudaMemcpyHostToDevice, stream));
-    for (uint32_t b = 0; b < nr; ++b) {
-      W.ranges = dRanges + b;
-      W.numRanges = 1;
-      W.numPaths = staged[b].nframes * uint32_t(npix);
-      P.cur = 0;
-      P.depth = 0;
-      const int rg = int(std::min<uint64_t>((W.numPaths + 255) / 256, uint64_t(raygenGrid)));
-      launchRaygen(P, std::max(rg, 1), stream);
-      for (int depth = 1; depth <= wavefrontPasses(maxDepth, s->view); ++depth) {
-        P.depth = uint32_t(depth);
-        launchExtend(P, traceGrid, stream);
-        launchShade(P, shadeGrid, stream);
-        launchConnect(P, traceGrid, stream);
-        P.cur ^= 1;
-      }
-      launchAccumulate(P, uint32_t(npix), 1, stream);
-      f += staged[b].nframes;
-    }
-    // the next group's range records overwrite dRanges: order after this group
-    if (f < shot->frames) ASUNA_CUDA_TRY(cudaStreamSynchronize(stream));
+    launchAccumulate(P, uint32_t(npix), 1, stream);
+    f += r.nframes;
   }
   ASUNA_CUDA_TRY(cudaGetLastError());
+  // wait for the work, then read the count of traversals cut short
+  unsigned long long cut = 0;
+  ASUNA_CUDA_TRY(cudaMemcpyAsync(&cut, &W.cnt->stackOverflow, sizeof(cut), cudaMemcpyDeviceToHost, stream));
+  ASUNA_CUDA_TRY(cudaStreamSynchronize(stream));
+  if (cut)
+    return fail(ASUNA_ERR_TRAVERSAL,
+                "asuna_render_noalloc: traversal cut short (stack full or a loop bound reached) in %llu warps or "
+                "rays: the image is wrong",
+                cut);
   return ASUNA_OK;
 }
 

@@ -136,7 +136,7 @@ struct Trav {
   WT wt;
   float tmin, best;
   uint32_t curInst;
-  int sp;
+  int sp, lim;  // stack entries in use / allowed
   int32_t ref, leaf;
   bool found, inBlas;
   HitOut h;
@@ -160,14 +160,14 @@ struct Trav {
   // Stack: the first kSharedStack entries in shared memory (stride
   // kTraceThreads: bank-conflict free), deeper ones in thread-local memory.
   __device__ __forceinline__ void push(int32_t* sh, int32_t* loc, int32_t v, bool& ovf) {
-    if (sp < kSharedStack)
-      sh[sp * kTraceThreads] = v;
-    else if (sp < kStackDepth)
-      loc[sp - kSharedStack] = v;
-    else {
+    if (sp >= lim) {
       ovf = true;
       return;
     }
+    if (sp < kSharedStack)
+      sh[sp * kTraceThreads] = v;
+    else
+      loc[sp - kSharedStack] = v;
     ++sp;
   }
   __device__ __forceinline__ int32_t popOrDone(const int32_t* sh, const int32_t* loc) {
@@ -262,7 +262,7 @@ struct Trav {
     curInst = leafFirst(ref);
     const InstDev* in = S.inst + curInst;
     const int32_t root = __ldg(&in->blasRoot);
-    if (root >= 0 && sp < kStackDepth) {
+    if (root >= 0 && sp < lim) {
       float3 d;
       xformRay(in->w2o, wo, wd, o, d);
       id = safeInv(d);
@@ -285,12 +285,13 @@ struct Trav {
 // finish(i, tr).
 template <bool ANY, bool COUNT, bool SPEC, class Src>
 __device__ __forceinline__ void traceWarp(const SceneDev& S, Src& src, int32_t* sh, int32_t* loc, uint32_t refill,
-                                          uint32_t& nNodes, uint32_t& nTris, bool& ovf) {
+                                          int stackLimit, uint32_t& nNodes, uint32_t& nTris, bool& ovf) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lanesBelow = (1u << lane) - 1u;
   bool active = false, drained = false;
   uint32_t idx = 0, events = 0;
   Trav tr;
+  tr.lim = stackLimit > 0 && stackLimit < kStackDepth ? stackLimit : kStackDepth;
   for (;;) {
     const unsigned idle = __ballot_sync(0xffffffffu, !active);
     if (idle && !drained && (uint32_t(__popc(idle)) >= refill || idle == 0xffffffffu)) {
@@ -410,7 +411,7 @@ __global__ void __launch_bounds__(kTraceThreads, OCC) k_trace(KParams P) {
   bool ovf = false;
   // (the instrumented variant walks without speculation, so its node counts
   // are those of the ordered traversal)
-  traceWarp<ANY, COUNT, SPEC>(P.S, src, sh, lstack, P.refillLanes, nNodes, nTris, ovf);
+  traceWarp<ANY, COUNT, SPEC>(P.S, src, sh, lstack, P.refillLanes, P.stackLimit, nNodes, nTris, ovf);
   if (ovf) atomicAdd(&W.cnt->stackOverflow, 1ull);
   if (COUNT) {
     const unsigned lane = threadIdx.x & 31u;
@@ -467,9 +468,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_query(SceneDev S, const float
   uint32_t a = 0, b = 0;
   bool ovf = false;
   if (anyHit)
-    traceWarp<true, false, true>(S, src, sh, lstack, kRefillLanes, a, b, ovf);
+    traceWarp<true, false, true>(S, src, sh, lstack, kRefillLanes, kStackDepth, a, b, ovf);
   else
-    traceWarp<false, false, true>(S, src, sh, lstack, kRefillLanes, a, b, ovf);
+    traceWarp<false, false, true>(S, src, sh, lstack, kRefillLanes, kStackDepth, a, b, ovf);
 }
 
 }  // namespace

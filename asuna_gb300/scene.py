@@ -7,6 +7,7 @@ triangle (mesh-facet) lights one-triangle emitter instances.  ``Context`` owns
 one CUDA device + stream of the native library; scenes, films and renders go
 through the C ABI in include/asuna_rt.h.
 """
+import contextlib
 import ctypes as C
 
 import numpy as np
@@ -71,6 +72,37 @@ def set_channels(state, names):
     return depth
 
 
+class _LibraryHelpers:
+    """Host preprocessing of a scene description through the library: the
+    diffuse-Fresnel integral of the plastics' substrate and the perspective
+    camera's matrices."""
+
+    @staticmethod
+    def diffuse_fresnel(ior):
+        return lib().asuna_diffuse_fresnel(C.c_float(ior), 1000)
+
+    @staticmethod
+    def camera_perspective(e, l, u, fov, aperture, focal_distance, width, height, cam):
+        check(lib().asuna_camera_perspective(A.fptr(e), A.fptr(l), A.fptr(u), fov, aperture, focal_distance, width,
+                                             height, C.byref(cam)))
+
+
+_helpers = _LibraryHelpers()
+
+
+@contextlib.contextmanager
+def host_helpers(provider):
+    """Builds scene descriptions with another provider of the host
+    preprocessing (an object with diffuse_fresnel and camera_perspective like
+    _LibraryHelpers), e.g. for a process that must not load the library."""
+    global _helpers
+    old, _helpers = _helpers, provider
+    try:
+        yield
+    finally:
+        _helpers = old
+
+
 def _length(v):
     # float32 length as the reference's host code computes it (no BLAS reduction)
     v = np.asarray(v, np.float32)
@@ -128,7 +160,7 @@ class SceneBuilder:
         m.diffuse = A.f3(*diffuse)
         m.aniso_alpha = (C.c_float * 2)(*alpha)
         m.ior = ior
-        m.radiance[0] = lib().asuna_diffuse_fresnel(C.c_float(ior), 1000)
+        m.radiance[0] = _helpers.diffuse_fresnel(ior)
         return self._add_material(name, m)
 
     def add_plastic(self, name, diffuse, ior=1.5):
@@ -137,7 +169,7 @@ class SceneBuilder:
         m.type = A.MAT_PLASTIC
         m.diffuse = A.f3(*diffuse)
         m.ior = ior
-        m.radiance[0] = lib().asuna_diffuse_fresnel(C.c_float(ior), 1000)
+        m.radiance[0] = _helpers.diffuse_fresnel(ior)
         return self._add_material(name, m)
 
     def add_mirror(self, name, reflectance=(1.0, 1.0, 1.0)):
@@ -395,8 +427,7 @@ def perspective_camera(eye, lookat, up, fov, width, height, aperture=0.0, focal_
     fov in degrees is horizontal."""
     cam = A.Camera()
     e, l, u = (np.asarray(x, np.float32) for x in (eye, lookat, up))
-    check(lib().asuna_camera_perspective(A.fptr(e), A.fptr(l), A.fptr(u), fov, aperture, focal_distance, width,
-                                         height, C.byref(cam)))
+    _helpers.camera_perspective(e, l, u, fov, aperture, focal_distance, width, height, cam)
     return cam
 
 
@@ -530,6 +561,11 @@ class Context:
         in Morton order, 3 the same with the origin cell major (True = 1).  Results
         do not depend on it."""
         check(lib().asuna_ctx_set_ray_sort(self.handle, int(mode)))
+
+    def set_traversal_stack(self, entries=0):
+        """Caps the traversal stack per ray (0 = the full 64 entries); a
+        traversal needing more is cut short and reported as ERR_TRAVERSAL."""
+        check(lib().asuna_ctx_set_traversal_stack(self.handle, int(entries)))
 
     def set_launch(self, trace_blocks_per_sm=0, shade_blocks_per_sm=0):
         check(lib().asuna_ctx_set_launch(self.handle, int(trace_blocks_per_sm), int(shade_blocks_per_sm)))

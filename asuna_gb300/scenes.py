@@ -397,3 +397,23 @@ def training_scene(seed, width=128, height=128, frames=4, max_depth=8, level=4):
     at = tuple(float(v) for v in rng.uniform(-4.0, 4.0, 3))
     return mixed_scene(width, height, frames=frames, max_depth=max_depth, n_spheres=n, level=level, seed=seed,
                        rr_depth=3, env_size=(128, 64), eye=eye, at=at)
+
+
+def stacked_instances_scene(n_instances, width=8, height=8):
+    """n copies of one triangle at the same place, facing the camera, lit by
+    a point light: every camera ray meets every copy at the same distance, so
+    its traversal enters and leaves all n instances.  For n in the tens of
+    thousands that passes the traversal's loop bound (65,536 leaves and
+    transitions per ray): a scene for the error path of a runaway traversal."""
+    b = SceneBuilder()
+    white = b.add_lambertian("white", (0.73, 0.73, 0.73))
+    b.add_point_light((0.0, 0.0, 2.0), (1.0, 1.0, 1.0))
+    v = np.zeros(3, A.VERTEX_DTYPE)
+    v["pos"] = [(-1, -1, 0), (1, -1, 0), (0, 1, 0)]
+    v["normal"] = (0, 0, 1)
+    b.add_mesh("tri", v, np.array([0, 1, 2], np.uint32))
+    for _ in range(n_instances):
+        b.add_instance("tri", white)
+    state, depth = b.state(spp=1, max_path_depth=1, channels=())
+    cam = perspective_camera((0, 0, 3.0), (0, 0, 0), (0, 1, 0), 10.0, width, height)
+    return b, make_shot(cam, state, width, height, 1, depth_channel=depth)

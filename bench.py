@@ -16,9 +16,17 @@ traversal kernel: algorithmic bytes = BVH nodes x 64 B + triangles x 48 B per
 ray (counted by a separate instrumented frame), over its event-timed
 duration, against the measured HBM copy bandwidth.
 
---impl reference: the CPU oracle (the reference's hot path restated in C++,
-pinned bit-exactly to the reference's own shader source) on all host cores
-over a bounded seeded pixel sample of the same workload.
+--impl reference: the reference's own implementation of the path — its GLSL
+shaders compiled as host C++ (oracle/_ref) — on all host cores over a
+bounded seeded pixel sample of the same workload, without Russian roulette
+(the reference has none); the process builds the workload with the oracle's
+host helpers and never loads the library.  Where the reference's shaders are
+not built, the oracle's restatement (bit-identical to them) stands in.
+
+Parity: the N=1 line also carries `parity`, the per-path comparison of the
+GPU against the oracle on a seeded 16,384-pixel subset of the workload over 4
+frames (outside the timed region), with Russian roulette as benchmarked and
+without it.
 Under torchrun (N > 1) every rank renders its own frames of the shot
 (replicas, weak scaling); rank 0 reports the max-over-ranks time.
 """
@@ -115,50 +123,167 @@ def build_workload(args, verbose):
     return b, shot
 
 
-def cpu_leg(b, shot, seconds, threads):
-    """Oracle throughput on a bounded seeded pixel sample of the same workload."""
+def _one_frame(shot, frame0=0, rr=True):
+    import copy
+
+    from asuna_gb300 import _abi as A
+
+    s = copy.copy(shot)
+    s.frames, s.frame0 = 1, frame0
+    if not rr:
+        s.flags &= ~A.SHOT_RR
+    return s
+
+
+class CpuSampler:
+    """Throughput of a CPU implementation of the path over seeded pixel
+    samples of the workload: the reference's own shaders compiled as host C++
+    (kind "reference"; without Russian roulette, which the reference does not
+    have) or the oracle's restatement (kind "port", as benchmarked).  The
+    scene set-up (the oracle's BVH build) is excluded from the timings."""
+
+    def __init__(self, b, shot, kind, threads):
+        from oracle import oracle_py
+
+        self.kind, self.threads = kind, threads
+        self.shot = _one_frame(shot, rr=(kind == "port"))
+        self.desc = b.desc()
+        t0 = time.time()
+        if kind == "reference":
+            self.impl = oracle_py.RefSampler(self.desc, self.shot)
+        else:
+            self.impl = oracle_py.OracleScene(self.desc)
+        self.setup_s = time.time() - t0
+        self.npix = shot.width * shot.height
+
+    def run(self, px, frame0=0):
+        s = _one_frame(self.shot, frame0, rr=(self.kind == "port"))
+        if self.kind == "reference":
+            return self.impl.run(s, px, self.threads)
+        _, _, st = self.impl.render(s, records=False, film=None, pixels=px, threads=self.threads)
+        return st
+
+    def calibrate(self, seconds):
+        """A seeded pixel sample that takes about `seconds` of CPU time."""
+        rng = np.random.default_rng(0)
+        n = 2048
+        while True:
+            px = np.sort(rng.choice(self.npix, size=min(n, self.npix), replace=False)).astype(np.uint32)
+            st = self.run(px)
+            if st["seconds"] >= seconds * 0.5 or n >= self.npix:
+                return px, st
+            n = int(min(self.npix, n * max(2.0, seconds / max(st["seconds"], 1e-3))))
+
+    def describe(self, px, st):
+        rays = st["extend_rays"] + st["shadow_rays"]
+        what = ("the reference's shaders compiled as host C++, no Russian roulette (the reference has none)"
+                if self.kind == "reference" else "the oracle's restatement, Russian roulette after depth 3")
+        return {"value": rays / st["seconds"] / 1e6, "unit": METRIC, "cores": st["threads"], "kind": self.kind,
+                "sample": f"{len(px)} seeded pixels x 1 frame (1 spp) of the benchmark workload, {what} "
+                          f"({st['paths']} paths, {rays} rays, {st['seconds']:.1f} s; scene set-up and the "
+                          f"oracle's BVH build, {self.setup_s:.1f} s, excluded)",
+                "msamples_per_s": st["paths"] / st["seconds"] / 1e6}
+
+    def close(self):
+        self.impl.close()
+
+
+def cpu_kind():
     from oracle import oracle_py
 
-    t0 = time.time()
-    osc = oracle_py.OracleScene(b.desc())
-    build_s = time.time() - t0
-    rng = np.random.default_rng(0)
-    npix = shot.width * shot.height
-    n = 2048
-    while True:
-        px = np.sort(rng.choice(npix, size=min(n, npix), replace=False)).astype(np.uint32)
-        _, _, st = osc.render(shot, records=False, film=None, pixels=px, threads=threads)
-        if st["seconds"] >= seconds * 0.5 or n >= npix:
-            break
-        n = int(min(npix, n * max(2.0, seconds / max(st["seconds"], 1e-3))))
-    rays = st["extend_rays"] + st["shadow_rays"]
-    return {"value": rays / st["seconds"] / 1e6, "unit": METRIC, "cores": st["threads"], "kind": "port",
-            "sample": f"{len(px)} seeded pixels x 1 frame of the benchmark workload ({st['paths']} paths, "
-                      f"{rays} rays, {st['seconds']:.1f} s; oracle BVH build {build_s:.1f} s excluded)",
-            "msamples_per_s": st["paths"] / st["seconds"] / 1e6}
+    return "reference" if oracle_py.ref() is not None else "port"
+
+
+def cpu_leg(b, shot, seconds, threads, kind=None):
+    """CPU throughput on a bounded seeded pixel sample of the same workload."""
+    cs = CpuSampler(b, shot, kind or cpu_kind(), threads)
+    try:
+        px, st = cs.calibrate(seconds)
+        return cs.describe(px, st)
+    finally:
+        cs.close()
+
+
+def mapped_libraries():
+    """The repository's shared libraries mapped into this process."""
+    try:
+        with open("/proc/self/maps") as f:
+            paths = {ln.split()[-1] for ln in f if ln.rstrip().endswith(".so")}
+    except OSError:
+        return []
+    return sorted(os.path.relpath(p, ROOT) for p in paths if p.startswith(ROOT))
+
+
+def parity_check(ctx, scene, b, shot, npixels=16384, frames=4, seed=0):
+    """Per-path GPU vs oracle agreement on a seeded pixel subset of the
+    workload (oracle/parity.py's bar), with Russian roulette as benchmarked
+    and without it (the reference's own estimator)."""
+    import copy
+
+    from asuna_gb300 import _abi as A
+    from oracle import oracle_py, parity
+
+    desc = b.desc()
+    osc = oracle_py.OracleScene(desc)
+    res = parity.sample_parity(ctx, scene, desc, shot, npixels, frames, seed, oracle_scene=osc)
+    off = copy.copy(shot)
+    off.flags &= ~A.SHOT_RR
+    res["rr_off"] = parity.sample_parity(ctx, scene, desc, off, npixels, frames, seed, oracle_scene=osc)
+    osc.close()
+    res.update({"rr_depth": int(shot.rr_depth),
+                "bar": f"per path every radiance channel within {parity.REL:g} relative + {parity.ABS:g}"})
+    return res
 
 
 def run_reference(args):
+    """The reference's own CPU implementation of the path, timed step by
+    step on a bounded pixel sample (rank 0 only; other ranks exit)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    b, shot = build_workload(args, verbose=False)
+    from asuna_gb300 import scene as sc
+    from oracle import oracle_py
+
+    with sc.host_helpers(oracle_py.OracleHelpers()):
+        b, shot = build_workload(args, verbose=False)
     threads = os.cpu_count() or 1
-    vals = []
-    cb = None
-    for _ in range(args.warmup):
-        cpu_leg(b, shot, 2.0, threads)
-    for _ in range(args.steps):
-        cb = cpu_leg(b, shot, args.ref_seconds, threads)
-        vals.append(cb["value"])
-    v = float(np.mean(vals))
+    kind = cpu_kind()
+    cs = CpuSampler(b, shot, kind, threads)
+    per_step = max(1.0, min(args.ref_seconds, args.ref_budget / max(1, args.steps + args.warmup)))
+    px, _ = cs.calibrate(per_step)
+    for i in range(args.warmup):
+        cs.run(px, frame0=1 + i)
+    vals, secs, rays = [], 0.0, 0
+    st = None
+    for i in range(args.steps):
+        st = cs.run(px, frame0=1 + args.warmup + i)
+        vals.append((st["extend_rays"] + st["shadow_rays"]) / st["seconds"] / 1e6)
+        secs += st["seconds"]
+        rays += st["extend_rays"] + st["shadow_rays"]
+    cs.close()
+    v = rays / secs / 1e6
+    cb = cs.describe(px, st)
+    cb.update({"value": v, "steps_mrays": [round(x, 3) for x in vals]})
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)", "config": CONFIG,
-            "cpu_baseline": {**cb, "value": v},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded procedural scene)", "config": workload_config(shot),
+            "cpu_baseline": cb,
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if kind == "reference":
+        # the oracle's restatement on the same sample, as a second figure
+        line["cpu_port"] = cpu_leg(b, shot, per_step, threads, kind="port")
+    libs = mapped_libraries()
+    line["libraries"] = libs
+    if any("libasuna_rt" in p for p in libs):
+        raise RuntimeError(f"the reference arm loaded the library: {libs}")
     print(json.dumps(line), flush=True)
     return 0
+
+
+def workload_config(shot):
+    """The `config` both arms print (identical by construction)."""
+    return {**CONFIG, "width": shot.width, "height": shot.height}
 
 
 def run(args):
@@ -275,11 +400,9 @@ def run(args):
         "metric": METRIC, "value": rays / (ms * 1e-3) / 1e6, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-        "config": {**CONFIG, "width": shot.width, "height": shot.height, "parallelism": f"replicas{world}",
-                   "frames_per_step": args.frames_per_step,
-                   "autotune": None if tuned is None else {k: tuned[k] for k in
-                                                           ("frames", "trace_blocks_per_sm", "shade_blocks_per_sm",
-                                                            "traversal", "ray_sort")}},
+        "config": workload_config(shot),
+        "run": {"parallelism": f"replicas{world}", "frames_per_step": args.frames_per_step,
+                "autotune": None if tuned is None else {k: tuned[k] for k in tuned if k != "trials"}},
         "msamples_per_s": tot["paths"] * world / (ms * 1e-3) / 1e6 if world == 1 else None,
         "rays_per_step": rays / args.steps,
         "instrumented_step": {"extend_rays": cst["extend_rays"], "shadow_rays": cst["shadow_rays"],
@@ -297,6 +420,8 @@ def run(args):
         "scene": {"triangles": sstats["triangles"], "device_bytes": sstats["device_bytes"],
                   "build_ms": sstats["build_ms"]},
     }
+    if world == 1 and not args.no_parity:
+        line["parity"] = parity_check(ctx, scene, b, shot)
     if not args.no_cpu and world == 1:
         line["cpu_baseline"] = cpu_leg(b, shot, args.cpu_seconds, os.cpu_count() or 1)
     print(json.dumps(line), flush=True)
@@ -640,8 +765,11 @@ def main():
                     help="with --frames-per-step: refill extend,refill shadow,speculate extend,speculate shadow,"
                          "blocks per SM (the autotuner's traversal tuple)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--ref-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-seconds", type=float, default=10.0, help="--impl reference: CPU seconds per step at most")
+    ap.add_argument("--ref-budget", type=float, default=100.0,
+                    help="--impl reference: CPU seconds of the warm-up and timed steps together")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--verbose", action="store_true")
     ap.add_argument("--denoise-rmse", action="store_true",
                     help="time to RMSE 0.01 vs the FP64 reference, plain vs denoised path")

@@ -52,7 +52,9 @@ enum {
   ASUNA_ERR_TIMEOUT = 6,     /* a bounded device wait gave up              */
   ASUNA_ERR_UNSUPPORTED = 7, /* feature outside the implemented plugin set */
   ASUNA_ERR_NO_DEVICE = 8,   /* no CUDA device / library built without it  */
-  ASUNA_ERR_BUSY = 9         /* server queue full: request rejected        */
+  ASUNA_ERR_BUSY = 9,        /* server queue full: request rejected        */
+  ASUNA_ERR_TRAVERSAL = 10   /* a BVH traversal was cut short (stack or
+                                loop bound): the rendered image is wrong  */
 };
 
 /* ---- enums of the reference's plugin dispatch --------------------------- */
@@ -351,6 +353,11 @@ int asuna_ctx_set_traversal(asuna_ctx* ctx, int refill_extend, int refill_shadow
  * origin cells, 2 octant x 8 x 8 x 8 cells in Morton order, 3 the same with
  * the origin cell major (the default).  Results do not depend on it. */
 int asuna_ctx_set_ray_sort(asuna_ctx* ctx, int mode);
+/* Caps the traversal stack at `entries` per ray (1..64; 0 = 64, the
+ * compiled capacity, which every scene asuna_scene_create accepts fits).
+ * A traversal that needs more entries is cut short and the render reports
+ * ASUNA_ERR_TRAVERSAL; a lower cap serves to test that error path. */
+int asuna_ctx_set_traversal_stack(asuna_ctx* ctx, int entries);
 
 /* ---- scene: upload + acceleration-structure build ------------------------ */
 /* Replaces Scene::submit + BLAS/TLAS build.  Host arrays are deep-copied; the
@@ -376,7 +383,11 @@ int asuna_film_clear(asuna_ctx* ctx, asuna_film* film);
 
 /* ---- render --------------------------------------------------------------- */
 /* Renders shot->frames frames into film (asynchronous on the context's
- * stream; stats, if non-NULL, forces a synchronisation and is filled). */
+ * stream; stats, if non-NULL, forces a synchronisation and is filled).
+ * A traversal cut short on the device (ASUNA_ERR_TRAVERSAL) is reported by
+ * the call itself when it synchronises (stats or records requested), else
+ * by the next call on the context that waits for the stream:
+ * asuna_ctx_sync, asuna_film_read, or a render with stats. */
 int asuna_render(asuna_ctx* ctx, const asuna_scene* scene, const asuna_shot* shot,
                  asuna_film* film, asuna_render_stats* stats);
 /* Renders n shots (any resolutions / frame counts) in one wavefront. */
@@ -404,7 +415,10 @@ int asuna_scene_trace(asuna_ctx* ctx, const asuna_scene* scene, const float* ray
  * every GPU that loads the library until exit); a frame with more pixels is
  * rejected with ASUNA_ERR_INVALID.  The array's address is set up on a
  * device by the first call there: make that call before any stream capture.
- * Calls share the array; calls that overlap on the GPU race. */
+ * Calls share the array; calls that overlap on the GPU race.  The call
+ * waits for its work on `stream` to finish and returns ASUNA_ERR_TRAVERSAL
+ * if a traversal was cut short; on a stream that is being captured it
+ * queues nothing and returns ASUNA_ERR_UNSUPPORTED. */
 #define ASUNA_NOALLOC_MAX_PATHS 262144
 int asuna_render_noalloc(const asuna_scene* scene, const asuna_shot* shot, asuna_film* film, void* stream);
 

@@ -2293,6 +2293,94 @@ float oracle_math(int which, float x, float y) {
   }
 }
 uint32_t oracle_pcg(uint32_t* state) { return pcg(*state); }
+
+// src/loader/material.cpp:6-22 (dielectricReflectance) and :24-37: the
+// trapezoid rule over cos^2 theta in [0, 1], float terms summed in double.
+static float oraDielectricReflectance(float eta, float cosI, float& cosT) {
+  if (cosI < 0.0f) {
+    eta = 1.0f / eta;
+    cosI = -cosI;
+  }
+  const float sin2T = eta * eta * (1.0f - cosI * cosI);
+  if (sin2T > 1.0f) {
+    cosT = 0.0f;
+    return 1.0f;
+  }
+  cosT = std::sqrt(std::max(1.0f - sin2T, 0.0f));
+  const float rs = (eta * cosI - cosT) / (eta * cosI + cosT);
+  const float rp = (eta * cosT - cosI) / (eta * cosT + cosI);
+  return (rs * rs + rp * rp) * 0.5f;
+}
+float oracle_diffuse_fresnel(float ior, int samples) {
+  float unused;
+  double acc = 0.0;
+  float prev = oraDielectricReflectance(ior, 0.0f, unused);
+  for (int i = 1; i <= samples; ++i) {
+    const float c2 = float(i) / samples;
+    const float cur = oraDielectricReflectance(ior, std::min(std::sqrt(c2), 1.0f), unused);
+    acc += double(cur + prev) * (0.5 / samples);
+    prev = cur;
+  }
+  return float(acc);
+}
+
+// The camera's two matrices, column-major as GpuCamera stores them
+// (src/shared/camera.h).  camera -> world: the look-at frame (x right,
+// y up, z back from the target) with y and z negated, translated to the eye
+// (view = scale(1,-1,-1) * lookAt).  raster -> camera: the inverse of
+// raster <- NDC <- screen <- camera (camera.cpp:28-62) in closed form: with
+// c = 1/tan(fov/2), aspect = w/h, a = f/(f-n), b = -n f/(f-n), raster =
+// (w c/2 x + w/2 z, h aspect c/2 y + h/2 z, a z + b, z), so x = 2/(w c) X -
+// W/c, y = 2/(h aspect c) Y - W/(aspect c), z = W, 1 = (Z - a W)/b.
+int oracle_camera_perspective(const float eye[3], const float at[3], const float up[3], float fov_deg,
+                              float aperture, float focal_distance, uint32_t width, uint32_t height,
+                              asuna_camera* out) {
+  if (!eye || !at || !up || !out || !width || !height || !(fov_deg > 0.0f && fov_deg < 180.0f))
+    return ASUNA_ERR_INVALID;
+  std::memset(out, 0, sizeof(*out));
+  out->type = ASUNA_CAMERA_PERSPECTIVE;
+  auto unit = [](double v[3]) {
+    const double l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (l > 0)
+      for (int k = 0; k < 3; ++k) v[k] /= l;
+  };
+  double z[3] = {double(eye[0]) - at[0], double(eye[1]) - at[1], double(eye[2]) - at[2]};
+  unit(z);
+  double x[3] = {up[1] * z[2] - up[2] * z[1], up[2] * z[0] - up[0] * z[2], up[0] * z[1] - up[1] * z[0]};
+  unit(x);
+  double y[3] = {z[1] * x[2] - z[2] * x[1], z[2] * x[0] - z[0] * x[2], z[0] * x[1] - z[1] * x[0]};
+  unit(y);
+  double c2w[4][4] = {};  // [row][col]
+  for (int k = 0; k < 3; ++k) {
+    c2w[k][0] = x[k];
+    c2w[k][1] = -y[k];
+    c2w[k][2] = -z[k];
+    c2w[k][3] = eye[k];
+  }
+  c2w[3][3] = 1.0;
+  const float nearz = 0.1f, farz = 100.0f;
+  const float aspect = float(width) / float(height);
+  const double c = double(float(1.0 / double(tanf(fov_deg * 0.017453292519943295f * 0.5f))));
+  const float recip = 1.0f / (farz - nearz);
+  const double a = double(farz * recip), b = double(-nearz * farz * recip);
+  double r2c[4][4] = {};
+  r2c[0][0] = 2.0 / (double(width) * c);
+  r2c[0][3] = -1.0 / c;
+  r2c[1][1] = 2.0 / (double(height) * double(aspect) * c);
+  r2c[1][3] = -1.0 / (double(aspect) * c);
+  r2c[2][3] = 1.0;
+  r2c[3][2] = 1.0 / b;
+  r2c[3][3] = -a / b;
+  for (int col = 0; col < 4; ++col)
+    for (int row = 0; row < 4; ++row) {
+      out->camera_to_world[col * 4 + row] = float(c2w[row][col]);
+      out->raster_to_camera[col * 4 + row] = float(r2c[row][col]);
+      out->env_transform[col * 4 + row] = row == col ? 1.0f : 0.0f;
+    }
+  out->aperture = aperture;
+  out->focal_distance = focal_distance;
+  return ASUNA_OK;
+}
 float oracle_rand(uint32_t* state) { return rnd<float>(*state); }
 
 

@@ -77,6 +77,16 @@ int oracle_envmap_tables(uint32_t w, uint32_t h, const float* rgba, float* marg_
 /* Post pass (tone mapping) of one RGBA image, as the library's asuna_tonemap. */
 int oracle_tonemap(const float* rgba, uint32_t w, uint32_t h, const asuna_post_state* post, float* out);
 
+/* Host preprocessing a scene description needs, restated here so that a run
+ * timing only the reference's code builds its workload without the library.
+ * computeDiffuseFresnel (src/loader/material.cpp:6-37). */
+float oracle_diffuse_fresnel(float ior, int samples);
+/* CameraPerspective::toGpuStruct (src/core/camera.cpp:28-62, 87-99; view =
+ * scale(1,-1,-1) * lookAt, src/core/camera.h:26-28); fov horizontal, degrees. */
+int oracle_camera_perspective(const float eye[3], const float lookat[3], const float up[3], float fov_deg,
+                              float aperture, float focal_distance, uint32_t width, uint32_t height,
+                              asuna_camera* out);
+
 #ifdef __cplusplus
 }
 #endif

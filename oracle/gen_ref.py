@@ -25,12 +25,33 @@ Rewrites (all mechanical, no logic changes):
     array has 8 entries (an out-of-bounds write on the GPU); the loop bound is
     reduced to 8 so host C++ stays defined.
 
-Usage: python oracle/gen_ref.py [--ref /root/reference] [--out oracle/_ref/gen]
+The reference's ``src/shared/*.h`` headers (the device-ABI structs the
+shaders and the harness include) are copied beside the translation, so the
+generated tree compiles where the reference checkout is absent (the GPU
+host): ``oracle/build_oracle.py`` builds from it there.
+
+Usage: python oracle/gen_ref.py [--ref <reference checkout>] [--out oracle/_ref/gen]
+The checkout defaults to $ASUNA_REFERENCE, else ``baseline/_ref`` in this
+repository, else the path the build container mounts it at (find_ref_tree).
 """
 import argparse
 import os
 import re
+import shutil
 import sys
+
+_REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+# where the build container mounts the reference checkout (read-only)
+_MOUNTED_CHECKOUT = "/root/reference"
+MANIFEST = "GENERATED_FROM"
+
+
+def find_ref_tree():
+    """The reference checkout holding src/shaders, or None."""
+    for cand in (os.environ.get("ASUNA_REFERENCE"), os.path.join(_REPO, "baseline", "_ref"), _MOUNTED_CHECKOUT):
+        if cand and os.path.isdir(os.path.join(cand, "src", "shaders")):
+            return cand
+    return None
 
 SHADERS = {
     # file (relative to src/shaders) -> stage namespace (None = shared utility)
@@ -129,9 +150,14 @@ def sun_and_sky_min(text):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     here = os.path.dirname(os.path.abspath(__file__))
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None)
     ap.add_argument("--out", default=os.path.join(here, "_ref", "gen"))
     a = ap.parse_args(argv)
+    if a.ref is None:
+        a.ref = find_ref_tree()
+    if a.ref is None:
+        print("reference checkout not found ($ASUNA_REFERENCE, baseline/_ref)", file=sys.stderr)
+        return 2
     shaders = os.path.join(a.ref, "src", "shaders")
     if not os.path.isdir(shaders):
         print(f"reference shaders not found under {shaders}", file=sys.stderr)
@@ -146,6 +172,13 @@ def main(argv=None):
         txt = f.read()
     with open(os.path.join(a.out, "sun_and_sky_min.glsl.h"), "w") as f:
         f.write(sun_and_sky_min(txt))
+    shared_in, shared_out = os.path.join(a.ref, "src", "shared"), os.path.join(a.out, "shared")
+    os.makedirs(shared_out, exist_ok=True)
+    for name in sorted(os.listdir(shared_in)):
+        if name.endswith(".h"):
+            shutil.copyfile(os.path.join(shared_in, name), os.path.join(shared_out, name))
+    with open(os.path.join(a.out, MANIFEST), "w") as f:
+        f.write(os.path.abspath(a.ref) + "\n")
     return 0
 
 

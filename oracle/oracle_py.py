@@ -1,8 +1,8 @@
 """ctypes access to the CPU oracle (test infrastructure only).
 
 ``port`` is the C++ restatement (oracle/asuna_oracle.cpp); ``ref`` is the
-reference's own shader source compiled as host C++ (built only where the
-reference tree exists).  Both take the same asuna_scene_desc / asuna_shot as
+reference's own shader source compiled as host C++ (built where the reference
+checkout, or an earlier translation of it, is present).  Both take the same asuna_scene_desc / asuna_shot as
 the library.  Imported only by tests, the smoke check and the benchmark's CPU
 baseline.
 """
@@ -53,6 +53,10 @@ def port():
         L.oracle_math.argtypes = [C.c_int, C.c_float, C.c_float]
         L.oracle_envmap_tables.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_tonemap.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]
+        L.oracle_diffuse_fresnel.restype = C.c_float
+        L.oracle_diffuse_fresnel.argtypes = [C.c_float, C.c_int]
+        L.oracle_camera_perspective.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_float,
+                                                C.c_uint32, C.c_uint32, C.POINTER(A.Camera)]
         _port = L
     return _port
 
@@ -70,6 +74,11 @@ def ref():
         L.ref_xxhash32.argtypes = [C.c_uint32] * 3
         L.ref_rand.restype = C.c_float
         L.ref_rand.argtypes = [C.POINTER(C.c_uint32)]
+        L.ref_sample_begin.restype = C.c_void_p
+        L.ref_sample_begin.argtypes = [C.POINTER(A.SceneDesc), C.POINTER(A.Shot), C.c_void_p]
+        L.ref_sample_run.argtypes = [C.c_void_p, C.POINTER(A.Shot), C.c_void_p, C.c_uint32, C.c_int,
+                                     C.POINTER(OracleStats)]
+        L.ref_sample_end.argtypes = [C.c_void_p]
         _ref = L
     return _ref
 
@@ -145,3 +154,50 @@ def ref_render(desc, shot, threads=0):
     if rc:
         raise RuntimeError(f"ref_render failed: {rc}")
     return film, rec
+
+
+class OracleHelpers:
+    """The oracle's restatements of the host preprocessing a scene
+    description needs (asuna_gb300.scene.host_helpers), so that a process
+    timing only reference code builds its workload without the library."""
+
+    @staticmethod
+    def diffuse_fresnel(ior):
+        return port().oracle_diffuse_fresnel(C.c_float(ior), 1000)
+
+    @staticmethod
+    def camera_perspective(e, l, u, fov, aperture, focal_distance, width, height, cam):
+        rc = port().oracle_camera_perspective(e.ctypes.data, l.ctypes.data, u.ctypes.data, fov, aperture,
+                                              focal_distance, width, height, C.byref(cam))
+        if rc:
+            raise RuntimeError(f"oracle_camera_perspective failed: {rc}")
+
+
+class RefSampler:
+    """The reference's own shader code over pixel samples of one shot size
+    (one session at a time): run(shot, pixels) -> stats of the rays traced."""
+
+    def __init__(self, desc, shot):
+        self.L = ref()
+        if self.L is None:
+            raise RuntimeError("reference shader library not available")
+        self.film = np.zeros((A.NUM_OUTPUT_IMAGES, shot.height, shot.width, 4), np.float32)
+        self._desc = desc
+        self.h = self.L.ref_sample_begin(desc.ptr, C.byref(shot), self.film.ctypes.data)
+        if not self.h:
+            raise RuntimeError("ref_sample_begin failed")
+
+    def run(self, shot, pixels, threads=0):
+        px = np.ascontiguousarray(pixels, np.uint32)
+        st = OracleStats()
+        rc = self.L.ref_sample_run(self.h, C.byref(shot), px.ctypes.data, len(px), threads, C.byref(st))
+        if rc:
+            raise RuntimeError(f"ref_sample_run failed: {rc}")
+        return {k: getattr(st, k) for k, _ in OracleStats._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ref_sample_end(self.h)
+            self.h = None
+
+    __del__ = close

@@ -14,6 +14,9 @@
 // reference tree is present; pins oracle/asuna_oracle.cpp.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
+#include <cstring>
+#include <new>
 #include <cstdint>
 #include <thread>
 #include <vector>
@@ -116,6 +119,8 @@ struct PathTls {
   uint32_t sig, events, shadows;
 };
 thread_local PathTls tls;
+// rays this thread traced (closest hit, occlusion)
+thread_local uint64_t tlsExtendRays = 0, tlsShadowRays = 0;
 
 inline uint32_t sigMix(uint32_t h, uint32_t v) { return h ^ (v + 0x9e3779b9u + (h << 6) + (h >> 2)); }
 
@@ -133,6 +138,7 @@ void traceRayEXT(accelerationStructureEXT, uint, uint, uint, uint, uint, vec3 or
   const uint32_t bit = 1u << (payload.pRec.depth - 1);
   if (payloadLoc == 1) {
     // occlusion ray: terminate on first hit, no closest-hit shader
+    ++tlsShadowRays;
     tls.shadows |= bit;
     if (!oracle_occluded(gS->os, o, d, tmin, tmax)) {
       stage_shadow::main();
@@ -142,6 +148,7 @@ void traceRayEXT(accelerationStructureEXT, uint, uint, uint, uint, uint, vec3 or
   }
   float t, bu, bv;
   uint32_t inst, prim;
+  ++tlsExtendRays;
   if (!oracle_trace(gS->os, o, d, tmin, tmax, &t, &inst, &prim, &bu, &bv)) {
     stage_miss::main();
     tls.sig = sigMix(tls.sig, 0xffffffffu);
@@ -214,15 +221,12 @@ float ref_rand(uint32_t* state) {
 // W*H*4 floats; records (optional) hold the clamped per-path radiance (the
 // rgen writes the clamp back into the payload, rgen:147), depth, signature
 // and shadow bits.  Only seed 0 (the reference's streams) is meaningful.
-int ref_render(const asuna_scene_desc* d, const asuna_shot* shot, float* film, asuna_path_record* records,
-               int nthreads) {
+// Scene state of the shaders' descriptors, set up for one render.
+static int refSetup(const asuna_scene_desc* d, const asuna_shot* shot, float* film, RefScene& S) {
   using namespace glslx;
-  if (!d || !shot || !film) return ASUNA_ERR_INVALID;
-  if (shot->seed != 0 || (shot->flags & ASUNA_SHOT_RR)) return ASUNA_ERR_UNSUPPORTED;
   oracle_scene* os = nullptr;
   int rc = oracle_scene_create(d, &os);
   if (rc) return rc;
-  RefScene S;
   S.os = os;
   const uint32_t W = shot->width, H = shot->height;
   S.lights.assign(reinterpret_cast<const GpuLight*>(d->lights), reinterpret_cast<const GpuLight*>(d->lights) + d->num_lights);
@@ -269,16 +273,32 @@ int ref_render(const asuna_scene_desc* d, const asuna_shot* shot, float* film, a
   sunAndSky = GpuSunAndSky{};
   sunAndSky.in_use = 0;
   for (int k = 0; k < NUM_OUTPUT_IMAGES; ++k) images[k] = image2D{film + size_t(k) * W * H * 4, int(W), int(H)};
+  return ASUNA_OK;
+}
+
+static void refTeardown(RefScene& S) {
+  gS = nullptr;
+  oracle_scene_destroy(const_cast<oracle_scene*>(S.os));
+}
+
+// Runs the rgen for frames [frame0, frame0 + frames) of the listed pixels
+// (all pixels when `pixels` is NULL) on `nthreads` threads.
+static void refRun(const asuna_shot* shot, const uint32_t* pixels, uint32_t npix, asuna_path_record* records,
+                   int nthreads, uint64_t* extendRays, uint64_t* shadowRays) {
+  using namespace glslx;
+  const uint32_t W = shot->width;
   GpuPushConstantRaytrace base;
   std::memcpy(&base, &shot->state, sizeof(base));
   base.spp = 1;
   if (nthreads <= 0) nthreads = int(std::max(1u, std::thread::hardware_concurrency()));
   std::atomic<uint32_t> next{0};
-  const uint32_t npix = W * H;
+  std::atomic<uint64_t> ext{0}, sh{0};
   auto worker = [&] {
+    tlsExtendRays = tlsShadowRays = 0;
     for (;;) {
-      uint32_t i = next.fetch_add(1);
-      if (i >= npix) break;
+      uint32_t k = next.fetch_add(1);
+      if (k >= npix) break;
+      const uint32_t i = pixels ? pixels[k] : k;
       for (uint32_t f = 0; f < shot->frames; ++f) {
         uint32_t frame = shot->frame0 + f;
         pc = base;
@@ -287,7 +307,7 @@ int ref_render(const asuna_scene_desc* d, const asuna_shot* shot, float* film, a
         tls = PathTls{0, 0, 0};
         stage_rgen::main();
         if (records) {
-          asuna_path_record& r = records[size_t(f) * npix + i];
+          asuna_path_record& r = records[size_t(f) * npix + k];
           r.radiance[0] = payload.pRec.radiance.x;
           r.radiance[1] = payload.pRec.radiance.y;
           r.radiance[2] = payload.pRec.radiance.z;
@@ -300,14 +320,79 @@ int ref_render(const asuna_scene_desc* d, const asuna_shot* shot, float* film, a
         }
       }
     }
+    ext += tlsExtendRays;
+    sh += tlsShadowRays;
   };
   std::vector<std::thread> th;
   for (int t = 1; t < nthreads; ++t) th.emplace_back(worker);
   worker();
   for (auto& t : th) t.join();
-  gS = nullptr;
-  oracle_scene_destroy(os);
+  if (extendRays) *extendRays = ext.load();
+  if (shadowRays) *shadowRays = sh.load();
+}
+
+// Renders a shot with the reference's shader code; film = 9 images of
+// W*H*4 floats; records (optional) hold the clamped per-path radiance (the
+// rgen writes the clamp back into the payload, rgen:147), depth, signature
+// and shadow bits.  Only seed 0 (the reference's streams) is meaningful.
+int ref_render(const asuna_scene_desc* d, const asuna_shot* shot, float* film, asuna_path_record* records,
+               int nthreads) {
+  if (!d || !shot || !film) return ASUNA_ERR_INVALID;
+  if (shot->seed != 0 || (shot->flags & ASUNA_SHOT_RR)) return ASUNA_ERR_UNSUPPORTED;
+  RefScene S;
+  int rc = refSetup(d, shot, film, S);
+  if (rc) return rc;
+  refRun(shot, nullptr, shot->width * shot->height, records, nthreads, nullptr, nullptr);
+  refTeardown(S);
   return ASUNA_OK;
+}
+
+// The reference's shader code over pixel samples (throughput measurement).
+// ref_sample_begin sets the shaders' scene state up once (the oracle's BVH
+// build included) for shots of `shot`'s size writing into `film` (9 images
+// of W*H*4 floats, kept by the caller); ref_sample_run renders frames
+// [frame0, frame0 + frames) of the listed pixels and reports the rays traced
+// and the seconds spent; ref_sample_end releases the state.  One session at
+// a time (the shaders' descriptors are process-wide).  The reference has no
+// Russian roulette: a shot asking for it is rejected.
+void* ref_sample_begin(const asuna_scene_desc* d, const asuna_shot* shot, float* film) {
+  if (!d || !shot || !film || gS) return nullptr;
+  RefScene* S = new (std::nothrow) RefScene;
+  if (!S) return nullptr;
+  if (refSetup(d, shot, film, *S) != ASUNA_OK) {
+    delete S;
+    return nullptr;
+  }
+  return S;
+}
+
+int ref_sample_run(void* session, const asuna_shot* shot, const uint32_t* pixels, uint32_t npixels, int nthreads,
+                   oracle_stats* stats) {
+  if (!session || session != gS || !shot || !pixels || !stats) return ASUNA_ERR_INVALID;
+  if (shot->seed != 0 || (shot->flags & ASUNA_SHOT_RR)) return ASUNA_ERR_UNSUPPORTED;
+  const uint32_t npix = shot->width * shot->height;
+  for (uint32_t k = 0; k < npixels; ++k)
+    if (pixels[k] >= npix) return ASUNA_ERR_INVALID;
+  std::memcpy(&glslx::cameraInfo, &shot->camera, sizeof(GpuCamera));
+  if (nthreads <= 0) nthreads = int(std::max(1u, std::thread::hardware_concurrency()));
+  const auto t0 = std::chrono::steady_clock::now();
+  uint64_t ext = 0, sh = 0;
+  refRun(shot, pixels, npixels, nullptr, nthreads, &ext, &sh);
+  const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  std::memset(stats, 0, sizeof(*stats));
+  stats->paths = uint64_t(npixels) * shot->frames;
+  stats->extend_rays = ext;
+  stats->shadow_rays = sh;
+  stats->seconds = sec;
+  stats->threads = nthreads;
+  return ASUNA_OK;
+}
+
+void ref_sample_end(void* session) {
+  if (!session || session != gS) return;
+  RefScene* S = static_cast<RefScene*>(session);
+  refTeardown(*S);
+  delete S;
 }
 
 }  // extern "C"

@@ -101,3 +101,41 @@ def test_furnace_closed_form(ctx, albedo):
     sigma = img[inside].std(0) / math.sqrt(inside.sum())
     assert np.all(np.abs(got - expect) <= 4 * sigma + 1e-4), (got, expect, sigma)
     assert np.all(img[outside] == 1.0)
+
+
+@pytest.fixture(scope="module")
+def benchmark_workload(ctx):
+    """The benchmarked configuration itself: 64 level-7 icospheres
+    (20,971,520 triangles + ground + 4 light triangles), 1920x1080, depth 12,
+    1024x512 lognormal environment with a x1000 hotspot, 4 triangle lights,
+    aperture 0.05; the scene seed of bench.py."""
+    b, shot = scenes.mixed_scene(1920, 1080, frames=4, max_depth=12, n_spheres=64, level=7, seed=1234, rr_depth=3)
+    d = b.desc()
+    scene = ctx.create_scene(d)
+    osc = oracle_py.OracleScene(d)
+    yield b, d, shot, scene, osc
+    osc.close()
+    scene.close()
+
+
+@pytest.mark.parametrize("rr", [True, False], ids=["rr3", "rr_off"])
+def test_benchmark_workload_parity(ctx, benchmark_workload, rr):
+    """Per-path parity on the 21M-triangle 1080p benchmark workload: a seeded
+    subset of 16,384 pixels x 4 frames (65,536 paths), once with Russian
+    roulette after depth 3 as benchmarked and once without it (the
+    reference's estimator); every radiance channel within 1e-4 relative on
+    >= 99.9% of paths, branch flips counted and bounded."""
+    import copy
+
+    from asuna_gb300 import _abi as A
+    from oracle import parity
+
+    b, d, shot, scene, osc = benchmark_workload
+    s = copy.copy(shot)
+    if not rr:
+        s.flags &= ~A.SHOT_RR
+    c = parity.sample_parity(ctx, scene, d, s, npixels=16384, frames=4, seed=0, oracle_scene=osc)
+    print(c)
+    assert c["paths"] == 65536
+    assert c["within"] >= 0.999, c
+    assert c["flip_frac"] <= 1e-3, c

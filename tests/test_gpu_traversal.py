@@ -88,3 +88,54 @@ def test_tmin_tmax_contract(ctx):
     assert np.all(occ[:, 0] > 0)
     hits, inst = scene.trace(o, dirs, tmin=1.5, tmax=np.float32(1e10))
     assert np.all(inst == 0xFFFFFFFF)
+
+
+def test_truncated_traversal_is_reported(ctx):
+    """A traversal cut short by a full stack makes every render entry point
+    fail with ERR_TRAVERSAL: the call itself when it waits (stats, records),
+    else the next call that waits (film read, sync).  Each cut is reported
+    once, and the context renders normally afterwards."""
+    from asuna_gb300 import _abi as A
+
+    b, shot = scenes.box_scene(32, 32, frames=1, max_depth=3)
+    scene = ctx.create_scene(b.desc())
+    film = ctx.create_film(32, 32)
+    try:
+        ctx.set_traversal_stack(1)  # entering any instance needs a second entry
+        ctx.render(scene, shot, film)  # asynchronous: queued without error
+        with pytest.raises(A.AsunaError) as e:
+            film.read(0)
+        assert e.value.code == A.ERR_TRAVERSAL
+        with pytest.raises(A.AsunaError) as e:
+            ctx.render(scene, shot, film, stats=True)
+        assert e.value.code == A.ERR_TRAVERSAL
+        with pytest.raises(A.AsunaError) as e:
+            ctx.render_paths(scene, shot, film)
+        assert e.value.code == A.ERR_TRAVERSAL
+        ctx.render(scene, shot, film)
+        with pytest.raises(A.AsunaError) as e:
+            ctx.sync()
+        assert e.value.code == A.ERR_TRAVERSAL
+    finally:
+        ctx.set_traversal_stack(0)
+    ctx.render(scene, shot, film, stats=True)
+    film.read(0)
+    ctx.sync()
+
+
+def test_runaway_traversal_is_reported(ctx):
+    """A ray that would walk past the traversal's loop bound (70,000
+    coincident instances) is stopped and reported, not left running."""
+    from asuna_gb300 import _abi as A
+
+    b, shot = scenes.stacked_instances_scene(70000)
+    scene = ctx.create_scene(b.desc())
+    film = ctx.create_film(shot.width, shot.height)
+    with pytest.raises(A.AsunaError) as e:
+        ctx.render(scene, shot, film, stats=True)
+    assert e.value.code == A.ERR_TRAVERSAL
+    # a few hundred copies stay far inside the bound
+    b2, shot2 = scenes.stacked_instances_scene(300)
+    scene2 = ctx.create_scene(b2.desc())
+    ctx.render(scene2, shot2, film, stats=True)
+    assert float(film.read(0)[..., :3].max()) > 0.0

@@ -118,3 +118,28 @@ def test_furnace_closed_form(albedo):
     sigma = img[inside].std(0) / math.sqrt(inside.sum())
     assert np.all(np.abs(got - expect) <= 4 * sigma + 1e-4), (got, expect, sigma)
     assert np.all(img[outside] == 1.0)
+
+
+def test_oracle_host_helpers_match_the_library():
+    """The oracle's own restatements of the diffuse-Fresnel integral
+    (material.cpp:6-37) and the perspective camera (camera.cpp:28-99), which
+    the reference arm of the benchmark builds its workload with, agree with
+    the library's: the integral bit for bit, the matrices to float rounding."""
+    import asuna_gb300 as ag
+    from asuna_gb300 import _abi as A
+    from asuna_gb300 import scene as sc
+
+    for ior in (1.1, 1.33, 1.5, 2.4):
+        assert oracle_py.OracleHelpers.diffuse_fresnel(ior) == sc._LibraryHelpers.diffuse_fresnel(ior)
+    for eye, at, fov, w, h in [((0, 0, 3.9), (0, 0, 0), 40.0, 256, 256), ((30, 5, -12), (1, 2, 3), 55.0, 1920, 1080),
+                               ((-3, 8, 1), (0, 0, 0), 20.0, 512, 300)]:
+        cams = []
+        for prov in (sc._LibraryHelpers, oracle_py.OracleHelpers):
+            with sc.host_helpers(prov):
+                cams.append(ag.perspective_camera(eye, at, (0, 1, 0), fov, w, h, aperture=0.05, focal_distance=7.0))
+        a, b = cams
+        assert a.type == b.type == A.CAMERA_PERSPECTIVE
+        for f in ("camera_to_world", "raster_to_camera", "env_transform"):
+            x, y = np.array(getattr(a, f)), np.array(getattr(b, f))
+            assert np.allclose(x, y, rtol=2e-6, atol=1e-7), (f, x, y)
+        assert (a.aperture, a.focal_distance) == (b.aperture, b.focal_distance)

@@ -6,7 +6,9 @@ allocator).  Its scratch lives in one fixed array compiled into the library.
 Checked through the C ABI against asuna_render on two calls in a row (the
 second call starts from the array the first one left behind), within the
 tolerance of the other GPU tests (identical kernels, so the films agree to
-float rounding of the same operations), and the size limit is enforced.
+float rounding of the same operations); on shots that take several batches
+of the fixed path slots (3 and 65 batches); the size limit is enforced, a
+traversal cut short is reported, and a capturing stream is refused.
 Collected last so that a failure here leaves every other test already run;
 it also passes alone in a fresh process.
 """
@@ -73,3 +75,61 @@ def test_noalloc_rejects_frames_beyond_its_scratch():
     rc = fn(scene.handle, C.byref(s), film.handle, None)
     assert rc == A.ERR_INVALID
     assert b"exceeds the scratch maximum" in A.lib().asuna_last_error()
+
+
+@pytest.mark.parametrize("width,height,frames", [(512, 512, 3), (512, 256, 129)])
+def test_noalloc_matches_render_over_many_batches(width, height, frames):
+    """512 x 512 takes one frame per batch (3 batches); 512 x 256 two frames
+    per batch (65 batches), each reusing the same path slots."""
+    ctx = ag.Context(0)
+    fn = _noalloc()
+    b, s = scenes.box_scene(width, height, frames=frames, max_depth=3)
+    sc = ctx.create_scene(b.desc())
+    want = _expect(ctx, sc, s)
+    f = ctx.create_film(width, height)
+    stream = A.lib().asuna_ctx_stream(ctx.handle)
+    A.check(fn(sc.handle, C.byref(s), f.handle, stream))
+    got = _films(f)
+    assert _close(got, want)
+    assert float(got[8, ..., 0].min()) > 0.0  # every pixel has its filter weight
+
+
+def test_noalloc_reports_a_runaway_traversal_and_recovers():
+    """70,000 coincident instances drive every camera ray into the
+    traversal's loop bound: the call returns ERR_TRAVERSAL.  The next call
+    starts from a cleared count and succeeds."""
+    ctx = ag.Context(0)
+    fn = _noalloc()
+    b, s = scenes.stacked_instances_scene(70000)
+    sc = ctx.create_scene(b.desc())
+    f = ctx.create_film(s.width, s.height)
+    rc = fn(sc.handle, C.byref(s), f.handle, None)
+    assert rc == A.ERR_TRAVERSAL
+    assert b"cut short" in A.lib().asuna_last_error()
+    b2, s2 = scenes.box_scene(16, 16, frames=1, max_depth=2)
+    sc2 = ctx.create_scene(b2.desc())
+    f2 = ctx.create_film(16, 16)
+    A.check(fn(sc2.handle, C.byref(s2), f2.handle, None))
+
+
+def test_noalloc_refuses_a_capturing_stream():
+    """The call waits for its work, so on a stream being captured it queues
+    nothing and returns ERR_UNSUPPORTED; the capture itself stays valid."""
+    import torch
+
+    ctx = ag.Context(0)
+    fn = _noalloc()
+    b, s = scenes.box_scene(16, 16, frames=1, max_depth=2)
+    sc = ctx.create_scene(b.desc())
+    f = ctx.create_film(16, 16)
+    A.check(fn(sc.handle, C.byref(s), f.handle, None))  # set-up on this device happens outside the capture
+    x = torch.zeros(4, device="cuda:0")
+    g = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    with torch.cuda.graph(g, stream=side):
+        rc = fn(sc.handle, C.byref(s), f.handle, C.c_void_p(side.cuda_stream))
+        x.add_(1.0)
+    assert rc == A.ERR_UNSUPPORTED
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(x.sum()) == 4.0
