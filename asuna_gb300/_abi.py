@@ -13,6 +13,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libasuna_rt.so")
 
 # ---- status codes and enums (asuna_rt.h) -----------------------------------
+ABI_VERSION = 2
 OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_IO, ERR_PARSE, ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_NO_DEVICE, ERR_BUSY, \
     ERR_TRAVERSAL = range(11)
 CAMERA_PERSPECTIVE, CAMERA_OPENCV = 0, 1
@@ -89,11 +90,25 @@ class TextureDesc(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("rgba", C.c_void_p)]
 
 
+class SunAndSky(C.Structure):
+    """GpuSunAndSky (src/shared/sun_and_sky.h:6-27), 96 bytes."""
+    _fields_ = [("rgb_unit_conversion", C.c_float * 3), ("multiplier", C.c_float), ("haze", C.c_float),
+                ("redblueshift", C.c_float), ("saturation", C.c_float), ("horizon_height", C.c_float),
+                ("ground_color", C.c_float * 3), ("horizon_blur", C.c_float), ("night_color", C.c_float * 3),
+                ("sun_disk_intensity", C.c_float), ("sun_direction", C.c_float * 3), ("sun_disk_scale", C.c_float),
+                ("sun_glow_intensity", C.c_float), ("y_is_up", C.c_int32), ("physically_scaled_sun", C.c_int32),
+                ("in_use", C.c_int32)]
+
+
+assert C.sizeof(SunAndSky) == 96
+
+
 class SceneDesc(C.Structure):
     _fields_ = [("num_meshes", C.c_uint32), ("meshes", C.POINTER(MeshDesc)), ("num_instances", C.c_uint32),
                 ("instances", C.POINTER(InstanceDesc)), ("num_materials", C.c_uint32),
                 ("materials", C.POINTER(Material)), ("num_lights", C.c_uint32), ("lights", C.POINTER(Light)),
-                ("envmap", EnvmapDesc), ("num_textures", C.c_uint32), ("textures", C.POINTER(TextureDesc))]
+                ("envmap", EnvmapDesc), ("num_textures", C.c_uint32), ("textures", C.POINTER(TextureDesc)),
+                ("sun_and_sky", C.POINTER(SunAndSky))]
 
 
 class Shot(C.Structure):
@@ -156,6 +171,7 @@ SIGNATURES = [
     ("asuna_ctx_set_ray_sort", C.c_int, [P, C.c_int]),
     ("asuna_ctx_set_traversal_stack", C.c_int, [P, C.c_int]),
     ("asuna_scene_create", C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(P)]),
+    ("asuna_sun_and_sky_default", None, [C.POINTER(SunAndSky)]),
     ("asuna_scene_validate", C.c_int, [C.POINTER(SceneDesc)]),
     ("asuna_scene_destroy", C.c_int, [P]),
     ("asuna_scene_get_stats", C.c_int, [P, C.POINTER(SceneStats)]),
@@ -248,7 +264,7 @@ def lib():
             fn = getattr(L, name)
             fn.restype = res
             fn.argtypes = args
-        if L.asuna_abi_version() != 1:
+        if L.asuna_abi_version() != ABI_VERSION:
             raise AsunaError(ERR_INVALID, "ABI version mismatch")
         _lib = L
     return _lib

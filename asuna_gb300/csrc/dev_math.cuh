@@ -9,6 +9,7 @@
 #include <cstdint>
 
 #include "../../include/asuna_math.h"
+#include "../../include/asuna_sunsky.h"
 #include "dev_types.h"
 
 namespace asuna {
@@ -241,6 +242,19 @@ __device__ __forceinline__ f3 tex4rgb(const float4* t, int w, int h, float u, fl
             blerp(a, b, t00.z, t10.z, t01.z, t11.z)};
 }
 
+// math.glsl:134-139
+__device__ __forceinline__ f3 uniformSampleSphere(f2 u) {
+  float z = 1.0f - 2.0f * u.x;
+  float r = sqrtf(gmax(0.0f, 1.0f - z * z));
+  float phi = TWO_PI * u.y;
+  return f3{r * mcos(phi), r * msin(phi), z};
+}
+// sun_and_sky.glsl:405-533 (include/asuna_sunsky.h) in world direction L
+__device__ __noinline__ f3 evalSunSky(const SceneDev& S, f3 L) {
+  const asuna_sky::Params<float> p = asuna_sky::paramsOf<float>(S.sky);
+  const asuna_sky::V<float> r = asuna_sky::sunAndSky<float>(p, asuna_sky::V<float>{L.x, L.y, L.z});
+  return f3{r.x, r.y, r.z};
+}
 // sample_light.glsl:84-95
 __device__ __forceinline__ float pdfEnvmap(const SceneDev& S, const ShotDev& sh, f3 L) {
   L = transformDirectionT(sh.cam.env_transform, L);

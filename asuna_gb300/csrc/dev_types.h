@@ -106,6 +106,7 @@ struct SceneDev {
   int32_t numInst;
   uint32_t classMask;  // shading classes some instance can reach (bit k = class k)
   uint32_t passThrough;  // 1: some material can pass rays through (opacity)
+  asuna_sun_and_sky sky;  // in_use = 1: the sun & sky replaces the environment map
 };
 // Wavefront passes of a batch: one per bounce, plus the pass-through reserve.
 inline int wavefrontPasses(int maxDepth, const SceneDev& S) {

@@ -552,6 +552,8 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
       (rc = devUpload(s, texInfo.data(), texInfo.size(), &v.texInfo)))
     return rc;
   v.tlasRoot = int32_t(tlasBase);
+  std::memset(&v.sky, 0, sizeof(v.sky));
+  if (d->sun_and_sky && d->sun_and_sky->in_use == 1) v.sky = *d->sun_and_sky;
   v.envW = int32_t(ew);
   v.envH = int32_t(eh);
   v.numInst = int32_t(ni);

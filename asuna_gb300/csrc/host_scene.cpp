@@ -1383,6 +1383,31 @@ extern "C" {
 
 int asuna_abi_version(void) { return ASUNA_ABI_VERSION; }
 
+// Scene::reset's sun & sky (src/scene/scene.cpp:112-129)
+void asuna_sun_and_sky_default(asuna_sun_and_sky* out) {
+  if (!out) return;
+  std::memset(out, 0, sizeof(*out));
+  for (int k = 0; k < 3; ++k) {
+    out->rgb_unit_conversion[k] = 1.0f;
+    out->ground_color[k] = 0.4f;
+  }
+  out->multiplier = 0.0000101320f;
+  out->haze = 0.0f;
+  out->redblueshift = 0.0f;
+  out->saturation = 1.0f;
+  out->horizon_height = 0.0f;
+  out->horizon_blur = 0.1f;
+  out->night_color[2] = 0.01f;
+  out->sun_disk_intensity = 0.8f;
+  out->sun_direction[1] = 0.78f;
+  out->sun_direction[2] = 0.62f;
+  out->sun_disk_scale = 5.0f;
+  out->sun_glow_intensity = 1.0f;
+  out->y_is_up = 1;
+  out->physically_scaled_sun = 1;
+  out->in_use = 0;
+}
+
 int asuna_scene_validate(const asuna_scene_desc* desc) {
   clearError();
   if (!desc) return fail(ASUNA_ERR_INVALID, "null argument");

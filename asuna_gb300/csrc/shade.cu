@@ -255,7 +255,8 @@ __device__ __forceinline__ f3 sampleLights(const SceneDev& S, const ShotDev& sh,
                                            bool& visible, LRec& lRec) {
   bool allowDoubleSide = false;
   f3 radiance = splat(0.0f);
-  const bool hasEnv = sh.state.has_env_map == 1u;
+  const bool sky = S.sky.in_use == 1;
+  const bool hasEnv = sh.state.has_env_map == 1u || sky;
   const bool hasLight = sh.state.num_lights > 0;
   float envSel, anaSel;
   if (hasEnv && hasLight) {
@@ -275,7 +276,14 @@ __device__ __forceinline__ f3 sampleLights(const SceneDev& S, const ShotDev& sh,
     lRec.dist = INF;
     lRec.n = -makeNormal(rd);
     f2 u = rnd2(io.seed);
-    radiance = sampleEnvmap(S, sh, u, lRec.d, lRec.pdf) / envSel;
+    if (sky) {
+      // sample_light.glsl:137-141
+      lRec.d = uniformSampleSphere(u);
+      lRec.pdf = INV_4PI;
+      radiance = evalSunSky(S, lRec.d) / envSel;
+    } else {
+      radiance = sampleEnvmap(S, sh, u, lRec.d, lRec.pdf) / envSel;
+    }
     allowDoubleSide = true;
   } else if (sel < envSel + anaSel) {
     const int n = sh.state.num_lights;
@@ -1160,10 +1168,11 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
       if (CLS == kClsTerminal && inst == 0xffffffffu) {
         // raytrace.default.rmiss:24-56
         io.stop = true;
-        f3 env = (sh.state.has_env_map == 1u) ? evalEnvmap(S, sh, rd) : ld3(sh.state.bg_color);
+        const bool sky = S.sky.in_use == 1;
+        f3 env = sky ? evalSunSky(S, rd) : (sh.state.has_env_map == 1u) ? evalEnvmap(S, sh, rd) : ld3(sh.state.bg_color);
         float mis = 1.0f;
         if (depth != 1u && isNonSpecular(io.bflags)) {
-          float envPdf = (sh.state.has_env_map == 1u) ? pdfEnvmap(S, sh, rd) : INV_4PI;
+          float envPdf = sky ? INV_4PI : (sh.state.has_env_map == 1u) ? pdfEnvmap(S, sh, rd) : INV_4PI;
           mis = powerHeuristic(io.bpdf, envPdf);
         }
         io.rad = io.rad + io.thp * env * mis;

@@ -90,6 +90,22 @@ class _LibraryHelpers:
 _helpers = _LibraryHelpers()
 
 
+def _default_sky(s):
+    """Scene::reset's sun & sky (src/scene/scene.cpp:112-129); equal to the
+    library's asuna_sun_and_sky_default (tested), set here so scene
+    descriptions build without the library."""
+    s.rgb_unit_conversion = (C.c_float * 3)(1, 1, 1)
+    s.multiplier = 0.0000101320
+    s.haze, s.redblueshift, s.saturation, s.horizon_height = 0.0, 0.0, 1.0, 0.0
+    s.ground_color = (C.c_float * 3)(0.4, 0.4, 0.4)
+    s.horizon_blur = 0.1
+    s.night_color = (C.c_float * 3)(0.0, 0.0, 0.01)
+    s.sun_disk_intensity = 0.8
+    s.sun_direction = (C.c_float * 3)(0.00, 0.78, 0.62)
+    s.sun_disk_scale, s.sun_glow_intensity = 5.0, 1.0
+    s.y_is_up, s.physically_scaled_sun, s.in_use = 1, 1, 0
+
+
 @contextlib.contextmanager
 def host_helpers(provider):
     """Builds scene descriptions with another provider of the host
@@ -124,6 +140,7 @@ class SceneBuilder:
         self.lights = []
         self.instances = []  # (transform 3x4, mesh, material, light)
         self.env = None
+        self.sky = None
         # textures[0] is the reference's dummy texture (src/scene/scene.cpp:87-130)
         self.textures = [np.zeros((1, 1, 4), np.float32)]
         self.texture_names = ["add_by_default_dummy_texture"]
@@ -354,6 +371,22 @@ class SceneBuilder:
             rgba = np.concatenate([rgba, np.ones(rgba.shape[:2] + (1,), np.float32)], axis=2)
         self.env = np.ascontiguousarray(rgba)
 
+    def set_sun_and_sky(self, **fields):
+        """Turns the sun & sky environment on (GpuSunAndSky, in_use = 1):
+        the reference's defaults (Scene::reset, scene.cpp:112-129) with the
+        given fields replaced, e.g. sun_direction=(0.3, 0.8, 0.5)."""
+        s = A.SunAndSky()
+        _default_sky(s)
+        for k, v in fields.items():
+            f = getattr(s, k)
+            if hasattr(f, "__len__"):
+                setattr(s, k, type(f)(*v))
+            else:
+                setattr(s, k, v)
+        s.in_use = 1
+        self.sky = s
+        return s
+
     @property
     def num_lights(self):
         return len(self.lights) - 1  # Scene::submit, scene.cpp:33
@@ -415,6 +448,9 @@ class SceneDescHandle:
             self._keep.append(t)
         d.num_textures = len(b.textures)
         d.textures = self.textures
+        if b.sky is not None:
+            self.sky = A.SunAndSky.from_buffer_copy(b.sky)
+            d.sun_and_sky = C.pointer(self.sky)
         self.desc = d
 
     @property

@@ -417,3 +417,45 @@ def stacked_instances_scene(n_instances, width=8, height=8):
     state, depth = b.state(spp=1, max_path_depth=1, channels=())
     cam = perspective_camera((0, 0, 3.0), (0, 0, 0), (0, 1, 0), 10.0, width, height)
     return b, make_shot(cam, state, width, height, 1, depth_channel=depth)
+
+
+def sky_scene(width=48, height=32, frames=3, max_depth=6, dusk=False, point_light=False,
+              channels=("albedo", "normal", "depth")):
+    """Three level-3 icospheres (Lambertian, rough plastic, dielectric) over a
+    small ground quad under the sun & sky environment (GpuSunAndSky in use,
+    no environment map).  Day: the reference's default sky, the camera
+    pitched up toward the sun so the sun disk and glow are in view; dusk: the
+    sun 3 degrees below the horizon (night factor), haze 4, red/blue shift
+    0.2, saturation 0.6, a raised horizon, blur 0.5, no physical sun scaling
+    and a level camera, half of whose rays miss below the horizon (ground
+    colour branch).  With `point_light` a point light shares the light
+    sample with the sky."""
+    b = SceneBuilder()
+    if point_light:
+        b.add_point_light((1.5, 3.0, 1.0), (6.0, 5.0, 4.0))
+    if dusk:
+        a = math.radians(-3.0)
+        b.set_sun_and_sky(sun_direction=(0.6 * math.cos(a), math.sin(a), 0.8 * math.cos(a)), haze=4.0,
+                          redblueshift=0.2, saturation=0.6, horizon_height=0.5, horizon_blur=0.5,
+                          physically_scaled_sun=0, multiplier=2e-5)
+    else:
+        b.set_sun_and_sky()
+    ground = b.add_lambertian("ground", (0.4, 0.4, 0.4))
+    v, i = _quad(np.array((-2, -1, 2), np.float32), np.array((2, -1, 2), np.float32),
+                 np.array((2, -1, -2), np.float32), np.array((-2, -1, -2), np.float32), np.array((0, 1, 0), np.float32))
+    b.add_mesh("ground", v, i)
+    b.add_instance("ground", ground)
+    base_v, faces = icosphere(3)
+    idx = faces.astype(np.uint32).reshape(-1)
+    mats = [b.add_lambertian("lam", (0.7, 0.6, 0.5)), b.add_rough_plastic("plastic", (0.2, 0.4, 0.8), (0.2, 0.2)),
+            b.add_dielectric("glass", 1.5)]
+    for k, (mat, pos) in enumerate(zip(mats, [(-1.3, 0.0, 0.0), (0.0, 0.2, 0.6), (1.3, 0.0, 0.0)])):
+        verts = np.zeros(len(base_v), A.VERTEX_DTYPE)
+        verts["pos"] = base_v * 0.6
+        verts["normal"] = base_v
+        b.add_mesh(f"s{k}", verts, idx)
+        b.add_instance(f"s{k}", mat, np.array([[1, 0, 0, pos[0]], [0, 1, 0, pos[1]], [0, 0, 1, pos[2]]], np.float32))
+    state, depth = b.state(spp=frames, max_path_depth=max_depth, channels=channels)
+    eye, at = ((0.0, 0.3, -5.0), (0.0, 0.3, 0.0)) if dusk else ((0.0, 0.0, -5.0), (0.0, 4.5, 3.0))
+    cam = perspective_camera(eye, at, (0, 1, 0), 70.0, width, height)
+    return b, make_shot(cam, state, width, height, frames, depth_channel=depth)

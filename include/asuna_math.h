@@ -11,6 +11,7 @@
  *         polynomial of e^r, scaled by 2^n.
  *   sin,  reduction by pi/2 with a three-part Cody-Waite constant,
  *   cos   |r| <= pi/4, Taylor polynomials of degree 9 (sin) and 10 (cos).
+ *   tan   the same reduction; the quotient of the two polynomials.
  *   atan2 the range reduction and degree-9 odd minimax polynomial of the
  *         Cephes library's atanf (S. L. Moshier, "Methods and Programs for
  *         Mathematical Functions", 1989), with IEEE quadrant handling.
@@ -20,7 +21,7 @@
  *   log   the same ln m plus e ln 2 (ln 2 split in two parts).
  *   exp2  t = n + r, |r| <= 1/2: the exp polynomial at r ln 2, times 2^n.
  *   pow   exp2(y log2 x) (x > 0; GLSL leaves x < 0 undefined: NaN here).
- * Errors: sin, cos, exp within 1 ulp; atan2, acos, log2, log within 3 ulp; exp2
+ * Errors: sin, cos, exp within 1 ulp; tan within 3 ulp; atan2, acos, log2, log within 3 ulp; exp2
  * within 2 ulp; pow within 2 ulp plus |y log2 x| ulp of the exponent,
  * over the ranges the path tracer uses (tested against double precision).
  */
@@ -142,6 +143,15 @@ ASUNA_MATH_FN float cosf_(float x) {
     case 2: return -cos_poly(r);
     default: return sin_poly(r);
   }
+}
+
+/* tan = sin / cos of the one reduced argument: sin_poly(r) / cos_poly(r) for
+ * an even quadrant, -cos_poly(r) / sin_poly(r) for an odd one. */
+ASUNA_MATH_FN float tanf_(float x) {
+  if (fl_isnan(x) || fl_abs(x) == bits_to_float(0x7f800000u)) return bits_to_float(0x7fc00000u);
+  int k;
+  float r = reduce_pio2(x, &k);
+  return (k & 1) ? -cos_poly(r) / sin_poly(r) : sin_poly(r) / cos_poly(r);
 }
 
 /* atan of t >= 0 (Cephes atanf reduction and polynomial). */

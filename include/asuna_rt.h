@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define ASUNA_ABI_VERSION 1
+#define ASUNA_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------ */
 enum {
@@ -236,6 +236,31 @@ typedef struct asuna_texture_desc {
   const float* rgba;
 } asuna_texture_desc;
 
+/* GpuSunAndSky, src/shared/sun_and_sky.h:6-27 — 96 bytes, scalar layout:
+ * the analytic sun & sky environment (src/shaders/utils/sun_and_sky.glsl).
+ * With in_use = 1 it replaces the environment map in the miss shading and
+ * the environment light sample (raytrace.default.rmiss:30-31,
+ * rchit_layouts.glsl:105-107); asuna_sun_and_sky_default gives the
+ * reference's defaults (Scene::reset, src/scene/scene.cpp:112-129). */
+typedef struct asuna_sun_and_sky {
+  float rgb_unit_conversion[3];
+  float multiplier;
+  float haze;
+  float redblueshift;
+  float saturation;
+  float horizon_height;
+  float ground_color[3];
+  float horizon_blur;
+  float night_color[3];
+  float sun_disk_intensity;
+  float sun_direction[3];
+  float sun_disk_scale;
+  float sun_glow_intensity;
+  int32_t y_is_up;
+  int32_t physically_scaled_sun;
+  int32_t in_use;
+} asuna_sun_and_sky;
+
 typedef struct asuna_scene_desc {
   uint32_t num_meshes;
   const asuna_mesh_desc* meshes;
@@ -248,6 +273,7 @@ typedef struct asuna_scene_desc {
   asuna_envmap_desc envmap;
   uint32_t num_textures; /* the materials' *_texture_id index this list; */
   const asuna_texture_desc* textures; /* textures[0] is the dummy texture */
+  const asuna_sun_and_sky* sun_and_sky; /* NULL = not in use (the reference's default) */
 } asuna_scene_desc;
 
 /* ---- shots ----------------------------------------------------------------
@@ -364,6 +390,8 @@ int asuna_ctx_set_traversal_stack(asuna_ctx* ctx, int entries);
  * scene is immutable afterwards and may be shared by renders on any context
  * of the same device. */
 int asuna_scene_create(asuna_ctx* ctx, const asuna_scene_desc* desc, asuna_scene** out);
+/* The reference's sun & sky defaults (Scene::reset, scene.cpp:112-129; in_use 0). */
+void asuna_sun_and_sky_default(asuna_sun_and_sky* out);
 int asuna_scene_destroy(asuna_scene* scene);
 int asuna_scene_get_stats(const asuna_scene* scene, asuna_scene_stats* out);
 /* The checks asuna_scene_create runs before any upload (indices in range,

@@ -9,6 +9,7 @@
 // the GLSL source spells it.
 #include "asuna_oracle.h"
 #include "../include/asuna_math.h"
+#include "../include/asuna_sunsky.h"
 
 #include <algorithm>
 #include <atomic>
@@ -356,7 +357,22 @@ struct Scene {
   bool hasEnv = false;
   Tex env, marg, cond;
   std::vector<Tex> texs;  // material textures (RGBA)
+  // sun & sky (GpuSunAndSky.in_use = 1), in both precisions
+  bool sky = false;
+  asuna_sky::Params<float> skyF{};
+  asuna_sky::Params<double> skyD{};
 };
+
+// sun_and_sky.glsl:405-533 through include/asuna_sunsky.h
+template <class R> V3<R> sunSky(const Scene& s, V3<R> d);
+template <> V3<float> sunSky(const Scene& s, V3<float> d) {
+  const auto r = asuna_sky::sunAndSky<float>(s.skyF, asuna_sky::V<float>{d.x, d.y, d.z});
+  return {r.x, r.y, r.z};
+}
+template <> V3<double> sunSky(const Scene& s, V3<double> d) {
+  const auto r = asuna_sky::sunAndSky<double>(s.skyD, asuna_sky::V<double>{d.x, d.y, d.z});
+  return {r.x, r.y, r.z};
+}
 
 static void buildBvh(Mesh& m) {
   const uint32_t n = m.ntri;
@@ -746,7 +762,7 @@ V3<R> sampleLights(const Scene& s, const asuna_shot& sh, PathState<R>& p, V3<R> 
                    LRec<R>& lRec) {
   bool allowDoubleSide = false;
   V3<R> radiance = splat(R(0));
-  bool hasEnv = sh.state.has_env_map == 1;
+  bool hasEnv = sh.state.has_env_map == 1 || s.sky;
   bool hasLight = sh.state.num_lights > 0;
   R envSel, anaSel;
   if (hasEnv && hasLight)
@@ -759,12 +775,19 @@ V3<R> sampleLights(const Scene& s, const asuna_shot& sh, PathState<R>& p, V3<R> 
     envSel = anaSel = R(0);
   R sel = rnd<R>(p.seed);
   if (sel < envSel) {
-    // rchit_layouts.glsl:98-116 (sun-sky branch not implemented: in_use = 0)
+    // rchit_layouts.glsl:98-116: sun & sky (sample_light.glsl:137-141,
+    // uniform sphere) or the environment map
     lRec.flags = EArea;
     lRec.dist = K<R>::INF;
     lRec.n = -makeNormal(p.rd);
     V2<R> u = rnd2<R>(p.seed);
-    radiance = sampleEnvmap<R>(s, sh, u, lRec.d, lRec.pdf) / envSel;
+    if (s.sky) {
+      lRec.d = uniformSampleSphere<R>(u);
+      lRec.pdf = K<R>::INV_4PI;
+      radiance = sunSky<R>(s, lRec.d) / envSel;
+    } else {
+      radiance = sampleEnvmap<R>(s, sh, u, lRec.d, lRec.pdf) / envSel;
+    }
     allowDoubleSide = true;
   } else if (sel < envSel + anaSel) {
     int n = sh.state.num_lights;
@@ -2107,13 +2130,15 @@ void tracePath(const Scene& s, const asuna_shot& sh, uint32_t x, uint32_t y, uin
       // raytrace.default.rmiss:24-56
       p.stop = true;
       V3<R> env;
-      if (ps.has_env_map == 1)
+      if (s.sky)
+        env = sunSky<R>(s, p.rd);
+      else if (ps.has_env_map == 1)
         env = evalEnvmap<R>(s, sh, p.rd);
       else
         env = L3<R>(ps.bg_color);
       R mis = R(1);
       if (p.depth != 1 && isNonSpecular(p.bflags)) {
-        R envPdf = (ps.has_env_map == 1) ? pdfEnvmap<R>(s, sh, p.rd) : K<R>::INV_4PI;
+        R envPdf = s.sky ? K<R>::INV_4PI : (ps.has_env_map == 1) ? pdfEnvmap<R>(s, sh, p.rd) : K<R>::INV_4PI;
         mis = powerHeuristic(p.bpdf, envPdf);
       }
       p.radiance = p.radiance + p.throughput * env * mis;
@@ -2289,6 +2314,7 @@ float oracle_math(int which, float x, float y) {
     case 6: return asuna_math::exp2f_(x);
     case 7: return asuna_math::powf_(x, y);
     case 8: return asuna_math::logf_(x);
+    case 9: return asuna_math::tanf_(x);
     default: return matan2(x, y);
   }
 }
@@ -2574,6 +2600,11 @@ int oracle_scene_create(const asuna_scene_desc* d, oracle_scene** out) {
     s.texs[i].h = int(t.height);
     s.texs[i].c = 4;
     s.texs[i].d.assign(t.rgba, t.rgba + size_t(t.width) * t.height * 4);
+  }
+  if (d->sun_and_sky && d->sun_and_sky->in_use == 1) {
+    s.sky = true;
+    s.skyF = asuna_sky::paramsOf<float>(*d->sun_and_sky);
+    s.skyD = asuna_sky::paramsOf<double>(*d->sun_and_sky);
   }
   if (d->envmap.rgba && d->envmap.width && d->envmap.height) {
     int w = int(d->envmap.width), h = int(d->envmap.height);

@@ -70,7 +70,7 @@ int oracle_occluded(const oracle_scene* s, const float o[3], const float d[3], f
 /* World-to-object 3x4 of an object-to-world 3x4 (double inverse, rounded once). */
 void oracle_invert3x4(const float* m12, float* out12);
 /* The float transcendentals of include/asuna_math.h: 0 sin, 1 cos, 2 exp,
- * 3 acos, 4 atan2(x, y), 5 log2, 6 exp2, 7 pow(x, y), 8 log. */
+ * 3 acos, 4 atan2(x, y), 5 log2, 6 exp2, 7 pow(x, y), 8 log, 9 tan. */
 float oracle_math(int which, float x, float y);
 /* Env tables (marginal/conditional .xy per texel). */
 int oracle_envmap_tables(uint32_t w, uint32_t h, const float* rgba, float* marg_xy, float* cond_xy);

@@ -19,8 +19,9 @@ Rewrites (all mechanical, no logic changes):
   * ``vec2(rand(s), rand(s))`` -> brace initialisation, because C++ does not
     order function arguments and GLSL evaluates them left to right;
   * stage bodies (rgen / rmiss / rchit) are wrapped in their own namespaces;
-  * only ``luminance`` is taken from utils/sun_and_sky.glsl (sun & sky itself
-    is disabled in the reference's default scene state, in_use = 0);
+  * utils/sun_and_sky.glsl's ``M_PI`` (its own 3.1415926535f, defined only
+    where the name is free) is renamed, as the host's <cmath> defines M_PI as
+    a double;
   * raytrace.projective.rgen clears ``mRec.channel[i]`` for i < 9 although the
     array has 8 entries (an out-of-bounds write on the GPU); the loop bound is
     reduced to 8 so host C++ stays defined.
@@ -57,6 +58,7 @@ SHADERS = {
     # file (relative to src/shaders) -> stage namespace (None = shared utility)
     "utils/structs.glsl": None,
     "utils/math.glsl": None,
+    "utils/sun_and_sky.glsl": None,
     "utils/sample_light.glsl": None,
     "utils/rchit_layouts.glsl": None,
     "raytrace.projective.rgen": "stage_rgen",
@@ -100,8 +102,6 @@ def translate(text, rel, stage):
             base = os.path.basename(inc)
             if "/shared/" in inc or inc.startswith("shared/"):
                 lines.append(f"// [shared header at global scope] {inc}")
-            elif base == "sun_and_sky.glsl":
-                lines.append('#include "sun_and_sky_min.glsl.h"')
             else:
                 lines.append(f'#include "{base}.h"')
             body_start = len(lines)
@@ -114,6 +114,7 @@ def translate(text, rel, stage):
     src = SWIZZLE.sub(lambda m: "." + m.group(1) + "()", src)
     src = FLOAT_LIT.sub(lambda m: m.group(1) + "f", src)
     src = re.sub(r"\bINFINITY\b", "GLSL_INFINITY", src)
+    src = re.sub(r"\bM_PI\b", "GLSL_SKY_PI", src)
     src = src.replace("vec2(rand(seed), rand(seed))", "vec2{rand(seed), rand(seed)}")
     src = src.replace("vec3(rand(seed), rand(seed), rand(seed))", "vec3{rand(seed), rand(seed), rand(seed)}")
     if rel == "raytrace.projective.rgen":
@@ -133,18 +134,6 @@ def translate(text, rel, stage):
         src = "\n".join(out)
     header = f"// Generated by oracle/gen_ref.py from the reference's src/shaders/{rel}; do not commit.\n"
     return header + src + "\n"
-
-
-def sun_and_sky_min(text):
-    m = re.search(r"float luminance\(vec3 rgb\)\s*\{[^}]*\}", text)
-    if not m:
-        raise SystemExit("luminance() not found in sun_and_sky.glsl")
-    fn = FLOAT_LIT.sub(lambda mm: mm.group(1) + "f", m.group(0))
-    return ("// Generated by oracle/gen_ref.py: luminance() of the reference's\n"
-            "// src/shaders/utils/sun_and_sky.glsl; the sun & sky model is disabled\n"
-            "// (GpuSunAndSky.in_use = 0 in Scene::reset) and stubbed.\n"
-            "#ifndef SUN_AND_SKY_MIN\n#define SUN_AND_SKY_MIN\n" + fn + "\n"
-            "inline vec3 sun_and_sky(GpuSunAndSky, vec3) { return vec3(0.0f); }\n#endif\n")
 
 
 def main(argv=None):
@@ -168,10 +157,6 @@ def main(argv=None):
             txt = f.read()
         with open(os.path.join(a.out, out_name(rel)), "w") as f:
             f.write(translate(txt, rel, stage))
-    with open(os.path.join(shaders, "utils", "sun_and_sky.glsl")) as f:
-        txt = f.read()
-    with open(os.path.join(a.out, "sun_and_sky_min.glsl.h"), "w") as f:
-        f.write(sun_and_sky_min(txt))
     shared_in, shared_out = os.path.join(a.ref, "src", "shared"), os.path.join(a.out, "shared")
     os.makedirs(shared_out, exist_ok=True)
     for name in sorted(os.listdir(shared_in)):

@@ -164,6 +164,7 @@ inline float cos(float x) { return asuna_math::cosf_(x); }
 inline float acos(float x) { return asuna_math::acosf_(x); }
 inline float atan(float y, float x) { return asuna_math::atan2f_(y, x); }
 inline float pow(float x, float y) { return asuna_math::powf_(x, y); }
+inline float tan(float x) { return asuna_math::tanf_(x); }
 inline float log(float x) { return asuna_math::logf_(x); }
 inline float inversesqrt(float x) { return 1.0f / std::sqrt(x); }
 inline float sign(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
@@ -206,6 +207,16 @@ inline vec3 mix(vec3 x, vec3 y, float a) { return x * (1.0f - a) + y * a; }
 template <class A, class B, class T, class = std::enable_if_t<is_num<A> && is_num<B>>>
 inline float mix(A x, B y, T a) {
   return float(x) * (1.0f - float(a)) + float(y) * float(a);
+}
+
+// component-wise exp / pow (GLSL 4.60 §8.2)
+inline vec3 exp(vec3 v) { return vec3(exp(v.x), exp(v.y), exp(v.z)); }
+inline vec3 pow(vec3 a, vec3 b) { return vec3(pow(a.x, b.x), pow(a.y, b.y), pow(a.z, b.z)); }
+// smoothstep as the specification writes it (GLSL 4.60 §8.3)
+template <class A, class B, class X, class = std::enable_if_t<is_num<A> && is_num<B> && is_num<X>>>
+inline float smoothstep(A e0, B e1, X x) {
+  float t = clamp((float(x) - float(e0)) / (float(e1) - float(e0)), 0.0f, 1.0f);
+  return t * t * (3.0f - 2.0f * t);
 }
 
 // ---- geometric built-ins ----------------------------------------------------

@@ -39,6 +39,7 @@ static_assert(sizeof(GpuMaterial) == sizeof(asuna_material), "GpuMaterial layout
 static_assert(sizeof(GpuLight) == sizeof(asuna_light), "GpuLight layout");
 static_assert(sizeof(GpuCamera) == sizeof(asuna_camera), "GpuCamera layout");
 static_assert(sizeof(GpuPushConstantRaytrace) == sizeof(asuna_rt_state), "push constant layout");
+static_assert(sizeof(GpuSunAndSky) == sizeof(asuna_sun_and_sky), "GpuSunAndSky layout");
 
 namespace glslx {
 // ---- globals the shaders reach through descriptors / built-ins ------------
@@ -272,6 +273,7 @@ static int refSetup(const asuna_scene_desc* d, const asuna_shot* shot, float* fi
   std::memcpy(&cameraInfo, &shot->camera, sizeof(GpuCamera));
   sunAndSky = GpuSunAndSky{};
   sunAndSky.in_use = 0;
+  if (d->sun_and_sky) std::memcpy(&sunAndSky, d->sun_and_sky, sizeof(GpuSunAndSky));
   for (int k = 0; k < NUM_OUTPUT_IMAGES; ++k) images[k] = image2D{film + size_t(k) * W * H * 4, int(W), int(H)};
   return ASUNA_OK;
 }

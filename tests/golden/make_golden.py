@@ -4,6 +4,7 @@ shader code compiled as host C++ (oracle/gen_ref.py + oracle/ref_harness.cpp).
 Needs the reference tree (it is read where it lies; nothing of it is copied).
 Writes small .npz fixtures: RNG known answers and per-path records + film
 images of seeded procedural scenes.  Run: python tests/golden/make_golden.py
+[case ...] (no argument: every fixture).
 """
 import ctypes as C
 import os
@@ -29,6 +30,9 @@ CASES = {
                                                                       "specular", "uv")),
     "plugins_opacity_40x28x3": lambda: scenes.plugin_scene(40, 28, frames=3, env=True, textured=True, opacity=True,
                                                            channels=("albedo", "normal", "depth")),
+    "sky_day_48x32x3": lambda: scenes.sky_scene(48, 32, frames=3, channels=("albedo", "normal")),
+    "sky_dusk_light_40x24x2": lambda: scenes.sky_scene(40, 24, frames=2, dusk=True, point_light=True,
+                                                       channels=("albedo", "normal")),
 }
 
 
@@ -47,12 +51,16 @@ def rng_kat():
     return dict(xyz=xyz, hash=h, seeds=seeds, rand=draws)
 
 
-def main():
+def main(argv=None):
+    """Regenerates every fixture, or only the cases named on the command line."""
+    names = list(argv if argv is not None else sys.argv[1:]) or list(CASES)
     if oracle_py.ref() is None:
         print("reference tree not found; golden vectors not regenerated", file=sys.stderr)
         return 2
-    np.savez_compressed(os.path.join(HERE, "rng_kat.npz"), **rng_kat())
-    for name, make in CASES.items():
+    if not argv and len(sys.argv) <= 1:
+        np.savez_compressed(os.path.join(HERE, "rng_kat.npz"), **rng_kat())
+    for name in names:
+        make = CASES[name]
         b, shot = make()
         shot.depth_out_channel = -1  # the reference has no depth channel
         film, rec = oracle_py.ref_render(b.desc(), shot, threads=1)

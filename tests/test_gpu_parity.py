@@ -103,6 +103,18 @@ def test_furnace_closed_form(ctx, albedo):
     assert np.all(img[outside] == 1.0)
 
 
+@pytest.mark.parametrize("dusk,light", [(False, False), (True, True)], ids=["day", "dusk_light"])
+def test_sun_and_sky(ctx, dusk, light):
+    """The sun & sky environment (GpuSunAndSky in use) in the miss shading
+    and the environment light sample: by day with the sun disk in view, and
+    at dusk (sun below the horizon, haze, shifted colours, raised and blurred
+    horizon) with a point light sharing the light sample."""
+    b, shot = scenes.sky_scene(64, 48, frames=4, dusk=dusk, point_light=light)
+    rec, orec, imgs, ofilm = _run(ctx, b, shot)
+    c = _check(rec, orec, imgs, ofilm)
+    assert c["exact"] > 0.5
+
+
 @pytest.fixture(scope="module")
 def benchmark_workload(ctx):
     """The benchmarked configuration itself: 64 level-7 icospheres

@@ -78,7 +78,8 @@ def test_oracle_double_precision_close_to_float():
 @pytest.mark.parametrize("which,fn,lo,hi,ulps", [(0, np.sin, -7, 7, 1), (1, np.cos, -7, 7, 1), (2, np.exp, -20, 1, 1),
                                                  (3, np.arccos, -1, 1, 3), (4, None, -3, 3, 3),
                                                  (5, np.log2, 1e-6, 40, 3), (6, np.exp2, -30, 30, 2),
-                                                 (7, "pow", 0.0, 1.0, 80), (8, np.log, 1e-6, 40, 3)])
+                                                 (7, "pow", 0.0, 1.0, 80), (8, np.log, 1e-6, 40, 3),
+                                                 (9, np.tan, -1.5, 1.5, 3)])
 def test_shared_math_accuracy(which, fn, lo, hi, ulps):
     """include/asuna_math.h (used by the CUDA kernels and the oracle) against
     double precision, in ulps of the float result (pow: bases in (0, 1],
@@ -143,3 +144,17 @@ def test_oracle_host_helpers_match_the_library():
             x, y = np.array(getattr(a, f)), np.array(getattr(b, f))
             assert np.allclose(x, y, rtol=2e-6, atol=1e-7), (f, x, y)
         assert (a.aperture, a.focal_distance) == (b.aperture, b.focal_distance)
+
+
+def test_sun_and_sky_defaults_match_the_library():
+    """The builder's sun & sky defaults (set without the library) equal the
+    library's asuna_sun_and_sky_default (Scene::reset, scene.cpp:112-129)."""
+    import ctypes as C
+
+    from asuna_gb300 import _abi as A
+    from asuna_gb300 import scene as sc
+
+    a, b = A.SunAndSky(), A.SunAndSky()
+    A.lib().asuna_sun_and_sky_default(C.byref(a))
+    sc._default_sky(b)
+    assert bytes(a) == bytes(b)
