@@ -21,7 +21,8 @@ CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc") if os.path.exists(os.path.join(CUDA, "bin", "nvcc")) else "nvcc"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU = {"trace.cu": [], "shade.cu": ["-fmad=false"], "engine.cu": [], "noalloc.cu": [], "denoise.cu": [], "post.cu": [], "conv_tc.cu": [], "queue_sort.cu": []}
+CU = {"trace.cu": [], "shade.cu": ["-fmad=false"], "engine.cu": [], "noalloc.cu": [], "denoise.cu": [], "post.cu": [],
+      "conv_tc.cu": [], "queue_sort.cu": [], "bvh_device.cu": ["-fmad=false"]}
 CPP = ["host_scene.cpp", "json.cpp", "bvh_build.cpp", "server.cpp"]
 
 

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "bvh_build.h"
+#include "bvh_device.h"
 #include "common.h"
 #include "host_scene.h"
 #include "kernels.h"
@@ -252,6 +253,14 @@ int asuna_ctx_set_traversal(asuna_ctx* c, int refillExtend, int refillShadow, in
   return ASUNA_OK;
 }
 
+int asuna_ctx_set_bvh_build(asuna_ctx* c, int mode) {
+  clearError();
+  if (!c) return fail(ASUNA_ERR_INVALID, "null context");
+  if (mode != 0 && mode != 1) return fail(ASUNA_ERR_INVALID, "BVH build mode %d not in {0, 1}", mode);
+  c->bvhBuild = mode;
+  return ASUNA_OK;
+}
+
 int asuna_ctx_set_traversal_stack(asuna_ctx* c, int entries) {
   clearError();
   if (!c) return fail(ASUNA_ERR_INVALID, "null context");
@@ -304,63 +313,113 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
     vtxBase[m + 1] = vtxBase[m] + d->meshes[m].num_vertices;
   }
   if (triBase[nm] > kMaxLeafFirst) return fail(ASUNA_ERR_UNSUPPORTED, "scene has more than 2^28 triangles");
-  std::vector<BvhBuildOut> blas(nm);
-  std::vector<int> okMesh(nm, 1);
+  // shading data first: the device build reads positions and indices from them
+  SceneDev& v = s->view;
   {
-    std::atomic<uint32_t> next{0};
-    unsigned nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
-    std::vector<std::thread> th;
-    for (unsigned t = 0; t < nt; ++t)
-      th.emplace_back([&] {
-        for (uint32_t m; (m = next++) < nm;) {
-          const asuna_mesh_desc& md = d->meshes[m];
-          std::vector<Aabb> boxes(md.num_triangles);
-          std::vector<float> cen(size_t(md.num_triangles) * 3);
-          for (uint32_t i = 0; i < md.num_triangles; ++i) {
-            const float* p0 = md.vertices[md.indices[3 * i]].pos;
-            const float* p1 = md.vertices[md.indices[3 * i + 1]].pos;
-            const float* p2 = md.vertices[md.indices[3 * i + 2]].pos;
-            for (int k = 0; k < 3; ++k) {
-              boxes[i].lo[k] = std::min(p0[k], std::min(p1[k], p2[k]));
-              boxes[i].hi[k] = std::max(p0[k], std::max(p1[k], p2[k]));
-              cen[3 * i + k] = 0.5f * (boxes[i].lo[k] + boxes[i].hi[k]);
-            }
-          }
-          okMesh[m] = buildBvh(boxes, cen, 4, triBase[m], blas[m]) ? 1 : 0;
-        }
-      });
-    for (auto& t : th) t.join();
-  }
-  for (uint32_t m = 0; m < nm; ++m)
-    if (!okMesh[m]) return fail(ASUNA_ERR_UNSUPPORTED, "mesh %u: BVH cannot be encoded", m);
-  std::vector<uint32_t> nodeBase(nm + 1, 0);
-  uint32_t blasDepth = 0;
-  for (uint32_t m = 0; m < nm; ++m) {
-    nodeBase[m + 1] = nodeBase[m] + uint32_t(blas[m].nodes.size());
-    blasDepth = std::max(blasDepth, blas[m].maxDepth);
-  }
-  std::vector<BvhNode> nodes;
-  nodes.reserve(nodeBase[nm] + 2 * d->num_instances + 2);
-  std::vector<TriDev> tris(triBase[nm]);
-  for (uint32_t m = 0; m < nm; ++m) {
-    const asuna_mesh_desc& md = d->meshes[m];
-    for (BvhNode n : blas[m].nodes) {
-      if (n.ref.x >= 0) n.ref.x += int32_t(nodeBase[m]);
-      if (n.ref.y >= 0) n.ref.y += int32_t(nodeBase[m]);
-      nodes.push_back(n);
+    std::vector<VtxDev> vtx(vtxBase[nm]);
+    std::vector<uint4> idx(triBase[nm]);
+    for (uint32_t m = 0; m < nm; ++m) {
+      const asuna_mesh_desc& md = d->meshes[m];
+      for (uint32_t k = 0; k < md.num_vertices; ++k) {
+        const asuna_vertex& gv = md.vertices[k];
+        vtx[vtxBase[m] + k].pu = make_float4(gv.pos[0], gv.pos[1], gv.pos[2], gv.uv[0]);
+        vtx[vtxBase[m] + k].nv = make_float4(gv.normal[0], gv.normal[1], gv.normal[2], gv.uv[1]);
+      }
+      for (uint32_t t = 0; t < md.num_triangles; ++t)
+        idx[triBase[m] + t] = make_uint4(md.indices[3 * t], md.indices[3 * t + 1], md.indices[3 * t + 2], 0u);
     }
-    for (uint32_t i = 0; i < md.num_triangles; ++i) {
-      const uint32_t prim = blas[m].order[i];
-      const float* p0 = md.vertices[md.indices[3 * prim]].pos;
-      const float* p1 = md.vertices[md.indices[3 * prim + 1]].pos;
-      const float* p2 = md.vertices[md.indices[3 * prim + 2]].pos;
-      TriDev& t = tris[triBase[m] + i];
-      uint32_t pb = prim;
-      float pf;
-      std::memcpy(&pf, &pb, 4);
-      t.v0 = make_float4(p0[0], p0[1], p0[2], pf);
-      t.v1 = make_float4(p1[0], p1[1], p1[2], 0.0f);
-      t.v2 = make_float4(p2[0], p2[1], p2[2], 0.0f);
+    if ((rc = devUpload(s, vtx.data(), vtx.size(), &v.vtx)) || (rc = devUpload(s, idx.data(), idx.size(), &v.idx)))
+      return rc;
+  }
+  // ---- bottom level: one BVH per mesh, on the device (default) or host threads ----
+  const bool onDevice = c->bvhBuild == 0;
+  std::vector<BvhBuildOut> blas(onDevice ? 0 : nm);
+  DeviceBlas dblas;
+  std::vector<BvhNode> nodes;
+  std::vector<TriDev> tris;
+  std::vector<int32_t> rootIndex(nm, -1);
+  std::vector<BvhNode> rootNode(nm);
+  uint32_t blasNodes = 0, blasDepth = 0;
+  const uint32_t extraNodes = 2 * d->num_instances + 4;
+  if (onDevice) {
+    rc = buildBlasDevice(v.vtx, v.idx, triBase, vtxBase, extraNodes, c->stream, dblas);
+    if (dblas.nodes) {
+      s->allocs.push_back(dblas.nodes);
+      s->stats.device_bytes += uint64_t(dblas.nodeCapacity) * sizeof(BvhNode);
+    }
+    if (dblas.tris) {
+      s->allocs.push_back(dblas.tris);
+      s->stats.device_bytes += uint64_t(std::max<uint32_t>(triBase[nm], 1)) * sizeof(TriDev);
+    }
+    if (rc) return rc;
+    blasNodes = dblas.nodeCount;
+    blasDepth = dblas.maxDepth;
+    for (uint32_t m = 0; m < nm; ++m)
+      if (dblas.roots[m] >= 0) {
+        rootIndex[m] = dblas.roots[m];
+        rootNode[m] = dblas.rootNodes[size_t(dblas.roots[m])];
+      }
+  } else {
+    std::vector<int> okMesh(nm, 1);
+    {
+      std::atomic<uint32_t> next{0};
+      unsigned nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+      std::vector<std::thread> th;
+      for (unsigned t = 0; t < nt; ++t)
+        th.emplace_back([&] {
+          for (uint32_t m; (m = next++) < nm;) {
+            const asuna_mesh_desc& md = d->meshes[m];
+            std::vector<Aabb> boxes(md.num_triangles);
+            std::vector<float> cen(size_t(md.num_triangles) * 3);
+            for (uint32_t i = 0; i < md.num_triangles; ++i) {
+              const float* p0 = md.vertices[md.indices[3 * i]].pos;
+              const float* p1 = md.vertices[md.indices[3 * i + 1]].pos;
+              const float* p2 = md.vertices[md.indices[3 * i + 2]].pos;
+              for (int k = 0; k < 3; ++k) {
+                boxes[i].lo[k] = std::min(p0[k], std::min(p1[k], p2[k]));
+                boxes[i].hi[k] = std::max(p0[k], std::max(p1[k], p2[k]));
+                cen[3 * i + k] = 0.5f * (boxes[i].lo[k] + boxes[i].hi[k]);
+              }
+            }
+            okMesh[m] = buildBvh(boxes, cen, 4, triBase[m], blas[m]) ? 1 : 0;
+          }
+        });
+      for (auto& t : th) t.join();
+    }
+    for (uint32_t m = 0; m < nm; ++m)
+      if (!okMesh[m]) return fail(ASUNA_ERR_UNSUPPORTED, "mesh %u: BVH cannot be encoded", m);
+    std::vector<uint32_t> nodeBase(nm + 1, 0);
+    for (uint32_t m = 0; m < nm; ++m) {
+      nodeBase[m + 1] = nodeBase[m] + uint32_t(blas[m].nodes.size());
+      blasDepth = std::max(blasDepth, blas[m].maxDepth);
+      if (d->meshes[m].num_triangles) {
+        rootIndex[m] = int32_t(nodeBase[m]);
+        rootNode[m] = blas[m].nodes[0];
+      }
+    }
+    blasNodes = nodeBase[nm];
+    nodes.reserve(nodeBase[nm] + extraNodes);
+    tris.resize(triBase[nm]);
+    for (uint32_t m = 0; m < nm; ++m) {
+      const asuna_mesh_desc& md = d->meshes[m];
+      for (BvhNode n : blas[m].nodes) {
+        if (n.ref.x >= 0) n.ref.x += int32_t(nodeBase[m]);
+        if (n.ref.y >= 0) n.ref.y += int32_t(nodeBase[m]);
+        nodes.push_back(n);
+      }
+      for (uint32_t i = 0; i < md.num_triangles; ++i) {
+        const uint32_t prim = blas[m].order[i];
+        const float* p0 = md.vertices[md.indices[3 * prim]].pos;
+        const float* p1 = md.vertices[md.indices[3 * prim + 1]].pos;
+        const float* p2 = md.vertices[md.indices[3 * prim + 2]].pos;
+        TriDev& t = tris[triBase[m] + i];
+        uint32_t pb = prim;
+        float pf;
+        std::memcpy(&pf, &pb, 4);
+        t.v0 = make_float4(p0[0], p0[1], p0[2], pf);
+        t.v1 = make_float4(p1[0], p1[1], p1[2], 0.0f);
+        t.v2 = make_float4(p2[0], p2[1], p2[2], 0.0f);
+      }
     }
   }
   // ---- instances + top level ----
@@ -382,7 +441,7 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
     }
     const uint32_t m = id.mesh_id;
     const bool empty = d->meshes[m].num_triangles == 0;
-    I.blasRoot = empty ? -1 : int32_t(nodeBase[m]);
+    I.blasRoot = empty ? -1 : rootIndex[m];
     I.vtxBase = vtxBase[m];
     I.idxBase = triBase[m];
     I.matId = id.light_id >= 0 ? -1 : id.material_id;
@@ -391,7 +450,7 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
     s->view.classMask |= 1u << (id.light_id >= 0 ? int(kClsTerminal) : shadeClassOf(I.matType));
     if (empty) continue;
     // world box of the BLAS root's children
-    const BvhNode& r = blas[m].nodes[0];
+    const BvhNode& r = rootNode[m];
     float lo[3] = {r.xs.x, r.ys.x, r.zs.x}, hi[3] = {r.xs.y, r.ys.y, r.zs.y};
     if (r.ref.y != kStackSentinel) {
       lo[0] = std::min(lo[0], r.xs.z);
@@ -437,7 +496,8 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
   }
   BvhBuildOut tlas;
   if (!buildBvh(iboxes, icen, 1, 0, tlas)) return fail(ASUNA_ERR_UNSUPPORTED, "TLAS cannot be encoded");
-  const uint32_t tlasBase = uint32_t(nodes.size());
+  const uint32_t tlasBase = blasNodes;
+  std::vector<BvhNode> tlasNodes;
   for (BvhNode n : tlas.nodes) {
     for (int side = 0; side < 2; ++side) {
       int32_t& ref = side == 0 ? n.ref.x : n.ref.y;
@@ -447,24 +507,13 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
       else
         ref = encodeLeaf(ids[tlas.order[leafFirst(ref)]], 1);
     }
-    nodes.push_back(n);
+    tlasNodes.push_back(n);
   }
+  if (tlasNodes.size() > extraNodes) return fail(ASUNA_ERR_INVALID, "TLAS larger than reserved");
   if (tlas.maxDepth + blasDepth + 1 > uint32_t(kStackDepth))
     return fail(ASUNA_ERR_UNSUPPORTED, "BVH too deep for the traversal stack (TLAS %u + BLAS %u levels, limit %d)",
                 tlas.maxDepth, blasDepth, kStackDepth - 1);
-  // ---- shading data ----
-  std::vector<VtxDev> vtx(vtxBase[nm]);
-  std::vector<uint4> idx(triBase[nm]);
-  for (uint32_t m = 0; m < nm; ++m) {
-    const asuna_mesh_desc& md = d->meshes[m];
-    for (uint32_t v = 0; v < md.num_vertices; ++v) {
-      const asuna_vertex& gv = md.vertices[v];
-      vtx[vtxBase[m] + v].pu = make_float4(gv.pos[0], gv.pos[1], gv.pos[2], gv.uv[0]);
-      vtx[vtxBase[m] + v].nv = make_float4(gv.normal[0], gv.normal[1], gv.normal[2], gv.uv[1]);
-    }
-    for (uint32_t t = 0; t < md.num_triangles; ++t)
-      idx[triBase[m] + t] = make_uint4(md.indices[3 * t], md.indices[3 * t + 1], md.indices[3 * t + 2], 0u);
-  }
+  // ---- materials, lights, textures, environment ----
   std::vector<MatDev> mats(d->num_materials);
   for (uint32_t i = 0; i < d->num_materials; ++i) {
     const asuna_material& m = d->materials[i];
@@ -540,10 +589,19 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
     asuna_envmap_tables(ew, eh, d->envmap.rgba, reinterpret_cast<float*>(marg.data()),
                         reinterpret_cast<float*>(cond.data()));
   }
-  SceneDev& v = s->view;
-  if ((rc = devUpload(s, nodes.data(), nodes.size(), &v.nodes)) ||
-      (rc = devUpload(s, tris.data(), tris.size(), &v.tris)) || (rc = devUpload(s, vtx.data(), vtx.size(), &v.vtx)) ||
-      (rc = devUpload(s, idx.data(), idx.size(), &v.idx)) || (rc = devUpload(s, inst.data(), inst.size(), &v.inst)) ||
+  if (onDevice) {
+    // the top level goes after the device-built bottom levels
+    v.nodes = dblas.nodes;
+    v.tris = dblas.tris;
+    if (!tlasNodes.empty())
+      ASUNA_CUDA_TRY(cudaMemcpy(dblas.nodes + tlasBase, tlasNodes.data(), tlasNodes.size() * sizeof(BvhNode),
+                                cudaMemcpyHostToDevice));
+  } else {
+    nodes.insert(nodes.end(), tlasNodes.begin(), tlasNodes.end());
+    if ((rc = devUpload(s, nodes.data(), nodes.size(), &v.nodes)) || (rc = devUpload(s, tris.data(), tris.size(), &v.tris)))
+      return rc;
+  }
+  if ((rc = devUpload(s, inst.data(), inst.size(), &v.inst)) ||
       (rc = devUpload(s, mats.data(), mats.size(), &v.mats)) ||
       (rc = devUpload(s, lights.data(), lights.size(), &v.lights)) ||
       (rc = devUpload(s, env.data(), env.size(), &v.env)) || (rc = devUpload(s, marg.data(), marg.size(), &v.marg)) ||
@@ -559,7 +617,7 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
   v.numInst = int32_t(ni);
   s->stats.triangles = triBase[nm];
   s->stats.instances = ni;
-  s->stats.blas_nodes = nodeBase[nm];
+  s->stats.blas_nodes = blasNodes;
   s->stats.tlas_nodes = tlas.nodes.size();
   s->stats.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   *out = guard.release();

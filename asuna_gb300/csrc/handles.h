@@ -45,6 +45,7 @@ struct asuna_ctx {
   int32_t occupancy = 8;  // traversal kernel variant: resident blocks per SM
   int32_t raySort = 3;    // extend-queue sort mode before secondary passes (0 off)
   int32_t stackLimit = 0; // traversal stack entries a ray may use (0 = the compiled capacity)
+  int32_t bvhBuild = 0;   // bottom-level BVHs: 0 built on the device, 1 on host threads
   // traversals cut short on the device: the cumulative device count is
   // copied to hostErr after every render (errEvent marks the copy); the
   // host reports each increase over errSeen as ASUNA_ERR_TRAVERSAL

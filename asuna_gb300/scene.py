@@ -598,6 +598,11 @@ class Context:
         do not depend on it."""
         check(lib().asuna_ctx_set_ray_sort(self.handle, int(mode)))
 
+    def set_bvh_build(self, on_device=True):
+        """Build the bottom-level BVHs of new scenes on the device (default)
+        or on host threads (the same binned-SAH algorithm)."""
+        check(lib().asuna_ctx_set_bvh_build(self.handle, 0 if on_device else 1))
+
     def set_traversal_stack(self, entries=0):
         """Caps the traversal stack per ray (0 = the full 64 entries); a
         traversal needing more is cut short and reported as ERR_TRAVERSAL."""

@@ -384,6 +384,11 @@ int asuna_ctx_set_ray_sort(asuna_ctx* ctx, int mode);
  * A traversal that needs more entries is cut short and the render reports
  * ASUNA_ERR_TRAVERSAL; a lower cap serves to test that error path. */
 int asuna_ctx_set_traversal_stack(asuna_ctx* ctx, int entries);
+/* Where asuna_scene_create builds the bottom-level BVHs: 0 on the device
+ * (the default), 1 on host threads.  Both run the same binned-SAH
+ * algorithm; rendered results do not depend on the choice (leaf order and
+ * node numbering may differ, hits do not). */
+int asuna_ctx_set_bvh_build(asuna_ctx* ctx, int mode);
 
 /* ---- scene: upload + acceleration-structure build ------------------------ */
 /* Replaces Scene::submit + BLAS/TLAS build.  Host arrays are deep-copied; the

@@ -139,3 +139,69 @@ def test_runaway_traversal_is_reported(ctx):
     scene2 = ctx.create_scene(b2.desc())
     ctx.render(scene2, shot2, film, stats=True)
     assert float(film.read(0)[..., :3].max()) > 0.0
+
+
+def test_device_bvh_build_matches_host_build(ctx):
+    """The bottom-level BVHs built on the device (the default) and on host
+    threads run the same binned-SAH algorithm: every closest hit and every
+    occlusion answer of 20,000 random rays is identical, and the trees are
+    of the same size and depth class."""
+    b, _ = scenes.mixed_scene(8, 8, frames=1, n_spheres=24, level=5, seed=9, env_size=(32, 16))
+    d = b.desc()
+    dev = ctx.create_scene(d)
+    ctx.set_bvh_build(on_device=False)
+    try:
+        host = ctx.create_scene(d)
+    finally:
+        ctx.set_bvh_build(on_device=True)
+    rng = np.random.default_rng(3)
+    o, dirs = _random_rays(rng, 20000, np.zeros(3), 10.0)
+    for any_hit in (False, True):
+        h1, i1 = dev.trace(o, dirs, any_hit=any_hit)
+        h2, i2 = host.trace(o, dirs, any_hit=any_hit)
+        assert np.array_equal(i1, i2)
+        assert np.array_equal(h1.view(np.uint32), h2.view(np.uint32))
+    s1, s2 = dev.stats(), host.stats()
+    assert s1["triangles"] == s2["triangles"]
+    # the same algorithm: node counts within a few percent (chunked allocation aside)
+    assert abs(s1["blas_nodes"] - s2["blas_nodes"]) <= 0.05 * s2["blas_nodes"] + 64 * 256
+
+
+@pytest.mark.parametrize("n_tris", [1, 3, 4, 5, 2049, 70000])
+def test_device_bvh_build_edge_sizes(ctx, n_tris):
+    """Single meshes around the builder's thresholds (one triangle, a leaf,
+    one above a leaf, one above a warp's subtree, many) plus coincident
+    triangles: device and host builds give identical hits."""
+    from asuna_gb300 import _abi as A
+
+    rng = np.random.default_rng(n_tris)
+    b = ag.SceneBuilder()
+    m = b.add_lambertian("m", (0.5, 0.5, 0.5))
+    p = rng.uniform(-1, 1, (n_tris, 3)).astype(np.float32)
+    p[: n_tris // 4] = 0.25  # a quarter of the triangles share one place
+    v = np.zeros(3 * n_tris, A.VERTEX_DTYPE)
+    v["pos"] = (p[:, None, :] + rng.uniform(-0.05, 0.05, (n_tris, 3, 3)).astype(np.float32)).reshape(-1, 3)
+    v["pos"][: 3 * (n_tris // 4)] = np.tile(np.array([[0.2, 0.2, 0.2], [0.3, 0.2, 0.2], [0.2, 0.3, 0.2]],
+                                                     np.float32), (n_tris // 4, 1))
+    v["normal"] = (0, 0, 1)
+    b.add_mesh("t", v, np.arange(3 * n_tris, dtype=np.uint32))
+    b.add_instance("t", m)
+    b.add_instance("t", m, np.array([[1, 0, 0, 3], [0, 1, 0, 0], [0, 0, 1, 0]], np.float32))
+    d = b.desc()
+    dev = ctx.create_scene(d)
+    ctx.set_bvh_build(on_device=False)
+    try:
+        host = ctx.create_scene(d)
+    finally:
+        ctx.set_bvh_build(on_device=True)
+    o, dirs = _random_rays(rng, 4000, np.array([1.5, 0.0, 0.0]), 2.0)
+    # half of the rays aim at triangle centres (of either instance)
+    tc = v["pos"].reshape(-1, 3, 3).mean(1)[rng.integers(0, n_tris, 2000)] + \
+        np.array([3.0, 0.0, 0.0], np.float32) * rng.integers(0, 2, (2000, 1))
+    dd = tc - o[:2000]
+    dirs[:2000] = (dd / np.linalg.norm(dd, axis=1, keepdims=True)).astype(np.float32)
+    h1, i1 = dev.trace(o, dirs)
+    h2, i2 = host.trace(o, dirs)
+    assert np.array_equal(i1, i2)
+    assert np.array_equal(h1.view(np.uint32), h2.view(np.uint32))
+    assert (i1 != 0xFFFFFFFF).sum() > 0
