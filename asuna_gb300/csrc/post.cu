@@ -15,6 +15,7 @@
 
 #include "common.h"
 #include "handles.h"
+#include "../../include/asuna_math.h"
 
 namespace asuna {
 namespace {
@@ -43,9 +44,15 @@ __device__ __forceinline__ float3 max3(float3 a, float s) { return make_float3(f
 __device__ __forceinline__ float3 clamp3(float3 a, float lo, float hi) {
   return make_float3(fminf(fmaxf(a.x, lo), hi), fminf(fmaxf(a.y, lo), hi), fminf(fmaxf(a.z, lo), hi));
 }
-__device__ __forceinline__ float3 pow3(float3 a, float e) { return make_float3(powf(a.x, e), powf(a.y, e), powf(a.z, e)); }
-__device__ __forceinline__ float3 mix3(float3 a, float3 b, float t) { return a + (b - a) * t; }
-__device__ __forceinline__ float3 mix3(float3 a, float3 b, float3 t) { return a + (b - a) * t; }
+// the shared transcendentals (include/asuna_math.h), as the CPU oracle
+__device__ __forceinline__ float3 pow3(float3 a, float e) {
+  return make_float3(asuna_math::powf_(a.x, e), asuna_math::powf_(a.y, e), asuna_math::powf_(a.z, e));
+}
+// GLSL mix as the specification writes it: x (1 - a) + y a
+__device__ __forceinline__ float3 mix3(float3 a, float3 b, float t) { return a * (1.0f - t) + b * t; }
+__device__ __forceinline__ float3 mix3(float3 a, float3 b, float3 t) {
+  return make_float3(a.x * (1.0f - t.x) + b.x * t.x, a.y * (1.0f - t.y) + b.y * t.y, a.z * (1.0f - t.z) + b.z * t.z);
+}
 
 constexpr float kGamma = 2.2f;
 __device__ __forceinline__ float3 linearTosRGB(float3 c) { return pow3(c, 1.0f / kGamma); }
@@ -76,7 +83,7 @@ __device__ __forceinline__ float3 aces(float3 c) {
   return linearTosRGB(clamp3((c * (c * A + B)) / (c * (c * C + D) + E), 0.0f, 1.0f));
 }
 __device__ __forceinline__ float srgbCurve(float c) {
-  return c < 0.0031308f ? 12.92f * c : 1.055f * powf(c, 1.0f / 2.4f) - 0.055f;
+  return c < 0.0031308f ? 12.92f * c : 1.055f * asuna_math::powf_(c, 1.0f / 2.4f) - 0.055f;
 }
 
 // PCG3D hash (M. Jarzynski and M. Olano, "Hash functions for GPU
@@ -159,7 +166,7 @@ __global__ void __launch_bounds__(256) k_tonemap(Pyramid pyr, asuna_post_state t
             const Level& b = pyr.l[min(i + 1, pyr.n - 1)];
             const float v1 = lum709(f3(sample(a, u, v))) * factor;
             const float v2 = lum709(f3(sample(b, u, v))) * factor;
-            if (fabsf(v1 - v2) / ((tm.key * powf(2.0f, phi) / (scale[i] * scale[i])) + v1) > epsilon) {
+            if (fabsf(v1 - v2) / ((tm.key * asuna_math::powf_(2.0f, phi) / (scale[i] * scale[i])) + v1) > epsilon) {
               La = v1;
               break;
             }

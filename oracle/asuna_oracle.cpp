@@ -2249,7 +2249,11 @@ inline F3 sub(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 inline F3 mul(F3 a, F3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
 inline F3 div(F3 a, F3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
 inline F3 s3(float v) { return {v, v, v}; }
-inline F3 pw(F3 a, float e) { return {std::pow(a.x, e), std::pow(a.y, e), std::pow(a.z, e)}; }
+// pow of the shared transcendentals (include/asuna_math.h), as the pinned
+// shader translation evaluates it
+inline F3 pw(F3 a, float e) { return {asuna_math::powf_(a.x, e), asuna_math::powf_(a.y, e), asuna_math::powf_(a.z, e)}; }
+// GLSL mix as the specification writes it: x (1 - a) + y a
+inline float mixs(float x, float y, float a) { return x * (1.0f - a) + y * a; }
 inline F3 lin2s(F3 c) { return pw(c, 1.0f / 2.2f); }
 inline F3 s2lin(F3 c) { return pw(c, 2.2f); }
 inline float lum709(F3 c) { return c.x * 0.2126f + c.y * 0.7152f + c.z * 0.0722f; }
@@ -2264,7 +2268,7 @@ inline F3 hejl(F3 c) {
   return div(mul(c, add(mul(c, s3(6.2f)), s3(0.5f))), add(mul(c, add(mul(c, s3(6.2f)), s3(1.7f))), s3(0.06f)));
 }
 inline float clamp01(float v) { return std::min(std::max(v, 0.0f), 1.0f); }
-inline float srgb(float c) { return c < 0.0031308f ? 12.92f * c : 1.055f * std::pow(c, 1.0f / 2.4f) - 0.055f; }
+inline float srgb(float c) { return c < 0.0031308f ? 12.92f * c : 1.055f * asuna_math::powf_(c, 1.0f / 2.4f) - 0.055f; }
 struct Lv {
   std::vector<float> p;
   int w, h;
@@ -2486,7 +2490,8 @@ int oracle_tonemap(const float* rgba, uint32_t w, uint32_t h, const asuna_post_s
                 const Lv& a = pyr[std::min<size_t>(i, pyr.size() - 1)];
                 const Lv& b = pyr[std::min<size_t>(i + 1, pyr.size() - 1)];
                 const float v1 = lum709(sample(a, u, v)) * factor, v2 = lum709(sample(b, u, v)) * factor;
-                if (std::fabs(v1 - v2) / ((tm->key * std::pow(2.0f, 2.0f) / (scale[i] * scale[i])) + v1) > 0.05f) {
+                if (std::fabs(v1 - v2) / ((tm->key * asuna_math::powf_(2.0f, 2.0f) / (scale[i] * scale[i])) + v1) >
+                    0.05f) {
                   La = v1;
                   break;
                 }
@@ -2520,19 +2525,18 @@ int oracle_tonemap(const float* rgba, uint32_t w, uint32_t h, const asuna_post_s
                            std::floor(sv.z / quant) * quant};
             const F3 c1 = add(c0, s3(quant));
             const F3 l0 = s2lin(c0), l1 = s2lin(c1);
-            const F3 discr = {l0.x + (l1.x - l0.x) * noise[0], l0.y + (l1.y - l0.y) * noise[1],
-                              l0.z + (l1.z - l0.z) * noise[2]};
+            const F3 discr = {mixs(l0.x, l1.x, noise[0]), mixs(l0.y, l1.y, noise[1]), mixs(l0.z, l1.z, noise[2])};
             col = {discr.x < lin.x ? c1.x : c0.x, discr.y < lin.y ? c1.y : c0.y, discr.z < lin.z ? c1.z : c0.z};
           }
           // GLSL clamp as NVIDIA hardware evaluates it (and fminf / fmaxf):
           // IEEE 754 minNum / maxNum, so a NaN (0/0 on a black pixel under
           // auto exposure, post.idle.frag:45,68) clamps to 0
           auto clampNum = [](float v) { return std::fmin(std::fmax(v, 0.0f), 1.0f); };
-          col = {clampNum(0.5f + (col.x - 0.5f) * tm->contrast), clampNum(0.5f + (col.y - 0.5f) * tm->contrast),
-                 clampNum(0.5f + (col.z - 0.5f) * tm->contrast)};
+          col = {clampNum(mixs(0.5f, col.x, tm->contrast)), clampNum(mixs(0.5f, col.y, tm->contrast)),
+                 clampNum(mixs(0.5f, col.z, tm->contrast))};
           col = pw(col, 1.0f / tm->brightness);
           const float g = col.x * 0.299f + col.y * 0.587f + col.z * 0.114f;
-          col = {g + (col.x - g) * tm->saturation, g + (col.y - g) * tm->saturation, g + (col.z - g) * tm->saturation};
+          col = {mixs(g, col.x, tm->saturation), mixs(g, col.y, tm->saturation), mixs(g, col.z, tm->saturation)};
           const float vx = ((float(x) + 0.5f) / float(w) * tm->rendering_ratio[0] - 0.5f) * 2.0f;
           const float vy = ((float(y) + 0.5f) / float(h) * tm->rendering_ratio[1] - 0.5f) * 2.0f;
           const float vg = 1.0f - (vx * vx + vy * vy) * tm->vignette;

@@ -58,7 +58,8 @@ def build_ref(ref_tree=None, force=False):
     if ref_tree is None:
         ref_tree = gen_ref.find_ref_tree()
     gen = GEN_DIR
-    srcs = [os.path.join(HERE, "ref_harness.cpp"), os.path.join(HERE, "asuna_oracle.cpp")]
+    srcs = [os.path.join(HERE, "ref_harness.cpp"), os.path.join(HERE, "post_harness.cpp"),
+            os.path.join(HERE, "asuna_oracle.cpp")]
     deps = srcs + [os.path.join(HERE, "asuna_oracle.h"), os.path.join(HERE, "glsl_shim.h"),
                    os.path.join(REPO, "include", "asuna_rt.h"), os.path.join(REPO, "include", "asuna_math.h")]
     if ref_tree is not None:

@@ -76,6 +76,10 @@ SHADERS = {
     "bxdf/raytrace.brdf_pbr_metalness_roughness.rchit": "stage_pbr",
     "bxdf/raytrace.brdf_disney.rchit": "stage_disney",
     "bxdf/raytrace.brdf_kang18.rchit": "stage_kang18",
+    # the post pass (oracle/post_harness.cpp)
+    "utils/tonemapping.glsl": None,
+    "utils/random.glsl": None,
+    "post.idle.frag": "stage_post",
 }
 
 FLOAT_LIT = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")
@@ -117,6 +121,18 @@ def translate(text, rel, stage):
     src = re.sub(r"\bM_PI\b", "GLSL_SKY_PI", src)
     src = src.replace("vec2(rand(seed), rand(seed))", "vec2{rand(seed), rand(seed)}")
     src = src.replace("vec3(rand(seed), rand(seed), rand(seed))", "vec3{rand(seed), rand(seed), rand(seed)}")
+    src = src.replace("vec2(rand(prev), rand(prev))", "vec2{rand(prev), rand(prev)}")
+    if rel == "post.idle.frag":
+        # a GLSL array constructor; the output's and the input's .g/.b/.a
+        # components (not accessor-rewritten above) name the harness's fields
+        if "float[7](1, 2, 4, 8, 16, 32, 64)" not in src:
+            raise SystemExit("post.idle.frag: the scale array constructor not found")
+        src = src.replace("float[7](1, 2, 4, 8, 16, 32, 64)", "{1, 2, 4, 8, 16, 32, 64}")
+        for a, b in ((r"\bfragColor\.g\b", "fragColor.c.y"), (r"\bfragColor\.b\b", "fragColor.c.z"),
+                     (r"\bhdr\.g\b", "hdr.y"), (r"\bhdr\.b\b", "hdr.z"), (r"\bhdr\.a\b", "hdr.w")):
+            src, k = re.subn(a, b, src)
+            if not k:
+                raise SystemExit(f"post.idle.frag: {a} not found")
     if rel == "raytrace.projective.rgen":
         new = src.replace("for (int i = 0; i < NUM_OUTPUT_IMAGES; i++)\n      payload.mRec.channel[i]",
                           "for (int i = 0; i < NUM_OUTPUT_IMAGES - 1; i++)\n      payload.mRec.channel[i]")
@@ -125,7 +141,8 @@ def translate(text, rel, stage):
         src = new
     # no other call may take two side-effecting rand() arguments
     for ln in src.splitlines():
-        if ln.count("rand(") + ln.count("rand2(") >= 2 and "{rand(seed)" not in ln and not ln.strip().startswith("//"):
+        if ln.count("rand(") + ln.count("rand2(") >= 2 and "{rand(seed)" not in ln and "{rand(prev)" not in ln \
+                and not ln.strip().startswith("//"):
             raise SystemExit(f"{rel}: multiple RNG draws in one expression: {ln.strip()}")
     if stage:
         out = src.splitlines()

@@ -80,10 +80,26 @@ struct ivec3 {
 struct uvec3 {
   uint x = 0, y = 0, z = 0;
   uvec3() = default;
+  explicit uvec3(uint s) : x(s), y(s), z(s) {}
+  uvec3(uint a, uint b, uint c) : x(a), y(b), z(c) {}
   template <class C>
   uvec3(uvec2 v, C c) : x(v.x), y(v.y), z(uint(c)) {}
+  template <class C>
+  uvec3(vec2 v, C c) : x(uint(v.x)), y(uint(v.y)), z(uint(c)) {}  // float -> uint conversion
   uvec2 xy() const { return uvec2{x, y}; }
 };
+// unsigned vector arithmetic (wrapping, as GLSL's uint)
+inline uvec2 operator*(uvec2 a, uint s) { return uvec2{a.x * s, a.y * s}; }
+inline uvec2 operator+(uvec2 a, uint s) { return uvec2{a.x + s, a.y + s}; }
+inline uvec2 operator^(uvec2 a, uvec2 b) { return uvec2{a.x ^ b.x, a.y ^ b.y}; }
+inline uvec2 operator>>(uvec2 a, uint s) { return uvec2{a.x >> s, a.y >> s}; }
+inline uvec3 operator*(uvec3 a, uint s) { return uvec3(a.x * s, a.y * s, a.z * s); }
+inline uvec3 operator+(uvec3 a, uvec3 b) { return uvec3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline uvec3 operator^(uvec3 a, uvec3 b) { return uvec3(a.x ^ b.x, a.y ^ b.y, a.z ^ b.z); }
+inline uvec3 operator>>(uvec3 a, uvec3 b) { return uvec3(a.x >> b.x, a.y >> b.y, a.z >> b.z); }
+inline uvec3 operator>>(uvec3 a, int s) { return uvec3(a.x >> s, a.y >> s, a.z >> s); }
+inline uvec3 operator|(int s, uvec3 a) { return uvec3(uint(s) | a.x, uint(s) | a.y, uint(s) | a.z); }
+inline uvec3& operator^=(uvec3& a, uvec3 b) { return a = a ^ b; }
 struct uvec4 {
   uint x = 0, y = 0, z = 0, w = 0;
   uvec4(uint a, uint b, uint c, uint d) : x(a), y(b), z(c), w(d) {}
@@ -95,6 +111,13 @@ struct mat4 {
 };
 struct mat3 {
   vec3 c[3];
+  mat3() = default;
+  // GLSL's column-major constructor: the first three values are column 0
+  template <class... A, class = std::enable_if_t<sizeof...(A) == 9>>
+  explicit mat3(A... v) {
+    const float f[9] = {float(v)...};
+    for (int k = 0; k < 3; ++k) c[k] = vec3(f[3 * k], f[3 * k + 1], f[3 * k + 2]);
+  }
 };
 // mat4x3: four vec3 columns (gl_ObjectToWorldEXT / gl_WorldToObjectEXT).
 struct mat4x3 {
@@ -204,9 +227,32 @@ inline vec3 clamp(vec3 v, B lo, C hi) {
 }
 // GLSL mix as the specification writes it: x * (1 - a) + y * a
 inline vec3 mix(vec3 x, vec3 y, float a) { return x * (1.0f - a) + y * a; }
+inline vec3 mix(vec3 x, vec3 y, vec3 a) { return x * (1.0f - a) + y * a; }
 template <class A, class B, class T, class = std::enable_if_t<is_num<A> && is_num<B>>>
 inline float mix(A x, B y, T a) {
   return float(x) * (1.0f - float(a)) + float(y) * float(a);
+}
+
+inline vec3 operator*(const mat3& m, vec3 v) { return m.c[0] * v.x + m.c[1] * v.y + m.c[2] * v.z; }
+// component-wise max (GLSL 4.60 §8.3: y if x < y, else x)
+inline vec3 max(vec3 a, vec3 b) { return vec3(a.x < b.x ? b.x : a.x, a.y < b.y ? b.y : a.y, a.z < b.z ? b.z : a.z); }
+struct bvec3 {
+  bool x, y, z;
+};
+inline bvec3 lessThan(vec3 a, vec3 b) { return bvec3{a.x < b.x, a.y < b.y, a.z < b.z}; }
+inline vec3 mix(vec3 x, vec3 y, bvec3 a) { return vec3(a.x ? y.x : x.x, a.y ? y.y : x.y, a.z ? y.z : x.z); }
+inline vec3 floor(vec3 v) { return vec3(std::floor(v.x), std::floor(v.y), std::floor(v.z)); }
+inline vec3 uintBitsToFloat(uvec3 u) {
+  float f[3];
+  std::memcpy(&f[0], &u.x, 4);
+  std::memcpy(&f[1], &u.y, 4);
+  std::memcpy(&f[2], &u.z, 4);
+  return vec3(f[0], f[1], f[2]);
+}
+inline float uintBitsToFloat(uint u) {
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
 }
 
 // component-wise exp / pow (GLSL 4.60 §8.2)

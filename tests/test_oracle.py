@@ -158,3 +158,37 @@ def test_sun_and_sky_defaults_match_the_library():
     A.lib().asuna_sun_and_sky_default(C.byref(a))
     sc._default_sky(b)
     assert bytes(a) == bytes(b)
+
+
+@pytest.mark.skipif(oracle_py.ref() is None, reason="reference shader library not built")
+@pytest.mark.parametrize("tm,auto,extra", [(0, 0, {}), (1, 0, {}), (2, 0, {}), (3, 0, {}), (4, 0, {}), (5, 0, {}),
+                                           (6, 0, {}), (6, 1, {}), (6, 3, {}),
+                                           (6, 0, {"contrast": 1.3, "brightness": 0.8, "saturation": 0.6,
+                                                   "vignette": 0.4, "avg_lum": 1.7}),
+                                           (3, 0, {"zoom": 0.75})])
+def test_oracle_tonemap_matches_reference_post_shader(tm, auto, extra):
+    """The oracle's tone mapping (oracle_tonemap, the checker of the GPU's
+    asuna_tonemap) equals the reference's own post.idle.frag compiled as
+    host C++ (oracle/post_harness.cpp) bit for bit, for every operator, with
+    and without auto / local exposure, with the custom operator's contrast,
+    brightness, saturation and vignette, and with zoom; the sampler's mip
+    chain and filtering are the harness's (the graphics driver's in the
+    reference)."""
+    import ctypes as C
+
+    import asuna_gb300 as ag
+
+    rng = np.random.default_rng(40 + tm + 10 * auto)
+    img = np.exp(rng.normal(-0.5, 1.5, (48, 64, 4))).astype(np.float32)
+    img[..., 3] = 1.0
+    post = ag.default_post(tm)
+    post.auto_exposure = auto
+    for k, v in extra.items():
+        setattr(post, k, v)
+    a = np.zeros_like(img)
+    b = np.zeros_like(img)
+    assert oracle_py.port().oracle_tonemap(img.ctypes.data, 64, 48, C.byref(post), a.ctypes.data) == 0
+    L = oracle_py.ref()
+    L.ref_post.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]
+    assert L.ref_post(img.ctypes.data, 64, 48, C.byref(post), b.ctypes.data) == 0
+    assert np.array_equal(a, b), (np.abs(a - b).max(), (a != b).mean())

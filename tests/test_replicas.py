@@ -64,3 +64,49 @@ def test_two_gloo_ranks_cover_all_frames():
     for p in procs:
         p.join(timeout=60)
     assert [o[1] for o in out] == [9, 9] and [o[2] for o in out] == [2.0, 2.0]
+
+
+def _render_worker(rank, world, port, q):
+    """Renders this rank's frames of the small box scene with the CPU oracle
+    and sends (radiance, weight sum) to rank 0, which merges them."""
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from asuna_gb300 import scenes
+    from oracle import oracle_py
+
+    b, shot = scenes.box_scene(24, 20, frames=10, max_depth=5)
+    first, count = replicas.frame_shard(rank, world, 0, shot.frames)
+    shot.frame0, shot.frames = first, count
+    film, _, _ = oracle_py.OracleScene(b.desc()).render(shot, records=False)
+    parts = [None] * world
+    dist.all_gather_object(parts, (film[0], film[8]))
+    if rank == 0:
+        merged, wsum = replicas.merge_films(parts)
+        q.put((merged, wsum))
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_render_and_merge_like_one_process():
+    """Two ranks render disjoint frame shards (the CPU oracle stands in for
+    each rank's GPU); the merged film equals a single-process render of all
+    frames.  The single process keeps the reference's float32 running mean
+    frame by frame (rgen:171-178); the merge sums the two shards' weighted
+    means in float64, so the two agree to float32 rounding (1e-5 relative),
+    and the weight sums exactly up to float32 summation order."""
+    from asuna_gb300 import scenes
+    from oracle import oracle_py
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29700 + os.getpid() % 1000
+    procs = [ctx.Process(target=_render_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    merged, wsum = q.get(timeout=300)
+    for p in procs:
+        p.join(timeout=60)
+    b, shot = scenes.box_scene(24, 20, frames=10, max_depth=5)
+    film, _, _ = oracle_py.OracleScene(b.desc()).render(shot, records=False)
+    assert np.allclose(merged[..., :3], film[0][..., :3], rtol=1e-5, atol=1e-7)
+    assert np.allclose(wsum, film[8][..., 0], rtol=1e-6)
+    assert float(film[0][..., :3].mean()) > 0.0
