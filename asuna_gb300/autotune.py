@@ -13,13 +13,16 @@ BYTES_PER_PATH = 244  # wavefront state per path slot (asuna_gb300/csrc/engine.c
 
 
 def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64, 128), trace_options=(0, 6),
-         shade_options=(0, 2), refill_options=(4, 8, 16, 24), occupancy_options=(8, 10, 12), memory_bytes=80 << 30,
-         reps=2, frame_base=1 << 20):
+         shade_options=(0, 2), refill_options=(4, 8, 16, 24), occupancy_options=(8, 10, 12),
+         shape_options=((64, 24), (256, 24), (128, 16), (128, 32)), memory_bytes=80 << 30, reps=2,
+         frame_base=1 << 20):
     """Returns {"frames": f, "trace_blocks_per_sm": t, "shade_blocks_per_sm": s, "traversal": (refill
-    extend, refill shadow, speculate extend, speculate shadow, traversal blocks per SM), "ray_sort": 0..3,
-    "mrays": best, "trials": [...]} and leaves the context configured with the best choice.  Coordinate
-    search: frames, then grids, then the traversal kernel variant and the refill thresholds and
-    speculation of each pass, then extend-queue sorting, then the refill thresholds again under it."""
+    extend, refill shadow, speculate extend, speculate shadow, traversal blocks per SM), "shape": (threads
+    per block, shared-memory stack entries), "ray_sort": 0..3, "mrays": best, "trials": [...]} and leaves
+    the context configured with the best choice.  Coordinate search: frames, then grids, then the
+    traversal kernel variant and the refill thresholds and speculation of each pass, then extend-queue
+    sorting, then the refill thresholds again under it, then the traversal block size and the
+    traversal stack's shared-memory depth."""
     npix = shot.width * shot.height
     saved = (shot.frame0, shot.frames)
     trials = []
@@ -90,9 +93,19 @@ def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64, 128), t
                            "mrays": v})
             if v > best["mrays"]:
                 best = {**best, "traversal": tuple(trav), "mrays": v}
+        # block shape and the shared-memory part of the traversal stack
+        trav = list(best["traversal"])
+        best["shape"] = (0, 0)
+        for shape in shape_options:
+            ctx.set_traversal_shape(*shape)
+            v = run(best["frames"], best["trace_blocks_per_sm"], best["shade_blocks_per_sm"])
+            trials.append({"frames": best["frames"], "shape": shape, "mrays": v})
+            if v > best["mrays"]:
+                best = {**best, "shape": shape, "mrays": v}
     finally:
         shot.frame0, shot.frames = saved
     ctx.set_traversal(*best["traversal"])
+    ctx.set_traversal_shape(*best.get("shape", (0, 0)))
     ctx.set_launch(best["trace_blocks_per_sm"], best["shade_blocks_per_sm"])
     ctx.set_path_budget(best["frames"] * npix * BYTES_PER_PATH)
     film.clear()

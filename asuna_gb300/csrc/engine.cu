@@ -241,7 +241,7 @@ int asuna_ctx_set_traversal(asuna_ctx* c, int refillExtend, int refillShadow, in
   const int occ = blocksPerSm == 0 ? kTraceMinBlocks : blocksPerSm;
   if (occ != c->occupancy) {
     c->occupancy = occ;
-    c->traceGrid = c->numSMs * traceBlocksPerSm(occ);
+    c->traceGrid = c->numSMs * traceBlocksPerSm(occ, c->traceThreads, c->sharedStack);
   }
   const int r[2] = {refillExtend, refillShadow}, sp[2] = {specExtend, specShadow};
   for (int k = 0; k < 2; ++k) {
@@ -270,9 +270,22 @@ int asuna_ctx_set_traversal_stack(asuna_ctx* c, int entries) {
   return ASUNA_OK;
 }
 
+int asuna_ctx_set_traversal_shape(asuna_ctx* c, int threadsPerBlock, int sharedStack) {
+  clearError();
+  if (!c) return fail(ASUNA_ERR_INVALID, "null context");
+  if (threadsPerBlock != 0 && threadsPerBlock != 64 && threadsPerBlock != 128 && threadsPerBlock != 256)
+    return fail(ASUNA_ERR_INVALID, "traversal block of %d threads not in {0, 64, 128, 256}", threadsPerBlock);
+  if (sharedStack != 0 && sharedStack != 16 && sharedStack != 24 && sharedStack != 32)
+    return fail(ASUNA_ERR_INVALID, "shared stack of %d entries not in {0, 16, 24, 32}", sharedStack);
+  c->traceThreads = threadsPerBlock ? threadsPerBlock : kTraceThreads;
+  c->sharedStack = sharedStack ? sharedStack : kSharedStack;
+  c->traceGrid = c->numSMs * traceBlocksPerSm(c->occupancy, c->traceThreads, c->sharedStack);
+  return ASUNA_OK;
+}
+
 int asuna_ctx_set_launch(asuna_ctx* c, int traceBlocks, int shadeBlocks) {
   if (!c) return fail(ASUNA_ERR_INVALID, "null context");
-  const int tmax = traceBlocksPerSm(c->occupancy), smax = shadeBlocksPerSm();
+  const int tmax = traceBlocksPerSm(c->occupancy, c->traceThreads, c->sharedStack), smax = shadeBlocksPerSm();
   const int t = traceBlocks <= 0 ? tmax : std::min(traceBlocks, tmax);
   const int sh = shadeBlocks <= 0 ? smax : std::min(shadeBlocks, smax);
   c->traceGrid = c->numSMs * t;
@@ -831,7 +844,7 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
            uint64_t(uintptr_t(dShots)), uint64_t(uintptr_t(dRanges)), uint64_t(c->traceGrid), uint64_t(c->shadeGrid),
            uint64_t(c->raygenGrid), uint64_t(c->counters), uint64_t(stats ? 1 : 0), uint64_t(c->refill[0]),
            uint64_t(c->refill[1]), uint64_t(c->speculate[0]), uint64_t(c->speculate[1]), uint64_t(c->occupancy),
-           uint64_t(c->raySort), uint64_t(c->stackLimit)});
+           uint64_t(c->raySort), uint64_t(c->stackLimit), uint64_t(c->traceThreads), uint64_t(c->sharedStack)});
     for (const Batch& b : batches)
       key.insert(key.end(), {b.rangeBegin, b.rangeEnd, b.paths, b.maxPix, uint64_t(b.maxDepth)});
     for (auto& g : c->gcache)
@@ -883,6 +896,8 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
         P.cur ^= 1;
       }
       P.occupancy = c->occupancy;
+      P.blockThreads = c->traceThreads;
+      P.sharedStack = c->sharedStack;
       P.refillLanes = c->refill[0];
       P.speculate = c->speculate[0];
       timedLaunch(0, [&] { launchExtend(P, c->traceGrid, c->stream); });

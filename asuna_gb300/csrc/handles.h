@@ -42,7 +42,9 @@ struct asuna_ctx {
   // traversal settings of the extend [0] and connect [1] passes
   uint32_t refill[2] = {8, 8};
   int32_t speculate[2] = {1, 1};
-  int32_t occupancy = 8;  // traversal kernel variant: resident blocks per SM
+  int32_t occupancy = 8;  // traversal kernel variant: resident 128-thread blocks per SM (8, 10, 12)
+  int32_t traceThreads = 128;  // traversal kernel variant: threads per block
+  int32_t sharedStack = 24;    // traversal kernel variant: stack entries in shared memory
   int32_t raySort = 3;    // extend-queue sort mode before secondary passes (0 off)
   int32_t stackLimit = 0; // traversal stack entries a ray may use (0 = the compiled capacity)
   int32_t bvhBuild = 0;   // bottom-level BVHs: 0 built on the device, 1 on host threads

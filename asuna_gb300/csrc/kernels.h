@@ -17,6 +17,8 @@ struct KParams {
   int32_t speculate;     // traversal: postponed leaves walk on speculatively
   int32_t occupancy;     // traversal: resident blocks per SM of the kernel variant (8, 10 or 12)
   int32_t stackLimit;    // traversal: stack entries a ray may use (<= kStackDepth)
+  int32_t blockThreads;  // traversal: threads per block (64, 128, 256; 0 = 128)
+  int32_t sharedStack;   // traversal: stack entries in shared memory (16, 24, 32; 0 = 24)
 };
 
 constexpr int kTraceThreads = 128;
@@ -37,7 +39,10 @@ void launchSortQueue(const KParams& P, int mode, int grid, cudaStream_t s);
 void launchRecords(const KParams& P, asuna_path_record* out, int grid, cudaStream_t s);
 void launchExtend(const KParams& P, int grid, cudaStream_t s);
 void launchConnect(const KParams& P, int grid, cudaStream_t s);
-int traceBlocksPerSm(int occupancy = kTraceMinBlocks);
+// resident blocks per SM of the traversal variant (occupancy class 8/10/12 =
+// 32/40/48 resident warps, block size, shared-memory stack entries)
+int traceBlocksPerSm(int occupancy = kTraceMinBlocks, int blockThreads = kTraceThreads,
+                     int sharedStack = kSharedStack);
 int shadeBlocksPerSm();
 
 // Standalone ray queries (tests): rays are (o.xyz, tmin), (d.xyz, tmax).

@@ -130,6 +130,7 @@ struct HitOut {
 // there is postponed and, when `speculate`, the lane goes on visiting inner
 // nodes while other lanes of the warp still look for a leaf.  leafOrMove()
 // then tests the triangles of one leaf, or makes one TLAS/BLAS transition.
+template <int TB, int SHS>  // threads per block, stack entries in shared memory
 struct Trav {
   float3 wo, wd, wid;  // world-space ray and its inverse direction
   float3 o, id;        // ray origin / inverse direction in the current space
@@ -157,23 +158,23 @@ struct Trav {
     inBlas = false;
   }
 
-  // Stack: the first kSharedStack entries in shared memory (stride
-  // kTraceThreads: bank-conflict free), deeper ones in thread-local memory.
+  // Stack: the first SHS entries in shared memory (stride TB: bank-conflict
+  // free), deeper ones in thread-local memory.
   __device__ __forceinline__ void push(int32_t* sh, int32_t* loc, int32_t v, bool& ovf) {
     if (sp >= lim) {
       ovf = true;
       return;
     }
-    if (sp < kSharedStack)
-      sh[sp * kTraceThreads] = v;
+    if (sp < SHS)
+      sh[sp * TB] = v;
     else
-      loc[sp - kSharedStack] = v;
+      loc[sp - SHS] = v;
     ++sp;
   }
   __device__ __forceinline__ int32_t popOrDone(const int32_t* sh, const int32_t* loc) {
     if (sp == 0) return kDone;
     --sp;
-    return sp < kSharedStack ? sh[sp * kTraceThreads] : loc[sp - kSharedStack];
+    return sp < SHS ? sh[sp * TB] : loc[sp - SHS];
   }
 
   template <bool COUNT>
@@ -283,14 +284,14 @@ struct Trav {
 // lanes keep traversing.  Src supplies count, fetch(n) -> first index (called
 // by one lane), commit(first, n) (called by every lane), load(i, tr) and
 // finish(i, tr).
-template <bool ANY, bool COUNT, bool SPEC, class Src>
+template <bool ANY, bool COUNT, bool SPEC, int TB, int SHS, class Src>
 __device__ __forceinline__ void traceWarp(const SceneDev& S, Src& src, int32_t* sh, int32_t* loc, uint32_t refill,
                                           int stackLimit, uint32_t& nNodes, uint32_t& nTris, bool& ovf) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lanesBelow = (1u << lane) - 1u;
   bool active = false, drained = false;
   uint32_t idx = 0, events = 0;
-  Trav tr;
+  Trav<TB, SHS> tr;
   tr.lim = stackLimit > 0 && stackLimit < kStackDepth ? stackLimit : kStackDepth;
   for (;;) {
     const unsigned idle = __ballot_sync(0xffffffffu, !active);
@@ -350,7 +351,8 @@ struct QueueSrc {
   uint32_t count;
   __device__ __forceinline__ uint32_t fetch(uint32_t n) { return atomicAdd(fetchCtr, n); }
   __device__ __forceinline__ void commit(uint32_t, uint32_t) {}
-  __device__ __forceinline__ void load(const SceneDev& S, uint32_t r, Trav& tr) {
+  template <class T>
+  __device__ __forceinline__ void load(const SceneDev& S, uint32_t r, T& tr) {
     const float4 o4 = __ldg(&rO[r]);
     const float4 d4 = __ldg(&rD[r]);
     if (ANY)
@@ -358,7 +360,8 @@ struct QueueSrc {
     else
       tr.init(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), 0.00001f, 10000000000.0f);
   }
-  __device__ __forceinline__ void finish(uint32_t i, const Trav& tr) {
+  template <class T>
+  __device__ __forceinline__ void finish(uint32_t i, const T& tr) {
     if (ANY) {
       if (!tr.found) {
         const uint32_t p = __float_as_uint(__ldg(&rD[i].w));
@@ -380,11 +383,12 @@ struct QueueSrc {
   }
 };
 
-// OCC: resident blocks per SM the variant is compiled for (its register cap)
-template <bool ANY, bool COUNT, bool SPEC, int OCC>
-__global__ void __launch_bounds__(kTraceThreads, OCC) k_trace(KParams P) {
-  __shared__ int32_t sstack[kSharedStack * kTraceThreads];
-  int32_t lstack[kStackDepth - kSharedStack];
+// TB: threads per block; MINB: resident blocks per SM the variant is
+// compiled for (its register cap); SHS: stack entries in shared memory
+template <bool ANY, bool COUNT, bool SPEC, int TB, int MINB, int SHS>
+__global__ void __launch_bounds__(TB, MINB) k_trace(KParams P) {
+  __shared__ int32_t sstack[SHS * TB];
+  int32_t lstack[kStackDepth - SHS];
   int32_t* sh = sstack + threadIdx.x;
   const WaveDev& W = P.W;
   const int cur = P.cur;
@@ -411,7 +415,7 @@ __global__ void __launch_bounds__(kTraceThreads, OCC) k_trace(KParams P) {
   bool ovf = false;
   // (the instrumented variant walks without speculation, so its node counts
   // are those of the ordered traversal)
-  traceWarp<ANY, COUNT, SPEC>(P.S, src, sh, lstack, P.refillLanes, P.stackLimit, nNodes, nTris, ovf);
+  traceWarp<ANY, COUNT, SPEC, TB, SHS>(P.S, src, sh, lstack, P.refillLanes, P.stackLimit, nNodes, nTris, ovf);
   if (ovf) atomicAdd(&W.cnt->stackOverflow, 1ull);
   if (COUNT) {
     const unsigned lane = threadIdx.x & 31u;
@@ -438,11 +442,13 @@ struct ArraySrc {
   __device__ __forceinline__ uint32_t fetch(uint32_t) { return cursor; }
   // every lane of the warp advances its copy of the cursor alike
   __device__ __forceinline__ void commit(uint32_t base, uint32_t n) { cursor = base + n; }
-  __device__ __forceinline__ void load(const SceneDev& S, uint32_t r, Trav& tr) {
+  template <class T>
+  __device__ __forceinline__ void load(const SceneDev& S, uint32_t r, T& tr) {
     const float4 o4 = o[r], d4 = d[r];
     tr.init(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), o4.w, d4.w);
   }
-  __device__ __forceinline__ void finish(uint32_t i, const Trav& tr) {
+  template <class T>
+  __device__ __forceinline__ void finish(uint32_t i, const T& tr) {
     if (tr.found) {
       hit[i] = anyHit ? make_float4(1.0f, 0.0f, 0.0f, 0.0f)
                       : make_float4(tr.h.t, tr.h.u, tr.h.v, __uint_as_float(tr.h.prim));
@@ -468,45 +474,80 @@ __global__ void __launch_bounds__(kTraceThreads) k_query(SceneDev S, const float
   uint32_t a = 0, b = 0;
   bool ovf = false;
   if (anyHit)
-    traceWarp<true, false, true>(S, src, sh, lstack, kRefillLanes, kStackDepth, a, b, ovf);
+    traceWarp<true, false, true, kTraceThreads, kSharedStack>(S, src, sh, lstack, kRefillLanes, kStackDepth, a, b,
+                                                              ovf);
   else
-    traceWarp<false, false, true>(S, src, sh, lstack, kRefillLanes, kStackDepth, a, b, ovf);
+    traceWarp<false, false, true, kTraceThreads, kSharedStack>(S, src, sh, lstack, kRefillLanes, kStackDepth, a, b,
+                                                               ovf);
 }
 
 }  // namespace
 
 namespace {
-template <bool ANY, int OCC>
-void launchTraceOcc(const KParams& P, int grid, cudaStream_t s) {
+// Kernel variants: threads per block (64, 128, 256) x resident warps per SM
+// (32, 40, 48: the occupancy class 8, 10, 12 of 128-thread blocks) x stack
+// entries in shared memory (16, 24, 32).
+template <bool ANY, int TB, int OCC, int SHS>
+void launchShape(const KParams& P, int grid, cudaStream_t s) {
+  constexpr int MINB = OCC * 128 / TB;
   if (P.speculate)
-    k_trace<ANY, false, true, OCC><<<grid, kTraceThreads, 0, s>>>(P);
+    k_trace<ANY, false, true, TB, MINB, SHS><<<grid, TB, 0, s>>>(P);
   else
-    k_trace<ANY, false, false, OCC><<<grid, kTraceThreads, 0, s>>>(P);
+    k_trace<ANY, false, false, TB, MINB, SHS><<<grid, TB, 0, s>>>(P);
+}
+template <bool ANY, int TB, int OCC>
+void launchOcc(const KParams& P, int grid, cudaStream_t s) {
+  if (P.sharedStack >= 32)
+    launchShape<ANY, TB, OCC, 32>(P, grid, s);
+  else if (P.sharedStack > 0 && P.sharedStack <= 16)
+    launchShape<ANY, TB, OCC, 16>(P, grid, s);
+  else
+    launchShape<ANY, TB, OCC, 24>(P, grid, s);
+}
+template <bool ANY, int TB>
+void launchTb(const KParams& P, int grid, cudaStream_t s) {
+  if (P.occupancy >= 12)
+    launchOcc<ANY, TB, 12>(P, grid, s);
+  else if (P.occupancy >= 10)
+    launchOcc<ANY, TB, 10>(P, grid, s);
+  else
+    launchOcc<ANY, TB, kTraceMinBlocks>(P, grid, s);
 }
 template <bool ANY>
 void launchTrace(const KParams& P, int grid, cudaStream_t s) {
   if (P.counters)
-    k_trace<ANY, true, false, kTraceMinBlocks><<<grid, kTraceThreads, 0, s>>>(P);
-  else if (P.occupancy >= 12)
-    launchTraceOcc<ANY, 12>(P, grid, s);
-  else if (P.occupancy >= 10)
-    launchTraceOcc<ANY, 10>(P, grid, s);
+    k_trace<ANY, true, false, kTraceThreads, kTraceMinBlocks, kSharedStack><<<grid, kTraceThreads, 0, s>>>(P);
+  else if (P.blockThreads == 64)
+    launchTb<ANY, 64>(P, grid, s);
+  else if (P.blockThreads == 256)
+    launchTb<ANY, 256>(P, grid, s);
   else
-    launchTraceOcc<ANY, kTraceMinBlocks>(P, grid, s);
+    launchTb<ANY, 128>(P, grid, s);
+}
+template <int TB, int OCC, int SHS>
+int blocksOf() {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace<false, false, true, TB, OCC * 128 / TB, SHS>, TB, 0);
+  return n;
+}
+template <int TB, int OCC>
+int blocksOcc(int sharedStack) {
+  return sharedStack >= 32 ? blocksOf<TB, OCC, 32>()
+         : (sharedStack > 0 && sharedStack <= 16) ? blocksOf<TB, OCC, 16>() : blocksOf<TB, OCC, 24>();
+}
+template <int TB>
+int blocksTb(int occupancy, int sharedStack) {
+  return occupancy >= 12 ? blocksOcc<TB, 12>(sharedStack)
+         : occupancy >= 10 ? blocksOcc<TB, 10>(sharedStack) : blocksOcc<TB, kTraceMinBlocks>(sharedStack);
 }
 }  // namespace
 
 void launchExtend(const KParams& P, int grid, cudaStream_t s) { launchTrace<false>(P, grid, s); }
 void launchConnect(const KParams& P, int grid, cudaStream_t s) { launchTrace<true>(P, grid, s); }
-int traceBlocksPerSm(int occupancy) {
-  int n = 0;
-  if (occupancy >= 12)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace<false, false, true, 12>, kTraceThreads, 0);
-  else if (occupancy >= 10)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace<false, false, true, 10>, kTraceThreads, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace<false, false, true, kTraceMinBlocks>, kTraceThreads,
-                                                  0);
+int traceBlocksPerSm(int occupancy, int blockThreads, int sharedStack) {
+  const int n = blockThreads == 64    ? blocksTb<64>(occupancy, sharedStack)
+                : blockThreads == 256 ? blocksTb<256>(occupancy, sharedStack)
+                                      : blocksTb<128>(occupancy, sharedStack);
   return n > 0 ? n : 1;
 }
 void launchTraceQuery(const SceneDev& S, const float4* o, const float4* d, uint32_t n, int anyHit, float4* hit,

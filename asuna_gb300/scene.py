@@ -603,6 +603,12 @@ class Context:
         or on host threads (the same binned-SAH algorithm)."""
         check(lib().asuna_ctx_set_bvh_build(self.handle, 0 if on_device else 1))
 
+    def set_traversal_shape(self, threads_per_block=0, shared_stack=0):
+        """Traversal kernel variant: threads per block (64, 128, 256) and
+        stack entries in shared memory (16, 24, 32); 0 = defaults.  Results
+        do not depend on them."""
+        check(lib().asuna_ctx_set_traversal_shape(self.handle, int(threads_per_block), int(shared_stack)))
+
     def set_traversal_stack(self, entries=0):
         """Caps the traversal stack per ray (0 = the full 64 entries); a
         traversal needing more is cut short and reported as ERR_TRAVERSAL."""

@@ -374,6 +374,11 @@ int asuna_ctx_set_launch(asuna_ctx* ctx, int trace_blocks_per_sm, int shade_bloc
  * not depend on them. */
 int asuna_ctx_set_traversal(asuna_ctx* ctx, int refill_extend, int refill_shadow, int speculate_extend,
                             int speculate_shadow, int blocks_per_sm);
+/* Shape of the traversal kernel variant: threads per block (64, 128 or 256)
+ * and traversal-stack entries kept in shared memory (16, 24 or 32; the rest
+ * of the 64 in thread-local memory); 0 = 128 / 24.  Results do not depend
+ * on them. */
+int asuna_ctx_set_traversal_shape(asuna_ctx* ctx, int threads_per_block, int shared_stack_entries);
 /* Reorders the extend queue before every secondary pass by direction and
  * origin so warps carry rays that walk alike: 0 off, 1 octant x 4 x 4 x 4
  * origin cells, 2 octant x 8 x 8 x 8 cells in Morton order, 3 the same with

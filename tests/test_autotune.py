@@ -15,6 +15,7 @@ class FakeCtx:
         self.launch = None
         self.sort = None
         self.budget = None
+        self.shape = (0, 0)
         self.renders = []
 
     def set_traversal(self, *t):
@@ -26,12 +27,16 @@ class FakeCtx:
     def set_ray_sort(self, m):
         self.sort = m
 
+    def set_traversal_shape(self, threads=0, shared=0):
+        self.shape = (threads, shared)
+
     def set_path_budget(self, b):
         self.budget = b
 
     def render(self, scene, shot, film, stats=False):
         self.renders.append((shot.frame0, shot.frames))
-        mrays = self.score(shot.frames, self.launch, self.trav, self.sort)
+        mrays = self.score(shot.frames, self.launch, self.trav, self.sort) + \
+            {(0, 0): 0, (128, 32): 4, (64, 24): -2, (256, 24): 1, (128, 16): -1}[self.shape]
         rays = 1e6
         return {"extend_rays": rays, "shadow_rays": 0, "ms_total": rays / (mrays * 1e3)}
 
@@ -68,6 +73,8 @@ def test_tune_finds_the_optimum_and_restores_the_shot():
     # the extend refill is tuned again once the sort is on
     assert best["traversal"] == (24, 4, 1, 1, 10)
     assert ctx.trav == best["traversal"] and ctx.sort == 3 and ctx.launch == (0, 0)
+    # block shape and shared stack depth: 128 threads, 32 entries
+    assert best["shape"] == (128, 32) and ctx.shape == (128, 32)
     assert ctx.budget == 16 * 64 * 32 * autotune.BYTES_PER_PATH
     assert (shot.frame0, shot.frames) == (5, 3) and film.cleared == 1
     # tuning frames never overlap the caller's sample streams

@@ -78,19 +78,23 @@ def test_graph_replay_equals_direct_launches(ctx):
 
 
 def test_traversal_settings_do_not_change_results(ctx):
-    """Refill thresholds, speculative walking and the kernel variant change the
-    visiting order only: closest hits (ties to the lowest instance /
+    """Refill thresholds, speculative walking and the kernel variant
+    (occupancy, block size, shared-memory stack entries) change the visiting
+    order only: closest hits (ties to the lowest instance /
     primitive) and occlusion answers are the same, so films are
     bit-identical."""
     b, shot = scenes.plugin_scene(64, 48, frames=2, max_depth=6)
     scene = ctx.create_scene(b.desc())
     films = []
-    for trav in ((8, 8, 1, 1, 8), (1, 32, 0, 0, 10), (32, 1, 1, 0, 12), (4, 16, 0, 1, 10), (24, 8, 1, 1, 10)):
+    for trav, shape in (((8, 8, 1, 1, 8), (0, 0)), ((1, 32, 0, 0, 10), (64, 16)), ((32, 1, 1, 0, 12), (256, 32)),
+                        ((4, 16, 0, 1, 10), (128, 32)), ((24, 8, 1, 1, 10), (64, 32)), ((24, 8, 1, 1, 12), (256, 16))):
         ctx.set_traversal(*trav)
+        ctx.set_traversal_shape(*shape)
         f = ctx.create_film(64, 48)
         ctx.render(scene, shot, f)
         films.append(np.stack([f.read(i) for i in range(9)]))
     ctx.set_traversal()
+    ctx.set_traversal_shape()
     for f in films[1:]:
         assert np.array_equal(films[0], f)
 
