@@ -1,18 +1,28 @@
 // server.cpp — continuous-batching render server.
 //
-// Requests (a resident scene + a shot: camera, resolution, spp) arrive at any
-// time.  `slots` worker threads each own a context (CUDA stream + wavefront
+// Requests (a scene + a shot: camera, resolution, spp) arrive at any time.
+// `slots` worker threads each own a context (CUDA stream + wavefront
 // buffers), so the work of several requests overlaps on the device.  A slot
 // keeps an active set of requests on the same scene and renders them as one
 // multi-shot wavefront per chunk of frames; after each chunk, finished
 // requests leave the set and pending requests of that scene join it (as long
 // as the memory budget admits their films), so new work enters as soon as
 // slots and memory free up.  Requests whose footprint can never fit, or that
-// arrive while the pending queue is full, are rejected.  Scene BVHs stay
-// resident on the device for the lifetime of the server.
+// arrive while the pending queue is full, are rejected.
 //
-// Each path's sample stream depends only on (pixel, frame, shot seed), so a
-// request renders the same film alone or in any mix (tested).
+// Scenes: added ones are built at once and stay resident; registered ones
+// are built by the worker that admits their first request (charged to the
+// budget with an estimate until the build reports its size) and dropped,
+// least recently used first, when an admission needs memory and no request
+// uses them.
+//
+// Denoised requests render the two halves of their frames into two films;
+// when both are done the slot's denoiser blends the denoise of all samples
+// with their plain average (asuna_denoise_blended) into the result image.
+//
+// Each path's sample stream depends only on (pixel, frame, shot seed) and
+// the denoiser is deterministic, so a request renders the same result alone
+// or in any mix (tested).
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -25,6 +35,9 @@
 #include <unordered_map>
 #include <vector>
 
+#include <cuda_runtime.h>
+
+#include "../../include/asuna_denoise.h"
 #include "../../include/asuna_rt.h"
 #include "common.h"
 
@@ -35,13 +48,30 @@ using Clock = std::chrono::steady_clock;
 struct Req {
   uint64_t id = 0;
   uint32_t scene = 0;
+  uint32_t flags = 0;
   asuna_shot shot{};
   double arrival = 0, start = -1, finish = -1;
-  uint32_t done = 0;  // frames rendered
+  uint32_t frames[2] = {0, 0};  // frames of each part (a denoised request has two)
+  uint32_t done[2] = {0, 0};    // frames rendered per part
   int status = ASUNA_OK;
-  uint64_t filmBytes = 0;
-  asuna_film* film = nullptr;
+  bool charged = false;  // admitted: `bytes` are counted in the server's memory
+  uint64_t bytes = 0;    // films + denoised image
+  asuna_film* film[2] = {nullptr, nullptr};
+  float* denoised = nullptr;  // device RGBA, denoised requests
   asuna_ctx* filmCtx = nullptr;
+  bool denoise() const { return (flags & ASUNA_REQUEST_DENOISE) != 0; }
+  int parts() const { return denoise() ? 2 : 1; }
+  bool complete() const { return done[0] >= frames[0] && done[1] >= frames[1]; }
+};
+
+struct SceneEntry {
+  const asuna_scene_desc* desc = nullptr;  // registered: built on demand
+  asuna_scene* dev = nullptr;
+  uint64_t bytes = 0;     // charged to the budget (the estimate while building)
+  uint64_t estimate = 0;
+  int users = 0;          // admitted requests not yet finished
+  bool building = false;
+  double lastUse = 0;
 };
 
 }  // namespace
@@ -54,38 +84,99 @@ struct asuna_server {
   std::deque<std::shared_ptr<Req>> pending;
   std::vector<std::shared_ptr<Req>> finished;  // not yet polled
   std::unordered_map<uint64_t, std::shared_ptr<Req>> byId;
-  std::vector<asuna_scene*> scenes;
-  std::vector<uint64_t> sceneBytes;
+  std::deque<SceneEntry> scenes;  // (a deque: entries keep their addresses as scenes are added)
   std::vector<asuna_ctx*> ctxs;
+  std::vector<asuna_denoiser*> denoisers;  // one per slot, or none
   std::vector<std::thread> workers;
   uint64_t memUsed = 0;  // films held + scenes
   uint64_t nextId = 1;
   int inFlight = 0;
   bool stop = false;
-  uint64_t rejected = 0, admitted = 0, samples = 0;
+  uint64_t rejected = 0, admitted = 0, samples = 0, built = 0, evicted = 0, denoised = 0;
 
   double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 };
 
 namespace {
 
-uint64_t filmFootprint(const asuna_shot& s) { return uint64_t(s.width) * s.height * 16ull * 9ull; }
+uint64_t filmBytes(const asuna_shot& s) { return uint64_t(s.width) * s.height * 16ull * 9ull; }
+
+uint64_t requestBytes(const asuna_shot& s, bool denoise) {
+  return denoise ? 2 * filmBytes(s) + uint64_t(s.width) * s.height * 16ull : filmBytes(s);
+}
+
+// Device bytes a scene will take: nodes (about one 64-byte node per
+// triangle at most), leaf triangles, shading vertices and indices,
+// instances, materials, lights, the environment map and its tables,
+// textures.
+uint64_t sceneEstimate(const asuna_scene_desc* d) {
+  uint64_t tris = 0, verts = 0, texels = 0;
+  for (uint32_t m = 0; m < d->num_meshes; ++m) {
+    tris += d->meshes[m].num_triangles;
+    verts += d->meshes[m].num_vertices;
+  }
+  for (uint32_t t = 0; t < d->num_textures; ++t) texels += uint64_t(d->textures[t].width) * d->textures[t].height;
+  const uint64_t env = d->envmap.rgba ? uint64_t(d->envmap.width) * d->envmap.height * 32 : 32;
+  return tris * (64 + 48 + 16) + verts * 32 + uint64_t(d->num_instances) * (128 + 128) +
+         uint64_t(d->num_materials) * 96 + uint64_t(d->num_lights) * 80 + env + texels * 16 + (1u << 20);
+}
+
+// Drops idle registered scenes, least recently used first, until `need`
+// more bytes fit or none is left to drop (caller holds the lock; returns
+// the scenes to destroy outside it).
+void evictFor(asuna_server* S, uint64_t need, uint32_t keep, std::vector<asuna_scene*>& drop) {
+  while (S->memUsed + need > S->opts.memory_budget) {
+    int victim = -1;
+    for (size_t i = 0; i < S->scenes.size(); ++i) {
+      const SceneEntry& e = S->scenes[i];
+      if (i == keep || !e.desc || !e.dev || e.building || e.users > 0) continue;
+      if (victim < 0 || e.lastUse < S->scenes[size_t(victim)].lastUse) victim = int(i);
+    }
+    if (victim < 0) return;
+    SceneEntry& e = S->scenes[size_t(victim)];
+    S->memUsed -= e.bytes;
+    drop.push_back(e.dev);
+    e.dev = nullptr;
+    e.bytes = 0;
+    S->evicted++;
+  }
+}
 
 // Takes pending requests of `scene` (any scene if scene < 0) that the memory
-// budget admits, up to `room`, oldest first.  Caller holds the lock.
-void admit(asuna_server* S, int scene, size_t room, std::vector<std::shared_ptr<Req>>& out) {
+// budget admits, up to `room`, oldest first.  A request whose registered
+// scene is not resident also needs the scene's estimate (its builder is
+// whoever admits it: `*build` receives the scene).  Caller holds the lock.
+void admit(asuna_server* S, int scene, size_t room, std::vector<std::shared_ptr<Req>>& out, int* build,
+           std::vector<asuna_scene*>& drop) {
   for (auto it = S->pending.begin(); it != S->pending.end() && room > 0;) {
     auto& r = *it;
     if (scene >= 0 && int(r->scene) != scene) {
       ++it;
       continue;
     }
-    if (S->memUsed + r->filmBytes > S->opts.memory_budget) {
+    SceneEntry& e = S->scenes[r->scene];
+    if (e.building) {  // another slot is building it: wait
+      if (scene < 0) break;
+      ++it;
+      continue;
+    }
+    const bool needBuild = !e.dev;
+    const uint64_t need = r->bytes + (needBuild ? e.estimate : 0);
+    if (S->memUsed + need > S->opts.memory_budget) evictFor(S, need, r->scene, drop);
+    if (S->memUsed + need > S->opts.memory_budget) {
       if (scene < 0) break;  // keep arrival order for new sets
       ++it;
       continue;
     }
-    S->memUsed += r->filmBytes;
+    if (needBuild) {
+      e.building = true;
+      e.bytes = e.estimate;
+      *build = int(r->scene);
+    }
+    S->memUsed += need;
+    r->charged = true;
+    e.users++;
+    e.lastUse = S->now();
     r->start = S->now();
     out.push_back(r);
     if (scene < 0) scene = int(r->scene);
@@ -94,18 +185,36 @@ void admit(asuna_server* S, int scene, size_t room, std::vector<std::shared_ptr<
   }
 }
 
+// Film images of the guides a denoised request needs (albedo, normal).
+bool guideImages(const asuna_shot& s, int* albedo, int* normal) {
+  *albedo = s.state.diffuse_out_channel >= 0 ? 1 + s.state.diffuse_out_channel : -1;
+  *normal = s.state.normal_out_channel >= 0 ? 1 + s.state.normal_out_channel : -1;
+  return *albedo > 0 && *normal > 0;
+}
+
+void finishRequest(asuna_server* S, const std::shared_ptr<Req>& r, double t) {
+  r->finish = t;
+  SceneEntry& e = S->scenes[r->scene];
+  e.users--;
+  e.lastUse = t;
+  S->finished.push_back(r);
+}
+
 void worker(asuna_server* S, int slot) {
   asuna_ctx* ctx = S->ctxs[slot];
   std::vector<std::shared_ptr<Req>> active;
   const size_t maxSet = std::max(1u, S->opts.max_batch);
   for (;;) {
+    int build = -1;
+    const asuna_scene_desc* buildDesc = nullptr;
+    std::vector<asuna_scene*> drop;
     {
       std::unique_lock<std::mutex> lk(S->mu);
       if (S->stop && !active.empty()) {
         // shutting down: abandon the active set
         for (auto& r : active) {
           r->status = ASUNA_ERR_TIMEOUT;
-          r->finish = S->now();
+          finishRequest(S, r, S->now());
         }
         active.clear();
         S->inFlight--;
@@ -114,62 +223,116 @@ void worker(asuna_server* S, int slot) {
       if (active.empty()) {
         S->cv.wait(lk, [&] { return S->stop || !S->pending.empty(); });
         if (S->stop && S->pending.empty()) return;
-        admit(S, -1, maxSet, active);
+        admit(S, -1, maxSet, active, &build, drop);
         if (active.empty()) {
+          lk.unlock();
+          for (auto* sc : drop) asuna_scene_destroy(sc);
+          lk.lock();
           // nothing fits right now: wait for memory to be released
           S->cv.wait_for(lk, std::chrono::milliseconds(2));
           continue;
         }
         S->inFlight++;
       } else {
-        admit(S, int(active[0]->scene), maxSet - active.size(), active);
+        admit(S, int(active[0]->scene), maxSet - active.size(), active, &build, drop);
+      }
+      if (build >= 0) buildDesc = S->scenes[size_t(build)].desc;
+    }
+    for (auto* sc : drop) asuna_scene_destroy(sc);
+    const uint32_t sid = active[0]->scene;
+    if (build >= 0) {
+      // the scene's device build, at admission of its first request
+      asuna_scene* dev = nullptr;
+      int rc = asuna_scene_create(ctx, buildDesc, &dev);
+      asuna_scene_stats st{};
+      if (rc == ASUNA_OK) asuna_scene_get_stats(dev, &st);
+      std::lock_guard<std::mutex> lk(S->mu);
+      SceneEntry& e = S->scenes[size_t(build)];
+      S->memUsed -= e.bytes;
+      e.building = false;
+      if (rc == ASUNA_OK) {
+        e.dev = dev;
+        e.bytes = st.device_bytes;
+        S->memUsed += e.bytes;
+        S->built++;
+      } else {
+        e.bytes = 0;
+        for (auto& r : active)
+          if (r->status == ASUNA_OK) r->status = rc;
       }
     }
     // films for newly admitted requests
     for (auto& r : active) {
-      if (r->film) continue;
-      if (asuna_film_create(ctx, r->shot.width, r->shot.height, &r->film) != ASUNA_OK) {
+      if (r->status != ASUNA_OK || r->film[0]) continue;
+      for (int k = 0; k < r->parts() && r->status == ASUNA_OK; ++k)
+        if (asuna_film_create(ctx, r->shot.width, r->shot.height, &r->film[k]) != ASUNA_OK) r->status = ASUNA_ERR_OOM;
+      if (r->status == ASUNA_OK && r->denoise() &&
+          cudaMalloc(reinterpret_cast<void**>(&r->denoised), size_t(r->shot.width) * r->shot.height * 16) !=
+              cudaSuccess) {
+        cudaGetLastError();
         r->status = ASUNA_ERR_OOM;
-        r->done = r->shot.frames;
       }
       r->filmCtx = ctx;
     }
-    // one chunk: every active request advances by up to frames_per_chunk frames
+    // one chunk: every active request (part) advances by up to frames_per_chunk frames
     std::vector<asuna_shot> shots;
     std::vector<asuna_film*> films;
-    std::vector<Req*> owners;
+    std::vector<std::pair<Req*, int>> owners;
     for (auto& r : active) {
-      if (r->status != ASUNA_OK || r->done >= r->shot.frames) continue;
-      asuna_shot s = r->shot;
-      s.frame0 = r->shot.frame0 + r->done;
-      s.frames = std::min(S->opts.frames_per_chunk, r->shot.frames - r->done);
-      shots.push_back(s);
-      films.push_back(r->film);
-      owners.push_back(r.get());
+      if (r->status != ASUNA_OK) continue;
+      for (int k = 0; k < r->parts(); ++k) {
+        if (r->done[k] >= r->frames[k]) continue;
+        asuna_shot s = r->shot;
+        s.frame0 = r->shot.frame0 + (k ? r->frames[0] : 0) + r->done[k];
+        s.frames = std::min(S->opts.frames_per_chunk, r->frames[k] - r->done[k]);
+        shots.push_back(s);
+        films.push_back(r->film[k]);
+        owners.push_back({r.get(), k});
+      }
     }
     int rc = ASUNA_OK;
     if (!shots.empty()) {
-      rc = asuna_render_batch(ctx, S->scenes[active[0]->scene], shots.data(), films.data(), uint32_t(shots.size()),
-                              nullptr);
+      asuna_scene* dev = nullptr;
+      {
+        std::lock_guard<std::mutex> lk(S->mu);
+        dev = S->scenes[sid].dev;
+      }
+      rc = dev ? asuna_render_batch(ctx, dev, shots.data(), films.data(), uint32_t(shots.size()), nullptr)
+               : ASUNA_ERR_INVALID;
       if (rc == ASUNA_OK) rc = asuna_ctx_sync(ctx);
+    }
+    for (size_t k = 0; k < owners.size(); ++k) {
+      Req* r = owners[k].first;
+      if (rc != ASUNA_OK)
+        r->status = rc;
+      else
+        r->done[owners[k].second] += shots[k].frames;
+    }
+    // denoise the requests whose halves are both rendered
+    uint64_t denoisedNow = 0;
+    for (auto& r : active) {
+      if (r->status != ASUNA_OK || !r->denoise() || !r->complete() || r->finish >= 0) continue;
+      int albedo, normal;
+      guideImages(r->shot, &albedo, &normal);
+      double err = 0, errPlain = 0, w = 0;
+      asuna_denoiser* d = S->denoisers.empty() ? nullptr : S->denoisers[slot];
+      int drc = d ? asuna_denoise_blended(ctx, d, r->film[0], r->film[1], albedo, normal, r->denoised, &err,
+                                          &errPlain, &w)
+                  : ASUNA_ERR_INVALID;
+      if (drc == ASUNA_OK) drc = asuna_ctx_sync(ctx);
+      if (drc != ASUNA_OK) r->status = drc;
+      else ++denoisedNow;
     }
     {
       std::lock_guard<std::mutex> lk(S->mu);
       const double t = S->now();
-      for (size_t k = 0; k < owners.size(); ++k) {
-        if (rc != ASUNA_OK) {
-          owners[k]->status = rc;
-          owners[k]->done = owners[k]->shot.frames;
-        } else {
-          owners[k]->done += shots[k].frames;
-          S->samples += uint64_t(shots[k].frames) * shots[k].width * shots[k].height;
-        }
-      }
+      S->denoised += denoisedNow;
+      for (size_t k = 0; k < owners.size(); ++k)
+        if (rc == ASUNA_OK) S->samples += uint64_t(shots[k].frames) * shots[k].width * shots[k].height;
       for (auto it = active.begin(); it != active.end();) {
         auto& r = *it;
-        if (r->done >= r->shot.frames) {
-          r->finish = t;
-          S->finished.push_back(r);
+        if (r->status != ASUNA_OK || r->complete()) {
+          finishRequest(S, r, t);
           it = active.erase(it);
         } else {
           ++it;
@@ -179,6 +342,48 @@ void worker(asuna_server* S, int slot) {
     }
     S->cv.notify_all();
   }
+}
+
+void freeRequest(Req& r) {
+  for (auto*& f : r.film) {
+    if (f) asuna_film_destroy(f);
+    f = nullptr;
+  }
+  if (r.denoised) cudaFree(r.denoised);
+  r.denoised = nullptr;
+}
+
+int addScene(asuna_server* S, const asuna_scene_desc* desc, bool registerOnly, uint32_t* scene_id) {
+  asuna::clearError();
+  if (!S || !desc || !scene_id) return asuna::fail(ASUNA_ERR_INVALID, "null argument");
+  SceneEntry e;
+  if (registerOnly) {
+    int rc = asuna_scene_validate(desc);
+    if (rc) return rc;
+    e.desc = desc;
+    e.estimate = sceneEstimate(desc);
+    if (e.estimate > S->opts.memory_budget)
+      return asuna::fail(ASUNA_ERR_OOM, "scene of about %llu bytes exceeds the server memory budget",
+                         (unsigned long long)e.estimate);
+  } else {
+    int rc = asuna_scene_create(S->ctxs[0], desc, &e.dev);
+    if (rc) return rc;
+    asuna_scene_stats st;
+    asuna_scene_get_stats(e.dev, &st);
+    e.bytes = st.device_bytes;
+  }
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (!registerOnly) {
+    if (S->memUsed + e.bytes > S->opts.memory_budget) {
+      asuna_scene_destroy(e.dev);
+      return asuna::fail(ASUNA_ERR_OOM, "scene of %llu bytes exceeds the server memory budget",
+                         (unsigned long long)e.bytes);
+    }
+    S->memUsed += e.bytes;
+  }
+  S->scenes.push_back(e);
+  *scene_id = uint32_t(S->scenes.size() - 1);
+  return ASUNA_OK;
 }
 
 }  // namespace
@@ -214,23 +419,34 @@ int asuna_server_create(const asuna_server_opts* opts, asuna_server** out) {
 }
 
 int asuna_server_add_scene(asuna_server* S, const asuna_scene_desc* desc, uint32_t* scene_id) {
+  return addScene(S, desc, false, scene_id);
+}
+
+int asuna_server_register_scene(asuna_server* S, const asuna_scene_desc* desc, uint32_t* scene_id) {
+  return addScene(S, desc, true, scene_id);
+}
+
+int asuna_server_set_denoiser(asuna_server* S, const asuna_denoiser_opts* opts, const float* params, uint64_t n) {
   asuna::clearError();
-  if (!S || !desc || !scene_id) return asuna::fail(ASUNA_ERR_INVALID, "null argument");
-  asuna_scene* sc = nullptr;
-  int rc = asuna_scene_create(S->ctxs[0], desc, &sc);
-  if (rc) return rc;
-  asuna_scene_stats st;
-  asuna_scene_get_stats(sc, &st);
-  std::lock_guard<std::mutex> lk(S->mu);
-  if (S->memUsed + st.device_bytes > S->opts.memory_budget) {
-    asuna_scene_destroy(sc);
-    return asuna::fail(ASUNA_ERR_OOM, "scene of %llu bytes exceeds the server memory budget",
-                       (unsigned long long)st.device_bytes);
+  if (!S || !opts || !params) return asuna::fail(ASUNA_ERR_INVALID, "asuna_server_set_denoiser: null argument");
+  std::vector<asuna_denoiser*> ds;
+  for (asuna_ctx* c : S->ctxs) {
+    asuna_denoiser* d = nullptr;
+    int rc = asuna_denoiser_create(c, opts, &d);
+    if (rc == ASUNA_OK) rc = asuna_denoiser_set_params(d, params, n);
+    if (rc != ASUNA_OK) {
+      if (d) asuna_denoiser_destroy(d);
+      for (auto* x : ds) asuna_denoiser_destroy(x);
+      return rc;
+    }
+    ds.push_back(d);
   }
-  S->memUsed += st.device_bytes;
-  S->scenes.push_back(sc);
-  S->sceneBytes.push_back(st.device_bytes);
-  *scene_id = uint32_t(S->scenes.size() - 1);
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (!S->denoisers.empty() || S->inFlight > 0) {
+    for (auto* x : ds) asuna_denoiser_destroy(x);
+    return asuna::fail(ASUNA_ERR_INVALID, "set the denoiser once, before submitting requests");
+  }
+  S->denoisers = ds;
   return ASUNA_OK;
 }
 
@@ -239,8 +455,12 @@ int asuna_server_submit(asuna_server* S, const asuna_request* req, uint64_t* id)
   if (!S || !req || !id) return asuna::fail(ASUNA_ERR_INVALID, "null argument");
   auto r = std::make_shared<Req>();
   r->scene = req->scene;
+  r->flags = req->flags;
   r->shot = req->shot;
-  r->filmBytes = filmFootprint(req->shot);
+  r->frames[0] = r->denoise() ? (req->shot.frames + 1) / 2 : req->shot.frames;
+  r->frames[1] = r->denoise() ? req->shot.frames - r->frames[0] : 0;
+  r->bytes = requestBytes(req->shot, r->denoise());
+  int albedo, normal;
   std::lock_guard<std::mutex> lk(S->mu);
   r->id = S->nextId++;
   r->arrival = S->now();
@@ -252,7 +472,9 @@ int asuna_server_submit(asuna_server* S, const asuna_request* req, uint64_t* id)
   else if (req->shot.width == 0 || req->shot.height == 0 || req->shot.frames == 0 ||
            req->shot.state.max_path_depth < 1 || req->shot.state.max_path_depth > 32)
     reason = ASUNA_ERR_INVALID;
-  else if (r->filmBytes > S->opts.memory_budget)
+  else if (r->denoise() && (S->denoisers.empty() || req->shot.frames < 2 || !guideImages(req->shot, &albedo, &normal)))
+    reason = ASUNA_ERR_INVALID;  // no denoiser, fewer than two frames or no albedo / normal channel
+  else if (r->bytes + (S->scenes[req->scene].dev ? 0 : S->scenes[req->scene].estimate) > S->opts.memory_budget)
     reason = ASUNA_ERR_OOM;  // can never be admitted
   else if (S->pending.size() >= S->opts.max_queue)
     reason = ASUNA_ERR_BUSY;
@@ -298,10 +520,16 @@ int asuna_server_read(asuna_server* S, uint64_t id, int image, float* host_rgba)
     if (it == S->byId.end()) return asuna::fail(ASUNA_ERR_INVALID, "unknown request %llu", (unsigned long long)id);
     r = it->second;
   }
-  if (r->status != ASUNA_OK || !r->film) return asuna::fail(ASUNA_ERR_INVALID, "request %llu has no film",
-                                                            (unsigned long long)id);
+  if (r->status != ASUNA_OK || !r->film[0])
+    return asuna::fail(ASUNA_ERR_INVALID, "request %llu has no film", (unsigned long long)id);
   if (r->finish < 0) return asuna::fail(ASUNA_ERR_INVALID, "request %llu is not finished", (unsigned long long)id);
-  return asuna_film_read(r->filmCtx, r->film, image, host_rgba);
+  if (image == 0 && r->denoised) {
+    if (!host_rgba) return asuna::fail(ASUNA_ERR_INVALID, "null output");
+    ASUNA_CUDA_TRY(cudaMemcpy(host_rgba, r->denoised, size_t(r->shot.width) * r->shot.height * 16,
+                              cudaMemcpyDeviceToHost));
+    return ASUNA_OK;
+  }
+  return asuna_film_read(r->filmCtx, r->film[0], image, host_rgba);
 }
 
 int asuna_server_release(asuna_server* S, uint64_t id) {
@@ -314,10 +542,10 @@ int asuna_server_release(asuna_server* S, uint64_t id) {
     r = it->second;
     if (r->finish < 0) return asuna::fail(ASUNA_ERR_INVALID, "request %llu is not finished", (unsigned long long)id);
     S->byId.erase(it);
-    if (r->film) S->memUsed -= r->filmBytes;
+    if (r->charged) S->memUsed -= r->bytes;
+    r->charged = false;
   }
-  if (r->film) asuna_film_destroy(r->film);
-  r->film = nullptr;
+  freeRequest(*r);
   S->cv.notify_all();
   return ASUNA_OK;
 }
@@ -333,12 +561,18 @@ int asuna_server_drain(asuna_server* S, double timeout_s) {
 int asuna_server_get_stats(asuna_server* S, asuna_server_stats* out) {
   if (!S || !out) return asuna::fail(ASUNA_ERR_INVALID, "null argument");
   std::lock_guard<std::mutex> lk(S->mu);
+  std::memset(out, 0, sizeof(*out));
   out->admitted = S->admitted;
   out->rejected = S->rejected;
   out->pending = S->pending.size();
   out->samples = S->samples;
   out->memory_used = S->memUsed;
   out->elapsed_s = S->now();
+  out->scenes_built = S->built;
+  out->scenes_evicted = S->evicted;
+  out->denoised = S->denoised;
+  for (const SceneEntry& e : S->scenes)
+    if (e.dev) out->scene_bytes += e.bytes;
   return ASUNA_OK;
 }
 
@@ -351,9 +585,10 @@ int asuna_server_destroy(asuna_server* S) {
   }
   S->cv.notify_all();
   for (auto& t : S->workers) t.join();
-  for (auto& kv : S->byId)
-    if (kv.second->film) asuna_film_destroy(kv.second->film);
-  for (auto* sc : S->scenes) asuna_scene_destroy(sc);
+  for (auto& kv : S->byId) freeRequest(*kv.second);
+  for (auto* d : S->denoisers) asuna_denoiser_destroy(d);
+  for (auto& e : S->scenes)
+    if (e.dev) asuna_scene_destroy(e.dev);
   for (auto* c : S->ctxs) asuna_ctx_destroy(c);
   delete S;
   return ASUNA_OK;

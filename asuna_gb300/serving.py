@@ -19,8 +19,11 @@ class ServerOpts(C.Structure):
                 ("memory_budget", C.c_uint64), ("path_budget", C.c_uint64)]
 
 
+REQUEST_DENOISE = 1
+
+
 class Request(C.Structure):
-    _fields_ = [("scene", C.c_uint32), ("reserved", C.c_uint32), ("shot", A.Shot)]
+    _fields_ = [("scene", C.c_uint32), ("flags", C.c_uint32), ("shot", A.Shot)]
 
 
 class RequestResult(C.Structure):
@@ -30,12 +33,16 @@ class RequestResult(C.Structure):
 
 class ServerStats(C.Structure):
     _fields_ = [("admitted", C.c_uint64), ("rejected", C.c_uint64), ("pending", C.c_uint64),
-                ("samples", C.c_uint64), ("memory_used", C.c_uint64), ("elapsed_s", C.c_double)]
+                ("samples", C.c_uint64), ("memory_used", C.c_uint64), ("elapsed_s", C.c_double),
+                ("scenes_built", C.c_uint64), ("scenes_evicted", C.c_uint64), ("denoised", C.c_uint64),
+                ("scene_bytes", C.c_uint64)]
 
 
 _SIGS = [
     ("asuna_server_create", [C.POINTER(ServerOpts), C.POINTER(C.c_void_p)]),
     ("asuna_server_add_scene", [C.c_void_p, C.POINTER(A.SceneDesc), C.POINTER(C.c_uint32)]),
+    ("asuna_server_register_scene", [C.c_void_p, C.POINTER(A.SceneDesc), C.POINTER(C.c_uint32)]),
+    ("asuna_server_set_denoiser", [C.c_void_p, C.POINTER(A.DenoiserOpts), C.c_void_p, C.c_uint64]),
     ("asuna_server_submit", [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_uint64)]),
     ("asuna_server_poll", [C.c_void_p, C.POINTER(RequestResult), C.c_uint32, C.POINTER(C.c_uint32)]),
     ("asuna_server_read", [C.c_void_p, C.c_uint64, C.c_int, C.c_void_p]),
@@ -60,17 +67,38 @@ class Server:
                  path_budget=0):
         self.L = _bind()
         o = ServerOpts(device, slots, frames_per_chunk, max_batch, max_queue, 0, memory_budget, path_budget)
+        self._keep = []
         h = C.c_void_p()
         check(self.L.asuna_server_create(C.byref(o), C.byref(h)))
         self.h = h
 
     def add_scene(self, desc):
+        """Builds the scene now; it stays resident."""
         sid = C.c_uint32()
         check(self.L.asuna_server_add_scene(self.h, desc.ptr, C.byref(sid)))
         return sid.value
 
-    def submit(self, scene, shot):
-        r = Request(scene, 0, shot)
+    def register_scene(self, desc):
+        """Registers a scene the server builds when its first request is
+        admitted and may drop when idle (keep `desc` alive)."""
+        sid = C.c_uint32()
+        check(self.L.asuna_server_register_scene(self.h, desc.ptr, C.byref(sid)))
+        self._keep.append(desc)
+        return sid.value
+
+    def set_denoiser(self, params, max_pixels=1088 * 1920, channels=(32, 48, 64, 96, 128)):
+        """Trained denoiser parameters (Denoiser.get_params) for denoised requests."""
+        o = A.DenoiserOpts()
+        o.levels = len(channels)
+        for k, c in enumerate(channels):
+            o.channels[k] = c
+        o.max_pixels = max_pixels
+        o.tensor_memory = 1
+        p = np.ascontiguousarray(params, np.float32)
+        check(self.L.asuna_server_set_denoiser(self.h, C.byref(o), p.ctypes.data, p.size))
+
+    def submit(self, scene, shot, denoise=False):
+        r = Request(scene, REQUEST_DENOISE if denoise else 0, shot)
         rid = C.c_uint64()
         check(self.L.asuna_server_submit(self.h, C.byref(r), C.byref(rid)))
         return rid.value
@@ -105,11 +133,12 @@ class Server:
     __del__ = close
 
 
-def poisson_load(server, requests, rate_hz, seed=0, keep=None, timeout_s=1800.0):
+def poisson_load(server, requests, rate_hz, seed=0, keep=None, timeout_s=1800.0, denoise=None):
     """Submits (scene, shot) pairs at Poisson arrival times (rate_hz per second
-    of wall-clock time), collects every result, releases films (except ids
-    listed in `keep` by request index, whose films are read first) and
-    returns a summary with latency percentiles."""
+    of wall-clock time; `denoise[k]` sets request k's denoise flag), collects
+    every result, releases films as they finish (except requests listed in
+    `keep` by index, whose image 0 is read first) and returns a summary with
+    latency percentiles."""
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate_hz, size=len(requests))
     t0 = time.perf_counter()
@@ -117,26 +146,28 @@ def poisson_load(server, requests, rate_hz, seed=0, keep=None, timeout_s=1800.0)
     ids, results, kept = [], {}, {}
     keep = set(keep or [])
     idx_of = {}
+    def collect():
+        # finished requests: read what is kept, release every film at once
+        for r in server.poll():
+            results[r["id"]] = r
+            if r["status"] == A.OK:
+                k = idx_of[r["id"]]
+                if k in keep:
+                    shot = requests[k][1]
+                    kept[k] = server.read(r["id"], shot.width, shot.height, 0)
+            server.release(r["id"])
+
     for k, (scene, shot) in enumerate(requests):
         while time.perf_counter() < due[k]:
-            for r in server.poll():
-                results[r["id"]] = r
+            collect()
             time.sleep(min(0.002, max(0.0, due[k] - time.perf_counter())))
-        rid = server.submit(scene, shot)
+        rid = server.submit(scene, shot, denoise=bool(denoise[k]) if denoise is not None else False)
         ids.append(rid)
         idx_of[rid] = k
     deadline = time.perf_counter() + timeout_s
     while len(results) < len(ids) and time.perf_counter() < deadline:
-        for r in server.poll():
-            results[r["id"]] = r
+        collect()
         time.sleep(0.002)
-    for rid, r in results.items():
-        if r["status"] == A.OK:
-            k = idx_of[rid]
-            if k in keep:
-                shot = requests[k][1]
-                kept[k] = server.read(rid, shot.width, shot.height, 0)
-            server.release(rid)
     ok = [r for r in results.values() if r["status"] == A.OK]
     lat = np.array([r["finish_s"] - r["arrival_s"] for r in ok]) if ok else np.zeros(1)
     wait = np.array([r["start_s"] - r["arrival_s"] for r in ok]) if ok else np.zeros(1)

@@ -635,16 +635,24 @@ def run_denoise_forward(args):
     return 0
 
 
-SERVE_SCENES = [(4, 7), (16, 6), (16, 7), (24, 7), (32, 7), (48, 7), (64, 6), (64, 7)]  # (spheres, level): 1.3M-21M triangles
+SERVE_CATALOG = [(4, 7), (8, 6), (8, 7), (16, 6), (16, 7), (24, 7), (32, 6), (32, 7), (48, 7), (64, 6), (64, 7),
+                 (12, 7)]  # (spheres, level): 0.33M-21M triangles
 
 
 def run_serve(args):
     """Serving loop: requests arrive as a Poisson process (wall clock) at
-    --serve-rate per second; each picks a resident scene of the mixed recipe
-    (4-64 spheres, 1.3-21M triangles), a resolution from {512x512, 1280x720,
-    1920x1080} and a sample count from {4, 16, 64}, with a seeded camera.
-    Reports latency percentiles (arrival to finish), Msamples/s and the
-    rejection / queueing rates under the 150 GB admission budget."""
+    --serve-rate per second; each names a scene of a catalog of the mixed
+    recipe (4-64 spheres, 0.33-21M triangles) registered with the server,
+    which builds a scene on the device when its first request is admitted
+    (charged to the 150 GB budget; idle scenes are dropped when an admission
+    needs the room), a resolution from {512x512, 1280x720, 1920x1080}, a
+    sample count from {4, 16, 64}, a seeded camera and, for a quarter of them,
+    the denoise flag (two half renders blended with their denoise).  The
+    denoiser's weights are its initialisation: request latency does not
+    depend on their values.  Reports latency percentiles (arrival to
+    finish), Msamples/s, the rejection and queueing rates and the scene
+    builds."""
+    from asuna_gb300 import denoise as dn
     from asuna_gb300 import scenes
     from asuna_gb300.serving import Server, poisson_load
 
@@ -653,12 +661,18 @@ def run_serve(args):
                  max_queue=args.serve_max_queue, memory_budget=150 << 30)
     t0 = time.time()
     pool = []
-    for k, (n, lvl) in enumerate(SERVE_SCENES):
+    for k, (n, lvl) in enumerate(SERVE_CATALOG):
         b, _ = scenes.mixed_scene(64, 64, frames=1, n_spheres=n, level=lvl, seed=3000 + k)
-        pool.append((srv.add_scene(b.desc()), b, n * 20 * 4 ** lvl))
-    build_s = time.time() - t0
+        pool.append((srv.register_scene(b.desc()), b, n * 20 * 4 ** lvl))
+    gen_s = time.time() - t0
+    import asuna_gb300 as ag
+
+    ctx = ag.Context(0)
+    net = dn.Denoiser(ctx, seed=0, max_pixels=1088 * 1920)
+    srv.set_denoiser(net.get_params(), max_pixels=1088 * 1920)
+    net.close()
     res = [(512, 512), (1280, 720), (1920, 1080)]
-    reqs = []
+    reqs, flags = [], []
     for i in range(args.serve_requests):
         sid, b, _ = pool[int(rng.integers(len(pool)))]
         w, h = res[int(rng.integers(3))]
@@ -666,19 +680,21 @@ def run_serve(args):
         ang = float(rng.uniform(0, 2 * np.pi))
         eye = (30.0 * np.sin(ang), float(rng.uniform(0.0, 10.0)), 30.0 * np.cos(ang))
         reqs.append((sid, scenes.mixed_shot(b, w, h, spp, eye=eye, seed=i)))
-    out = poisson_load(srv, reqs, rate_hz=args.serve_rate, seed=11)
+        flags.append(bool(rng.random() < args.serve_denoise_frac))
+    out = poisson_load(srv, reqs, rate_hz=args.serve_rate, seed=11, denoise=flags)
     st = srv.stats()
     srv.close()
     out.pop("films")
     line = {"metric": "serving latency p99 (s)", "value": out["p99_s"], "unit": "s", "higher_is_better": False,
             "n_gpus": 1, "data": "synthetic (seeded procedural scenes)",
             "config": {"workload": f"Poisson {args.serve_rate} req/s, {args.serve_requests} requests, "
-                                   f"{len(pool)} resident scenes of 1.3-21M triangles, "
-                                   "512^2 / 1280x720 / 1920x1080, 4 / 16 / 64 spp, depth 12",
+                                   f"{len(pool)} registered scenes of 0.33-21M triangles built at admission, "
+                                   "512^2 / 1280x720 / 1920x1080, 4 / 16 / 64 spp, depth 12, "
+                                   f"{args.serve_denoise_frac:.0%} denoised",
                        "slots": args.serve_slots, "frames_per_chunk": args.serve_chunk,
                        "max_queue": args.serve_max_queue, "memory_budget_gb": 150,
-                       "scene_triangles": [p[2] for p in pool], "scene_build_s": build_s},
-            **out, "server_stats": st}
+                       "scene_triangles": [p[2] for p in pool], "scene_generation_s": gen_s},
+            **out, "denoised_requests": int(sum(flags)), "server_stats": st}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -790,7 +806,8 @@ def main():
     ap.add_argument("--serve", action="store_true", help="serving loop: Poisson arrivals, latency percentiles")
     ap.add_argument("--batch", action="store_true", help="32 batched shots vs 32 sequential calls")
     ap.add_argument("--serve-rate", type=float, default=20.0)
-    ap.add_argument("--serve-requests", type=int, default=600)
+    ap.add_argument("--serve-requests", type=int, default=10000)
+    ap.add_argument("--serve-denoise-frac", type=float, default=0.25)
     ap.add_argument("--serve-slots", type=int, default=3)
     ap.add_argument("--serve-chunk", type=int, default=16)
     ap.add_argument("--serve-max-queue", type=int, default=256)

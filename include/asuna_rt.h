@@ -501,12 +501,16 @@ int asuna_complex_ior(const char* name, float* eta, float* k);
 
 /* ---- render server (continuous batching) -------------------------------------
  * No counterpart in the reference (an addition for serving).  Requests on
- * resident scenes arrive at any time; `slots` worker contexts render them
- * concurrently on the device, each slot batching the active requests of one
- * scene into one multi-shot wavefront per chunk of frames, with requests
- * leaving and joining at chunk boundaries.  Admission: a request's result
- * film must fit the memory budget (else it waits) and the pending queue must
- * have room (else it is rejected with ASUNA_ERR_BUSY, reported by poll). */
+ * the server's scenes arrive at any time; `slots` worker contexts render
+ * them concurrently on the device, each slot batching the active requests of
+ * one scene into one multi-shot wavefront per chunk of frames, with requests
+ * leaving and joining at chunk boundaries.  Admission is by memory
+ * footprint under the budget: a request is admitted when its result films
+ * fit (else it waits), and the pending queue must have room (else it is
+ * rejected with ASUNA_ERR_BUSY, reported by poll).  A scene registered with
+ * asuna_server_register_scene is built on the device when its first request
+ * is admitted, charged to the budget, and dropped again (least recently used
+ * first) when an admission needs the memory and no request uses it. */
 typedef struct asuna_server asuna_server;
 typedef struct asuna_server_opts {
   int32_t device;
@@ -515,12 +519,18 @@ typedef struct asuna_server_opts {
   uint32_t max_batch;        /* requests per active set (0 = 8) */
   uint32_t max_queue;        /* pending requests before arrivals are rejected (0 = unbounded) */
   uint32_t reserved;
-  uint64_t memory_budget;    /* bytes for resident scenes + result films (0 = 150 GiB) */
+  uint64_t memory_budget;    /* bytes for scenes + result films (0 = 150 GiB) */
   uint64_t path_budget;      /* wavefront state per slot, bytes (0 = default) */
 } asuna_server_opts;
+enum {
+  /* the result's image 0 is the denoised radiance: the request renders two
+   * halves of its frames into two films and asuna_denoise_blended combines
+   * them (needs asuna_server_set_denoiser and albedo + normal channels) */
+  ASUNA_REQUEST_DENOISE = 1u << 0
+};
 typedef struct asuna_request {
-  uint32_t scene; /* id from asuna_server_add_scene */
-  uint32_t reserved;
+  uint32_t scene; /* id from asuna_server_add_scene / _register_scene */
+  uint32_t flags; /* ASUNA_REQUEST_* */
   asuna_shot shot; /* shot.frames = spp */
 } asuna_request;
 typedef struct asuna_request_result {
@@ -533,12 +543,28 @@ typedef struct asuna_request_result {
 typedef struct asuna_server_stats {
   uint64_t admitted, rejected, pending, samples, memory_used;
   double elapsed_s;
+  uint64_t scenes_built;    /* device builds of registered scenes (admission time) */
+  uint64_t scenes_evicted;  /* registered scenes dropped to make room */
+  uint64_t denoised;        /* requests finished through the denoiser */
+  uint64_t scene_bytes;     /* device bytes of the scenes resident now */
 } asuna_server_stats;
 int asuna_server_create(const asuna_server_opts* opts, asuna_server** out);
+/* Builds the scene now; it stays resident for the server's lifetime. */
 int asuna_server_add_scene(asuna_server* server, const asuna_scene_desc* desc, uint32_t* scene_id);
+/* Registers a scene built on demand (see above).  The description's arrays
+ * must stay valid until the server is destroyed. */
+int asuna_server_register_scene(asuna_server* server, const asuna_scene_desc* desc, uint32_t* scene_id);
+/* One denoiser per slot with `opts`' network and the trained parameters
+ * `params` (n floats, asuna_denoiser_get_params); opts->max_pixels bounds
+ * the padded size of a denoised request. */
+struct asuna_denoiser_opts;
+int asuna_server_set_denoiser(asuna_server* server, const struct asuna_denoiser_opts* opts, const float* params,
+                              uint64_t n);
 int asuna_server_submit(asuna_server* server, const asuna_request* req, uint64_t* id);
 /* Finished (or rejected) requests since the last poll, oldest first. */
 int asuna_server_poll(asuna_server* server, asuna_request_result* out, uint32_t max, uint32_t* n);
+/* Film image `image` of a finished request (image 0 of a denoised request:
+ * the denoised radiance). */
 int asuna_server_read(asuna_server* server, uint64_t id, int image, float* host_rgba);
 /* Frees a finished request's film (returns its memory to the budget). */
 int asuna_server_release(asuna_server* server, uint64_t id);
