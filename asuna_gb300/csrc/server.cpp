@@ -86,6 +86,9 @@ struct asuna_server {
   std::unordered_map<uint64_t, std::shared_ptr<Req>> byId;
   std::deque<SceneEntry> scenes;  // (a deque: entries keep their addresses as scenes are added)
   std::vector<asuna_ctx*> ctxs;
+  // Reads of finished films: the slots' streams may be capturing the next
+  // request's graph, so copies out go on a stream of the server's own.
+  cudaStream_t readStream = nullptr;
   std::vector<asuna_denoiser*> denoisers;  // one per slot, or none
   std::vector<std::thread> workers;
   uint64_t memUsed = 0;  // films held + scenes
@@ -413,6 +416,12 @@ int asuna_server_create(const asuna_server_opts* opts, asuna_server** out) {
     if (opts->path_budget) asuna_ctx_set_path_budget(c, opts->path_budget);
     S->ctxs.push_back(c);
   }
+  if (cudaSetDevice(opts->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&S->readStream, cudaStreamNonBlocking) != cudaSuccess) {
+    for (auto* x : S->ctxs) asuna_ctx_destroy(x);
+    delete S;
+    return asuna::fail(ASUNA_ERR_CUDA, "asuna_server_create: stream creation failed");
+  }
   for (uint32_t i = 0; i < opts->slots; ++i) S->workers.emplace_back(worker, S, int(i));
   *out = S;
   return ASUNA_OK;
@@ -523,13 +532,21 @@ int asuna_server_read(asuna_server* S, uint64_t id, int image, float* host_rgba)
   if (r->status != ASUNA_OK || !r->film[0])
     return asuna::fail(ASUNA_ERR_INVALID, "request %llu has no film", (unsigned long long)id);
   if (r->finish < 0) return asuna::fail(ASUNA_ERR_INVALID, "request %llu is not finished", (unsigned long long)id);
+  if (!host_rgba) return asuna::fail(ASUNA_ERR_INVALID, "null output");
+  if (image < 0 || image >= ASUNA_NUM_OUTPUT_IMAGES) return asuna::fail(ASUNA_ERR_INVALID, "image %d out of range", image);
+  // the worker synchronised its stream before marking the request finished
+  float* src = nullptr;
   if (image == 0 && r->denoised) {
-    if (!host_rgba) return asuna::fail(ASUNA_ERR_INVALID, "null output");
-    ASUNA_CUDA_TRY(cudaMemcpy(host_rgba, r->denoised, size_t(r->shot.width) * r->shot.height * 16,
-                              cudaMemcpyDeviceToHost));
-    return ASUNA_OK;
+    src = r->denoised;
+  } else {
+    int rc = asuna_film_image(r->film[0], image, &src);
+    if (rc) return rc;
   }
-  return asuna_film_read(r->filmCtx, r->film[0], image, host_rgba);
+  ASUNA_CUDA_TRY(cudaSetDevice(S->opts.device));
+  ASUNA_CUDA_TRY(cudaMemcpyAsync(host_rgba, src, size_t(r->shot.width) * r->shot.height * 16,
+                                 cudaMemcpyDeviceToHost, S->readStream));
+  ASUNA_CUDA_TRY(cudaStreamSynchronize(S->readStream));
+  return ASUNA_OK;
 }
 
 int asuna_server_release(asuna_server* S, uint64_t id) {
@@ -590,6 +607,7 @@ int asuna_server_destroy(asuna_server* S) {
   for (auto& e : S->scenes)
     if (e.dev) asuna_scene_destroy(e.dev);
   for (auto* c : S->ctxs) asuna_ctx_destroy(c);
+  if (S->readStream) cudaStreamDestroy(S->readStream);
   delete S;
   return ASUNA_OK;
 }
