@@ -214,8 +214,8 @@ SIGNATURES = [
     ("asuna_denoiser_get_params", C.c_int, [P, P, C.c_uint64]),
     ("asuna_denoiser_set_params", C.c_int, [P, P, C.c_uint64]),
     ("asuna_denoiser_get_grads", C.c_int, [P, P, C.c_uint64]),
-    ("asuna_denoiser_forward", C.c_int, [P, P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, P]),
-    ("asuna_denoiser_loss_grad", C.c_int, [P, P, P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32,
+    ("asuna_denoiser_forward", C.c_int, [P, P, P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, P]),
+    ("asuna_denoiser_loss_grad", C.c_int, [P, P, P, P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32,
                                             C.POINTER(C.c_float)]),
     ("asuna_denoiser_adam", C.c_int, [P, C.c_float, C.c_float, C.c_float, C.c_float]),
     ("asuna_denoise", C.c_int, [P, P, P, C.c_int, C.c_int, P]),

@@ -490,17 +490,18 @@ __global__ void k_upsample_concat_v(const uint4* low, const uint4* skip, uint4* 
   }
 }
 
-// Network input: log1p(radiance), albedo, normal, zeros up to C; pixels
-// outside the h x w image (padding up to hp x wp) are zero.
 // Network input: log1p(radiance), albedo, normal, log2(1 + filter-weight
-// sum) / 16 (the sample count: how much noise there is to remove), zeros up
-// to C; pixels outside the h x w image (padding up to hp x wp) are zero.
+// sum) / 16 (the sample count: how much noise there is to remove), the
+// per-pixel noise as log1p of the mean over rgb of the input radiance's
+// standard-deviation estimate, and a flag that the noise is known (1) or
+// not (0, no estimate given); zeros up to C; pixels outside the h x w image
+// (padding up to hp x wp) are zero.
 __global__ void k_prep_input(const float4* rad, const float4* alb, const float4* nrm, const float4* wsum,
-                             __nv_bfloat16* out, int n, int h, int w, int hp, int wp, int C) {
+                             const float4* noise, __nv_bfloat16* out, int n, int h, int w, int hp, int wp, int C) {
   const size_t P = size_t(n) * hp * wp;
   for (size_t q = blockIdx.x * size_t(blockDim.x) + threadIdx.x; q < P; q += size_t(gridDim.x) * blockDim.x) {
     const int x = int(q % wp), y = int((q / wp) % hp), b = int(q / (size_t(wp) * hp));
-    float v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    float v[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (y < h && x < w) {
       const size_t p = (size_t(b) * h + y) * w + x;
       const float4 r = rad[p];
@@ -520,10 +521,28 @@ __global__ void k_prep_input(const float4* rad, const float4* alb, const float4*
         v[8] = m.z;
       }
       if (wsum) v[9] = log2f(1.0f + fmaxf(wsum[p].x, 0.0f)) * 0.0625f;
+      if (noise) {
+        const float4 e = noise[p];
+        v[10] = log1pf(fmaxf((e.x + e.y + e.z) * (1.0f / 3.0f), 0.0f));
+        v[11] = 1.0f;
+      }
     }
     __nv_bfloat162* o = reinterpret_cast<__nv_bfloat162*>(out + q * C);
     for (int c = 0; c < C; c += 2)
-      o[c / 2] = __floats2bfloat162_rn(c < 10 ? v[c] : 0.0f, c + 1 < 10 ? v[c + 1] : 0.0f);
+      o[c / 2] = __floats2bfloat162_rn(c < 12 ? v[c] : 0.0f, c + 1 < 12 ? v[c + 1] : 0.0f);
+  }
+}
+
+// Noise estimates from two independent half renders a, b of one shot:
+// per channel |a - b| / sqrt(2) for either half alone and |a - b| / 2 for
+// their average (the standard deviation of a difference of two equal-noise
+// estimates is sqrt(2) times either's).
+__global__ void k_half_noise(const float4* a, const float4* b, float4* half, float4* all, size_t P) {
+  for (size_t p = blockIdx.x * size_t(blockDim.x) + threadIdx.x; p < P; p += size_t(gridDim.x) * blockDim.x) {
+    const float4 x = a[p], y = b[p];
+    const float d[3] = {fabsf(x.x - y.x), fabsf(x.y - y.y), fabsf(x.z - y.z)};
+    if (half) half[p] = make_float4(d[0] * 0.70710678f, d[1] * 0.70710678f, d[2] * 0.70710678f, 0.0f);
+    if (all) all[p] = make_float4(d[0] * 0.5f, d[1] * 0.5f, d[2] * 0.5f, 0.0f);
   }
 }
 
@@ -1023,14 +1042,15 @@ int upsampleConcat(cudaStream_t stream, const __nv_bfloat16* low, const __nv_bfl
 }
 
 int forward(asuna_denoiser* d, const float* rad, const float* alb, const float* nrm, const float* wsum,
-            const Dims& D) {
+            const float* noise, const Dims& D) {
   const int L = d->L;
   cudaStream_t s = d->stream();
   if (d->useTc) NN_TRY(flipAll(d));
   const size_t P0 = size_t(D.n) * D.hp * D.wp;
   k_prep_input<<<grid1d(P0), 256, 0, s>>>(reinterpret_cast<const float4*>(rad), reinterpret_cast<const float4*>(alb),
                                           reinterpret_cast<const float4*>(nrm), reinterpret_cast<const float4*>(wsum),
-                                          d->lv[0].X, D.n, D.h, D.w, D.hp, D.wp, kInC);
+                                          reinterpret_cast<const float4*>(noise), d->lv[0].X, D.n, D.h, D.w, D.hp,
+                                          D.wp, kInC);
   ASUNA_CUDA_TRY(cudaGetLastError());
   for (int l = 0; l < L; ++l) {
     const int hl = D.hp >> l, wl = D.wp >> l;
@@ -1261,13 +1281,13 @@ int asuna_denoiser_get_grads(asuna_denoiser* d, float* host, uint64_t n) {
 }
 
 int asuna_denoiser_forward(asuna_denoiser* d, const float* radiance, const float* albedo, const float* normal,
-                           const float* weight, uint32_t n, uint32_t h, uint32_t w, float* out) {
+                           const float* weight, const float* noise, uint32_t n, uint32_t h, uint32_t w, float* out) {
   clearError();
   if (!d || !radiance || !out) return fail(ASUNA_ERR_INVALID, "asuna_denoiser_forward: null argument");
   Dims D;
   NN_TRY(dims(d, n, h, w, D));
   ASUNA_CUDA_TRY(cudaSetDevice(d->ctx->device));
-  NN_TRY(forward(d, radiance, albedo, normal, weight, D));
+  NN_TRY(forward(d, radiance, albedo, normal, weight, noise, D));
   k_output<<<grid1d(size_t(n) * h * w), 256, 0, d->stream()>>>(d->head, kHeadC,
                                                                reinterpret_cast<const float4*>(radiance),
                                                                reinterpret_cast<float4*>(out), D.n, D.h, D.w, D.hp,
@@ -1277,8 +1297,8 @@ int asuna_denoiser_forward(asuna_denoiser* d, const float* radiance, const float
 }
 
 int asuna_denoiser_loss_grad(asuna_denoiser* d, const float* radiance, const float* albedo, const float* normal,
-                             const float* weight, const float* target, uint32_t n, uint32_t h, uint32_t w,
-                             float* loss) {
+                             const float* weight, const float* noise, const float* target, uint32_t n, uint32_t h,
+                             uint32_t w, float* loss) {
   clearError();
   if (!d || !radiance || !target) return fail(ASUNA_ERR_INVALID, "asuna_denoiser_loss_grad: null argument");
   if (!d->training) return fail(ASUNA_ERR_INVALID, "denoiser was created without training state");
@@ -1288,7 +1308,7 @@ int asuna_denoiser_loss_grad(asuna_denoiser* d, const float* radiance, const flo
   cudaStream_t s = d->stream();
   ASUNA_CUDA_TRY(cudaMemsetAsync(d->grad, 0, d->nParams * sizeof(float), s));
   ASUNA_CUDA_TRY(cudaMemsetAsync(d->dLoss, 0, sizeof(float), s));
-  NN_TRY(forward(d, radiance, albedo, normal, weight, D));
+  NN_TRY(forward(d, radiance, albedo, normal, weight, noise, D));
   const size_t P0 = size_t(D.n) * D.hp * D.wp;
   const float invCount = float(1.0 / (3.0 * double(n) * h * w));
   if (d->loss == ASUNA_DENOISER_LOSS_RELMSE)
@@ -1328,7 +1348,18 @@ int asuna_denoise(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* film, int albed
   if (albedo_image > 7 || normal_image > 7 || albedo_image == 0 || normal_image == 0)
     return fail(ASUNA_ERR_INVALID, "asuna_denoise: guide images must be channels 1..7 or -1");
   return asuna_denoiser_forward(d, filmImage(film, 0), filmImage(film, albedo_image), filmImage(film, normal_image),
-                                filmImage(film, 8), 1, film->height, film->width, out);
+                                filmImage(film, 8), nullptr, 1, film->height, film->width, out);
+}
+
+// A film's radiance denoised with a per-pixel noise estimate (device RGBA).
+static int denoiseWithNoise(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* film, int albedo_image, int normal_image,
+                            const float4* noise, float* out) {
+  if (d->ctx != ctx) return fail(ASUNA_ERR_INVALID, "denoiser belongs to another context");
+  if (albedo_image > 7 || normal_image > 7 || albedo_image == 0 || normal_image == 0)
+    return fail(ASUNA_ERR_INVALID, "guide images must be channels 1..7 or -1");
+  return asuna_denoiser_forward(d, filmImage(film, 0), filmImage(film, albedo_image), filmImage(film, normal_image),
+                                filmImage(film, 8), reinterpret_cast<const float*>(noise), 1, film->height,
+                                film->width, out);
 }
 
 int asuna_denoise_estimate(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asuna_film* b, int albedo_image,
@@ -1337,9 +1368,19 @@ int asuna_denoise_estimate(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asu
   if (!a || !b) return fail(ASUNA_ERR_INVALID, "asuna_denoise_estimate: null film");
   if (a->width != b->width || a->height != b->height)
     return fail(ASUNA_ERR_INVALID, "asuna_denoise_estimate: films differ in size");
-  NN_TRY(asuna_denoise(ctx, d, a, albedo_image, normal_image, out));
+  if (!ctx || !d || !out) return fail(ASUNA_ERR_INVALID, "asuna_denoise_estimate: null argument");
   cudaStream_t s = ctx->stream;
   const size_t P = size_t(a->width) * a->height;
+  float4* noise = nullptr;
+  ASUNA_CUDA_TRY(cudaMallocAsync(&noise, P * sizeof(float4), s));
+  struct Free {
+    float4* p;
+    cudaStream_t s;
+    ~Free() { cudaFreeAsync(p, s); }
+  } guard{noise, s};
+  k_half_noise<<<grid1d(P), 256, 0, s>>>(a->rad, b->rad, noise, nullptr, P);
+  ASUNA_CUDA_TRY(cudaGetLastError());
+  NN_TRY(denoiseWithNoise(ctx, d, a, albedo_image, normal_image, noise, out));
   ASUNA_CUDA_TRY(cudaMemsetAsync(d->dSums, 0, 2 * sizeof(double), s));
   k_err_sums<<<grid1d(P), 256, 0, s>>>(reinterpret_cast<const float4*>(out), a->rad, b->rad, P, d->dSums);
   ASUNA_CUDA_TRY(cudaGetLastError());
@@ -1360,10 +1401,12 @@ int asuna_denoise_combined(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asu
     return fail(ASUNA_ERR_INVALID, "asuna_denoise_combined: films differ in size");
   cudaStream_t s = ctx->stream;
   const size_t P = size_t(a->width) * a->height;
-  float4 *db = nullptr, *rad = nullptr, *wsum = nullptr;
-  ASUNA_CUDA_TRY(cudaMallocAsync(&db, 3 * P * sizeof(float4), s));
+  float4 *db = nullptr, *rad = nullptr, *wsum = nullptr, *nHalf = nullptr, *nAll = nullptr;
+  ASUNA_CUDA_TRY(cudaMallocAsync(&db, 5 * P * sizeof(float4), s));
   rad = db + P;
   wsum = rad + P;
+  nHalf = wsum + P;
+  nAll = nHalf + P;
   struct Free {
     float4* p;
     cudaStream_t s;
@@ -1372,7 +1415,9 @@ int asuna_denoise_combined(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asu
   // D_A (into out) against film B, as asuna_denoise_estimate does
   double eA = 0.0, eP = 0.0;
   NN_TRY(asuna_denoise_estimate(ctx, d, a, b, albedo_image, normal_image, out, &eA, &eP));
-  NN_TRY(asuna_denoise(ctx, d, b, albedo_image, normal_image, reinterpret_cast<float*>(db)));
+  k_half_noise<<<grid1d(P), 256, 0, s>>>(a->rad, b->rad, nHalf, nAll, P);
+  ASUNA_CUDA_TRY(cudaGetLastError());
+  NN_TRY(denoiseWithNoise(ctx, d, b, albedo_image, normal_image, nHalf, reinterpret_cast<float*>(db)));
   ASUNA_CUDA_TRY(cudaMemsetAsync(d->dSums + 2, 0, sizeof(double), s));
   k_combine<<<grid1d(P), 256, 0, s>>>(reinterpret_cast<const float4*>(out), db, a->rad, b->rad, a->w, b->w, rad, wsum,
                                       P, d->dSums);
@@ -1380,8 +1425,8 @@ int asuna_denoise_combined(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asu
   double h = 0.0;
   ASUNA_CUDA_TRY(cudaMemcpyAsync(&h, d->dSums + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
   NN_TRY(asuna_denoiser_forward(d, reinterpret_cast<const float*>(rad), filmImage(a, albedo_image),
-                                filmImage(a, normal_image), reinterpret_cast<const float*>(wsum), 1, a->height,
-                                a->width, out));
+                                filmImage(a, normal_image), reinterpret_cast<const float*>(wsum),
+                                reinterpret_cast<const float*>(nAll), 1, a->height, a->width, out));
   ASUNA_CUDA_TRY(cudaStreamSynchronize(s));
   // the halves' denoised outputs differ by twice the output variance of a
   // half; doubling the samples is taken to halve that variance and keep the
@@ -1402,23 +1447,25 @@ int asuna_denoise_blended(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* a, asun
   cudaStream_t s = ctx->stream;
   const size_t P = size_t(a->width) * a->height;
   float4* scratch = nullptr;
-  ASUNA_CUDA_TRY(cudaMallocAsync(&scratch, 4 * P * sizeof(float4), s));
+  ASUNA_CUDA_TRY(cudaMallocAsync(&scratch, 6 * P * sizeof(float4), s));
   struct Free {
     float4* p;
     cudaStream_t s;
     ~Free() { cudaFreeAsync(p, s); }
   } guard{scratch, s};
-  float4 *da = scratch, *db = da + P, *rad = db + P, *wsum = rad + P;
-  NN_TRY(asuna_denoise(ctx, d, a, albedo_image, normal_image, reinterpret_cast<float*>(da)));
-  NN_TRY(asuna_denoise(ctx, d, b, albedo_image, normal_image, reinterpret_cast<float*>(db)));
+  float4 *da = scratch, *db = da + P, *rad = db + P, *wsum = rad + P, *nHalf = wsum + P, *nAll = nHalf + P;
+  k_half_noise<<<grid1d(P), 256, 0, s>>>(a->rad, b->rad, nHalf, nAll, P);
+  ASUNA_CUDA_TRY(cudaGetLastError());
+  NN_TRY(denoiseWithNoise(ctx, d, a, albedo_image, normal_image, nHalf, reinterpret_cast<float*>(da)));
+  NN_TRY(denoiseWithNoise(ctx, d, b, albedo_image, normal_image, nHalf, reinterpret_cast<float*>(db)));
   ASUNA_CUDA_TRY(cudaMemsetAsync(d->dSums + 3, 0, 5 * sizeof(double), s));
   k_blend_sums<<<grid1d(P), 256, 0, s>>>(da, db, a->rad, b->rad, a->w, b->w, rad, wsum, P, d->dSums);
   ASUNA_CUDA_TRY(cudaGetLastError());
   double h[5];
   ASUNA_CUDA_TRY(cudaMemcpyAsync(h, d->dSums + 3, sizeof(h), cudaMemcpyDeviceToHost, s));
   NN_TRY(asuna_denoiser_forward(d, reinterpret_cast<const float*>(rad), filmImage(a, albedo_image),
-                                filmImage(a, normal_image), reinterpret_cast<const float*>(wsum), 1, a->height,
-                                a->width, out));
+                                filmImage(a, normal_image), reinterpret_cast<const float*>(wsum),
+                                reinterpret_cast<const float*>(nAll), 1, a->height, a->width, out));
   ASUNA_CUDA_TRY(cudaStreamSynchronize(s));
   // X_half = w D_a + (1 - w) a, judged by b: err^2 = mean((X_half - b)^2) -
   // mean((a - b)^2) / 2; all samples: minus a quarter of mean((X_a - X_b)^2).

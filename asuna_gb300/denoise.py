@@ -22,7 +22,7 @@ from . import _abi as A
 from ._abi import check, lib
 
 DEFAULT_CHANNELS = (32, 48, 64, 96, 128)
-IN_CHANNELS = 16  # log1p(radiance), albedo, normal, zero padding
+IN_CHANNELS = 16  # log1p(radiance), albedo, normal, sample count, noise, noise known, zero padding
 HEAD_CHANNELS = 16  # outputs 0..2 used
 
 
@@ -111,22 +111,23 @@ class Denoiser:
         return d
 
     # compute -----------------------------------------------------------
-    def forward(self, rad, alb=None, nrm=None, wsum=None, out=None):
-        """rad/alb/nrm/wsum (film images 0, albedo, normal, 8): CUDA float32
+    def forward(self, rad, alb=None, nrm=None, wsum=None, out=None, noise=None):
+        """rad/alb/nrm/wsum (film images 0, albedo, normal, 8) and the
+        per-pixel noise estimate of rad (None = unknown): CUDA float32
         [n, h, w, 4]; returns the denoised radiance."""
         torch = _torch()
         n, h, w, _ = rad.shape
         if out is None:
             out = torch.empty_like(rad)
-        check(lib().asuna_denoiser_forward(self.handle, _ptr(rad), _ptr(alb), _ptr(nrm), _ptr(wsum), n, h, w,
-                                           _ptr(out)))
+        check(lib().asuna_denoiser_forward(self.handle, _ptr(rad), _ptr(alb), _ptr(nrm), _ptr(wsum), _ptr(noise),
+                                           n, h, w, _ptr(out)))
         return out
 
-    def loss_grad(self, rad, alb, nrm, wsum, target):
+    def loss_grad(self, rad, alb, nrm, wsum, target, noise=None):
         n, h, w, _ = rad.shape
         loss = C.c_float()
         check(lib().asuna_denoiser_loss_grad(self.handle, _ptr(rad), _ptr(alb), _ptr(nrm), _ptr(wsum),
-                                             _ptr(target), n, h, w, C.byref(loss)))
+                                             _ptr(noise), _ptr(target), n, h, w, C.byref(loss)))
         return loss.value
 
     def adam(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
@@ -183,44 +184,60 @@ class Denoiser:
 
 
 def render_pairs(ctx, seeds, width, height, spp_in=4, spp_target=256, level=4, max_depth=8):
-    """Renders each training scene with two independent sample streams: the
-    network input after each count of `spp_in` (an int or an increasing
-    tuple; one progressive render, with the albedo / normal channels) and
-    a `spp_target` render (the target).  Returns host arrays [n, h, w, 4]
-    float32 (radiance, albedo, normal, filter-weight sum, target), one entry
-    per scene and input count."""
+    """Renders each training scene as two independent half renders A and B
+    (own sample streams, progressive over the total counts `spp_in`: an even
+    int or an increasing tuple, with the albedo / normal channels) and a
+    `spp_target` render (the target).  Every (scene, count) gives two
+    network inputs, as the library's blended denoise uses them: all samples
+    (radiance (A + B) / 2, weight A + B, noise |A - B| / 2) and a half
+    (radiance A, weight A, noise |A - B| / sqrt 2).  Returns host arrays
+    [n, h, w, 4] float32: (radiance, albedo, normal, filter-weight sum,
+    target, noise)."""
     from . import scenes
 
     levels = (spp_in,) if np.isscalar(spp_in) else tuple(spp_in)
-    out = {k: [] for k in ("rad", "alb", "nrm", "wsum", "tgt")}
+    if any(t < 2 or t % 2 for t in levels):
+        raise ValueError("sample counts must be even (two equal halves)")
+    out = {k: [] for k in ("rad", "alb", "nrm", "wsum", "tgt", "noise")}
     for s in seeds:
         b, shot = scenes.training_scene(int(s), width, height, frames=levels[0], max_depth=max_depth, level=level)
         scene = ctx.create_scene(b.desc())
         g = ctx.create_film(width, height)
-        shot.frame0, shot.frames, shot.seed = 0, spp_target, 2 * int(s) + 1
+        shot.frame0, shot.frames, shot.seed = 0, spp_target, 3 * int(s) + 2
         ctx.render(scene, shot, g)
         tgt = g.read(0)
-        f = ctx.create_film(width, height)
-        shot.seed = 2 * int(s)
+        fa, fb = ctx.create_film(width, height), ctx.create_film(width, height)
         done = 0
-        for spp in levels:
-            shot.frame0, shot.frames = done, spp - done
-            ctx.render(scene, shot, f)
-            done = spp
-            out["rad"].append(f.read(0))
-            out["alb"].append(f.read(1))
-            out["nrm"].append(f.read(2))
-            out["wsum"].append(f.read(8))
-            out["tgt"].append(tgt)
-        f.close()
+        for total in levels:
+            half = total // 2
+            for f, seed in ((fa, 3 * int(s)), (fb, 3 * int(s) + 1)):
+                shot.frame0, shot.frames, shot.seed = done, half - done, seed
+                ctx.render(scene, shot, f)
+            done = half
+            a, bb = fa.read(0), fb.read(0)
+            wa, wb = fa.read(8), fb.read(8)
+            alb, nrm = fa.read(1), fa.read(2)
+            diff = np.abs(a - bb)
+            allr = 0.5 * (a + bb)
+            allr[..., 3] = 1.0
+            for rad, wsum, noise in ((allr, wa + wb, diff * np.float32(0.5)),
+                                     (a, wa, diff * np.float32(0.70710678))):
+                out["rad"].append(rad)
+                out["alb"].append(alb)
+                out["nrm"].append(nrm)
+                out["wsum"].append(wsum)
+                out["tgt"].append(tgt)
+                out["noise"].append(noise)
+        fa.close()
+        fb.close()
         g.close()
         del scene
-    return tuple(np.stack(out[k]) for k in ("rad", "alb", "nrm", "wsum", "tgt"))
+    return tuple(np.stack(out[k]) for k in ("rad", "alb", "nrm", "wsum", "tgt", "noise"))
 
 
 def train(den, data, steps, batch=8, crop=64, lr=1e-3, seed=0, log_every=0):
     """Adam on random crops of the training pairs.  `data` = (rad, alb, nrm,
-    wsum, tgt) host arrays [n, h, w, 4]; returns the loss history."""
+    wsum, tgt[, noise]) host arrays [n, h, w, 4]; returns the loss history."""
     torch = _torch()
     rng = np.random.default_rng(seed)
     dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in data]
@@ -235,7 +252,7 @@ def train(den, data, steps, batch=8, crop=64, lr=1e-3, seed=0, log_every=0):
             xs = rng.integers(0, w - crop + 1, batch)
             crops = [torch.stack([a[int(idx[k]), ys[k]:ys[k] + crop, xs[k]:xs[k] + crop] for k in range(batch)])
                      .contiguous() for a in dev]
-            loss = den.loss_grad(*crops)
+            loss = den.loss_grad(*crops[:5], noise=crops[5] if len(crops) > 5 else None)
             den.adam(lr)
             losses.append(loss)
             if log_every and (it + 1) % log_every == 0:

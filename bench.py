@@ -791,10 +791,10 @@ def main():
                     help="time to RMSE 0.01 vs the FP64 reference, plain vs denoised path")
     ap.add_argument("--rmse-target", type=float, default=0.01)
     ap.add_argument("--plain-max-spp", type=int, default=32768)
-    ap.add_argument("--denoise-max-spp", type=int, default=8192)
+    ap.add_argument("--denoise-max-spp", type=int, default=32768)
     ap.add_argument("--train-scenes", type=int, default=64)
     ap.add_argument("--train-size", type=int, default=256)
-    ap.add_argument("--train-spp-in", default="4,16,64,256,1024")
+    ap.add_argument("--train-spp-in", default="4,16,64,256,1024,4096")
     ap.add_argument("--train-target-spp", type=int, default=65536)
     ap.add_argument("--train-level", type=int, default=6)
     ap.add_argument("--train-steps", type=int, default=20000)

@@ -68,15 +68,18 @@ int asuna_denoiser_get_grads(asuna_denoiser* d, float* host, uint64_t n);
 
 /* Forward pass: out = expm1(log1p(radiance) + head), clamped at 0 (RGBA, alpha 1).
  * `weight` is the film's filter-weight sum image (image 8; NULL = unknown):
- * it tells the network how many samples the radiance holds. */
+ * it tells the network how many samples the radiance holds.  `noise`
+ * (RGBA, NULL = unknown) estimates, per pixel and channel, the standard
+ * deviation of `radiance`: where it is known (two independent half renders
+ * give it) the network sees how much noise there is at each pixel. */
 int asuna_denoiser_forward(asuna_denoiser* d, const float* radiance, const float* albedo, const float* normal,
-                           const float* weight, uint32_t n, uint32_t h, uint32_t w, float* out);
+                           const float* weight, const float* noise, uint32_t n, uint32_t h, uint32_t w, float* out);
 /* Zeroes the gradients, runs forward, the loss chosen at creation against
  * `target` (mean over valid pixels and 3 channels) and the backward pass.
  * *loss (host) receives the loss; the call synchronises the stream. */
 int asuna_denoiser_loss_grad(asuna_denoiser* d, const float* radiance, const float* albedo, const float* normal,
-                             const float* weight, const float* target, uint32_t n, uint32_t h, uint32_t w,
-                             float* loss);
+                             const float* weight, const float* noise, const float* target, uint32_t n, uint32_t h,
+                             uint32_t w, float* loss);
 /* One Adam step (bias-corrected) on the gradients of the last loss_grad. */
 int asuna_denoiser_adam(asuna_denoiser* d, float lr, float beta1, float beta2, float eps);
 
@@ -87,7 +90,8 @@ int asuna_denoise(asuna_ctx* ctx, asuna_denoiser* d, asuna_film* film, int albed
                   float* out);
 
 /* Error estimate of the denoised image from two independent half renders
- * `a` and `b` of the same shot (disjoint frames, equal counts): with D the
+ * `a` and `b` of the same shot (disjoint frames, equal counts; their
+ * difference also gives the network its per-pixel noise input): with D the
  * denoised a,  err_denoised^2 = mean((D - b)^2) - mean((a - b)^2) / 2  and
  * err_plain^2 = mean((a - b)^2) / 4  estimate the RMSE of D and of the plain
  * average of a and b against the converged image (means over pixels and RGB).

@@ -116,9 +116,11 @@ def upsample2_bwd(g):
     return g.reshape(n, h // 2, 2, w // 2, 2, c).sum(axis=(2, 4))
 
 
-def prep_input(rad, alb, nrm, hp, wp, wsum=None):
+def prep_input(rad, alb, nrm, hp, wp, wsum=None, noise=None):
     """[N,H,W,4] images -> padded [N,hp,wp,16] network input (channel 9:
-    log2(1 + filter-weight sum) / 16)."""
+    log2(1 + filter-weight sum) / 16; channel 10: log1p of the mean over rgb
+    of the radiance's per-pixel standard-deviation estimate, channel 11: 1
+    where that estimate is given)."""
     n, h, w, _ = rad.shape
     x = np.zeros((n, hp, wp, IN_C))
     x[:, :h, :w, 0:3] = np.log1p(np.maximum(rad[..., :3], 0.0))
@@ -128,6 +130,9 @@ def prep_input(rad, alb, nrm, hp, wp, wsum=None):
         x[:, :h, :w, 6:9] = nrm[..., :3]
     if wsum is not None:
         x[:, :h, :w, 9] = np.log2(1.0 + np.maximum(wsum[..., 0], 0.0)) / 16.0
+    if noise is not None:
+        x[:, :h, :w, 10] = np.log1p(np.maximum(noise[..., :3].astype(np.float64).mean(axis=3), 0.0))
+        x[:, :h, :w, 11] = 1.0
     return x
 
 
@@ -151,7 +156,7 @@ class UNetRef:
     def dec(self, l, k):
         return 2 * self.L + 2 * (self.L - 2 - l) + k
 
-    def forward(self, rad, alb, nrm, wsum=None):
+    def forward(self, rad, alb, nrm, wsum=None, noise=None):
         L = self.L
         n, h, w, _ = rad.shape
         a = 1 << (L - 1)
@@ -163,7 +168,7 @@ class UNetRef:
         U = [None] * L
         B = [None] * L
         D = [None] * L
-        X[0] = self.r(prep_input(rad, alb, nrm, hp, wp, wsum))
+        X[0] = self.r(prep_input(rad, alb, nrm, hp, wp, wsum, noise))
         for l in range(L):
             if l > 0:
                 X[l] = self.r(avgpool2(S[l - 1]))
@@ -186,8 +191,8 @@ class UNetRef:
         self.cache = c
         return head
 
-    def output(self, rad, alb, nrm, wsum=None):
-        head = self.forward(rad, alb, nrm, wsum)
+    def output(self, rad, alb, nrm, wsum=None, noise=None):
+        head = self.forward(rad, alb, nrm, wsum, noise)
         n, h, w, _ = rad.shape
         y = head[:, :h, :w, :3] + np.log1p(np.maximum(rad[..., :3], 0.0))
         return np.maximum(np.expm1(y), 0.0)
@@ -209,10 +214,10 @@ class UNetRef:
         d = o - np.maximum(target[..., :3], 0.0)
         return (d * d * inv).sum() / count, np.where(e > 0, 2.0 * d * (e + 1.0) * inv, 0.0) / count
 
-    def loss_grad(self, rad, alb, nrm, target, wsum=None, loss="l1log"):
+    def loss_grad(self, rad, alb, nrm, target, wsum=None, loss="l1log", noise=None):
         """Returns (loss, flat gradient) in the parameter layout."""
         L = self.L
-        head = self.forward(rad, alb, nrm, wsum)
+        head = self.forward(rad, alb, nrm, wsum, noise)
         c = self.cache
         n, h, w = rad.shape[:3]
         lv, gh = self.head_loss(head[:, :h, :w, :3], rad, target, loss)

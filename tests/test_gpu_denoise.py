@@ -218,12 +218,13 @@ def _net_inputs(rng, n, h, w):
     return rad, alb, nrm, wsum, tgt
 
 
-@pytest.mark.parametrize("loss_kind", ["l1log", "relmse"])
-def test_network_forward_loss_and_gradients(dctx, loss_kind):
+@pytest.mark.parametrize("loss_kind,with_noise", [("l1log", False), ("relmse", False), ("l1log", True)])
+def test_network_forward_loss_and_gradients(dctx, loss_kind, with_noise):
     ch = dn.DEFAULT_CHANNELS
     rng = np.random.default_rng(5)
     n, h, w = 2, 37, 45  # padded to 48 x 48
     rad, alb, nrm, wsum, tgt = _net_inputs(rng, n, h, w)
+    noise = rng.uniform(0.0, 2.0, rad.shape).astype(np.float32) if with_noise else None
     d = dn.Denoiser(dctx, ch, seed=3, max_pixels=n * 48 * 48, training=True, loss=loss_kind)
     p = U.he_init(ch, 3)
     assert np.allclose(d.get_params(), p, rtol=1e-6, atol=1e-9)
@@ -231,15 +232,17 @@ def test_network_forward_loss_and_gradients(dctx, loss_kind):
     d.set_params(p)
     ref = U.UNetRef(ch, p, bf16=True)
     drad, dalb, dnrm, dw, dtgt = f32(rad), f32(alb), f32(nrm), f32(wsum), f32(tgt)
+    dnoise = f32(noise) if with_noise else None
     torch.cuda.synchronize()
-    out = d.forward(drad, dalb, dnrm, dw)
+    out = d.forward(drad, dalb, dnrm, dw, noise=dnoise)
     dctx.sync()
-    ro = ref.output(rad.astype(np.float64), alb, nrm, wsum)
+    ro = ref.output(rad.astype(np.float64), alb, nrm, wsum, noise)
     got = out.cpu().numpy()[..., :3]
     med = np.median(np.abs(got - ro) / (np.abs(ro) + 1e-3))
     mx = np.abs(got - ro).max() / np.abs(ro).max()
-    loss = d.loss_grad(drad, dalb, dnrm, dw, dtgt)
-    rl, rg = ref.loss_grad(rad.astype(np.float64), alb, nrm, tgt.astype(np.float64), wsum, loss=loss_kind)
+    loss = d.loss_grad(drad, dalb, dnrm, dw, dtgt, noise=dnoise)
+    rl, rg = ref.loss_grad(rad.astype(np.float64), alb, nrm, tgt.astype(np.float64), wsum, loss=loss_kind,
+                           noise=noise)
     g = d.get_grads().astype(np.float64)
     print(f"\nforward: median rel {med:.2e}, max/scale {mx:.2e}; loss {loss:.6f} vs {rl:.6f}")
     off, rows = 0, []
@@ -264,20 +267,21 @@ def test_network_forward_loss_and_gradients(dctx, loss_kind):
 
 
 def test_training_gain_over_noisy_input(dctx):
-    """Train on 4-spp / 256-spp pairs of 24 seeded scenes; on 4 held-out
-    scenes the denoised 4-spp image is much closer to the 256-spp render
-    than the 4-spp input is."""
+    """Train on 4-spp / 256-spp pairs of 24 seeded scenes (two 2-spp halves
+    each, as all samples and as a half, with their per-pixel noise); on 4
+    held-out scenes the denoised input is much closer to the 256-spp render
+    than the input is."""
     train = dn.render_pairs(dctx, range(24), 96, 96, spp_in=4, spp_target=256, level=3)
     test = dn.render_pairs(dctx, range(100, 104), 96, 96, spp_in=4, spp_target=256, level=3)
     d = dn.Denoiser(dctx, seed=1, max_pixels=8 * 64 * 64, training=True)
     losses = dn.train(d, train, steps=400, batch=8, crop=64, lr=1e-3)
     assert np.mean(losses[-50:]) < 0.8 * np.mean(losses[:10])
-    e = dn.Denoiser(dctx, max_pixels=4 * 96 * 96)
+    e = dn.Denoiser(dctx, max_pixels=8 * 96 * 96)
     e.set_params(d.get_params())
-    rad, alb, nrm, wsum, tgt = test
+    rad, alb, nrm, wsum, tgt, noise = test
     drad, dalb, dnrm, dw = f32(rad), f32(alb), f32(nrm), f32(wsum)
     torch.cuda.synchronize()
-    out = e.forward(drad, dalb, dnrm, dw)
+    out = e.forward(drad, dalb, dnrm, dw, noise=f32(noise))
     dctx.sync()
     den = out.cpu().numpy()
     noisy_err = dn.rmse(rad, tgt)
@@ -314,15 +318,21 @@ def test_film_denoise_and_error_estimate(dctx):
     # the estimate subtracts half the halves' output variance
     full, ec, ep2 = d.combined(fa, fb)
     dctx.sync()
-    db_ = d.denoise(fb)
-    dctx.sync()  # the library's stream, not torch's: wait before the copy
-    db_ = db_.cpu().numpy()
     import torch
 
+    # the per-pixel noise the two halves give: |a - b| / sqrt(2) for a half,
+    # |a - b| / 2 for their average
+    diff = np.abs(a - bb).astype(np.float32)
+    n_half, n_all = torch.from_numpy(diff * np.float32(0.70710678))[None].cuda(), \
+        torch.from_numpy(diff * np.float32(0.5))[None].cuda()
+    db_ = d.forward(fb.tensor(0)[None].contiguous(), fb.tensor(1)[None].contiguous(), fb.tensor(2)[None].contiguous(),
+                    fb.tensor(8)[None].contiguous(), noise=n_half)
+    dctx.sync()  # the library's stream, not torch's: wait before the copy
+    db_ = db_[0].cpu().numpy()
     comb = 0.5 * (a + bb)
     comb[..., 3] = 1.0
     ref = d.forward(torch.from_numpy(comb)[None].cuda(), fa.tensor(1)[None].contiguous(),
-                    fa.tensor(2)[None].contiguous(), (fa.tensor(8) + fb.tensor(8))[None])
+                    fa.tensor(2)[None].contiguous(), (fa.tensor(8) + fb.tensor(8))[None], noise=n_all)
     dctx.sync()
     assert np.allclose(full.cpu().numpy(), ref[0].cpu().numpy(), atol=1e-6)
     var_half = 0.5 * np.mean((den.cpu().numpy()[..., :3].astype(np.float64) - db_[..., :3]) ** 2)
