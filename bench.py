@@ -644,10 +644,10 @@ def run_serve(args):
     --serve-rate per second; each names a scene of a catalog of the mixed
     recipe (4-64 spheres, 0.33-21M triangles) registered with the server,
     which builds a scene on the device when its first request is admitted
-    (charged to the 150 GB budget; idle scenes are dropped when an admission
-    needs the room), a resolution from {512x512, 1280x720, 1920x1080}, a
-    sample count from {4, 16, 64}, a seeded camera and, for a quarter of them,
-    the denoise flag (two half renders blended with their denoise).  The
+    (charged to the memory budget, 150 GB by default; idle scenes are
+    dropped, least recently used first, when an admission needs the room),
+    a resolution from {512x512, 1280x720, 1920x1080}, a sample count from
+    {4, 16, 64}, a seeded camera and, for a quarter of them, the denoise flag (two half renders blended with their denoise).  The
     denoiser's weights are its initialisation: request latency does not
     depend on their values.  Reports latency percentiles (arrival to
     finish), Msamples/s, the rejection and queueing rates and the scene
@@ -658,7 +658,7 @@ def run_serve(args):
 
     rng = np.random.default_rng(7)
     srv = Server(slots=args.serve_slots, frames_per_chunk=args.serve_chunk, max_batch=8,
-                 max_queue=args.serve_max_queue, memory_budget=150 << 30)
+                 max_queue=args.serve_max_queue, memory_budget=int(args.serve_budget_gb * (1 << 30)))
     t0 = time.time()
     pool = []
     for k, (n, lvl) in enumerate(SERVE_CATALOG):
@@ -692,7 +692,7 @@ def run_serve(args):
                                    "512^2 / 1280x720 / 1920x1080, 4 / 16 / 64 spp, depth 12, "
                                    f"{args.serve_denoise_frac:.0%} denoised",
                        "slots": args.serve_slots, "frames_per_chunk": args.serve_chunk,
-                       "max_queue": args.serve_max_queue, "memory_budget_gb": 150,
+                       "max_queue": args.serve_max_queue, "memory_budget_gb": args.serve_budget_gb,
                        "scene_triangles": [p[2] for p in pool], "scene_generation_s": gen_s},
             **out, "denoised_requests": int(sum(flags)), "server_stats": st}
     print(json.dumps(line), flush=True)
@@ -811,6 +811,8 @@ def main():
     ap.add_argument("--serve-slots", type=int, default=3)
     ap.add_argument("--serve-chunk", type=int, default=16)
     ap.add_argument("--serve-max-queue", type=int, default=256)
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0,
+                    help="device memory budget for scenes and films (a small one makes the server drop and rebuild)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
