@@ -164,15 +164,7 @@ inline void widen(Aabb& b) {
 }
 
 void setChild(BvhNode& n, int side, const Aabb& b, int32_t ref) {
-  float* xs = &n.xs.x;
-  float* ys = &n.ys.x;
-  float* zs = &n.zs.x;
-  xs[2 * side] = b.lo[0];
-  xs[2 * side + 1] = b.hi[0];
-  ys[2 * side] = b.lo[1];
-  ys[2 * side + 1] = b.hi[1];
-  zs[2 * side] = b.lo[2];
-  zs[2 * side + 1] = b.hi[2];
+  nodeSetBox(n, side, b.lo, b.hi);
   (side == 0 ? n.ref.x : n.ref.y) = ref;
 }
 

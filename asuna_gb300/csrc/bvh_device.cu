@@ -110,15 +110,7 @@ __device__ __forceinline__ void widen(float& lo, float& hi) {
 __device__ __forceinline__ void setChild(BvhNode* n, int side, const float* blo, const float* bhi, int32_t ref) {
   float lo[3] = {blo[0], blo[1], blo[2]}, hi[3] = {bhi[0], bhi[1], bhi[2]};
   for (int k = 0; k < 3; ++k) widen(lo[k], hi[k]);
-  float* xs = &n->xs.x;
-  float* ys = &n->ys.x;
-  float* zs = &n->zs.x;
-  xs[2 * side] = lo[0];
-  xs[2 * side + 1] = hi[0];
-  ys[2 * side] = lo[1];
-  ys[2 * side + 1] = hi[1];
-  zs[2 * side] = lo[2];
-  zs[2 * side + 1] = hi[2];
+  nodeSetBox(*n, side, lo, hi);
   (side == 0 ? n->ref.x : n->ref.y) = ref;
 }
 
@@ -826,9 +818,7 @@ int buildBlasDevice(const VtxDev* vtx, const uint4* idx, const std::vector<uint3
     const int32_t r = int32_t(rootInit.size());
     out.roots[m] = r;
     BvhNode e{};
-    e.xs = make_float4(1e30f, 1e30f, 1e30f, 1e30f);
-    e.ys = e.xs;
-    e.zs = e.xs;
+    e.xy[0] = e.xy[1] = e.zs = make_float4(1e30f, 1e30f, 1e30f, 1e30f);
     e.ref = make_int4(kStackSentinel, kStackSentinel, 0, 0);
     rootInit.push_back(e);
     BTask t{};

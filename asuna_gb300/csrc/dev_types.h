@@ -13,16 +13,37 @@
 namespace asuna {
 
 // ---- acceleration structure -------------------------------------------------
-// Binary BVH node, 64 B: the two child boxes as x/y/z slab quads, then the
-// child references.  ref >= 0: inner node index; ref < 0: leaf, decoded by
-// leafFirst/leafCount (BLAS: first triangle, count <= 8; TLAS: instance).
+// Binary BVH node, 64 B: the two child boxes, then the child references.
+// ref >= 0: inner node index; ref < 0: leaf, decoded by leafFirst/leafCount
+// (BLAS: first triangle, count <= 8; TLAS: instance).  The planes are laid
+// out in (x, y) pairs and a z quad, so the traversal computes the six slab
+// distances of a child with three packed two-lane operations against the
+// ray's (o.x, o.y) / (o.z, o.z) pairs.
 struct __align__(16) BvhNode {
-  float4 xs;  // c0.lo.x, c0.hi.x, c1.lo.x, c1.hi.x
-  float4 ys;
-  float4 zs;
-  int4 ref;   // c0, c1, unused, unused
+  float4 xy[2];  // child c: lo.x, lo.y, hi.x, hi.y
+  float4 zs;     // c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z
+  int4 ref;      // c0, c1, unused, unused
 };
 static_assert(sizeof(BvhNode) == 64, "BvhNode is 64 bytes");
+
+inline __host__ __device__ void nodeSetBox(BvhNode& n, int c, const float* lo, const float* hi) {
+  n.xy[c].x = lo[0];
+  n.xy[c].y = lo[1];
+  n.xy[c].z = hi[0];
+  n.xy[c].w = hi[1];
+  float* z = &n.zs.x;
+  z[2 * c] = lo[2];
+  z[2 * c + 1] = hi[2];
+}
+inline __host__ __device__ void nodeGetBox(const BvhNode& n, int c, float* lo, float* hi) {
+  const float* z = &n.zs.x;
+  lo[0] = n.xy[c].x;
+  lo[1] = n.xy[c].y;
+  lo[2] = z[2 * c];
+  hi[0] = n.xy[c].z;
+  hi[1] = n.xy[c].w;
+  hi[2] = z[2 * c + 1];
+}
 
 constexpr int kMaxLeafTris = 8;
 constexpr int32_t kStackSentinel = INT32_MIN;  // "leave the BLAS" marker

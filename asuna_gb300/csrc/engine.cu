@@ -464,14 +464,15 @@ int asuna_scene_create(asuna_ctx* c, const asuna_scene_desc* d, asuna_scene** ou
     if (empty) continue;
     // world box of the BLAS root's children
     const BvhNode& r = rootNode[m];
-    float lo[3] = {r.xs.x, r.ys.x, r.zs.x}, hi[3] = {r.xs.y, r.ys.y, r.zs.y};
+    float lo[3], hi[3];
+    nodeGetBox(r, 0, lo, hi);
     if (r.ref.y != kStackSentinel) {
-      lo[0] = std::min(lo[0], r.xs.z);
-      hi[0] = std::max(hi[0], r.xs.w);
-      lo[1] = std::min(lo[1], r.ys.z);
-      hi[1] = std::max(hi[1], r.ys.w);
-      lo[2] = std::min(lo[2], r.zs.z);
-      hi[2] = std::max(hi[2], r.zs.w);
+      float lo1[3], hi1[3];
+      nodeGetBox(r, 1, lo1, hi1);
+      for (int k = 0; k < 3; ++k) {
+        lo[k] = std::min(lo[k], lo1[k]);
+        hi[k] = std::max(hi[k], hi1[k]);
+      }
     }
     Aabb wb;
     for (int k = 0; k < 3; ++k) {

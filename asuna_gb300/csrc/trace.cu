@@ -10,7 +10,8 @@
 // Persistent warps fetch 32 rays at a time from the queue (one atomic per
 // warp); each thread walks TLAS -> BLAS with a per-thread stack in shared
 // memory (entry k of thread t at sstack[k * 128 + t], bank-conflict free).
-// Node and triangle records are read with 128-bit read-only loads.  The ray
+// Node and triangle records are read with 128-bit read-only loads; the slab
+// distances of a node are computed with packed two-lane (f32x2) arithmetic.  The ray
 // is moved into object space and tested against triangles with the watertight
 // algorithm of Woop, Benthin and Wald (JCGT 2013) using explicitly rounded
 // operations, so the hits equal the CPU oracle's bit for bit; box tests use
@@ -96,9 +97,42 @@ __device__ __forceinline__ float fmax3(float a, float b, float c) {
   return r;
 }
 
+// Inverse direction for the slab tests, from the hardware reciprocal
+// (rcp.approx, within one ulp of 1/x for the normal values it is given):
+// the box tests stay conservative, as the far distance is widened by 2^-20
+// (16 ulp), far more than the reciprocal's error; hits come from the
+// watertight triangle test alone, so they do not depend on it.
+__device__ __forceinline__ float rcpApprox(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+// (magnitudes clamped to [1e-30, 1e30], so the reciprocal stays a normal
+// number that the flush-to-zero form returns unchanged)
 __device__ __forceinline__ float3 safeInv(float3 d) {
-  auto inv = [](float x) { return 1.0f / (fabsf(x) > 1e-30f ? x : copysignf(1e-30f, x)); };
+  auto inv = [](float x) { return rcpApprox(copysignf(fminf(fmaxf(fabsf(x), 1e-30f), 1e30f), x)); };
   return make_float3(inv(d.x), inv(d.y), inv(d.z));
+}
+
+// Packed pairs of IEEE single-precision values in one 64-bit register pair:
+// the f32x2 add / mul of sm_100 and later issue as one instruction and round
+// each lane to nearest, like the scalar operations they replace, so the slab
+// distances are bit-identical to (plane - o) * (1/d) computed one by one.
+typedef unsigned long long F2;
+__device__ __forceinline__ F2 pack2(float a, float b) {
+  F2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void unpack2(F2 p, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(p));
+}
+// (planes - o) * inv, lane by lane; returns the two distances
+__device__ __forceinline__ void slab2(F2 planes, F2 o, F2 inv, float& t0, float& t1) {
+  F2 d, t;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(planes), "l"(o));
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(t) : "l"(d), "l"(inv));
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(t0), "=f"(t1) : "l"(t));
 }
 
 __device__ __forceinline__ void xformRay(const float4* w, float3 o, float3 d, float3& oo, float3& dd) {
@@ -132,8 +166,9 @@ struct HitOut {
 // then tests the triangles of one leaf, or makes one TLAS/BLAS transition.
 template <int TB, int SHS>  // threads per block, stack entries in shared memory
 struct Trav {
-  float3 wo, wd, wid;  // world-space ray and its inverse direction
-  float3 o, id;        // ray origin / inverse direction in the current space
+  float3 wo, wd;  // world-space ray
+  F2 oxy, oz2;    // ray origin in the current space: (o.x, o.y), (o.z, o.z)
+  F2 ixy, iz2;    // inverse direction in the current space, likewise
   WT wt;
   float tmin, best;
   uint32_t curInst;
@@ -145,9 +180,7 @@ struct Trav {
   __device__ __forceinline__ void init(const SceneDev& S, float3 ro, float3 rd, float t0, float t1) {
     wo = ro;
     wd = rd;
-    wid = safeInv(rd);
-    o = ro;
-    id = wid;
+    setSpace(ro, safeInv(rd));
     tmin = t0;
     best = t1;
     curInst = 0;
@@ -156,6 +189,19 @@ struct Trav {
     leaf = kNoLeaf;
     found = false;
     inBlas = false;
+  }
+
+  __device__ __forceinline__ void setSpace(float3 o, float3 inv) {
+    oxy = pack2(o.x, o.y);
+    oz2 = pack2(o.z, o.z);
+    ixy = pack2(inv.x, inv.y);
+    iz2 = pack2(inv.z, inv.z);
+  }
+  __device__ __forceinline__ float3 origin() const {
+    float x, y, z, z2;
+    unpack2(oxy, x, y);
+    unpack2(oz2, z, z2);
+    return make_float3(x, y, z);
   }
 
   // Stack: the first SHS entries in shared memory (stride TB: bank-conflict
@@ -181,15 +227,20 @@ struct Trav {
   __device__ __forceinline__ void innerStep(const SceneDev& S, int32_t* sh, int32_t* loc, uint32_t& nNodes,
                                             bool& ovf) {
     const BvhNode* n = S.nodes + ref;
-    const float4 xs = __ldg(&n->xs), ys = __ldg(&n->ys), zs = __ldg(&n->zs);
+    // the 16-byte plane records as pairs: (lo.x, lo.y), (hi.x, hi.y) of
+    // each child; (lo.z, hi.z) of child 0, of child 1
+    const ulonglong2 c0 = __ldg(reinterpret_cast<const ulonglong2*>(&n->xy[0]));
+    const ulonglong2 c1 = __ldg(reinterpret_cast<const ulonglong2*>(&n->xy[1]));
+    const ulonglong2 zs = __ldg(reinterpret_cast<const ulonglong2*>(&n->zs));
     const int4 rr = __ldg(&n->ref);
     if (COUNT) ++nNodes;
-    const float tx0 = (xs.x - o.x) * id.x, tx1 = (xs.y - o.x) * id.x;
-    const float ty0 = (ys.x - o.y) * id.y, ty1 = (ys.y - o.y) * id.y;
-    const float tz0 = (zs.x - o.z) * id.z, tz1 = (zs.y - o.z) * id.z;
-    const float ux0 = (xs.z - o.x) * id.x, ux1 = (xs.w - o.x) * id.x;
-    const float uy0 = (ys.z - o.y) * id.y, uy1 = (ys.w - o.y) * id.y;
-    const float uz0 = (zs.z - o.z) * id.z, uz1 = (zs.w - o.z) * id.z;
+    float tx0, tx1, ty0, ty1, tz0, tz1, ux0, ux1, uy0, uy1, uz0, uz1;
+    slab2(c0.x, oxy, ixy, tx0, ty0);
+    slab2(c0.y, oxy, ixy, tx1, ty1);
+    slab2(zs.x, oz2, iz2, tz0, tz1);
+    slab2(c1.x, oxy, ixy, ux0, uy0);
+    slab2(c1.y, oxy, ixy, ux1, uy1);
+    slab2(zs.y, oz2, iz2, uz0, uz1);
     const float a0 = fmax3(fminf(tx0, tx1), fminf(ty0, ty1), fmaxf(fminf(tz0, tz1), tmin));
     const float a1 = fmin3(fmaxf(tx0, tx1), fmaxf(ty0, ty1), fminf(fmaxf(tz0, tz1), best)) * kFarScale;
     const float b0 = fmax3(fminf(ux0, ux1), fminf(uy0, uy1), fmaxf(fminf(uz0, uz1), tmin));
@@ -229,7 +280,7 @@ struct Trav {
         const float4 p0 = __ldg(&tr->v0), p1 = __ldg(&tr->v1), p2 = __ldg(&tr->v2);
         if (COUNT) ++nTris;
         float t, b1, b2;
-        if (wtTri(wt, o, p0, p1, p2, tmin, best, t, b1, b2)) {
+        if (wtTri(wt, origin(), p0, p1, p2, tmin, best, t, b1, b2)) {
           if (ANY) {
             found = true;
             return true;
@@ -254,8 +305,7 @@ struct Trav {
     if (ref == kStackSentinel) {
       // leaving a BLAS: back to the world-space ray
       inBlas = false;
-      o = wo;
-      id = wid;
+      setSpace(wo, safeInv(wd));
       ref = popOrDone(sh, loc);
       return false;
     }
@@ -264,9 +314,9 @@ struct Trav {
     const InstDev* in = S.inst + curInst;
     const int32_t root = __ldg(&in->blasRoot);
     if (root >= 0 && sp < lim) {
-      float3 d;
+      float3 o, d;
       xformRay(in->w2o, wo, wd, o, d);
-      id = safeInv(d);
+      setSpace(o, safeInv(d));
       wt = wtPre(d);
       inBlas = true;
       push(sh, loc, kStackSentinel, ovf);

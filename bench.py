@@ -435,14 +435,19 @@ def run_denoise_rmse(args):
     subset of the 1080p workload at 262,144 spp, tests/golden) for the plain
     wavefront path and for the denoised path.
 
-    Plain: progressive doubling of the sample count; RMSE on the subset with
-    the reference's own variance subtracted; the time at RMSE 0.01 is
-    interpolated on the 1/sqrt(spp) law from the first count that reaches it.
+    Plain: progressive rendering, the sample count doubling rung by rung;
+    RMSE on the subset with the reference's own variance subtracted.
     Denoised: two progressive films A and B on disjoint frames; the output
     blends the denoise of all their samples with their plain average at the
     weight that minimises the error estimated from the two halves
     (asuna_denoise_blended; weight 0 is the plain path).  Its time
-    counts every render and every estimate.  The network is trained first,
+    counts every render and every estimate.  Both ladders step alike: once
+    a rung's error is within 4x of the target, the next rung is the count
+    the 1/sqrt(spp) law predicts for the target from that rung (plus 2%, at
+    most double), so each path stops at the first measured rung below the
+    target, close to its crossing; the time at the target is that rung's.
+    The other targets' times are interpolated on the same law between the
+    rungs around them, for both paths alike.  The network is trained first,
     on the GPU, on pairs the renderer makes of other seeded scenes of the
     same recipe (inputs at several sample counts, a high-count target)."""
     import torch
@@ -501,22 +506,28 @@ def run_denoise_rmse(args):
             f += k
         return ms
 
-    # 2a. plain path
+    def next_count(n, e, lo):
+        # doubling, or near the target the 1/sqrt(spp) prediction (+2%)
+        nxt = max(lo, 2 * n)
+        if n and e < 4 * target:
+            nxt = min(nxt, max(n + 1, int(np.ceil(n * (e / target) ** 2 * 1.02))))
+        return nxt
+
+    # 2a. plain path (clocks sampled from here through both ladders)
+    clk = ClockSampler(int(os.environ.get("LOCAL_RANK", 0))).__enter__()
     film = ctx.create_film(W, H)
-    plain, spp, ms = [], 0, 0.0
+    plain, spp, ms, e = [], 0, 0.0, float("inf")
+    t_plain = None
     while spp < args.plain_max_spp:
-        nxt = max(16, 2 * spp)
+        nxt = min(next_count(spp, e, 16), args.plain_max_spp)
         ms += render_frames(film, spp, nxt - spp, 0)
         spp = nxt
         e = rmse(film.read(0))
         plain.append({"spp": spp, "seconds": ms / 1e3, "rmse": e})
         if e <= target:
+            t_plain = ms / 1e3
             break
-    last = plain[-1]
-    spp_star = last["spp"] * (last["rmse"] / target) ** 2  # 1/sqrt(spp) law
-    t_plain = last["seconds"] / last["spp"] * spp_star
-    out["plain"] = {"ladder": plain, "spp_at_target": spp_star, "seconds_at_target": t_plain,
-                    "reached": last["rmse"] <= target}
+    out["plain"] = {"ladder": plain, "seconds_at_target": t_plain, "reached": t_plain is not None}
     # 2b. denoised path: the all-sample denoise blended with the plain
     # average at the weight that minimises the error estimate (weight 0 is the
     # plain path); the denoiser's first calls (workspace, weight staging) run
@@ -532,10 +543,10 @@ def run_denoise_rmse(args):
     fa.clear()
     fb.clear()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    dres, half, ms = [], 0, 0.0
+    dres, half, ms, e = [], 0, 0.0, float("inf")
     t_den = None
     while 2 * half < args.denoise_max_spp:
-        nh = max(2, 2 * half)
+        nh = min((next_count(2 * half, e, 4) + 1) // 2, args.denoise_max_spp // 2)
         ms += render_frames(fa, half, nh - half, 0)
         ms += render_frames(fb, half, nh - half, 7)
         half = nh
@@ -558,15 +569,30 @@ def run_denoise_rmse(args):
         if e <= target:
             t_den = ms / 1e3
             break
+    clk.__exit__(None, None, None)
+    out["clocks"] = clk.summary()
     out["denoised"] = {"ladder": dres, "seconds_at_target": t_den, "reached": t_den is not None}
-    # the same ladders at other targets: plain by the 1/sqrt(spp) law from its
-    # last rung; denoised = the first rung whose blended output is below it
+    # the other targets: the time between the two rungs around the target,
+    # interpolated on the 1/sqrt(spp) law (error linear in 1/sqrt(spp),
+    # seconds proportional to spp), for both ladders; the main target is the
+    # measured rung
+    def at(ladder, tgt):
+        for i, r in enumerate(ladder):
+            if r["rmse"] <= tgt:
+                if i == 0 or tgt == target:
+                    return r["seconds"], "measured"
+                p = ladder[i - 1]
+                x0, x1 = p["spp"] ** -0.5, r["spp"] ** -0.5
+                x = x1 + (tgt - r["rmse"]) * (x0 - x1) / (p["rmse"] - r["rmse"])
+                return r["seconds"] / r["spp"] * x ** -2, "interpolated"
+        return None, None
+
     rows = []
     for tgt in (0.05, 0.03, 0.02, target):
-        tp = last["seconds"] / last["spp"] * last["spp"] * (last["rmse"] / tgt) ** 2
-        td = next((r["seconds"] for r in dres if r["rmse"] <= tgt), None)
+        tp, kp = at(plain, tgt)
+        td, kd = at(dres, tgt)
         rows.append({"rmse": tgt, "plain_seconds": tp, "denoised_seconds": td,
-                     "speedup": (tp / td) if td else None})
+                     "speedup": (tp / td) if (tp and td) else None, "how": kd or kp})
     out["targets"] = rows
     # denoiser forward throughput at 1080p
     with torch.cuda.stream(stream):
@@ -581,7 +607,7 @@ def run_denoise_rmse(args):
     fl = dn.forward_flops(dn.DEFAULT_CHANNELS, (H + 15) // 16 * 16, (W + 15) // 16 * 16)
     out["denoiser_forward"] = {"ms": fwd_ms, "tflops": fl / (fwd_ms * 1e-3) / 1e12, "flop": fl}
     out["value"] = t_den
-    out["speedup"] = (t_plain / t_den) if t_den else None
+    out["speedup"] = (t_plain / t_den) if (t_plain and t_den) else None
     print(json.dumps(out), flush=True)
     return 0
 
