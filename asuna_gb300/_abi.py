@@ -172,6 +172,7 @@ SIGNATURES = [
     ("asuna_ctx_set_traversal_stack", C.c_int, [P, C.c_int]),
     ("asuna_ctx_set_bvh_build", C.c_int, [P, C.c_int]),
     ("asuna_ctx_set_traversal_shape", C.c_int, [P, C.c_int, C.c_int]),
+    ("asuna_ctx_set_traversal_occupancy", C.c_int, [P, C.c_int, C.c_int]),
     ("asuna_scene_create", C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(P)]),
     ("asuna_sun_and_sky_default", None, [C.POINTER(SunAndSky)]),
     ("asuna_scene_validate", C.c_int, [C.POINTER(SceneDesc)]),

@@ -18,11 +18,12 @@ def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64, 128), t
          frame_base=1 << 20):
     """Returns {"frames": f, "trace_blocks_per_sm": t, "shade_blocks_per_sm": s, "traversal": (refill
     extend, refill shadow, speculate extend, speculate shadow, traversal blocks per SM), "shape": (threads
-    per block, shared-memory stack entries), "ray_sort": 0..3, "mrays": best, "trials": [...]} and leaves
-    the context configured with the best choice.  Coordinate search: frames, then grids, then the
-    traversal kernel variant and the refill thresholds and speculation of each pass, then extend-queue
-    sorting, then the refill thresholds again under it, then the traversal block size and the
-    traversal stack's shared-memory depth."""
+    per block, shared-memory stack entries), "shadow_occupancy": the occlusion pass's blocks per SM,
+    "ray_sort": 0..3, "mrays": best, "trials": [...]} and leaves the context configured with the best
+    choice.  Coordinate search: frames, then grids, then the traversal kernel variant and the refill
+    thresholds and speculation of each pass, then extend-queue sorting, then the refill thresholds again
+    under it, then the traversal block size and the traversal stack's shared-memory depth, then the
+    occlusion pass's kernel variant on its own."""
     npix = shot.width * shot.height
     saved = (shot.frame0, shot.frames)
     trials = []
@@ -33,6 +34,9 @@ def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64, 128), t
 
     def run(frames, t, s):
         ctx.set_traversal(*trav)
+        return run_set(frames, t, s)
+
+    def run_set(frames, t, s):  # with the traversal settings already made
         ctx.set_launch(t, s)
         ctx.set_path_budget(max(frames * npix * BYTES_PER_PATH, 1))
         shot.frames = frames
@@ -102,9 +106,26 @@ def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64, 128), t
             trials.append({"frames": best["frames"], "shape": shape, "mrays": v})
             if v > best["mrays"]:
                 best = {**best, "shape": shape, "mrays": v}
+        ctx.set_traversal_shape(*best["shape"])
+        # the occlusion pass's kernel variant apart from the extend pass's
+        # (shorter queues, no hit record to keep: its best occupancy differs)
+        trav = list(best["traversal"])
+        ext = trav[4]
+        best["shadow_occupancy"] = ext
+        for occ in occupancy_options:
+            if occ == ext:
+                continue
+            ctx.set_traversal(*trav)
+            ctx.set_traversal_occupancy(ext, occ)
+            v = run_set(best["frames"], best["trace_blocks_per_sm"], best["shade_blocks_per_sm"])
+            trials.append({"frames": best["frames"], "shadow_occupancy": occ, "mrays": v})
+            if v > best["mrays"]:
+                best = {**best, "shadow_occupancy": occ, "mrays": v}
     finally:
         shot.frame0, shot.frames = saved
     ctx.set_traversal(*best["traversal"])
+    if "shadow_occupancy" in best:
+        ctx.set_traversal_occupancy(best["traversal"][4], best["shadow_occupancy"])
     ctx.set_traversal_shape(*best.get("shape", (0, 0)))
     ctx.set_launch(best["trace_blocks_per_sm"], best["shade_blocks_per_sm"])
     ctx.set_path_budget(best["frames"] * npix * BYTES_PER_PATH)

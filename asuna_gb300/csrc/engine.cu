@@ -184,7 +184,7 @@ int asuna_ctx_create(int device_ordinal, asuna_ctx** out) {
   }
   *c->hostErr = 0;
   cudaMemset(c->cnt, 0, sizeof(DevCounters));
-  c->traceGrid = c->numSMs * traceBlocksPerSm();
+  c->traceGrid = c->traceGridShadow = c->numSMs * traceBlocksPerSm();
   c->shadeGrid = c->numSMs * shadeBlocksPerSm();
   c->raygenGrid = c->numSMs * 16;
   *out = c;
@@ -232,17 +232,28 @@ int asuna_ctx_set_ray_sort(asuna_ctx* c, int enable) {
   return ASUNA_OK;
 }
 
+namespace {
+// Persistent traversal grids of the two passes: every resident block of the
+// pass's kernel variant, capped by asuna_ctx_set_launch's blocks per SM.
+void updateTraceGrids(asuna_ctx* c) {
+  auto grid = [&](int occ) {
+    const int m = traceBlocksPerSm(occ, c->traceThreads, c->sharedStack);
+    return c->numSMs * (c->traceBlocksCap > 0 ? std::min(c->traceBlocksCap, m) : m);
+  };
+  c->traceGrid = grid(c->occupancy);
+  c->traceGridShadow = grid(c->occupancyShadow);
+}
+bool validOccupancy(int b) { return b == 0 || b == 8 || b == 10 || b == 12; }
+}  // namespace
+
 int asuna_ctx_set_traversal(asuna_ctx* c, int refillExtend, int refillShadow, int specExtend, int specShadow,
                             int blocksPerSm) {
   clearError();
   if (!c) return fail(ASUNA_ERR_INVALID, "null context");
-  if (blocksPerSm != 0 && blocksPerSm != 8 && blocksPerSm != 10 && blocksPerSm != 12)
+  if (!validOccupancy(blocksPerSm))
     return fail(ASUNA_ERR_INVALID, "traversal blocks per SM %d not in {0, 8, 10, 12}", blocksPerSm);
-  const int occ = blocksPerSm == 0 ? kTraceMinBlocks : blocksPerSm;
-  if (occ != c->occupancy) {
-    c->occupancy = occ;
-    c->traceGrid = c->numSMs * traceBlocksPerSm(occ, c->traceThreads, c->sharedStack);
-  }
+  c->occupancy = c->occupancyShadow = blocksPerSm == 0 ? kTraceMinBlocks : blocksPerSm;
+  updateTraceGrids(c);
   const int r[2] = {refillExtend, refillShadow}, sp[2] = {specExtend, specShadow};
   for (int k = 0; k < 2; ++k) {
     if (r[k] < 0 || r[k] > 32) return fail(ASUNA_ERR_INVALID, "refill lanes %d not in [0, 32]", r[k]);
@@ -250,6 +261,18 @@ int asuna_ctx_set_traversal(asuna_ctx* c, int refillExtend, int refillShadow, in
     c->refill[k] = r[k] == 0 ? uint32_t(kRefillLanes) : uint32_t(r[k]);
     c->speculate[k] = sp[k] < 0 ? 1 : sp[k];
   }
+  return ASUNA_OK;
+}
+
+int asuna_ctx_set_traversal_occupancy(asuna_ctx* c, int extendBlocksPerSm, int shadowBlocksPerSm) {
+  clearError();
+  if (!c) return fail(ASUNA_ERR_INVALID, "null context");
+  if (!validOccupancy(extendBlocksPerSm) || !validOccupancy(shadowBlocksPerSm))
+    return fail(ASUNA_ERR_INVALID, "traversal blocks per SM %d / %d not in {0, 8, 10, 12}", extendBlocksPerSm,
+                shadowBlocksPerSm);
+  c->occupancy = extendBlocksPerSm == 0 ? kTraceMinBlocks : extendBlocksPerSm;
+  c->occupancyShadow = shadowBlocksPerSm == 0 ? kTraceMinBlocks : shadowBlocksPerSm;
+  updateTraceGrids(c);
   return ASUNA_OK;
 }
 
@@ -279,16 +302,16 @@ int asuna_ctx_set_traversal_shape(asuna_ctx* c, int threadsPerBlock, int sharedS
     return fail(ASUNA_ERR_INVALID, "shared stack of %d entries not in {0, 16, 24, 32}", sharedStack);
   c->traceThreads = threadsPerBlock ? threadsPerBlock : kTraceThreads;
   c->sharedStack = sharedStack ? sharedStack : kSharedStack;
-  c->traceGrid = c->numSMs * traceBlocksPerSm(c->occupancy, c->traceThreads, c->sharedStack);
+  updateTraceGrids(c);
   return ASUNA_OK;
 }
 
 int asuna_ctx_set_launch(asuna_ctx* c, int traceBlocks, int shadeBlocks) {
   if (!c) return fail(ASUNA_ERR_INVALID, "null context");
-  const int tmax = traceBlocksPerSm(c->occupancy, c->traceThreads, c->sharedStack), smax = shadeBlocksPerSm();
-  const int t = traceBlocks <= 0 ? tmax : std::min(traceBlocks, tmax);
+  const int smax = shadeBlocksPerSm();
   const int sh = shadeBlocks <= 0 ? smax : std::min(shadeBlocks, smax);
-  c->traceGrid = c->numSMs * t;
+  c->traceBlocksCap = traceBlocks > 0 ? traceBlocks : 0;
+  updateTraceGrids(c);
   c->shadeGrid = c->numSMs * sh;
   return ASUNA_OK;
 }
@@ -845,7 +868,8 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
            uint64_t(uintptr_t(dShots)), uint64_t(uintptr_t(dRanges)), uint64_t(c->traceGrid), uint64_t(c->shadeGrid),
            uint64_t(c->raygenGrid), uint64_t(c->counters), uint64_t(stats ? 1 : 0), uint64_t(c->refill[0]),
            uint64_t(c->refill[1]), uint64_t(c->speculate[0]), uint64_t(c->speculate[1]), uint64_t(c->occupancy),
-           uint64_t(c->raySort), uint64_t(c->stackLimit), uint64_t(c->traceThreads), uint64_t(c->sharedStack)});
+           uint64_t(c->raySort), uint64_t(c->stackLimit), uint64_t(c->traceThreads), uint64_t(c->sharedStack),
+           uint64_t(c->occupancyShadow), uint64_t(c->traceGridShadow)});
     for (const Batch& b : batches)
       key.insert(key.end(), {b.rangeBegin, b.rangeEnd, b.paths, b.maxPix, uint64_t(b.maxDepth)});
     for (auto& g : c->gcache)
@@ -905,7 +929,8 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
       timedLaunch(1, [&] { launchShade(P, c->shadeGrid, c->stream); });
       P.refillLanes = c->refill[1];
       P.speculate = c->speculate[1];
-      timedLaunch(2, [&] { launchConnect(P, c->traceGrid, c->stream); });
+      P.occupancy = c->occupancyShadow;
+      timedLaunch(2, [&] { launchConnect(P, c->traceGridShadow, c->stream); });
       P.cur ^= 1;
     }
     launchAccumulate(P, b.maxPix, P.W.numRanges, c->stream);

@@ -27,6 +27,8 @@ struct asuna_ctx {
   cudaStream_t stream = nullptr;
   int numSMs = 0;
   int traceGrid = 0, shadeGrid = 0, raygenGrid = 0;
+  int traceGridShadow = 0;  // the occlusion pass's traversal grid
+  int traceBlocksCap = 0;   // asuna_ctx_set_launch's traversal blocks per SM (0 = all that fit)
   asuna::DevCounters* cnt = nullptr;
   asuna::DevCounters* hostCnt = nullptr;
   WaveAlloc wave;
@@ -43,6 +45,7 @@ struct asuna_ctx {
   uint32_t refill[2] = {8, 8};
   int32_t speculate[2] = {1, 1};
   int32_t occupancy = 8;  // traversal kernel variant: resident 128-thread blocks per SM (8, 10, 12)
+  int32_t occupancyShadow = 8;  // the same for the occlusion pass
   int32_t traceThreads = 128;  // traversal kernel variant: threads per block
   int32_t sharedStack = 24;    // traversal kernel variant: stack entries in shared memory
   int32_t raySort = 3;    // extend-queue sort mode before secondary passes (0 off)

@@ -609,6 +609,13 @@ class Context:
         do not depend on them."""
         check(lib().asuna_ctx_set_traversal_shape(self.handle, int(threads_per_block), int(shared_stack)))
 
+    def set_traversal_occupancy(self, extend_blocks_per_sm=0, shadow_blocks_per_sm=0):
+        """Traversal kernel variant (resident blocks per SM: 8, 10, 12; 0 = 8)
+        of the extend and occlusion passes separately.  Results do not depend
+        on them."""
+        check(lib().asuna_ctx_set_traversal_occupancy(self.handle, int(extend_blocks_per_sm),
+                                                      int(shadow_blocks_per_sm)))
+
     def set_traversal_stack(self, entries=0):
         """Caps the traversal stack per ray (0 = the full 64 entries); a
         traversal needing more is cut short and reported as ERR_TRAVERSAL."""

@@ -379,6 +379,11 @@ int asuna_ctx_set_traversal(asuna_ctx* ctx, int refill_extend, int refill_shadow
  * of the 64 in thread-local memory); 0 = 128 / 24.  Results do not depend
  * on them. */
 int asuna_ctx_set_traversal_shape(asuna_ctx* ctx, int threads_per_block, int shared_stack_entries);
+/* The traversal kernel variant's resident blocks per SM of the closest-hit
+ * (extend) and occlusion (shadow) passes separately (8, 10 or 12; 0 = 8);
+ * asuna_ctx_set_traversal sets both to its value.  Results do not depend on
+ * them. */
+int asuna_ctx_set_traversal_occupancy(asuna_ctx* ctx, int extend_blocks_per_sm, int shadow_blocks_per_sm);
 /* Reorders the extend queue before every secondary pass by direction and
  * origin so warps carry rays that walk alike: 0 off, 1 octant x 4 x 4 x 4
  * origin cells, 2 octant x 8 x 8 x 8 cells in Morton order, 3 the same with

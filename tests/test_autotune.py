@@ -20,6 +20,11 @@ class FakeCtx:
 
     def set_traversal(self, *t):
         self.trav = tuple(t)
+        self.shadow_occ = t[4] if len(t) > 4 else 0
+
+    def set_traversal_occupancy(self, extend, shadow):
+        self.trav = self.trav[:4] + (extend,)
+        self.shadow_occ = shadow
 
     def set_launch(self, t, s):
         self.launch = (t, s)
@@ -36,7 +41,8 @@ class FakeCtx:
     def render(self, scene, shot, film, stats=False):
         self.renders.append((shot.frame0, shot.frames))
         mrays = self.score(shot.frames, self.launch, self.trav, self.sort) + \
-            {(0, 0): 0, (128, 32): 4, (64, 24): -2, (256, 24): 1, (128, 16): -1}[self.shape]
+            {(0, 0): 0, (128, 32): 4, (64, 24): -2, (256, 24): 1, (128, 16): -1}[self.shape] + \
+            {8: 0, 10: 1, 12: 2}[self.shadow_occ] - {8: 0, 10: 1, 12: 2}[self.trav[4]]
         rays = 1e6
         return {"extend_rays": rays, "shadow_rays": 0, "ms_total": rays / (mrays * 1e3)}
 
@@ -75,6 +81,8 @@ def test_tune_finds_the_optimum_and_restores_the_shot():
     assert ctx.trav == best["traversal"] and ctx.sort == 3 and ctx.launch == (0, 0)
     # block shape and shared stack depth: 128 threads, 32 entries
     assert best["shape"] == (128, 32) and ctx.shape == (128, 32)
+    # the occlusion pass's own kernel variant
+    assert best["shadow_occupancy"] == 12 and ctx.shadow_occ == 12 and ctx.trav[4] == 10
     assert ctx.budget == 16 * 64 * 32 * autotune.BYTES_PER_PATH
     assert (shot.frame0, shot.frames) == (5, 3) and film.cleared == 1
     # tuning frames never overlap the caller's sample streams

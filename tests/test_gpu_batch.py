@@ -97,6 +97,13 @@ def test_traversal_settings_do_not_change_results(ctx):
     ctx.set_traversal_shape()
     for f in films[1:]:
         assert np.array_equal(films[0], f)
+    # the two passes on different kernel variants
+    for ext, sh in ((8, 12), (12, 8), (10, 10)):
+        ctx.set_traversal_occupancy(ext, sh)
+        f = ctx.create_film(64, 48)
+        ctx.render(scene, shot, f)
+        assert np.array_equal(films[0], np.stack([f.read(i) for i in range(9)]))
+    ctx.set_traversal()
 
 
 def test_film_image_tensor_is_the_film(ctx):
