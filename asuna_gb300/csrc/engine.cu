@@ -888,7 +888,7 @@ static int renderImpl(asuna_ctx* c, const asuna_scene* s, const asuna_shot* shot
   P.W.shots = dShots;
   P.records = hostRecords ? 1 : 0;
   P.counters = c->counters;
-  P.stackLimit = c->stackLimit;
+  P.stackLimit = c->stackLimit > 0 && c->stackLimit < kStackDepth ? c->stackLimit : kStackDepth;
   for (const Batch& b : batches) {
     P.W.ranges = dRanges + b.rangeBegin;
     P.W.numRanges = b.rangeEnd - b.rangeBegin;

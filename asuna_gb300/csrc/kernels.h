@@ -16,7 +16,7 @@ struct KParams {
   uint32_t refillLanes;  // traversal: idle lanes of a warp that trigger a queue fetch
   int32_t speculate;     // traversal: postponed leaves walk on speculatively
   int32_t occupancy;     // traversal: resident blocks per SM of the kernel variant (8, 10 or 12)
-  int32_t stackLimit;    // traversal: stack entries a ray may use (<= kStackDepth)
+  int32_t stackLimit;    // traversal: stack entries a ray may use, in [1, kStackDepth] (the host clamps it)
   int32_t blockThreads;  // traversal: threads per block (64, 128, 256; 0 = 128)
   int32_t sharedStack;   // traversal: stack entries in shared memory (16, 24, 32; 0 = 24)
 };

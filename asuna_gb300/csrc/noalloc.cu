@@ -142,6 +142,7 @@ int renderNoAlloc(const asuna_scene* s, const asuna_shot* shot, asuna_film* film
   P.refillLanes = kRefillLanes;
   P.speculate = 1;
   P.occupancy = kTraceMinBlocks;
+  P.stackLimit = kStackDepth;
   WaveDev& W = P.W;
   float4* f16[12];
   for (int k = 0; k < 12; ++k) f16[k] = reinterpret_cast<float4*>(base + uint64_t(k) * kPerPath16);

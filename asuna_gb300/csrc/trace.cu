@@ -154,7 +154,7 @@ constexpr uint32_t kTraceRayCap = 1u << 16;            // leaves + transitions o
 __device__ __forceinline__ bool isLeafRef(int32_t r) { return r < 0 && r != kStackSentinel && r != kDone; }
 
 struct HitOut {
-  float t, u, v;
+  float u, v;  // (the distance is the traversal's `best`)
   uint32_t prim, inst;
 };
 
@@ -164,22 +164,43 @@ struct HitOut {
 // there is postponed and, when `speculate`, the lane goes on visiting inner
 // nodes while other lanes of the warp still look for a leaf.  leafOrMove()
 // then tests the triangles of one leaf, or makes one TLAS/BLAS transition.
+//
+// The state is kept small (the kernel is bound by the latency of its node
+// fetches, so resident warps matter): the world-space ray is read again from
+// its source at the few instance transitions instead of being held, the
+// watertight test's axis permutation is packed into one word, the closest
+// distance is `best`, and the stack cap comes from the launch.
 template <int TB, int SHS>  // threads per block, stack entries in shared memory
 struct Trav {
-  float3 wo, wd;  // world-space ray
-  F2 oxy, oz2;    // ray origin in the current space: (o.x, o.y), (o.z, o.z)
-  F2 ixy, iz2;    // inverse direction in the current space, likewise
-  WT wt;
+  F2 oxy, oz2;  // ray origin in the current space: (o.x, o.y), (o.z, o.z)
+  F2 ixy, iz2;  // inverse direction in the current space, likewise
+  float Sx, Sy, Sz;  // watertight shear of the current space's direction
+  uint32_t kxyz;     // its axis permutation, kx | ky << 2 | kz << 4
   float tmin, best;
   uint32_t curInst;
-  int sp, lim;  // stack entries in use / allowed
+  int sp;  // stack entries in use
   int32_t ref, leaf;
   bool found, inBlas;
   HitOut h;
 
+  __device__ __forceinline__ void setShear(const WT& w) {
+    Sx = w.Sx;
+    Sy = w.Sy;
+    Sz = w.Sz;
+    kxyz = uint32_t(w.kx) | uint32_t(w.ky) << 2 | uint32_t(w.kz) << 4;
+  }
+  __device__ __forceinline__ WT shear() const {
+    WT w;
+    w.kx = int(kxyz & 3u);
+    w.ky = int((kxyz >> 2) & 3u);
+    w.kz = int(kxyz >> 4);
+    w.Sx = Sx;
+    w.Sy = Sy;
+    w.Sz = Sz;
+    return w;
+  }
+
   __device__ __forceinline__ void init(const SceneDev& S, float3 ro, float3 rd, float t0, float t1) {
-    wo = ro;
-    wd = rd;
     setSpace(ro, safeInv(rd));
     tmin = t0;
     best = t1;
@@ -206,7 +227,7 @@ struct Trav {
 
   // Stack: the first SHS entries in shared memory (stride TB: bank-conflict
   // free), deeper ones in thread-local memory.
-  __device__ __forceinline__ void push(int32_t* sh, int32_t* loc, int32_t v, bool& ovf) {
+  __device__ __forceinline__ void push(int32_t* sh, int32_t* loc, int32_t v, int lim, bool& ovf) {
     if (sp >= lim) {
       ovf = true;
       return;
@@ -224,7 +245,7 @@ struct Trav {
   }
 
   template <bool COUNT>
-  __device__ __forceinline__ void innerStep(const SceneDev& S, int32_t* sh, int32_t* loc, uint32_t& nNodes,
+  __device__ __forceinline__ void innerStep(const SceneDev& S, int32_t* sh, int32_t* loc, int lim, uint32_t& nNodes,
                                             bool& ovf) {
     const BvhNode* n = S.nodes + ref;
     // the 16-byte plane records as pairs: (lo.x, lo.y), (hi.x, hi.y) of
@@ -248,7 +269,7 @@ struct Trav {
     const bool h0 = a0 <= a1, h1 = b0 <= b1;
     if (h0 && h1) {
       const bool swap = b0 < a0;
-      push(sh, loc, swap ? rr.x : rr.y, ovf);
+      push(sh, loc, swap ? rr.x : rr.y, lim, ovf);
       ref = swap ? rr.y : rr.x;
     } else if (h0 || h1) {
       ref = h0 ? rr.x : rr.y;
@@ -261,10 +282,11 @@ struct Trav {
     }
   }
 
-  // Returns true when the traversal is over.
-  template <bool ANY, bool COUNT>
-  __device__ __forceinline__ bool leafOrMove(const SceneDev& S, int32_t* sh, int32_t* loc, uint32_t& nTris,
-                                             bool& ovf) {
+  // Returns true when the traversal is over.  `src.world(i, o, d)` gives
+  // ray i's world-space origin and direction again.
+  template <bool ANY, bool COUNT, class Src>
+  __device__ __forceinline__ bool leafOrMove(const SceneDev& S, const Src& src, uint32_t idx, int32_t* sh,
+                                             int32_t* loc, int lim, uint32_t& nTris, bool& ovf) {
     int32_t L = kNoLeaf;
     if (leaf != kNoLeaf) {
       L = leaf;
@@ -275,12 +297,14 @@ struct Trav {
     }
     if (L != kNoLeaf) {
       const uint32_t first = leafFirst(L), cnt = leafCount(L);
+      const WT wt = shear();
+      const float3 o = origin();
       for (uint32_t k = 0; k < cnt; ++k) {
         const TriDev* tr = S.tris + first + k;
         const float4 p0 = __ldg(&tr->v0), p1 = __ldg(&tr->v1), p2 = __ldg(&tr->v2);
         if (COUNT) ++nTris;
         float t, b1, b2;
-        if (wtTri(wt, origin(), p0, p1, p2, tmin, best, t, b1, b2)) {
+        if (wtTri(wt, o, p0, p1, p2, tmin, best, t, b1, b2)) {
           if (ANY) {
             found = true;
             return true;
@@ -291,7 +315,6 @@ struct Trav {
           if (!found || t < best || (curInst < h.inst || (curInst == h.inst && prim < h.prim))) {
             found = true;
             best = t;
-            h.t = t;
             h.u = b1;
             h.v = b2;
             h.prim = prim;
@@ -305,6 +328,8 @@ struct Trav {
     if (ref == kStackSentinel) {
       // leaving a BLAS: back to the world-space ray
       inBlas = false;
+      float3 wo, wd;
+      src.world(idx, wo, wd);
       setSpace(wo, safeInv(wd));
       ref = popOrDone(sh, loc);
       return false;
@@ -314,12 +339,13 @@ struct Trav {
     const InstDev* in = S.inst + curInst;
     const int32_t root = __ldg(&in->blasRoot);
     if (root >= 0 && sp < lim) {
-      float3 o, d;
+      float3 wo, wd, o, d;
+      src.world(idx, wo, wd);
       xformRay(in->w2o, wo, wd, o, d);
       setSpace(o, safeInv(d));
-      wt = wtPre(d);
+      setShear(wtPre(d));
       inBlas = true;
-      push(sh, loc, kStackSentinel, ovf);
+      push(sh, loc, kStackSentinel, lim, ovf);
       ref = root;
       return false;
     }
@@ -336,13 +362,12 @@ struct Trav {
 // finish(i, tr).
 template <bool ANY, bool COUNT, bool SPEC, int TB, int SHS, class Src>
 __device__ __forceinline__ void traceWarp(const SceneDev& S, Src& src, int32_t* sh, int32_t* loc, uint32_t refill,
-                                          int stackLimit, uint32_t& nNodes, uint32_t& nTris, bool& ovf) {
+                                          int lim, uint32_t& nNodes, uint32_t& nTris, bool& ovf) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lanesBelow = (1u << lane) - 1u;
   bool active = false, drained = false;
   uint32_t idx = 0, events = 0;
   Trav<TB, SHS> tr;
-  tr.lim = stackLimit > 0 && stackLimit < kStackDepth ? stackLimit : kStackDepth;
   for (;;) {
     const unsigned idle = __ballot_sync(0xffffffffu, !active);
     if (idle && !drained && (uint32_t(__popc(idle)) >= refill || idle == 0xffffffffu)) {
@@ -377,13 +402,14 @@ __device__ __forceinline__ void traceWarp(const SceneDev& S, Src& src, int32_t* 
       const bool needy = stepping && tr.leaf == kNoLeaf;
       if (!__any_sync(0xffffffffu, needy)) break;
       if (++spin > kTraceSpinCap) break;
-      if (SPEC ? stepping : needy) tr.template innerStep<COUNT>(S, sh, loc, nNodes, ovf);
+      if (SPEC ? stepping : needy) tr.template innerStep<COUNT>(S, sh, loc, lim, nNodes, ovf);
     }
     if (spin > kTraceSpinCap) {
       ovf = true;
       break;
     }
-    if (active && (tr.template leafOrMove<ANY, COUNT>(S, sh, loc, nTris, ovf) || ++events > kTraceRayCap)) {
+    if (active && (tr.template leafOrMove<ANY, COUNT>(S, src, idx, sh, loc, lim, nTris, ovf) ||
+                   ++events > kTraceRayCap)) {
       if (events > kTraceRayCap) ovf = true;
       active = false;
       src.finish(idx, tr);
@@ -410,6 +436,12 @@ struct QueueSrc {
     else
       tr.init(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), 0.00001f, 10000000000.0f);
   }
+  __device__ __forceinline__ void world(uint32_t r, float3& o, float3& d) const {
+    const float4 o4 = __ldg(&rO[r]);
+    const float4 d4 = __ldg(&rD[r]);
+    o = make_float3(o4.x, o4.y, o4.z);
+    d = make_float3(d4.x, d4.y, d4.z);
+  }
   template <class T>
   __device__ __forceinline__ void finish(uint32_t i, const T& tr) {
     if (ANY) {
@@ -424,7 +456,7 @@ struct QueueSrc {
         if (P->records) W->rec[p].y |= 1u << (P->depth - (W->info[p].y >> kPassShift) - 1u);
       }
     } else if (tr.found) {
-      W->hit[i] = make_float4(tr.h.t, tr.h.u, tr.h.v, __uint_as_float(tr.h.prim));
+      W->hit[i] = make_float4(tr.best, tr.h.u, tr.h.v, __uint_as_float(tr.h.prim));
       W->hitInst[i] = tr.h.inst;
     } else {
       W->hit[i] = make_float4(-1.0f, 0.0f, 0.0f, 0.0f);
@@ -465,6 +497,7 @@ __global__ void __launch_bounds__(TB, MINB) k_trace(KParams P) {
   bool ovf = false;
   // (the instrumented variant walks without speculation, so its node counts
   // are those of the ordered traversal)
+  // (P.stackLimit is in [1, kStackDepth]: the host clamps it)
   traceWarp<ANY, COUNT, SPEC, TB, SHS>(P.S, src, sh, lstack, P.refillLanes, P.stackLimit, nNodes, nTris, ovf);
   if (ovf) atomicAdd(&W.cnt->stackOverflow, 1ull);
   if (COUNT) {
@@ -497,11 +530,16 @@ struct ArraySrc {
     const float4 o4 = o[r], d4 = d[r];
     tr.init(S, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z), o4.w, d4.w);
   }
+  __device__ __forceinline__ void world(uint32_t r, float3& wo, float3& wd) const {
+    const float4 o4 = o[r], d4 = d[r];
+    wo = make_float3(o4.x, o4.y, o4.z);
+    wd = make_float3(d4.x, d4.y, d4.z);
+  }
   template <class T>
   __device__ __forceinline__ void finish(uint32_t i, const T& tr) {
     if (tr.found) {
       hit[i] = anyHit ? make_float4(1.0f, 0.0f, 0.0f, 0.0f)
-                      : make_float4(tr.h.t, tr.h.u, tr.h.v, __uint_as_float(tr.h.prim));
+                      : make_float4(tr.best, tr.h.u, tr.h.v, __uint_as_float(tr.h.prim));
       inst[i] = anyHit ? 0u : tr.h.inst;
     } else {
       hit[i] = make_float4(-1.0f, 0.0f, 0.0f, 0.0f);
