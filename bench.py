@@ -319,7 +319,12 @@ def run(args):
     else:
         ctx.set_path_budget(args.frames_per_step * shot.width * shot.height * BYTES_PER_PATH)
         if args.traversal:
-            ctx.set_traversal(*(int(x) for x in args.traversal.split(",")))
+            trav = [int(x) for x in args.traversal.split(",")]
+            ctx.set_traversal(*trav)
+            if args.shadow_occupancy:
+                ctx.set_traversal_occupancy(trav[4] if len(trav) > 4 else 0, args.shadow_occupancy)
+        if args.shape:
+            ctx.set_traversal_shape(*(int(x) for x in args.shape.split(",")))
         ctx.set_ray_sort(args.ray_sort)
     # per-rank frames: replicas render disjoint frames of the same shot
     from asuna_gb300 import replicas
@@ -806,6 +811,10 @@ def main():
     ap.add_argument("--traversal", default="",
                     help="with --frames-per-step: refill extend,refill shadow,speculate extend,speculate shadow,"
                          "blocks per SM (the autotuner's traversal tuple)")
+    ap.add_argument("--shape", default="",
+                    help="with --frames-per-step: traversal threads per block,shared-memory stack entries")
+    ap.add_argument("--shadow-occupancy", type=int, default=0, choices=(0, 8, 10, 12),
+                    help="with --frames-per-step and --traversal: the occlusion pass's blocks per SM")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=10.0, help="--impl reference: CPU seconds per step at most")
     ap.add_argument("--ref-budget", type=float, default=100.0,
