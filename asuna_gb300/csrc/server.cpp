@@ -59,6 +59,7 @@ struct Req {
   asuna_film* film[2] = {nullptr, nullptr};
   float* denoised = nullptr;  // device RGBA, denoised requests
   asuna_ctx* filmCtx = nullptr;
+  std::mutex io;  // a read of the films and their release exclude each other
   bool denoise() const { return (flags & ASUNA_REQUEST_DENOISE) != 0; }
   int parts() const { return denoise() ? 2 : 1; }
   bool complete() const { return done[0] >= frames[0] && done[1] >= frames[1]; }
@@ -529,6 +530,7 @@ int asuna_server_read(asuna_server* S, uint64_t id, int image, float* host_rgba)
     if (it == S->byId.end()) return asuna::fail(ASUNA_ERR_INVALID, "unknown request %llu", (unsigned long long)id);
     r = it->second;
   }
+  std::lock_guard<std::mutex> io(r->io);
   if (r->status != ASUNA_OK || !r->film[0])
     return asuna::fail(ASUNA_ERR_INVALID, "request %llu has no film", (unsigned long long)id);
   if (r->finish < 0) return asuna::fail(ASUNA_ERR_INVALID, "request %llu is not finished", (unsigned long long)id);
@@ -562,7 +564,10 @@ int asuna_server_release(asuna_server* S, uint64_t id) {
     if (r->charged) S->memUsed -= r->bytes;
     r->charged = false;
   }
-  freeRequest(*r);
+  {
+    std::lock_guard<std::mutex> io(r->io);  // after any read in progress
+    freeRequest(*r);
+  }
   S->cv.notify_all();
   return ASUNA_OK;
 }

@@ -569,7 +569,9 @@ int asuna_server_submit(asuna_server* server, const asuna_request* req, uint64_t
 /* Finished (or rejected) requests since the last poll, oldest first. */
 int asuna_server_poll(asuna_server* server, asuna_request_result* out, uint32_t max, uint32_t* n);
 /* Film image `image` of a finished request (image 0 of a denoised request:
- * the denoised radiance). */
+ * the denoised radiance).  Safe to call from any thread; a release of the
+ * same request waits for the read, and a read after it fails with
+ * ASUNA_ERR_INVALID (unknown request). */
 int asuna_server_read(asuna_server* server, uint64_t id, int image, float* host_rgba);
 /* Frees a finished request's film (returns its memory to the budget). */
 int asuna_server_release(asuna_server* server, uint64_t id);
