@@ -827,12 +827,12 @@ def main():
     ap.add_argument("--rmse-target", type=float, default=0.01)
     ap.add_argument("--plain-max-spp", type=int, default=32768)
     ap.add_argument("--denoise-max-spp", type=int, default=32768)
-    ap.add_argument("--train-scenes", type=int, default=64)
+    ap.add_argument("--train-scenes", type=int, default=160)
     ap.add_argument("--train-size", type=int, default=256)
     ap.add_argument("--train-spp-in", default="4,16,64,256,1024,4096")
     ap.add_argument("--train-target-spp", type=int, default=65536)
     ap.add_argument("--train-level", type=int, default=6)
-    ap.add_argument("--train-steps", type=int, default=20000)
+    ap.add_argument("--train-steps", type=int, default=40000)
     ap.add_argument("--train-batch", type=int, default=16)
     ap.add_argument("--train-crop", type=int, default=128)
     ap.add_argument("--train-loss", default="l1log", choices=("l1log", "relmse"),
