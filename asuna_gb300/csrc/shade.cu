@@ -34,15 +34,31 @@ namespace {
 
 __device__ __forceinline__ uint32_t laneId() { return threadIdx.x & 31u; }
 
-// Warp-aggregated queue append: every lane of the warp calls it.
-__device__ __forceinline__ uint32_t warpAppend(bool want, uint32_t* counter) {
-  unsigned mask = __ballot_sync(0xffffffffu, want);
-  if (!mask) return 0;
-  int leader = __ffs(mask) - 1;
-  uint32_t base = 0;
-  if (int(laneId()) == leader) base = atomicAdd(counter, uint32_t(__popc(mask)));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  return base + uint32_t(__popc(mask & ((1u << laneId()) - 1u)));
+// Block-aggregated appends to the shadow queue and the next extend queue:
+// every thread of the block calls it once per round (the barriers are
+// uniform); one shared-memory add per warp and queue, then one global add per
+// queue and block, so the two hot queue counters see an eighth of the
+// atomics of per-warp appends.  Returns the slots of the thread's entries.
+__device__ __forceinline__ void blockAppend2(bool wantA, bool wantB, uint32_t* counterA, uint32_t* counterB,
+                                             uint32_t* shCount, uint32_t* shBase, uint32_t& slotA,
+                                             uint32_t& slotB) {
+  if (threadIdx.x < 2) shCount[threadIdx.x] = 0u;
+  __syncthreads();
+  const unsigned ma = __ballot_sync(0xffffffffu, wantA), mb = __ballot_sync(0xffffffffu, wantB);
+  uint32_t offA = 0, offB = 0;
+  if (laneId() == 0) {
+    if (ma) offA = atomicAdd(&shCount[0], uint32_t(__popc(ma)));
+    if (mb) offB = atomicAdd(&shCount[1], uint32_t(__popc(mb)));
+  }
+  offA = __shfl_sync(0xffffffffu, offA, 0);
+  offB = __shfl_sync(0xffffffffu, offB, 0);
+  __syncthreads();
+  if (threadIdx.x == 0 && shCount[0]) shBase[0] = atomicAdd(counterA, shCount[0]);
+  if (threadIdx.x == 1 && shCount[1]) shBase[1] = atomicAdd(counterB, shCount[1]);
+  __syncthreads();
+  const unsigned below = (1u << laneId()) - 1u;
+  slotA = wantA ? shBase[0] + offA + uint32_t(__popc(ma & below)) : 0u;
+  slotB = wantB ? shBase[1] + offB + uint32_t(__popc(mb & below)) : 0u;
 }
 
 __device__ __forceinline__ uint32_t findRange(const RangeDev* r, uint32_t n, uint32_t p) {
@@ -1085,9 +1101,13 @@ __device__ __forceinline__ void sampleDielectric(PathIO& io, const HitSt& st, co
 
 // ---------------------------------------------------------------------------
 // Splits the hits of the extend queue into the shading classes (material
-// sort): one warp-aggregated append per class present in a warp.  Classes that no hit
+// sort).  A block takes 256 hits at a time: lanes are grouped by class in
+// each warp (one shared-memory add per class present), then one global
+// append per class present in the block, so the few class counters see
+// eight times fewer atomics than with per-warp appends.  Classes that no hit
 // of a pass uses cost one empty launch.
 __global__ void __launch_bounds__(256) k_classify(KParams P) {
+  __shared__ uint32_t count[kNumShadeClasses], base[kNumShadeClasses];
   const WaveDev& W = P.W;
   const SceneDev& S = P.S;
   const uint32_t n = W.cnt->c[kCntExtend0 + P.cur];
@@ -1096,7 +1116,10 @@ __global__ void __launch_bounds__(256) k_classify(KParams P) {
     W.cnt->c[kCntFetchShadow] = 0;
   }
   const uint32_t stride = gridDim.x * blockDim.x;
+  // (i0 is the same for every thread of the block: the barriers are uniform)
   for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+    if (threadIdx.x < kNumShadeClasses) count[threadIdx.x] = 0u;
+    __syncthreads();
     const uint32_t i = i0 + threadIdx.x;
     int cls = -1;
     if (i < n) {
@@ -1109,13 +1132,18 @@ __global__ void __launch_bounds__(256) k_classify(KParams P) {
         }
       }
     }
-    // lanes grouped by class: one append per class present in the warp
     const unsigned peers = __match_any_sync(0xffffffffu, cls);
     const int leader = __ffs(peers) - 1;
-    uint32_t base = 0;
-    if (int(laneId()) == leader && cls >= 0) base = atomicAdd(&W.cnt->c[kCntCls0 + cls], uint32_t(__popc(peers)));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (cls >= 0) W.cls[cls][base + uint32_t(__popc(peers & ((1u << laneId()) - 1u)))] = i;
+    uint32_t off = 0;
+    if (int(laneId()) == leader && cls >= 0) off = atomicAdd(&count[cls], uint32_t(__popc(peers)));
+    off = __shfl_sync(0xffffffffu, off, leader);
+    __syncthreads();
+    if (threadIdx.x < kNumShadeClasses && count[threadIdx.x])
+      base[threadIdx.x] = atomicAdd(&W.cnt->c[kCntCls0 + threadIdx.x], count[threadIdx.x]);
+    __syncthreads();
+    // (count was last read before the barrier above and base is written
+    // again only after two more: the next round may start at once)
+    if (cls >= 0) W.cls[cls][base[cls] + off + uint32_t(__popc(peers & ((1u << laneId()) - 1u)))] = i;
   }
 }
 
@@ -1124,6 +1152,7 @@ __global__ void __launch_bounds__(256) k_classify(KParams P) {
 // next-event estimation and BSDF sampling.
 template <int CLS>
 __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) {
+  __shared__ uint32_t appendCount[2], appendBase[2];
   const WaveDev& W = P.W;
   const SceneDev& S = P.S;
   const int cur = P.cur, nxt = cur ^ 1;
@@ -1322,8 +1351,11 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
     }
     __syncwarp();
     if (CLS != kClsTerminal) {  // terminal paths append nothing
-      const uint32_t sslot = warpAppend(wantShadow, &W.cnt->c[kCntShadow]);
-      const uint32_t nslot = warpAppend(wantNext, &W.cnt->c[kCntExtend0 + nxt]);
+      // (i0 is the same for every thread of the block: the barriers inside
+      // are reached by all of them, round by round)
+      uint32_t sslot, nslot;
+      blockAppend2(wantShadow, wantNext, &W.cnt->c[kCntShadow], &W.cnt->c[kCntExtend0 + nxt], appendCount,
+                   appendBase, sslot, nslot);
       if (wantShadow) {
         float maxDist = io.ddist - 2.0f * EPS;
         W.shO[sslot] = make_float4(io.dro.x, io.dro.y, io.dro.z, maxDist);
