@@ -230,6 +230,12 @@ struct DevCounters {
   unsigned long long stackOverflow;
 };
 
+struct __align__(32) PathDev {
+  float4 thp;
+  uint4 info;
+};
+static_assert(sizeof(PathDev) == 32, "PathDev is 32 bytes");
+
 // Wavefront buffers (structure of arrays, indexed by queue slot or path).
 struct WaveDev {
   // extend queues (ping-pong): (o.xyz, tmax), (d.xyz, path index bits)
@@ -242,11 +248,15 @@ struct WaveDev {
   float4* shO;
   float4* shD;
   float4* shC;
-  // path state
-  float4* thp;  // throughput.xyz, pdf of the last BSDF sample
-  float4* rad;  // radiance.xyz, filter weight
-  uint4* info;  // seed, last BSDF lobe flags, range index, local index
-  uint4* rec;   // parity records: signature, unoccluded bits, shadow bits, depth
+  // path state.  The shading passes reach it by path index, scattered: the
+  // throughput and the path's counters share one 32-byte record (one sector
+  // per gather instead of two); the radiance stays an array of its own, as
+  // the occlusion pass adds to it and the accumulation reads it in path
+  // order; the parity records are only written when asked for.
+  PathDev* path;  // thp = throughput.xyz, pdf of the last BSDF sample;
+                  // info = seed, last BSDF lobe flags, range index, local index
+  float4* rad;    // radiance.xyz, filter weight
+  uint4* rec;     // parity records: signature, unoccluded bits, shadow bits, depth
   uint32_t* cls[kNumShadeClasses];  // extend-queue indices of each shading class
   DevCounters* cnt;
   const RangeDev* ranges;

@@ -69,9 +69,8 @@ int ensureWave(asuna_ctx* c, uint64_t paths) {
   uint64_t o_shO = off; off += pad(paths * 16);
   uint64_t o_shD = off; off += pad(paths * 16);
   uint64_t o_shC = off; off += pad(paths * 16);
-  uint64_t o_thp = off; off += pad(paths * 16);
+  uint64_t o_path = off; off += pad(paths * sizeof(PathDev));
   uint64_t o_rad = off; off += pad(paths * 16);
-  uint64_t o_info = off; off += pad(paths * 16);
   uint64_t o_rec = off; off += pad(paths * 16);
   uint64_t o_cls[kNumShadeClasses];
   for (int k = 0; k < kNumShadeClasses; ++k) {
@@ -91,9 +90,8 @@ int ensureWave(asuna_ctx* c, uint64_t paths) {
   v.shO = reinterpret_cast<float4*>(b + o_shO);
   v.shD = reinterpret_cast<float4*>(b + o_shD);
   v.shC = reinterpret_cast<float4*>(b + o_shC);
-  v.thp = reinterpret_cast<float4*>(b + o_thp);
+  v.path = reinterpret_cast<PathDev*>(b + o_path);
   v.rad = reinterpret_cast<float4*>(b + o_rad);
-  v.info = reinterpret_cast<uint4*>(b + o_info);
   v.rec = reinterpret_cast<uint4*>(b + o_rec);
   for (int k = 0; k < kNumShadeClasses; ++k) v.cls[k] = reinterpret_cast<uint32_t*>(b + o_cls[k]);
   v.cnt = c->cnt;

@@ -154,9 +154,8 @@ int renderNoAlloc(const asuna_scene* s, const asuna_shot* shot, asuna_film* film
   W.shO = f16[5];
   W.shD = f16[6];
   W.shC = f16[7];
-  W.thp = f16[8];
-  W.rad = f16[9];
-  W.info = reinterpret_cast<uint4*>(f16[10]);
+  W.path = reinterpret_cast<PathDev*>(f16[8]);  // 32 B per path: the 16-byte regions 8 and 9
+  W.rad = f16[10];
   W.rec = reinterpret_cast<uint4*>(f16[11]);
   W.hitInst = reinterpret_cast<uint32_t*>(base + 12 * kPerPath16);
   for (int k = 0; k < kNumShadeClasses; ++k)

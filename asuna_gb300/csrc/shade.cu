@@ -132,9 +132,9 @@ __global__ void __launch_bounds__(256) k_raygen(KParams P) {
     float fw = gmax(0.0f, mexp(alpha * ox * ox) - expXY) * gmax(0.0f, mexp(alpha * oy * oy) - expXY);
     W.rayO[0][p] = make_float4(ro.x, ro.y, ro.z, INF);
     W.rayD[0][p] = make_float4(rd.x, rd.y, rd.z, __uint_as_float(p));
-    W.thp[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    W.path[p].thp = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     W.rad[p] = make_float4(0.0f, 0.0f, 0.0f, fw);
-    W.info[p] = make_uint4(seed, EBsdfNull, ri, local);
+    W.path[p].info = make_uint4(seed, EBsdfNull, ri, local);
     if (P.records) W.rec[p] = make_uint4(0u, 0u, 0u, 1u);
     if (frame == 0) {
       // AOV images are rewritten at frame 0 (rgen:155-162): clear to (0,0,0,1)
@@ -1173,9 +1173,9 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
       const f3 ro = ld3(o4), rd = ld3(d4);
       const float4 h4 = W.hit[i];
       const uint32_t inst = W.hitInst[i];
-      const float4 t4 = W.thp[p];
+      const float4 t4 = W.path[p].thp;
       const float4 r4 = W.rad[p];
-      const uint4 inf = W.info[p];
+      const uint4 inf = W.path[p].info;
       if (P.records) rc = W.rec[p];
       const RangeDev R = W.ranges[inf.z];
       const ShotDev& sh = W.shots[R.shot];
@@ -1344,9 +1344,9 @@ __global__ void __launch_bounds__(256, kShadeMinBlocks) k_shadeClass(KParams P) 
         if (wantShadow) rc.z |= 1u << (depth - 1u);
       }
       // path state
-      W.thp[p] = make_float4(io.thp.x, io.thp.y, io.thp.z, io.bpdf);
+      W.path[p].thp = make_float4(io.thp.x, io.thp.y, io.thp.z, io.bpdf);
       W.rad[p] = make_float4(io.rad.x, io.rad.y, io.rad.z, r4.w);
-      W.info[p] = make_uint4(io.seed, io.bflags | (passes << kPassShift), inf.z, inf.w);
+      W.path[p].info = make_uint4(io.seed, io.bflags | (passes << kPassShift), inf.z, inf.w);
       if (P.records) W.rec[p] = rc;
     }
     __syncwarp();

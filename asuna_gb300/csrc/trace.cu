@@ -453,7 +453,7 @@ struct QueueSrc {
         r.y = r.y + c.y;
         r.z = r.z + c.z;
         W->rad[p] = r;
-        if (P->records) W->rec[p].y |= 1u << (P->depth - (W->info[p].y >> kPassShift) - 1u);
+        if (P->records) W->rec[p].y |= 1u << (P->depth - (W->path[p].info.y >> kPassShift) - 1u);
       }
     } else if (tr.found) {
       W->hit[i] = make_float4(tr.best, tr.h.u, tr.h.v, __uint_as_float(tr.h.prim));
