@@ -7,12 +7,13 @@
 // instances set VK_GEOMETRY_INSTANCE_TRIANGLE_FACING_CULL_DISABLE_BIT_KHR
 // (src/pipeline/pipeline_raytrace.cpp:132).
 //
-// Persistent warps fetch 32 rays at a time from the queue (one atomic per
-// warp); each thread walks TLAS -> BLAS with a per-thread stack in shared
-// memory (entry k of thread t at sstack[k * 128 + t], bank-conflict free).
-// Node and triangle records are read with 128-bit read-only loads; the slab
-// distances of a node are computed with packed two-lane (f32x2) arithmetic.  The ray
-// is moved into object space and tested against triangles with the watertight
+// Persistent warps refill their idle lanes from the queue (one atomic per
+// refill and warp); each thread walks TLAS -> BLAS with a per-thread stack
+// in shared memory (entry k of thread t at sstack[k * TB + t], bank-conflict
+// free) that spills into thread-local memory past its shared part.  Node and
+// triangle records are read with 128-bit read-only loads; the slab distances
+// of a node are computed with packed two-lane (f32x2) arithmetic.  The ray is
+// moved into object space and tested against triangles with the watertight
 // algorithm of Woop, Benthin and Wald (JCGT 2013) using explicitly rounded
 // operations, so the hits equal the CPU oracle's bit for bit; box tests use
 // (lo - o) * (1/d) with the far distance widened by 2^-20, which keeps them
