@@ -12,9 +12,9 @@ import itertools
 BYTES_PER_PATH = 244  # wavefront state per path slot (asuna_gb300/csrc/engine.cu)
 
 
-def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64, 128), trace_options=(0, 6),
+def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64, 128, 256), trace_options=(0, 6),
          shade_options=(0, 2), refill_options=(4, 8, 16, 24), occupancy_options=(8, 10, 12),
-         shape_options=((64, 24), (256, 24), (128, 16), (128, 32)), memory_bytes=80 << 30, reps=2,
+         shape_options=((64, 24), (256, 24), (128, 16), (128, 32)), memory_bytes=160 << 30, reps=2,
          frame_base=1 << 20):
     """Returns {"frames": f, "trace_blocks_per_sm": t, "shade_blocks_per_sm": s, "traversal": (refill
     extend, refill shadow, speculate extend, speculate shadow, traversal blocks per SM), "shape": (threads
