@@ -48,9 +48,10 @@ namespace {
 constexpr uint64_t kNoAllocMaxPaths = ASUNA_NOALLOC_MAX_PATHS;
 
 constexpr uint64_t pad256(uint64_t b) { return (b + 255) / 256 * 256; }
-// scratch layout: per-path arrays (12 x 16 B; 4 B each for the hit
-// instances and every shading-class list), counters, shot, the current
-// batch's range record
+// scratch layout: per-path arrays (12 x 16 B, regions 8 and 9 together
+// holding the 32-byte path records; 4 B each for the hit instances and
+// every shading-class list), counters, shot, the current batch's range
+// record
 constexpr uint64_t kPerPath16 = pad256(kNoAllocMaxPaths * 16);
 constexpr uint64_t kPerPath4 = pad256(kNoAllocMaxPaths * 4);
 constexpr uint64_t kOffCounters = 12 * kPerPath16 + (1 + kNumShadeClasses) * kPerPath4;
