@@ -435,6 +435,35 @@ def run(args):
     return 0
 
 
+def ladder_next(n, e, lo, target):
+    """Sample count of the next rung of a progressive time-to-RMSE ladder
+    after a rung at n samples with error e: doubling (at least lo), or,
+    once e is within 4x of the target, the count the 1/sqrt(spp) law
+    predicts for the target (+2%), at least n + 1 and at most double."""
+    nxt = max(lo, 2 * n)
+    if n and e < 4 * target:
+        nxt = min(nxt, max(n + 1, int(np.ceil(n * (e / target) ** 2 * 1.02))))
+    return nxt
+
+
+def ladder_time(ladder, tgt, target):
+    """Seconds at which a ladder (rungs {spp, seconds, rmse} in order)
+    reaches RMSE tgt, and how: the first rung at or below it when tgt is
+    the ladder's own target (or the first rung is already below it),
+    otherwise interpolated between the two rungs around it on the 1/sqrt(spp)
+    law (error linear in 1/sqrt(spp), seconds proportional to spp).  (None,
+    None) when no rung reaches it."""
+    for i, r in enumerate(ladder):
+        if r["rmse"] <= tgt:
+            if i == 0 or tgt == target:
+                return r["seconds"], "measured"
+            p = ladder[i - 1]
+            x0, x1 = p["spp"] ** -0.5, r["spp"] ** -0.5
+            x = x1 + (tgt - r["rmse"]) * (x0 - x1) / (p["rmse"] - r["rmse"])
+            return r["seconds"] / r["spp"] * x ** -2, "interpolated"
+    return None, None
+
+
 def run_denoise_rmse(args):
     """Time to image RMSE 0.01 against the FP64 reference (a seeded 1,024-pixel
     subset of the 1080p workload at 262,144 spp, tests/golden) for the plain
@@ -512,11 +541,7 @@ def run_denoise_rmse(args):
         return ms
 
     def next_count(n, e, lo):
-        # doubling, or near the target the 1/sqrt(spp) prediction (+2%)
-        nxt = max(lo, 2 * n)
-        if n and e < 4 * target:
-            nxt = min(nxt, max(n + 1, int(np.ceil(n * (e / target) ** 2 * 1.02))))
-        return nxt
+        return ladder_next(n, e, lo, target)
 
     # 2a. plain path (clocks sampled from here through both ladders)
     clk = ClockSampler(int(os.environ.get("LOCAL_RANK", 0))).__enter__()
@@ -582,15 +607,7 @@ def run_denoise_rmse(args):
     # seconds proportional to spp), for both ladders; the main target is the
     # measured rung
     def at(ladder, tgt):
-        for i, r in enumerate(ladder):
-            if r["rmse"] <= tgt:
-                if i == 0 or tgt == target:
-                    return r["seconds"], "measured"
-                p = ladder[i - 1]
-                x0, x1 = p["spp"] ** -0.5, r["spp"] ** -0.5
-                x = x1 + (tgt - r["rmse"]) * (x0 - x1) / (p["rmse"] - r["rmse"])
-                return r["seconds"] / r["spp"] * x ** -2, "interpolated"
-        return None, None
+        return ladder_time(ladder, tgt, target)
 
     rows = []
     for tgt in (0.05, 0.03, 0.02, target):
