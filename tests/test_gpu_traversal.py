@@ -75,6 +75,54 @@ def test_watertight_shared_edges_and_vertices(ctx):
     assert np.all(inst != 0xFFFFFFFF), int(np.sum(inst == 0xFFFFFFFF))
 
 
+def test_watertight_tiled_plane_matches_oracle(ctx):
+    # an irregular tiled plane (random diagonals, jittered interior vertices):
+    # rays at random slants aimed at every vertex and edge midpoint all hit,
+    # and hit what the oracle hits, bit for bit, but for at most a few per
+    # thousand: each ray meets two or more triangles at one point, on the
+    # corner of their leaf boxes, and the two traversals (the oracle's
+    # object-median tree with boxes widened by 1e-6 of their coordinates and
+    # no widening of t; the GPU's SAH tree with t widened by 2^-20) need not
+    # test the same candidates there
+    n = 12
+    rng = np.random.default_rng(4)
+    xs, ys = np.meshgrid(np.linspace(-1.0, 1.0, n + 1), np.linspace(-1.0, 1.0, n + 1), indexing="ij")
+    pos = np.stack([xs, ys, np.zeros_like(xs)], axis=-1).reshape(-1, 3)
+    inner = (np.abs(pos[:, 0]) < 0.999) & (np.abs(pos[:, 1]) < 0.999)
+    pos[inner, :2] += rng.uniform(-0.3, 0.3, size=(int(inner.sum()), 2)) / n
+    faces = []
+    for i in range(n):
+        for j in range(n):
+            a, b_, c, d = i * (n + 1) + j, (i + 1) * (n + 1) + j, (i + 1) * (n + 1) + j + 1, i * (n + 1) + j + 1
+            faces += [(a, b_, c), (a, c, d)] if rng.random() < 0.5 else [(a, b_, d), (b_, c, d)]
+    faces = np.array(faces)
+    b = ag.SceneBuilder()
+    m = b.add_lambertian("m", (0.5, 0.5, 0.5))
+    verts = np.zeros(len(pos), ag._abi.VERTEX_DTYPE)
+    verts["pos"] = pos.astype(np.float32)
+    b.add_mesh("plane", verts, faces.astype(np.uint32))
+    b.add_instance("plane", m)
+    d = b.desc()
+    scene = ctx.create_scene(d)
+    o_sc = oracle_py.OracleScene(d)
+    p = verts["pos"].astype(np.float64)
+    edges = np.concatenate([faces[:, [0, 1]], faces[:, [1, 2]], faces[:, [2, 0]]])
+    targets = np.concatenate([p[inner], 0.5 * (p[edges[:, 0]] + p[edges[:, 1]])])
+    targets = targets[(np.abs(targets[:, 0]) < 0.99) & (np.abs(targets[:, 1]) < 0.99)]
+    slant = rng.uniform(-0.6, 0.6, size=(len(targets), 2))
+    origins = (targets + np.column_stack([slant, np.ones(len(targets))])).astype(np.float32)
+    dirs = (targets - origins)
+    dirs = (dirs / np.linalg.norm(dirs, axis=1, keepdims=True)).astype(np.float32)
+    hits, inst = scene.trace(origins, dirs, tmin=0.0)
+    assert np.all(inst != 0xFFFFFFFF), int(np.sum(inst == 0xFFFFFFFF))
+    same = 0
+    for k in range(len(origins)):
+        t, ii, prim, u, v = o_sc.trace(origins[k], dirs[k], 0.0, 1e10)
+        same += (hits[k, 0] == np.float32(t) and hits[k, 3].view(np.uint32) == prim and
+                 hits[k, 1] == np.float32(u) and hits[k, 2] == np.float32(v))
+    assert same >= len(origins) - 2, (same, len(origins))
+
+
 def test_tmin_tmax_contract(ctx):
     b, _ = scenes.box_scene(8, 8, frames=1)
     scene = ctx.create_scene(b.desc())
