@@ -506,6 +506,11 @@ inline void xformRay(const float* w, const float o[3], const float d[3], float o
   }
 }
 
+// Box test.  The box is widened in space when built; the far distance is
+// widened by 2^-20 here as well, so that the rounding of the distances
+// (relative to t, not to the box's coordinates) never rejects a box whose
+// triangle the watertight test would accept, as where a ray meets several
+// triangles at the corner of their boxes.
 inline bool slab(const float lo[3], const float hi[3], const float o[3], const float inv[3], float tmin, float tmax) {
   float t0 = tmin, t1 = tmax;
   for (int k = 0; k < 3; ++k) {
@@ -518,7 +523,7 @@ inline bool slab(const float lo[3], const float hi[3], const float o[3], const f
     t0 = std::max(t0, a);
     t1 = std::min(t1, b);
   }
-  return t0 <= t1;
+  return t0 <= t1 * 1.00000095367431640625f;  // 1 + 2^-20
 }
 
 struct Hit {
