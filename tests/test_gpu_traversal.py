@@ -38,7 +38,10 @@ def test_closest_hit_matches_oracle(ctx):
         if not (got[0] == np.float32(t) and got[1] == ii and got[2] == prim and got[3] == np.float32(u)
                 and got[4] == np.float32(v)):
             mism += 1
-    assert mism <= 2, mism  # only exact-tie order may differ
+    # (closest hits resolve exact ties to the lowest instance and primitive
+    # and both box tests are conservative, so none is expected; two of the
+    # 4,000 are allowed)
+    assert mism <= 2, mism
 
 
 def test_occlusion_matches_oracle(ctx):
