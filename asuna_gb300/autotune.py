@@ -9,6 +9,8 @@ caller's, so they never touch its sample streams.
 """
 import itertools
 
+from ._abi import ERR_OOM, AsunaError
+
 BYTES_PER_PATH = 244  # wavefront state per path slot (asuna_gb300/csrc/engine.cu)
 
 
@@ -51,7 +53,15 @@ def tune(ctx, scene, shot, film, frames_options=(1, 2, 4, 8, 16, 32, 64, 128, 25
         cands = [f for f in frames_options if f * npix * BYTES_PER_PATH <= memory_bytes]
         # frames first with the default grids, then the grids at the best frame count
         for f in cands:
-            v = run(f, 0, 0)
+            try:
+                v = run(f, 0, 0)
+            except AsunaError as e:
+                # the device has less free memory than the cap assumed: larger
+                # wavefronts will not fit either
+                if e.code != ERR_OOM or best is None:
+                    raise
+                trials.append({"frames": f, "trace": 0, "shade": 0, "mrays": None, "error": "out of memory"})
+                break
             trials.append({"frames": f, "trace": 0, "shade": 0, "mrays": v})
             if best is None or v > best["mrays"]:
                 best = {"frames": f, "trace_blocks_per_sm": 0, "shade_blocks_per_sm": 0, "mrays": v}

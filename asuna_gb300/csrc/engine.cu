@@ -78,7 +78,13 @@ int ensureWave(asuna_ctx* c, uint64_t paths) {
     off += pad(paths * 4);
   }
   void* base = nullptr;
-  ASUNA_CUDA_TRY(cudaMalloc(&base, off));
+  const cudaError_t me = cudaMalloc(&base, off);
+  if (me == cudaErrorMemoryAllocation) {
+    cudaGetLastError();  // not sticky: a smaller path budget can still render
+    return fail(ASUNA_ERR_OOM, "wavefront buffers of %llu bytes (%llu path slots) do not fit in device memory",
+                (unsigned long long)off, (unsigned long long)paths);
+  }
+  ASUNA_CUDA_TRY(me);
   char* b = static_cast<char*>(base);
   WaveDev& v = c->wave.view;
   v.rayO[0] = reinterpret_cast<float4*>(b + o_rayO0);

@@ -95,3 +95,24 @@ def test_tune_respects_the_memory_bound():
     shot = types.SimpleNamespace(width=64, height=32, frame0=0, frames=1)
     best = autotune.tune(ctx, object(), shot, FakeFilm(), memory_bytes=4 * 64 * 32 * autotune.BYTES_PER_PATH)
     assert best["frames"] == 4
+
+
+def test_tune_skips_wavefronts_that_do_not_fit():
+    """A frame count whose wavefront does not fit in the device memory left
+    (ERR_OOM from the render) ends the frame sweep; the tuner keeps the best
+    count that rendered."""
+    from asuna_gb300._abi import ERR_OOM, AsunaError
+
+    class OomCtx(FakeCtx):
+        def render(self, scene, shot, film, stats=False):
+            if shot.frames > 8:
+                raise AsunaError(ERR_OOM, "wavefront buffers do not fit")
+            return super().render(scene, shot, film, stats)
+
+    ctx = OomCtx(_score)
+    shot = types.SimpleNamespace(width=64, height=32, frame0=5, frames=3)
+    best = autotune.tune(ctx, object(), shot, FakeFilm(), memory_bytes=1 << 40)
+    assert best["frames"] == 8
+    assert any(t.get("error") == "out of memory" and t["frames"] == 16 for t in best["trials"])
+    assert not any(t.get("frames") == 32 for t in best["trials"] if "trace" in t)
+    assert (shot.frame0, shot.frames) == (5, 3)
